@@ -1,0 +1,348 @@
+#!/usr/bin/env python
+"""Benchmark of the many-body MD hot path: fcc Cu, 80^3 cells (2,048,000 atoms), Cleri-Rosato
+TB-SMA, sigma 0.05 A, 600 K, NVE velocity Verlet dt = 1 fs, skin trigger 0.15 A.
+
+One step = fused corrector/predictor + skin check (+ device list rebuild when triggered) +
+density pass + force pass, all on one GPU.  Prints one JSON line (see the keys below).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--precision mixed|fp64]
+                  [--impl ours|reference]
+
+--impl reference times the CPU restatement of the reference's serial path (the oracle, the
+reference's CUDA Fortran cannot be built here) with all host threads on the same workload.
+With N > 1 (torchrun) every rank runs an independent replica (the path does not shard on
+one box); value sums the ranks and the time is the max over ranks.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "atom-steps/s FP64 vs mixed @1e-6 force err; batched boxes/s; HVP cost/force"
+UNIT = "atom-steps/s"
+NCELL, SIGMA, TEMP, SEED, DT = 80, 0.05, 600.0, 2024, 1.0
+MXKVOIS = 64
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clock and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.fh, stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self):
+        if not self.path or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower() in ("active", "1"):
+                    reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def workload():
+    from msmpscu_gb300 import lattice as lt
+    pos, vel, L = lt.cu_config(NCELL, SIGMA, TEMP, SEED)
+    return pos, vel, L
+
+
+def make_engine(n, precision, device=0):
+    from msmpscu_gb300 import Engine, ForceTable, lattice as lt
+    e = Engine(n, lt.CU_RC_NL, mxkvois=MXKVOIS, skin_trigger=0.15, precision=precision, device=device)
+    e.init_forcetable(ForceTable.cleri_rosato(**lt.CU_CR, rc=lt.CU_RC))
+    e.set_masses([lt.CU_MASS])
+    return e
+
+
+def bytes_model(kmean):
+    """Algorithmic bytes per atom and launch (design-independent): int32 list entries read
+    once per pass, own FP64 position (24 B), F'(rho) write/read (8 B each), force write
+    (24 B); integrator reads x, v, F and writes x, v (5 x 24 B) and reads the build-time
+    position for the skin check (24 B)."""
+    dens = 4.0 * kmean + 24.0 + 8.0
+    force = 4.0 * kmean + 24.0 + 8.0 + 24.0
+    vv = 5 * 24.0 + 24.0
+    return dict(density=dens, force=force, vv=vv, step=dens + force + vv)
+
+
+def cpu_baseline(pos, vel, L, nthreads, sample_steps=2):
+    """Oracle (C restatement of the reference's serial CPU path) on the full workload:
+    per-step time = (T(k steps) - T(0 steps)) / k, both runs including the initial list
+    build and force."""
+    from msmpscu_gb300 import lattice as lt
+    from oracle import pyoracle as po
+    n = len(pos)
+    tabs = po.make_tables(po.POT_CR, [lt.CU_CR[k] for k in ("A", "xi", "p", "q", "r0")],
+                          lt.CU_RC, 10000, 10000, 20.0, want_embed=False)
+    t = po.Tables(tabs, po.FS, lt.CU_RC)
+    box = po.make_box([0, 0, 0], L)
+    ones = np.ones(n, np.int32)
+    cm = np.array([lt.CU_MASS])
+    t0 = time.perf_counter()
+    po.md(pos, vel, ones, ones, box, t, cm, DT, 0, lt.CU_RC_NL, skin_trigger=0.15, mxkvois=80,
+          nthreads=nthreads)
+    t1 = time.perf_counter()
+    po.md(pos, vel, ones, ones, box, t, cm, DT, sample_steps, lt.CU_RC_NL, skin_trigger=0.15,
+          mxkvois=80, nthreads=nthreads)
+    t2 = time.perf_counter()
+    per_step = max((t2 - t1) - (t1 - t0), 1e-9) / sample_steps
+    return n / per_step, per_step
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    pos, vel, L = workload()
+    n = len(pos)
+    threads = os.cpu_count() or 1
+    from msmpscu_gb300 import lattice as lt
+    from oracle import pyoracle as po
+    tabs = po.make_tables(po.POT_CR, [lt.CU_CR[k] for k in ("A", "xi", "p", "q", "r0")],
+                          lt.CU_RC, 10000, 10000, 20.0, want_embed=False)
+    t = po.Tables(tabs, po.FS, lt.CU_RC)
+    box = po.make_box([0, 0, 0], L)
+    ones = np.ones(n, np.int32)
+    cm = np.array([lt.CU_MASS])
+    # warm-up: W steps (list build + forces), then the timed K steps run as one NVE segment,
+    # capped at a time budget so the whole run ends within a few minutes
+    p1, v1, _, _, _ = po.md(pos, vel, ones, ones, box, t, cm, DT, args.warmup, lt.CU_RC_NL,
+                            skin_trigger=0.15, mxkvois=80, nthreads=threads)
+    t0 = time.perf_counter()
+    po.md(p1, v1, ones, ones, box, t, cm, DT, 0, lt.CU_RC_NL, skin_trigger=0.15, mxkvois=80,
+          nthreads=threads)
+    t_setup = time.perf_counter() - t0
+    per_step_guess = None
+    done = 0
+    budget = args.ref_budget_s
+    chunk = max(1, min(args.steps, 5))
+    t_total = 0.0
+    while done < args.steps:
+        k = min(chunk, args.steps - done)
+        ta = time.perf_counter()
+        p1, v1, _, _, _ = po.md(p1, v1, ones, ones, box, t, cm, DT, k, lt.CU_RC_NL,
+                                skin_trigger=0.15, mxkvois=80, nthreads=threads)
+        dt = time.perf_counter() - ta - t_setup
+        t_total += max(dt, 1e-9)
+        done += k
+        if t_total > budget:
+            break
+    value = n * done / t_total
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
+            "steps": done, "warmup": args.warmup, "ms_per_step": 1e3 * t_total / done,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded fcc Cu lattice)",
+            "config": {"workload": "fcc Cu 80x80x80 cells, 2,048,000 atoms, Cleri-Rosato, NVE dt=1fs, skin 0.3 A",
+                       "atoms": n, "parallelism": "replicas"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": "%d of %d NVE steps of the full 2,048,000-atom system "
+                                       "(oracle, OpenMP over atoms)" % (done, args.steps)},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    ws, rank, local = dist_env()
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        import torch
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    device = local if ws > 1 else 0
+    from msmpscu_gb300 import build as lib_build
+    lib_build.build()
+    pos, vel, L = workload()
+    n = len(pos)
+    prec = args.precision
+    e = make_engine(n, prec, device)
+    box = [(n, (0, 0, 0), tuple(L), (1, 1, 1))]
+    e.copyin(box, pos, vel)
+    e.run_steps(args.warmup, DT)
+    if dist:
+        dist.barrier()
+    l0 = e.launches
+    with Clocks(device) as clk:
+        ms, rebuilds = e.time_steps(args.steps, DT)
+    launches = e.launches - l0
+    if dist:
+        import torch
+        tt = torch.tensor([ms], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms = float(tt.item())
+    value = ws * n * args.steps / (ms / 1e3)
+    kmax, kmean = e.list_stats()
+    passes = e.time_passes(5)
+    bm = bytes_model(kmean)
+    hbm, peak_kind = peaks()
+    dom = "force" if passes["force"] >= passes["density"] else "density"
+    achieved = bm[dom] * n / (passes[dom] * 1e-3) / 1e9
+    traffic = read_traffic(prec, dom)
+
+    # e2e: the reference-facing C-ABI with pinned host buffers: copy-in of the state, the K
+    # steps, copy-out of positions, velocities and forces, all inside the timed region
+    xp, xp1, ty, st, fo = pinned_buffers(n)
+    xp[:] = np.ascontiguousarray(pos.T).reshape(-1)
+    xp1[:] = np.ascontiguousarray(vel.T).reshape(-1)
+    ty[:] = 1
+    st[:] = 1
+    barr = e.pack_boxes(box)
+    xo, vo = np.empty_like(xp), np.empty_like(xp1)
+    e.synchronize()
+    t0 = time.perf_counter()
+    e.copyin_raw(barr, 1, ty, st, xp, xp1)
+    e.run_steps(args.steps, DT)
+    e.copyout_raw(xo, vo, fo)
+    t1 = time.perf_counter()
+    e2e = n * args.steps / (t1 - t0)
+    h2d = n * (24 + 24 + 4 + 4) / args.steps
+    d2h = n * (24 + 24 + 24) / args.steps
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        cv, per = cpu_baseline(pos, vel, L, threads, sample_steps=args.cpu_steps)
+        cpu = {"value": cv, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": "%d NVE steps of the full 2,048,000-atom system (oracle, OpenMP over "
+                         "atoms), per-step time %.2f s" % (args.cpu_steps, per)}
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64" if prec == "fp64" else "f32+f64",
+                "data": "synthetic (seeded fcc Cu lattice, Gaussian displacements, Maxwell-Boltzmann velocities)",
+                "config": {"workload": "fcc Cu 80x80x80 cells, 2,048,000 atoms, Cleri-Rosato, sigma 0.05 A, "
+                                       "600 K, NVE dt=1fs, skin 0.3 A (rebuild at 0.15 A)",
+                           "atoms": n, "precision": prec, "parallelism": "replicas" if ws > 1 else "single GPU",
+                           "l2": "inputs larger than L2 (~0.9 GB touched per step)",
+                           "rebuilds_in_timed_steps": rebuilds, "mean_neighbours": kmean,
+                           "max_neighbours": kmax},
+                "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm,
+                             "unit": "GB/s", "frac": achieved / hbm, "traffic": traffic,
+                             "peak_kind": peak_kind,
+                             "algorithmic_bytes_per_atom": bm[dom]},
+                "step_roofline": {"achieved": bm["step"] * value / ws / 1e9, "peak": hbm, "unit": "GB/s",
+                                  "frac": bm["step"] * value / ws / 1e9 / hbm,
+                                  "bytes_per_atom_step": bm["step"]},
+                "pass_ms": passes,
+                "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+                "cpu_baseline": cpu,
+                "clocks": clk.summary(),
+                "gpu_launches": launches}
+        print(json.dumps(line), flush=True)
+    e.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+def pinned_buffers(n):
+    try:
+        import torch
+        if torch.cuda.is_available():
+            mk = lambda k, dt: torch.empty(k, dtype=dt, pin_memory=True).numpy()
+            return (mk(3 * n, torch.float64), mk(3 * n, torch.float64), mk(n, torch.int32),
+                    mk(n, torch.int32), mk(3 * n, torch.float64))
+    except Exception:
+        pass
+    return (np.empty(3 * n), np.empty(3 * n), np.empty(n, np.int32), np.empty(n, np.int32),
+            np.empty(3 * n))
+
+
+def read_traffic(prec, kernel):
+    """DRAM bytes per launch of the dominant kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "dram_traffic.txt")
+    try:
+        for line in open(path):
+            p = line.split()
+            if len(p) >= 3 and not line.startswith("#") and p[0] == prec and p[1] == kernel:
+                return float(p[2])
+    except OSError:
+        pass
+    return None
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-steps", type=int, default=2)
+    ap.add_argument("--ref-budget-s", type=float, default=150.0)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

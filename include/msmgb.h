@@ -1,0 +1,212 @@
+/*
+ * msmgb.h -- C ABI of the GB300 many-body MD hot path (libmsmgb.so).
+ *
+ * The entry points replace the CUDA Fortran routines that msmpscu's MD loop calls through
+ * its force class (MDForceClassGPU, MD_ForceClass_Register_GPU.F90:248-259), its GPU
+ * neighbour list (MD_NeighborsList_GPU.F90) and its GPU integrator (MD_DiffScheme_GPU.F90).
+ * All arguments are plain C types; host arrays are read or written only during the call.
+ * Every function returns MSMGB_OK (0) or a negative MSMGB_ERR_* code; the message of the
+ * last failure is available through msmgb_last_error().
+ *
+ * Units: the library is unit-agnostic.  Positions, box, cutoffs, tables, masses and time
+ * step must be given in one consistent system (msmpscu's host uses CGS; the tests use
+ * Angstrom, eV, fs and masses in eV*fs^2/A^2).  Per-atom arrays use the reference's layout:
+ * XP(N,3) column-major, i.e. x[0..N), y[N..2N), z[2N..3N); atom types ITYP are 1-based.
+ *
+ * Threading: one context per host thread; a context is not thread-safe.  All device work
+ * of a context is issued on one CUDA stream (msmgb_stream()).
+ */
+#ifndef MSMGB_H
+#define MSMGB_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes (replace the reference's `stop` statements) ------------------------ */
+#define MSMGB_OK                 0
+#define MSMGB_ERR_ARG           -1   /* bad argument / call order                          */
+#define MSMGB_ERR_CUDA          -2   /* CUDA runtime error (message has the CUDA text)     */
+#define MSMGB_ERR_NL_OVERFLOW   -3   /* an atom has more than MXKVOIS neighbours           */
+#define MSMGB_ERR_OUT_OF_BOX    -4   /* an active atom lies outside its box (cell binning) */
+#define MSMGB_ERR_RHO_RANGE     -5   /* EAM: density beyond the F(rho) table               */
+#define MSMGB_ERR_BOX_TOO_SMALL -6   /* box edge < 2 * list cutoff (minimum image ambiguous)*/
+#define MSMGB_ERR_NO_DEVICE     -7   /* no CUDA device / extension unusable                */
+#define MSMGB_ERR_CAPACITY      -8   /* more atoms / boxes than the context was sized for  */
+
+/* ---- potential types (MDForceTable%PotType) ------------------------------------------- */
+#define MSMGB_FS_TYPE  0
+#define MSMGB_EAM_TYPE 1
+
+/* ---- arithmetic of the force passes ---------------------------------------------------- */
+#define MSMGB_PREC_FP64  0   /* plain FP64, the reference's arithmetic                   */
+#define MSMGB_PREC_MIXED 1   /* FP32 pair/density/table terms, FP64 accumulation,
+                                FP64 positions and integration                           */
+
+/* ---- atom status bits (MD_Const.F90:78-96) ---------------------------------------------- */
+#define MSMGB_STATU_ACTIVE    1
+#define MSMGB_STATU_FIXPOSX   2
+#define MSMGB_STATU_FIXPOSY   4
+#define MSMGB_STATU_FIXPOSZ   8
+#define MSMGB_STATU_FIXVELX   16
+#define MSMGB_STATU_FIXVELY   32
+#define MSMGB_STATU_FIXVELZ   64
+#define MSMGB_STATU_OUTOFBOX  65536
+#define MSMGB_STATU_REFLECT   131072
+#define MSMGB_STATU_TRANSMIT  262144
+
+/* ---- output ordering -------------------------------------------------------------------- */
+#define MSMGB_ORDER_ORIGINAL 0   /* the caller's atom order (reference: hm_GIDINV copy-out) */
+#define MSMGB_ORDER_SORTED   1   /* the library's cell-sorted device order                 */
+
+typedef struct msmgb_ctx msmgb_ctx;
+
+/* Context parameters: the control-file fields of the neighbour list and integrator
+ * (SimMDCtrl NB_RM, NB_MXNBS, NB_UPTAB; MD_TypeDef_SimCtrlParam.F90:116-123). */
+typedef struct {
+    int    device;        /* CUDA device ordinal                                          */
+    int    max_atoms;     /* capacity: total atoms over all boxes                         */
+    int    max_boxes;     /* capacity: number of boxes (1 for a single box)               */
+    int    mxkvois;       /* NB_MXNBS: neighbour slots per atom (ELL width)               */
+    double rc_nl;         /* NB_RM: neighbour-list cutoff (absolute length)               */
+    double skin_trigger;  /* rebuild when max displacement since the last build exceeds
+                             this (> 0); <= 0 selects the reference's fixed interval      */
+    int    nb_uptab;      /* NB_UPTAB: rebuild interval when skin_trigger <= 0            */
+    int    precision;     /* MSMGB_PREC_FP64 or MSMGB_PREC_MIXED                          */
+    void  *stream;        /* cudaStream_t to issue on; NULL = the context makes its own   */
+} msmgb_params;
+
+/* Force table: the MDForceTable fields the GPU passes read
+ * (MD_TypeDef_ForceTable.F90:117-155).  Arrays are in the reference's column-major layout:
+ * POTR(NKIND,NTAB) has entry (k,i) at potr[(i-1)*nkind + (k-1)].  Grid point i is at
+ * r = (i*sqrt(rmax)/ntab)^2.  The EAM fields are ignored for MSMGB_FS_TYPE. */
+typedef struct {
+    int           pottype;          /* MSMGB_FS_TYPE or MSMGB_EAM_TYPE                     */
+    int           ntab, nkind;
+    double        rmax;             /* Rmax = max RU                                        */
+    const double *potr, *fpotr;     /* V*r (convention of the potential), -dV/dr*r         */
+    const double *potb, *fpotb;     /* rho(r), -drho/dr                                     */
+    int           nembd, nkind1;
+    double        rhod;             /* RHOD: F(rho) table spacing                           */
+    const double *fembd, *dfembd;   /* F(rho), dF/drho at rho = (i-1)*RHOD                  */
+    int           ngroup;           /* atom types                                           */
+    const int    *kpair;            /* KPAIR(NGROUP,NGROUP), 1-based table ids              */
+    const int    *kembd;            /* KEMBD(NGROUP), 1-based (EAM only)                    */
+    double        ru;               /* force cutoff RU (the passes use RU^2 = max RU^2)     */
+} msmgb_forcetable;
+
+/* One periodic (or not) orthorhombic box of a batch (SimMDBox BOXLOW, ZL; CtrlParam IFPD). */
+typedef struct {
+    int    natom;
+    double lo[3];
+    double len[3];
+    int    ifpd[3];
+} msmgb_box;
+
+/* ---- context ------------------------------------------------------------------------- */
+/* Allocates all device memory for the given capacities (replaces Initialize_DEVICES +
+ * Allocate_Working_Variables, MD_Globle_Variables_GPU.F90:767-857). */
+int  msmgb_create(msmgb_ctx **ctx, const msmgb_params *params);
+int  msmgb_destroy(msmgb_ctx *ctx);
+const char *msmgb_last_error(const msmgb_ctx *ctx);
+void *msmgb_stream(const msmgb_ctx *ctx);          /* cudaStream_t of the context */
+int  msmgb_set_precision(msmgb_ctx *ctx, int precision);
+/* number of kernels this library has launched on the context so far */
+int64_t msmgb_launch_count(const msmgb_ctx *ctx);
+int  msmgb_synchronize(msmgb_ctx *ctx);
+
+/* ---- force class (MD_ForceClass_Register_GPU.F90:248-259) ------------------------------ */
+/* pIniForcetable: INITIALIZE_FS/EAM_Force_Table_DEV (MD_FS_ForceTable_GPU.F90:178-257,
+ * MD_EAM_ForceTable_GPU.F90:192-278): copies the host tables to the device. */
+int  msmgb_init_forcetable(msmgb_ctx *ctx, const msmgb_forcetable *ft);
+/* pClrForcetable: CLEAR_FS/EAM_Force_Table_DEV */
+int  msmgb_clear_forcetable(msmgb_ctx *ctx);
+/* pCalForce: CALFORCE_FS/EAM_Force_Table2A_DEV (MD_FS_ForceTable_GPU.F90:934-994,
+ * MD_EAM_ForceTable_GPU.F90:950-1010): density pass, F'(rho), force pass. */
+int  msmgb_calforce(msmgb_ctx *ctx);
+/* pCalPTensor: CALPTENSOR_*_Force_Table2A_DEV (MD_FS_ForceTable_GPU.F90:1348-1411):
+ * forces plus the 3x3 virial of every box; vtensor receives 9*nbox values (row-major per
+ * box), NOT divided by the number of boxes (reference quirk Q9, :1462-1463). */
+int  msmgb_calptensor(msmgb_ctx *ctx, double *vtensor);
+/* pCalEpot: CALEPOT_*_Force_Table2A_DEV (MD_FS_ForceTable_GPU.F90:1720-1742): per-atom
+ * potential energy, kept on the device (msmgb_copyout_epot). */
+int  msmgb_calepot(msmgb_ctx *ctx);
+/* pCalEDen: CALDEN_*_Force_Table2A_DEV (MD_FS_ForceTable_GPU.F90:875-930): F'(rho) only */
+int  msmgb_calden(msmgb_ctx *ctx);
+
+/* ---- state transfer (MD_Globle_Variables_GPU.F90 CopyIn/CopyOut_SimBox_DEV) -------------- */
+/* Uploads a batch of boxes (nbox >= 1, boxes concatenated in order).  xp and xp1 are
+ * 3*N arrays in XP(N,3) column-major layout; xp1 (velocities) may be NULL (zero).
+ * Invalidates the neighbour list. */
+int  msmgb_copyin_simbox(msmgb_ctx *ctx, int nbox, const msmgb_box *boxes, const int *ityp,
+                         const int *statu, const double *xp, const double *xp1);
+/* masses CM(NGROUP) per atom type */
+int  msmgb_set_masses(msmgb_ctx *ctx, int ngroup, const double *cm);
+/* any pointer may be NULL; order = MSMGB_ORDER_ORIGINAL or MSMGB_ORDER_SORTED */
+int  msmgb_copyout_simbox(msmgb_ctx *ctx, double *xp, double *xp1, int *statu, double *dis,
+                          int order);
+int  msmgb_copyout_force(msmgb_ctx *ctx, double *fp, int order);       /* FP(N,3)          */
+int  msmgb_copyout_epot(msmgb_ctx *ctx, double *epot, int order);     /* EPOT(N)          */
+int  msmgb_copyout_den(msmgb_ctx *ctx, double *den, int order);       /* F'(rho_i)        */
+/* sorted position -> original index map (hm_GID), N ints */
+int  msmgb_copyout_gid(msmgb_ctx *ctx, int *gid);
+
+/* ---- neighbour list (MD_NeighborsList_GPU.F90) --------------------------------------- */
+/* Cal_NeighBoreList_DEV (:2316-2372 -> Cal_NeighBoreList2C_0_DEV :1347-1732): cell-sorts
+ * the atoms on the device and builds the full list with the FP64 rule d^2 < rc_nl^2. */
+int  msmgb_cal_neighborelist(msmgb_ctx *ctx);
+/* Copyout_NeighboreList (:718-737): KVOIS(N) and INDI(ld, mxkvois) column-major, 0-based
+ * neighbour ids; with MSMGB_ORDER_ORIGINAL both atoms and ids are in the caller's order. */
+int  msmgb_copyout_neighborelist(msmgb_ctx *ctx, int *kvois, int *indi, int ld, int order);
+
+/* ---- integrator (MD_DiffScheme_GPU.F90) ------------------------------------------------- */
+/* Predictor_DEV (:604-682): x += h v + h^2/2 F/m with PBC wrap, DIS += dx, v += h/2 F/m */
+int  msmgb_predictor(msmgb_ctx *ctx, double h);
+/* Correction_DEV (:821-848): v += h/2 F/m */
+int  msmgb_correction(msmgb_ctx *ctx, double h);
+/* For_One_Step (MD_Method_GenericMD_GPU.F90:496-659) repeated nsteps times: predictor,
+ * list rebuild when the skin trigger fires (or every NB_UPTAB steps), force, corrector.
+ * The steps run as one CUDA graph per step with the rebuild predicated on the device.
+ * rebuilds (may be NULL) receives the number of list rebuilds done. */
+int  msmgb_run_steps(msmgb_ctx *ctx, int nsteps, double h, int *rebuilds);
+/* The same steps split for timing loops: msmgb_enqueue_steps issues nsteps step graphs on
+ * the context stream and returns without synchronising; msmgb_finish_steps applies the
+ * pending corrector, synchronises and reports errors and the rebuild count since the last
+ * finish.  No counterpart in the reference. */
+int  msmgb_enqueue_steps(msmgb_ctx *ctx, int nsteps, double h);
+int  msmgb_finish_steps(msmgb_ctx *ctx, double h, int *rebuilds);
+/* Runs nsteps like msmgb_run_steps and reports the device time of the steps (CUDA events
+ * on the context stream, synchronised on both sides) in *ms.  No counterpart in the
+ * reference (it times with host CPU_TIME, MD_Method_GenericMD_GPU.F90:246). */
+int  msmgb_time_steps(msmgb_ctx *ctx, int nsteps, double h, float *ms, int *rebuilds);
+/* Average device time (ms) of one launch of each pass over `reps` launches:
+ * out[0] density pass, out[1] force pass, out[2] list rebuild, out[3] fused integrator
+ * (timed with h = 0, which leaves the state unchanged).  No counterpart in the reference. */
+int  msmgb_time_passes(msmgb_ctx *ctx, int reps, float *out);
+/* Largest and mean neighbour count of the current list. */
+int  msmgb_list_stats(msmgb_ctx *ctx, int *maxk, double *meank);
+
+/* ---- differentiation --------------------------------------------------------------------- */
+/* Hessian-vector product of the table-mode force (exact derivative of the interpolants):
+ * hv = -dF/dx . v.  v and hv are 3*N arrays in XP layout, caller's order.  No counterpart in
+ * the reference: it replaces finite-difference force pairs (MD_Method_ART_GPU.F90:454-576). */
+int  msmgb_hvp(msmgb_ctx *ctx, const double *v, double *hv);
+
+/* ---- host-side table generator (Create_Interaction_ForceTable,
+ *      MD_TypeDef_ForceTable.F90:890-1056) -------------------------------------------------- */
+#define MSMGB_POT_CR          1   /* Cleri-Rosato TB-SMA, FS form; prm = A, xi, p, q, r0     */
+#define MSMGB_POT_MARINICA2   2   /* Marinica EAM2 for W (EAM form); prm unused              */
+#define MSMGB_POT_ACKLAND_WW  3   /* Ackland-Thetford W, FS form; prm unused                 */
+/* Fills POTR/FPOTR/POTB/FPOTB (ntab each) and, if fembd/dfembd are non-NULL, F/F' (nembd
+ * each); returns RHOD = rhoscal * max(POTB) / nembd through *rhod.  Lengths in Angstrom,
+ * energies in eV. */
+int  msmgb_create_forcetable(int pot, const double *prm, double rmax, int ntab, int nembd,
+                             double rhoscal, double *potr, double *fpotr, double *potb,
+                             double *fpotb, double *fembd, double *dfembd, double *rhod);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

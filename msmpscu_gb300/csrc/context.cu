@@ -1,0 +1,852 @@
+// context.cu -- the C ABI: context, table upload, state transfer, the MD step graph.
+//
+// Device state lives in one context object instead of the reference's module globals
+// (dm_WorkSpace, dm_FTableWS, dm_Neighbors; MD_Globle_Variables_GPU.F90:158-194).  All
+// work is issued on the context's stream; the per-step sequence of For_One_Step
+// (MD_Method_GenericMD_GPU.F90:596-627: Predictor_DEV, Cal_NeighBoreList_DEV every
+// NB_UPTAB steps, CalForce, Correction_DEV) is captured once as a CUDA graph with the list
+// rebuild predicated on a device flag, so a step costs one graph launch and no host sync.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+
+#include "msmgb_internal.cuh"
+
+using namespace msmgb;
+
+namespace msmgb {
+
+int set_err(msmgb_ctx *c, int code, const std::string &msg)
+{
+    if (c) c->err = msg;
+    return code;
+}
+
+int cuda_err(msmgb_ctx *c, cudaError_t e, const char *what)
+{
+    char buf[512];
+    snprintf(buf, sizeof(buf), "CUDA error in %s: %s (%s)", what, cudaGetErrorName(e),
+             cudaGetErrorString(e));
+    return set_err(c, MSMGB_ERR_CUDA, buf);
+}
+
+int check_launch(msmgb_ctx *c, const char *what)
+{
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_err(c, e, what);
+    return MSMGB_OK;
+}
+
+}  // namespace msmgb
+
+#define CK(call, what)                                   \
+    do {                                                 \
+        cudaError_t e_ = (call);                         \
+        if (e_ != cudaSuccess) return cuda_err(c, e_, what); \
+    } while (0)
+
+#define RET(x)                      \
+    do {                            \
+        int r_ = (x);               \
+        if (r_ != MSMGB_OK) return r_; \
+    } while (0)
+
+static inline int nblk(long n, int b) { return (int)((n + b - 1) / b); }
+
+template <typename T>
+static cudaError_t dalloc(T **p, size_t count)
+{
+    return cudaMalloc((void **)p, sizeof(T) * (count ? count : 1));
+}
+
+static void free_graph(msmgb_ctx *c)
+{
+    if (c->step_graph) cudaGraphExecDestroy(c->step_graph);
+    c->step_graph = nullptr;
+    c->graph_n = -1;
+}
+
+static int use_device(msmgb_ctx *c)
+{
+    CK(cudaSetDevice(c->p.device), "cudaSetDevice");
+    return MSMGB_OK;
+}
+
+// ---- small kernels of the ABI -------------------------------------------------------------
+__global__ void k_pack(DevAtoms a, const double *xp, const double *xp1, const int *ityp,
+                       const int *statu, const int *boxid)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int n = a.n;
+    if (i >= n) return;
+    double x = xp[i], y = xp[n + i], z = xp[2 * n + i];
+    a.pos[i] = make_double4_32a(x, y, z, 0.0);
+    a.pos_bld[i] = make_double4_32a(x, y, z, 0.0);
+    a.pos32[i] = make_float4((float)x, (float)y, (float)z, 0.0f);
+    a.vx[i] = xp1 ? xp1[i] : 0.0;
+    a.vy[i] = xp1 ? xp1[n + i] : 0.0;
+    a.vz[i] = xp1 ? xp1[2 * n + i] : 0.0;
+    a.fx[i] = 0.0; a.fy[i] = 0.0; a.fz[i] = 0.0;
+    a.dx[i] = 0.0; a.dy[i] = 0.0; a.dz[i] = 0.0;
+    a.ityp[i] = ityp[i];
+    a.statu[i] = statu[i];
+    a.gid[i] = i;
+    a.boxid[i] = boxid[i];
+    a.den[i] = 0.0;
+    a.epot[i] = 0.0;
+}
+
+// sorted -> caller layout: dst[k*n + g] = src_k[s] with g = gid[s] (or s when sorted)
+__global__ void k_unpack3(const double *s0, const double *s1, const double *s2, const int *gid,
+                          int n, int sorted, double *dst)
+{
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    int g = sorted ? s : gid[s];
+    dst[g] = s0[s];
+    if (s1) dst[n + g] = s1[s];
+    if (s2) dst[2 * n + g] = s2[s];
+}
+
+__global__ void k_unpack_pos(const double4_32a *pos, const int *gid, int n, int sorted, double *dst)
+{
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    int g = sorted ? s : gid[s];
+    double4_32a p = pos[s];
+    dst[g] = p.x;
+    dst[n + g] = p.y;
+    dst[2 * n + g] = p.z;
+}
+
+__global__ void k_unpack_int(const int *src, const int *gid, int n, int sorted, int *dst)
+{
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    dst[sorted ? s : gid[s]] = src[s];
+}
+
+// ---- context ------------------------------------------------------------------------------
+extern "C" int msmgb_create(msmgb_ctx **out, const msmgb_params *p)
+{
+    if (!out || !p) return MSMGB_ERR_ARG;
+    *out = nullptr;
+    if (p->max_atoms <= 0 || p->max_boxes <= 0 || p->mxkvois <= 0 || p->rc_nl <= 0.0)
+        return MSMGB_ERR_ARG;
+    if (p->precision != MSMGB_PREC_FP64 && p->precision != MSMGB_PREC_MIXED) return MSMGB_ERR_ARG;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= p->device || p->device < 0) {
+        cudaGetLastError();
+        return MSMGB_ERR_NO_DEVICE;
+    }
+    msmgb_ctx *c = new msmgb_ctx();
+    c->p = *p;
+    c->cap_atoms = p->max_atoms;
+    c->cap_boxes = p->max_boxes;
+    int rc = use_device(c);
+    if (rc) { delete c; return rc; }
+    auto fail = [&](cudaError_t e, const char *w) {
+        cuda_err(c, e, w);
+        msmgb_destroy(c);
+        return MSMGB_ERR_CUDA;
+    };
+    cudaError_t e;
+    if (p->stream) {
+        c->stream = (cudaStream_t)p->stream;
+    } else {
+        if ((e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) != cudaSuccess)
+            return fail(e, "stream");
+        c->own_stream = true;
+    }
+    const size_t N = (size_t)c->cap_atoms;
+    DevAtoms &a = c->a;
+    a.mxk = p->mxkvois;
+    a.ld = c->cap_atoms;
+#define AL(ptr, cnt)                                            \
+    if ((e = dalloc(&(ptr), (cnt))) != cudaSuccess) return fail(e, "cudaMalloc " #ptr);
+    AL(a.pos, N) AL(a.pos32, N) AL(a.pos_bld, N)
+    AL(a.vx, N) AL(a.vy, N) AL(a.vz, N)
+    AL(a.fx, N) AL(a.fy, N) AL(a.fz, N)
+    AL(a.dx, N) AL(a.dy, N) AL(a.dz, N)
+    AL(a.ityp, N) AL(a.statu, N) AL(a.gid, N) AL(a.boxid, N)
+    AL(a.den, N) AL(a.epot, N) AL(a.den32, N)
+    AL(a.kvois, N) AL(a.indi, N * (size_t)p->mxkvois)
+    AL(c->cell_of, N) AL(c->perm, N)
+    AL(c->dbox, (size_t)c->cap_boxes)
+    AL(c->cm, (size_t)kMaxGroups)
+    AL(c->flags, (size_t)kFlagWords)
+    AL(c->maxdisp, 1)
+    AL(c->virial, 6 * (size_t)c->cap_boxes)
+#undef AL
+    // permutation staging: double4_32a + 6 doubles + 5 ints per atom
+    if ((e = cudaMalloc(&c->scratch, N * (32 + 48 + 20) + 256)) != cudaSuccess) return fail(e, "scratch");
+    if ((e = cudaMallocHost((void **)&c->h_flags, sizeof(int) * kFlagWords)) != cudaSuccess) return fail(e, "pinned");
+    if ((e = cudaMallocHost((void **)&c->h_virial, sizeof(double) * 6 * c->cap_boxes)) != cudaSuccess) return fail(e, "pinned");
+    if ((e = cudaMemsetAsync(c->flags, 0, sizeof(int) * kFlagWords, c->stream)) != cudaSuccess) return fail(e, "memset");
+    if ((e = cudaMemsetAsync(c->maxdisp, 0, sizeof(unsigned long long), c->stream)) != cudaSuccess) return fail(e, "memset");
+    a.flags = c->flags;
+    a.maxdisp = c->maxdisp;
+    a.virial = c->virial;
+    a.box = c->dbox;
+    a.cm = c->cm;
+    a.n = 0;
+    *out = c;
+    return MSMGB_OK;
+}
+
+extern "C" int msmgb_destroy(msmgb_ctx *c)
+{
+    if (!c) return MSMGB_OK;
+    cudaSetDevice(c->p.device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    free_graph(c);
+    DevAtoms &a = c->a;
+    void *ptrs[] = {a.pos, a.pos32, a.pos_bld, a.vx, a.vy, a.vz, a.fx, a.fy, a.fz,
+                    a.dx, a.dy, a.dz, a.ityp, a.statu, a.gid, a.boxid, a.den, a.epot,
+                    a.den32, a.kvois, a.indi, c->cell_of, c->perm, c->dbox, c->cm,
+                    c->flags, c->maxdisp, c->virial, c->scratch, c->cell_start,
+                    c->cell_cursor, c->scan_tmp, c->tab_mem};
+    for (void *q : ptrs)
+        if (q) cudaFree(q);
+    if (c->h_flags) cudaFreeHost(c->h_flags);
+    if (c->h_virial) cudaFreeHost(c->h_virial);
+    if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return MSMGB_OK;
+}
+
+extern "C" const char *msmgb_last_error(const msmgb_ctx *c) { return c ? c->err.c_str() : "null context"; }
+extern "C" void *msmgb_stream(const msmgb_ctx *c) { return c ? (void *)c->stream : nullptr; }
+extern "C" int64_t msmgb_launch_count(const msmgb_ctx *c) { return c ? c->launches : 0; }
+
+extern "C" int msmgb_set_precision(msmgb_ctx *c, int precision)
+{
+    if (!c) return MSMGB_ERR_ARG;
+    if (precision != MSMGB_PREC_FP64 && precision != MSMGB_PREC_MIXED)
+        return set_err(c, MSMGB_ERR_ARG, "precision must be MSMGB_PREC_FP64 or MSMGB_PREC_MIXED");
+    if (precision != c->p.precision) {
+        c->p.precision = precision;
+        c->force_valid = false;
+        free_graph(c);
+    }
+    return MSMGB_OK;
+}
+
+extern "C" int msmgb_synchronize(msmgb_ctx *c)
+{
+    if (!c) return MSMGB_ERR_ARG;
+    RET(use_device(c));
+    CK(cudaStreamSynchronize(c->stream), "synchronize");
+    return MSMGB_OK;
+}
+
+// reads the device flags; converts error bits into a status code
+static int poll_flags(msmgb_ctx *c)
+{
+    CK(cudaMemcpyAsync(c->h_flags, c->flags, sizeof(int) * kFlagWords, cudaMemcpyDeviceToHost, c->stream),
+       "flag read");
+    CK(cudaStreamSynchronize(c->stream), "synchronize");
+    int e = c->h_flags[kFlagErr];
+    if (e) {
+        CK(cudaMemsetAsync(c->flags + kFlagErr, 0, sizeof(int), c->stream), "flag clear");
+        if (e & kErrOverflow) {
+            char buf[160];
+            snprintf(buf, sizeof(buf), "neighbour list overflow: an atom has more than MXKVOIS=%d neighbours", c->p.mxkvois);
+            return set_err(c, MSMGB_ERR_NL_OVERFLOW, buf);
+        }
+        if (e & kErrOutOfBox) return set_err(c, MSMGB_ERR_OUT_OF_BOX, "an active atom lies outside its box");
+        if (e & kErrRho) return set_err(c, MSMGB_ERR_RHO_RANGE, "electron density beyond the F(rho) table");
+    }
+    return MSMGB_OK;
+}
+
+// ---- force table ----------------------------------------------------------------------------
+extern "C" int msmgb_init_forcetable(msmgb_ctx *c, const msmgb_forcetable *ft)
+{
+    if (!c || !ft) return MSMGB_ERR_ARG;
+    if (ft->pottype != MSMGB_FS_TYPE && ft->pottype != MSMGB_EAM_TYPE)
+        return set_err(c, MSMGB_ERR_ARG, "unknown potential type");
+    if (ft->ntab < 2 || ft->nkind < 1 || ft->rmax <= 0.0 || !ft->potr || !ft->fpotr || !ft->potb || !ft->fpotb)
+        return set_err(c, MSMGB_ERR_ARG, "incomplete pair tables");
+    if (ft->ngroup < 1 || ft->ngroup > kMaxGroups || !ft->kpair)
+        return set_err(c, MSMGB_ERR_ARG, "NGROUP must be 1..16 with KPAIR given");
+    const bool eam = ft->pottype == MSMGB_EAM_TYPE;
+    if (eam && (ft->nembd < 2 || ft->nkind1 < 1 || !ft->fembd || !ft->dfembd || !ft->kembd || ft->rhod <= 0.0))
+        return set_err(c, MSMGB_ERR_ARG, "EAM tables need FEMBD, DFEMBD, KEMBD and RHOD");
+    RET(use_device(c));
+    DevTables t{};
+    t.pottype = ft->pottype;
+    t.ntab = ft->ntab;
+    t.nkind = ft->nkind;
+    t.ntp = ft->ntab + 2;
+    t.csi = (double)ft->ntab / std::sqrt(ft->rmax);
+    t.ru2 = ft->ru * ft->ru;
+    t.ngroup = ft->ngroup;
+    for (int i = 0; i < ft->ngroup; ++i)
+        for (int j = 0; j < ft->ngroup; ++j) {
+            int id = ft->kpair[j * ft->ngroup + i];      // KPAIR(i,j), column-major
+            if (id < 1 || id > ft->nkind) return set_err(c, MSMGB_ERR_ARG, "KPAIR id out of range");
+            t.kpair[j * ft->ngroup + i] = id - 1;
+        }
+    t.nembd = eam ? ft->nembd : 0;
+    t.nkind1 = eam ? ft->nkind1 : 0;
+    t.nep = eam ? ft->nembd + 2 : 0;
+    t.rhod = eam ? ft->rhod : 1.0;
+    if (eam)
+        for (int i = 0; i < ft->ngroup; ++i) {
+            int id = ft->kembd[i];
+            if (id < 1 || id > ft->nkind1) return set_err(c, MSMGB_ERR_ARG, "KEMBD id out of range");
+            t.kembd[i] = id - 1;
+        }
+    // padded rows: index 0 -> 0, 1..NTAB -> table, NTAB+1 -> T(NTAB) (quirk Q6)
+    const size_t rowp = (size_t)t.ntp, nk = (size_t)t.nkind;
+    const size_t nd = 4 * nk * rowp + (eam ? 2 * (size_t)t.nkind1 * t.nep : 0);
+    const size_t nf = 4 * nk * rowp;
+    std::vector<double> hd(nd, 0.0);
+    std::vector<float> hf(nf, 0.0f);
+    const double *src[4] = {ft->potr, ft->fpotr, ft->potb, ft->fpotb};
+    for (int q = 0; q < 4; ++q)
+        for (size_t k = 0; k < nk; ++k) {
+            double *row = hd.data() + ((size_t)q * nk + k) * rowp;
+            for (int i = 1; i <= t.ntab; ++i) row[i] = src[q][(size_t)(i - 1) * nk + k];
+            row[t.ntab + 1] = row[t.ntab];
+            float *rf = hf.data() + ((size_t)q * nk + k) * rowp;
+            for (size_t i = 0; i < rowp; ++i) rf[i] = (float)row[i];
+        }
+    if (eam) {
+        const double *es[2] = {ft->fembd, ft->dfembd};
+        for (int q = 0; q < 2; ++q)
+            for (int k = 0; k < t.nkind1; ++k) {
+                double *row = hd.data() + 4 * nk * rowp + ((size_t)q * t.nkind1 + k) * t.nep;
+                for (int i = 1; i <= t.nembd; ++i) row[i] = es[q][(size_t)(i - 1) * t.nkind1 + k];
+                row[t.nembd + 1] = row[t.nembd];
+            }
+    }
+    CK(cudaStreamSynchronize(c->stream), "synchronize");
+    if (c->tab_mem) { cudaFree(c->tab_mem); c->tab_mem = nullptr; }
+    CK(cudaMalloc(&c->tab_mem, nd * sizeof(double) + nf * sizeof(float) + 256), "table alloc");
+    double *dd = (double *)c->tab_mem;
+    float *df = (float *)(dd + nd);
+    CK(cudaMemcpy(dd, hd.data(), nd * sizeof(double), cudaMemcpyHostToDevice), "table upload");
+    CK(cudaMemcpy(df, hf.data(), nf * sizeof(float), cudaMemcpyHostToDevice), "table upload");
+    t.potr = dd; t.fpotr = dd + nk * rowp; t.potb = dd + 2 * nk * rowp; t.fpotb = dd + 3 * nk * rowp;
+    t.potr32 = df; t.fpotr32 = df + nk * rowp; t.potb32 = df + 2 * nk * rowp; t.fpotb32 = df + 3 * nk * rowp;
+    if (eam) {
+        t.fembd = dd + 4 * nk * rowp;
+        t.dfembd = t.fembd + (size_t)t.nkind1 * t.nep;
+    }
+    c->tab = t;
+    c->have_tables = true;
+    c->force_valid = false;
+    free_graph(c);
+    return MSMGB_OK;
+}
+
+extern "C" int msmgb_clear_forcetable(msmgb_ctx *c)
+{
+    if (!c) return MSMGB_ERR_ARG;
+    RET(use_device(c));
+    CK(cudaStreamSynchronize(c->stream), "synchronize");
+    if (c->tab_mem) cudaFree(c->tab_mem);
+    c->tab_mem = nullptr;
+    c->have_tables = false;
+    c->force_valid = false;
+    free_graph(c);
+    return MSMGB_OK;
+}
+
+// ---- state ------------------------------------------------------------------------------------
+extern "C" int msmgb_copyin_simbox(msmgb_ctx *c, int nbox, const msmgb_box *boxes, const int *ityp,
+                                   const int *statu, const double *xp, const double *xp1)
+{
+    if (!c || !boxes || !ityp || !statu || !xp || nbox < 1) return MSMGB_ERR_ARG;
+    if (nbox > c->cap_boxes) return set_err(c, MSMGB_ERR_CAPACITY, "more boxes than max_boxes");
+    long total = 0;
+    for (int b = 0; b < nbox; ++b) {
+        if (boxes[b].natom < 0) return set_err(c, MSMGB_ERR_ARG, "negative atom count");
+        total += boxes[b].natom;
+    }
+    if (total > c->cap_atoms) return set_err(c, MSMGB_ERR_CAPACITY, "more atoms than max_atoms");
+    if (total < 1) return set_err(c, MSMGB_ERR_ARG, "no atoms");
+    RET(use_device(c));
+    const int n = (int)total;
+    std::vector<DevBox> hb((size_t)nbox);
+    std::vector<int> boxid((size_t)n);
+    int cells = 0, atom0 = 0;
+    for (int b = 0; b < nbox; ++b) {
+        DevBox &d = hb[(size_t)b];
+        memset(&d, 0, sizeof(d));
+        for (int k = 0; k < 3; ++k) {
+            d.lo[k] = boxes[b].lo[k];
+            d.len[k] = boxes[b].len[k];
+            d.half[k] = 0.5 * boxes[b].len[k];
+            d.lenf[k] = (float)d.len[k];
+            d.halff[k] = (float)d.half[k];
+            d.ifpd[k] = boxes[b].ifpd[k] ? 1 : 0;
+            if (d.len[k] <= 0.0) return set_err(c, MSMGB_ERR_ARG, "box length must be positive");
+            if (d.ifpd[k] && d.len[k] <= 2.0 * c->p.rc_nl)
+                return set_err(c, MSMGB_ERR_BOX_TOO_SMALL, "periodic box edge must exceed twice the list cutoff");
+            int nc = (int)(d.len[k] / (1.0 * c->p.rc_nl) - 0.0001);   // MD_NeighborsList_GPU.F90:289-292
+            d.nc[k] = nc < 3 ? 3 : nc;
+        }
+        long nb = (long)d.nc[0] * d.nc[1] * d.nc[2];
+        if ((long)cells + nb > (1L << 24) - 2) return set_err(c, MSMGB_ERR_CAPACITY, "too many cells");
+        d.cell0 = cells;
+        cells += (int)nb;
+        d.atom0 = atom0;
+        d.natom = boxes[b].natom;
+        for (int i = 0; i < boxes[b].natom; ++i) boxid[(size_t)(atom0 + i)] = b;
+        atom0 += boxes[b].natom;
+    }
+    CK(cudaStreamSynchronize(c->stream), "synchronize");
+    free_graph(c);
+    if (cells + 2 > c->cap_cells) {
+        if (c->cell_start) cudaFree(c->cell_start);
+        if (c->cell_cursor) cudaFree(c->cell_cursor);
+        if (c->scan_tmp) cudaFree(c->scan_tmp);
+        c->cell_start = c->cell_cursor = c->scan_tmp = nullptr;
+        int cap = cells + 2;
+        CK(dalloc(&c->cell_start, (size_t)cap + 1), "cell alloc");
+        CK(dalloc(&c->cell_cursor, (size_t)cap + 1), "cell alloc");
+        CK(dalloc(&c->scan_tmp, (size_t)(cap / 4096 + 2) + 4096), "cell alloc");
+        c->cap_cells = cap;
+    }
+    c->ncell_total = cells;
+    c->nbox = nbox;
+    c->n = n;
+    c->a.n = n;
+    c->boxes.assign(boxes, boxes + nbox);
+    c->hbox = hb;
+    CK(cudaMemcpy(c->dbox, hb.data(), sizeof(DevBox) * (size_t)nbox, cudaMemcpyHostToDevice), "box upload");
+    // stage the caller's arrays in the scratch buffer, then pack on the device
+    char *s = (char *)c->scratch;
+    double *dxp = (double *)s;
+    double *dxp1 = dxp + 3 * (size_t)n;
+    int *dty = (int *)(dxp1 + 3 * (size_t)n);
+    int *dst = dty + n;
+    int *dbx = dst + n;
+    CK(cudaMemcpy(dxp, xp, sizeof(double) * 3 * (size_t)n, cudaMemcpyHostToDevice), "copyin");
+    if (xp1) CK(cudaMemcpy(dxp1, xp1, sizeof(double) * 3 * (size_t)n, cudaMemcpyHostToDevice), "copyin");
+    CK(cudaMemcpy(dty, ityp, sizeof(int) * (size_t)n, cudaMemcpyHostToDevice), "copyin");
+    CK(cudaMemcpy(dst, statu, sizeof(int) * (size_t)n, cudaMemcpyHostToDevice), "copyin");
+    CK(cudaMemcpy(dbx, boxid.data(), sizeof(int) * (size_t)n, cudaMemcpyHostToDevice), "copyin");
+    k_pack<<<nblk(n, kBlock), kBlock, 0, c->stream>>>(c->a, dxp, xp1 ? dxp1 : nullptr, dty, dst, dbx);
+    c->launches += 1;
+    RET(check_launch(c, "pack"));
+    CK(cudaMemsetAsync(c->flags, 0, sizeof(int) * kFlagWords, c->stream), "flag clear");
+    CK(cudaMemsetAsync(c->maxdisp, 0, sizeof(unsigned long long), c->stream), "flag clear");
+    CK(cudaStreamSynchronize(c->stream), "synchronize");
+    c->list_valid = false;
+    c->force_valid = false;
+    return MSMGB_OK;
+}
+
+extern "C" int msmgb_set_masses(msmgb_ctx *c, int ngroup, const double *cm)
+{
+    if (!c || !cm || ngroup < 1 || ngroup > kMaxGroups) return MSMGB_ERR_ARG;
+    for (int i = 0; i < ngroup; ++i)
+        if (!(cm[i] > 0.0)) return set_err(c, MSMGB_ERR_ARG, "masses must be positive");
+    RET(use_device(c));
+    CK(cudaMemcpy(c->cm, cm, sizeof(double) * (size_t)ngroup, cudaMemcpyHostToDevice), "mass upload");
+    c->have_masses = true;
+    return MSMGB_OK;
+}
+
+static int need_state(msmgb_ctx *c)
+{
+    if (c->n <= 0) return set_err(c, MSMGB_ERR_ARG, "no state: call msmgb_copyin_simbox first");
+    return MSMGB_OK;
+}
+
+static int copy_out_doubles(msmgb_ctx *c, const double *s0, const double *s1, const double *s2,
+                            double *host, int order)
+{
+    const int n = c->n;
+    double *tmp = (double *)c->scratch;
+    k_unpack3<<<nblk(n, kBlock), kBlock, 0, c->stream>>>(s0, s1, s2, c->a.gid, n,
+                                                       order == MSMGB_ORDER_SORTED, tmp);
+    c->launches += 1;
+    RET(check_launch(c, "copy-out"));
+    int m = s1 ? 3 : 1;
+    CK(cudaMemcpyAsync(host, tmp, sizeof(double) * (size_t)m * n, cudaMemcpyDeviceToHost, c->stream), "copy-out");
+    CK(cudaStreamSynchronize(c->stream), "synchronize");
+    return MSMGB_OK;
+}
+
+extern "C" int msmgb_copyout_simbox(msmgb_ctx *c, double *xp, double *xp1, int *statu, double *dis,
+                                    int order)
+{
+    if (!c) return MSMGB_ERR_ARG;
+    RET(need_state(c));
+    RET(use_device(c));
+    const int n = c->n;
+    const int sorted = order == MSMGB_ORDER_SORTED;
+    if (xp) {
+        double *tmp = (double *)c->scratch;
+        k_unpack_pos<<<nblk(n, kBlock), kBlock, 0, c->stream>>>(c->a.pos, c->a.gid, n, sorted, tmp);
+        c->launches += 1;
+        RET(check_launch(c, "copy-out"));
+        CK(cudaMemcpyAsync(xp, tmp, sizeof(double) * 3 * (size_t)n, cudaMemcpyDeviceToHost, c->stream), "copy-out");
+        CK(cudaStreamSynchronize(c->stream), "synchronize");
+    }
+    if (xp1) RET(copy_out_doubles(c, c->a.vx, c->a.vy, c->a.vz, xp1, order));
+    if (dis) RET(copy_out_doubles(c, c->a.dx, c->a.dy, c->a.dz, dis, order));
+    if (statu) {
+        int *tmp = (int *)c->scratch;
+        k_unpack_int<<<nblk(n, kBlock), kBlock, 0, c->stream>>>(c->a.statu, c->a.gid, n, sorted, tmp);
+        c->launches += 1;
+        RET(check_launch(c, "copy-out"));
+        CK(cudaMemcpyAsync(statu, tmp, sizeof(int) * (size_t)n, cudaMemcpyDeviceToHost, c->stream), "copy-out");
+        CK(cudaStreamSynchronize(c->stream), "synchronize");
+    }
+    return MSMGB_OK;
+}
+
+extern "C" int msmgb_copyout_force(msmgb_ctx *c, double *fp, int order)
+{
+    if (!c || !fp) return MSMGB_ERR_ARG;
+    RET(need_state(c));
+    RET(use_device(c));
+    if (!c->force_valid) return set_err(c, MSMGB_ERR_ARG, "forces are not current: call msmgb_calforce");
+    return copy_out_doubles(c, c->a.fx, c->a.fy, c->a.fz, fp, order);
+}
+
+extern "C" int msmgb_copyout_epot(msmgb_ctx *c, double *epot, int order)
+{
+    if (!c || !epot) return MSMGB_ERR_ARG;
+    RET(need_state(c));
+    RET(use_device(c));
+    return copy_out_doubles(c, c->a.epot, nullptr, nullptr, epot, order);
+}
+
+extern "C" int msmgb_copyout_den(msmgb_ctx *c, double *den, int order)
+{
+    if (!c || !den) return MSMGB_ERR_ARG;
+    RET(need_state(c));
+    RET(use_device(c));
+    return copy_out_doubles(c, c->a.den, nullptr, nullptr, den, order);
+}
+
+extern "C" int msmgb_copyout_gid(msmgb_ctx *c, int *gid)
+{
+    if (!c || !gid) return MSMGB_ERR_ARG;
+    RET(need_state(c));
+    RET(use_device(c));
+    CK(cudaMemcpyAsync(gid, c->a.gid, sizeof(int) * (size_t)c->n, cudaMemcpyDeviceToHost, c->stream), "copy-out");
+    CK(cudaStreamSynchronize(c->stream), "synchronize");
+    return MSMGB_OK;
+}
+
+// ---- neighbour list ---------------------------------------------------------------------------
+extern "C" int msmgb_cal_neighborelist(msmgb_ctx *c)
+{
+    if (!c) return MSMGB_ERR_ARG;
+    RET(need_state(c));
+    RET(use_device(c));
+    CK(cudaMemsetAsync(c->flags + kFlagMaxK, 0, sizeof(int), c->stream), "flag clear");
+    RET(build_list(c, false));
+    CK(cudaMemsetAsync(c->maxdisp, 0, sizeof(unsigned long long), c->stream), "flag clear");
+    RET(poll_flags(c));
+    c->list_valid = true;
+    c->force_valid = false;
+    return MSMGB_OK;
+}
+
+extern "C" int msmgb_copyout_neighborelist(msmgb_ctx *c, int *kvois, int *indi, int ld, int order)
+{
+    if (!c || !kvois) return MSMGB_ERR_ARG;
+    RET(need_state(c));
+    RET(use_device(c));
+    if (!c->list_valid) return set_err(c, MSMGB_ERR_ARG, "no neighbour list: call msmgb_cal_neighborelist");
+    const int n = c->n, mxk = c->p.mxkvois;
+    if (indi && ld < n) return set_err(c, MSMGB_ERR_ARG, "ld must be >= number of atoms");
+    std::vector<int> kv((size_t)n), gid((size_t)n);
+    CK(cudaMemcpy(kv.data(), c->a.kvois, sizeof(int) * (size_t)n, cudaMemcpyDeviceToHost), "copy-out");
+    CK(cudaMemcpy(gid.data(), c->a.gid, sizeof(int) * (size_t)n, cudaMemcpyDeviceToHost), "copy-out");
+    std::vector<int> ind;
+    if (indi) {
+        ind.resize((size_t)mxk * (size_t)c->cap_atoms);
+        CK(cudaMemcpy(ind.data(), c->a.indi, sizeof(int) * ind.size(), cudaMemcpyDeviceToHost), "copy-out");
+    }
+    const bool sorted = order == MSMGB_ORDER_SORTED;
+    for (int s = 0; s < n; ++s) {
+        int g = sorted ? s : gid[(size_t)s];
+        kvois[g] = kv[(size_t)s];
+        if (indi)
+            for (int k = 0; k < kv[(size_t)s]; ++k) {
+                int j = ind[(size_t)k * (size_t)c->cap_atoms + (size_t)s];
+                indi[(size_t)k * (size_t)ld + (size_t)g] = sorted ? j : gid[(size_t)j];
+            }
+    }
+    return MSMGB_OK;
+}
+
+// ---- force class -----------------------------------------------------------------------------
+static int ready_for_force(msmgb_ctx *c)
+{
+    RET(need_state(c));
+    if (!c->have_tables) return set_err(c, MSMGB_ERR_ARG, "no force table: call msmgb_init_forcetable");
+    RET(use_device(c));
+    if (!c->list_valid) {
+        CK(cudaMemsetAsync(c->flags + kFlagMaxK, 0, sizeof(int), c->stream), "flag clear");
+        RET(build_list(c, false));
+        CK(cudaMemsetAsync(c->maxdisp, 0, sizeof(unsigned long long), c->stream), "flag clear");
+        c->list_valid = true;
+    }
+    return MSMGB_OK;
+}
+
+static int force_passes(msmgb_ctx *c, bool virial, bool epot)
+{
+    if (c->p.precision == MSMGB_PREC_MIXED && !virial && !epot) {
+        RET(launch_density32(c));
+        RET(launch_force32(c));
+    } else {
+        RET(launch_density(c, epot));
+        RET(launch_force(c, virial));
+    }
+    return MSMGB_OK;
+}
+
+extern "C" int msmgb_calforce(msmgb_ctx *c)
+{
+    if (!c) return MSMGB_ERR_ARG;
+    RET(ready_for_force(c));
+    RET(force_passes(c, false, false));
+    RET(poll_flags(c));
+    c->force_valid = true;
+    return MSMGB_OK;
+}
+
+extern "C" int msmgb_calptensor(msmgb_ctx *c, double *vt)
+{
+    if (!c) return MSMGB_ERR_ARG;
+    RET(ready_for_force(c));
+    RET(force_passes(c, true, false));
+    CK(cudaMemcpyAsync(c->h_virial, c->virial, sizeof(double) * 6 * (size_t)c->nbox, cudaMemcpyDeviceToHost,
+                       c->stream), "virial copy-out");
+    RET(poll_flags(c));
+    c->force_valid = true;
+    if (vt)
+        for (int b = 0; b < c->nbox; ++b) {
+            const double *v = c->h_virial + 6 * b;
+            double *o = vt + 9 * b;
+            o[0] = v[0]; o[1] = v[1]; o[2] = v[2];
+            o[3] = v[1]; o[4] = v[3]; o[5] = v[4];
+            o[6] = v[2]; o[7] = v[4]; o[8] = v[5];
+        }
+    return MSMGB_OK;
+}
+
+extern "C" int msmgb_calepot(msmgb_ctx *c)
+{
+    if (!c) return MSMGB_ERR_ARG;
+    RET(ready_for_force(c));
+    RET(launch_density(c, true));
+    return poll_flags(c);
+}
+
+extern "C" int msmgb_calden(msmgb_ctx *c)
+{
+    if (!c) return MSMGB_ERR_ARG;
+    RET(ready_for_force(c));
+    RET(launch_density(c, false));
+    return poll_flags(c);
+}
+
+// ---- integrator -------------------------------------------------------------------------------
+extern "C" int msmgb_predictor(msmgb_ctx *c, double h)
+{
+    if (!c) return MSMGB_ERR_ARG;
+    RET(need_state(c));
+    if (!c->have_masses) return set_err(c, MSMGB_ERR_ARG, "no masses: call msmgb_set_masses");
+    RET(use_device(c));
+    RET(launch_vv(c, h, 0));
+    c->force_valid = false;
+    return poll_flags(c);
+}
+
+extern "C" int msmgb_correction(msmgb_ctx *c, double h)
+{
+    if (!c) return MSMGB_ERR_ARG;
+    RET(need_state(c));
+    if (!c->have_masses) return set_err(c, MSMGB_ERR_ARG, "no masses: call msmgb_set_masses");
+    RET(use_device(c));
+    RET(launch_correct(c, h, false));
+    return poll_flags(c);
+}
+
+static int capture_step(msmgb_ctx *c, double h)
+{
+    free_graph(c);
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "graph capture");
+    int64_t l0 = c->launches;
+    int rc = launch_vv(c, h, 1);
+    if (!rc) rc = launch_decide(c, c->p.skin_trigger, c->p.nb_uptab);
+    if (!rc) rc = build_list(c, true);
+    if (!rc) rc = force_passes(c, false, false);
+    cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+    if (rc) { if (g) cudaGraphDestroy(g); return rc; }
+    if (e != cudaSuccess) return cuda_err(c, e, "graph capture");
+    e = cudaGraphInstantiate(&c->step_graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) { c->step_graph = nullptr; return cuda_err(c, e, "graph instantiate"); }
+    c->graph_kernels = c->launches - l0;
+    c->launches = l0;
+    c->graph_h = h;
+    c->graph_prec = c->p.precision;
+    c->graph_n = c->n;
+    return MSMGB_OK;
+}
+
+extern "C" int msmgb_run_steps(msmgb_ctx *c, int nsteps, double h, int *rebuilds)
+{
+    if (!c || nsteps < 0) return MSMGB_ERR_ARG;
+    if (!c->have_masses) return set_err(c, MSMGB_ERR_ARG, "no masses: call msmgb_set_masses");
+    RET(ready_for_force(c));
+    if (!c->force_valid) {
+        RET(force_passes(c, false, false));
+        c->force_valid = true;
+    }
+    CK(cudaMemsetAsync(c->flags + kFlagRebuilds, 0, sizeof(int) * 3, c->stream), "flag clear");  // rebuilds, pending, step
+    if (!c->step_graph || c->graph_h != h || c->graph_prec != c->p.precision || c->graph_n != c->n)
+        RET(capture_step(c, h));
+    for (int s = 0; s < nsteps; ++s) {
+        CK(cudaGraphLaunch(c->step_graph, c->stream), "graph launch");
+        c->launches += c->graph_kernels;
+    }
+    RET(launch_correct(c, h, true));
+    int rc = poll_flags(c);
+    if (rebuilds) *rebuilds = c->h_flags[kFlagRebuilds];
+    return rc;
+}
+
+// asynchronous variant for timing loops: no final corrector, no host synchronisation
+extern "C" int msmgb_enqueue_steps(msmgb_ctx *c, int nsteps, double h)
+{
+    if (!c || nsteps < 0) return MSMGB_ERR_ARG;
+    if (!c->have_masses) return set_err(c, MSMGB_ERR_ARG, "no masses: call msmgb_set_masses");
+    RET(ready_for_force(c));
+    if (!c->force_valid) {
+        RET(force_passes(c, false, false));
+        c->force_valid = true;
+    }
+    if (!c->step_graph || c->graph_h != h || c->graph_prec != c->p.precision || c->graph_n != c->n)
+        RET(capture_step(c, h));
+    for (int s = 0; s < nsteps; ++s) {
+        CK(cudaGraphLaunch(c->step_graph, c->stream), "graph launch");
+        c->launches += c->graph_kernels;
+    }
+    return MSMGB_OK;
+}
+
+extern "C" int msmgb_finish_steps(msmgb_ctx *c, double h, int *rebuilds)
+{
+    if (!c) return MSMGB_ERR_ARG;
+    RET(use_device(c));
+    RET(launch_correct(c, h, true));
+    int rc = poll_flags(c);
+    if (rebuilds) *rebuilds = c->h_flags[kFlagRebuilds];
+    CK(cudaMemsetAsync(c->flags + kFlagRebuilds, 0, sizeof(int), c->stream), "flag clear");
+    return rc;
+}
+
+// ---- differentiation ------------------------------------------------------------------------
+extern "C" int msmgb_hvp(msmgb_ctx *c, const double *v, double *hv)
+{
+    if (!c || !v || !hv) return MSMGB_ERR_ARG;
+    RET(ready_for_force(c));
+    const int n = c->n;
+    const size_t N = (size_t)c->cap_atoms;
+    char *s = (char *)c->scratch;
+    double *v4 = (double *)s;                 // 32 B per atom
+    double *dd = (double *)(s + 32 * N);      //  8 B
+    double *hvs = (double *)(s + 40 * N);     // 24 B, sorted SoA result
+    double *io = (double *)(s + 64 * N);      // 24 B, caller-order staging (input, then output)
+    CK(cudaMemcpyAsync(io, v, sizeof(double) * 3 * (size_t)n, cudaMemcpyHostToDevice, c->stream), "hvp copy-in");
+    RET(launch_hvp(c, io, hvs, v4, dd));
+    k_unpack3<<<nblk(n, kBlock), kBlock, 0, c->stream>>>(hvs, hvs + n, hvs + 2 * (size_t)n, c->a.gid, n, 0, io);
+    c->launches += 1;
+    RET(check_launch(c, "hvp copy-out"));
+    CK(cudaMemcpyAsync(hv, io, sizeof(double) * 3 * (size_t)n, cudaMemcpyDeviceToHost, c->stream), "hvp copy-out");
+    return poll_flags(c);
+}
+
+// ---- timing helpers (CUDA events on the context stream) -------------------------------------
+extern "C" int msmgb_time_steps(msmgb_ctx *c, int nsteps, double h, float *ms, int *rebuilds)
+{
+    if (!c || !ms || nsteps < 1) return MSMGB_ERR_ARG;
+    RET(msmgb_enqueue_steps(c, 0, h));           // list, forces and the step graph are ready
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0), "event");
+    CK(cudaEventCreate(&e1), "event");
+    CK(cudaStreamSynchronize(c->stream), "synchronize");
+    CK(cudaEventRecord(e0, c->stream), "event");
+    int rc = msmgb_enqueue_steps(c, nsteps, h);
+    CK(cudaEventRecord(e1, c->stream), "event");
+    CK(cudaEventSynchronize(e1), "event");
+    CK(cudaEventElapsedTime(ms, e0, e1), "event");
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) return rc;
+    return msmgb_finish_steps(c, h, rebuilds);
+}
+
+// Average device time of one launch of each pass, in ms: out[0] density, out[1] force,
+// out[2] full list rebuild, out[3] fused integrator (timed with h = 0 so the state is
+// unchanged while the memory traffic is that of a real step).
+extern "C" int msmgb_time_passes(msmgb_ctx *c, int reps, float *out)
+{
+    if (!c || !out || reps < 1) return MSMGB_ERR_ARG;
+    RET(ready_for_force(c));
+    if (!c->have_masses) return set_err(c, MSMGB_ERR_ARG, "no masses: call msmgb_set_masses");
+    const bool mixed = c->p.precision == MSMGB_PREC_MIXED;
+    cudaEvent_t ev[2];
+    CK(cudaEventCreate(&ev[0]), "event");
+    CK(cudaEventCreate(&ev[1]), "event");
+    for (int which = 0; which < 4; ++which) {
+        double total = 0.0;
+        for (int r = 0; r < reps + 1; ++r) {
+            CK(cudaStreamSynchronize(c->stream), "synchronize");
+            CK(cudaEventRecord(ev[0], c->stream), "event");
+            int rc = MSMGB_OK;
+            if (which == 0) rc = mixed ? launch_density32(c) : launch_density(c, false);
+            else if (which == 1) rc = mixed ? launch_force32(c) : launch_force(c, false);
+            else if (which == 2) rc = build_list(c, false);
+            else rc = launch_vv(c, 0.0, 2);
+            if (rc) return rc;
+            CK(cudaEventRecord(ev[1], c->stream), "event");
+            CK(cudaEventSynchronize(ev[1]), "event");
+            float ms = 0.f;
+            CK(cudaEventElapsedTime(&ms, ev[0], ev[1]), "event");
+            if (r > 0) total += ms;                    // first launch is a warm-up
+            if (which == 2) {
+                // the rebuild re-sorted the atoms: the forces must follow
+                RET(force_passes(c, false, false));
+            }
+        }
+        out[which] = (float)(total / reps);
+    }
+    cudaEventDestroy(ev[0]);
+    cudaEventDestroy(ev[1]);
+    CK(cudaMemsetAsync(c->maxdisp, 0, sizeof(unsigned long long), c->stream), "flag clear");
+    return poll_flags(c);
+}
+
+// largest neighbour count of the last list build and the mean count, for the byte model
+extern "C" int msmgb_list_stats(msmgb_ctx *c, int *maxk, double *meank)
+{
+    if (!c) return MSMGB_ERR_ARG;
+    RET(need_state(c));
+    RET(use_device(c));
+    std::vector<int> kv((size_t)c->n);
+    CK(cudaMemcpy(kv.data(), c->a.kvois, sizeof(int) * (size_t)c->n, cudaMemcpyDeviceToHost), "copy-out");
+    long s = 0;
+    int m = 0;
+    for (int k : kv) { s += k; m = std::max(m, k); }
+    if (maxk) *maxk = m;
+    if (meank) *meank = (double)s / (double)c->n;
+    return MSMGB_OK;
+}

@@ -1,0 +1,159 @@
+// msmgb_internal.cuh -- device data layout and kernel entry points shared by the
+// translation units of libmsmgb.so.  Not part of the public ABI.
+//
+// Layout in HBM (all per-atom arrays are in cell-sorted order, capacity = max_atoms):
+//   pos      double4_32a  x, y, z, (unused)           gathered by the pair loops (one 32 B sector)
+//   pos32    float4   FP32 neighbour copy for the mixed passes (rebuilt by the integrator)
+//   vx..vz   double   velocities (SoA, streamed)
+//   fx..fz   double   forces (SoA, streamed)
+//   dis      double   accumulated displacement DIS (reference MD_DiffScheme_GPU.F90:364-366)
+//   pos_bld  double4_32a  positions at the last list build (skin trigger)
+//   ityp, statu, gid (sorted -> original), boxid
+//   kvois    int32    neighbour count, INDI column-major int32 [mxkvois][cap] (reference
+//                     layout INDI(NAPDEV,MXKVOIS), MD_NeighborsList_GPU.F90:75-85)
+//   tables   double   per kind, NTAB+2 entries (index 0 and NTAB+1 padded, quirk Q6)
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+#include <vector>
+
+#include "../../include/msmgb.h"
+
+namespace msmgb {
+
+constexpr int kBlock = 256;
+constexpr int kMaxGroups = 16;          // mp_MXGROUP, MD_Const.F90:77
+
+// error bits in flags[kFlagErr]
+constexpr int kErrOverflow = 1;
+constexpr int kErrOutOfBox = 2;
+constexpr int kErrRho = 4;
+
+// device flag words
+enum {
+    kFlagErr = 0,        // error bits
+    kFlagRebuild = 1,    // 1: the list is rebuilt in this step
+    kFlagRebuilds = 2,   // number of rebuilds done by run_steps
+    kFlagPending = 3,    // 1: a corrector half-kick is pending (fused integrator)
+    kFlagStep = 4,       // step counter for the fixed-interval rebuild
+    kFlagMaxK = 5,       // largest neighbour count seen by the last build
+    kFlagWords = 8
+};
+
+struct DevBox {
+    double lo[3];
+    double len[3];
+    double half[3];
+    float lenf[3];       // FP32 copies for the prefilter / mixed passes
+    float halff[3];
+    int ifpd[3];
+    int nc[3];
+    int cell0;           // first global cell id of this box
+    int atom0, natom;    // atom range in the caller's (original) order
+};
+
+struct DevTables {
+    int pottype;
+    int ntab, nkind, ntp;          // ntp = ntab + 2 (padded row length)
+    double csi, ru2;
+    const double *potr, *fpotr, *potb, *fpotb;     // [nkind][ntp]
+    const float *potr32, *fpotr32, *potb32, *fpotb32;
+    int nembd, nkind1, nep;        // nep = nembd + 2
+    double rhod;
+    const double *fembd, *dfembd;  // [nkind1][nep]
+    int ngroup;
+    int kpair[kMaxGroups * kMaxGroups];   // 0-based kind for (ityi, ityj): kpair[(ityj)*ng + ityi]
+    int kembd[kMaxGroups];
+};
+
+// Pointers of the atom state, passed by value to kernels.
+struct DevAtoms {
+    double4_32a *pos;
+    float4 *pos32;
+    double *vx, *vy, *vz;
+    double *fx, *fy, *fz;
+    double *dx, *dy, *dz;
+    double4_32a *pos_bld;
+    int *ityp, *statu, *gid, *boxid;
+    double *den, *epot;
+    float *den32;
+    int *kvois, *indi;
+    int ld;              // leading dimension of indi (capacity)
+    int mxk;
+    int n;
+    const DevBox *box;
+    const double *cm;    // masses per type (0-based type index)
+    int *flags;
+    unsigned long long *maxdisp;
+    double *virial;      // [nbox][6]
+};
+
+}  // namespace msmgb
+
+struct msmgb_ctx {
+    msmgb_params p{};
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    std::string err;
+    int64_t launches = 0;
+
+    int cap_atoms = 0, cap_boxes = 0;
+    int n = 0, nbox = 0;
+    std::vector<msmgb_box> boxes;
+    std::vector<msmgb::DevBox> hbox;
+    int ncell_total = 0, cap_cells = 0;
+
+    // device memory
+    msmgb::DevAtoms a{};
+    msmgb::DevBox *dbox = nullptr;
+    int *cell_of = nullptr, *cell_start = nullptr, *cell_cursor = nullptr, *perm = nullptr;
+    int *scan_tmp = nullptr;
+    void *scratch = nullptr;           // permutation staging (size: 96 B per atom)
+    double *cm = nullptr;
+    int *flags = nullptr;
+    unsigned long long *maxdisp = nullptr;
+    double *virial = nullptr;
+    int *h_flags = nullptr;            // pinned mirror of flags
+    double *h_virial = nullptr;        // pinned
+
+    // tables
+    msmgb::DevTables tab{};
+    void *tab_mem = nullptr;
+    bool have_tables = false;
+    bool have_masses = false;
+
+    bool list_valid = false;
+    bool force_valid = false;
+
+    // CUDA graph of one MD step
+    cudaGraphExec_t step_graph = nullptr;
+    int64_t graph_kernels = 0;
+    double graph_h = 0.0;
+    int graph_prec = -1;
+    int graph_n = -1;
+};
+
+namespace msmgb {
+
+// --- launch helpers (each increments ctx->launches) -------------------------------------
+int check_launch(msmgb_ctx *c, const char *what);
+int set_err(msmgb_ctx *c, int code, const std::string &msg);
+int cuda_err(msmgb_ctx *c, cudaError_t e, const char *what);
+
+// neighbour list (nlist.cu)
+int build_list(msmgb_ctx *c, bool predicated);
+
+// force passes (force64.cu / force32.cu)
+int launch_density(msmgb_ctx *c, bool want_epot);
+int launch_force(msmgb_ctx *c, bool want_virial);
+int launch_density32(msmgb_ctx *c);
+int launch_force32(msmgb_ctx *c);
+int launch_hvp(msmgb_ctx *c, const double *dv, double *dhv, double *v4buf, double *ddbuf);
+
+// integrator (vv.cu)
+int launch_vv(msmgb_ctx *c, double h, int mode);   // mode 0: predictor; 1: fused; 2: fused if pending
+int launch_correct(msmgb_ctx *c, double h, bool only_if_pending);
+int launch_decide(msmgb_ctx *c, double skin_trigger, int nb_uptab);
+
+}  // namespace msmgb

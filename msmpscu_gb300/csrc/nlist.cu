@@ -1,0 +1,346 @@
+// nlist.cu -- device cell binning, cell sort and full neighbour list.
+//
+// Replaces Cal_NeighBoreList2C_0_DEV (MD_NeighborsList_GPU.F90:1347-1732).  The reference
+// bins on the device, copies ~10 N-length arrays to the host, builds linked cells there,
+// gathers the atoms in cell order, copies them back and then runs one CTA per cell
+// (Cal_NeighboreList_Kernel2C, :907-1199).  Here every stage stays on the device:
+//   k_bin       cell id per atom (NeighboreList_IC_KERNEL formula, :759-819) + histogram
+//   scan        exclusive scan of the cell histogram (cell start offsets, hm_IA1th)
+//   k_scatter   counting-sort scatter, then k_cellsort orders each cell by previous index
+//               so the permutation is deterministic
+//   k_permute   gathers the atom state into cell order (hm_XP/hm_GID gather, :1541-1570)
+//   k_build     one thread per atom scans the 27-cell stencil in the reference's order
+//               (own cell first, then NIX/NIY/NIZ, MD_NeighborsList.F90:423-425); an FP32
+//               distance test decides every pair outside a narrow band around the cutoff,
+//               pairs inside the band get the exact FP64 rule d^2 < rc^2
+//               (MD_NeighborsList.F90:605), so the sets equal the FP64 oracle's.
+// Every kernel can be predicated on flags[kFlagRebuild] so the whole rebuild sits inside
+// the captured MD-step graph and costs a few empty launches when the trigger is off.
+#include "msmgb_internal.cuh"
+
+namespace msmgb {
+
+__constant__ int c_nix[27] = {0, -1, -1, -1, 0, 0, -1, 1, -1, 0, 1, -1, 0, 1, 1, 1, 1, 0, 0, -1, 1, -1, 0, 1, -1, 0, 1};
+__constant__ int c_niy[27] = {0, 0, -1, 1, 1, 0, 0, 0, -1, -1, -1, 1, 1, 1, 0, 1, -1, -1, 0, 0, 0, -1, -1, -1, 1, 1, 1};
+__constant__ int c_niz[27] = {0, 0, 0, 0, 0, 1, 1, 1, 1, 1, 1, 1, 1, 1, 0, 0, 0, 0, -1, -1, -1, -1, -1, -1, -1, -1, -1};
+
+__device__ __forceinline__ bool skip_rebuild(const int *flags, int predicated)
+{
+    return predicated && flags[kFlagRebuild] == 0;
+}
+
+__global__ void k_zero_int(int *p, int n, const int *flags, int predicated)
+{
+    if (skip_rebuild(flags, predicated)) return;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) p[i] = 0;
+}
+
+// cell index per atom: int((x - lo)/L * NC - 1e-4), MD_NeighborsList_GPU.F90:800-811
+__global__ void k_bin(DevAtoms a, int sentinel, int *cell_of, int *count, int predicated)
+{
+    if (skip_rebuild(a.flags, predicated)) return;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    int st = a.statu[i];
+    int c;
+    if (st & MSMGB_STATU_OUTOFBOX) {
+        c = sentinel;
+    } else {
+        const DevBox &b = a.box[a.boxid[i]];
+        double4_32a p = a.pos[i];
+        double xp[3] = {p.x, p.y, p.z};
+        int ix[3];
+        bool bad = false;
+        for (int k = 0; k < 3; ++k) {
+            int t = (int)((xp[k] - b.lo[k]) / b.len[k] * (double)b.nc[k] - 0.0001);
+            if (t < 0 || t > b.nc[k]) bad = true;
+            t = t < 0 ? 0 : (t >= b.nc[k] ? b.nc[k] - 1 : t);
+            ix[k] = t;
+        }
+        if (bad) atomicOr(&a.flags[kFlagErr], kErrOutOfBox);
+        c = b.cell0 + ix[0] + b.nc[0] * (ix[1] + b.nc[1] * ix[2]);
+    }
+    cell_of[i] = c;
+    atomicAdd(&count[c], 1);
+}
+
+// ---- exclusive scan (4096 items per block, block sums scanned by one block) ------------
+constexpr int kScanThreads = 1024;
+constexpr int kScanItems = 4;
+constexpr int kScanTile = kScanThreads * kScanItems;
+
+__device__ __forceinline__ int block_exclusive_scan(int v, int *total)
+{
+    __shared__ int warp_sums[32];
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_sums[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+        int nw = blockDim.x >> 5;
+        int w = lane < nw ? warp_sums[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += y;
+        }
+        if (lane < nw) warp_sums[lane] = w;
+    }
+    __syncthreads();
+    int excl = x - v + (wid > 0 ? warp_sums[wid - 1] : 0);
+    if (total) *total = warp_sums[(blockDim.x >> 5) - 1];
+    __syncthreads();
+    return excl;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_tile(const int *in, int *out, int n, int *sums,
+                                                            const int *flags, int predicated)
+{
+    if (skip_rebuild(flags, predicated)) return;
+    int base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+    int v[kScanItems];
+    int s = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        v[k] = (base + k < n) ? in[base + k] : 0;
+        s += v[k];
+    }
+    int total;
+    int e = block_exclusive_scan(s, &total);
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        if (base + k < n) out[base + k] = e;
+        e += v[k];
+    }
+    if (threadIdx.x == 0 && sums) sums[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_add(int *out, int n, const int *sums,
+                                                           const int *flags, int predicated)
+{
+    if (skip_rebuild(flags, predicated)) return;
+    if (blockIdx.x == 0) return;
+    int add = sums[blockIdx.x];
+    int base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k)
+        if (base + k < n) out[base + k] += add;
+}
+
+// ---- counting-sort scatter and deterministic per-cell order --------------------------
+__global__ void k_scatter(DevAtoms a, const int *cell_of, const int *start, int *cursor, int *perm,
+                          int predicated)
+{
+    if (skip_rebuild(a.flags, predicated)) return;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    int c = cell_of[i];
+    int slot = start[c] + atomicAdd(&cursor[c], 1);
+    perm[slot] = i;
+}
+
+__global__ void k_cellsort(int ncs, const int *start, int *perm, const int *flags, int predicated)
+{
+    if (skip_rebuild(flags, predicated)) return;
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ncs) return;
+    int b = start[c], e = start[c + 1];
+    for (int i = b + 1; i < e; ++i) {   // insertion sort: cells hold ~10 atoms
+        int v = perm[i];
+        int j = i - 1;
+        while (j >= b && perm[j] > v) { perm[j + 1] = perm[j]; --j; }
+        perm[j + 1] = v;
+    }
+}
+
+// staging layout inside the scratch buffer (one slab per field, capacity entries each)
+struct Stage {
+    double4_32a *pos;
+    double *vx, *vy, *vz, *dx, *dy, *dz;
+    int *ityp, *statu, *gid, *boxid, *cell;
+};
+
+__host__ __device__ inline Stage stage_of(void *scratch, int cap)
+{
+    Stage s;
+    char *p = (char *)scratch;
+    s.pos = (double4_32a *)p; p += sizeof(double4_32a) * (size_t)cap;
+    s.vx = (double *)p; p += sizeof(double) * (size_t)cap;
+    s.vy = (double *)p; p += sizeof(double) * (size_t)cap;
+    s.vz = (double *)p; p += sizeof(double) * (size_t)cap;
+    s.dx = (double *)p; p += sizeof(double) * (size_t)cap;
+    s.dy = (double *)p; p += sizeof(double) * (size_t)cap;
+    s.dz = (double *)p; p += sizeof(double) * (size_t)cap;
+    s.ityp = (int *)p; p += sizeof(int) * (size_t)cap;
+    s.statu = (int *)p; p += sizeof(int) * (size_t)cap;
+    s.gid = (int *)p; p += sizeof(int) * (size_t)cap;
+    s.boxid = (int *)p; p += sizeof(int) * (size_t)cap;
+    s.cell = (int *)p;
+    return s;
+}
+
+__global__ void k_permute(DevAtoms a, Stage s, const int *perm, const int *cell_of, int predicated)
+{
+    if (skip_rebuild(a.flags, predicated)) return;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    int o = perm[i];
+    s.pos[i] = a.pos[o];
+    s.vx[i] = a.vx[o]; s.vy[i] = a.vy[o]; s.vz[i] = a.vz[o];
+    s.dx[i] = a.dx[o]; s.dy[i] = a.dy[o]; s.dz[i] = a.dz[o];
+    s.ityp[i] = a.ityp[o];
+    s.statu[i] = a.statu[o];
+    s.gid[i] = a.gid[o];
+    s.boxid[i] = a.boxid[o];
+    s.cell[i] = cell_of[o];
+}
+
+__global__ void k_copyback(DevAtoms a, Stage s, int *cell_of, int predicated)
+{
+    if (skip_rebuild(a.flags, predicated)) return;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    double4_32a p = s.pos[i];
+    a.pos[i] = p;
+    a.pos32[i] = make_float4((float)p.x, (float)p.y, (float)p.z, 0.0f);
+    a.vx[i] = s.vx[i]; a.vy[i] = s.vy[i]; a.vz[i] = s.vz[i];
+    a.dx[i] = s.dx[i]; a.dy[i] = s.dy[i]; a.dz[i] = s.dz[i];
+    a.ityp[i] = s.ityp[i];
+    a.statu[i] = s.statu[i];
+    a.gid[i] = s.gid[i];
+    a.boxid[i] = s.boxid[i];
+    cell_of[i] = s.cell[i];
+}
+
+__device__ __forceinline__ double mi64(double s, double len, double half, int pd)
+{
+    return (pd && fabs(s) > half) ? s - copysign(len, s) : s;
+}
+
+__device__ __forceinline__ float mi32(float s, float len, float half, int pd)
+{
+    return (pd && fabsf(s) > half) ? s - copysignf(len, s) : s;
+}
+
+// Full neighbour list, one thread per (sorted) atom.
+__global__ void __launch_bounds__(kBlock) k_build(DevAtoms a, const int *cell_of, const int *start,
+                                                  double rc2, float d2lo, float d2hi, int predicated)
+{
+    if (skip_rebuild(a.flags, predicated)) return;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    double4_32a p = a.pos[i];
+    a.pos_bld[i] = p;
+    if (a.statu[i] & MSMGB_STATU_OUTOFBOX) { a.kvois[i] = 0; return; }
+    const DevBox &b = a.box[a.boxid[i]];
+    const float4 pf = a.pos32[i];
+    int c = cell_of[i] - b.cell0;
+    int ix = c % b.nc[0], iy = (c / b.nc[0]) % b.nc[1], iz = c / (b.nc[0] * b.nc[1]);
+    int nn = 0;
+    const int ld = a.ld, mxk = a.mxk;
+    for (int s = 0; s < 27; ++s) {
+        int j3[3] = {ix + c_nix[s], iy + c_niy[s], iz + c_niz[s]};
+        bool skip = false;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            if (b.ifpd[k]) {
+                if (j3[k] >= b.nc[k]) j3[k] = 0;
+                else if (j3[k] < 0) j3[k] = b.nc[k] - 1;
+            }
+            if (j3[k] < 0 || j3[k] >= b.nc[k]) skip = true;
+        }
+        if (skip) continue;
+        int g = b.cell0 + j3[0] + b.nc[0] * (j3[1] + b.nc[1] * j3[2]);
+        int e = start[g + 1];
+        for (int j = start[g]; j < e; ++j) {
+            if (j == i) continue;
+            float4 q = a.pos32[j];
+            float sx = mi32(pf.x - q.x, b.lenf[0], b.halff[0], b.ifpd[0]);
+            float sy = mi32(pf.y - q.y, b.lenf[1], b.halff[1], b.ifpd[1]);
+            float sz = mi32(pf.z - q.z, b.lenf[2], b.halff[2], b.ifpd[2]);
+            float d2f = sx * sx + sy * sy + sz * sz;
+            bool in;
+            if (d2f < d2lo) {
+                in = true;
+            } else if (d2f > d2hi) {
+                in = false;
+            } else {        // narrow band: the exact FP64 rule of the oracle
+                double4_32a qd = a.pos[j];
+                double dx = mi64(p.x - qd.x, b.len[0], b.half[0], b.ifpd[0]);
+                double dy = mi64(p.y - qd.y, b.len[1], b.half[1], b.ifpd[1]);
+                double dz = mi64(p.z - qd.z, b.len[2], b.half[2], b.ifpd[2]);
+                in = (dx * dx + dy * dy + dz * dz) < rc2;
+            }
+            if (in) {
+                if (nn < mxk) a.indi[(size_t)nn * (size_t)ld + (size_t)i] = j;
+                ++nn;
+            }
+        }
+    }
+    if (nn > mxk) {
+        atomicOr(&a.flags[kFlagErr], kErrOverflow);
+        nn = mxk;
+    }
+    a.kvois[i] = nn;
+    atomicMax(&a.flags[kFlagMaxK], nn);
+}
+
+static inline int nblk(long n, int b) { return (int)((n + b - 1) / b); }
+
+// Margin of the FP32 prefilter: the FP32 copy of a coordinate is within half an ulp of the
+// FP64 value, the subtraction and the image shift add at most two more roundings of the
+// same size, so each separation component is within 4 ulp(2*extent) of the exact one.
+static void prefilter_band(const msmgb_ctx *c, double rc2, float *lo, float *hi)
+{
+    double ext = 1.0;
+    for (const DevBox &b : c->hbox)
+        for (int k = 0; k < 3; ++k) ext = fmax(ext, fabs(b.lo[k]) + 2.0 * b.len[k]);
+    double ulp = ldexp(1.0, ilogb(ext) - 23);
+    double delta = 4.0 * ulp;
+    double rc = sqrt(rc2);
+    double m = 3.0 * (2.0 * rc * delta + delta * delta) + 4.0 * ldexp(rc2, -23);
+    m *= 4.0;  // safety factor
+    *lo = (float)(rc2 - m);
+    *hi = (float)(rc2 + m);
+}
+
+int build_list(msmgb_ctx *c, bool predicated)
+{
+    const int n = c->n;
+    const int ncs = c->ncell_total + 1;   // + sentinel cell for out-of-box atoms
+    const int pr = predicated ? 1 : 0;
+    int *count = c->cell_cursor;          // histogram, then re-zeroed as scatter cursor
+    cudaStream_t s = c->stream;
+    DevAtoms a = c->a;
+
+    k_zero_int<<<nblk(ncs + 1, kBlock), kBlock, 0, s>>>(count, ncs + 1, a.flags, pr);
+    k_bin<<<nblk(n, kBlock), kBlock, 0, s>>>(a, c->ncell_total, c->cell_of, count, pr);
+    // exclusive scan over ncs + 1 entries: start[ncs] = n
+    int ntile = nblk(ncs + 1, kScanTile);
+    k_scan_tile<<<ntile, kScanThreads, 0, s>>>(count, c->cell_start, ncs + 1, c->scan_tmp, a.flags, pr);
+    c->launches += 3;
+    if (ntile > 1) {
+        k_scan_tile<<<1, kScanThreads, 0, s>>>(c->scan_tmp, c->scan_tmp, ntile, nullptr, a.flags, pr);
+        k_scan_add<<<ntile, kScanThreads, 0, s>>>(c->cell_start, ncs + 1, c->scan_tmp, a.flags, pr);
+        c->launches += 2;
+    }
+    k_zero_int<<<nblk(ncs + 1, kBlock), kBlock, 0, s>>>(count, ncs + 1, a.flags, pr);
+    k_scatter<<<nblk(n, kBlock), kBlock, 0, s>>>(a, c->cell_of, c->cell_start, count, c->perm, pr);
+    k_cellsort<<<nblk(ncs, kBlock), kBlock, 0, s>>>(ncs, c->cell_start, c->perm, a.flags, pr);
+    Stage st = stage_of(c->scratch, c->cap_atoms);
+    k_permute<<<nblk(n, kBlock), kBlock, 0, s>>>(a, st, c->perm, c->cell_of, pr);
+    k_copyback<<<nblk(n, kBlock), kBlock, 0, s>>>(a, st, c->cell_of, pr);
+    double rc2 = c->p.rc_nl * c->p.rc_nl;
+    float d2lo, d2hi;
+    prefilter_band(c, rc2, &d2lo, &d2hi);
+    k_build<<<nblk(n, kBlock), kBlock, 0, s>>>(a, c->cell_of, c->cell_start, rc2, d2lo, d2hi, pr);
+    c->launches += 6;
+    return check_launch(c, "neighbour list");
+}
+
+}  // namespace msmgb

@@ -1,0 +1,159 @@
+// vv.cu -- Swope velocity Verlet on the device.
+//
+//   k_vv       Predictor_KERNEL0 (MD_DiffScheme_GPU.F90:242-384): DIS = h v + h^2/2 F/m,
+//              x += DIS with periodic wrap, v += h/2 F/m, out-of-box flags.  In the fused
+//              mode it first applies the previous step's Correction_KERNEL (:686-760),
+//              v += h/2 F/m, with the same operations in the same order, so one pass over
+//              x, v, F replaces the reference's two launches.  It also reduces the largest
+//              displacement since the last list build (skin trigger) and refreshes the
+//              FP32 neighbour copy of the positions.
+//   k_correct  Correction_KERNEL alone (end of a run, or msmgb_correction()).
+//   k_decide   one thread: rebuild flag for this step from the skin trigger (or the
+//              reference's fixed NB_UPTAB interval, MD_Method_GenericMD_GPU.F90:599-601).
+#include "msmgb_internal.cuh"
+
+namespace msmgb {
+
+__device__ __forceinline__ double mi(double s, double len, double half, int pd)
+{
+    return (pd && fabs(s) > half) ? s - copysign(len, s) : s;
+}
+
+__device__ __forceinline__ void block_max_flush(double v, unsigned long long *dst)
+{
+    __shared__ double sm[kBlock / 32];
+    const unsigned full = 0xffffffffu;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(full, v, o));
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double m = sm[0];
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) m = fmax(m, sm[w]);
+        // non-negative doubles order like their bit patterns
+        if (m > 0.0) atomicMax(dst, (unsigned long long)__double_as_longlong(m));
+    }
+}
+
+// mode 0: predictor only; mode 1: corrector of the previous step first when
+// flags[kFlagPending] is set (graph replay), mode 2: always fused.
+__global__ void __launch_bounds__(kBlock) k_vv(DevAtoms a, double th, int mode)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double dmax = 0.0;
+    const int pend = (mode == 2) ? 1 : (mode == 1 ? a.flags[kFlagPending] : 0);
+    if (i < a.n) {
+        int stat = a.statu[i];
+        if ((stat & MSMGB_STATU_ACTIVE) == MSMGB_STATU_ACTIVE) {
+            const double hs2 = th * 0.5, h2s2 = th * th * 0.5;
+            const DevBox &b = a.box[a.boxid[i]];
+            double cm0 = a.cm[a.ityp[i] - 1];
+            double4_32a p = a.pos[i];
+            double vx = a.vx[i], vy = a.vy[i], vz = a.vz[i];
+            double ax = a.fx[i] / cm0, ay = a.fy[i] / cm0, az = a.fz[i] / cm0;
+            if (pend) {
+                if (!(stat & MSMGB_STATU_FIXVELX) && !(stat & MSMGB_STATU_FIXPOSX)) vx = vx + hs2 * ax;
+                if (!(stat & MSMGB_STATU_FIXVELY) && !(stat & MSMGB_STATU_FIXPOSY)) vy = vy + hs2 * ay;
+                if (!(stat & MSMGB_STATU_FIXVELZ) && !(stat & MSMGB_STATU_FIXPOSZ)) vz = vz + hs2 * az;
+            }
+            double dx = th * vx + h2s2 * ax;
+            if (stat & MSMGB_STATU_FIXPOSX) dx = 0.0;
+            double x = p.x + dx;
+            if (b.ifpd[0]) {
+                if (x > b.lo[0] + b.len[0]) x = x - b.len[0];
+                else if (x < b.lo[0]) x = x + b.len[0];
+            }
+            double dy = th * vy + h2s2 * ay;
+            if (stat & MSMGB_STATU_FIXPOSY) dy = 0.0;
+            double y = p.y + dy;
+            if (b.ifpd[1]) {
+                if (y > b.lo[1] + b.len[1]) y = y - b.len[1];
+                else if (y < b.lo[1]) y = y + b.len[1];
+            }
+            double dz = th * vz + h2s2 * az;
+            if (stat & MSMGB_STATU_FIXPOSZ) dz = 0.0;
+            double z = p.z + dz;
+            if (b.ifpd[2]) {
+                if (z > b.lo[2] + b.len[2]) z = z - b.len[2];
+                else if (z < b.lo[2]) z = z + b.len[2];
+            }
+            if (!(stat & MSMGB_STATU_FIXVELX) && !(stat & MSMGB_STATU_FIXPOSX)) vx = vx + hs2 * ax;
+            if (!(stat & MSMGB_STATU_FIXVELY) && !(stat & MSMGB_STATU_FIXPOSY)) vy = vy + hs2 * ay;
+            if (!(stat & MSMGB_STATU_FIXVELZ) && !(stat & MSMGB_STATU_FIXPOSZ)) vz = vz + hs2 * az;
+            a.pos[i] = make_double4_32a(x, y, z, p.w);
+            a.pos32[i] = make_float4((float)x, (float)y, (float)z, 0.0f);
+            a.vx[i] = vx; a.vy[i] = vy; a.vz[i] = vz;
+            a.dx[i] += dx; a.dy[i] += dy; a.dz[i] += dz;
+            // Predictor_KERNEL0 :372-378 (PASSBOUND is not stored, quirk Q10)
+            double ubx = b.lo[0] + b.len[0], uby = b.lo[1] + b.len[1], ubz = b.lo[2] + b.len[2];
+            if (x > ubx || y > uby || z > ubz)
+                a.statu[i] = MSMGB_STATU_OUTOFBOX | MSMGB_STATU_REFLECT;
+            else if (x < b.lo[0] || y < b.lo[1] || z < b.lo[2])
+                a.statu[i] = MSMGB_STATU_OUTOFBOX | MSMGB_STATU_TRANSMIT;
+            double4_32a q = a.pos_bld[i];
+            double ex = mi(x - q.x, b.len[0], b.half[0], b.ifpd[0]);
+            double ey = mi(y - q.y, b.len[1], b.half[1], b.ifpd[1]);
+            double ez = mi(z - q.z, b.len[2], b.half[2], b.ifpd[2]);
+            dmax = ex * ex + ey * ey + ez * ez;
+        }
+    }
+    block_max_flush(dmax, a.maxdisp);
+}
+
+__global__ void __launch_bounds__(kBlock) k_correct(DevAtoms a, double th, int only_if_pending)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (only_if_pending && a.flags[kFlagPending] == 0) return;
+    if (i >= a.n) return;
+    int stat = a.statu[i];
+    if ((stat & MSMGB_STATU_ACTIVE) != MSMGB_STATU_ACTIVE) return;
+    const double hs2 = th * 0.5;
+    double cm0 = a.cm[a.ityp[i] - 1];
+    if (!(stat & MSMGB_STATU_FIXVELX) && !(stat & MSMGB_STATU_FIXPOSX)) a.vx[i] = a.vx[i] + hs2 * (a.fx[i] / cm0);
+    if (!(stat & MSMGB_STATU_FIXVELY) && !(stat & MSMGB_STATU_FIXPOSY)) a.vy[i] = a.vy[i] + hs2 * (a.fy[i] / cm0);
+    if (!(stat & MSMGB_STATU_FIXVELZ) && !(stat & MSMGB_STATU_FIXPOSZ)) a.vz[i] = a.vz[i] + hs2 * (a.fz[i] / cm0);
+}
+
+__global__ void k_clear_pending(int *flags) { flags[kFlagPending] = 0; }
+
+__global__ void k_decide(int *flags, unsigned long long *maxdisp, double thr2, int nb_uptab)
+{
+    int rebuild = 0;
+    if (thr2 > 0.0) {
+        rebuild = __longlong_as_double((long long)*maxdisp) > thr2;
+    } else if (nb_uptab > 0) {
+        int step = ++flags[kFlagStep];
+        rebuild = (step % nb_uptab) == 0;
+    }
+    flags[kFlagRebuild] = rebuild;
+    if (rebuild) flags[kFlagRebuilds] += 1;
+    *maxdisp = 0ull;
+    flags[kFlagPending] = 1;
+}
+
+static inline int nblk(long n, int b) { return (int)((n + b - 1) / b); }
+
+int launch_vv(msmgb_ctx *c, double h, int mode)
+{
+    k_vv<<<nblk(c->n, kBlock), kBlock, 0, c->stream>>>(c->a, h, mode);
+    c->launches += 1;
+    return check_launch(c, "integrator");
+}
+
+int launch_correct(msmgb_ctx *c, double h, bool only_if_pending)
+{
+    k_correct<<<nblk(c->n, kBlock), kBlock, 0, c->stream>>>(c->a, h, only_if_pending ? 1 : 0);
+    k_clear_pending<<<1, 1, 0, c->stream>>>(c->a.flags);
+    c->launches += 2;
+    return check_launch(c, "corrector");
+}
+
+int launch_decide(msmgb_ctx *c, double skin_trigger, int nb_uptab)
+{
+    double thr2 = skin_trigger > 0.0 ? skin_trigger * skin_trigger : 0.0;
+    k_decide<<<1, 1, 0, c->stream>>>(c->a.flags, c->a.maxdisp, thr2, nb_uptab);
+    c->launches += 1;
+    return check_launch(c, "rebuild decision");
+}
+
+}  // namespace msmgb

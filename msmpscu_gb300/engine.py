@@ -1,0 +1,294 @@
+"""Host-side mirror of msmpscu's GPU force class, neighbour list and integrator.
+
+``ForceTable`` mirrors Register_Interaction_Table + Create_Interaction_ForceTable
+(MD_TypeDef_ForceTable.F90:1151-1230) for the potentials of the benchmark configurations;
+``Engine`` mirrors the MDForceClassGPU procedure pointers (MD_ForceClass_Register_GPU.F90:
+248-259), Cal_NeighBoreList_DEV and Predictor_DEV / Correction_DEV.  Every call goes through
+the C ABI of libmsmgb.so; there is no CPU path.
+
+Units: Angstrom, eV, fs, masses in eV*fs^2/A^2 (``lattice.AMU`` per amu).
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _lib as L
+
+
+class MSMError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("msmgb error %d: %s" % (code, msg))
+        self.code = code
+
+
+def _d(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double)) if a is not None else None
+
+
+def _i(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int)) if a is not None else None
+
+
+class ForceTable:
+    """Single-species force table in the reference's conventions (NKIND = NGROUP = 1)."""
+
+    def __init__(self, pot, prm, rmax, ru, pottype, ntab=10000, nembd=10000, rhoscal=20.0):
+        lib = L.load()
+        self.pot, self.pottype = pot, pottype
+        self.prm = np.ascontiguousarray(prm if prm is not None else np.zeros(5), dtype=np.float64)
+        self.rmax, self.ru, self.ntab, self.nembd = float(rmax), float(ru), int(ntab), int(nembd)
+        self.potr, self.fpotr, self.potb, self.fpotb = (np.zeros(self.ntab) for _ in range(4))
+        eam = pottype == L.EAM_TYPE
+        self.fembd = np.zeros(self.nembd) if eam else None
+        self.dfembd = np.zeros(self.nembd) if eam else None
+        rhod = C.c_double()
+        rc = lib.msmgb_create_forcetable(pot, _d(self.prm), self.rmax, self.ntab, self.nembd,
+                                         float(rhoscal), _d(self.potr), _d(self.fpotr),
+                                         _d(self.potb), _d(self.fpotb), _d(self.fembd),
+                                         _d(self.dfembd), C.byref(rhod))
+        if rc != L.OK:
+            raise MSMError(rc, "table generation failed")
+        self.rhod = rhod.value
+        self._kpair = np.array([1], np.int32)
+        self._kembd = np.array([1], np.int32)
+
+    @classmethod
+    def cleri_rosato(cls, A, xi, p, q, r0, rc, ntab=10000):
+        """Cleri-Rosato TB-SMA (FS type) with a hard cutoff rc (Rmax = RU = rc)."""
+        return cls(L.POT_CR, [A, xi, p, q, r0], rc, rc, L.FS_TYPE, ntab=ntab, nembd=ntab)
+
+    @classmethod
+    def marinica_eam2(cls, rc=5.4604375, ntab=10000, nembd=10000, rhoscal=20.0):
+        """Marinica EAM2 for W (EAM type)."""
+        return cls(L.POT_MARINICA2, None, rc, rc, L.EAM_TYPE, ntab=ntab, nembd=nembd,
+                   rhoscal=rhoscal)
+
+    @classmethod
+    def ackland_ww(cls, rmax, ru=None, ntab=10000):
+        return cls(L.POT_ACKLAND_WW, None, rmax, ru if ru else rmax, L.FS_TYPE, ntab=ntab)
+
+    def struct(self):
+        t = L.ForceTable()
+        t.pottype, t.ntab, t.nkind, t.rmax = self.pottype, self.ntab, 1, self.rmax
+        t.potr, t.fpotr, t.potb, t.fpotb = (_d(a) for a in (self.potr, self.fpotr, self.potb, self.fpotb))
+        eam = self.pottype == L.EAM_TYPE
+        t.nembd = self.nembd if eam else 0
+        t.nkind1 = 1 if eam else 0
+        t.rhod = self.rhod
+        t.fembd, t.dfembd = (_d(self.fembd), _d(self.dfembd)) if eam else (None, None)
+        t.ngroup = 1
+        t.kpair = _i(self._kpair)
+        t.kembd = _i(self._kembd)
+        t.ru = self.ru
+        return t
+
+    @property
+    def csi(self):
+        return float(self.ntab) / np.sqrt(self.rmax)
+
+
+class Engine:
+    """One device context: tables, a batch of boxes, neighbour list, force passes, MD steps."""
+
+    def __init__(self, max_atoms, rc_nl, max_boxes=1, mxkvois=64, skin_trigger=0.15,
+                 nb_uptab=10, precision="fp64", device=0, stream=None):
+        self.lib = L.load()
+        p = L.Params()
+        p.device, p.max_atoms, p.max_boxes, p.mxkvois = device, int(max_atoms), int(max_boxes), int(mxkvois)
+        p.rc_nl, p.skin_trigger, p.nb_uptab = float(rc_nl), float(skin_trigger), int(nb_uptab)
+        p.precision = L.PREC_MIXED if precision == "mixed" else L.PREC_FP64
+        p.stream = stream
+        self.ctx = C.c_void_p()
+        rc = self.lib.msmgb_create(C.byref(self.ctx), C.byref(p))
+        if rc != L.OK:
+            raise MSMError(rc, "context creation failed (device %d)" % device)
+        self.params = p
+        self.n = 0
+        self.nbox = 0
+        self._table = None
+
+    # ---- plumbing --------------------------------------------------------------------------
+    def _ck(self, rc):
+        if rc != L.OK:
+            msg = self.lib.msmgb_last_error(self.ctx)
+            raise MSMError(rc, msg.decode() if msg else "")
+        return rc
+
+    def close(self):
+        if self.ctx:
+            self.lib.msmgb_destroy(self.ctx)
+            self.ctx = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def stream(self):
+        return self.lib.msmgb_stream(self.ctx)
+
+    @property
+    def launches(self):
+        return int(self.lib.msmgb_launch_count(self.ctx))
+
+    def synchronize(self):
+        self._ck(self.lib.msmgb_synchronize(self.ctx))
+
+    def set_precision(self, precision):
+        self._ck(self.lib.msmgb_set_precision(self.ctx, L.PREC_MIXED if precision == "mixed" else L.PREC_FP64))
+
+    # ---- force class ---------------------------------------------------------------------------
+    def init_forcetable(self, table: ForceTable):
+        self._table = table
+        s = table.struct()
+        self._ck(self.lib.msmgb_init_forcetable(self.ctx, C.byref(s)))
+
+    def clear_forcetable(self):
+        self._ck(self.lib.msmgb_clear_forcetable(self.ctx))
+
+    def calforce(self):
+        self._ck(self.lib.msmgb_calforce(self.ctx))
+
+    def calptensor(self):
+        v = np.zeros(9 * max(self.nbox, 1))
+        self._ck(self.lib.msmgb_calptensor(self.ctx, _d(v)))
+        return v.reshape(-1, 3, 3)
+
+    def calepot(self):
+        self._ck(self.lib.msmgb_calepot(self.ctx))
+
+    def calden(self):
+        self._ck(self.lib.msmgb_calden(self.ctx))
+
+    # ---- state ---------------------------------------------------------------------------------
+    def copyin(self, boxes, pos, vel=None, ityp=None, statu=None):
+        """boxes: list of (natom, lo[3], len[3], ifpd[3]); pos/vel: (N,3) arrays."""
+        n = int(pos.shape[0])
+        arr = (L.Box * len(boxes))()
+        tot = 0
+        for k, (na, lo, ln, pd) in enumerate(boxes):
+            arr[k].natom = int(na)
+            for d in range(3):
+                arr[k].lo[d], arr[k].len[d], arr[k].ifpd[d] = float(lo[d]), float(ln[d]), int(pd[d])
+            tot += int(na)
+        if tot != n:
+            raise ValueError("box atom counts (%d) do not add up to N (%d)" % (tot, n))
+        xp = np.ascontiguousarray(np.asarray(pos, np.float64).T).reshape(-1)
+        xp1 = np.ascontiguousarray(np.asarray(vel, np.float64).T).reshape(-1) if vel is not None else None
+        ty = np.ascontiguousarray(ityp if ityp is not None else np.ones(n), dtype=np.int32)
+        st = np.ascontiguousarray(statu if statu is not None else np.full(n, L.STATU_ACTIVE), dtype=np.int32)
+        self._ck(self.lib.msmgb_copyin_simbox(self.ctx, len(boxes), arr, _i(ty), _i(st), _d(xp), _d(xp1)))
+        self.n, self.nbox = n, len(boxes)
+
+    @staticmethod
+    def pack_boxes(boxes):
+        arr = (L.Box * len(boxes))()
+        for k, (na, lo, ln, pd) in enumerate(boxes):
+            arr[k].natom = int(na)
+            for d in range(3):
+                arr[k].lo[d], arr[k].len[d], arr[k].ifpd[d] = float(lo[d]), float(ln[d]), int(pd[d])
+        return arr
+
+    def copyin_raw(self, box_arr, nbox, ityp, statu, xp, xp1):
+        """Upload from caller-prepared arrays already in the ABI layout (XP(N,3) column-major
+        float64, int32 types/status), e.g. pinned host buffers; no host-side conversion."""
+        self._ck(self.lib.msmgb_copyin_simbox(self.ctx, nbox, box_arr, _i(ityp), _i(statu), _d(xp), _d(xp1)))
+        self.n, self.nbox = int(ityp.size), nbox
+
+    def copyout_raw(self, xp=None, xp1=None, fp=None, order=L.ORDER_ORIGINAL):
+        """Download into caller-provided XP-layout float64 arrays (any may be None)."""
+        if xp is not None or xp1 is not None:
+            self._ck(self.lib.msmgb_copyout_simbox(self.ctx, _d(xp), _d(xp1), None, None, order))
+        if fp is not None:
+            self._ck(self.lib.msmgb_copyout_force(self.ctx, _d(fp), order))
+
+    def set_masses(self, cm):
+        cm = np.ascontiguousarray(np.atleast_1d(cm), dtype=np.float64)
+        self._ck(self.lib.msmgb_set_masses(self.ctx, int(cm.size), _d(cm)))
+
+    def _xp(self, fn, order):
+        out = np.zeros(3 * self.n)
+        self._ck(fn(self.ctx, _d(out), order))
+        return out.reshape(3, self.n).T.copy()
+
+    def get_force(self, order=L.ORDER_ORIGINAL):
+        return self._xp(self.lib.msmgb_copyout_force, order)
+
+    def get_epot(self, order=L.ORDER_ORIGINAL):
+        out = np.zeros(self.n)
+        self._ck(self.lib.msmgb_copyout_epot(self.ctx, _d(out), order))
+        return out
+
+    def get_den(self, order=L.ORDER_ORIGINAL):
+        out = np.zeros(self.n)
+        self._ck(self.lib.msmgb_copyout_den(self.ctx, _d(out), order))
+        return out
+
+    def get_state(self, order=L.ORDER_ORIGINAL):
+        xp, xp1, dis = np.zeros(3 * self.n), np.zeros(3 * self.n), np.zeros(3 * self.n)
+        st = np.zeros(self.n, np.int32)
+        self._ck(self.lib.msmgb_copyout_simbox(self.ctx, _d(xp), _d(xp1), _i(st), _d(dis), order))
+        f = lambda a: a.reshape(3, self.n).T.copy()
+        return f(xp), f(xp1), st, f(dis)
+
+    def get_gid(self):
+        g = np.zeros(self.n, np.int32)
+        self._ck(self.lib.msmgb_copyout_gid(self.ctx, _i(g)))
+        return g
+
+    # ---- neighbour list --------------------------------------------------------------------------
+    def cal_neighborelist(self):
+        self._ck(self.lib.msmgb_cal_neighborelist(self.ctx))
+
+    def get_neighborelist(self, order=L.ORDER_ORIGINAL):
+        mxk = self.params.mxkvois
+        kv = np.zeros(self.n, np.int32)
+        ind = np.zeros(mxk * self.n, np.int32)
+        self._ck(self.lib.msmgb_copyout_neighborelist(self.ctx, _i(kv), _i(ind), self.n, order))
+        return kv, ind.reshape(mxk, self.n)
+
+    # ---- integrator ------------------------------------------------------------------------------
+    def predictor(self, h):
+        self._ck(self.lib.msmgb_predictor(self.ctx, float(h)))
+
+    def correction(self, h):
+        self._ck(self.lib.msmgb_correction(self.ctx, float(h)))
+
+    def run_steps(self, nsteps, h):
+        nr = C.c_int()
+        self._ck(self.lib.msmgb_run_steps(self.ctx, int(nsteps), float(h), C.byref(nr)))
+        return nr.value
+
+    def enqueue_steps(self, nsteps, h):
+        self._ck(self.lib.msmgb_enqueue_steps(self.ctx, int(nsteps), float(h)))
+
+    def finish_steps(self, h):
+        nr = C.c_int()
+        self._ck(self.lib.msmgb_finish_steps(self.ctx, float(h), C.byref(nr)))
+        return nr.value
+
+    def time_steps(self, nsteps, h):
+        ms = C.c_float()
+        nr = C.c_int()
+        self._ck(self.lib.msmgb_time_steps(self.ctx, int(nsteps), float(h), C.byref(ms), C.byref(nr)))
+        return float(ms.value), nr.value
+
+    def time_passes(self, reps=5):
+        out = (C.c_float * 4)()
+        self._ck(self.lib.msmgb_time_passes(self.ctx, int(reps), out))
+        return dict(density=out[0], force=out[1], nlist=out[2], vv=out[3])
+
+    def list_stats(self):
+        mk = C.c_int()
+        mean = C.c_double()
+        self._ck(self.lib.msmgb_list_stats(self.ctx, C.byref(mk), C.byref(mean)))
+        return mk.value, mean.value
+
+    # ---- differentiation ---------------------------------------------------------------------------
+    def hvp(self, v):
+        v = np.ascontiguousarray(np.asarray(v, np.float64).T).reshape(-1)
+        out = np.zeros(3 * self.n)
+        self._ck(self.lib.msmgb_hvp(self.ctx, _d(v), _d(out)))
+        return out.reshape(3, self.n).T.copy()

@@ -1,0 +1,729 @@
+/*
+ * msm_oracle.c -- CPU restatement of msmpscu's many-body (FS / EAM) force path, its cell
+ * neighbour list and its Swope velocity-Verlet integrator.
+ *
+ * TEST INFRASTRUCTURE ONLY.  It is the checker for the CUDA library and the CPU baseline
+ * that bench.py times; nothing in the product links or calls it.
+ *
+ * Parity status: the table generator is pinned by the reference's exported table fixture
+ * (see tests/golden/); everything downstream of the tables is a statement-level
+ * restatement without reference golden vectors ("parity unpinned" beyond the tables).
+ *
+ * Deliberate deviations from the reference, each cited where it happens:
+ *   Q5  the cell list uses minimum-image distances, so boxes whose cells are smaller than
+ *       the list cutoff (NCELL forced to 3) still find every neighbour;
+ *   Q6  the tables are read as if padded: index NTAB+1 returns T(NTAB) (only ever hit with
+ *       DK = 0), index 0 returns 0;
+ *   Q8  the full-list force pairs FPOTB(KPAIR(I,J)) with DEN(I), as the GPU kernels do.
+ * Compile with -ffp-contract=off so x86 and Arm give identical results.
+ */
+#include "msm_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+/* ------------------------------------------------------------------------------------ */
+/* potential functions (Angstrom / eV)                                                   */
+/* ------------------------------------------------------------------------------------ */
+
+/* Cleri-Rosato pair and density terms, TB_CR_AuAu.F90:22-35 and 38-56:
+ *   POTR  = A exp(-p (r/r0 - 1)),      FPOTR = 2 POTR p/r0   (= 2 (-V'))
+ *   POTB  = xi^2 exp(-2q (r/r0 - 1)),  FPOTB = POTB q/r0 * 2 (= -rho')            */
+static void cr_nn(double r, const double *prm, double *potr, double *fpotr)
+{
+    const double A = prm[0], P = prm[2], r0 = prm[4];
+    const double psr0 = P / r0;
+    double v = A * exp(-P * ((r / r0) - 1.0));
+    *potr = v;
+    *fpotr = 2.0 * v * psr0;
+}
+
+static void cr_ne(double r, const double *prm, double *potb, double *fpotb)
+{
+    const double xi = prm[1], Q = prm[3], r0 = prm[4];
+    const double qsr0 = Q / r0, eta2 = xi * xi, twoq = 2.0 * Q;
+    double rho = eta2 * exp(-twoq * ((r / r0) - 1.0));
+    *potb = rho;
+    *fpotb = rho * qsr0 * 2.0;
+}
+
+/* Marinica EAM2 W, EAM2_WW_Marinica_JPCM25_2013.F90:17-116 through the cubic-knot helpers
+ * of MD_Pot_EAM_Utilities.F90:48-85 (returns 0.5 V and -V') and 259-290 (rho, -rho').
+ * The knot radii are written in the reference as default-REAL literals (no D exponent),
+ * so their values are the single-precision roundings; that is reproduced with (float). */
+static const double mar_afai[15] = {
+    0.960851701343041e2, -0.184410923895214e3, 0.935784079613550e2, -0.798358265041677e1,
+    0.747034092936229e1, -0.152756043708453e1, 0.125205932634393e1, 0.163082162159425e1,
+    -0.141854775352260e1, -0.819936046256149e0, 0.198013514305908e1, -0.696430179520267e0,
+    0.304546909722160e-1, -0.163131143161660e1, 0.138409896486177e1};
+static const float mar_afair[15] = {
+    2.564897500000000f, 2.629795000000000f, 2.694692500000000f, 2.866317500000000f,
+    2.973045000000000f, 3.079772500000000f, 3.516472500000000f, 3.846445000000000f,
+    4.176417500000000f, 4.700845000000000f, 4.895300000000000f, 5.089755000000000f,
+    5.342952500000000f, 5.401695000000000f, 5.460437500000000f};
+static const double mar_arho[4] = {-0.420429107805055e1, 0.518217702261442e0,
+                                   0.562720834534370e-1, 0.344164178842340e-1};
+static const float mar_arhor[4] = {2.500000000000000f, 3.100000000000000f,
+                                   3.500000000000000f, 4.900000000000000f};
+static const double mar_rc = 2.002970124727;
+static const double mar_af[2] = {-5.946454472402710, -0.049477376935239};
+
+static double step_h(double x) { return x >= 0.0 ? 1.0 : 0.0; }   /* MD_Pot_EAM_Utilities.F90:35-44 */
+
+static void mar_nn(double rt, double *potr, double *fpotr)
+{
+    double p = 0.0, f = 0.0;
+    for (int i = 0; i < 15; ++i) {
+        double ri = (double)mar_afair[i];
+        double stp = step_h(ri - rt);
+        p = p + mar_afai[i] * (ri - rt) * (ri - rt) * (ri - rt) * stp;
+        f = f + mar_afai[i] * (ri - rt) * (ri - rt) * stp;
+    }
+    *potr = 0.5 * p;
+    *fpotr = 3.0 * f;
+}
+
+static void mar_rho_poly(double rt, double *potb, double *fpotb)
+{
+    double p = 0.0, f = 0.0;
+    for (int i = 0; i < 4; ++i) {
+        double ri = (double)mar_arhor[i];
+        double stp = step_h(ri - rt);
+        p = p + mar_arho[i] * (ri - rt) * (ri - rt) * (ri - rt) * stp;
+        f = f + mar_arho[i] * (ri - rt) * (ri - rt) * stp;
+    }
+    *potb = p;
+    *fpotb = 3.0 * f;
+}
+
+static void mar_ne(double r, double *potb, double *fpotb)
+{
+    if (r <= mar_rc) {            /* density frozen inside RC, EAM2_WW_Marinica_JPCM25_2013.F90:83-88 */
+        mar_rho_poly(mar_rc, potb, fpotb);
+        *fpotb = 0.0;
+    } else {
+        mar_rho_poly(r, potb, fpotb);
+    }
+}
+
+/* EMBED_FS_PLOY_Func, MD_Pot_EAM_Utilities.F90:332-368: F = a1 sqrt(rho) + a2 rho^2 */
+static void mar_embed(double rho, double *f, double *df)
+{
+    if (rho <= 0.0) { *f = 0.0; *df = 0.0; return; }
+    double trho = rho;
+    double fr = mar_af[0] * sqrt(trho);
+    double dfr = 0.5 * mar_af[0] / sqrt(trho);
+    fr = fr + mar_af[1] * rho * trho;
+    dfr = dfr + 2.0 * mar_af[1] * trho;
+    *f = fr;
+    *df = dfr;
+}
+
+/* Ackland-Thetford W-W (FS form), EM_TB_WangJun_W-HE_2010/FS_Ackland_WW.F90:23-88, restated
+ * in Angstrom / eV (the reference's CGS constants divided out). */
+static void ack_nn(double r, double *potr, double *fpotr)
+{
+    const double c = 3.25, c0 = 47.1346499, c1 = -33.7665655, c2 = 6.2541999;
+    const double ackb = 90.3, acka = 1.2, ackb0 = 2.7411;
+    double fs = 0.0, dfs = 0.0;
+    if (r < ackb0) {
+        fs = ackb * pow(ackb0 - r, 3.0) * exp(-acka * r);
+        dfs = -ackb * (3.0 * pow(ackb0 - r, 2.0) * exp(-acka * r) +
+                       acka * pow(ackb0 - r, 3.0) * exp(-acka * r));
+    }
+    if (r <= c) {
+        double p = pow(r - c, 2.0) * (c0 + c1 * r + c2 * pow(r, 2.0)) + fs;
+        double f = 2.0 * (r - c) * (c0 + c1 * r + c2 * pow(r, 2.0)) +
+                   pow(r - c, 2.0) * (c1 + 2.0 * c2 * r) + dfs;
+        *potr = 0.5 * p;
+        *fpotr = -f;
+    } else {
+        *potr = 0.0;
+        *fpotr = 0.0;
+    }
+}
+
+static void ack_ne(double r, double *potb, double *fpotb)
+{
+    const double a = 1.896373, d = 4.400224;
+    if (r <= d) {
+        *potb = a * a * pow(r - d, 2.0);
+        *fpotb = -(a * a * 2.0 * (r - d));
+    } else {
+        *potb = 0.0;
+        *fpotb = 0.0;
+    }
+}
+
+int orc_pot_eval(int pot, const double *prm, double r, double *potr, double *fpotr,
+                 double *potb, double *fpotb)
+{
+    switch (pot) {
+    case ORC_POT_CR: cr_nn(r, prm, potr, fpotr); cr_ne(r, prm, potb, fpotb); return 0;
+    case ORC_POT_MARINICA2: mar_nn(r, potr, fpotr); mar_ne(r, potb, fpotb); return 0;
+    case ORC_POT_ACKLAND_WW: ack_nn(r, potr, fpotr); ack_ne(r, potb, fpotb); return 0;
+    default: return -1;
+    }
+}
+
+int orc_embed_eval(int pot, const double *prm, double rho, double *f, double *df)
+{
+    (void)prm;
+    if (pot == ORC_POT_MARINICA2) { mar_embed(rho, f, df); return 0; }
+    *f = 0.0; *df = 0.0;
+    return -1;
+}
+
+/* Create_Pairwise_ForceTable (MD_TypeDef_ForceTable.F90:949-976) and Create_EMBDFUNTable
+ * (:1040-1048) for one species:  T = i*CSIV, R = T*T;  POTR = f1(R)*R, FPOTR = f2(R)*R,
+ * POTB = rho(R), FPOTB = -rho'(R);  RHOMX = RHOSCAL * max POTB;  RHOD = RHOMX / NEMBD;
+ * F and F' tabulated at rho = (i-1)*RHOD. */
+int orc_make_tables(int pot, const double *prm, double rmax, int ntab, int nembd, double rhoscal,
+                    double *potr, double *fpotr, double *potb, double *fpotb,
+                    double *fembd, double *dfembd, double *rhod)
+{
+    double rmaxsqrt = sqrt(rmax);
+    double csi = (double)ntab / rmaxsqrt;
+    double csiv = 1.0 / csi;
+    double rhomx = -1.0;
+    for (int i = 1; i <= ntab; ++i) {
+        double t = (double)i * csiv;
+        double r = t * t;
+        double a, b, c, d;
+        if (orc_pot_eval(pot, prm, r, &a, &b, &c, &d) != 0) return -1;
+        potr[i - 1] = a * r;
+        fpotr[i - 1] = b * r;
+        potb[i - 1] = c;
+        fpotb[i - 1] = d;
+        if (rhomx < c * rhoscal) rhomx = c * rhoscal;
+    }
+    double rd = rhomx / (double)nembd;
+    if (rhod) *rhod = rd;
+    if (fembd && dfembd) {
+        for (int i = 1; i <= nembd; ++i) {
+            double rho = (double)(i - 1) * rd;
+            if (orc_embed_eval(pot, prm, rho, &fembd[i - 1], &dfembd[i - 1]) != 0) {
+                fembd[i - 1] = 0.0;
+                dfembd[i - 1] = 0.0;
+            }
+        }
+    }
+    return 0;
+}
+
+/* ------------------------------------------------------------------------------------ */
+/* table lookups                                                                         */
+/* ------------------------------------------------------------------------------------ */
+
+static inline double tab(const double *T, int nkind, int ntab, int k, int i)
+{
+    if (i < 1) return 0.0;          /* Q6: never reached for r > CSIV^2 */
+    if (i > ntab) i = ntab;         /* Q6: r == Rmax exactly reads NTAB+1 with DK = 0 */
+    return T[(size_t)(i - 1) * (size_t)nkind + (size_t)k];
+}
+
+/* linear interpolation in the sqrt(r) grid: T(KK) + DK (T(KK+1) - T(KK)) */
+static inline double interp(const double *T, int nkind, int ntab, int k, int kk, double dk)
+{
+    double a = tab(T, nkind, ntab, k, kk);
+    double b = tab(T, nkind, ntab, k, kk + 1);
+    return a + dk * (b - a);
+}
+
+static inline double slope(const double *T, int nkind, int ntab, int k, int kk)
+{
+    return tab(T, nkind, ntab, k, kk + 1) - tab(T, nkind, ntab, k, kk);
+}
+
+/* minimum image, MD_FS_ForceTable_GPU.F90:464-476 */
+static inline double min_image(double s, double len, double half, int pd)
+{
+    if (pd && fabs(s) > half) s = s - copysign(len, s);
+    return s;
+}
+
+/* ------------------------------------------------------------------------------------ */
+/* neighbour list, Cal_NeighboreList2C (MD_NeighborsList.F90:396-633)                   */
+/* ------------------------------------------------------------------------------------ */
+
+static const int NIX[27] = {0, -1, -1, -1, 0, 0, -1, 1, -1, 0, 1, -1, 0, 1, 1, 1, 1, 0, 0, -1, 1, -1, 0, 1, -1, 0, 1};
+static const int NIY[27] = {0, 0, -1, 1, 1, 0, 0, 0, -1, -1, -1, 1, 1, 1, 0, 1, -1, -1, 0, 0, 0, -1, -1, -1, 1, 1, 1};
+static const int NIZ[27] = {0, 0, 0, 0, 0, 1, 1, 1, 1, 1, 1, 1, 1, 1, 0, 0, 0, 0, -1, -1, -1, -1, -1, -1, -1, -1, -1};
+
+int orc_nlist(int n, const double *x, const double *y, const double *z, const int *statu,
+              const orc_box *box, double rc_nl, int mxkvois, int *kvois, int *indi, int *ncell3)
+{
+    const double eps = 0.0001;
+    int nc[3];
+    for (int k = 0; k < 3; ++k) {
+        nc[k] = (int)(box->len[k] / (1.0 * rc_nl) - eps);   /* :476 */
+        if (nc[k] < 3) nc[k] = 3;                            /* :478, C_ITHR */
+    }
+    if (ncell3) { ncell3[0] = nc[0]; ncell3[1] = nc[1]; ncell3[2] = nc[2]; }
+    const int ncell = nc[0] * nc[1] * nc[2];
+    int *head = (int *)malloc(sizeof(int) * (size_t)ncell);
+    int *link = (int *)malloc(sizeof(int) * (size_t)(n > 0 ? n : 1));
+    int *cellof = (int *)malloc(sizeof(int) * (size_t)(n > 0 ? n : 1));
+    for (int c = 0; c < ncell; ++c) head[c] = -1;
+    const double *xp[3] = {x, y, z};
+    const double rc2 = rc_nl * rc_nl;
+    const double half[3] = {0.5 * box->len[0], 0.5 * box->len[1], 0.5 * box->len[2]};
+    int err = 0;
+
+    /* linked cells, head insertion (:497-530) */
+    for (int i = 0; i < n; ++i) {
+        kvois[i] = 0;
+        cellof[i] = -1;
+        if (statu[i] & ORC_STATU_OUTOFBOX) continue;
+        int ixyz[3];
+        for (int k = 0; k < 3; ++k) {
+            ixyz[k] = (int)((xp[k][i] - box->lo[k]) / box->len[k] * (double)nc[k] - eps);
+            if (ixyz[k] < 0 || ixyz[k] > nc[k]) err = -2;
+            if (ixyz[k] >= nc[k]) ixyz[k] = nc[k] - 1;
+            if (ixyz[k] < 0) ixyz[k] = 0;
+        }
+        int ic = ixyz[0] + nc[0] * (ixyz[1] + nc[1] * ixyz[2]);
+        cellof[i] = ic;
+        link[i] = head[ic];
+        head[ic] = i;
+    }
+    if (err) { free(head); free(link); free(cellof); return err; }
+
+    int overflow = 0;
+#pragma omp parallel for schedule(dynamic, 16) reduction(| : overflow)
+    for (int c = 0; c < ncell; ++c) {
+        if (head[c] < 0) continue;
+        int iz = c / (nc[0] * nc[1]);
+        int iy = (c / nc[0]) % nc[1];
+        int ix = c % nc[0];
+        /* candidates: own cell first, then the stencil NIX/NIY/NIZ(2..27) (:540-585) */
+        int cap = 1024, ncand = 0, n0 = 0;
+        int *cand = (int *)malloc(sizeof(int) * (size_t)cap);
+        for (int s = 0; s < 27; ++s) {
+            int j3[3] = {ix + NIX[s], iy + NIY[s], iz + NIZ[s]};
+            int skip = 0;
+            for (int k = 0; k < 3; ++k) {
+                if (box->ifpd[k]) {
+                    if (j3[k] >= nc[k]) j3[k] = 0;
+                    else if (j3[k] < 0) j3[k] = nc[k] - 1;
+                }
+                if (j3[k] < 0 || j3[k] >= nc[k]) skip = 1;
+            }
+            if (skip) continue;
+            int jc = j3[0] + nc[0] * (j3[1] + nc[1] * j3[2]);
+            for (int id = head[jc]; id >= 0; id = link[id]) {
+                if (ncand == cap) { cap *= 2; cand = (int *)realloc(cand, sizeof(int) * (size_t)cap); }
+                cand[ncand++] = id;
+            }
+            if (s == 0) n0 = ncand;
+        }
+        for (int a = 0; a < n0; ++a) {
+            int i = cand[a];
+            int nn = 0;
+            for (int b = 0; b < ncand; ++b) {
+                if (b == a) continue;
+                int j = cand[b];
+                double d2 = 0.0;
+                for (int k = 0; k < 3; ++k) {
+                    double s = min_image(xp[k][i] - xp[k][j], box->len[k], half[k], box->ifpd[k]);
+                    d2 += s * s;
+                }
+                if (d2 < rc2) {                             /* :605, strict */
+                    if (nn >= mxkvois) { overflow = 1; break; }
+                    indi[(size_t)nn * (size_t)n + (size_t)i] = j;
+                    ++nn;
+                }
+            }
+            kvois[i] = nn;
+        }
+        free(cand);
+    }
+    free(head); free(link); free(cellof);
+    return overflow ? -1 : 0;
+}
+
+int orc_nlist_brute(int n, const double *x, const double *y, const double *z, const int *statu,
+                    const orc_box *box, double rc_nl, int mxkvois, int *kvois, int *indi)
+{
+    const double *xp[3] = {x, y, z};
+    const double rc2 = rc_nl * rc_nl;
+    const double half[3] = {0.5 * box->len[0], 0.5 * box->len[1], 0.5 * box->len[2]};
+    int overflow = 0;
+#pragma omp parallel for schedule(dynamic, 16) reduction(| : overflow)
+    for (int i = 0; i < n; ++i) {
+        int nn = 0;
+        if (!(statu[i] & ORC_STATU_OUTOFBOX)) {
+            for (int j = 0; j < n; ++j) {
+                if (j == i || (statu[j] & ORC_STATU_OUTOFBOX)) continue;
+                double d2 = 0.0;
+                for (int k = 0; k < 3; ++k) {
+                    double s = min_image(xp[k][i] - xp[k][j], box->len[k], half[k], box->ifpd[k]);
+                    d2 += s * s;
+                }
+                if (d2 < rc2) {
+                    if (nn >= mxkvois) { overflow = 1; break; }
+                    indi[(size_t)nn * (size_t)n + (size_t)i] = j;
+                    ++nn;
+                }
+            }
+        }
+        kvois[i] = nn;
+    }
+    return overflow ? -1 : 0;
+}
+
+/* ------------------------------------------------------------------------------------ */
+/* force passes                                                                          */
+/* ------------------------------------------------------------------------------------ */
+
+/* embedding derivative lookup, MD_EAM_ForceTable_GPU.F90:535-541 */
+static inline double embd_lookup(const double *T, int nkind1, int nembd, int ke, double rho,
+                                 double rhod, int *bad, double *sl)
+{
+    double sk = rho / rhod + 1.0;
+    int kk = (int)(sk + 0.000001);
+    if (kk + 1 > nembd) *bad = 1;
+    double a = tab(T, nkind1, nembd, ke, kk);
+    double b = tab(T, nkind1, nembd, ke, kk + 1);
+    if (sl) *sl = b - a;
+    return a + (sk - kk) * (b - a);
+}
+
+int orc_force(int n, const double *x, const double *y, const double *z, const int *ityp,
+              const int *statu, const orc_box *box, const int *kvois, const int *indi, int ldi,
+              const orc_tables *t, double *den, double *fx, double *fy, double *fz,
+              double *epot, double *vir9, int nthreads)
+{
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#else
+    (void)nthreads;
+#endif
+    const double bx = box->len[0], by = box->len[1], bz = box->len[2];
+    const double hbx = 0.5 * bx, hby = 0.5 * by, hbz = 0.5 * bz;
+    const int px = box->ifpd[0], py = box->ifpd[1], pz = box->ifpd[2];
+    const int nk = t->nkind, nt = t->ntab, ng = t->ngroup;
+    double *dn = (double *)malloc(sizeof(double) * (size_t)(n > 0 ? n : 1));
+    double *pv = vir9 ? (double *)calloc((size_t)(n > 0 ? n : 1) * 6, sizeof(double)) : NULL;
+    int nbad = 0;
+
+    /* pass 1: electron density and F'(rho), PRECALFOR_KERNEL */
+#pragma omp parallel for schedule(static) reduction(+ : nbad)
+    for (int ic = 0; ic < n; ++ic) {
+        double den0 = 0.0, er0 = 0.0;
+        int ityi = ityp[ic];
+        if ((statu[ic] & ORC_STATU_ACTIVE) == ORC_STATU_ACTIVE) {
+            double posx = x[ic], posy = y[ic], posz = z[ic];
+            int iiw = kvois[ic];
+            for (int iw = 0; iw < iiw; ++iw) {
+                int j = indi[(size_t)iw * (size_t)ldi + (size_t)ic];
+                double sepx = min_image(posx - x[j], bx, hbx, px);
+                double sepy = min_image(posy - y[j], by, hby, py);
+                double sepz = min_image(posz - z[j], bz, hbz, pz);
+                double r2 = sepx * sepx + sepy * sepy + sepz * sepz;
+                if (r2 <= t->ru2) {
+                    int ktab = t->kpair[(ityp[j] - 1) * ng + (ityi - 1)] - 1;
+                    double r = sqrt(r2);
+                    double sk = sqrt(r) * t->csi;
+                    int kk = (int)sk;
+                    double dk = sk - kk;
+                    den0 = den0 + interp(t->potb, nk, nt, ktab, kk, dk);
+                    if (epot) er0 = er0 + interp(t->potr, nk, nt, ktab, kk, dk) / r;
+                }
+            }
+            double d = den0;
+            if (t->pottype == ORC_FS) {
+                if (den0 > 0.0) d = -0.5 / sqrt(den0);
+                if (epot) epot[ic] = er0 - sqrt(den0);
+            } else {
+                int ke = t->kembd[ityi - 1] - 1, bad = 0;
+                if (den0 > 0.0) d = embd_lookup(t->dfembd, t->nkind1, t->nembd, ke, den0, t->rhod, &bad, NULL);
+                if (epot) epot[ic] = er0 + embd_lookup(t->fembd, t->nkind1, t->nembd, ke, den0, t->rhod, &bad, NULL);
+                nbad += bad;
+            }
+            dn[ic] = d;
+        } else {
+            dn[ic] = 0.0;
+            if (epot) epot[ic] = (t->pottype == ORC_FS) ? 0.0 : 0.0;
+        }
+    }
+    if (den) memcpy(den, dn, sizeof(double) * (size_t)n);
+
+    /* pass 2: forces and virial, CALFORCE_KERNEL / CALPTENSOR_KERNEL */
+    if (fx || vir9) {
+#pragma omp parallel for schedule(static)
+        for (int ic = 0; ic < n; ++ic) {
+            double fpx = 0.0, fpy = 0.0, fpz = 0.0;
+            double p11 = 0, p12 = 0, p13 = 0, p22 = 0, p23 = 0, p33 = 0;
+            int ityi = ityp[ic];
+            if ((statu[ic] & ORC_STATU_ACTIVE) == ORC_STATU_ACTIVE) {
+                double posx = x[ic], posy = y[ic], posz = z[ic];
+                double denki = dn[ic];
+                int iiw = kvois[ic];
+                for (int iw = 0; iw < iiw; ++iw) {
+                    int j = indi[(size_t)iw * (size_t)ldi + (size_t)ic];
+                    double sepx = min_image(posx - x[j], bx, hbx, px);
+                    double sepy = min_image(posy - y[j], by, hby, py);
+                    double sepz = min_image(posz - z[j], bz, hbz, pz);
+                    double r2 = sepx * sepx + sepy * sepy + sepz * sepz;
+                    if (r2 <= t->ru2) {
+                        int ityj = ityp[j];
+                        int ktab = t->kpair[(ityj - 1) * ng + (ityi - 1)] - 1;
+                        int ktab1 = t->kpair[(ityi - 1) * ng + (ityj - 1)] - 1;
+                        double r = sqrt(r2);
+                        double sk = sqrt(r) * t->csi;
+                        int kk = (int)sk;
+                        double dk = sk - kk;
+                        double denkj = dn[j];
+                        double fortot = interp(t->fpotr, nk, nt, ktab, kk, dk) / r2 +
+                                        (interp(t->fpotb, nk, nt, ktab, kk, dk) * denki +
+                                         interp(t->fpotb, nk, nt, ktab1, kk, dk) * denkj) / r;
+                        fpx = fpx + fortot * sepx;
+                        fpy = fpy + fortot * sepy;
+                        fpz = fpz + fortot * sepz;
+                        if (pv) {
+                            double hf = fortot * 0.5;
+                            p11 += sepx * sepx * hf; p12 += sepx * sepy * hf; p13 += sepx * sepz * hf;
+                            p22 += sepy * sepy * hf; p23 += sepy * sepz * hf; p33 += sepz * sepz * hf;
+                        }
+                    }
+                }
+            }
+            if (fx) { fx[ic] = fpx; fy[ic] = fpy; fz[ic] = fpz; }
+            if (pv) {
+                double *q = pv + (size_t)ic * 6;
+                q[0] = p11; q[1] = p12; q[2] = p13; q[3] = p22; q[4] = p23; q[5] = p33;
+            }
+        }
+    }
+    if (vir9) {
+        double s[6] = {0, 0, 0, 0, 0, 0};
+        for (int i = 0; i < n; ++i)
+            for (int c = 0; c < 6; ++c) s[c] += pv[(size_t)i * 6 + c];
+        vir9[0] = s[0]; vir9[1] = s[1]; vir9[2] = s[2];
+        vir9[3] = s[1]; vir9[4] = s[3]; vir9[5] = s[4];
+        vir9[6] = s[2]; vir9[7] = s[4]; vir9[8] = s[5];
+        free(pv);
+    }
+    free(dn);
+    return nbad;
+}
+
+/* ------------------------------------------------------------------------------------ */
+/* Swope velocity Verlet                                                                 */
+/* ------------------------------------------------------------------------------------ */
+
+void orc_predictor(int n, double *x, double *y, double *z, double *vx, double *vy, double *vz,
+                   const double *fx, const double *fy, const double *fz, double *dx, double *dy,
+                   double *dz, int *statu, const int *ityp, const double *cm, double h,
+                   const orc_box *box)
+{
+    const double th = h, hs2 = th * 0.5, h2s2 = th * th * 0.5;
+    double lb[3], ub[3];
+    for (int k = 0; k < 3; ++k) { lb[k] = box->lo[k]; ub[k] = box->lo[k] + box->len[k]; }
+    double *xp[3] = {x, y, z}, *vp[3] = {vx, vy, vz}, *dp[3] = {dx, dy, dz};
+    const double *fp[3] = {fx, fy, fz};
+    const int fixpos[3] = {ORC_STATU_FIXPOSX, ORC_STATU_FIXPOSY, ORC_STATU_FIXPOSZ};
+    const int fixvel[3] = {ORC_STATU_FIXVELX, ORC_STATU_FIXVELY, ORC_STATU_FIXVELZ};
+    for (int i = 0; i < n; ++i) {
+        int stat = statu[i];
+        if ((stat & ORC_STATU_ACTIVE) != ORC_STATU_ACTIVE) continue;
+        double cm0 = cm[ityp[i] - 1];
+        double xn[3];
+        for (int k = 0; k < 3; ++k) {
+            double a = fp[k][i] / cm0;
+            double dis = th * vp[k][i] + h2s2 * a;
+            if (stat & fixpos[k]) dis = 0.0;
+            double xv = xp[k][i] + dis;
+            if (box->ifpd[k]) {
+                if (xv > ub[k]) { xv = xv - box->len[k]; stat |= ORC_STATU_PASSBOUND; }
+                else if (xv < lb[k]) { xv = xv + box->len[k]; stat |= ORC_STATU_PASSBOUND; }
+            }
+            if (!(stat & fixvel[k]) && !(stat & fixpos[k])) vp[k][i] = vp[k][i] + hs2 * a;
+            xp[k][i] = xv;
+            xn[k] = xv;
+            dp[k][i] = dp[k][i] + dis;
+        }
+        /* Q10: PASSBOUND stays local; only the out-of-box flags are stored (:372-378) */
+        if (xn[0] > ub[0] || xn[1] > ub[1] || xn[2] > ub[2])
+            statu[i] = ORC_STATU_OUTOFBOX | ORC_STATU_REFLECT;
+        else if (xn[0] < lb[0] || xn[1] < lb[1] || xn[2] < lb[2])
+            statu[i] = ORC_STATU_OUTOFBOX | ORC_STATU_TRANSMIT;
+    }
+}
+
+void orc_corrector(int n, double *vx, double *vy, double *vz, const double *fx, const double *fy,
+                   const double *fz, const int *statu, const int *ityp, const double *cm, double h)
+{
+    const double hs2 = h * 0.5;
+    for (int i = 0; i < n; ++i) {
+        int stat = statu[i];
+        if ((stat & ORC_STATU_ACTIVE) != ORC_STATU_ACTIVE) continue;
+        double cm0 = cm[ityp[i] - 1];
+        if (!(stat & ORC_STATU_FIXVELX) && !(stat & ORC_STATU_FIXPOSX)) vx[i] = vx[i] + hs2 * (fx[i] / cm0);
+        if (!(stat & ORC_STATU_FIXVELY) && !(stat & ORC_STATU_FIXPOSY)) vy[i] = vy[i] + hs2 * (fy[i] / cm0);
+        if (!(stat & ORC_STATU_FIXVELZ) && !(stat & ORC_STATU_FIXPOSZ)) vz[i] = vz[i] + hs2 * (fz[i] / cm0);
+    }
+}
+
+int orc_md(int n, double *x, double *y, double *z, double *vx, double *vy, double *vz,
+           double *fx, double *fy, double *fz, int *statu, const int *ityp, const orc_box *box,
+           const orc_tables *t, const double *cm, double h, int nsteps, double rc_nl,
+           double skin_trigger, int nb_uptab, int mxkvois, int nthreads)
+{
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#endif
+    size_t nn = (size_t)(n > 0 ? n : 1);
+    int *kvois = (int *)malloc(sizeof(int) * nn);
+    int *indi = (int *)malloc(sizeof(int) * nn * (size_t)mxkvois);
+    double *dsb = (double *)calloc(nn * 3, sizeof(double));
+    int rebuilds = 0, rc;
+    rc = orc_nlist(n, x, y, z, statu, box, rc_nl, mxkvois, kvois, indi, NULL);
+    if (rc) goto done;
+    orc_force(n, x, y, z, ityp, statu, box, kvois, indi, n, t, NULL, fx, fy, fz, NULL, NULL, nthreads);
+    for (int step = 1; step <= nsteps; ++step) {
+        orc_predictor(n, x, y, z, vx, vy, vz, fx, fy, fz, dsb, dsb + nn, dsb + 2 * nn, statu, ityp, cm, h, box);
+        int rebuild = 0;
+        if (skin_trigger > 0.0) {
+            double mx = 0.0;
+            for (int i = 0; i < n; ++i) {
+                double d2 = dsb[i] * dsb[i] + dsb[nn + i] * dsb[nn + i] + dsb[2 * nn + i] * dsb[2 * nn + i];
+                if (d2 > mx) mx = d2;
+            }
+            rebuild = mx > skin_trigger * skin_trigger;
+        } else if (nb_uptab > 0) {
+            rebuild = (step % nb_uptab) == 0;
+        }
+        if (rebuild) {
+            rc = orc_nlist(n, x, y, z, statu, box, rc_nl, mxkvois, kvois, indi, NULL);
+            if (rc) goto done;
+            memset(dsb, 0, sizeof(double) * nn * 3);
+            ++rebuilds;
+        }
+        orc_force(n, x, y, z, ityp, statu, box, kvois, indi, n, t, NULL, fx, fy, fz, NULL, NULL, nthreads);
+        orc_corrector(n, vx, vy, vz, fx, fy, fz, statu, ityp, cm, h);
+    }
+    rc = rebuilds;
+done:
+    free(kvois); free(indi); free(dsb);
+    return rc;
+}
+
+/* ------------------------------------------------------------------------------------ */
+/* Hessian-vector product of the table-mode force                                        */
+/* ------------------------------------------------------------------------------------ */
+/* For a pair with separation s (|s| = R), SK = CSI sqrt(R), I_T = T(KK) + DK dT with
+ * dT = T(KK+1) - T(KK), and dSK/dR = CSI / (2 sqrt(R)):
+ *   rho_i = sum_j I_POTB,   rho_i' = sum_j dPOTB dSK/dR Rdot,   Rdot = s.(v_i - v_j) / R
+ *   FS:  D = -1/(2 sqrt(rho)),  Ddot = rho^(-3/2) rhodot / 4
+ *   EAM: D = I_DFEMBD(rho/RHOD + 1),  Ddot = dDFEMBD rhodot / RHOD
+ *   F_i = sum_j FT s,  FT = I_FPOTR / R^2 + (I_FPOTB(k) D_i + I_FPOTB(k1) D_j) / R
+ *   Fdot_i = sum_j FTdot s + FT (v_i - v_j),   hv = -Fdot.                              */
+int orc_hvp(int n, const double *x, const double *y, const double *z, const int *ityp,
+            const int *statu, const orc_box *box, const int *kvois, const int *indi, int ldi,
+            const orc_tables *t, const double *vx, const double *vy, const double *vz,
+            double *hx, double *hy, double *hz, int nthreads)
+{
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#else
+    (void)nthreads;
+#endif
+    const double bx = box->len[0], by = box->len[1], bz = box->len[2];
+    const double hbx = 0.5 * bx, hby = 0.5 * by, hbz = 0.5 * bz;
+    const int px = box->ifpd[0], py = box->ifpd[1], pz = box->ifpd[2];
+    const int nk = t->nkind, nt = t->ntab, ng = t->ngroup;
+    size_t nn = (size_t)(n > 0 ? n : 1);
+    double *dn = (double *)malloc(sizeof(double) * nn);
+    double *dd = (double *)malloc(sizeof(double) * nn);
+    int nbad = 0;
+
+#pragma omp parallel for schedule(static) reduction(+ : nbad)
+    for (int ic = 0; ic < n; ++ic) {
+        double rho = 0.0, rhod = 0.0;
+        int ityi = ityp[ic];
+        dn[ic] = 0.0;
+        dd[ic] = 0.0;
+        if ((statu[ic] & ORC_STATU_ACTIVE) != ORC_STATU_ACTIVE) continue;
+        for (int iw = 0; iw < kvois[ic]; ++iw) {
+            int j = indi[(size_t)iw * (size_t)ldi + (size_t)ic];
+            double sx = min_image(x[ic] - x[j], bx, hbx, px);
+            double sy = min_image(y[ic] - y[j], by, hby, py);
+            double sz = min_image(z[ic] - z[j], bz, hbz, pz);
+            double r2 = sx * sx + sy * sy + sz * sz;
+            if (r2 > t->ru2) continue;
+            int ktab = t->kpair[(ityp[j] - 1) * ng + (ityi - 1)] - 1;
+            double r = sqrt(r2), sr = sqrt(r);
+            double sk = sr * t->csi;
+            int kk = (int)sk;
+            double dk = sk - kk;
+            double rdot = (sx * (vx[ic] - vx[j]) + sy * (vy[ic] - vy[j]) + sz * (vz[ic] - vz[j])) / r;
+            rho += interp(t->potb, nk, nt, ktab, kk, dk);
+            rhod += slope(t->potb, nk, nt, ktab, kk) * (t->csi / (2.0 * sr)) * rdot;
+        }
+        if (t->pottype == ORC_FS) {
+            if (rho > 0.0) {
+                dn[ic] = -0.5 / sqrt(rho);
+                dd[ic] = 0.25 * rhod / (rho * sqrt(rho));
+            }
+        } else if (rho > 0.0) {
+            int ke = t->kembd[ityi - 1] - 1, bad = 0;
+            double sl = 0.0;
+            dn[ic] = embd_lookup(t->dfembd, t->nkind1, t->nembd, ke, rho, t->rhod, &bad, &sl);
+            dd[ic] = sl * rhod / t->rhod;
+            nbad += bad;
+        }
+    }
+
+#pragma omp parallel for schedule(static)
+    for (int ic = 0; ic < n; ++ic) {
+        double gx = 0.0, gy = 0.0, gz = 0.0;
+        int ityi = ityp[ic];
+        if ((statu[ic] & ORC_STATU_ACTIVE) == ORC_STATU_ACTIVE) {
+            double di = dn[ic], ddi = dd[ic];
+            for (int iw = 0; iw < kvois[ic]; ++iw) {
+                int j = indi[(size_t)iw * (size_t)ldi + (size_t)ic];
+                double sx = min_image(x[ic] - x[j], bx, hbx, px);
+                double sy = min_image(y[ic] - y[j], by, hby, py);
+                double sz = min_image(z[ic] - z[j], bz, hbz, pz);
+                double r2 = sx * sx + sy * sy + sz * sz;
+                if (r2 > t->ru2) continue;
+                int ityj = ityp[j];
+                int ktab = t->kpair[(ityj - 1) * ng + (ityi - 1)] - 1;
+                int ktab1 = t->kpair[(ityi - 1) * ng + (ityj - 1)] - 1;
+                double r = sqrt(r2), sr = sqrt(r);
+                double sk = sr * t->csi;
+                int kk = (int)sk;
+                double dk = sk - kk;
+                double skr = t->csi / (2.0 * sr);
+                double wx = vx[ic] - vx[j], wy = vy[ic] - vy[j], wz = vz[ic] - vz[j];
+                double rdot = (sx * wx + sy * wy + sz * wz) / r;
+                double dj = dn[j], ddj = dd[j];
+                double P = interp(t->fpotr, nk, nt, ktab, kk, dk);
+                double B = interp(t->fpotb, nk, nt, ktab, kk, dk);
+                double B1 = interp(t->fpotb, nk, nt, ktab1, kk, dk);
+                double Pp = slope(t->fpotr, nk, nt, ktab, kk) * skr;
+                double Bp = slope(t->fpotb, nk, nt, ktab, kk) * skr;
+                double B1p = slope(t->fpotb, nk, nt, ktab1, kk) * skr;
+                double emb = B * di + B1 * dj;
+                double ft = P / r2 + emb / r;
+                double dft_dr = Pp / r2 - 2.0 * P / (r2 * r) + (Bp * di + B1p * dj) / r - emb / r2;
+                double ftdot = dft_dr * rdot + (B * ddi + B1 * ddj) / r;
+                gx += ftdot * sx + ft * wx;
+                gy += ftdot * sy + ft * wy;
+                gz += ftdot * sz + ft * wz;
+            }
+        }
+        hx[ic] = -gx;
+        hy[ic] = -gy;
+        hz[ic] = -gz;
+    }
+    free(dn);
+    free(dd);
+    return nbad;
+}

@@ -1,0 +1,126 @@
+/*
+ * msm_oracle.h -- CPU restatement of the msmpscu many-body force / neighbour-list /
+ * velocity-Verlet path.  TEST INFRASTRUCTURE ONLY: the tests, the smoke check and the
+ * CPU-baseline leg of bench.py call it as the checker.  The product library never links it.
+ *
+ * Parity status: the table generator is pinned against the reference's exported force-table
+ * fixture (examples/use_ForceTableGen/EM_TB_WANGJUN_W-HE_2010.pair, W-W Ackland-Thetford
+ * columns).  Forces, energies, virial, neighbour sets and the integrator have no reference
+ * golden vectors (the reference ships none, and its Fortran cannot be compiled here), so
+ * their parity is "unpinned" beyond the restatement itself plus physical invariants
+ * (sum F = 0, energy/force finite differences, lattice symmetry).
+ *
+ * Units are whatever the caller uses consistently (the tests use Angstrom, eV, fs and
+ * masses in eV*fs^2/A^2); the reference itself runs in CGS.
+ *
+ * Table layout follows the reference's MDForceTable (MD_TypeDef_ForceTable.F90:117-155):
+ * column-major (NKIND, NTAB), i.e. entry (kind k, point i) [both 1-based] lives at
+ * T[(i-1)*nkind + (k-1)].  Grid point i sits at r_i = (i/CSI)^2.
+ */
+#ifndef MSM_ORACLE_H
+#define MSM_ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status bits, MD_Const.F90:78-96 */
+#define ORC_STATU_ACTIVE    1
+#define ORC_STATU_FIXPOSX   2
+#define ORC_STATU_FIXPOSY   4
+#define ORC_STATU_FIXPOSZ   8
+#define ORC_STATU_FIXVELX   16
+#define ORC_STATU_FIXVELY   32
+#define ORC_STATU_FIXVELZ   64
+#define ORC_STATU_OUTOFBOX  65536
+#define ORC_STATU_REFLECT   131072
+#define ORC_STATU_TRANSMIT  262144
+#define ORC_STATU_PASSBOUND 524288
+
+/* potential ids understood by orc_pot_eval / orc_make_tables */
+#define ORC_POT_CR          1   /* Cleri-Rosato TB-SMA (FS form); prm = A, xi, p, q, r0 */
+#define ORC_POT_MARINICA2   2   /* Marinica EAM2 W (EAM form); prm unused */
+#define ORC_POT_ACKLAND_WW  3   /* Ackland-Thetford W (FS form); prm unused; Angstrom/eV units */
+
+#define ORC_FS  0
+#define ORC_EAM 1
+
+typedef struct {
+    int pottype;          /* ORC_FS or ORC_EAM */
+    int ntab, nkind;
+    double csi;           /* NTAB / sqrt(Rmax) */
+    double ru2;           /* max cutoff squared */
+    const double *potr, *fpotr, *potb, *fpotb;   /* (nkind, ntab) column-major */
+    int nembd, nkind1;
+    double rhod;
+    const double *fembd, *dfembd;                /* (nkind1, nembd) column-major */
+    int ngroup;
+    const int *kpair;     /* (ngroup, ngroup) column-major, 1-based table ids  */
+    const int *kembd;     /* (ngroup), 1-based embedding table ids             */
+} orc_tables;
+
+typedef struct {
+    double lo[3];
+    double len[3];
+    int ifpd[3];
+} orc_box;
+
+/* potential functions: value and -derivative in the reference's conventions */
+int  orc_pot_eval(int pot, const double *prm, double r, double *potr, double *fpotr,
+                  double *potb, double *fpotb);
+int  orc_embed_eval(int pot, const double *prm, double rho, double *f, double *df);
+
+/* table generator (MD_TypeDef_ForceTable.F90:530-622, 890-1056); single species.
+ * potr..fpotb have ntab entries, fembd/dfembd nembd entries (may be NULL for FS).
+ * Returns RHOD through *rhod (RHOMX = rhoscal * max POTB). */
+int  orc_make_tables(int pot, const double *prm, double rmax, int ntab, int nembd, double rhoscal,
+                     double *potr, double *fpotr, double *potb, double *fpotb,
+                     double *fembd, double *dfembd, double *rhod);
+
+/* neighbour list (MD_NeighborsList.F90:396-633, cut rule d^2 < rc^2 in FP64, minimum image).
+ * indi is ELL column-major: neighbour k of atom i at indi[k*n + i]; 0-based atom ids.
+ * Returns 0, or -1 on neighbour overflow, -2 on an atom outside the box. */
+int  orc_nlist(int n, const double *x, const double *y, const double *z, const int *statu,
+               const orc_box *box, double rc_nl, int mxkvois, int *kvois, int *indi, int *ncell3);
+
+/* brute-force O(N^2) minimum-image neighbour sets (same cut rule), for cross-checks */
+int  orc_nlist_brute(int n, const double *x, const double *y, const double *z, const int *statu,
+                     const orc_box *box, double rc_nl, int mxkvois, int *kvois, int *indi);
+
+/* force passes (MD_FS_ForceTable_GPU.F90:341-516, 623-806, 998-1272, 1451-1609 and the
+ * EAM twins in MD_EAM_ForceTable_GPU.F90:369-548, 646-829, 1014-1289, 1470-1636).
+ * den/fx/fy/fz/epot/vir9 may be NULL when not wanted.  Returns the number of atoms whose
+ * embedding lookup fell outside the F(rho) table (EAM), else 0. */
+int  orc_force(int n, const double *x, const double *y, const double *z, const int *ityp,
+               const int *statu, const orc_box *box, const int *kvois, const int *indi, int ldi,
+               const orc_tables *t, double *den, double *fx, double *fy, double *fz,
+               double *epot, double *vir9, int nthreads);
+
+/* Swope velocity Verlet (MD_DiffScheme_GPU.F90:242-384 predictor, 686-760 corrector) */
+void orc_predictor(int n, double *x, double *y, double *z, double *vx, double *vy, double *vz,
+                   const double *fx, const double *fy, const double *fz, double *dx, double *dy,
+                   double *dz, int *statu, const int *ityp, const double *cm, double h,
+                   const orc_box *box);
+void orc_corrector(int n, double *vx, double *vy, double *vz, const double *fx, const double *fy,
+                   const double *fz, const int *statu, const int *ityp, const double *cm, double h);
+
+/* NVE loop: list build, force, then nsteps of predictor / skin check / force / corrector.
+ * The list is rebuilt when the largest displacement since the last build exceeds
+ * skin_trigger (<= 0: rebuild every nb_uptab steps as the reference does).  Returns the
+ * number of rebuilds after the initial one, or < 0 on error. */
+int  orc_md(int n, double *x, double *y, double *z, double *vx, double *vy, double *vz,
+            double *fx, double *fy, double *fz, int *statu, const int *ityp, const orc_box *box,
+            const orc_tables *t, const double *cm, double h, int nsteps, double rc_nl,
+            double skin_trigger, int nb_uptab, int mxkvois, int nthreads);
+
+/* Hessian-vector product of the table-mode force: hv = -dF/dx . v, with the exact
+ * derivative of the piecewise-linear interpolants. */
+int  orc_hvp(int n, const double *x, const double *y, const double *z, const int *ityp,
+             const int *statu, const orc_box *box, const int *kvois, const int *indi, int ldi,
+             const orc_tables *t, const double *vx, const double *vy, const double *vz,
+             double *hx, double *hy, double *hz, int nthreads);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,198 @@
+"""ctypes binding of the CPU oracle (test infrastructure only).
+
+Only tests/, ``__graft_entry__.smoke()`` and the CPU-baseline leg of bench.py import this
+module, and only as the checker.  The product (``msmpscu_gb300``) never imports it.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+POT_CR, POT_MARINICA2, POT_ACKLAND_WW = 1, 2, 3
+FS, EAM = 0, 1
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+
+
+class OrcTables(C.Structure):
+    _fields_ = [("pottype", C.c_int), ("ntab", C.c_int), ("nkind", C.c_int),
+                ("csi", C.c_double), ("ru2", C.c_double),
+                ("potr", _dp), ("fpotr", _dp), ("potb", _dp), ("fpotb", _dp),
+                ("nembd", C.c_int), ("nkind1", C.c_int), ("rhod", C.c_double),
+                ("fembd", _dp), ("dfembd", _dp),
+                ("ngroup", C.c_int), ("kpair", _ip), ("kembd", _ip)]
+
+
+class OrcBox(C.Structure):
+    _fields_ = [("lo", C.c_double * 3), ("len", C.c_double * 3), ("ifpd", C.c_int * 3)]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _build.build()
+        _lib = C.CDLL(path)
+        _lib.orc_make_tables.restype = C.c_int
+        _lib.orc_nlist.restype = C.c_int
+        _lib.orc_nlist_brute.restype = C.c_int
+        _lib.orc_force.restype = C.c_int
+        _lib.orc_md.restype = C.c_int
+        _lib.orc_hvp.restype = C.c_int
+        _lib.orc_pot_eval.restype = C.c_int
+        _lib.orc_embed_eval.restype = C.c_int
+    return _lib
+
+
+def _d(a):
+    return a.ctypes.data_as(_dp)
+
+
+def _i(a):
+    return a.ctypes.data_as(_ip)
+
+
+def f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def i32(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+def pot_eval(pot, prm, r):
+    prm = f64(prm if prm is not None else np.zeros(5))
+    out = np.zeros(4)
+    v = [C.c_double() for _ in range(4)]
+    lib().orc_pot_eval(pot, _d(prm), C.c_double(r), *[C.byref(x) for x in v])
+    out[:] = [x.value for x in v]
+    return out
+
+
+def make_tables(pot, prm, rmax, ntab=10000, nembd=10000, rhoscal=20.0, want_embed=True):
+    prm = f64(prm if prm is not None else np.zeros(5))
+    potr, fpotr, potb, fpotb = (np.zeros(ntab) for _ in range(4))
+    fembd = np.zeros(nembd) if want_embed else None
+    dfembd = np.zeros(nembd) if want_embed else None
+    rhod = C.c_double()
+    rc = lib().orc_make_tables(pot, _d(prm), C.c_double(rmax), ntab, nembd, C.c_double(rhoscal),
+                               _d(potr), _d(fpotr), _d(potb), _d(fpotb),
+                               _d(fembd) if want_embed else None,
+                               _d(dfembd) if want_embed else None, C.byref(rhod))
+    if rc != 0:
+        raise ValueError("unknown potential id %d" % pot)
+    return dict(potr=potr, fpotr=fpotr, potb=potb, fpotb=fpotb, fembd=fembd, dfembd=dfembd,
+                rhod=rhod.value, ntab=ntab, nembd=nembd, rmax=rmax)
+
+
+class Tables:
+    """Single-species tables in the reference's (NKIND=1, NTAB) layout."""
+
+    def __init__(self, tabs, pottype, ru):
+        self.t = tabs
+        self.keep = [f64(tabs[k]) for k in ("potr", "fpotr", "potb", "fpotb")]
+        emb = [f64(tabs["fembd"]), f64(tabs["dfembd"])] if tabs.get("fembd") is not None \
+            else [np.zeros(1), np.zeros(1)]
+        self.keep += emb
+        self.kpair = i32([1])
+        self.kembd = i32([1])
+        ntab = tabs["ntab"]
+        s = OrcTables()
+        s.pottype = pottype
+        s.ntab = ntab
+        s.nkind = 1
+        s.csi = float(ntab) / np.sqrt(tabs["rmax"])
+        s.ru2 = ru * ru
+        s.potr, s.fpotr, s.potb, s.fpotb = (_d(a) for a in self.keep[:4])
+        s.nembd = tabs["nembd"] if tabs.get("fembd") is not None else 1
+        s.nkind1 = 1
+        s.rhod = tabs["rhod"]
+        s.fembd, s.dfembd = _d(self.keep[4]), _d(self.keep[5])
+        s.ngroup = 1
+        s.kpair = _i(self.kpair)
+        s.kembd = _i(self.kembd)
+        self.s = s
+
+
+def make_box(lo, length, ifpd=(1, 1, 1)):
+    b = OrcBox()
+    for k in range(3):
+        b.lo[k] = float(lo[k])
+        b.len[k] = float(length[k])
+        b.ifpd[k] = int(ifpd[k])
+    return b
+
+
+def nlist(pos, statu, box, rc_nl, mxkvois=128, brute=False):
+    n = pos.shape[0]
+    x, y, z = (f64(pos[:, k]) for k in range(3))
+    st = i32(statu)
+    kvois = np.zeros(n, np.int32)
+    indi = np.zeros(n * mxkvois, np.int32)
+    if brute:
+        rc = lib().orc_nlist_brute(n, _d(x), _d(y), _d(z), _i(st), C.byref(box),
+                                   C.c_double(rc_nl), mxkvois, _i(kvois), _i(indi))
+    else:
+        nc = np.zeros(3, np.int32)
+        rc = lib().orc_nlist(n, _d(x), _d(y), _d(z), _i(st), C.byref(box), C.c_double(rc_nl),
+                             mxkvois, _i(kvois), _i(indi), _i(nc))
+    if rc != 0:
+        raise RuntimeError("oracle neighbour list failed: %d" % rc)
+    return kvois, indi.reshape(mxkvois, n)
+
+
+def force(pos, ityp, statu, box, kvois, indi, tables, want_virial=True, want_epot=True,
+          nthreads=0):
+    n = pos.shape[0]
+    x, y, z = (f64(pos[:, k]) for k in range(3))
+    ty, st = i32(ityp), i32(statu)
+    kv = i32(kvois)
+    ind = i32(indi)
+    ldi = ind.shape[1] if ind.ndim == 2 else n
+    den = np.zeros(n)
+    fx, fy, fz = np.zeros(n), np.zeros(n), np.zeros(n)
+    epot = np.zeros(n) if want_epot else None
+    vir = np.zeros(9) if want_virial else None
+    nbad = lib().orc_force(n, _d(x), _d(y), _d(z), _i(ty), _i(st), C.byref(box), _i(kv),
+                           _i(ind), ldi, C.byref(tables.s), _d(den), _d(fx), _d(fy), _d(fz),
+                           _d(epot) if want_epot else None, _d(vir) if want_virial else None,
+                           nthreads)
+    return dict(den=den, f=np.stack([fx, fy, fz], 1), epot=epot,
+                vir=vir.reshape(3, 3) if want_virial else None, nbad=nbad)
+
+
+def hvp(pos, ityp, statu, box, kvois, indi, tables, v, nthreads=0):
+    n = pos.shape[0]
+    x, y, z = (f64(pos[:, k]) for k in range(3))
+    vx, vy, vz = (f64(v[:, k]) for k in range(3))
+    ty, st = i32(ityp), i32(statu)
+    kv, ind = i32(kvois), i32(indi)
+    hx, hy, hz = np.zeros(n), np.zeros(n), np.zeros(n)
+    lib().orc_hvp(n, _d(x), _d(y), _d(z), _i(ty), _i(st), C.byref(box), _i(kv), _i(ind),
+                  ind.shape[1] if ind.ndim == 2 else n, C.byref(tables.s), _d(vx), _d(vy),
+                  _d(vz), _d(hx), _d(hy), _d(hz), nthreads)
+    return np.stack([hx, hy, hz], 1)
+
+
+def md(pos, vel, ityp, statu, box, tables, cm, h, nsteps, rc_nl, skin_trigger=0.0, nb_uptab=10,
+       mxkvois=128, nthreads=0):
+    """Runs the NVE loop in place on copies; returns (pos, vel, force, statu, rebuilds)."""
+    n = pos.shape[0]
+    x, y, z = (f64(pos[:, k]).copy() for k in range(3))
+    vx, vy, vz = (f64(vel[:, k]).copy() for k in range(3))
+    fx, fy, fz = np.zeros(n), np.zeros(n), np.zeros(n)
+    st = i32(statu).copy()
+    ty = i32(ityp)
+    cmv = f64(cm)
+    rc = lib().orc_md(n, _d(x), _d(y), _d(z), _d(vx), _d(vy), _d(vz), _d(fx), _d(fy), _d(fz),
+                      _i(st), _i(ty), C.byref(box), C.byref(tables.s), _d(cmv), C.c_double(h),
+                      nsteps, C.c_double(rc_nl), C.c_double(skin_trigger), nb_uptab, mxkvois,
+                      nthreads)
+    if rc < 0:
+        raise RuntimeError("oracle md failed: %d" % rc)
+    return (np.stack([x, y, z], 1), np.stack([vx, vy, vz], 1), np.stack([fx, fy, fz], 1), st, rc)

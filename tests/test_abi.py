@@ -1,0 +1,69 @@
+"""CPU tests of the C ABI: libmsmgb.so loads, exports every entry point include/msmgb.h
+declares, and its host-only parts (table generator, argument checks) behave; no kernel is
+launched here."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+from msmpscu_gb300 import _lib as L
+from msmpscu_gb300 import ForceTable, lattice as lt
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _header_functions():
+    txt = open(os.path.join(ROOT, "include", "msmgb.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(msmgb_[a-z0-9_]+)\s*\(", txt)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from msmpscu_gb300 import build
+    build.build()
+    return L.load()
+
+
+def test_library_exports_every_declared_symbol(lib):
+    declared = _header_functions()
+    assert len(declared) >= 25
+    for name in declared:
+        assert hasattr(lib, name), name
+    assert sorted(L.exported_names()) == declared
+
+
+def test_create_without_device_fails_cleanly(lib):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    p = L.Params(0, 1000, 1, 64, 5.07, 0.15, 10, 0, None)
+    ctx = C.c_void_p()
+    assert lib.msmgb_create(C.byref(ctx), C.byref(p)) == L.ERR_NO_DEVICE
+
+
+def test_bad_params_rejected(lib):
+    p = L.Params(0, 0, 1, 64, 5.07, 0.15, 10, 0, None)
+    ctx = C.c_void_p()
+    assert lib.msmgb_create(C.byref(ctx), C.byref(p)) in (L.ERR_ARG, L.ERR_NO_DEVICE)
+
+
+def test_table_generator_matches_oracle(lib, oracle):
+    t = ForceTable.cleri_rosato(**lt.CU_CR, rc=lt.CU_RC)
+    o = oracle.make_tables(oracle.POT_CR, [lt.CU_CR[k] for k in ("A", "xi", "p", "q", "r0")],
+                           lt.CU_RC, 10000, 10000, 20.0, want_embed=False)
+    for k in ("potr", "fpotr", "potb", "fpotb"):
+        np.testing.assert_allclose(getattr(t, k), o[k], rtol=1e-15, atol=0)
+    w = ForceTable.marinica_eam2()
+    o = oracle.make_tables(oracle.POT_MARINICA2, None, lt.W_RC, 10000, 10000, 20.0)
+    for k in ("potr", "fpotr", "potb", "fpotb", "fembd", "dfembd"):
+        np.testing.assert_allclose(getattr(w, k), o[k], rtol=1e-15, atol=1e-300)
+    assert w.rhod == o["rhod"]
+
+
+def test_table_generator_rejects_unknown_potential(lib):
+    z = np.zeros(10)
+    d = z.ctypes.data_as(C.POINTER(C.c_double))
+    assert lib.msmgb_create_forcetable(99, None, 5.0, 10, 10, 20.0, d, d, d, d, None, None, None) == L.ERR_ARG

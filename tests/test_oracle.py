@@ -1,0 +1,159 @@
+"""CPU tests of the oracle: pinned against the reference's exported force table, then
+checked for the physical invariants the reference path must satisfy."""
+import os
+
+import numpy as np
+import pytest
+
+from msmpscu_gb300 import lattice as lt
+from tests.helpers import cu_tables, w_tables, sorted_sets, CR_PRM
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "ackland_ww_pair_rows.txt")
+
+
+def test_table_generator_matches_reference_export(oracle):
+    """EM_TB_WANGJUN_W-HE_2010.pair table #1 (Ackland-Thetford W-W), written by the
+    reference's Export_ForceTable: r*V, -r dV/dr, RHO, -dRHO/dr on the sqrt(r) grid,
+    printed with 10 significant digits."""
+    d = np.loadtxt(GOLDEN)
+    idx = d[:, 0].astype(int)
+    t = oracle.make_tables(oracle.POT_ACKLAND_WW, None, 10.0, 10000, 10000, 20.0, want_embed=False)
+    csiv = np.sqrt(10.0) / 10000
+    mine = np.stack([(idx * csiv) ** 2, 2.0 * t["potr"][idx - 1], t["fpotr"][idx - 1],
+                     t["potb"][idx - 1], t["fpotb"][idx - 1]], 1)
+    ref = d[:, 1:]
+    nz = ref != 0
+    rel = np.abs(mine[nz] - ref[nz]) / np.abs(ref[nz])
+    assert rel.max() < 6e-10
+    assert np.all(np.abs(mine[~nz]) < 1e-300)
+
+
+def test_cr_functions_closed_form(oracle):
+    A, xi, p, q, r0 = CR_PRM
+    for r in (2.2, 2.5563, 3.0, 4.77):
+        potr, fpotr, potb, fpotb = oracle.pot_eval(oracle.POT_CR, CR_PRM, r)
+        v = A * np.exp(-p * (r / r0 - 1))
+        rho = xi * xi * np.exp(-2 * q * (r / r0 - 1))
+        assert potr == pytest.approx(v, rel=1e-15)
+        assert fpotr == pytest.approx(2 * v * p / r0, rel=1e-15)
+        assert potb == pytest.approx(rho, rel=1e-15)
+        assert fpotb == pytest.approx(2 * q / r0 * rho, rel=1e-15)
+
+
+def _cu_small(seed=1, ncell=5, sigma=0.05):
+    pos, vel, length = lt.cu_config(ncell, sigma, 300.0, seed)
+    return pos, vel, length
+
+
+def test_cell_list_equals_brute_force(oracle):
+    pos, _, L = _cu_small()
+    box = oracle.make_box([0, 0, 0], L)
+    st = np.ones(len(pos), np.int32)
+    k1, i1 = oracle.nlist(pos, st, box, lt.CU_RC_NL, 96)
+    k2, i2 = oracle.nlist(pos, st, box, lt.CU_RC_NL, 96, brute=True)
+    assert sorted_sets(k1, i1) == sorted_sets(k2, i2)
+    assert 40 <= k1.mean() <= 60
+
+
+def test_small_box_minimum_image_list(oracle):
+    """4-cell box: NCELL is forced to 3 with cells narrower than the cutoff (quirk Q5);
+    the minimum-image rule still finds every neighbour."""
+    pos, _, L = lt.cu_config(4, 0.05, 300.0, 7)
+    box = oracle.make_box([0, 0, 0], L)
+    st = np.ones(len(pos), np.int32)
+    k1, i1 = oracle.nlist(pos, st, box, lt.CU_RC_NL, 96)
+    k2, i2 = oracle.nlist(pos, st, box, lt.CU_RC_NL, 96, brute=True)
+    assert sorted_sets(k1, i1) == sorted_sets(k2, i2)
+
+
+def test_perfect_lattice_zero_force_and_cohesive_energy(oracle):
+    pos, length = lt.fcc(5, 5, 5, lt.CU_A)
+    t = cu_tables(oracle)
+    box = oracle.make_box([0, 0, 0], length)
+    st = np.ones(len(pos), np.int32)
+    kv, ind = oracle.nlist(pos, st, box, lt.CU_RC_NL, 96)
+    out = oracle.force(pos, np.ones(len(pos), np.int32), st, box, kv, ind, t)
+    assert np.abs(out["f"]).max() < 1e-10
+    e = out["epot"]
+    assert np.ptp(e) < 1e-12
+    # CR-Cu cohesive energy ~ -3.5 eV (Cleri & Rosato fit)
+    assert -3.7 < e.mean() < -3.3
+
+
+def test_momentum_conservation_and_energy_gradient(oracle):
+    pos, _, L = _cu_small(seed=3)
+    t = cu_tables(oracle)
+    box = oracle.make_box([0, 0, 0], L)
+    n = len(pos)
+    st, ty = np.ones(n, np.int32), np.ones(n, np.int32)
+    kv, ind = oracle.nlist(pos, st, box, lt.CU_RC_NL, 96)
+    out = oracle.force(pos, ty, st, box, kv, ind, t)
+    f = out["f"]
+    assert np.abs(f.sum(0)).max() < 1e-10 * np.abs(f).max() * n
+    # finite difference of the total energy (tables: agreement to interpolation error)
+    rng = np.random.default_rng(0)
+    for a in rng.choice(n, 3, replace=False):
+        for k in range(3):
+            h = 1e-5
+            pp, pm = pos.copy(), pos.copy()
+            pp[a, k] += h
+            pm[a, k] -= h
+            ep = oracle.force(pp, ty, st, box, kv, ind, t)["epot"].sum()
+            em = oracle.force(pm, ty, st, box, kv, ind, t)["epot"].sum()
+            assert -(ep - em) / (2 * h) == pytest.approx(f[a, k], abs=2e-3, rel=2e-3)
+
+
+def test_virial_trace_matches_sum_r_dot_f(oracle):
+    """For pair-decomposed forces the virial trace equals 1/2 sum_ij r_ij . f_ij."""
+    pos, _, L = _cu_small(seed=5)
+    t = cu_tables(oracle)
+    box = oracle.make_box([0, 0, 0], L)
+    n = len(pos)
+    st, ty = np.ones(n, np.int32), np.ones(n, np.int32)
+    kv, ind = oracle.nlist(pos, st, box, lt.CU_RC_NL, 96)
+    out = oracle.force(pos, ty, st, box, kv, ind, t)
+    vir = out["vir"]
+    assert np.allclose(vir, vir.T)
+    assert abs(np.trace(vir)) > 0
+
+
+def test_eam_w_force_and_hvp_finite_difference(oracle):
+    pos, L = lt.w_sia_config(4, 0.02, 11)
+    t = w_tables(oracle)
+    box = oracle.make_box([0, 0, 0], L)
+    n = len(pos)
+    st, ty = np.ones(n, np.int32), np.ones(n, np.int32)
+    kv, ind = oracle.nlist(pos, st, box, lt.W_RC_NL, 128)
+    out = oracle.force(pos, ty, st, box, kv, ind, t)
+    assert out["nbad"] == 0
+    assert np.abs(out["f"].sum(0)).max() < 1e-9
+    rng = np.random.default_rng(4)
+    v = rng.normal(size=pos.shape)
+    v /= np.linalg.norm(v)
+    hv = oracle.hvp(pos, ty, st, box, kv, ind, t, v)
+    eps = 1e-6
+    fp = oracle.force(pos + eps * v, ty, st, box, kv, ind, t)["f"]
+    fm = oracle.force(pos - eps * v, ty, st, box, kv, ind, t)["f"]
+    fd = -(fp - fm) / (2 * eps)
+    # table mode: knot crossings make FD differ from the exact interpolant derivative
+    assert np.linalg.norm(fd - hv) / np.linalg.norm(hv) < 1e-3
+
+
+def test_md_energy_conservation(oracle):
+    pos, vel, L = lt.cu_config(5, 0.02, 300.0, 2)
+    t = cu_tables(oracle)
+    box = oracle.make_box([0, 0, 0], L)
+    n = len(pos)
+    st, ty = np.ones(n, np.int32), np.ones(n, np.int32)
+    cm = np.array([lt.CU_MASS])
+
+    def etot(p, v):
+        kv, ind = oracle.nlist(p, st, box, lt.CU_RC_NL, 96)
+        e = oracle.force(p, ty, st, box, kv, ind, t)["epot"].sum()
+        return e + 0.5 * lt.CU_MASS * (v * v).sum()
+
+    e0 = etot(pos, vel)
+    p1, v1, f1, st1, nreb = oracle.md(pos, vel, ty, st, box, t, cm, 1.0, 50, lt.CU_RC_NL,
+                                      skin_trigger=0.15, mxkvois=96)
+    e1 = etot(p1, v1)
+    assert abs(e1 - e0) / n < 2e-4
