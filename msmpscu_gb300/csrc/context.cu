@@ -83,7 +83,7 @@ __global__ void k_pack(DevAtoms a, const double *xp, const double *xp1, const in
     double x = xp[i], y = xp[n + i], z = xp[2 * n + i];
     a.pos[i] = make_double4_32a(x, y, z, 0.0);
     a.pos_bld[i] = make_double4_32a(x, y, z, 0.0);
-    a.pos32[i] = make_float4((float)x, (float)y, (float)z, 0.0f);
+    a.posff[i] = make_posff(x, y, z, a.box[boxid[i]]);
     a.vx[i] = xp1 ? xp1[i] : 0.0;
     a.vy[i] = xp1 ? xp1[n + i] : 0.0;
     a.vz[i] = xp1 ? xp1[2 * n + i] : 0.0;
@@ -118,6 +118,12 @@ __global__ void k_unpack_pos(const double4_32a *pos, const int *gid, int n, int 
     dst[g] = p.x;
     dst[n + g] = p.y;
     dst[2 * n + g] = p.z;
+}
+
+__global__ void k_f32_to_f64(const float *src, int n, double *dst)
+{
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < n) dst[s] = (double)src[s];
 }
 
 __global__ void k_unpack_int(const int *src, const int *gid, int n, int sorted, int *dst)
@@ -165,7 +171,7 @@ extern "C" int msmgb_create(msmgb_ctx **out, const msmgb_params *p)
     a.ld = c->cap_atoms;
 #define AL(ptr, cnt)                                            \
     if ((e = dalloc(&(ptr), (cnt))) != cudaSuccess) return fail(e, "cudaMalloc " #ptr);
-    AL(a.pos, N) AL(a.pos32, N) AL(a.pos_bld, N)
+    AL(a.pos, N) AL(a.posff, N) AL(a.pos_bld, N)
     AL(a.vx, N) AL(a.vy, N) AL(a.vz, N)
     AL(a.fx, N) AL(a.fy, N) AL(a.fz, N)
     AL(a.dx, N) AL(a.dy, N) AL(a.dz, N)
@@ -202,7 +208,7 @@ extern "C" int msmgb_destroy(msmgb_ctx *c)
     if (c->stream) cudaStreamSynchronize(c->stream);
     free_graph(c);
     DevAtoms &a = c->a;
-    void *ptrs[] = {a.pos, a.pos32, a.pos_bld, a.vx, a.vy, a.vz, a.fx, a.fy, a.fz,
+    void *ptrs[] = {a.pos, a.posff, a.pos_bld, a.vx, a.vy, a.vz, a.fx, a.fy, a.fz,
                     a.dx, a.dy, a.dz, a.ityp, a.statu, a.gid, a.boxid, a.den, a.epot,
                     a.den32, a.kvois, a.indi, c->cell_of, c->perm, c->dbox, c->cm,
                     c->flags, c->maxdisp, c->virial, c->scratch, c->cell_start,
@@ -300,42 +306,74 @@ extern "C" int msmgb_init_forcetable(msmgb_ctx *c, const msmgb_forcetable *ft)
             t.kembd[i] = id - 1;
         }
     // padded rows: index 0 -> 0, 1..NTAB -> table, NTAB+1 -> T(NTAB) (quirk Q6)
-    const size_t rowp = (size_t)t.ntp, nk = (size_t)t.nkind;
-    const size_t nd = 4 * nk * rowp + (eam ? 2 * (size_t)t.nkind1 * t.nep : 0);
-    const size_t nf = 4 * nk * rowp;
+    const size_t rowp = (size_t)t.ntp, nk = (size_t)t.nkind, nk1 = (size_t)t.nkind1, nep = (size_t)t.nep;
+    const size_t nd = 4 * nk * rowp + (eam ? 2 * nk1 * nep : 0);
     std::vector<double> hd(nd, 0.0);
-    std::vector<float> hf(nf, 0.0f);
     const double *src[4] = {ft->potr, ft->fpotr, ft->potb, ft->fpotb};
     for (int q = 0; q < 4; ++q)
         for (size_t k = 0; k < nk; ++k) {
             double *row = hd.data() + ((size_t)q * nk + k) * rowp;
             for (int i = 1; i <= t.ntab; ++i) row[i] = src[q][(size_t)(i - 1) * nk + k];
             row[t.ntab + 1] = row[t.ntab];
-            float *rf = hf.data() + ((size_t)q * nk + k) * rowp;
-            for (size_t i = 0; i < rowp; ++i) rf[i] = (float)row[i];
         }
     if (eam) {
         const double *es[2] = {ft->fembd, ft->dfembd};
         for (int q = 0; q < 2; ++q)
-            for (int k = 0; k < t.nkind1; ++k) {
-                double *row = hd.data() + 4 * nk * rowp + ((size_t)q * t.nkind1 + k) * t.nep;
-                for (int i = 1; i <= t.nembd; ++i) row[i] = es[q][(size_t)(i - 1) * t.nkind1 + k];
+            for (size_t k = 0; k < nk1; ++k) {
+                double *row = hd.data() + 4 * nk * rowp + ((size_t)q * nk1 + k) * nep;
+                for (int i = 1; i <= t.nembd; ++i) row[i] = es[q][(size_t)(i - 1) * nk1 + k];
                 row[t.nembd + 1] = row[t.nembd];
+            }
+    }
+    // FP32 interleaved tables of the mixed passes: value and slope (slope taken in FP64)
+    const double *hpotr = hd.data(), *hfpotr = hpotr + nk * rowp, *hpotb = hpotr + 2 * nk * rowp,
+                 *hfpotb = hpotr + 3 * nk * rowp;
+    std::vector<float> f2((size_t)2 * nk * rowp), f4((size_t)4 * nk * rowp), e2((size_t)2 * nk1 * nep);
+    for (size_t k = 0; k < nk; ++k)
+        for (size_t i = 0; i < rowp; ++i) {
+            size_t o = k * rowp + i, o1 = i + 1 < rowp ? o + 1 : o;
+            f2[2 * o] = (float)hpotb[o];
+            f2[2 * o + 1] = (float)(hpotb[o1] - hpotb[o]);
+            f4[4 * o] = (float)hfpotr[o];
+            f4[4 * o + 1] = (float)(hfpotr[o1] - hfpotr[o]);
+            f4[4 * o + 2] = (float)hfpotb[o];
+            f4[4 * o + 3] = (float)(hfpotb[o1] - hfpotb[o]);
+        }
+    if (eam) {
+        const double *hdf = hpotr + 4 * nk * rowp + nk1 * nep;
+        for (size_t k = 0; k < nk1; ++k)
+            for (size_t i = 0; i < nep; ++i) {
+                size_t o = k * nep + i, o1 = i + 1 < nep ? o + 1 : o;
+                e2[2 * o] = (float)hdf[o];
+                e2[2 * o + 1] = (float)(hdf[o1] - hdf[o]);
             }
     }
     CK(cudaStreamSynchronize(c->stream), "synchronize");
     if (c->tab_mem) { cudaFree(c->tab_mem); c->tab_mem = nullptr; }
-    CK(cudaMalloc(&c->tab_mem, nd * sizeof(double) + nf * sizeof(float) + 256), "table alloc");
-    double *dd = (double *)c->tab_mem;
-    float *df = (float *)(dd + nd);
+    const size_t bytes = nd * sizeof(double) + (f2.size() + f4.size() + e2.size()) * sizeof(float) + 1024;
+    CK(cudaMalloc(&c->tab_mem, bytes), "table alloc");
+    char *base = (char *)c->tab_mem;
+    double *dd = (double *)base;
+    float *df4 = (float *)(base + ((nd * sizeof(double) + 255) / 256) * 256);
+    float *df2 = df4 + f4.size();
+    float *de2 = df2 + f2.size();
     CK(cudaMemcpy(dd, hd.data(), nd * sizeof(double), cudaMemcpyHostToDevice), "table upload");
-    CK(cudaMemcpy(df, hf.data(), nf * sizeof(float), cudaMemcpyHostToDevice), "table upload");
+    CK(cudaMemcpy(df4, f4.data(), f4.size() * sizeof(float), cudaMemcpyHostToDevice), "table upload");
+    CK(cudaMemcpy(df2, f2.data(), f2.size() * sizeof(float), cudaMemcpyHostToDevice), "table upload");
+    if (eam) CK(cudaMemcpy(de2, e2.data(), e2.size() * sizeof(float), cudaMemcpyHostToDevice), "table upload");
     t.potr = dd; t.fpotr = dd + nk * rowp; t.potb = dd + 2 * nk * rowp; t.fpotb = dd + 3 * nk * rowp;
-    t.potr32 = df; t.fpotr32 = df + nk * rowp; t.potb32 = df + 2 * nk * rowp; t.fpotb32 = df + 3 * nk * rowp;
     if (eam) {
         t.fembd = dd + 4 * nk * rowp;
-        t.dfembd = t.fembd + (size_t)t.nkind1 * t.nep;
+        t.dfembd = t.fembd + nk1 * nep;
     }
+    t.force4 = (const float4 *)df4;
+    t.dens2 = (const float2 *)df2;
+    t.embd2 = eam ? (const float2 *)de2 : nullptr;
+    t.csih = (float)t.csi;
+    t.csil = (float)(t.csi - (double)t.csih);
+    t.ru2h = (float)t.ru2;
+    t.ru2l = (float)(t.ru2 - (double)t.ru2h);
+    t.rhodf = (float)t.rhod;
     c->tab = t;
     c->have_tables = true;
     c->force_valid = false;
@@ -382,6 +420,7 @@ extern "C" int msmgb_copyin_simbox(msmgb_ctx *c, int nbox, const msmgb_box *boxe
             d.len[k] = boxes[b].len[k];
             d.half[k] = 0.5 * boxes[b].len[k];
             d.lenf[k] = (float)d.len[k];
+            d.lenlo[k] = (float)(d.len[k] - (double)d.lenf[k]);
             d.halff[k] = (float)d.half[k];
             d.ifpd[k] = boxes[b].ifpd[k] ? 1 : 0;
             if (d.len[k] <= 0.0) return set_err(c, MSMGB_ERR_ARG, "box length must be positive");
@@ -525,6 +564,13 @@ extern "C" int msmgb_copyout_den(msmgb_ctx *c, double *den, int order)
     if (!c || !den) return MSMGB_ERR_ARG;
     RET(need_state(c));
     RET(use_device(c));
+    if (c->den_is32) {   // the last density pass was the mixed one: F'(rho) is held in FP32
+        double *conv = (double *)((char *)c->scratch + 64 * (size_t)c->cap_atoms);
+        k_f32_to_f64<<<nblk(c->n, kBlock), kBlock, 0, c->stream>>>(c->a.den32, c->n, conv);
+        c->launches += 1;
+        RET(check_launch(c, "copy-out"));
+        return copy_out_doubles(c, conv, nullptr, nullptr, den, order);
+    }
     return copy_out_doubles(c, c->a.den, nullptr, nullptr, den, order);
 }
 

@@ -212,6 +212,7 @@ int launch_density(msmgb_ctx *c, bool want_epot)
         else dens_dispatch<MSMGB_EAM_TYPE, false>(c, want_epot);
     }
     c->launches += 1;
+    c->den_is32 = false;
     return check_launch(c, "density pass");
 }
 

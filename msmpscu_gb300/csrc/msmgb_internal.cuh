@@ -3,7 +3,9 @@
 //
 // Layout in HBM (all per-atom arrays are in cell-sorted order, capacity = max_atoms):
 //   pos      double4_32a  x, y, z, (unused)           gathered by the pair loops (one 32 B sector)
-//   pos32    float4   FP32 neighbour copy for the mixed passes (rebuilt by the integrator)
+//   posff    2xfloat4 float-float copy of the position in the shifted frame u = x - lo + L
+//                     (u in [L, 2L], so hi_i - hi_j is exact); rebuilt by the integrator,
+//                     gathered by the list prefilter and the mixed passes
 //   vx..vz   double   velocities (SoA, streamed)
 //   fx..fz   double   forces (SoA, streamed)
 //   dis      double   accumulated displacement DIS (reference MD_DiffScheme_GPU.F90:364-366)
@@ -41,11 +43,17 @@ enum {
     kFlagWords = 8
 };
 
+struct __align__(32) PosFF {
+    float hx, hy, hz, hw;
+    float lx, ly, lz, lw;
+};
+
 struct DevBox {
     double lo[3];
     double len[3];
     double half[3];
-    float lenf[3];       // FP32 copies for the prefilter / mixed passes
+    float lenf[3];       // float-float box length (hi, lo) and FP32 half length
+    float lenlo[3];
     float halff[3];
     int ifpd[3];
     int nc[3];
@@ -58,7 +66,13 @@ struct DevTables {
     int ntab, nkind, ntp;          // ntp = ntab + 2 (padded row length)
     double csi, ru2;
     const double *potr, *fpotr, *potb, *fpotb;     // [nkind][ntp]
-    const float *potr32, *fpotr32, *potb32, *fpotb32;
+    // mixed-precision tables: value and slope to the next grid point, interleaved
+    const float2 *dens2;           // [nkind][ntp] {POTB(k), POTB(k+1)-POTB(k)}
+    const float4 *force4;          // [nkind][ntp] {FPOTR, dFPOTR, FPOTB, dFPOTB}
+    const float2 *embd2;           // [nkind1][nep] {DFEMBD, dDFEMBD}
+    float csih, csil;              // CSI as float-float
+    float ru2h, ru2l;              // RU^2 as float-float
+    float rhodf;
     int nembd, nkind1, nep;        // nep = nembd + 2
     double rhod;
     const double *fembd, *dfembd;  // [nkind1][nep]
@@ -70,7 +84,7 @@ struct DevTables {
 // Pointers of the atom state, passed by value to kernels.
 struct DevAtoms {
     double4_32a *pos;
-    float4 *pos32;
+    PosFF *posff;
     double *vx, *vy, *vz;
     double *fx, *fy, *fz;
     double *dx, *dy, *dz;
@@ -88,6 +102,23 @@ struct DevAtoms {
     unsigned long long *maxdisp;
     double *virial;      // [nbox][6]
 };
+
+__device__ __forceinline__ void split_ff(double u, float &h, float &l)
+{
+    h = __double2float_rn(u);
+    l = __double2float_rn(u - (double)h);
+}
+
+__device__ __forceinline__ PosFF make_posff(double x, double y, double z, const DevBox &b)
+{
+    PosFF p;
+    split_ff(x - b.lo[0] + b.len[0], p.hx, p.lx);
+    split_ff(y - b.lo[1] + b.len[1], p.hy, p.ly);
+    split_ff(z - b.lo[2] + b.len[2], p.hz, p.lz);
+    p.hw = 0.0f;
+    p.lw = 0.0f;
+    return p;
+}
 
 }  // namespace msmgb
 
@@ -125,6 +156,7 @@ struct msmgb_ctx {
 
     bool list_valid = false;
     bool force_valid = false;
+    bool den_is32 = false;             // the last density pass was the mixed one
 
     // CUDA graph of one MD step
     cudaGraphExec_t step_graph = nullptr;

@@ -207,7 +207,7 @@ __global__ void k_copyback(DevAtoms a, Stage s, int *cell_of, int predicated)
     if (i >= a.n) return;
     double4_32a p = s.pos[i];
     a.pos[i] = p;
-    a.pos32[i] = make_float4((float)p.x, (float)p.y, (float)p.z, 0.0f);
+    a.posff[i] = make_posff(p.x, p.y, p.z, a.box[s.boxid[i]]);
     a.vx[i] = s.vx[i]; a.vy[i] = s.vy[i]; a.vz[i] = s.vz[i];
     a.dx[i] = s.dx[i]; a.dy[i] = s.dy[i]; a.dz[i] = s.dz[i];
     a.ityp[i] = s.ityp[i];
@@ -238,7 +238,7 @@ __global__ void __launch_bounds__(kBlock) k_build(DevAtoms a, const int *cell_of
     a.pos_bld[i] = p;
     if (a.statu[i] & MSMGB_STATU_OUTOFBOX) { a.kvois[i] = 0; return; }
     const DevBox &b = a.box[a.boxid[i]];
-    const float4 pf = a.pos32[i];
+    const PosFF pf = a.posff[i];
     int c = cell_of[i] - b.cell0;
     int ix = c % b.nc[0], iy = (c / b.nc[0]) % b.nc[1], iz = c / (b.nc[0] * b.nc[1]);
     int nn = 0;
@@ -259,10 +259,10 @@ __global__ void __launch_bounds__(kBlock) k_build(DevAtoms a, const int *cell_of
         int e = start[g + 1];
         for (int j = start[g]; j < e; ++j) {
             if (j == i) continue;
-            float4 q = a.pos32[j];
-            float sx = mi32(pf.x - q.x, b.lenf[0], b.halff[0], b.ifpd[0]);
-            float sy = mi32(pf.y - q.y, b.lenf[1], b.halff[1], b.ifpd[1]);
-            float sz = mi32(pf.z - q.z, b.lenf[2], b.halff[2], b.ifpd[2]);
+            const PosFF q = a.posff[j];
+            float sx = mi32(pf.hx - q.hx, b.lenf[0], b.halff[0], b.ifpd[0]);
+            float sy = mi32(pf.hy - q.hy, b.lenf[1], b.halff[1], b.ifpd[1]);
+            float sz = mi32(pf.hz - q.hz, b.lenf[2], b.halff[2], b.ifpd[2]);
             float d2f = sx * sx + sy * sy + sz * sz;
             bool in;
             if (d2f < d2lo) {
@@ -292,9 +292,10 @@ __global__ void __launch_bounds__(kBlock) k_build(DevAtoms a, const int *cell_of
 
 static inline int nblk(long n, int b) { return (int)((n + b - 1) / b); }
 
-// Margin of the FP32 prefilter: the FP32 copy of a coordinate is within half an ulp of the
-// FP64 value, the subtraction and the image shift add at most two more roundings of the
-// same size, so each separation component is within 4 ulp(2*extent) of the exact one.
+// Margin of the FP32 prefilter: it uses the hi parts of the shifted coordinates
+// (u in [L, 2L]): hi_i - hi_j and the image shift by float(L) are exact (Sterbenz), so a
+// separation component is off by at most |lo_i - lo_j| + |L - float(L)| <= 1.5 ulp(2L);
+// the band below allows 4 ulp of the largest coordinate extent plus the rounding of d^2.
 static void prefilter_band(const msmgb_ctx *c, double rc2, float *lo, float *hi)
 {
     double ext = 1.0;

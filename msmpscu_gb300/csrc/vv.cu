@@ -6,7 +6,8 @@
 //              v += h/2 F/m, with the same operations in the same order, so one pass over
 //              x, v, F replaces the reference's two launches.  It also reduces the largest
 //              displacement since the last list build (skin trigger) and refreshes the
-//              FP32 neighbour copy of the positions.
+//              float-float copy of the positions used by the list prefilter and the mixed
+//              passes.
 //   k_correct  Correction_KERNEL alone (end of a run, or msmgb_correction()).
 //   k_decide   one thread: rebuild flag for this step from the skin trigger (or the
 //              reference's fixed NB_UPTAB interval, MD_Method_GenericMD_GPU.F90:599-601).
@@ -81,7 +82,7 @@ __global__ void __launch_bounds__(kBlock) k_vv(DevAtoms a, double th, int mode)
             if (!(stat & MSMGB_STATU_FIXVELY) && !(stat & MSMGB_STATU_FIXPOSY)) vy = vy + hs2 * ay;
             if (!(stat & MSMGB_STATU_FIXVELZ) && !(stat & MSMGB_STATU_FIXPOSZ)) vz = vz + hs2 * az;
             a.pos[i] = make_double4_32a(x, y, z, p.w);
-            a.pos32[i] = make_float4((float)x, (float)y, (float)z, 0.0f);
+            a.posff[i] = make_posff(x, y, z, b);
             a.vx[i] = vx; a.vy[i] = vy; a.vz[i] = vz;
             a.dx[i] += dx; a.dy[i] += dy; a.dz[i] += dz;
             // Predictor_KERNEL0 :372-378 (PASSBOUND is not stored, quirk Q10)

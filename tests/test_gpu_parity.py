@@ -297,3 +297,80 @@ def test_full_size_c2_fp64_properties_and_sample_parity(oracle):
     for i in rng.choice(n, 2000, replace=False):
         assert sorted(ind[:kv[i], i].tolist()) == sorted(oind[:okv[i], i].tolist())
     e.close()
+
+
+# ---- mixed precision ------------------------------------------------------------------------
+
+def _force_err(f, ref):
+    return (np.linalg.norm(f - ref) / np.linalg.norm(ref), np.abs(f - ref).max() / np.abs(ref).max())
+
+
+@pytest.mark.parametrize("ncell,sigma,seed", [(10, 0.05, 2024), (8, 0.1, 5)])
+def test_mixed_force_error_below_1e6(oracle, ncell, sigma, seed):
+    """FP32 pair/density/table terms: force error against the FP64 oracle (norm-wise and
+    max-abs, both relative) below 1e-6."""
+    pos, vel, L_ = lt.cu_config(ncell, sigma, 600.0, seed)
+    t = cu_tables(oracle)
+    ref, _, _ = _oracle_force(oracle, pos, L_, t)
+    e = _cu_engine(len(pos), precision="mixed")
+    e.copyin(_box(len(pos), L_), pos, vel)
+    e.calforce()
+    nrm, mx = _force_err(e.get_force(), ref["f"])
+    assert nrm < 1e-6 and mx < 1e-6, (nrm, mx)
+    assert rel_err(e.get_den(), ref["den"]) < 1e-6
+    # FP64 virial / energy requests still run the FP64 passes
+    vir = e.calptensor()[0]
+    assert rel_err(vir, ref["vir"]) < TOL
+    e.close()
+
+
+def test_mixed_md_tracks_fp64(oracle):
+    pos, vel, L_ = lt.cu_config(8, 0.05, 600.0, 6)
+    n = len(pos)
+    t = cu_tables(oracle)
+    box = oracle.make_box([0, 0, 0], L_)
+    ox, ov, of, _, _ = oracle.md(pos, vel, np.ones(n, np.int32), np.ones(n, np.int32), box, t,
+                                 np.array([lt.CU_MASS]), 1.0, 50, lt.CU_RC_NL, skin_trigger=0.15,
+                                 mxkvois=96)
+    e = _cu_engine(n, precision="mixed")
+    e.copyin(_box(n, L_), pos, vel)
+    e.run_steps(50, 1.0)
+    gx, gv, _, _ = e.get_state()
+    dx = gx - ox
+    dx -= np.round(dx / L_) * L_
+    assert np.max(np.abs(dx)) < 1e-6
+    nrm, mx = _force_err(e.get_force(), of)
+    assert nrm < 2e-6
+    e.close()
+
+
+def test_mixed_eam_force_error(oracle):
+    pos, L_ = lt.w_sia_config(8, 0.03, 13)
+    t = w_tables(oracle)
+    ref, _, _ = _oracle_force(oracle, pos, L_, t, rc_nl=lt.W_RC_NL, mxk=128)
+    e = Engine(len(pos), lt.W_RC_NL, mxkvois=96, precision="mixed")
+    e.init_forcetable(ForceTable.marinica_eam2())
+    e.copyin(_box(len(pos), L_), pos)
+    e.calforce()
+    nrm, mx = _force_err(e.get_force(), ref["f"])
+    assert nrm < 1e-6 and mx < 2e-6, (nrm, mx)
+    e.close()
+
+
+def test_mixed_batched_boxes(oracle):
+    boxes = lt.uneven_batch(5, seed=33, cmin=4, cmax=6)
+    pos = np.vstack([b[0] for b in boxes])
+    vel = np.vstack([b[1] for b in boxes])
+    desc = [(len(b[0]), (0, 0, 0), tuple(b[2]), (1, 1, 1)) for b in boxes]
+    e = _cu_engine(len(pos), nbox=len(boxes), precision="mixed")
+    e.copyin(desc, pos, vel)
+    e.calforce()
+    f = e.get_force()
+    t = cu_tables(oracle)
+    off = 0
+    for p, v, L_ in boxes:
+        ref, _, _ = _oracle_force(oracle, p, L_, t)
+        nrm, mx = _force_err(f[off:off + len(p)], ref["f"])
+        assert nrm < 1e-6 and mx < 1e-6
+        off += len(p)
+    e.close()
