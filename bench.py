@@ -105,10 +105,31 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def workload():
+def workload(ncell=NCELL):
     from msmpscu_gb300 import lattice as lt
-    pos, vel, L = lt.cu_config(NCELL, SIGMA, TEMP, SEED)
+    pos, vel, L = lt.cu_config(ncell, SIGMA, TEMP, SEED)
     return pos, vel, L
+
+
+def precision_compare(e, box, pos, vel, steps):
+    """FP64 form on the same state: its atom-steps/s and the mixed force error against it
+    (norm-wise and max-abs, relative).  The FP64 form is itself parity-checked against the
+    oracle at 1e-10 by the GPU tests."""
+    e.copyin(box, pos, vel)
+    e.set_precision("fp64")
+    e.calforce()
+    f64 = e.get_force()
+    e.set_precision("mixed")
+    e.calforce()
+    f32 = e.get_force()
+    d = f32 - f64
+    err_norm = float(np.linalg.norm(d) / np.linalg.norm(f64))
+    err_max = float(np.abs(d).max() / np.abs(f64).max())
+    e.set_precision("fp64")
+    e.run_steps(3, DT)
+    ms64, _ = e.time_steps(steps, DT)
+    e.set_precision("mixed")
+    return err_norm, err_max, len(pos) * steps / (ms64 / 1e3)
 
 
 def make_engine(n, precision, device=0):
@@ -217,7 +238,7 @@ def run_ours(args):
     device = local if ws > 1 else 0
     from msmpscu_gb300 import build as lib_build
     lib_build.build()
-    pos, vel, L = workload()
+    pos, vel, L = workload(args.ncell)
     n = len(pos)
     prec = args.precision
     e = make_engine(n, prec, device)
@@ -263,6 +284,12 @@ def run_ours(args):
     h2d = n * (24 + 24 + 4 + 4) / args.steps
     d2h = n * (24 + 24 + 24) / args.steps
 
+    cmp = None
+    if prec == "mixed" and not args.no_compare:
+        en, em, v64 = precision_compare(e, box, pos, vel, max(3, min(args.steps, 40)))
+        cmp = {"fp64_value": v64, "mixed_value": value / ws, "speedup": value / ws / v64,
+               "mixed_force_err_norm": en, "mixed_force_err_max": em}
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         threads = os.cpu_count() or 1
@@ -275,8 +302,9 @@ def run_ours(args):
                 "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64" if prec == "fp64" else "f32+f64",
                 "data": "synthetic (seeded fcc Cu lattice, Gaussian displacements, Maxwell-Boltzmann velocities)",
-                "config": {"workload": "fcc Cu 80x80x80 cells, 2,048,000 atoms, Cleri-Rosato, sigma 0.05 A, "
-                                       "600 K, NVE dt=1fs, skin 0.3 A (rebuild at 0.15 A)",
+                "config": {"workload": "fcc Cu %dx%dx%d cells, %d atoms, Cleri-Rosato, sigma 0.05 A, "
+                                       "600 K, NVE dt=1fs, skin 0.3 A (rebuild at 0.15 A)"
+                                       % (args.ncell, args.ncell, args.ncell, n),
                            "atoms": n, "precision": prec, "parallelism": "replicas" if ws > 1 else "single GPU",
                            "l2": "inputs larger than L2 (~0.9 GB touched per step)",
                            "rebuilds_in_timed_steps": rebuilds, "mean_neighbours": kmean,
@@ -289,6 +317,7 @@ def run_ours(args):
                                   "frac": bm["step"] * value / ws / 1e9 / hbm,
                                   "bytes_per_atom_step": bm["step"]},
                 "pass_ms": passes,
+                "precision_compare": cmp,
                 "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
                 "cpu_baseline": cpu,
                 "clocks": clk.summary(),
@@ -331,7 +360,10 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
+    ap.add_argument("--ncell", type=int, default=NCELL,
+                    help="fcc cells per edge (80 = the benchmark; smaller for profiling captures)")
+    ap.add_argument("--no-compare", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--ref-budget-s", type=float, default=150.0)
