@@ -194,6 +194,18 @@ int  msmgb_list_stats(msmgb_ctx *ctx, int *maxk, double *meank);
  * the reference: it replaces finite-difference force pairs (MD_Method_ART_GPU.F90:454-576). */
 int  msmgb_hvp(msmgb_ctx *ctx, const double *v, double *hv);
 
+/* Force-matching adjoint for the Cleri-Rosato parameters theta = (A, xi, p, q, r0) of the
+ * tables currently loaded (which must have been generated from prm): computes the FP64
+ * forces F of every box, L = sum_i |F_i - Ft_i|^2 and dL/dtheta (grad[5]) by one adjoint
+ * pass pair (density recomputed).  ft: 3*N target forces, XP layout, caller order.
+ * No counterpart in the reference (it has no potential fitting). */
+int  msmgb_param_adjoint(msmgb_ctx *ctx, int pot, const double *prm, const double *ft,
+                         double *loss, double *grad);
+/* Parameter derivatives of the Cleri-Rosato tables on the sqrt(r) grid of
+ * msmgb_create_forcetable: d[(m*3 + t)*ntab + i-1] for theta_m, m = 0..4, and t = 0 FPOTR,
+ * 1 POTB, 2 FPOTB.  Host only. */
+int  msmgb_cr_param_tables(const double *prm, double rmax, int ntab, double *d);
+
 /* ---- host-side table generator (Create_Interaction_ForceTable,
  *      MD_TypeDef_ForceTable.F90:890-1056) -------------------------------------------------- */
 #define MSMGB_POT_CR          1   /* Cleri-Rosato TB-SMA, FS form; prm = A, xi, p, q, r0     */

@@ -74,6 +74,8 @@ SIGNATURES = [
     ("msmgb_time_passes", C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_float)]),
     ("msmgb_list_stats", C.c_int, [C.c_void_p, _ip, _dp]),
     ("msmgb_hvp", C.c_int, [C.c_void_p, _dp, _dp]),
+    ("msmgb_param_adjoint", C.c_int, [C.c_void_p, C.c_int, _dp, _dp, _dp, _dp]),
+    ("msmgb_cr_param_tables", C.c_int, [_dp, C.c_double, C.c_int, _dp]),
     ("msmgb_create_forcetable", C.c_int, [C.c_int, _dp, C.c_double, C.c_int, C.c_int, C.c_double,
                                           _dp, _dp, _dp, _dp, _dp, _dp, _dp]),
 ]

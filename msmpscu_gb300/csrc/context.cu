@@ -212,7 +212,7 @@ extern "C" int msmgb_destroy(msmgb_ctx *c)
                     a.dx, a.dy, a.dz, a.ityp, a.statu, a.gid, a.boxid, a.den, a.epot,
                     a.den32, a.kvois, a.indi, c->cell_of, c->perm, c->dbox, c->cm,
                     c->flags, c->maxdisp, c->virial, c->scratch, c->cell_start,
-                    c->cell_cursor, c->scan_tmp, c->tab_mem};
+                    c->cell_cursor, c->scan_tmp, c->tab_mem, c->adj_mem};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     if (c->h_flags) cudaFreeHost(c->h_flags);
@@ -375,6 +375,7 @@ extern "C" int msmgb_init_forcetable(msmgb_ctx *c, const msmgb_forcetable *ft)
     t.ru2l = (float)(t.ru2 - (double)t.ru2h);
     t.rhodf = (float)t.rhod;
     c->tab = t;
+    c->tab_rmax = ft->rmax;
     c->have_tables = true;
     c->force_valid = false;
     free_graph(c);
@@ -818,6 +819,56 @@ extern "C" int msmgb_hvp(msmgb_ctx *c, const double *v, double *hv)
     RET(check_launch(c, "hvp copy-out"));
     CK(cudaMemcpyAsync(hv, io, sizeof(double) * 3 * (size_t)n, cudaMemcpyDeviceToHost, c->stream), "hvp copy-out");
     return poll_flags(c);
+}
+
+extern "C" int msmgb_cr_param_tables(const double *prm, double rmax, int ntab, double *d);
+
+extern "C" int msmgb_param_adjoint(msmgb_ctx *c, int pot, const double *prm, const double *ft,
+                                   double *loss, double *grad)
+{
+    if (!c || !prm || !ft || !grad) return MSMGB_ERR_ARG;
+    if (pot != MSMGB_POT_CR) return set_err(c, MSMGB_ERR_ARG, "the adjoint supports the Cleri-Rosato parameters");
+    RET(ready_for_force(c));
+    if (c->tab.pottype != MSMGB_FS_TYPE || c->tab.nkind != 1 || c->tab.ngroup != 1)
+        return set_err(c, MSMGB_ERR_ARG, "the adjoint needs single-species FS tables");
+    const int n = c->n, ntab = c->tab.ntab;
+    const size_t ntp = (size_t)c->tab.ntp, N = (size_t)c->cap_atoms;
+    // parameter-derivative tables, padded like the force tables
+    std::vector<double> raw((size_t)15 * ntab), pad((size_t)15 * ntp, 0.0);
+    RET(msmgb_cr_param_tables(prm, c->tab_rmax, ntab, raw.data()));
+    for (int r = 0; r < 15; ++r) {
+        double *row = pad.data() + (size_t)r * ntp;
+        for (int i = 1; i <= ntab; ++i) row[i] = raw[(size_t)r * ntab + (i - 1)];
+        row[ntab + 1] = row[ntab];
+    }
+    const size_t need = pad.size() * sizeof(double) + 8 * sizeof(double);
+    if (c->adj_bytes < need) {
+        CK(cudaStreamSynchronize(c->stream), "synchronize");
+        if (c->adj_mem) cudaFree(c->adj_mem);
+        c->adj_mem = nullptr;
+        CK(cudaMalloc(&c->adj_mem, need), "adjoint alloc");
+        c->adj_bytes = need;
+    }
+    double *dtab = (double *)c->adj_mem;
+    double *acc = dtab + pad.size();
+    CK(cudaMemcpyAsync(dtab, pad.data(), pad.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream),
+       "adjoint upload");
+    char *s = (char *)c->scratch;
+    double *w4 = (double *)s;                  // 32 B per atom
+    double *dd = (double *)(s + 32 * N);       // 5 x 8 B
+    double *io = (double *)(s + 72 * N);       // 24 B: target forces, caller order
+    CK(cudaMemcpyAsync(io, ft, sizeof(double) * 3 * (size_t)n, cudaMemcpyHostToDevice, c->stream), "adjoint copy-in");
+    RET(launch_density(c, false));             // FP64 forces at the current parameters
+    RET(launch_force(c, false));
+    RET(launch_adjoint(c, io, dtab, w4, dd, acc));
+    double h[6];
+    CK(cudaMemcpyAsync(h, acc, sizeof(h), cudaMemcpyDeviceToHost, c->stream), "adjoint copy-out");
+    RET(poll_flags(c));
+    c->force_valid = true;
+    c->den_is32 = false;
+    for (int m = 0; m < 5; ++m) grad[m] = 2.0 * h[m];
+    if (loss) *loss = h[5];
+    return MSMGB_OK;
 }
 
 // ---- timing helpers (CUDA events on the context stream) -------------------------------------

@@ -151,6 +151,9 @@ struct msmgb_ctx {
     // tables
     msmgb::DevTables tab{};
     void *tab_mem = nullptr;
+    double tab_rmax = 0.0;
+    void *adj_mem = nullptr;           // parameter-derivative tables + accumulators
+    size_t adj_bytes = 0;
     bool have_tables = false;
     bool have_masses = false;
 
@@ -182,6 +185,8 @@ int launch_force(msmgb_ctx *c, bool want_virial);
 int launch_density32(msmgb_ctx *c);
 int launch_force32(msmgb_ctx *c);
 int launch_hvp(msmgb_ctx *c, const double *dv, double *dhv, double *v4buf, double *ddbuf);
+int launch_adjoint(msmgb_ctx *c, const double *ft, const double *dtab, double *w4buf, double *ddbuf,
+                   double *acc);
 
 // integrator (vv.cu)
 int launch_vv(msmgb_ctx *c, double h, int mode);   // mode 0: predictor; 1: fused; 2: fused if pending

@@ -149,3 +149,39 @@ extern "C" int msmgb_create_forcetable(int pot, const double *prm, double rmax, 
     }
     return MSMGB_OK;
 }
+
+// Derivatives of the Cleri-Rosato pair tables with respect to theta = (A, xi, p, q, r0), on the
+// same sqrt(r) grid, for the force-matching adjoint.  With a = r/r0 - 1, V = A exp(-p a),
+// rho = xi^2 exp(-2 q a):
+//   FPOTR = 2 V p r / r0:  d/dA = FPOTR/A,  d/dp = 2 r V (1 - p a)/r0,
+//                          d/dr0 = 2 p r V (p r/r0 - 1)/r0^2
+//   POTB  = rho:           d/dxi = 2 rho/xi, d/dq = -2 a rho, d/dr0 = 2 q r rho/r0^2
+//   FPOTB = 2 q rho/r0:    d/dxi = 2 FPOTB/xi, d/dq = 2 rho (1 - 2 q a)/r0,
+//                          d/dr0 = 2 q rho (2 q r/r0 - 1)/r0^2
+// Output layout: d[(m*3 + t)*ntab + (i-1)] for parameter m = 0..4 and table t = 0 (FPOTR),
+// 1 (POTB), 2 (FPOTB).
+extern "C" int msmgb_cr_param_tables(const double *prm, double rmax, int ntab, double *d)
+{
+    if (!prm || !d || ntab < 2 || rmax <= 0.0) return MSMGB_ERR_ARG;
+    const double A = prm[0], xi = prm[1], P = prm[2], Q = prm[3], r0 = prm[4];
+    const double csiv = 1.0 / ((double)ntab / std::sqrt(rmax));
+    for (int i = 1; i <= ntab; ++i) {
+        double t = (double)i * csiv;
+        double r = t * t;
+        double a = r / r0 - 1.0;
+        double V = A * std::exp(-P * a);
+        double rho = xi * xi * std::exp(-2.0 * Q * a);
+        double fpotr = 2.0 * V * P * r / r0;
+        double fpotb = 2.0 * Q * rho / r0;
+        double v[5][3] = {
+            {fpotr / A, 0.0, 0.0},
+            {0.0, 2.0 * rho / xi, 2.0 * fpotb / xi},
+            {2.0 * r * V * (1.0 - P * a) / r0, 0.0, 0.0},
+            {0.0, -2.0 * a * rho, 2.0 * rho * (1.0 - 2.0 * Q * a) / r0},
+            {2.0 * P * r * V * (P * r / r0 - 1.0) / (r0 * r0), 2.0 * Q * r * rho / (r0 * r0),
+             2.0 * Q * rho * (2.0 * Q * r / r0 - 1.0) / (r0 * r0)}};
+        for (int m = 0; m < 5; ++m)
+            for (int k = 0; k < 3; ++k) d[(size_t)(m * 3 + k) * ntab + (i - 1)] = v[m][k];
+    }
+    return MSMGB_OK;
+}

@@ -287,6 +287,16 @@ class Engine:
         return mk.value, mean.value
 
     # ---- differentiation ---------------------------------------------------------------------------
+    def param_adjoint(self, prm, ft, pot=L.POT_CR):
+        """Force-matching loss sum|F - Ft|^2 and its gradient with respect to the potential
+        parameters (Cleri-Rosato: A, xi, p, q, r0) of the loaded tables."""
+        prm = np.ascontiguousarray(prm, dtype=np.float64)
+        ft = np.ascontiguousarray(np.asarray(ft, np.float64).T).reshape(-1)
+        loss = C.c_double()
+        grad = np.zeros(5)
+        self._ck(self.lib.msmgb_param_adjoint(self.ctx, pot, _d(prm), _d(ft), C.byref(loss), _d(grad)))
+        return loss.value, grad
+
     def hvp(self, v):
         v = np.ascontiguousarray(np.asarray(v, np.float64).T).reshape(-1)
         out = np.zeros(3 * self.n)

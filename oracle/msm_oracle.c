@@ -19,6 +19,7 @@
  */
 #include "msm_oracle.h"
 
+#include <complex.h>
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
@@ -726,4 +727,117 @@ int orc_hvp(int n, const double *x, const double *y, const double *z, const int 
     free(dn);
     free(dd);
     return nbad;
+}
+
+/* ------------------------------------------------------------------------------------ */
+/* force-matching gradient (forward mode, independent of the device adjoint)            */
+/* ------------------------------------------------------------------------------------ */
+
+/* complex-step derivative of the Cleri-Rosato table columns: with theta_m -> theta_m + i h,
+ * Im(f)/h is the exact derivative to rounding. */
+int orc_cr_dtables(const double *prm, double rmax, int ntab, double *d)
+{
+    const double csiv = 1.0 / ((double)ntab / sqrt(rmax));
+    for (int m = 0; m < 5; ++m) {
+        double h = 1e-30 * fabs(prm[m]);
+        for (int i = 1; i <= ntab; ++i) {
+            double t = (double)i * csiv;
+            double r = t * t;
+            double complex q[5];
+            for (int k = 0; k < 5; ++k) q[k] = prm[k];
+            q[m] += I * h;
+            double complex A = q[0], xi = q[1], P = q[2], Q = q[3], r0 = q[4];
+            double complex v = A * cexp(-P * ((r / r0) - 1.0));
+            double complex fpotr = 2.0 * v * (P / r0) * r;
+            double complex rho = (xi * xi) * cexp(-(2.0 * Q) * ((r / r0) - 1.0));
+            double complex fpotb = rho * (Q / r0) * 2.0;
+            d[(size_t)(m * 3 + 0) * ntab + (i - 1)] = cimag(fpotr) / h;
+            d[(size_t)(m * 3 + 1) * ntab + (i - 1)] = cimag(rho) / h;
+            d[(size_t)(m * 3 + 2) * ntab + (i - 1)] = cimag(fpotb) / h;
+        }
+    }
+    return 0;
+}
+
+int orc_adjoint_cr(int n, const double *x, const double *y, const double *z, const int *ityp,
+                   const int *statu, const orc_box *box, const int *kvois, const int *indi,
+                   int ldi, const orc_tables *t, const double *dtab, const double *ftx,
+                   const double *fty, const double *ftz, double *loss, double *grad,
+                   int nthreads)
+{
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#else
+    (void)nthreads;
+#endif
+    size_t nn = (size_t)(n > 0 ? n : 1);
+    double *fx = (double *)malloc(sizeof(double) * nn), *fy = (double *)malloc(sizeof(double) * nn);
+    double *fz = (double *)malloc(sizeof(double) * nn), *dn = (double *)malloc(sizeof(double) * nn);
+    double *rho = (double *)calloc(nn, sizeof(double)), *drho = (double *)calloc(nn, sizeof(double));
+    orc_force(n, x, y, z, ityp, statu, box, kvois, indi, ldi, t, dn, fx, fy, fz, NULL, NULL, nthreads);
+    double l = 0.0;
+    for (int i = 0; i < n; ++i) {
+        double a = fx[i] - ftx[i], b = fy[i] - fty[i], c = fz[i] - ftz[i];
+        l += a * a + b * b + c * c;
+    }
+    *loss = l;
+    const double bx = box->len[0], by = box->len[1], bz = box->len[2];
+    const int px = box->ifpd[0], py = box->ifpd[1], pz = box->ifpd[2];
+    const int nt = t->ntab;
+    for (int m = 0; m < 5; ++m) {
+        const double *dP = dtab + (size_t)(m * 3 + 0) * nt;
+        const double *dQ = dtab + (size_t)(m * 3 + 1) * nt;
+        const double *dB = dtab + (size_t)(m * 3 + 2) * nt;
+        /* d rho_i / d theta_m and d F'_i / d theta_m */
+#pragma omp parallel for schedule(static)
+        for (int i = 0; i < n; ++i) {
+            double r0 = 0.0, d0 = 0.0;
+            if ((statu[i] & ORC_STATU_ACTIVE) == ORC_STATU_ACTIVE) {
+                for (int w = 0; w < kvois[i]; ++w) {
+                    int j = indi[(size_t)w * (size_t)ldi + (size_t)i];
+                    double sx = min_image(x[i] - x[j], bx, 0.5 * bx, px);
+                    double sy = min_image(y[i] - y[j], by, 0.5 * by, py);
+                    double sz = min_image(z[i] - z[j], bz, 0.5 * bz, pz);
+                    double r2 = sx * sx + sy * sy + sz * sz;
+                    if (r2 > t->ru2) continue;
+                    double sk = sqrt(sqrt(r2)) * t->csi;
+                    int kk = (int)sk;
+                    double dk = sk - kk;
+                    r0 += interp(t->potb, 1, nt, 0, kk, dk);
+                    d0 += interp(dQ, 1, nt, 0, kk, dk);
+                }
+            }
+            rho[i] = r0;
+            drho[i] = r0 > 0.0 ? 0.25 * d0 / (r0 * sqrt(r0)) : 0.0;   /* dD_i */
+        }
+        double g = 0.0;
+#pragma omp parallel for schedule(static) reduction(+ : g)
+        for (int i = 0; i < n; ++i) {
+            if ((statu[i] & ORC_STATU_ACTIVE) != ORC_STATU_ACTIVE) continue;
+            double gx = 0.0, gy = 0.0, gz = 0.0;
+            for (int w = 0; w < kvois[i]; ++w) {
+                int j = indi[(size_t)w * (size_t)ldi + (size_t)i];
+                double sx = min_image(x[i] - x[j], bx, 0.5 * bx, px);
+                double sy = min_image(y[i] - y[j], by, 0.5 * by, py);
+                double sz = min_image(z[i] - z[j], bz, 0.5 * bz, pz);
+                double r2 = sx * sx + sy * sy + sz * sz;
+                if (r2 > t->ru2) continue;
+                double r = sqrt(r2);
+                double sk = sqrt(r) * t->csi;
+                int kk = (int)sk;
+                double dk = sk - kk;
+                double B = interp(t->fpotb, 1, nt, 0, kk, dk);
+                double dft = interp(dP, 1, nt, 0, kk, dk) / r2 +
+                             (interp(dB, 1, nt, 0, kk, dk) * (dn[i] + dn[j]) +
+                              B * (drho[i] + drho[j])) / r;
+                gx += dft * sx;
+                gy += dft * sy;
+                gz += dft * sz;
+            }
+            g += (fx[i] - ftx[i]) * gx + (fy[i] - fty[i]) * gy + (fz[i] - ftz[i]) * gz;
+        }
+        grad[m] = 2.0 * g;
+    }
+    free(fx); free(fy); free(fz); free(dn); free(rho); free(drho);
+    return 0;
 }

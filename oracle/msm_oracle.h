@@ -120,6 +120,19 @@ int  orc_hvp(int n, const double *x, const double *y, const double *z, const int
              const orc_tables *t, const double *vx, const double *vy, const double *vz,
              double *hx, double *hy, double *hz, int nthreads);
 
+/* Cleri-Rosato parameter derivatives of FPOTR, POTB, FPOTB on the table grid, by complex-step
+ * differentiation of the potential functions: d[(m*3 + t)*ntab + i-1]. */
+int  orc_cr_dtables(const double *prm, double rmax, int ntab, double *d);
+
+/* Force-matching gradient by forward mode: for each parameter, dF/dtheta of every atom
+ * through the tables and the FS embedding, dotted with w = F - Ft (active atoms).
+ * dtab from orc_cr_dtables.  Returns L = sum |F - Ft|^2 and grad[5] = dL/dtheta. */
+int  orc_adjoint_cr(int n, const double *x, const double *y, const double *z, const int *ityp,
+                    const int *statu, const orc_box *box, const int *kvois, const int *indi,
+                    int ldi, const orc_tables *t, const double *dtab, const double *ftx,
+                    const double *fty, const double *ftz, double *loss, double *grad,
+                    int nthreads);
+
 #ifdef __cplusplus
 }
 #endif

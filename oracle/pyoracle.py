@@ -44,6 +44,7 @@ def lib():
         _lib.orc_force.restype = C.c_int
         _lib.orc_md.restype = C.c_int
         _lib.orc_hvp.restype = C.c_int
+        _lib.orc_adjoint_cr.restype = C.c_int
         _lib.orc_pot_eval.restype = C.c_int
         _lib.orc_embed_eval.restype = C.c_int
     return _lib
@@ -196,3 +197,24 @@ def md(pos, vel, ityp, statu, box, tables, cm, h, nsteps, rc_nl, skin_trigger=0.
     if rc < 0:
         raise RuntimeError("oracle md failed: %d" % rc)
     return (np.stack([x, y, z], 1), np.stack([vx, vy, vz], 1), np.stack([fx, fy, fz], 1), st, rc)
+
+
+def cr_dtables(prm, rmax, ntab=10000):
+    prm = f64(prm)
+    d = np.zeros(15 * ntab)
+    lib().orc_cr_dtables(_d(prm), C.c_double(rmax), ntab, _d(d))
+    return d
+
+
+def adjoint_cr(pos, ityp, statu, box, kvois, indi, tables, dtab, ft, nthreads=0):
+    n = pos.shape[0]
+    x, y, z = (f64(pos[:, k]) for k in range(3))
+    tx, ty_, tz = (f64(ft[:, k]) for k in range(3))
+    kv, ind = i32(kvois), i32(indi)
+    loss = C.c_double()
+    grad = np.zeros(5)
+    d = f64(dtab)
+    lib().orc_adjoint_cr(n, _d(x), _d(y), _d(z), _i(i32(ityp)), _i(i32(statu)), C.byref(box),
+                         _i(kv), _i(ind), ind.shape[1] if ind.ndim == 2 else n, C.byref(tables.s),
+                         _d(d), _d(tx), _d(ty_), _d(tz), C.byref(loss), _d(grad), nthreads)
+    return loss.value, grad

@@ -374,3 +374,53 @@ def test_mixed_batched_boxes(oracle):
         assert nrm < 1e-6 and mx < 1e-6
         off += len(p)
     e.close()
+
+
+# ---- parameter adjoint ------------------------------------------------------------------
+
+def test_param_adjoint_parity_and_fd(oracle):
+    """Force-matching gradient w.r.t. (A, xi, p, q, r0): device adjoint vs the oracle's
+    forward-mode gradient (1e-10) and vs central FD of the device FP64 loss (step 1e-6)."""
+    boxes = [lt.cu_config(6, 0.1, 300.0, s) for s in (41, 42, 43)]
+    pos = np.vstack([b[0] for b in boxes])
+    desc = [(len(b[0]), (0, 0, 0), tuple(b[2]), (1, 1, 1)) for b in boxes]
+    prm = np.array([lt.CU_CR[k] for k in ("A", "xi", "p", "q", "r0")])
+    e = Engine(len(pos), lt.CU_RC_NL, max_boxes=len(boxes), mxkvois=64)
+    e.init_forcetable(ForceTable(L.POT_CR, prm * 1.02, lt.CU_RC, lt.CU_RC, L.FS_TYPE))
+    e.copyin(desc, pos)
+    e.calforce()
+    ft = e.get_force()
+    e.init_forcetable(ForceTable(L.POT_CR, prm, lt.CU_RC, lt.CU_RC, L.FS_TYPE))
+    loss, grad = e.param_adjoint(prm, ft)
+    # oracle, box by box
+    og = np.zeros(5)
+    ol = 0.0
+    off = 0
+    t = oracle.Tables(oracle.make_tables(oracle.POT_CR, prm, lt.CU_RC, 10000, 10000, 20.0,
+                                         want_embed=False), oracle.FS, lt.CU_RC)
+    d = oracle.cr_dtables(prm, lt.CU_RC)
+    for p, _, L_ in boxes:
+        n = len(p)
+        box = oracle.make_box([0, 0, 0], L_)
+        st = np.ones(n, np.int32)
+        kv, ind = oracle.nlist(p, st, box, lt.CU_RC_NL, 96)
+        l, g = oracle.adjoint_cr(p, st, st, box, kv, ind, t, d, ft[off:off + n])
+        ol += l
+        og += g
+        off += n
+    assert loss == pytest.approx(ol, rel=1e-10)
+    assert rel_err(grad, og) < 1e-10
+
+    def dev_loss(q):
+        e.init_forcetable(ForceTable(L.POT_CR, q, lt.CU_RC, lt.CU_RC, L.FS_TYPE))
+        e.calforce()
+        return float(((e.get_force() - ft) ** 2).sum())
+
+    for m in range(5):
+        h = 1e-6 * prm[m]
+        pp, pm = prm.copy(), prm.copy()
+        pp[m] += h
+        pm[m] -= h
+        fd = (dev_loss(pp) - dev_loss(pm)) / (2 * h)
+        assert grad[m] == pytest.approx(fd, rel=1e-6), (m, grad[m], fd)
+    e.close()

@@ -157,3 +157,38 @@ def test_md_energy_conservation(oracle):
                                       skin_trigger=0.15, mxkvois=96)
     e1 = etot(p1, v1)
     assert abs(e1 - e0) / n < 2e-4
+
+
+def _loss(oracle, prm, pos, box, kv, ind, ft, rc=lt.CU_RC):
+    tabs = oracle.make_tables(oracle.POT_CR, prm, rc, 10000, 10000, 20.0, want_embed=False)
+    t = oracle.Tables(tabs, oracle.FS, rc)
+    n = len(pos)
+    f = oracle.force(pos, np.ones(n, np.int32), np.ones(n, np.int32), box, kv, ind, t,
+                     want_virial=False, want_epot=False)["f"]
+    return float(((f - ft) ** 2).sum())
+
+
+def test_force_matching_gradient_vs_central_fd(oracle):
+    """Oracle's forward-mode parameter gradient against central finite differences of the
+    loss (relative step 1e-6) with targets from parameters scaled by +2%."""
+    pos, _, L = lt.cu_config(5, 0.1, 300.0, 17)
+    n = len(pos)
+    box = oracle.make_box([0, 0, 0], L)
+    st = np.ones(n, np.int32)
+    kv, ind = oracle.nlist(pos, st, box, lt.CU_RC_NL, 96)
+    prm = np.array(CR_PRM)
+    tt = oracle.Tables(oracle.make_tables(oracle.POT_CR, prm * 1.02, lt.CU_RC, 10000, 10000, 20.0,
+                                          want_embed=False), oracle.FS, lt.CU_RC)
+    ft = oracle.force(pos, st, st, box, kv, ind, tt)["f"]
+    t = oracle.Tables(oracle.make_tables(oracle.POT_CR, prm, lt.CU_RC, 10000, 10000, 20.0,
+                                         want_embed=False), oracle.FS, lt.CU_RC)
+    d = oracle.cr_dtables(prm, lt.CU_RC)
+    loss, grad = oracle.adjoint_cr(pos, st, st, box, kv, ind, t, d, ft)
+    assert loss == pytest.approx(_loss(oracle, prm, pos, box, kv, ind, ft), rel=1e-14)
+    for m in range(5):
+        h = 1e-6 * prm[m]
+        pp, pm = prm.copy(), prm.copy()
+        pp[m] += h
+        pm[m] -= h
+        fd = (_loss(oracle, pp, pos, box, kv, ind, ft) - _loss(oracle, pm, pos, box, kv, ind, ft)) / (2 * h)
+        assert grad[m] == pytest.approx(fd, rel=1e-6), m
