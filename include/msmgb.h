@@ -206,6 +206,46 @@ int  msmgb_param_adjoint(msmgb_ctx *ctx, int pot, const double *prm, const doubl
  * 1 POTB, 2 FPOTB.  Host only. */
 int  msmgb_cr_param_tables(const double *prm, double rmax, int ntab, double *d);
 
+/* ---- force call without device allocation ------------------------------------------------ */
+/* No counterpart in the reference.  For callers that cannot let this library call cudaMalloc:
+ * a host code whose device arrays are already owned by its own runtime (such as msmpscu's
+ * CUDA Fortran work arrays), a code held to a fixed device-memory budget by its own
+ * allocator, or one that must not let cudaMalloc's implicit device synchronisation stall its
+ * other streams mid-step.  The caller passes device pointers to all inputs and the output;
+ * the only extra memory, F'(rho) of every atom between the two passes plus one error word,
+ * sits in a fixed array compiled into the library (8 MiB per GPU, held until exit), so at
+ * most MSMGB_NOALLOC_MAX_ATOMS atoms can be handled (larger n returns MSMGB_ERR_CAPACITY).
+ * The first call on a device, made with that device current, looks up the device address of
+ * that array; make this first call before any stream capture.  All calls on a device share
+ * the array and it keeps the last call's contents (the error word is cleared at the start of
+ * every call); calls whose work overlaps on the GPU race on it, so serialise them.
+ * FP64, single species (tables of kind 1), orthorhombic box; the call synchronises `stream`.
+ * Results equal msmgb_calforce's to rounding. */
+#define MSMGB_NOALLOC_MAX_ATOMS 1048576
+typedef struct {
+    int           n;          /* atoms (<= MSMGB_NOALLOC_MAX_ATOMS)                          */
+    const double *xp;         /* device: XP(N,3) column-major positions                     */
+    const int    *statu;      /* device: STATU(N)                                            */
+    const int    *kvois;      /* device: KVOIS(N)                                            */
+    const int    *indi;       /* device: INDI(ld, *) column-major, 0-based neighbour ids    */
+    int           ld;         /* leading dimension of indi (>= n)                           */
+    double        box_len[3]; /* box edges                                                  */
+    int           ifpd[3];    /* periodic flags                                             */
+    int           pottype;    /* MSMGB_FS_TYPE or MSMGB_EAM_TYPE                            */
+    int           ntab;       /* pair table points                                          */
+    double        rmax;       /* table Rmax                                                 */
+    double        ru;         /* force cutoff                                               */
+    const double *potb, *fpotr, *fpotb;   /* device: NTAB entries each (reference layout)   */
+    int           nembd;      /* EAM: F'(rho) table points                                  */
+    double        rhod;       /* EAM: F'(rho) table spacing                                 */
+    const double *dfembd;     /* EAM, device: NEMBD entries                                 */
+    double       *fp;         /* device output: FP(N,3) column-major forces                 */
+    void         *stream;     /* cudaStream_t (NULL: legacy default stream)                 */
+    char         *errbuf;     /* optional host buffer for an error message                  */
+    int           errlen;
+} msmgb_force_noalloc;
+int  msmgb_calforce_noalloc(const msmgb_force_noalloc *args);
+
 /* ---- host-side table generator (Create_Interaction_ForceTable,
  *      MD_TypeDef_ForceTable.F90:890-1056) -------------------------------------------------- */
 #define MSMGB_POT_CR          1   /* Cleri-Rosato TB-SMA, FS form; prm = A, xi, p, q, r0     */

@@ -41,6 +41,19 @@ class Box(C.Structure):
                 ("ifpd", C.c_int * 3)]
 
 
+NOALLOC_MAX_ATOMS = 1048576
+
+
+class ForceNoAlloc(C.Structure):
+    _fields_ = [("n", C.c_int), ("xp", C.c_void_p), ("statu", C.c_void_p), ("kvois", C.c_void_p),
+                ("indi", C.c_void_p), ("ld", C.c_int), ("box_len", C.c_double * 3),
+                ("ifpd", C.c_int * 3), ("pottype", C.c_int), ("ntab", C.c_int),
+                ("rmax", C.c_double), ("ru", C.c_double), ("potb", C.c_void_p),
+                ("fpotr", C.c_void_p), ("fpotb", C.c_void_p), ("nembd", C.c_int),
+                ("rhod", C.c_double), ("dfembd", C.c_void_p), ("fp", C.c_void_p),
+                ("stream", C.c_void_p), ("errbuf", C.c_char_p), ("errlen", C.c_int)]
+
+
 # (name, restype, argtypes) of every exported entry point
 SIGNATURES = [
     ("msmgb_create", C.c_int, [C.POINTER(C.c_void_p), C.POINTER(Params)]),
@@ -76,6 +89,7 @@ SIGNATURES = [
     ("msmgb_hvp", C.c_int, [C.c_void_p, _dp, _dp]),
     ("msmgb_param_adjoint", C.c_int, [C.c_void_p, C.c_int, _dp, _dp, _dp, _dp]),
     ("msmgb_cr_param_tables", C.c_int, [_dp, C.c_double, C.c_int, _dp]),
+    ("msmgb_calforce_noalloc", C.c_int, [C.POINTER(ForceNoAlloc)]),
     ("msmgb_create_forcetable", C.c_int, [C.c_int, _dp, C.c_double, C.c_int, C.c_int, C.c_double,
                                           _dp, _dp, _dp, _dp, _dp, _dp, _dp]),
 ]
