@@ -42,6 +42,22 @@ def peaks():
         return 6800.0, "fallback"
 
 
+def reduce_max(value, dist=None):
+    """Max of a float over the ranks of the default process group (identity without one)."""
+    if dist is None or not dist.is_initialized():
+        return float(value)
+    import torch
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(value)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(atoms_per_rank, steps, ms_max, world):
+    """Whole-job atom-steps/s of `world` independent replicas timed by the slowest rank."""
+    return world * atoms_per_rank * steps / (ms_max / 1e3)
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -130,6 +146,105 @@ def precision_compare(e, box, pos, vel, steps):
     ms64, _ = e.time_steps(steps, DT)
     e.set_precision("mixed")
     return err_norm, err_max, len(pos) * steps / (ms64 / 1e3)
+
+
+def batched_c3(steps, steps_perbox, device=0):
+    """512 independent periodic Cu boxes, edge uniform in 4..12 fcc cells, 0-3 vacancies,
+    300-1200 K: all boxes in one context (one launch per pass over every box, the whole step
+    one CUDA graph) against one context per box (512 graphs per step, each on its own
+    stream so they may overlap).  Metric: box-steps per second."""
+    from msmpscu_gb300 import Engine, ForceTable, lattice as lt
+    boxes = lt.uneven_batch(512, seed=512)
+    pos = np.vstack([b[0] for b in boxes])
+    vel = np.vstack([b[1] for b in boxes])
+    desc = [(len(b[0]), (0, 0, 0), tuple(b[2]), (1, 1, 1)) for b in boxes]
+    table = ForceTable.cleri_rosato(**lt.CU_CR, rc=lt.CU_RC)
+    out = {"boxes": len(boxes), "atoms": int(len(pos)),
+           "box_atoms_min": int(min(len(b[0]) for b in boxes)),
+           "box_atoms_max": int(max(len(b[0]) for b in boxes))}
+    for prec in ("mixed", "fp64"):
+        e = Engine(len(pos), lt.CU_RC_NL, max_boxes=len(boxes), mxkvois=MXKVOIS, skin_trigger=0.15,
+                   precision=prec, device=device)
+        e.init_forcetable(table)
+        e.set_masses([lt.CU_MASS])
+        e.copyin(desc, pos, vel)
+        e.run_steps(3, DT)
+        ms, reb = e.time_steps(steps, DT)
+        out["batched_%s_box_steps_per_s" % prec] = len(boxes) * steps / (ms / 1e3)
+        out["batched_%s_atom_steps_per_s" % prec] = len(pos) * steps / (ms / 1e3)
+        out["batched_%s_ms_per_step" % prec] = ms / steps
+        out["batched_%s_launches_per_step" % prec] = None
+        e.close()
+    engines = []
+    for (p, v, L), d in zip(boxes, desc):
+        e = Engine(len(p), lt.CU_RC_NL, max_boxes=1, mxkvois=MXKVOIS, skin_trigger=0.15,
+                   precision="mixed", device=device)
+        e.init_forcetable(table)
+        e.set_masses([lt.CU_MASS])
+        e.copyin([d], p, v)
+        e.run_steps(2, DT)
+        engines.append(e)
+    for e in engines:
+        e.synchronize()
+    t0 = time.perf_counter()
+    for e in engines:
+        e.enqueue_steps(steps_perbox, DT)
+    for e in engines:
+        e.finish_steps(DT)
+    t1 = time.perf_counter()
+    for e in engines:
+        e.close()
+    out["perbox_mixed_box_steps_per_s"] = len(boxes) * steps_perbox / (t1 - t0)
+    out["batched_vs_perbox"] = out["batched_mixed_box_steps_per_s"] / out["perbox_mixed_box_steps_per_s"]
+    out["perbox_timing"] = "host wall clock around %d steps of 512 contexts (device synchronised both sides)" % steps_perbox
+    return out
+
+
+def hvp_c4(device=0):
+    """bcc W 20^3 cells + <111> dumbbell (16,001 atoms), Marinica EAM2: device time of one
+    HVP against one FP64 force call on the same state."""
+    from msmpscu_gb300 import Engine, ForceTable, lattice as lt
+    pos, L = lt.w_sia_config(20, 0.0, 1)
+    e = Engine(len(pos), lt.W_RC_NL, mxkvois=96, device=device)
+    e.init_forcetable(ForceTable.marinica_eam2())
+    e.copyin([(len(pos), (0, 0, 0), tuple(L), (1, 1, 1))], pos)
+    v = np.random.default_rng(0).normal(size=pos.shape)
+    v /= np.linalg.norm(v)
+    ms_hvp, ms_force = e.time_hvp(v, reps=20)
+    e.close()
+    return {"atoms": len(pos), "hvp_ms": ms_hvp, "force_call_ms": ms_force,
+            "hvp_cost_force_calls": ms_hvp / ms_force}
+
+
+def adjoint_c5(device=0):
+    """64 fcc Cu snapshots of 4,000 atoms (sigma 0.1 A), targets from parameters x 1.02:
+    wall time of one adjoint call (FP64 forces + adjoint passes + host derivative tables)
+    against one FP64 force call with copy-out."""
+    from msmpscu_gb300 import Engine, ForceTable, lattice as lt
+    from msmpscu_gb300 import _lib as L
+    snaps = [lt.cu_config(10, 0.1, 300.0, 1000 + s) for s in range(64)]
+    pos = np.vstack([s[0] for s in snaps])
+    desc = [(len(s[0]), (0, 0, 0), tuple(s[2]), (1, 1, 1)) for s in snaps]
+    prm = np.array([lt.CU_CR[k] for k in ("A", "xi", "p", "q", "r0")])
+    e = Engine(len(pos), lt.CU_RC_NL, max_boxes=64, mxkvois=MXKVOIS, device=device)
+    e.init_forcetable(ForceTable(L.POT_CR, prm * 1.02, lt.CU_RC, lt.CU_RC, L.FS_TYPE))
+    e.copyin(desc, pos)
+    e.calforce()
+    ft = e.get_force()
+    e.init_forcetable(ForceTable(L.POT_CR, prm, lt.CU_RC, lt.CU_RC, L.FS_TYPE))
+    e.param_adjoint(prm, ft)
+    t0 = time.perf_counter()
+    for _ in range(5):
+        loss, grad = e.param_adjoint(prm, ft)
+    t1 = time.perf_counter()
+    for _ in range(5):
+        e.calforce()
+        e.get_force()
+    t2 = time.perf_counter()
+    e.close()
+    return {"atoms": len(pos), "adjoint_ms": (t1 - t0) / 5 * 1e3, "force_call_ms": (t2 - t1) / 5 * 1e3,
+            "adjoint_cost_force_calls": (t1 - t0) / (t2 - t1), "loss": loss,
+            "grad": [float(g) for g in grad]}
 
 
 def make_engine(n, precision, device=0):
@@ -251,14 +366,11 @@ def run_ours(args):
     with Clocks(device) as clk:
         ms, rebuilds = e.time_steps(args.steps, DT)
     launches = e.launches - l0
-    if dist:
-        import torch
-        tt = torch.tensor([ms], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        ms = float(tt.item())
-    value = ws * n * args.steps / (ms / 1e3)
+    ms = reduce_max(ms, dist)
+    value = replica_value(n, args.steps, ms, ws)
     kmax, kmean = e.list_stats()
     passes = e.time_passes(5)
+    tune = e.tuning() if prec == "mixed" else None
     bm = bytes_model(kmean)
     hbm, peak_kind = peaks()
     dom = "force" if passes["force"] >= passes["density"] else "density"
@@ -290,6 +402,14 @@ def run_ours(args):
         cmp = {"fp64_value": v64, "mixed_value": value / ws, "speedup": value / ws / v64,
                "mixed_force_err_norm": en, "mixed_force_err_max": em}
 
+    extras = {}
+    if not args.no_extras:
+        e.close()
+        extras["batched_c3"] = batched_c3(max(10, min(args.steps, 100)), 20, device)
+        extras["hvp_c4"] = hvp_c4(device)
+        extras["adjoint_c5"] = adjoint_c5(device)
+        e = None
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         threads = os.cpu_count() or 1
@@ -317,13 +437,16 @@ def run_ours(args):
                                   "frac": bm["step"] * value / ws / 1e9 / hbm,
                                   "bytes_per_atom_step": bm["step"]},
                 "pass_ms": passes,
+                "autotune": tune,
                 "precision_compare": cmp,
                 "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
                 "cpu_baseline": cpu,
+                **extras,
                 "clocks": clk.summary(),
                 "gpu_launches": launches}
         print(json.dumps(line), flush=True)
-    e.close()
+    if e is not None:
+        e.close()
     if dist:
         dist.destroy_process_group()
 
@@ -364,6 +487,8 @@ def main():
     ap.add_argument("--ncell", type=int, default=NCELL,
                     help="fcc cells per edge (80 = the benchmark; smaller for profiling captures)")
     ap.add_argument("--no-compare", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the batched-box, HVP and adjoint measurements")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--ref-budget-s", type=float, default=150.0)

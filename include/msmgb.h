@@ -185,10 +185,18 @@ int  msmgb_time_steps(msmgb_ctx *ctx, int nsteps, double h, float *ms, int *rebu
  * out[0] density pass, out[1] force pass, out[2] list rebuild, out[3] fused integrator
  * (timed with h = 0, which leaves the state unchanged).  No counterpart in the reference. */
 int  msmgb_time_passes(msmgb_ctx *ctx, int reps, float *out);
+/* Variants picked by the autotuner for the mixed passes: out[0] neighbours in flight per
+ * thread in the density pass, out[1] in the force pass; ms (may be NULL) their time per
+ * launch.  Tuning runs at the first mixed force call for a given atom count. */
+int  msmgb_get_tuning(const msmgb_ctx *ctx, int *out, float *ms);
 /* Largest and mean neighbour count of the current list. */
 int  msmgb_list_stats(msmgb_ctx *ctx, int *maxk, double *meank);
 
 /* ---- differentiation --------------------------------------------------------------------- */
+/* Device time of one Hessian-vector product and of one FP64 force call (density + force
+ * pass) on the current state, averaged over reps launches (CUDA events on the context
+ * stream).  v: 3*N probe, XP layout, caller order.  No counterpart in the reference. */
+int  msmgb_time_hvp(msmgb_ctx *ctx, const double *v, int reps, float *ms_hvp, float *ms_force);
 /* Hessian-vector product of the table-mode force (exact derivative of the interpolants):
  * hv = -dF/dx . v.  v and hv are 3*N arrays in XP layout, caller's order.  No counterpart in
  * the reference: it replaces finite-difference force pairs (MD_Method_ART_GPU.F90:454-576). */

@@ -86,7 +86,9 @@ SIGNATURES = [
     ("msmgb_time_steps", C.c_int, [C.c_void_p, C.c_int, C.c_double, C.POINTER(C.c_float), _ip]),
     ("msmgb_time_passes", C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_float)]),
     ("msmgb_list_stats", C.c_int, [C.c_void_p, _ip, _dp]),
+    ("msmgb_get_tuning", C.c_int, [C.c_void_p, _ip, C.POINTER(C.c_float)]),
     ("msmgb_hvp", C.c_int, [C.c_void_p, _dp, _dp]),
+    ("msmgb_time_hvp", C.c_int, [C.c_void_p, _dp, C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
     ("msmgb_param_adjoint", C.c_int, [C.c_void_p, C.c_int, _dp, _dp, _dp, _dp]),
     ("msmgb_cr_param_tables", C.c_int, [_dp, C.c_double, C.c_int, _dp]),
     ("msmgb_calforce_noalloc", C.c_int, [C.POINTER(ForceNoAlloc)]),

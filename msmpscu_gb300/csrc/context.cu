@@ -82,8 +82,9 @@ __global__ void k_pack(DevAtoms a, const double *xp, const double *xp1, const in
     if (i >= n) return;
     double x = xp[i], y = xp[n + i], z = xp[2 * n + i];
     a.pos[i] = make_double4_32a(x, y, z, 0.0);
-    a.pos_bld[i] = make_double4_32a(x, y, z, 0.0);
-    a.posff[i] = make_posff(x, y, z, a.box[boxid[i]]);
+    PosFF f = make_posff(x, y, z, a.box[boxid[i]]);
+    a.posff[i] = f;
+    a.pos_bld[i] = make_float4(f.hx, f.hy, f.hz, 0.0f);
     a.vx[i] = xp1 ? xp1[i] : 0.0;
     a.vy[i] = xp1 ? xp1[n + i] : 0.0;
     a.vz[i] = xp1 ? xp1[2 * n + i] : 0.0;
@@ -181,6 +182,7 @@ extern "C" int msmgb_create(msmgb_ctx **out, const msmgb_params *p)
     AL(c->cell_of, N) AL(c->perm, N)
     AL(c->dbox, (size_t)c->cap_boxes)
     AL(c->cm, (size_t)kMaxGroups)
+    AL(c->icm, (size_t)kMaxGroups)
     AL(c->flags, (size_t)kFlagWords)
     AL(c->maxdisp, 1)
     AL(c->virial, 6 * (size_t)c->cap_boxes)
@@ -191,11 +193,14 @@ extern "C" int msmgb_create(msmgb_ctx **out, const msmgb_params *p)
     if ((e = cudaMallocHost((void **)&c->h_virial, sizeof(double) * 6 * c->cap_boxes)) != cudaSuccess) return fail(e, "pinned");
     if ((e = cudaMemsetAsync(c->flags, 0, sizeof(int) * kFlagWords, c->stream)) != cudaSuccess) return fail(e, "memset");
     if ((e = cudaMemsetAsync(c->maxdisp, 0, sizeof(unsigned long long), c->stream)) != cudaSuccess) return fail(e, "memset");
+    if (p->precision == MSMGB_PREC_MIXED && (e = dalloc(&a.pk, N * (size_t)p->mxkvois)) != cudaSuccess)
+        return fail(e, "cudaMalloc pair index");
     a.flags = c->flags;
     a.maxdisp = c->maxdisp;
     a.virial = c->virial;
     a.box = c->dbox;
     a.cm = c->cm;
+    a.icm = c->icm;
     a.n = 0;
     *out = c;
     return MSMGB_OK;
@@ -210,7 +215,7 @@ extern "C" int msmgb_destroy(msmgb_ctx *c)
     DevAtoms &a = c->a;
     void *ptrs[] = {a.pos, a.posff, a.pos_bld, a.vx, a.vy, a.vz, a.fx, a.fy, a.fz,
                     a.dx, a.dy, a.dz, a.ityp, a.statu, a.gid, a.boxid, a.den, a.epot,
-                    a.den32, a.kvois, a.indi, c->cell_of, c->perm, c->dbox, c->cm,
+                    a.den32, a.kvois, a.indi, a.pk, c->cell_of, c->perm, c->dbox, c->cm, c->icm,
                     c->flags, c->maxdisp, c->virial, c->scratch, c->cell_start,
                     c->cell_cursor, c->scan_tmp, c->tab_mem, c->adj_mem};
     for (void *q : ptrs)
@@ -231,6 +236,11 @@ extern "C" int msmgb_set_precision(msmgb_ctx *c, int precision)
     if (!c) return MSMGB_ERR_ARG;
     if (precision != MSMGB_PREC_FP64 && precision != MSMGB_PREC_MIXED)
         return set_err(c, MSMGB_ERR_ARG, "precision must be MSMGB_PREC_FP64 or MSMGB_PREC_MIXED");
+    if (precision == MSMGB_PREC_MIXED && !c->a.pk) {
+        RET(use_device(c));
+        CK(cudaStreamSynchronize(c->stream), "synchronize");
+        CK(dalloc(&c->a.pk, (size_t)c->cap_atoms * (size_t)c->p.mxkvois), "cudaMalloc pair index");
+    }
     if (precision != c->p.precision) {
         c->p.precision = precision;
         c->force_valid = false;
@@ -430,6 +440,10 @@ extern "C" int msmgb_copyin_simbox(msmgb_ctx *c, int nbox, const msmgb_box *boxe
             int nc = (int)(d.len[k] / (1.0 * c->p.rc_nl) - 0.0001);   // MD_NeighborsList_GPU.F90:289-292
             d.nc[k] = nc < 3 ? 3 : nc;
         }
+        {   // |lo_i - lo_j| <= ulp(2L) (u in [L, 2L]) and |L - float(L)| <= ulp(L)/2
+            double ext = 2.0 * std::max(d.len[0], std::max(d.len[1], d.len[2]));
+            d.dlmax = (float)(2.0 * ldexp(1.0, ilogb(ext) - 23));
+        }
         long nb = (long)d.nc[0] * d.nc[1] * d.nc[2];
         if ((long)cells + nb > (1L << 24) - 2) return set_err(c, MSMGB_ERR_CAPACITY, "too many cells");
         d.cell0 = cells;
@@ -489,6 +503,9 @@ extern "C" int msmgb_set_masses(msmgb_ctx *c, int ngroup, const double *cm)
         if (!(cm[i] > 0.0)) return set_err(c, MSMGB_ERR_ARG, "masses must be positive");
     RET(use_device(c));
     CK(cudaMemcpy(c->cm, cm, sizeof(double) * (size_t)ngroup, cudaMemcpyHostToDevice), "mass upload");
+    double inv[kMaxGroups];
+    for (int i = 0; i < ngroup; ++i) inv[i] = 1.0 / cm[i];
+    CK(cudaMemcpy(c->icm, inv, sizeof(double) * (size_t)ngroup, cudaMemcpyHostToDevice), "mass upload");
     c->have_masses = true;
     return MSMGB_OK;
 }
@@ -647,6 +664,11 @@ static int ready_for_force(msmgb_ctx *c)
 static int force_passes(msmgb_ctx *c, bool virial, bool epot)
 {
     if (c->p.precision == MSMGB_PREC_MIXED && !virial && !epot) {
+        if (c->tuned_n != c->n) {
+            cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+            cudaStreamIsCapturing(c->stream, &cs);
+            if (cs == cudaStreamCaptureStatusNone) RET(autotune_mixed(c));
+        }
         RET(launch_density32(c));
         RET(launch_force32(c));
     } else {
@@ -745,6 +767,7 @@ static int capture_step(msmgb_ctx *c, double h)
     c->graph_h = h;
     c->graph_prec = c->p.precision;
     c->graph_n = c->n;
+    c->graph_tune = c->tune_dens_unroll * 16 + c->tune_force_unroll;
     return MSMGB_OK;
 }
 
@@ -758,7 +781,8 @@ extern "C" int msmgb_run_steps(msmgb_ctx *c, int nsteps, double h, int *rebuilds
         c->force_valid = true;
     }
     CK(cudaMemsetAsync(c->flags + kFlagRebuilds, 0, sizeof(int) * 3, c->stream), "flag clear");  // rebuilds, pending, step
-    if (!c->step_graph || c->graph_h != h || c->graph_prec != c->p.precision || c->graph_n != c->n)
+    if (!c->step_graph || c->graph_h != h || c->graph_prec != c->p.precision || c->graph_n != c->n ||
+        c->graph_tune != c->tune_dens_unroll * 16 + c->tune_force_unroll)
         RET(capture_step(c, h));
     for (int s = 0; s < nsteps; ++s) {
         CK(cudaGraphLaunch(c->step_graph, c->stream), "graph launch");
@@ -780,7 +804,8 @@ extern "C" int msmgb_enqueue_steps(msmgb_ctx *c, int nsteps, double h)
         RET(force_passes(c, false, false));
         c->force_valid = true;
     }
-    if (!c->step_graph || c->graph_h != h || c->graph_prec != c->p.precision || c->graph_n != c->n)
+    if (!c->step_graph || c->graph_h != h || c->graph_prec != c->p.precision || c->graph_n != c->n ||
+        c->graph_tune != c->tune_dens_unroll * 16 + c->tune_force_unroll)
         RET(capture_step(c, h));
     for (int s = 0; s < nsteps; ++s) {
         CK(cudaGraphLaunch(c->step_graph, c->stream), "graph launch");
@@ -945,5 +970,51 @@ extern "C" int msmgb_list_stats(msmgb_ctx *c, int *maxk, double *meank)
     for (int k : kv) { s += k; m = std::max(m, k); }
     if (maxk) *maxk = m;
     if (meank) *meank = (double)s / (double)c->n;
+    return MSMGB_OK;
+}
+
+// Device time of one Hessian-vector product (gather of v + the two HVP passes) and of one
+// FP64 force call (density + force pass) on the current state, averaged over `reps`
+// launches after a warm-up; v (caller order, XP layout) is uploaded once before timing.
+extern "C" int msmgb_time_hvp(msmgb_ctx *c, const double *v, int reps, float *ms_hvp, float *ms_force)
+{
+    if (!c || !v || !ms_hvp || !ms_force || reps < 1) return MSMGB_ERR_ARG;
+    RET(ready_for_force(c));
+    const int n = c->n;
+    const size_t N = (size_t)c->cap_atoms;
+    char *s = (char *)c->scratch;
+    double *v4 = (double *)s, *dd = (double *)(s + 32 * N), *hvs = (double *)(s + 40 * N);
+    double *io = (double *)(s + 64 * N);
+    CK(cudaMemcpyAsync(io, v, sizeof(double) * 3 * (size_t)n, cudaMemcpyHostToDevice, c->stream), "hvp copy-in");
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0), "event");
+    CK(cudaEventCreate(&e1), "event");
+    float t[2] = {0.f, 0.f};
+    for (int which = 0; which < 2; ++which) {
+        for (int r = 0; r < reps + 1; ++r) {
+            if (r == 1) CK(cudaEventRecord(e0, c->stream), "event");
+            if (which == 0) RET(launch_hvp(c, io, hvs, v4, dd));
+            else { RET(launch_density(c, false)); RET(launch_force(c, false)); }
+        }
+        CK(cudaEventRecord(e1, c->stream), "event");
+        CK(cudaEventSynchronize(e1), "event");
+        CK(cudaEventElapsedTime(&t[which], e0, e1), "event");
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *ms_hvp = t[0] / reps;
+    *ms_force = t[1] / reps;
+    c->force_valid = true;
+    return poll_flags(c);
+}
+
+// Launch variants chosen by the autotuner: out[0] density unroll, out[1] force unroll;
+// ms[0], ms[1]: their measured time per launch (0 before tuning).
+extern "C" int msmgb_get_tuning(const msmgb_ctx *c, int *out, float *ms)
+{
+    if (!c || !out) return MSMGB_ERR_ARG;
+    out[0] = c->tune_dens_unroll;
+    out[1] = c->tune_force_unroll;
+    if (ms) { ms[0] = c->tune_ms[0]; ms[1] = c->tune_ms[1]; }
     return MSMGB_OK;
 }

@@ -5,173 +5,262 @@
 // The reference's tables are linear in sqrt(r) with a step of ~7e-4 A near the first
 // neighbour shell, and the Cleri-Rosato exponentials change by ~11x the relative change of r,
 // so an index SK = CSI sqrt(r) taken from FP32 r^2 alone would carry ~1e-6 relative error
-// into every pair term.  The index is therefore computed from a float-float separation:
+// into every pair term.  The index is therefore computed from an exact separation:
 //   * positions are kept as float-float in the shifted frame u = x - lo + L in [L, 2L], so
-//     hi_i - hi_j is exact (Sterbenz) and so is the image shift by float(L);
-//   * r^2 is formed in float-float (exact squares through fma), the cutoff test compares
-//     float-float r^2 with float-float RU^2 (the FP64 rule, up to ~1e-13 relative);
+//     dh = hi_i - hi_j is exact (Sterbenz) and so is the image shift by float(L); the rest
+//     dl = lo_i - lo_j (+ the low part of L) is below 1e-4 A;
+//   * r^2 = sum dh^2 + 2 dh dl is formed in float-float (exact squares through fma, exact
+//     sums through two-sum); the cutoff test compares it with float-float RU^2, i.e. the
+//     FP64 rule up to ~1e-13 relative;
 //   * SK = CSI r2^(1/4): two MUFU reciprocal square roots and one Newton correction
-//     evaluated in float-float, giving DK to ~1e-7.
+//     evaluated in float-float give DK to ~1e-7.
+// The density pass stores the table index of every pair it accepts (KK << 18 | DK * 2^18,
+// DK quantised to 4e-6, i.e. a table-value error below 1e-8) in the ELL layout of the
+// list; the force pass reads it back instead of recomputing the separation in float-float
+// and only forms the FP32 separation for the force direction and 1/R.
 // Table values come from interleaved {value, slope} FP32 rows (one 8 B or 16 B load per
-// pair), accumulation of rho and F is FP32 (measured error ~3e-7 of the FP64 result);
-// positions, the integrator and the list stay FP64.
+// pair); rho and F accumulate in FP32 (measured error ~3e-7 of the FP64 forces).
+// Positions, the integrator and the list stay FP64.
+#include <algorithm>
+
 #include "msmgb_internal.cuh"
 
 namespace msmgb {
 
-struct FF {
-    float h, l;
+constexpr unsigned kSkip = 0xffffffffu;     // pair beyond RU
+constexpr int kDkBits = 18;
+constexpr float kDkScale = 262144.0f;       // 2^18
+constexpr float kDkInv = 1.0f / 262144.0f;
+
+struct BoxF {
+    float lh[3], ll[3], half[3];
+    int pd[3];
+    float dlmax;          // bound on |dl| per component
 };
 
-// exact separation component (hi part exact, lo carries the rest)
-__device__ __forceinline__ FF sep_ff(float hi_i, float lo_i, float hi_j, float lo_j, float lh,
-                                     float ll, float half, int pd)
+__device__ __forceinline__ BoxF load_boxf(const DevBox &b)
 {
-    float dh = hi_i - hi_j;             // exact: both in [L, 2L]
-    float dl = lo_i - lo_j;
-    if (pd && fabsf(dh) > half) {
-        float s = copysignf(1.0f, dh);
-        dh = dh - s * lh;               // exact (Sterbenz)
-        dl = dl - s * ll;
+    BoxF o;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        o.lh[k] = b.lenf[k];
+        o.ll[k] = b.lenlo[k];
+        o.half[k] = b.halff[k];
+        o.pd[k] = b.ifpd[k];
     }
-    FF r;
-    r.h = dh + dl;                      // Fast2Sum: |dh| >= |dl| for all non-coincident atoms
-    r.l = dl - (r.h - dh);
-    return r;
+    o.dlmax = b.dlmax;
+    return o;
+}
+
+// exact high part and small low part of one separation component (minimum image)
+__device__ __forceinline__ void sep2(float hi, float lo, float hj, float lj, float lh, float ll,
+                                     float half, int pd, float &dh, float &dl)
+{
+    dh = hi - hj;                        // exact: both in [L, 2L]
+    dl = lo - lj;
+    if (pd && fabsf(dh) > half) {
+        const float s = copysignf(1.0f, dh);
+        dh = fmaf(-s, lh, dh);           // exact (Sterbenz)
+        dl = fmaf(-s, ll, dl);
+    }
 }
 
 __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e)
 {
     s = a + b;
-    float bb = s - a;
+    const float bb = s - a;
     e = (a - (s - bb)) + (b - bb);
 }
 
-struct PairGeom {
-    float sx, sy, sz;     // separation (hi parts)
-    float y;              // 1/R
-    int kk;               // table index
-    float dk;             // fraction in [0, 1)
-};
-
-// Returns false when the pair is beyond RU (float-float comparison of r^2 with RU^2).
-__device__ __forceinline__ bool pair_geom(const PosFF &pi, const PosFF &pj, const DevBox &b,
-                                          const DevTables &t, PairGeom &g)
+// Packed table index of a pair, or kSkip beyond RU.
+__device__ __forceinline__ unsigned pair_index(const PosFF &pi, const PosFF &pj, const BoxF &b,
+                                               const DevTables &t, float rej, float &dk_out, int &kk_out)
 {
-    FF x = sep_ff(pi.hx, pi.lx, pj.hx, pj.lx, b.lenf[0], b.lenlo[0], b.halff[0], b.ifpd[0]);
-    FF y = sep_ff(pi.hy, pi.ly, pj.hy, pj.ly, b.lenf[1], b.lenlo[1], b.halff[1], b.ifpd[1]);
-    FF z = sep_ff(pi.hz, pi.lz, pj.hz, pj.lz, b.lenf[2], b.lenlo[2], b.halff[2], b.ifpd[2]);
-    // float-float r^2
-    float px = x.h * x.h, py = y.h * y.h, pz = z.h * z.h;
-    float ex = fmaf(x.h, x.h, -px), ey = fmaf(y.h, y.h, -py), ez = fmaf(z.h, z.h, -pz);
+    float xh, xl, yh, yl, zh, zl;
+    sep2(pi.hx, pi.lx, pj.hx, pj.lx, b.lh[0], b.ll[0], b.half[0], b.pd[0], xh, xl);
+    sep2(pi.hy, pi.ly, pj.hy, pj.ly, b.lh[1], b.ll[1], b.half[1], b.pd[1], yh, yl);
+    sep2(pi.hz, pi.lz, pj.hz, pj.lz, b.lh[2], b.ll[2], b.half[2], b.pd[2], zh, zl);
+    const float px = xh * xh, py = yh * yh, pz = zh * zh;
+    const float approx = px + py + pz;
+    // early reject: sum dh^2 differs from r^2 by at most 2 sqrt(3) R max|dl| (+ rounding)
+    if (approx > rej) return kSkip;
     float t1, e1, t2, e2;
     two_sum(px, py, t1, e1);
     two_sum(t1, pz, t2, e2);
-    float cross = 2.0f * (x.h * x.l + y.h * y.l + z.h * z.l);
-    float lo = (e1 + e2) + (ex + ey + ez) + cross;
-    float r2h = t2 + lo;
-    float r2l = lo - (r2h - t2);
-    if (r2h > t.ru2h || (r2h == t.ru2h && r2l > t.ru2l)) return false;
-    // SK = CSI * r2^(1/4) with one Newton correction in float-float
-    float ti = rsqrtf(r2h);              // ~ 1/R
-    float u = rsqrtf(ti);                // ~ sqrt(R) = r2^(1/4)
-    float u2h = u * u, u2l = fmaf(u, u, -u2h);
-    float u4h = u2h * u2h, u4l = fmaf(u2h, u2h, -u4h) + 2.0f * u2h * u2l;
-    float diff = (r2h - u4h) + (r2l - u4l);
-    float delta = 0.25f * diff * (ti * ti);          // relative correction of u
-    float skh = t.csih * u;
-    float skl = fmaf(t.csih, u, -skh) + t.csih * u * delta + t.csil * u;
+    const float small = (e1 + e2) + fmaf(xh, xh, -px) + fmaf(yh, yh, -py) + fmaf(zh, zh, -pz) +
+                        2.0f * (xh * xl + yh * yl + zh * zl);
+    const float r2h = t2 + small;
+    const float r2l = small - (r2h - t2);
+    if (r2h > t.ru2h || (r2h == t.ru2h && r2l > t.ru2l)) return kSkip;
+    // SK = CSI * r2^(1/4), one Newton correction of u = rsqrt(rsqrt(r2)) in float-float
+    const float ti = rsqrtf(r2h);
+    const float u = rsqrtf(ti);
+    const float u2h = u * u, u2l = fmaf(u, u, -u2h);
+    const float u4h = u2h * u2h, u4l = fmaf(u2h, u2h, -u4h) + 2.0f * u2h * u2l;
+    const float delta = 0.25f * ((r2h - u4h) + (r2l - u4l)) * (ti * ti);
+    const float skh = t.csih * u;
+    const float skl = fmaf(t.csih, u, -skh) + (t.csih * u) * delta + t.csil * u;
     int kk = (int)skh;
     float dk = (skh - (float)kk) + skl;
     if (dk < 0.0f) { kk -= 1; dk += 1.0f; }
     else if (dk >= 1.0f) { kk += 1; dk -= 1.0f; }
     kk = min(max(kk, 0), t.ntab);
-    g.sx = x.h; g.sy = y.h; g.sz = z.h;
-    g.y = ti;
-    g.kk = kk;
-    g.dk = dk;
-    return true;
+    unsigned q = (unsigned)fminf(fmaf(dk, kDkScale, 0.5f), kDkScale - 1.0f);
+    dk_out = dk;
+    kk_out = kk;
+    return ((unsigned)kk << kDkBits) | q;
 }
 
-template <int POT, bool MULTI>
+template <int POT, bool MULTI, int UNR>
 __global__ void __launch_bounds__(kBlock) k_density32(DevAtoms a, DevTables t)
 {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
-    if ((a.statu[i] & MSMGB_STATU_ACTIVE) != MSMGB_STATU_ACTIVE) {
+    const int kn = a.kvois[i];
+    unsigned *__restrict__ pk = a.pk + i;
+    const int ld = a.ld;
+    if ((a.statu[i] & MSMGB_STATU_ACTIVE) != MSMGB_STATU_ACTIVE) {   // the force pass skips it
         a.den32[i] = 0.0f;
         return;
     }
-    const DevBox &b = a.box[a.boxid[i]];
+    const BoxF b = load_boxf(a.box[a.boxid[i]]);
+    const float rej = t.ru2h + 4.0f * sqrtf(t.ru2h) * b.dlmax + 1e-5f * t.ru2h;
     const PosFF pi = a.posff[i];
     const int ti = MULTI ? a.ityp[i] - 1 : 0;
-    const int kn = a.kvois[i];
     const int *__restrict__ nb = a.indi + i;
-    const size_t ld = (size_t)a.ld;
+    const float2 *__restrict__ row0 = t.dens2;
     float rho = 0.0f;
-    for (int w = 0; w < kn; ++w) {
-        int j = __ldg(nb + w * ld);
-        const PosFF pj = a.posff[j];
-        PairGeom g;
-        if (!pair_geom(pi, pj, b, t, g)) continue;
-        int k = MULTI ? t.kpair[(a.ityp[j] - 1) * t.ngroup + ti] : 0;
-        float2 e = __ldg(t.dens2 + (size_t)k * t.ntp + g.kk);
-        rho += fmaf(g.dk, e.y, e.x);
+    int w = 0;
+    // UNR neighbours per iteration keep UNR independent gathers in flight
+    for (; w + UNR <= kn; w += UNR) {
+        int j[UNR];
+        PosFF p[UNR];
+#pragma unroll
+        for (int u = 0; u < UNR; ++u) j[u] = __ldg(nb + (w + u) * ld);
+#pragma unroll
+        for (int u = 0; u < UNR; ++u) p[u] = a.posff[j[u]];
+#pragma unroll
+        for (int u = 0; u < UNR; ++u) {
+            float dk;
+            int kk;
+            const unsigned c = pair_index(pi, p[u], b, t, rej, dk, kk);
+            pk[(w + u) * ld] = c;
+            if (c != kSkip) {
+                const int k = MULTI ? t.kpair[(a.ityp[j[u]] - 1) * t.ngroup + ti] : 0;
+                const float2 e = __ldg(row0 + k * t.ntp + kk);
+                rho += fmaf(dk, e.y, e.x);
+            }
+        }
+    }
+    for (; w < kn; ++w) {
+        const int j0 = __ldg(nb + w * ld);
+        const PosFF p0 = a.posff[j0];
+        float dk;
+        int kk;
+        const unsigned c = pair_index(pi, p0, b, t, rej, dk, kk);
+        pk[w * ld] = c;
+        if (c != kSkip) {
+            const int k = MULTI ? t.kpair[(a.ityp[j0] - 1) * t.ngroup + ti] : 0;
+            const float2 e = __ldg(row0 + k * t.ntp + kk);
+            rho += fmaf(dk, e.y, e.x);
+        }
     }
     float d = rho;
     if (POT == MSMGB_FS_TYPE) {
         if (rho > 0.0f) d = -0.5f * rsqrtf(rho);
     } else if (rho > 0.0f) {
         const int ke = MULTI ? t.kembd[ti] : 0;
-        float sk = rho / t.rhodf + 1.0f;
+        const float sk = rho / t.rhodf + 1.0f;
         int kk = (int)(sk + 0.000001f);
         if (kk + 1 > t.nembd) {
             atomicOr(&a.flags[kFlagErr], kErrRho);
             kk = t.nembd;
         }
-        float2 e = __ldg(t.embd2 + (size_t)ke * t.nep + kk);
+        const float2 e = __ldg(t.embd2 + ke * t.nep + kk);
         d = fmaf(sk - (float)kk, e.y, e.x);
     }
     a.den32[i] = d;
 }
 
+// FP32 separation for the force direction (dh exact, dl small)
+__device__ __forceinline__ float sep1(float hi, float lo, float hj, float lj, float lh, float ll,
+                                      float half, int pd)
+{
+    float dh, dl;
+    sep2(hi, lo, hj, lj, lh, ll, half, pd, dh, dl);
+    return dh + dl;
+}
+
 template <bool MULTI>
+__device__ __forceinline__ void force_pair(const PosFF &pi, const PosFF &pj, unsigned c, float di,
+                                           float dj, int ti, int tj, const BoxF &b, const DevTables &t,
+                                           float &fx, float &fy, float &fz)
+{
+    const float sx = sep1(pi.hx, pi.lx, pj.hx, pj.lx, b.lh[0], b.ll[0], b.half[0], b.pd[0]);
+    const float sy = sep1(pi.hy, pi.ly, pj.hy, pj.ly, b.lh[1], b.ll[1], b.half[1], b.pd[1]);
+    const float sz = sep1(pi.hz, pi.lz, pj.hz, pj.lz, b.lh[2], b.ll[2], b.half[2], b.pd[2]);
+    const float y = rsqrtf(fmaf(sx, sx, fmaf(sy, sy, sz * sz)));
+    const int kk = (int)(c >> kDkBits);
+    const float dk = (float)(c & ((1u << kDkBits) - 1)) * kDkInv;
+    const int k = MULTI ? t.kpair[tj * t.ngroup + ti] : 0;
+    const float4 e = __ldg(t.force4 + k * t.ntp + kk);
+    const float P = fmaf(dk, e.y, e.x);
+    const float B = fmaf(dk, e.w, e.z);
+    float emb = B * (di + dj);
+    if (MULTI) {
+        const int k1 = t.kpair[ti * t.ngroup + tj];
+        if (k1 != k) {
+            const float4 e1 = __ldg(t.force4 + k1 * t.ntp + kk);
+            emb = B * di + fmaf(dk, e1.w, e1.z) * dj;
+        }
+    }
+    const float ft = fmaf(P, y, emb) * y;
+    fx = fmaf(ft, sx, fx);
+    fy = fmaf(ft, sy, fy);
+    fz = fmaf(ft, sz, fz);
+}
+
+template <bool MULTI, int UNR>
 __global__ void __launch_bounds__(kBlock) k_force32(DevAtoms a, DevTables t)
 {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
     float fx = 0.0f, fy = 0.0f, fz = 0.0f;
     if ((a.statu[i] & MSMGB_STATU_ACTIVE) == MSMGB_STATU_ACTIVE) {
-        const DevBox &b = a.box[a.boxid[i]];
+        const BoxF b = load_boxf(a.box[a.boxid[i]]);
         const PosFF pi = a.posff[i];
         const int ti = MULTI ? a.ityp[i] - 1 : 0;
         const float di = a.den32[i];
         const int kn = a.kvois[i];
+        const int ld = a.ld;
         const int *__restrict__ nb = a.indi + i;
-        const size_t ld = (size_t)a.ld;
-        for (int w = 0; w < kn; ++w) {
-            int j = __ldg(nb + w * ld);
-            const PosFF pj = a.posff[j];
-            PairGeom g;
-            if (!pair_geom(pi, pj, b, t, g)) continue;
-            int tj = MULTI ? a.ityp[j] - 1 : 0;
-            int k = MULTI ? t.kpair[tj * t.ngroup + ti] : 0;
-            float dj = __ldg(a.den32 + j);
-            float4 e = __ldg(t.force4 + (size_t)k * t.ntp + g.kk);
-            float P = fmaf(g.dk, e.y, e.x);
-            float B = fmaf(g.dk, e.w, e.z);
-            float B1 = B;
-            if (MULTI) {
-                int k1 = t.kpair[ti * t.ngroup + tj];
-                if (k1 != k) {
-                    float4 e1 = __ldg(t.force4 + (size_t)k1 * t.ntp + g.kk);
-                    B1 = fmaf(g.dk, e1.w, e1.z);
+        const unsigned *__restrict__ pk = a.pk + i;
+        int w = 0;
+        for (; w + UNR <= kn; w += UNR) {
+            unsigned c[UNR];
+            int j[UNR];
+#pragma unroll
+            for (int u = 0; u < UNR; ++u) {
+                c[u] = __ldg(pk + (w + u) * ld);
+                j[u] = __ldg(nb + (w + u) * ld);
+            }
+#pragma unroll
+            for (int u = 0; u < UNR; ++u) {
+                if (c[u] != kSkip) {
+                    const PosFF pj = a.posff[j[u]];
+                    force_pair<MULTI>(pi, pj, c[u], di, __ldg(a.den32 + j[u]), ti,
+                                      MULTI ? a.ityp[j[u]] - 1 : 0, b, t, fx, fy, fz);
                 }
             }
-            float ft = (P * g.y + (B * di + B1 * dj)) * g.y;
-            fx = fmaf(ft, g.sx, fx);
-            fy = fmaf(ft, g.sy, fy);
-            fz = fmaf(ft, g.sz, fz);
+        }
+        for (; w < kn; ++w) {
+            const unsigned c0 = __ldg(pk + w * ld);
+            if (c0 != kSkip) {
+                const int j0 = __ldg(nb + w * ld);
+                const PosFF p0 = a.posff[j0];
+                force_pair<MULTI>(pi, p0, c0, di, __ldg(a.den32 + j0), ti, MULTI ? a.ityp[j0] - 1 : 0, b, t,
+                                  fx, fy, fz);
+            }
         }
     }
     a.fx[i] = (double)fx;
@@ -179,18 +268,207 @@ __global__ void __launch_bounds__(kBlock) k_force32(DevAtoms a, DevTables t)
     a.fz[i] = (double)fz;
 }
 
+// ---- persistent variants with the used table range in shared memory -----------------
+// One block per SM slot (grid = resident blocks x SMs), grid-stride over the atoms.  The
+// last `cnt` rows of the single-kind table (the short-distance end is rarely reached) are
+// copied to shared memory once per block, so the divergent per-lane table reads of a warp
+// hit shared memory banks instead of distinct L1 lines; rows below `kmin` fall back to the
+// global table.
+template <int POT, int UNR>
+__global__ void __launch_bounds__(kBlock) k_density32s(DevAtoms a, DevTables t, int kmin, int cnt)
+{
+    extern __shared__ float2 sdens[];
+    for (int k = threadIdx.x; k < cnt; k += blockDim.x) sdens[k] = t.dens2[kmin + k];
+    __syncthreads();
+    const int ld = a.ld;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += gridDim.x * blockDim.x) {
+        const int kn = a.kvois[i];
+        unsigned *__restrict__ pk = a.pk + i;
+        if ((a.statu[i] & MSMGB_STATU_ACTIVE) != MSMGB_STATU_ACTIVE) {
+            a.den32[i] = 0.0f;
+            continue;
+        }
+        const BoxF b = load_boxf(a.box[a.boxid[i]]);
+        const float rej = t.ru2h + 4.0f * sqrtf(t.ru2h) * b.dlmax + 1e-5f * t.ru2h;
+        const PosFF pi = a.posff[i];
+        const int *__restrict__ nb = a.indi + i;
+        float rho = 0.0f;
+        int w = 0;
+        for (; w + UNR <= kn; w += UNR) {
+            int j[UNR];
+            PosFF p[UNR];
+#pragma unroll
+            for (int u = 0; u < UNR; ++u) j[u] = __ldg(nb + (w + u) * ld);
+#pragma unroll
+            for (int u = 0; u < UNR; ++u) p[u] = a.posff[j[u]];
+#pragma unroll
+            for (int u = 0; u < UNR; ++u) {
+                float dk;
+                int kk;
+                const unsigned c = pair_index(pi, p[u], b, t, rej, dk, kk);
+                pk[(w + u) * ld] = c;
+                if (c != kSkip) {
+                    const float2 e = kk >= kmin ? sdens[kk - kmin] : __ldg(t.dens2 + kk);
+                    rho += fmaf(dk, e.y, e.x);
+                }
+            }
+        }
+        for (; w < kn; ++w) {
+            const int j0 = __ldg(nb + w * ld);
+            const PosFF p0 = a.posff[j0];
+            float dk;
+            int kk;
+            const unsigned c = pair_index(pi, p0, b, t, rej, dk, kk);
+            pk[w * ld] = c;
+            if (c != kSkip) {
+                const float2 e = kk >= kmin ? sdens[kk - kmin] : __ldg(t.dens2 + kk);
+                rho += fmaf(dk, e.y, e.x);
+            }
+        }
+        float d = rho;
+        if (POT == MSMGB_FS_TYPE) {
+            if (rho > 0.0f) d = -0.5f * rsqrtf(rho);
+        } else if (rho > 0.0f) {
+            const float sk = rho / t.rhodf + 1.0f;
+            int kk = (int)(sk + 0.000001f);
+            if (kk + 1 > t.nembd) {
+                atomicOr(&a.flags[kFlagErr], kErrRho);
+                kk = t.nembd;
+            }
+            const float2 e = __ldg(t.embd2 + kk);
+            d = fmaf(sk - (float)kk, e.y, e.x);
+        }
+        a.den32[i] = d;
+    }
+}
+
+template <int UNR>
+__global__ void __launch_bounds__(kBlock) k_force32s(DevAtoms a, DevTables t, int kmin, int cnt)
+{
+    extern __shared__ float4 sforce[];
+    for (int k = threadIdx.x; k < cnt; k += blockDim.x) sforce[k] = t.force4[kmin + k];
+    __syncthreads();
+    const int ld = a.ld;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += gridDim.x * blockDim.x) {
+        float fx = 0.0f, fy = 0.0f, fz = 0.0f;
+        if ((a.statu[i] & MSMGB_STATU_ACTIVE) == MSMGB_STATU_ACTIVE) {
+            const BoxF b = load_boxf(a.box[a.boxid[i]]);
+            const PosFF pi = a.posff[i];
+            const float di = a.den32[i];
+            const int kn = a.kvois[i];
+            const int *__restrict__ nb = a.indi + i;
+            const unsigned *__restrict__ pk = a.pk + i;
+            for (int w = 0; w < kn; w += UNR) {
+                unsigned c[UNR];
+                int j[UNR];
+#pragma unroll
+                for (int u = 0; u < UNR; ++u) {
+                    c[u] = (w + u < kn) ? __ldg(pk + (w + u) * ld) : kSkip;
+                    j[u] = (w + u < kn) ? __ldg(nb + (w + u) * ld) : 0;
+                }
+#pragma unroll
+                for (int u = 0; u < UNR; ++u) {
+                    if (c[u] == kSkip) continue;
+                    const PosFF pj = a.posff[j[u]];
+                    const float dj = __ldg(a.den32 + j[u]);
+                    const float sx = sep1(pi.hx, pi.lx, pj.hx, pj.lx, b.lh[0], b.ll[0], b.half[0], b.pd[0]);
+                    const float sy = sep1(pi.hy, pi.ly, pj.hy, pj.ly, b.lh[1], b.ll[1], b.half[1], b.pd[1]);
+                    const float sz = sep1(pi.hz, pi.lz, pj.hz, pj.lz, b.lh[2], b.ll[2], b.half[2], b.pd[2]);
+                    const float y = rsqrtf(fmaf(sx, sx, fmaf(sy, sy, sz * sz)));
+                    const int kk = (int)(c[u] >> kDkBits);
+                    const float dk = (float)(c[u] & ((1u << kDkBits) - 1)) * kDkInv;
+                    const float4 e = kk >= kmin ? sforce[kk - kmin] : __ldg(t.force4 + kk);
+                    const float P = fmaf(dk, e.y, e.x);
+                    const float B = fmaf(dk, e.w, e.z);
+                    const float ft = fmaf(P, y, B * (di + dj)) * y;
+                    fx = fmaf(ft, sx, fx);
+                    fy = fmaf(ft, sy, fy);
+                    fz = fmaf(ft, sz, fz);
+                }
+            }
+        }
+        a.fx[i] = (double)fx;
+        a.fy[i] = (double)fy;
+        a.fz[i] = (double)fz;
+    }
+}
+
 static inline int nblk(long n, int b) { return (int)((n + b - 1) / b); }
+
+// shared-memory table window of the persistent variants (rows [kmin, ntp))
+static void smem_window(const msmgb_ctx *c, int bytes_per_row, int *kmin, int *cnt)
+{
+    const int budget = 48 * 1024 / bytes_per_row;
+    *cnt = std::min(budget, c->tab.ntp);
+    *kmin = c->tab.ntp - *cnt;
+}
+
+static int persistent_grid(const void *kernel, int smem)
+{
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, kBlock, smem);
+    return std::max(1, per) * std::max(1, sms);
+}
+
+template <int POT, bool MULTI>
+static void dens_variant(msmgb_ctx *c, int unr)
+{
+    const int g = nblk(c->n, kBlock);
+    if (!MULTI && unr >= 8) {
+        int kmin, cnt;
+        smem_window(c, (int)sizeof(float2), &kmin, &cnt);
+        const int smem = cnt * (int)sizeof(float2);
+        if ((unr & 7) == 1) {
+            k_density32s<POT, 1><<<persistent_grid((const void *)k_density32s<POT, 1>, smem), kBlock, smem, c->stream>>>(c->a, c->tab, kmin, cnt);
+        } else {
+            k_density32s<POT, 2><<<persistent_grid((const void *)k_density32s<POT, 2>, smem), kBlock, smem, c->stream>>>(c->a, c->tab, kmin, cnt);
+        }
+        return;
+    }
+    switch (unr & 7) {
+    case 1: k_density32<POT, MULTI, 1><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
+    case 4: k_density32<POT, MULTI, 4><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
+    default: k_density32<POT, MULTI, 2><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
+    }
+}
+
+template <bool MULTI>
+static void force_variant(msmgb_ctx *c, int unr)
+{
+    const int g = nblk(c->n, kBlock);
+    if (!MULTI && unr >= 8) {
+        int kmin, cnt;
+        smem_window(c, (int)sizeof(float4), &kmin, &cnt);
+        const int smem = cnt * (int)sizeof(float4);
+        if ((unr & 7) == 1) {
+            k_force32s<1><<<persistent_grid((const void *)k_force32s<1>, smem), kBlock, smem, c->stream>>>(c->a, c->tab, kmin, cnt);
+        } else {
+            k_force32s<2><<<persistent_grid((const void *)k_force32s<2>, smem), kBlock, smem, c->stream>>>(c->a, c->tab, kmin, cnt);
+        }
+        return;
+    }
+    switch (unr & 7) {
+    case 1: k_force32<MULTI, 1><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
+    case 4: k_force32<MULTI, 4><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
+    default: k_force32<MULTI, 2><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
+    }
+}
 
 int launch_density32(msmgb_ctx *c)
 {
-    int g = nblk(c->n, kBlock);
-    bool multi = c->tab.ngroup > 1;
+    if (!c->a.pk) return set_err(c, MSMGB_ERR_ARG, "mixed passes need the pair-index buffer (set MIXED precision)");
+    if (c->tab.ntab >= (1 << (32 - kDkBits)) - 1)
+        return set_err(c, MSMGB_ERR_ARG, "mixed passes support NTAB < 16383");
+    const bool multi = c->tab.ngroup > 1;
+    const int unr = c->tune_dens_unroll;
     if (c->tab.pottype == MSMGB_FS_TYPE) {
-        if (multi) k_density32<MSMGB_FS_TYPE, true><<<g, kBlock, 0, c->stream>>>(c->a, c->tab);
-        else k_density32<MSMGB_FS_TYPE, false><<<g, kBlock, 0, c->stream>>>(c->a, c->tab);
+        if (multi) dens_variant<MSMGB_FS_TYPE, true>(c, unr);
+        else dens_variant<MSMGB_FS_TYPE, false>(c, unr);
     } else {
-        if (multi) k_density32<MSMGB_EAM_TYPE, true><<<g, kBlock, 0, c->stream>>>(c->a, c->tab);
-        else k_density32<MSMGB_EAM_TYPE, false><<<g, kBlock, 0, c->stream>>>(c->a, c->tab);
+        if (multi) dens_variant<MSMGB_EAM_TYPE, true>(c, unr);
+        else dens_variant<MSMGB_EAM_TYPE, false>(c, unr);
     }
     c->launches += 1;
     c->den_is32 = true;
@@ -199,11 +477,63 @@ int launch_density32(msmgb_ctx *c)
 
 int launch_force32(msmgb_ctx *c)
 {
-    int g = nblk(c->n, kBlock);
-    if (c->tab.ngroup > 1) k_force32<true><<<g, kBlock, 0, c->stream>>>(c->a, c->tab);
-    else k_force32<false><<<g, kBlock, 0, c->stream>>>(c->a, c->tab);
+    if (c->tab.ngroup > 1) force_variant<true>(c, c->tune_force_unroll);
+    else force_variant<false>(c, c->tune_force_unroll);
     c->launches += 1;
     return check_launch(c, "mixed force pass");
+}
+
+// Autotuner: times every unroll depth of both mixed passes on the context's current data
+// (three launches each after one warm-up, CUDA events on the context stream) and keeps the
+// fastest.  Runs once per context and atom count, outside any stream capture.
+int autotune_mixed(msmgb_ctx *c)
+{
+    // unroll 1, 2, 4 with the table read through L1; +8: persistent grid, table in shared memory
+    const bool single = c->tab.ngroup == 1;
+    const int cands[5] = {1, 2, 4, 9, 10};
+    const int ncand = single ? 5 : 3;
+    cudaEvent_t e0, e1;
+    cudaError_t err = cudaEventCreate(&e0);
+    if (err == cudaSuccess) err = cudaEventCreate(&e1);
+    if (err != cudaSuccess) return cuda_err(c, err, "autotune events");
+    float best_d = 1e30f, best_f = 1e30f;
+    int bd = 2, bf = 2;
+    for (int k = 0; k < ncand; ++k) {
+        c->tune_dens_unroll = cands[k];
+        for (int r = 0; r < 4; ++r) {
+            if (r == 1) cudaEventRecord(e0, c->stream);
+            int rc = launch_density32(c);
+            if (rc) return rc;
+        }
+        cudaEventRecord(e1, c->stream);
+        cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (ms < best_d) { best_d = ms; bd = cands[k]; }
+    }
+    c->tune_dens_unroll = bd;
+    int rc = launch_density32(c);
+    if (rc) return rc;
+    for (int k = 0; k < ncand; ++k) {
+        c->tune_force_unroll = cands[k];
+        for (int r = 0; r < 4; ++r) {
+            if (r == 1) cudaEventRecord(e0, c->stream);
+            rc = launch_force32(c);
+            if (rc) return rc;
+        }
+        cudaEventRecord(e1, c->stream);
+        cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (ms < best_f) { best_f = ms; bf = cands[k]; }
+    }
+    c->tune_force_unroll = bf;
+    c->tune_ms[0] = best_d / 3.0f;
+    c->tune_ms[1] = best_f / 3.0f;
+    c->tuned_n = c->n;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return check_launch(c, "autotune");
 }
 
 }  // namespace msmgb

@@ -9,7 +9,8 @@
 //   vx..vz   double   velocities (SoA, streamed)
 //   fx..fz   double   forces (SoA, streamed)
 //   dis      double   accumulated displacement DIS (reference MD_DiffScheme_GPU.F90:364-366)
-//   pos_bld  double4_32a  positions at the last list build (skin trigger)
+//   pos_bld  float4   hi parts of the shifted positions at the last list build (skin
+//                     trigger; hi_i - hi_bld is exact)
 //   ityp, statu, gid (sorted -> original), boxid
 //   kvois    int32    neighbour count, INDI column-major int32 [mxkvois][cap] (reference
 //                     layout INDI(NAPDEV,MXKVOIS), MD_NeighborsList_GPU.F90:75-85)
@@ -55,6 +56,7 @@ struct DevBox {
     float lenf[3];       // float-float box length (hi, lo) and FP32 half length
     float lenlo[3];
     float halff[3];
+    float dlmax;         // bound on the low part of a float-float separation component
     int ifpd[3];
     int nc[3];
     int cell0;           // first global cell id of this box
@@ -88,7 +90,7 @@ struct DevAtoms {
     double *vx, *vy, *vz;
     double *fx, *fy, *fz;
     double *dx, *dy, *dz;
-    double4_32a *pos_bld;
+    float4 *pos_bld;
     int *ityp, *statu, *gid, *boxid;
     double *den, *epot;
     float *den32;
@@ -98,6 +100,8 @@ struct DevAtoms {
     int n;
     const DevBox *box;
     const double *cm;    // masses per type (0-based type index)
+    const double *icm;   // reciprocal masses per type
+    unsigned *pk;        // mixed passes: per-pair table index (KK << 18 | DK * 2^18), ELL layout
     int *flags;
     unsigned long long *maxdisp;
     double *virial;      // [nbox][6]
@@ -142,6 +146,7 @@ struct msmgb_ctx {
     int *scan_tmp = nullptr;
     void *scratch = nullptr;           // permutation staging (size: 96 B per atom)
     double *cm = nullptr;
+    double *icm = nullptr;
     int *flags = nullptr;
     unsigned long long *maxdisp = nullptr;
     double *virial = nullptr;
@@ -161,12 +166,18 @@ struct msmgb_ctx {
     bool force_valid = false;
     bool den_is32 = false;             // the last density pass was the mixed one
 
+    // autotuned launch variants of the mixed passes (neighbours in flight per thread)
+    int tune_dens_unroll = 2, tune_force_unroll = 2;
+    int tuned_n = -1;
+    float tune_ms[2] = {0.f, 0.f};
+
     // CUDA graph of one MD step
     cudaGraphExec_t step_graph = nullptr;
     int64_t graph_kernels = 0;
     double graph_h = 0.0;
     int graph_prec = -1;
     int graph_n = -1;
+    int graph_tune = -1;
 };
 
 namespace msmgb {
@@ -184,6 +195,7 @@ int launch_density(msmgb_ctx *c, bool want_epot);
 int launch_force(msmgb_ctx *c, bool want_virial);
 int launch_density32(msmgb_ctx *c);
 int launch_force32(msmgb_ctx *c);
+int autotune_mixed(msmgb_ctx *c);
 int launch_hvp(msmgb_ctx *c, const double *dv, double *dhv, double *v4buf, double *ddbuf);
 int launch_adjoint(msmgb_ctx *c, const double *ft, const double *dtab, double *w4buf, double *ddbuf,
                    double *acc);

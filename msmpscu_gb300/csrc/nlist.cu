@@ -235,10 +235,10 @@ __global__ void __launch_bounds__(kBlock) k_build(DevAtoms a, const int *cell_of
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
     double4_32a p = a.pos[i];
-    a.pos_bld[i] = p;
+    const PosFF pf = a.posff[i];
+    a.pos_bld[i] = make_float4(pf.hx, pf.hy, pf.hz, 0.0f);
     if (a.statu[i] & MSMGB_STATU_OUTOFBOX) { a.kvois[i] = 0; return; }
     const DevBox &b = a.box[a.boxid[i]];
-    const PosFF pf = a.posff[i];
     int c = cell_of[i] - b.cell0;
     int ix = c % b.nc[0], iy = (c / b.nc[0]) % b.nc[1], iz = c / (b.nc[0] * b.nc[1]);
     int nn = 0;

@@ -20,6 +20,11 @@ __device__ __forceinline__ double mi(double s, double len, double half, int pd)
     return (pd && fabs(s) > half) ? s - copysign(len, s) : s;
 }
 
+__device__ __forceinline__ float mi32(float s, float len, float half, int pd)
+{
+    return (pd && fabsf(s) > half) ? s - copysignf(len, s) : s;
+}
+
 __device__ __forceinline__ void block_max_flush(double v, unsigned long long *dst)
 {
     __shared__ double sm[kBlock / 32];
@@ -48,10 +53,12 @@ __global__ void __launch_bounds__(kBlock) k_vv(DevAtoms a, double th, int mode)
         if ((stat & MSMGB_STATU_ACTIVE) == MSMGB_STATU_ACTIVE) {
             const double hs2 = th * 0.5, h2s2 = th * th * 0.5;
             const DevBox &b = a.box[a.boxid[i]];
-            double cm0 = a.cm[a.ityp[i] - 1];
+            // F/m as a product with the reciprocal mass: FP64 division is emulated and
+            // costly on this GPU's FP64 pipe; the result differs from FP/CM0 by <= 1 ulp
+            const double icm = a.icm[a.ityp[i] - 1];
             double4_32a p = a.pos[i];
             double vx = a.vx[i], vy = a.vy[i], vz = a.vz[i];
-            double ax = a.fx[i] / cm0, ay = a.fy[i] / cm0, az = a.fz[i] / cm0;
+            double ax = a.fx[i] * icm, ay = a.fy[i] * icm, az = a.fz[i] * icm;
             if (pend) {
                 if (!(stat & MSMGB_STATU_FIXVELX) && !(stat & MSMGB_STATU_FIXPOSX)) vx = vx + hs2 * ax;
                 if (!(stat & MSMGB_STATU_FIXVELY) && !(stat & MSMGB_STATU_FIXPOSY)) vy = vy + hs2 * ay;
@@ -82,7 +89,8 @@ __global__ void __launch_bounds__(kBlock) k_vv(DevAtoms a, double th, int mode)
             if (!(stat & MSMGB_STATU_FIXVELY) && !(stat & MSMGB_STATU_FIXPOSY)) vy = vy + hs2 * ay;
             if (!(stat & MSMGB_STATU_FIXVELZ) && !(stat & MSMGB_STATU_FIXPOSZ)) vz = vz + hs2 * az;
             a.pos[i] = make_double4_32a(x, y, z, p.w);
-            a.posff[i] = make_posff(x, y, z, b);
+            const PosFF f = make_posff(x, y, z, b);
+            a.posff[i] = f;
             a.vx[i] = vx; a.vy[i] = vy; a.vz[i] = vz;
             a.dx[i] += dx; a.dy[i] += dy; a.dz[i] += dz;
             // Predictor_KERNEL0 :372-378 (PASSBOUND is not stored, quirk Q10)
@@ -91,11 +99,13 @@ __global__ void __launch_bounds__(kBlock) k_vv(DevAtoms a, double th, int mode)
                 a.statu[i] = MSMGB_STATU_OUTOFBOX | MSMGB_STATU_REFLECT;
             else if (x < b.lo[0] || y < b.lo[1] || z < b.lo[2])
                 a.statu[i] = MSMGB_STATU_OUTOFBOX | MSMGB_STATU_TRANSMIT;
-            double4_32a q = a.pos_bld[i];
-            double ex = mi(x - q.x, b.len[0], b.half[0], b.ifpd[0]);
-            double ey = mi(y - q.y, b.len[1], b.half[1], b.ifpd[1]);
-            double ez = mi(z - q.z, b.len[2], b.half[2], b.ifpd[2]);
-            dmax = ex * ex + ey * ey + ez * ez;
+            // displacement since the last build from the exact FP32 hi parts (the trigger
+            // needs ~1e-4 A, the hi parts are within 3e-5 A of the FP64 positions)
+            const float4 q = a.pos_bld[i];
+            float ex = mi32(f.hx - q.x, b.lenf[0], b.halff[0], b.ifpd[0]);
+            float ey = mi32(f.hy - q.y, b.lenf[1], b.halff[1], b.ifpd[1]);
+            float ez = mi32(f.hz - q.z, b.lenf[2], b.halff[2], b.ifpd[2]);
+            dmax = (double)(ex * ex + ey * ey + ez * ez);
         }
     }
     block_max_flush(dmax, a.maxdisp);
@@ -109,10 +119,10 @@ __global__ void __launch_bounds__(kBlock) k_correct(DevAtoms a, double th, int o
     int stat = a.statu[i];
     if ((stat & MSMGB_STATU_ACTIVE) != MSMGB_STATU_ACTIVE) return;
     const double hs2 = th * 0.5;
-    double cm0 = a.cm[a.ityp[i] - 1];
-    if (!(stat & MSMGB_STATU_FIXVELX) && !(stat & MSMGB_STATU_FIXPOSX)) a.vx[i] = a.vx[i] + hs2 * (a.fx[i] / cm0);
-    if (!(stat & MSMGB_STATU_FIXVELY) && !(stat & MSMGB_STATU_FIXPOSY)) a.vy[i] = a.vy[i] + hs2 * (a.fy[i] / cm0);
-    if (!(stat & MSMGB_STATU_FIXVELZ) && !(stat & MSMGB_STATU_FIXPOSZ)) a.vz[i] = a.vz[i] + hs2 * (a.fz[i] / cm0);
+    const double icm = a.icm[a.ityp[i] - 1];
+    if (!(stat & MSMGB_STATU_FIXVELX) && !(stat & MSMGB_STATU_FIXPOSX)) a.vx[i] = a.vx[i] + hs2 * (a.fx[i] * icm);
+    if (!(stat & MSMGB_STATU_FIXVELY) && !(stat & MSMGB_STATU_FIXPOSY)) a.vy[i] = a.vy[i] + hs2 * (a.fy[i] * icm);
+    if (!(stat & MSMGB_STATU_FIXVELZ) && !(stat & MSMGB_STATU_FIXPOSZ)) a.vz[i] = a.vz[i] + hs2 * (a.fz[i] * icm);
 }
 
 __global__ void k_clear_pending(int *flags) { flags[kFlagPending] = 0; }

@@ -280,6 +280,13 @@ class Engine:
         self._ck(self.lib.msmgb_time_passes(self.ctx, int(reps), out))
         return dict(density=out[0], force=out[1], nlist=out[2], vv=out[3])
 
+    def tuning(self):
+        out = (C.c_int * 2)()
+        ms = (C.c_float * 2)()
+        self._ck(self.lib.msmgb_get_tuning(self.ctx, out, ms))
+        return {"density_unroll": out[0], "force_unroll": out[1],
+                "density_ms": ms[0], "force_ms": ms[1]}
+
     def list_stats(self):
         mk = C.c_int()
         mean = C.c_double()
@@ -296,6 +303,13 @@ class Engine:
         grad = np.zeros(5)
         self._ck(self.lib.msmgb_param_adjoint(self.ctx, pot, _d(prm), _d(ft), C.byref(loss), _d(grad)))
         return loss.value, grad
+
+    def time_hvp(self, v, reps=10):
+        """(ms per Hessian-vector product, ms per FP64 force call) on the device."""
+        v = np.ascontiguousarray(np.asarray(v, np.float64).T).reshape(-1)
+        a, b = C.c_float(), C.c_float()
+        self._ck(self.lib.msmgb_time_hvp(self.ctx, _d(v), int(reps), C.byref(a), C.byref(b)))
+        return float(a.value), float(b.value)
 
     def hvp(self, v):
         v = np.ascontiguousarray(np.asarray(v, np.float64).T).reshape(-1)
