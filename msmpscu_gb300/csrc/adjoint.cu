@@ -169,9 +169,10 @@ int launch_adjoint(msmgb_ctx *c, const double *ft, const double *dtab, double *w
     cudaError_t e = cudaMemsetAsync(acc, 0, 6 * sizeof(double), c->stream);
     if (e != cudaSuccess) return cuda_err(c, e, "adjoint clear");
     double4_32a *w4 = (double4_32a *)w4buf;
-    k_adj_residual<<<nblk(n, kBlock), kBlock, 0, c->stream>>>(c->a, ft, w4, acc);
-    k_adj_density<<<nblk(n, kBlock), kBlock, 0, c->stream>>>(c->a, c->tab, d, ddbuf, c->cap_atoms);
-    k_adj_force<<<nblk(n, kBlock), kBlock, 0, c->stream>>>(c->a, c->tab, d, w4, ddbuf, c->cap_atoms, acc);
+    const int bs = block_for(n);
+    k_adj_residual<<<nblk(n, bs), bs, 0, c->stream>>>(c->a, ft, w4, acc);
+    k_adj_density<<<nblk(n, bs), bs, 0, c->stream>>>(c->a, c->tab, d, ddbuf, c->cap_atoms);
+    k_adj_force<<<nblk(n, bs), bs, 0, c->stream>>>(c->a, c->tab, d, w4, ddbuf, c->cap_atoms, acc);
     c->launches += 3;
     return check_launch(c, "adjoint");
 }

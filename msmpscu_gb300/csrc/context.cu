@@ -54,6 +54,14 @@ int check_launch(msmgb_ctx *c, const char *what)
 
 static inline int nblk(long n, int b) { return (int)((n + b - 1) / b); }
 
+// integer key that orders like the double value (for the integrator's box tests)
+static long long order_key(double x)
+{
+    long long k;
+    memcpy(&k, &x, sizeof(k));
+    return k ^ ((k >> 63) & 0x7fffffffffffffffLL);
+}
+
 template <typename T>
 static cudaError_t dalloc(T **p, size_t count)
 {
@@ -217,7 +225,7 @@ extern "C" int msmgb_destroy(msmgb_ctx *c)
                     a.dx, a.dy, a.dz, a.ityp, a.statu, a.gid, a.boxid, a.den, a.epot,
                     a.den32, a.kvois, a.indi, a.pk, c->cell_of, c->perm, c->dbox, c->cm, c->icm,
                     c->flags, c->maxdisp, c->virial, c->scratch, c->cell_start,
-                    c->cell_cursor, c->scan_tmp, c->tab_mem, c->adj_mem};
+                    c->cell_cursor, c->scan_tmp, c->tab_mem, c->adj_mem, c->hvp_pair};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     if (c->h_flags) cudaFreeHost(c->h_flags);
@@ -430,6 +438,9 @@ extern "C" int msmgb_copyin_simbox(msmgb_ctx *c, int nbox, const msmgb_box *boxe
             d.lo[k] = boxes[b].lo[k];
             d.len[k] = boxes[b].len[k];
             d.half[k] = 0.5 * boxes[b].len[k];
+            d.ushift[k] = boxes[b].len[k] - boxes[b].lo[k];
+            d.klo[k] = order_key(boxes[b].lo[k]);
+            d.kub[k] = order_key(boxes[b].lo[k] + boxes[b].len[k]);
             d.lenf[k] = (float)d.len[k];
             d.lenlo[k] = (float)(d.len[k] - (double)d.lenf[k]);
             d.halff[k] = (float)d.half[k];
@@ -473,6 +484,7 @@ extern "C" int msmgb_copyin_simbox(msmgb_ctx *c, int nbox, const msmgb_box *boxe
     c->boxes.assign(boxes, boxes + nbox);
     c->hbox = hb;
     CK(cudaMemcpy(c->dbox, hb.data(), sizeof(DevBox) * (size_t)nbox, cudaMemcpyHostToDevice), "box upload");
+
     // stage the caller's arrays in the scratch buffer, then pack on the device
     char *s = (char *)c->scratch;
     double *dxp = (double *)s;
@@ -826,17 +838,27 @@ extern "C" int msmgb_finish_steps(msmgb_ctx *c, double h, int *rebuilds)
 }
 
 // ---- differentiation ------------------------------------------------------------------------
+static int ensure_hvp_pair(msmgb_ctx *c)
+{
+    if (c->hvp_pair) return MSMGB_OK;
+    CK(cudaStreamSynchronize(c->stream), "synchronize");
+    CK(cudaMalloc(&c->hvp_pair, sizeof(double) * 2 * (size_t)c->cap_atoms * (size_t)c->p.mxkvois),
+       "HVP pair buffer");
+    return MSMGB_OK;
+}
+
 extern "C" int msmgb_hvp(msmgb_ctx *c, const double *v, double *hv)
 {
     if (!c || !v || !hv) return MSMGB_ERR_ARG;
     RET(ready_for_force(c));
+    RET(ensure_hvp_pair(c));
     const int n = c->n;
     const size_t N = (size_t)c->cap_atoms;
     char *s = (char *)c->scratch;
     double *v4 = (double *)s;                 // 32 B per atom
-    double *dd = (double *)(s + 32 * N);      //  8 B
-    double *hvs = (double *)(s + 40 * N);     // 24 B, sorted SoA result
-    double *io = (double *)(s + 64 * N);      // 24 B, caller-order staging (input, then output)
+    double *dd = (double *)(s + 32 * N);      // 16 B: F'(rho) and its directional derivative
+    double *hvs = (double *)(s + 48 * N);     // 24 B, sorted SoA result
+    double *io = (double *)(s + 72 * N);      // 24 B, caller-order staging (input, then output)
     CK(cudaMemcpyAsync(io, v, sizeof(double) * 3 * (size_t)n, cudaMemcpyHostToDevice, c->stream), "hvp copy-in");
     RET(launch_hvp(c, io, hvs, v4, dd));
     k_unpack3<<<nblk(n, kBlock), kBlock, 0, c->stream>>>(hvs, hvs + n, hvs + 2 * (size_t)n, c->a.gid, n, 0, io);
@@ -980,11 +1002,12 @@ extern "C" int msmgb_time_hvp(msmgb_ctx *c, const double *v, int reps, float *ms
 {
     if (!c || !v || !ms_hvp || !ms_force || reps < 1) return MSMGB_ERR_ARG;
     RET(ready_for_force(c));
+    RET(ensure_hvp_pair(c));
     const int n = c->n;
     const size_t N = (size_t)c->cap_atoms;
     char *s = (char *)c->scratch;
-    double *v4 = (double *)s, *dd = (double *)(s + 32 * N), *hvs = (double *)(s + 40 * N);
-    double *io = (double *)(s + 64 * N);
+    double *v4 = (double *)s, *dd = (double *)(s + 32 * N), *hvs = (double *)(s + 48 * N);
+    double *io = (double *)(s + 72 * N);
     CK(cudaMemcpyAsync(io, v, sizeof(double) * 3 * (size_t)n, cudaMemcpyHostToDevice, c->stream), "hvp copy-in");
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0), "event");

@@ -111,14 +111,14 @@ __device__ __forceinline__ unsigned pair_index(const PosFF &pi, const PosFF &pj,
     return ((unsigned)kk << kDkBits) | q;
 }
 
-template <int POT, bool MULTI, int UNR>
-__global__ void __launch_bounds__(kBlock) k_density32(DevAtoms a, DevTables t)
+template <int POT, bool MULTI, int UNR, int MINB>
+__global__ void __launch_bounds__(kBlock, MINB) k_density32(DevAtoms a, DevTables t)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
     const int kn = a.kvois[i];
     unsigned *__restrict__ pk = a.pk + i;
-    const int ld = a.ld;
+    const size_t ld = (size_t)a.ld;
     if ((a.statu[i] & MSMGB_STATU_ACTIVE) != MSMGB_STATU_ACTIVE) {   // the force pass skips it
         a.den32[i] = 0.0f;
         return;
@@ -220,8 +220,8 @@ __device__ __forceinline__ void force_pair(const PosFF &pi, const PosFF &pj, uns
     fz = fmaf(ft, sz, fz);
 }
 
-template <bool MULTI, int UNR>
-__global__ void __launch_bounds__(kBlock) k_force32(DevAtoms a, DevTables t)
+template <bool MULTI, int UNR, int MINB>
+__global__ void __launch_bounds__(kBlock, MINB) k_force32(DevAtoms a, DevTables t)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
@@ -232,7 +232,7 @@ __global__ void __launch_bounds__(kBlock) k_force32(DevAtoms a, DevTables t)
         const int ti = MULTI ? a.ityp[i] - 1 : 0;
         const float di = a.den32[i];
         const int kn = a.kvois[i];
-        const int ld = a.ld;
+        const size_t ld = (size_t)a.ld;
         const int *__restrict__ nb = a.indi + i;
         const unsigned *__restrict__ pk = a.pk + i;
         int w = 0;
@@ -280,7 +280,7 @@ __global__ void __launch_bounds__(kBlock) k_density32s(DevAtoms a, DevTables t, 
     extern __shared__ float2 sdens[];
     for (int k = threadIdx.x; k < cnt; k += blockDim.x) sdens[k] = t.dens2[kmin + k];
     __syncthreads();
-    const int ld = a.ld;
+    const size_t ld = (size_t)a.ld;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += gridDim.x * blockDim.x) {
         const int kn = a.kvois[i];
         unsigned *__restrict__ pk = a.pk + i;
@@ -348,7 +348,7 @@ __global__ void __launch_bounds__(kBlock) k_force32s(DevAtoms a, DevTables t, in
     extern __shared__ float4 sforce[];
     for (int k = threadIdx.x; k < cnt; k += blockDim.x) sforce[k] = t.force4[kmin + k];
     __syncthreads();
-    const int ld = a.ld;
+    const size_t ld = (size_t)a.ld;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += gridDim.x * blockDim.x) {
         float fx = 0.0f, fy = 0.0f, fz = 0.0f;
         if ((a.statu[i] & MSMGB_STATU_ACTIVE) == MSMGB_STATU_ACTIVE) {
@@ -428,9 +428,11 @@ static void dens_variant(msmgb_ctx *c, int unr)
         return;
     }
     switch (unr & 7) {
-    case 1: k_density32<POT, MULTI, 1><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
-    case 4: k_density32<POT, MULTI, 4><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
-    default: k_density32<POT, MULTI, 2><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
+    case 1: k_density32<POT, MULTI, 1, 1><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
+    case 4: k_density32<POT, MULTI, 4, 1><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
+    case 5: k_density32<POT, MULTI, 4, 6><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
+    case 3: k_density32<POT, MULTI, 2, 6><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
+    default: k_density32<POT, MULTI, 2, 1><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
     }
 }
 
@@ -450,9 +452,11 @@ static void force_variant(msmgb_ctx *c, int unr)
         return;
     }
     switch (unr & 7) {
-    case 1: k_force32<MULTI, 1><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
-    case 4: k_force32<MULTI, 4><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
-    default: k_force32<MULTI, 2><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
+    case 1: k_force32<MULTI, 1, 1><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
+    case 4: k_force32<MULTI, 4, 1><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
+    case 5: k_force32<MULTI, 4, 6><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
+    case 3: k_force32<MULTI, 2, 6><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
+    default: k_force32<MULTI, 2, 1><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
     }
 }
 
@@ -488,10 +492,11 @@ int launch_force32(msmgb_ctx *c)
 // fastest.  Runs once per context and atom count, outside any stream capture.
 int autotune_mixed(msmgb_ctx *c)
 {
-    // unroll 1, 2, 4 with the table read through L1; +8: persistent grid, table in shared memory
+    // code & 7: 1, 2, 4 = neighbours in flight per thread; 3 = 2 and 5 = 4 with registers
+    // capped for 6 blocks (75% occupancy); +8: persistent grid with the table in shared memory
     const bool single = c->tab.ngroup == 1;
-    const int cands[5] = {1, 2, 4, 9, 10};
-    const int ncand = single ? 5 : 3;
+    const int cands[7] = {1, 2, 4, 3, 5, 9, 10};
+    const int ncand = single ? 7 : 5;
     cudaEvent_t e0, e1;
     cudaError_t err = cudaEventCreate(&e0);
     if (err == cudaSuccess) err = cudaEventCreate(&e1);

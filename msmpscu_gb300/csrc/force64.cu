@@ -188,17 +188,17 @@ static inline int nblk(long n, int b) { return (int)((n + b - 1) / b); }
 template <int POT, bool MULTI>
 static void dens_dispatch(msmgb_ctx *c, bool epot)
 {
-    int g = nblk(c->n, kBlock);
-    if (epot) k_density64<POT, MULTI, true><<<g, kBlock, 0, c->stream>>>(c->a, c->tab);
-    else k_density64<POT, MULTI, false><<<g, kBlock, 0, c->stream>>>(c->a, c->tab);
+    const int bs = block_for(c->n), g = nblk(c->n, bs);
+    if (epot) k_density64<POT, MULTI, true><<<g, bs, 0, c->stream>>>(c->a, c->tab);
+    else k_density64<POT, MULTI, false><<<g, bs, 0, c->stream>>>(c->a, c->tab);
 }
 
 template <int POT, bool MULTI>
 static void force_dispatch(msmgb_ctx *c, bool vir)
 {
-    int g = nblk(c->n, kBlock);
-    if (vir) k_force64<POT, MULTI, true><<<g, kBlock, 0, c->stream>>>(c->a, c->tab);
-    else k_force64<POT, MULTI, false><<<g, kBlock, 0, c->stream>>>(c->a, c->tab);
+    const int bs = block_for(c->n), g = nblk(c->n, bs);
+    if (vir) k_force64<POT, MULTI, true><<<g, bs, 0, c->stream>>>(c->a, c->tab);
+    else k_force64<POT, MULTI, false><<<g, bs, 0, c->stream>>>(c->a, c->tab);
 }
 
 int launch_density(msmgb_ctx *c, bool want_epot)

@@ -13,8 +13,9 @@
 //     FT = P/R^2 + (B F'_i + B1 F'_j)/R,
 //     dFT/dR = P'/R^2 - 2P/R^3 + (B' F'_i + B1' F'_j)/R - (B F'_i + B1 F'_j)/R^2,
 //     FTdot = dFT/dR Rdot + (B F'dot_i + B1 F'dot_j)/R;   hv = -Fdot.
-// The density pass is recomputed (not stored), so the product costs two passes like a
-// force call.
+// The density pass is recomputed (nothing is kept from an earlier force call); its pair
+// geometry (1/R, sqrt(R)) is handed to the second pass through a per-pair buffer in the
+// list's ELL layout, so the second pass evaluates no square roots.
 #include "msmgb_internal.cuh"
 
 namespace msmgb {
@@ -32,15 +33,14 @@ __device__ __forceinline__ void lerp2(const double *__restrict__ T, int kk, doub
     *val = a + dk * (b - a);
 }
 
-template <int POT>
+template <int POT, bool MULTI>
 __global__ void __launch_bounds__(kBlock) k_hvp_density(DevAtoms a, DevTables t, const double4_32a *v,
-                                                        double *dd)
+                                                        double2 *dd, double2 *pg)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
     if ((a.statu[i] & MSMGB_STATU_ACTIVE) != MSMGB_STATU_ACTIVE) {
-        a.den[i] = 0.0;
-        dd[i] = 0.0;
+        dd[i] = make_double2(0.0, 0.0);
         return;
     }
     const DevBox &b = a.box[a.boxid[i]];
@@ -57,20 +57,26 @@ __global__ void __launch_bounds__(kBlock) k_hvp_density(DevAtoms a, DevTables t,
         double sy = mi(p.y - q.y, b.len[1], b.half[1], b.ifpd[1]);
         double sz = mi(p.z - q.z, b.len[2], b.half[2], b.ifpd[2]);
         double r2 = sx * sx + sy * sy + sz * sz;
-        if (r2 > t.ru2) continue;
-        int k = t.kpair[(a.ityp[j] - 1) * t.ngroup + ti];
+        if (r2 > t.ru2) {
+            pg[w * ld + i] = make_double2(0.0, 0.0);     // beyond RU: skipped by the second pass
+            continue;
+        }
+        const int k = MULTI ? t.kpair[(a.ityp[j] - 1) * t.ngroup + ti] : 0;
         double y = rsqrt(r2);
         double sr = rsqrt(y);
+        pg[w * ld + i] = make_double2(y, sr);
         double sk = sr * t.csi;
         int kk = min((int)sk, t.ntab);
         double dk = sk - kk;
         double4_32a vj = v[j];
-        double rdot = (sx * (vi.x - vj.x) + sy * (vi.y - vj.y) + sz * (vi.z - vj.z)) * y;
+        const double sw = sx * (vi.x - vj.x) + sy * (vi.y - vj.y) + sz * (vi.z - vj.z);
         double val, sl;
         lerp2(t.potb + (size_t)k * t.ntp, kk, dk, &val, &sl);
         rho += val;
-        rhod += sl * (0.5 * t.csi * y * sr) * rdot;      // dSK/dR = CSI / (2 sqrt(R))
+        // dSK/dR * Rdot = (CSI/2) sqrt(R) / R^2 * (s.w); CSI/2 is applied once below
+        rhod += sl * (sr * (y * y)) * sw;
     }
+    rhod *= 0.5 * t.csi;
     double d = 0.0, ddot = 0.0;
     if (POT == MSMGB_FS_TYPE) {
         if (rho > 0.0) {
@@ -79,7 +85,7 @@ __global__ void __launch_bounds__(kBlock) k_hvp_density(DevAtoms a, DevTables t,
             ddot = 0.25 * rhod / (rho * s);
         }
     } else if (rho > 0.0) {
-        const double *T = t.dfembd + (size_t)t.kembd[ti] * t.nep;
+        const double *T = t.dfembd + (size_t)(MULTI ? t.kembd[ti] : 0) * t.nep;
         double sk = rho / t.rhod + 1.0;
         int kk = (int)(sk + 0.000001);
         if (kk + 1 > t.nembd) {
@@ -92,55 +98,77 @@ __global__ void __launch_bounds__(kBlock) k_hvp_density(DevAtoms a, DevTables t,
     } else {
         d = rho;
     }
-    a.den[i] = d;
-    dd[i] = ddot;
+    dd[i] = make_double2(d, ddot);
 }
 
+template <bool MULTI>
 __global__ void __launch_bounds__(kBlock) k_hvp_force(DevAtoms a, DevTables t, const double4_32a *v,
-                                                      const double *dd, double *hx, double *hy, double *hz)
+                                                      const double2 *dd, const double2 *pg, double *hx,
+                                                      double *hy, double *hz)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
     double gx = 0.0, gy = 0.0, gz = 0.0;
     if ((a.statu[i] & MSMGB_STATU_ACTIVE) == MSMGB_STATU_ACTIVE) {
         const DevBox &b = a.box[a.boxid[i]];
+        const double lx = b.len[0], ly = b.len[1], lz = b.len[2];
+        const double hlx = b.half[0], hly = b.half[1], hlz = b.half[2];
+        const int px = b.ifpd[0], py = b.ifpd[1], pz = b.ifpd[2];
         const double4_32a p = a.pos[i];
         const double4_32a vi = v[i];
-        const int ti = a.ityp[i] - 1;
-        const double di = a.den[i], ddi = dd[i];
+        const int ti = MULTI ? a.ityp[i] - 1 : 0;
+        const double2 e_i = dd[i];
+        const double di = e_i.x, ddi = e_i.y;
         const int kn = a.kvois[i];
         const size_t ld = (size_t)a.ld;
+        const double hcsi = 0.5 * t.csi;
         for (int w = 0; w < kn; ++w) {
             int j = __ldg(a.indi + i + w * ld);
             double4_32a q = a.pos[j];
-            double sx = mi(p.x - q.x, b.len[0], b.half[0], b.ifpd[0]);
-            double sy = mi(p.y - q.y, b.len[1], b.half[1], b.ifpd[1]);
-            double sz = mi(p.z - q.z, b.len[2], b.half[2], b.ifpd[2]);
-            double r2 = sx * sx + sy * sy + sz * sz;
-            if (r2 > t.ru2) continue;
-            int tj = a.ityp[j] - 1;
-            int k = t.kpair[tj * t.ngroup + ti];
-            int k1 = t.kpair[ti * t.ngroup + tj];
-            double y = rsqrt(r2);           // 1/R
-            double sr = rsqrt(y);           // sqrt(R)
+            // 1/R and sqrt(R) of the first pass (0 beyond RU): no second square-root pair
+            const double2 g = pg[w * ld + i];
+            if (g.x == 0.0) continue;
+            double sx = mi(p.x - q.x, lx, hlx, px);
+            double sy = mi(p.y - q.y, ly, hly, py);
+            double sz = mi(p.z - q.z, lz, hlz, pz);
+            const double y = g.x;           // 1/R
+            const double sr = g.y;          // sqrt(R)
             double sk = sr * t.csi;
             int kk = min((int)sk, t.ntab);
             double dk = sk - kk;
-            double skr = 0.5 * t.csi * y * sr;
+            double skr = hcsi * y * sr;     // dSK/dR
             double4_32a vj = v[j];
             double wx = vi.x - vj.x, wy = vi.y - vj.y, wz = vi.z - vj.z;
             double rdot = (sx * wx + sy * wy + sz * wz) * y;
-            double dj = a.den[j], ddj = dd[j];
-            double P, Ps, B, Bs, B1, B1s;
-            lerp2(t.fpotr + (size_t)k * t.ntp, kk, dk, &P, &Ps);
-            lerp2(t.fpotb + (size_t)k * t.ntp, kk, dk, &B, &Bs);
-            if (k1 != k) lerp2(t.fpotb + (size_t)k1 * t.ntp, kk, dk, &B1, &B1s);
-            else { B1 = B; B1s = Bs; }
-            double y2 = y * y;
-            double emb = B * di + B1 * dj;
-            double ft = P * y2 + emb * y;
-            double dft = (Ps * skr) * y2 - 2.0 * P * y2 * y + (Bs * di + B1s * dj) * skr * y - emb * y2;
-            double ftd = dft * rdot + (B * ddi + B1 * ddj) * y;
+            const double2 e_j = dd[j];
+            const double dj = e_j.x, ddj = e_j.y;
+            double ft, ftd;
+            if (!MULTI) {
+                double P, Ps, B, Bs;
+                const int k = 0;
+                lerp2(t.fpotr + (size_t)k * t.ntp, kk, dk, &P, &Ps);
+                lerp2(t.fpotb + (size_t)k * t.ntp, kk, dk, &B, &Bs);
+                const double dsum = di + dj;
+                const double emb = B * dsum;
+                const double py_ = P * y;
+                ft = (py_ + emb) * y;
+                // dFT/dR = y (skr (Ps y + Bs dsum) - y (2 P y + emb))
+                const double dft = y * (skr * (Ps * y + Bs * dsum) - y * (2.0 * py_ + emb));
+                ftd = dft * rdot + B * (ddi + ddj) * y;
+            } else {
+                int tj = a.ityp[j] - 1;
+                int k = t.kpair[tj * t.ngroup + ti];
+                int k1 = t.kpair[ti * t.ngroup + tj];
+                double P, Ps, B, Bs, B1, B1s;
+                lerp2(t.fpotr + (size_t)k * t.ntp, kk, dk, &P, &Ps);
+                lerp2(t.fpotb + (size_t)k * t.ntp, kk, dk, &B, &Bs);
+                lerp2(t.fpotb + (size_t)k1 * t.ntp, kk, dk, &B1, &B1s);
+                double y2 = y * y;
+                double emb = B * di + B1 * dj;
+                ft = P * y2 + emb * y;
+                double dft = (Ps * skr) * y2 - 2.0 * P * y2 * y + (Bs * di + B1s * dj) * skr * y - emb * y2;
+                ftd = dft * rdot + (B * ddi + B1 * ddj) * y;
+            }
             gx += ftd * sx + ft * wx;
             gy += ftd * sy + ft * wy;
             gz += ftd * sz + ft * wz;
@@ -165,15 +193,23 @@ static inline int nblk(long n, int b) { return (int)((n + b - 1) / b); }
 // dv: caller-order XP layout on the device; dhv: sorted SoA output (3 slabs of n)
 int launch_hvp(msmgb_ctx *c, const double *dv, double *dhv, double *v4buf, double *ddbuf)
 {
+    if (!c->hvp_pair) return set_err(c, MSMGB_ERR_ARG, "HVP pair buffer not allocated");
+    double2 *pg = (double2 *)c->hvp_pair;
     const int n = c->n;
+    const int bs = block_for(n), g = nblk(n, bs);
+    const bool multi = c->tab.ngroup > 1;
     double4_32a *v4 = (double4_32a *)v4buf;
-    k_gather_v<<<nblk(n, kBlock), kBlock, 0, c->stream>>>(dv, c->a.gid, n, v4);
-    if (c->tab.pottype == MSMGB_FS_TYPE)
-        k_hvp_density<MSMGB_FS_TYPE><<<nblk(n, kBlock), kBlock, 0, c->stream>>>(c->a, c->tab, v4, ddbuf);
-    else
-        k_hvp_density<MSMGB_EAM_TYPE><<<nblk(n, kBlock), kBlock, 0, c->stream>>>(c->a, c->tab, v4, ddbuf);
-    k_hvp_force<<<nblk(n, kBlock), kBlock, 0, c->stream>>>(c->a, c->tab, v4, ddbuf, dhv, dhv + n,
-                                                         dhv + 2 * (size_t)n);
+    double2 *dd2 = (double2 *)ddbuf;
+    k_gather_v<<<g, bs, 0, c->stream>>>(dv, c->a.gid, n, v4);
+    if (c->tab.pottype == MSMGB_FS_TYPE) {
+        if (multi) k_hvp_density<MSMGB_FS_TYPE, true><<<g, bs, 0, c->stream>>>(c->a, c->tab, v4, dd2, pg);
+        else k_hvp_density<MSMGB_FS_TYPE, false><<<g, bs, 0, c->stream>>>(c->a, c->tab, v4, dd2, pg);
+    } else {
+        if (multi) k_hvp_density<MSMGB_EAM_TYPE, true><<<g, bs, 0, c->stream>>>(c->a, c->tab, v4, dd2, pg);
+        else k_hvp_density<MSMGB_EAM_TYPE, false><<<g, bs, 0, c->stream>>>(c->a, c->tab, v4, dd2, pg);
+    }
+    if (multi) k_hvp_force<true><<<g, bs, 0, c->stream>>>(c->a, c->tab, v4, dd2, pg, dhv, dhv + n, dhv + 2 * (size_t)n);
+    else k_hvp_force<false><<<g, bs, 0, c->stream>>>(c->a, c->tab, v4, dd2, pg, dhv, dhv + n, dhv + 2 * (size_t)n);
     c->launches += 3;
     return check_launch(c, "hvp");
 }

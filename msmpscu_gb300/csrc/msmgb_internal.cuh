@@ -53,6 +53,8 @@ struct DevBox {
     double lo[3];
     double len[3];
     double half[3];
+    double ushift[3];    // L - lo: u = x + ushift is the float-float frame coordinate
+    long long klo[3], kub[3];   // order-preserving integer keys of lo and lo + L
     float lenf[3];       // float-float box length (hi, lo) and FP32 half length
     float lenlo[3];
     float halff[3];
@@ -107,6 +109,16 @@ struct DevAtoms {
     double *virial;      // [nbox][6]
 };
 
+// Threads per block for the one-thread-per-atom kernels: 256 for large systems, smaller
+// blocks when fewer than two blocks per SM (152 SMs) would be launched, so small systems
+// (16,001-atom W, 4,000-atom Cu) still spread over every SM.
+inline int block_for(int n)
+{
+    if (n >= 256 * 2 * 152) return 256;
+    if (n >= 128 * 2 * 152) return 128;
+    return 64;
+}
+
 __device__ __forceinline__ void split_ff(double u, float &h, float &l)
 {
     h = __double2float_rn(u);
@@ -116,9 +128,9 @@ __device__ __forceinline__ void split_ff(double u, float &h, float &l)
 __device__ __forceinline__ PosFF make_posff(double x, double y, double z, const DevBox &b)
 {
     PosFF p;
-    split_ff(x - b.lo[0] + b.len[0], p.hx, p.lx);
-    split_ff(y - b.lo[1] + b.len[1], p.hy, p.ly);
-    split_ff(z - b.lo[2] + b.len[2], p.hz, p.lz);
+    split_ff(x + b.ushift[0], p.hx, p.lx);
+    split_ff(y + b.ushift[1], p.hy, p.ly);
+    split_ff(z + b.ushift[2], p.hz, p.lz);
     p.hw = 0.0f;
     p.lw = 0.0f;
     return p;
@@ -158,6 +170,7 @@ struct msmgb_ctx {
     void *tab_mem = nullptr;
     double tab_rmax = 0.0;
     void *adj_mem = nullptr;           // parameter-derivative tables + accumulators
+    void *hvp_pair = nullptr;          // HVP: (1/R, sqrt R) per list entry, allocated at first use
     size_t adj_bytes = 0;
     bool have_tables = false;
     bool have_masses = false;

@@ -41,6 +41,33 @@ __device__ __forceinline__ void block_max_flush(double v, unsigned long long *ds
     }
 }
 
+// order-preserving integer key of a double: x > y <=> key(x) > key(y)
+__device__ __forceinline__ long long okey(double x)
+{
+    const long long k = __double_as_longlong(x);
+    return k ^ ((k >> 63) & 0x7fffffffffffffffLL);
+}
+
+// one coordinate of Predictor_KERNEL0 (:314-349): DIS = h v + h^2/2 a (0 if FIXPOS), x += DIS,
+// periodic wrap when x > lo + L or x < lo.  The box tests compare integer keys (same order
+// as the doubles) so they stay off the FP64 pipe, which bounds this kernel on GB300.
+__device__ __forceinline__ double advance(double x0, double v, double a, double th, double h2s2, bool fix,
+                                          int pd, double len, long long klo, long long kub, double &dis,
+                                          int &oob_hi, int &oob_lo)
+{
+    double d = fix ? 0.0 : fma(h2s2, a, th * v);
+    double x = x0 + d;
+    long long k = okey(x);
+    if (pd) {
+        if (k > kub) { x = x - len; k = okey(x); }
+        else if (k < klo) { x = x + len; k = okey(x); }
+    }
+    oob_hi |= k > kub;
+    oob_lo |= k < klo;
+    dis = d;
+    return x;
+}
+
 // mode 0: predictor only; mode 1: corrector of the previous step first when
 // flags[kFlagPending] is set (graph replay), mode 2: always fused.
 __global__ void __launch_bounds__(kBlock) k_vv(DevAtoms a, double th, int mode)
@@ -58,47 +85,34 @@ __global__ void __launch_bounds__(kBlock) k_vv(DevAtoms a, double th, int mode)
             const double icm = a.icm[a.ityp[i] - 1];
             double4_32a p = a.pos[i];
             double vx = a.vx[i], vy = a.vy[i], vz = a.vz[i];
-            double ax = a.fx[i] * icm, ay = a.fy[i] * icm, az = a.fz[i] * icm;
-            if (pend) {
-                if (!(stat & MSMGB_STATU_FIXVELX) && !(stat & MSMGB_STATU_FIXPOSX)) vx = vx + hs2 * ax;
-                if (!(stat & MSMGB_STATU_FIXVELY) && !(stat & MSMGB_STATU_FIXPOSY)) vy = vy + hs2 * ay;
-                if (!(stat & MSMGB_STATU_FIXVELZ) && !(stat & MSMGB_STATU_FIXPOSZ)) vz = vz + hs2 * az;
+            const double ax = a.fx[i] * icm, ay = a.fy[i] * icm, az = a.fz[i] * icm;
+            const bool fvx = (stat & (MSMGB_STATU_FIXVELX | MSMGB_STATU_FIXPOSX)) != 0;
+            const bool fvy = (stat & (MSMGB_STATU_FIXVELY | MSMGB_STATU_FIXPOSY)) != 0;
+            const bool fvz = (stat & (MSMGB_STATU_FIXVELZ | MSMGB_STATU_FIXPOSZ)) != 0;
+            if (pend) {                 // Correction_KERNEL of the previous step
+                if (!fvx) vx = fma(hs2, ax, vx);
+                if (!fvy) vy = fma(hs2, ay, vy);
+                if (!fvz) vz = fma(hs2, az, vz);
             }
-            double dx = th * vx + h2s2 * ax;
-            if (stat & MSMGB_STATU_FIXPOSX) dx = 0.0;
-            double x = p.x + dx;
-            if (b.ifpd[0]) {
-                if (x > b.lo[0] + b.len[0]) x = x - b.len[0];
-                else if (x < b.lo[0]) x = x + b.len[0];
-            }
-            double dy = th * vy + h2s2 * ay;
-            if (stat & MSMGB_STATU_FIXPOSY) dy = 0.0;
-            double y = p.y + dy;
-            if (b.ifpd[1]) {
-                if (y > b.lo[1] + b.len[1]) y = y - b.len[1];
-                else if (y < b.lo[1]) y = y + b.len[1];
-            }
-            double dz = th * vz + h2s2 * az;
-            if (stat & MSMGB_STATU_FIXPOSZ) dz = 0.0;
-            double z = p.z + dz;
-            if (b.ifpd[2]) {
-                if (z > b.lo[2] + b.len[2]) z = z - b.len[2];
-                else if (z < b.lo[2]) z = z + b.len[2];
-            }
-            if (!(stat & MSMGB_STATU_FIXVELX) && !(stat & MSMGB_STATU_FIXPOSX)) vx = vx + hs2 * ax;
-            if (!(stat & MSMGB_STATU_FIXVELY) && !(stat & MSMGB_STATU_FIXPOSY)) vy = vy + hs2 * ay;
-            if (!(stat & MSMGB_STATU_FIXVELZ) && !(stat & MSMGB_STATU_FIXPOSZ)) vz = vz + hs2 * az;
+            int hi = 0, lo = 0;
+            double dx, dy, dz;
+            const double x = advance(p.x, vx, ax, th, h2s2, (stat & MSMGB_STATU_FIXPOSX) != 0, b.ifpd[0],
+                                     b.len[0], b.klo[0], b.kub[0], dx, hi, lo);
+            const double y = advance(p.y, vy, ay, th, h2s2, (stat & MSMGB_STATU_FIXPOSY) != 0, b.ifpd[1],
+                                     b.len[1], b.klo[1], b.kub[1], dy, hi, lo);
+            const double z = advance(p.z, vz, az, th, h2s2, (stat & MSMGB_STATU_FIXPOSZ) != 0, b.ifpd[2],
+                                     b.len[2], b.klo[2], b.kub[2], dz, hi, lo);
+            if (!fvx) vx = fma(hs2, ax, vx);
+            if (!fvy) vy = fma(hs2, ay, vy);
+            if (!fvz) vz = fma(hs2, az, vz);
             a.pos[i] = make_double4_32a(x, y, z, p.w);
             const PosFF f = make_posff(x, y, z, b);
             a.posff[i] = f;
             a.vx[i] = vx; a.vy[i] = vy; a.vz[i] = vz;
             a.dx[i] += dx; a.dy[i] += dy; a.dz[i] += dz;
             // Predictor_KERNEL0 :372-378 (PASSBOUND is not stored, quirk Q10)
-            double ubx = b.lo[0] + b.len[0], uby = b.lo[1] + b.len[1], ubz = b.lo[2] + b.len[2];
-            if (x > ubx || y > uby || z > ubz)
-                a.statu[i] = MSMGB_STATU_OUTOFBOX | MSMGB_STATU_REFLECT;
-            else if (x < b.lo[0] || y < b.lo[1] || z < b.lo[2])
-                a.statu[i] = MSMGB_STATU_OUTOFBOX | MSMGB_STATU_TRANSMIT;
+            if (hi) a.statu[i] = MSMGB_STATU_OUTOFBOX | MSMGB_STATU_REFLECT;
+            else if (lo) a.statu[i] = MSMGB_STATU_OUTOFBOX | MSMGB_STATU_TRANSMIT;
             // displacement since the last build from the exact FP32 hi parts (the trigger
             // needs ~1e-4 A, the hi parts are within 3e-5 A of the FP64 positions)
             const float4 q = a.pos_bld[i];
@@ -146,14 +160,16 @@ static inline int nblk(long n, int b) { return (int)((n + b - 1) / b); }
 
 int launch_vv(msmgb_ctx *c, double h, int mode)
 {
-    k_vv<<<nblk(c->n, kBlock), kBlock, 0, c->stream>>>(c->a, h, mode);
+    const int bs = block_for(c->n);
+    k_vv<<<nblk(c->n, bs), bs, 0, c->stream>>>(c->a, h, mode);
     c->launches += 1;
     return check_launch(c, "integrator");
 }
 
 int launch_correct(msmgb_ctx *c, double h, bool only_if_pending)
 {
-    k_correct<<<nblk(c->n, kBlock), kBlock, 0, c->stream>>>(c->a, h, only_if_pending ? 1 : 0);
+    const int bs = block_for(c->n);
+    k_correct<<<nblk(c->n, bs), bs, 0, c->stream>>>(c->a, h, only_if_pending ? 1 : 0);
     k_clear_pending<<<1, 1, 0, c->stream>>>(c->a.flags);
     c->launches += 2;
     return check_launch(c, "corrector");
