@@ -185,9 +185,10 @@ int  msmgb_time_steps(msmgb_ctx *ctx, int nsteps, double h, float *ms, int *rebu
  * out[0] density pass, out[1] force pass, out[2] list rebuild, out[3] fused integrator
  * (timed with h = 0, which leaves the state unchanged).  No counterpart in the reference. */
 int  msmgb_time_passes(msmgb_ctx *ctx, int reps, float *out);
-/* Variants picked by the autotuner for the mixed passes: out[0] neighbours in flight per
- * thread in the density pass, out[1] in the force pass; ms (may be NULL) their time per
- * launch.  Tuning runs at the first mixed force call for a given atom count. */
+/* Variants picked by the autotuner for the mixed passes (3 entries each): out[0] density
+ * pass, out[1] force pass, out[2] fused force pass + integrator; ms (may be NULL) their
+ * time per launch.  Tuning runs at the first mixed force call / step graph for a given
+ * atom count. */
 int  msmgb_get_tuning(const msmgb_ctx *ctx, int *out, float *ms);
 /* Largest and mean neighbour count of the current list. */
 int  msmgb_list_stats(msmgb_ctx *ctx, int *maxk, double *meank);

@@ -73,6 +73,12 @@ static void free_graph(msmgb_ctx *c)
     if (c->step_graph) cudaGraphExecDestroy(c->step_graph);
     c->step_graph = nullptr;
     c->graph_n = -1;
+    cudaGraphExec_t *gs[5] = {&c->g_pre, &c->g_loop[0], &c->g_loop[1], &c->g_final[0], &c->g_final[1]};
+    for (cudaGraphExec_t *g : gs) {
+        if (*g) cudaGraphExecDestroy(*g);
+        *g = nullptr;
+    }
+    c->fg_n = -1;
 }
 
 static int use_device(msmgb_ctx *c)
@@ -225,7 +231,7 @@ extern "C" int msmgb_destroy(msmgb_ctx *c)
                     a.dx, a.dy, a.dz, a.ityp, a.statu, a.gid, a.boxid, a.den, a.epot,
                     a.den32, a.kvois, a.indi, a.pk, c->cell_of, c->perm, c->dbox, c->cm, c->icm,
                     c->flags, c->maxdisp, c->virial, c->scratch, c->cell_start,
-                    c->cell_cursor, c->scan_tmp, c->tab_mem, c->adj_mem, c->hvp_pair};
+                    c->cell_cursor, c->scan_tmp, c->tab_mem, c->adj_mem, c->hvp_pair, c->pos2, c->posff2};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     if (c->h_flags) cudaFreeHost(c->h_flags);
@@ -783,6 +789,137 @@ static int capture_step(msmgb_ctx *c, double h)
     return MSMGB_OK;
 }
 
+// ---- fused mixed step (single species): force pass + integrator in one kernel ----------
+static bool fused_mixed(const msmgb_ctx *c)
+{
+    return c->p.precision == MSMGB_PREC_MIXED && c->tab.ngroup == 1;
+}
+
+// atom view whose positions are buffer p (0: c->a's own, 1: the second buffer) and whose
+// next-step positions are the other buffer
+static DevAtoms atoms_on(const msmgb_ctx *c, const DevAtoms &base, int p)
+{
+    DevAtoms a = base;
+    a.pos = p ? c->pos2 : base.pos;
+    a.posff = p ? c->posff2 : base.posff;
+    a.pos_nxt = p ? base.pos : c->pos2;
+    a.posff_nxt = p ? base.posff : c->posff2;
+    return a;
+}
+
+static int end_capture(msmgb_ctx *c, int rc, cudaGraphExec_t *out)
+{
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+    if (rc) { if (g) cudaGraphDestroy(g); return rc; }
+    if (e != cudaSuccess) return cuda_err(c, e, "graph capture");
+    e = cudaGraphInstantiate(out, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) { *out = nullptr; return cuda_err(c, e, "graph instantiate"); }
+    return MSMGB_OK;
+}
+
+// Graphs of the fused mixed step: PRE (predictor of step 1, decision, rebuild), LOOP[p]
+// (density on buffer p, force + corrector n + predictor n+1 into buffer 1-p, decision,
+// rebuild of buffer 1-p) and FINAL[p] (density, force, corrector of the last step).
+static int capture_fused(msmgb_ctx *c, double h)
+{
+    free_graph(c);
+    if (!c->pos2) {
+        CK(cudaStreamSynchronize(c->stream), "synchronize");
+        CK(dalloc(&c->pos2, (size_t)c->cap_atoms), "cudaMalloc second position buffer");
+        CK(dalloc(&c->posff2, (size_t)c->cap_atoms), "cudaMalloc second position buffer");
+    }
+    const DevAtoms base = c->a;
+    int rc = MSMGB_OK;
+    // tune the fused kernel on the current state (h = 0 changes nothing), outside capture
+    c->a = atoms_on(c, base, 0);
+    rc = autotune_fused(c);
+    c->a = base;
+    RET(rc);
+    const int64_t l_start = c->launches;
+    int64_t l0 = c->launches;
+    CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "graph capture");
+    c->a = atoms_on(c, base, 0);
+    rc = launch_vv(c, h, 0);
+    if (!rc) rc = launch_decide(c, c->p.skin_trigger, c->p.nb_uptab);
+    if (!rc) rc = build_list(c, true);
+    c->a = base;
+    RET(end_capture(c, rc, &c->g_pre));
+    c->gk_pre = c->launches - l0;
+    for (int p = 0; p < 2; ++p) {
+        l0 = c->launches;
+        CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "graph capture");
+        c->a = atoms_on(c, base, p);
+        rc = launch_density32(c);
+        if (!rc) rc = launch_force32_vv(c, h);
+        if (!rc) rc = launch_decide(c, c->p.skin_trigger, c->p.nb_uptab);
+        c->a = atoms_on(c, base, 1 - p);
+        if (!rc) rc = build_list(c, true);
+        c->a = base;
+        RET(end_capture(c, rc, &c->g_loop[p]));
+        c->gk_loop = c->launches - l0;
+        l0 = c->launches;
+        CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "graph capture");
+        c->a = atoms_on(c, base, p);
+        rc = launch_density32(c);
+        if (!rc) rc = launch_force32(c);
+        if (!rc) rc = launch_correct(c, h, false);
+        c->a = base;
+        RET(end_capture(c, rc, &c->g_final[p]));
+        c->gk_final = c->launches - l0;
+    }
+    c->launches = l_start;            // capturing launches nothing; graph launches are counted
+    c->fg_h = h;
+    c->fg_n = c->n;
+    c->fg_tune = c->tune_dens_unroll * 16 + c->tune_force_unroll;
+    return MSMGB_OK;
+}
+
+static int ensure_graphs(msmgb_ctx *c, double h)
+{
+    if (fused_mixed(c)) {
+        if (!c->g_pre || c->fg_h != h || c->fg_n != c->n ||
+            c->fg_tune != c->tune_dens_unroll * 16 + c->tune_force_unroll)
+            return capture_fused(c, h);
+        return MSMGB_OK;
+    }
+    if (!c->step_graph || c->graph_h != h || c->graph_prec != c->p.precision || c->graph_n != c->n ||
+        c->graph_tune != c->tune_dens_unroll * 16 + c->tune_force_unroll)
+        return capture_step(c, h);
+    return MSMGB_OK;
+}
+
+// issues nsteps complete steps (the fused path ends with its own corrector)
+static int issue_steps(msmgb_ctx *c, int nsteps, double h)
+{
+    if (nsteps <= 0) return MSMGB_OK;
+    if (!fused_mixed(c)) {
+        for (int s = 0; s < nsteps; ++s) {
+            CK(cudaGraphLaunch(c->step_graph, c->stream), "graph launch");
+            c->launches += c->graph_kernels;
+        }
+        return MSMGB_OK;
+    }
+    CK(cudaGraphLaunch(c->g_pre, c->stream), "graph launch");
+    c->launches += c->gk_pre;
+    int p = 0;
+    for (int s = 1; s < nsteps; ++s) {
+        CK(cudaGraphLaunch(c->g_loop[p], c->stream), "graph launch");
+        c->launches += c->gk_loop;
+        p ^= 1;
+    }
+    CK(cudaGraphLaunch(c->g_final[p], c->stream), "graph launch");
+    c->launches += c->gk_final;
+    if (p) {   // the state ended in the second buffer: bring it back to the primary one
+        CK(cudaMemcpyAsync(c->a.pos, c->pos2, sizeof(double4_32a) * (size_t)c->n, cudaMemcpyDeviceToDevice,
+                           c->stream), "position copy");
+        CK(cudaMemcpyAsync(c->a.posff, c->posff2, sizeof(PosFF) * (size_t)c->n, cudaMemcpyDeviceToDevice,
+                           c->stream), "position copy");
+    }
+    return MSMGB_OK;
+}
+
 extern "C" int msmgb_run_steps(msmgb_ctx *c, int nsteps, double h, int *rebuilds)
 {
     if (!c || nsteps < 0) return MSMGB_ERR_ARG;
@@ -793,20 +930,16 @@ extern "C" int msmgb_run_steps(msmgb_ctx *c, int nsteps, double h, int *rebuilds
         c->force_valid = true;
     }
     CK(cudaMemsetAsync(c->flags + kFlagRebuilds, 0, sizeof(int) * 3, c->stream), "flag clear");  // rebuilds, pending, step
-    if (!c->step_graph || c->graph_h != h || c->graph_prec != c->p.precision || c->graph_n != c->n ||
-        c->graph_tune != c->tune_dens_unroll * 16 + c->tune_force_unroll)
-        RET(capture_step(c, h));
-    for (int s = 0; s < nsteps; ++s) {
-        CK(cudaGraphLaunch(c->step_graph, c->stream), "graph launch");
-        c->launches += c->graph_kernels;
-    }
-    RET(launch_correct(c, h, true));
+    RET(ensure_graphs(c, h));
+    RET(issue_steps(c, nsteps, h));
+    RET(launch_correct(c, h, true));          // no-op unless the last step left a pending half-kick
     int rc = poll_flags(c);
     if (rebuilds) *rebuilds = c->h_flags[kFlagRebuilds];
     return rc;
 }
 
-// asynchronous variant for timing loops: no final corrector, no host synchronisation
+// asynchronous variant for timing loops: no host synchronisation; nsteps = 0 only prepares
+// the list, the forces and the step graphs
 extern "C" int msmgb_enqueue_steps(msmgb_ctx *c, int nsteps, double h)
 {
     if (!c || nsteps < 0) return MSMGB_ERR_ARG;
@@ -816,14 +949,8 @@ extern "C" int msmgb_enqueue_steps(msmgb_ctx *c, int nsteps, double h)
         RET(force_passes(c, false, false));
         c->force_valid = true;
     }
-    if (!c->step_graph || c->graph_h != h || c->graph_prec != c->p.precision || c->graph_n != c->n ||
-        c->graph_tune != c->tune_dens_unroll * 16 + c->tune_force_unroll)
-        RET(capture_step(c, h));
-    for (int s = 0; s < nsteps; ++s) {
-        CK(cudaGraphLaunch(c->step_graph, c->stream), "graph launch");
-        c->launches += c->graph_kernels;
-    }
-    return MSMGB_OK;
+    RET(ensure_graphs(c, h));
+    return issue_steps(c, nsteps, h);
 }
 
 extern "C" int msmgb_finish_steps(msmgb_ctx *c, double h, int *rebuilds)
@@ -842,7 +969,7 @@ static int ensure_hvp_pair(msmgb_ctx *c)
 {
     if (c->hvp_pair) return MSMGB_OK;
     CK(cudaStreamSynchronize(c->stream), "synchronize");
-    CK(cudaMalloc(&c->hvp_pair, sizeof(double) * 2 * (size_t)c->cap_atoms * (size_t)c->p.mxkvois),
+    CK(cudaMalloc(&c->hvp_pair, sizeof(double) * 5 * (size_t)c->cap_atoms * (size_t)c->p.mxkvois),
        "HVP pair buffer");
     return MSMGB_OK;
 }
@@ -1038,6 +1165,7 @@ extern "C" int msmgb_get_tuning(const msmgb_ctx *c, int *out, float *ms)
     if (!c || !out) return MSMGB_ERR_ARG;
     out[0] = c->tune_dens_unroll;
     out[1] = c->tune_force_unroll;
-    if (ms) { ms[0] = c->tune_ms[0]; ms[1] = c->tune_ms[1]; }
+    out[2] = c->tune_fused;
+    if (ms) { ms[0] = c->tune_ms[0]; ms[1] = c->tune_ms[1]; ms[2] = c->tune_ms_fused; }
     return MSMGB_OK;
 }

@@ -393,7 +393,124 @@ __global__ void __launch_bounds__(kBlock) k_force32s(DevAtoms a, DevTables t, in
     }
 }
 
+// ---- fused force pass + integrator (mixed step) ---------------------------------------
+// The force pass of step n followed, per atom, by the corrector of step n and the predictor
+// of step n+1 (vv_atom): positions are read from a.pos / a.posff (neighbours of step n) and
+// written to a.pos_nxt / a.posff_nxt, so no thread overwrites a position another thread is
+// still gathering.  The integrator's FP64 work then runs on the FP64 pipe while other warps
+// of the same kernel keep the FP32 pipes busy, and one pass over x, v and F disappears.
+// Single species only (the multi-species mixed step keeps the separate integrator).
+template <int UNR, int MINB>
+__global__ void __launch_bounds__(kBlock, MINB) k_force32_vv(DevAtoms a, DevTables t, double th)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double dmax = 0.0;
+    if (i < a.n) {
+        const int stat = a.statu[i];
+        float fx = 0.0f, fy = 0.0f, fz = 0.0f;
+        const DevBox &bb = a.box[a.boxid[i]];
+        if ((stat & MSMGB_STATU_ACTIVE) == MSMGB_STATU_ACTIVE) {
+            const BoxF b = load_boxf(bb);
+            const PosFF pi = a.posff[i];
+            const float di = a.den32[i];
+            const int kn = a.kvois[i];
+            const size_t ld = (size_t)a.ld;
+            const int *__restrict__ nb = a.indi + i;
+            const unsigned *__restrict__ pk = a.pk + i;
+            int w = 0;
+            for (; w + UNR <= kn; w += UNR) {
+                unsigned c[UNR];
+                int j[UNR];
+#pragma unroll
+                for (int u = 0; u < UNR; ++u) {
+                    c[u] = __ldg(pk + (w + u) * ld);
+                    j[u] = __ldg(nb + (w + u) * ld);
+                }
+#pragma unroll
+                for (int u = 0; u < UNR; ++u) {
+                    if (c[u] != kSkip) {
+                        const PosFF pj = a.posff[j[u]];
+                        force_pair<false>(pi, pj, c[u], di, __ldg(a.den32 + j[u]), 0, 0, b, t, fx, fy, fz);
+                    }
+                }
+            }
+            for (; w < kn; ++w) {
+                const unsigned c0 = __ldg(pk + w * ld);
+                if (c0 != kSkip) {
+                    const int j0 = __ldg(nb + w * ld);
+                    const PosFF p0 = a.posff[j0];
+                    force_pair<false>(pi, p0, c0, di, __ldg(a.den32 + j0), 0, 0, b, t, fx, fy, fz);
+                }
+            }
+        }
+        const double Fx = (double)fx, Fy = (double)fy, Fz = (double)fz;
+        a.fx[i] = Fx;
+        a.fy[i] = Fy;
+        a.fz[i] = Fz;
+        const double4_32a p = a.pos[i];
+        if ((stat & MSMGB_STATU_ACTIVE) == MSMGB_STATU_ACTIVE) {
+            dmax = vv_atom(a, i, stat, bb, th, true, Fx, Fy, Fz, p, a.pos_nxt, a.posff_nxt);
+        } else {
+            a.pos_nxt[i] = p;
+            a.posff_nxt[i] = a.posff[i];
+        }
+    }
+    block_max_flush(dmax, a.maxdisp);
+}
+
 static inline int nblk(long n, int b) { return (int)((n + b - 1) / b); }
+
+// variant codes of the fused kernel: (neighbours in flight, minimum resident blocks)
+static void fused_variant(msmgb_ctx *c, int code, double h)
+{
+    const int g = nblk(c->n, kBlock);
+    switch (code) {
+    case 1: k_force32_vv<4, 1><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
+    case 2: k_force32_vv<2, 4><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
+    case 3: k_force32_vv<4, 4><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
+    case 4: k_force32_vv<2, 5><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
+    case 5: k_force32_vv<4, 5><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
+    default: k_force32_vv<2, 1><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
+    }
+}
+
+int launch_force32_vv(msmgb_ctx *c, double h)
+{
+    fused_variant(c, c->tune_fused, h);
+    c->launches += 1;
+    return check_launch(c, "fused force pass + integrator");
+}
+
+// Times the fused variants with h = 0, which leaves positions, velocities and DIS unchanged
+// (the next-step buffer receives the current positions), on the atom view c->a.
+int autotune_fused(msmgb_ctx *c)
+{
+    cudaEvent_t e0, e1;
+    cudaError_t err = cudaEventCreate(&e0);
+    if (err == cudaSuccess) err = cudaEventCreate(&e1);
+    if (err != cudaSuccess) return cuda_err(c, err, "autotune events");
+    float best = 1e30f;
+    int bestc = 0;
+    for (int code = 0; code < 6; ++code) {
+        for (int r = 0; r < 4; ++r) {
+            if (r == 1) cudaEventRecord(e0, c->stream);
+            fused_variant(c, code, 0.0);
+        }
+        cudaEventRecord(e1, c->stream);
+        cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (ms < best) { best = ms; bestc = code; }
+    }
+    c->tune_fused = bestc;
+    c->tune_ms_fused = best / 3.0f;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaMemsetAsync(c->a.maxdisp, 0, sizeof(unsigned long long), c->stream);
+    return check_launch(c, "autotune fused");
+}
+
+
 
 // shared-memory table window of the persistent variants (rows [kmin, ntp))
 static void smem_window(const msmgb_ctx *c, int bytes_per_row, int *kmin, int *cnt)

@@ -14,8 +14,9 @@
 //     dFT/dR = P'/R^2 - 2P/R^3 + (B' F'_i + B1' F'_j)/R - (B F'_i + B1 F'_j)/R^2,
 //     FTdot = dFT/dR Rdot + (B F'dot_i + B1 F'dot_j)/R;   hv = -Fdot.
 // The density pass is recomputed (nothing is kept from an earlier force call); its pair
-// geometry (1/R, sqrt(R)) is handed to the second pass through a per-pair buffer in the
-// list's ELL layout, so the second pass evaluates no square roots.
+// geometry (separation, 1/R, SK) is handed to the second pass through per-pair buffers in
+// the list's ELL layout, so the second pass reads no positions and evaluates no square
+// roots or image shifts.
 #include "msmgb_internal.cuh"
 
 namespace msmgb {
@@ -35,7 +36,7 @@ __device__ __forceinline__ void lerp2(const double *__restrict__ T, int kk, doub
 
 template <int POT, bool MULTI>
 __global__ void __launch_bounds__(kBlock) k_hvp_density(DevAtoms a, DevTables t, const double4_32a *v,
-                                                        double2 *dd, double2 *pg)
+                                                        double2 *dd, double4_32a *pg, double *psk)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
@@ -58,14 +59,15 @@ __global__ void __launch_bounds__(kBlock) k_hvp_density(DevAtoms a, DevTables t,
         double sz = mi(p.z - q.z, b.len[2], b.half[2], b.ifpd[2]);
         double r2 = sx * sx + sy * sy + sz * sz;
         if (r2 > t.ru2) {
-            pg[w * ld + i] = make_double2(0.0, 0.0);     // beyond RU: skipped by the second pass
+            pg[w * ld + i] = make_double4_32a(0.0, 0.0, 0.0, 0.0);   // beyond RU: skipped later
             continue;
         }
         const int k = MULTI ? t.kpair[(a.ityp[j] - 1) * t.ngroup + ti] : 0;
         double y = rsqrt(r2);
         double sr = rsqrt(y);
-        pg[w * ld + i] = make_double2(y, sr);
         double sk = sr * t.csi;
+        pg[w * ld + i] = make_double4_32a(sx, sy, sz, y);
+        psk[w * ld + i] = sk;
         int kk = min((int)sk, t.ntab);
         double dk = sk - kk;
         double4_32a vj = v[j];
@@ -103,40 +105,30 @@ __global__ void __launch_bounds__(kBlock) k_hvp_density(DevAtoms a, DevTables t,
 
 template <bool MULTI>
 __global__ void __launch_bounds__(kBlock) k_hvp_force(DevAtoms a, DevTables t, const double4_32a *v,
-                                                      const double2 *dd, const double2 *pg, double *hx,
-                                                      double *hy, double *hz)
+                                                      const double2 *dd, const double4_32a *pg,
+                                                      const double *psk, double *hx, double *hy, double *hz)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
     double gx = 0.0, gy = 0.0, gz = 0.0;
     if ((a.statu[i] & MSMGB_STATU_ACTIVE) == MSMGB_STATU_ACTIVE) {
-        const DevBox &b = a.box[a.boxid[i]];
-        const double lx = b.len[0], ly = b.len[1], lz = b.len[2];
-        const double hlx = b.half[0], hly = b.half[1], hlz = b.half[2];
-        const int px = b.ifpd[0], py = b.ifpd[1], pz = b.ifpd[2];
-        const double4_32a p = a.pos[i];
         const double4_32a vi = v[i];
         const int ti = MULTI ? a.ityp[i] - 1 : 0;
         const double2 e_i = dd[i];
         const double di = e_i.x, ddi = e_i.y;
         const int kn = a.kvois[i];
         const size_t ld = (size_t)a.ld;
-        const double hcsi = 0.5 * t.csi;
         for (int w = 0; w < kn; ++w) {
-            int j = __ldg(a.indi + i + w * ld);
-            double4_32a q = a.pos[j];
-            // 1/R and sqrt(R) of the first pass (0 beyond RU): no second square-root pair
-            const double2 g = pg[w * ld + i];
-            if (g.x == 0.0) continue;
-            double sx = mi(p.x - q.x, lx, hlx, px);
-            double sy = mi(p.y - q.y, ly, hly, py);
-            double sz = mi(p.z - q.z, lz, hlz, pz);
-            const double y = g.x;           // 1/R
-            const double sr = g.y;          // sqrt(R)
-            double sk = sr * t.csi;
+            // separation, 1/R and SK of the first pass (1/R = 0 beyond RU): the second pass
+            // needs neither the positions nor square roots
+            const double4_32a g = pg[w * ld + i];
+            if (g.w == 0.0) continue;
+            const int j = __ldg(a.indi + i + w * ld);
+            const double sx = g.x, sy = g.y, sz = g.z, y = g.w;
+            const double sk = psk[w * ld + i];
             int kk = min((int)sk, t.ntab);
             double dk = sk - kk;
-            double skr = hcsi * y * sr;     // dSK/dR
+            double skr = 0.5 * sk * y;      // dSK/dR = CSI / (2 sqrt(R)) = SK / (2 R)
             double4_32a vj = v[j];
             double wx = vi.x - vj.x, wy = vi.y - vj.y, wz = vi.z - vj.z;
             double rdot = (sx * wx + sy * wy + sz * wz) * y;
@@ -194,7 +186,8 @@ static inline int nblk(long n, int b) { return (int)((n + b - 1) / b); }
 int launch_hvp(msmgb_ctx *c, const double *dv, double *dhv, double *v4buf, double *ddbuf)
 {
     if (!c->hvp_pair) return set_err(c, MSMGB_ERR_ARG, "HVP pair buffer not allocated");
-    double2 *pg = (double2 *)c->hvp_pair;
+    double4_32a *pg = (double4_32a *)c->hvp_pair;
+    double *psk = (double *)(pg + (size_t)c->cap_atoms * (size_t)c->p.mxkvois);
     const int n = c->n;
     const int bs = block_for(n), g = nblk(n, bs);
     const bool multi = c->tab.ngroup > 1;
@@ -202,14 +195,14 @@ int launch_hvp(msmgb_ctx *c, const double *dv, double *dhv, double *v4buf, doubl
     double2 *dd2 = (double2 *)ddbuf;
     k_gather_v<<<g, bs, 0, c->stream>>>(dv, c->a.gid, n, v4);
     if (c->tab.pottype == MSMGB_FS_TYPE) {
-        if (multi) k_hvp_density<MSMGB_FS_TYPE, true><<<g, bs, 0, c->stream>>>(c->a, c->tab, v4, dd2, pg);
-        else k_hvp_density<MSMGB_FS_TYPE, false><<<g, bs, 0, c->stream>>>(c->a, c->tab, v4, dd2, pg);
+        if (multi) k_hvp_density<MSMGB_FS_TYPE, true><<<g, bs, 0, c->stream>>>(c->a, c->tab, v4, dd2, pg, psk);
+        else k_hvp_density<MSMGB_FS_TYPE, false><<<g, bs, 0, c->stream>>>(c->a, c->tab, v4, dd2, pg, psk);
     } else {
-        if (multi) k_hvp_density<MSMGB_EAM_TYPE, true><<<g, bs, 0, c->stream>>>(c->a, c->tab, v4, dd2, pg);
-        else k_hvp_density<MSMGB_EAM_TYPE, false><<<g, bs, 0, c->stream>>>(c->a, c->tab, v4, dd2, pg);
+        if (multi) k_hvp_density<MSMGB_EAM_TYPE, true><<<g, bs, 0, c->stream>>>(c->a, c->tab, v4, dd2, pg, psk);
+        else k_hvp_density<MSMGB_EAM_TYPE, false><<<g, bs, 0, c->stream>>>(c->a, c->tab, v4, dd2, pg, psk);
     }
-    if (multi) k_hvp_force<true><<<g, bs, 0, c->stream>>>(c->a, c->tab, v4, dd2, pg, dhv, dhv + n, dhv + 2 * (size_t)n);
-    else k_hvp_force<false><<<g, bs, 0, c->stream>>>(c->a, c->tab, v4, dd2, pg, dhv, dhv + n, dhv + 2 * (size_t)n);
+    if (multi) k_hvp_force<true><<<g, bs, 0, c->stream>>>(c->a, c->tab, v4, dd2, pg, psk, dhv, dhv + n, dhv + 2 * (size_t)n);
+    else k_hvp_force<false><<<g, bs, 0, c->stream>>>(c->a, c->tab, v4, dd2, pg, psk, dhv, dhv + n, dhv + 2 * (size_t)n);
     c->launches += 3;
     return check_launch(c, "hvp");
 }

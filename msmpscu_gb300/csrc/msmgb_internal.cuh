@@ -89,6 +89,8 @@ struct DevTables {
 struct DevAtoms {
     double4_32a *pos;
     PosFF *posff;
+    double4_32a *pos_nxt;    // fused mixed step: positions of step n+1 (second buffer)
+    PosFF *posff_nxt;
     double *vx, *vy, *vz;
     double *fx, *fy, *fz;
     double *dx, *dy, *dz;
@@ -136,6 +138,102 @@ __device__ __forceinline__ PosFF make_posff(double x, double y, double z, const 
     return p;
 }
 
+__device__ __forceinline__ float mi32f(float s, float len, float half, int pd)
+{
+    return (pd && fabsf(s) > half) ? s - copysignf(len, s) : s;
+}
+
+// order-preserving integer key of a double: x > y <=> key(x) > key(y)
+__device__ __forceinline__ long long okey(double x)
+{
+    const long long k = __double_as_longlong(x);
+    return k ^ ((k >> 63) & 0x7fffffffffffffffLL);
+}
+
+// one coordinate of Predictor_KERNEL0 (MD_DiffScheme_GPU.F90:314-349): DIS = h v + h^2/2 a
+// (0 if FIXPOS), x += DIS, periodic wrap when x > lo + L or x < lo.  The box tests compare
+// integer keys (same order as the doubles) so they stay off the FP64 pipe.
+__device__ __forceinline__ double advance(double x0, double v, double a, double th, double h2s2, bool fix,
+                                          int pd, double len, long long klo, long long kub, double &dis,
+                                          int &oob_hi, int &oob_lo)
+{
+    double d = fix ? 0.0 : fma(h2s2, a, th * v);
+    double x = x0 + d;
+    long long k = okey(x);
+    if (pd) {
+        if (k > kub) { x = x - len; k = okey(x); }
+        else if (k < klo) { x = x + len; k = okey(x); }
+    }
+    oob_hi |= k > kub;
+    oob_lo |= k < klo;
+    dis = d;
+    return x;
+}
+
+// Corrector of step n (v += h/2 F/m) followed by the predictor of step n+1 for one active
+// atom (Correction_KERNEL :741-749 then Predictor_KERNEL0 :290-378); positions are read from
+// pin and written to pout / fout.  Returns the squared displacement since the last build.
+__device__ __forceinline__ double vv_atom(const DevAtoms &a, int i, int stat, const DevBox &b, double th,
+                                          bool corrector, double fx, double fy, double fz,
+                                          const double4_32a &p, double4_32a *pout, PosFF *fout)
+{
+    const double hs2 = th * 0.5, h2s2 = th * th * 0.5;
+    const double icm = a.icm[a.ityp[i] - 1];
+    double vx = a.vx[i], vy = a.vy[i], vz = a.vz[i];
+    const double ax = fx * icm, ay = fy * icm, az = fz * icm;
+    const bool fvx = (stat & (MSMGB_STATU_FIXVELX | MSMGB_STATU_FIXPOSX)) != 0;
+    const bool fvy = (stat & (MSMGB_STATU_FIXVELY | MSMGB_STATU_FIXPOSY)) != 0;
+    const bool fvz = (stat & (MSMGB_STATU_FIXVELZ | MSMGB_STATU_FIXPOSZ)) != 0;
+    if (corrector) {
+        if (!fvx) vx = fma(hs2, ax, vx);
+        if (!fvy) vy = fma(hs2, ay, vy);
+        if (!fvz) vz = fma(hs2, az, vz);
+    }
+    int hi = 0, lo = 0;
+    double dx, dy, dz;
+    const double x = advance(p.x, vx, ax, th, h2s2, (stat & MSMGB_STATU_FIXPOSX) != 0, b.ifpd[0], b.len[0],
+                             b.klo[0], b.kub[0], dx, hi, lo);
+    const double y = advance(p.y, vy, ay, th, h2s2, (stat & MSMGB_STATU_FIXPOSY) != 0, b.ifpd[1], b.len[1],
+                             b.klo[1], b.kub[1], dy, hi, lo);
+    const double z = advance(p.z, vz, az, th, h2s2, (stat & MSMGB_STATU_FIXPOSZ) != 0, b.ifpd[2], b.len[2],
+                             b.klo[2], b.kub[2], dz, hi, lo);
+    if (!fvx) vx = fma(hs2, ax, vx);
+    if (!fvy) vy = fma(hs2, ay, vy);
+    if (!fvz) vz = fma(hs2, az, vz);
+    pout[i] = make_double4_32a(x, y, z, p.w);
+    const PosFF f = make_posff(x, y, z, b);
+    fout[i] = f;
+    a.vx[i] = vx; a.vy[i] = vy; a.vz[i] = vz;
+    a.dx[i] += dx; a.dy[i] += dy; a.dz[i] += dz;
+    // PASSBOUND is not stored (reference quirk, :372-378)
+    if (hi) a.statu[i] = MSMGB_STATU_OUTOFBOX | MSMGB_STATU_REFLECT;
+    else if (lo) a.statu[i] = MSMGB_STATU_OUTOFBOX | MSMGB_STATU_TRANSMIT;
+    // displacement since the last build from the exact FP32 hi parts (the trigger needs
+    // ~1e-4 A, the hi parts are within 3e-5 A of the FP64 positions)
+    const float4 q = a.pos_bld[i];
+    const float ex = mi32f(f.hx - q.x, b.lenf[0], b.halff[0], b.ifpd[0]);
+    const float ey = mi32f(f.hy - q.y, b.lenf[1], b.halff[1], b.ifpd[1]);
+    const float ez = mi32f(f.hz - q.z, b.lenf[2], b.halff[2], b.ifpd[2]);
+    return (double)(ex * ex + ey * ey + ez * ez);
+}
+
+// block max of a non-negative double, one atomicMax (on its bit pattern) per block
+__device__ __forceinline__ void block_max_flush(double v, unsigned long long *dst)
+{
+    __shared__ double sm[32];
+    const unsigned full = 0xffffffffu;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(full, v, o));
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double m = sm[0];
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) m = fmax(m, sm[w]);
+        // non-negative doubles order like their bit patterns
+        if (m > 0.0) atomicMax(dst, (unsigned long long)__double_as_longlong(m));
+    }
+}
+
 }  // namespace msmgb
 
 struct msmgb_ctx {
@@ -170,7 +268,7 @@ struct msmgb_ctx {
     void *tab_mem = nullptr;
     double tab_rmax = 0.0;
     void *adj_mem = nullptr;           // parameter-derivative tables + accumulators
-    void *hvp_pair = nullptr;          // HVP: (1/R, sqrt R) per list entry, allocated at first use
+    void *hvp_pair = nullptr;          // HVP: separation, 1/R and SK per list entry (40 B), at first use
     size_t adj_bytes = 0;
     bool have_tables = false;
     bool have_masses = false;
@@ -180,9 +278,18 @@ struct msmgb_ctx {
     bool den_is32 = false;             // the last density pass was the mixed one
 
     // autotuned launch variants of the mixed passes (neighbours in flight per thread)
-    int tune_dens_unroll = 2, tune_force_unroll = 2;
+    int tune_dens_unroll = 2, tune_force_unroll = 2, tune_fused = 0;
+    float tune_ms_fused = 0.f;
     int tuned_n = -1;
     float tune_ms[2] = {0.f, 0.f};
+
+    // second position buffers and graphs of the fused mixed step
+    double4_32a *pos2 = nullptr;
+    msmgb::PosFF *posff2 = nullptr;
+    cudaGraphExec_t g_pre = nullptr, g_loop[2] = {nullptr, nullptr}, g_final[2] = {nullptr, nullptr};
+    int64_t gk_pre = 0, gk_loop = 0, gk_final = 0;
+    double fg_h = 0.0;
+    int fg_n = -1, fg_tune = -1;
 
     // CUDA graph of one MD step
     cudaGraphExec_t step_graph = nullptr;
@@ -208,6 +315,8 @@ int launch_density(msmgb_ctx *c, bool want_epot);
 int launch_force(msmgb_ctx *c, bool want_virial);
 int launch_density32(msmgb_ctx *c);
 int launch_force32(msmgb_ctx *c);
+int launch_force32_vv(msmgb_ctx *c, double h);
+int autotune_fused(msmgb_ctx *c);
 int autotune_mixed(msmgb_ctx *c);
 int launch_hvp(msmgb_ctx *c, const double *dv, double *dhv, double *v4buf, double *ddbuf);
 int launch_adjoint(msmgb_ctx *c, const double *ft, const double *dtab, double *w4buf, double *ddbuf,

@@ -281,11 +281,11 @@ class Engine:
         return dict(density=out[0], force=out[1], nlist=out[2], vv=out[3])
 
     def tuning(self):
-        out = (C.c_int * 2)()
-        ms = (C.c_float * 2)()
+        out = (C.c_int * 3)()
+        ms = (C.c_float * 3)()
         self._ck(self.lib.msmgb_get_tuning(self.ctx, out, ms))
-        return {"density_unroll": out[0], "force_unroll": out[1],
-                "density_ms": ms[0], "force_ms": ms[1]}
+        return {"density_variant": out[0], "force_variant": out[1], "fused_variant": out[2],
+                "density_ms": ms[0], "force_ms": ms[1], "fused_ms": ms[2]}
 
     def list_stats(self):
         mk = C.c_int()
