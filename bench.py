@@ -263,7 +263,8 @@ def bytes_model(kmean):
     dens = 4.0 * kmean + 24.0 + 8.0
     force = 4.0 * kmean + 24.0 + 8.0 + 24.0
     vv = 5 * 24.0 + 24.0
-    return dict(density=dens, force=force, vv=vv, step=dens + force + vv)
+    # fused force pass + integrator: the force it writes is not read back
+    return dict(density=dens, force=force, vv=vv, fused=force + vv - 24.0, step=dens + force + vv)
 
 
 def cpu_baseline(pos, vel, L, nthreads, sample_steps=2):
@@ -373,7 +374,8 @@ def run_ours(args):
     tune = e.tuning() if prec == "mixed" else None
     bm = bytes_model(kmean)
     hbm, peak_kind = peaks()
-    dom = "force" if passes["force"] >= passes["density"] else "density"
+    cands = ["density", "fused"] if passes.get("fused", 0.0) > 0.0 else ["density", "force"]
+    dom = max(cands, key=lambda k: passes[k])
     achieved = bm[dom] * n / (passes[dom] * 1e-3) / 1e9
     traffic = read_traffic(prec, dom)
 

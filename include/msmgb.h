@@ -181,9 +181,10 @@ int  msmgb_finish_steps(msmgb_ctx *ctx, double h, int *rebuilds);
  * on the context stream, synchronised on both sides) in *ms.  No counterpart in the
  * reference (it times with host CPU_TIME, MD_Method_GenericMD_GPU.F90:246). */
 int  msmgb_time_steps(msmgb_ctx *ctx, int nsteps, double h, float *ms, int *rebuilds);
-/* Average device time (ms) of one launch of each pass over `reps` launches:
- * out[0] density pass, out[1] force pass, out[2] list rebuild, out[3] fused integrator
- * (timed with h = 0, which leaves the state unchanged).  No counterpart in the reference. */
+/* Average device time (ms) of one launch of each pass over `reps` launches (out has 5
+ * entries): out[0] density pass, out[1] force pass, out[2] list rebuild, out[3] integrator,
+ * out[4] fused mixed force pass + integrator (0 when not in use); the integrator kernels are
+ * timed with h = 0, which leaves the state unchanged.  No counterpart in the reference. */
 int  msmgb_time_passes(msmgb_ctx *ctx, int reps, float *out);
 /* Variants picked by the autotuner for the mixed passes (3 entries each): out[0] density
  * pass, out[1] force pass, out[2] fused force pass + integrator; ms (may be NULL) their

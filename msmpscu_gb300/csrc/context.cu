@@ -1065,19 +1065,23 @@ extern "C" int msmgb_time_steps(msmgb_ctx *c, int nsteps, double h, float *ms, i
     return msmgb_finish_steps(c, h, rebuilds);
 }
 
-// Average device time of one launch of each pass, in ms: out[0] density, out[1] force,
-// out[2] full list rebuild, out[3] fused integrator (timed with h = 0 so the state is
-// unchanged while the memory traffic is that of a real step).
+// Average device time (ms) of one launch of each pass: out[0] density, out[1] force,
+// out[2] full list rebuild, out[3] integrator (timed with h = 0 so the state is unchanged
+// while the memory traffic is that of a real step), out[4] the fused mixed force pass +
+// integrator of the step graph (h = 0 as well; 0 when the fused step is not in use).
 extern "C" int msmgb_time_passes(msmgb_ctx *c, int reps, float *out)
 {
     if (!c || !out || reps < 1) return MSMGB_ERR_ARG;
     RET(ready_for_force(c));
     if (!c->have_masses) return set_err(c, MSMGB_ERR_ARG, "no masses: call msmgb_set_masses");
     const bool mixed = c->p.precision == MSMGB_PREC_MIXED;
+    const bool fused = fused_mixed(c) && c->pos2;
     cudaEvent_t ev[2];
     CK(cudaEventCreate(&ev[0]), "event");
     CK(cudaEventCreate(&ev[1]), "event");
-    for (int which = 0; which < 4; ++which) {
+    out[4] = 0.0f;
+    for (int which = 0; which < 5; ++which) {
+        if (which == 4 && !fused) break;
         double total = 0.0;
         for (int r = 0; r < reps + 1; ++r) {
             CK(cudaStreamSynchronize(c->stream), "synchronize");
@@ -1086,7 +1090,13 @@ extern "C" int msmgb_time_passes(msmgb_ctx *c, int reps, float *out)
             if (which == 0) rc = mixed ? launch_density32(c) : launch_density(c, false);
             else if (which == 1) rc = mixed ? launch_force32(c) : launch_force(c, false);
             else if (which == 2) rc = build_list(c, false);
-            else rc = launch_vv(c, 0.0, 2);
+            else if (which == 3) rc = launch_vv(c, 0.0, 2);
+            else {
+                const DevAtoms base = c->a;
+                c->a = atoms_on(c, base, 0);
+                rc = launch_force32_vv(c, 0.0);
+                c->a = base;
+            }
             if (rc) return rc;
             CK(cudaEventRecord(ev[1], c->stream), "event");
             CK(cudaEventSynchronize(ev[1]), "event");

@@ -145,6 +145,28 @@ class Engine:
         s = table.struct()
         self._ck(self.lib.msmgb_init_forcetable(self.ctx, C.byref(s)))
 
+    def init_forcetable_raw(self, pottype, ntab, nkind, rmax, ru, potr, fpotr, potb, fpotb, ngroup,
+                            kpair, nembd=0, nkind1=0, rhod=1.0, fembd=None, dfembd=None, kembd=None):
+        """Tables already in the reference layout (NKIND, NTAB) column-major, i.e. numpy
+        arrays of shape (NTAB, NKIND) in C order; kpair (NGROUP, NGROUP) 1-based ids with
+        KPAIR(i, j) at kpair[i-1, j-1]."""
+        keep = [np.ascontiguousarray(a, dtype=np.float64) for a in (potr, fpotr, potb, fpotb)]
+        kp = np.ascontiguousarray(np.asarray(kpair, np.int32).T)      # column-major (i fastest)
+        t = L.ForceTable()
+        t.pottype, t.ntab, t.nkind, t.rmax, t.ru = pottype, int(ntab), int(nkind), float(rmax), float(ru)
+        t.potr, t.fpotr, t.potb, t.fpotb = (_d(a) for a in keep)
+        t.ngroup = int(ngroup)
+        t.kpair = _i(kp)
+        if pottype == L.EAM_TYPE:
+            ke = np.ascontiguousarray(kembd, np.int32)
+            fe = np.ascontiguousarray(fembd, np.float64)
+            dfe = np.ascontiguousarray(dfembd, np.float64)
+            keep += [ke, fe, dfe]
+            t.nembd, t.nkind1, t.rhod = int(nembd), int(nkind1), float(rhod)
+            t.fembd, t.dfembd, t.kembd = _d(fe), _d(dfe), _i(ke)
+        self._raw_keep = (keep, kp)
+        self._ck(self.lib.msmgb_init_forcetable(self.ctx, C.byref(t)))
+
     def clear_forcetable(self):
         self._ck(self.lib.msmgb_clear_forcetable(self.ctx))
 
@@ -276,9 +298,9 @@ class Engine:
         return float(ms.value), nr.value
 
     def time_passes(self, reps=5):
-        out = (C.c_float * 4)()
+        out = (C.c_float * 5)()
         self._ck(self.lib.msmgb_time_passes(self.ctx, int(reps), out))
-        return dict(density=out[0], force=out[1], nlist=out[2], vv=out[3])
+        return dict(density=out[0], force=out[1], nlist=out[2], vv=out[3], fused=out[4])
 
     def tuning(self):
         out = (C.c_int * 3)()

@@ -120,6 +120,28 @@ class Tables:
         self.s = s
 
 
+class RawTables:
+    """Multi-kind tables in the reference layout: arrays (NTAB, NKIND) C-order = Fortran
+    (NKIND, NTAB); kpair (NGROUP, NGROUP) with KPAIR(i, j) at kpair[i-1, j-1]."""
+
+    def __init__(self, pottype, ntab, nkind, rmax, ru, potr, fpotr, potb, fpotb, kpair):
+        self.keep = [f64(a) for a in (potr, fpotr, potb, fpotb)] + [np.zeros(1), np.zeros(1)]
+        ng = np.asarray(kpair).shape[0]
+        self.kpair = i32(np.asarray(kpair, np.int32).T)
+        self.kembd = i32(np.ones(ng))
+        s = OrcTables()
+        s.pottype, s.ntab, s.nkind = pottype, ntab, nkind
+        s.csi = float(ntab) / np.sqrt(rmax)
+        s.ru2 = ru * ru
+        s.potr, s.fpotr, s.potb, s.fpotb = (_d(a) for a in self.keep[:4])
+        s.nembd, s.nkind1, s.rhod = 1, 1, 1.0
+        s.fembd, s.dfembd = _d(self.keep[4]), _d(self.keep[5])
+        s.ngroup = ng
+        s.kpair = _i(self.kpair)
+        s.kembd = _i(self.kembd)
+        self.s = s
+
+
 def make_box(lo, length, ifpd=(1, 1, 1)):
     b = OrcBox()
     for k in range(3):

@@ -1,0 +1,122 @@
+"""GPU edge cases against the oracle: two atom types with asymmetric density tables
+(KPAIR(1,2) != KPAIR(2,1)), non-periodic directions with atoms leaving the box, and the
+FIXPOS / FIXVEL status bits of the integrator."""
+import numpy as np
+import pytest
+
+from msmpscu_gb300 import Engine, ForceTable, lattice as lt
+from msmpscu_gb300 import _lib as L
+from tests.helpers import cu_tables, rel_err, sorted_sets, CR_PRM
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-10
+
+
+def _two_species_tables(oracle, ntab=10000):
+    """Four CR tables: 1-1, 2-2, and two different cross densities 1<-2 and 2<-1."""
+    base = np.array(CR_PRM)
+    prms = [base, base * np.array([1.1, 0.95, 1.0, 1.05, 1.0]),
+            base * np.array([1.05, 1.02, 0.98, 1.0, 1.0]), base * np.array([1.05, 0.97, 0.98, 1.03, 1.0])]
+    cols = {k: [] for k in ("potr", "fpotr", "potb", "fpotb")}
+    for p in prms:
+        t = oracle.make_tables(oracle.POT_CR, p, lt.CU_RC, ntab, ntab, 20.0, want_embed=False)
+        for k in cols:
+            cols[k].append(t[k])
+    arr = {k: np.stack(v, 1) for k, v in cols.items()}          # (NTAB, NKIND)
+    kpair = np.array([[1, 3], [4, 2]])                          # KPAIR(1,2)=3, KPAIR(2,1)=4
+    return arr, kpair
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_two_species_asymmetric_density(oracle, precision):
+    pos, vel, L_ = lt.cu_config(8, 0.05, 300.0, 31)
+    n = len(pos)
+    rng = np.random.default_rng(3)
+    ityp = (rng.random(n) < 0.3).astype(np.int32) + 1
+    arr, kpair = _two_species_tables(oracle)
+    ot = oracle.RawTables(oracle.FS, 10000, 4, lt.CU_RC, lt.CU_RC, arr["potr"], arr["fpotr"],
+                          arr["potb"], arr["fpotb"], kpair)
+    box = oracle.make_box([0, 0, 0], L_)
+    st = np.ones(n, np.int32)
+    kv, ind = oracle.nlist(pos, st, box, lt.CU_RC_NL, 96)
+    ref = oracle.force(pos, ityp, st, box, kv, ind, ot)
+    e = Engine(n, lt.CU_RC_NL, mxkvois=64, precision=precision)
+    e.init_forcetable_raw(L.FS_TYPE, 10000, 4, lt.CU_RC, lt.CU_RC, arr["potr"], arr["fpotr"],
+                          arr["potb"], arr["fpotb"], 2, kpair)
+    e.set_masses([lt.CU_MASS, 1.3 * lt.CU_MASS])
+    e.copyin([(n, (0, 0, 0), tuple(L_), (1, 1, 1))], pos, vel, ityp=ityp)
+    e.calforce()
+    f = e.get_force()
+    if precision == "fp64":
+        assert rel_err(f, ref["f"]) < TOL
+        vir = e.calptensor()[0]
+        assert rel_err(vir, ref["vir"]) < TOL
+        e.calepot()
+        assert rel_err(e.get_epot(), ref["epot"]) < TOL
+    else:
+        assert np.linalg.norm(f - ref["f"]) / np.linalg.norm(ref["f"]) < 1e-6
+    # MD with two masses (unfused mixed path / FP64 graph)
+    cm = np.array([lt.CU_MASS, 1.3 * lt.CU_MASS])
+    ox, ov, _, _, _ = oracle.md(pos, vel, ityp, st, box, ot, cm, 1.0, 20, lt.CU_RC_NL, skin_trigger=0.15,
+                                mxkvois=96)
+    e.run_steps(20, 1.0)
+    gx, gv, _, _ = e.get_state()
+    dx = gx - ox
+    dx -= np.round(dx / L_) * L_
+    assert np.abs(dx).max() < (1e-9 if precision == "fp64" else 1e-6)
+    e.close()
+
+
+def test_non_periodic_z_atoms_leave_box(oracle):
+    """z not periodic: a slab whose top atoms fly out; statuses and forces match the oracle."""
+    pos, vel, L_ = lt.cu_config(6, 0.02, 300.0, 41)
+    n = len(pos)
+    Lz = L_[2] + 4.0                      # vacuum above the slab
+    top = pos[:, 2] > L_[2] - 2.0
+    vel = vel.copy()
+    vel[top, 2] = 0.2                     # 0.2 A/fs upward
+    box_len = np.array([L_[0], L_[1], Lz])
+    t = cu_tables(oracle)
+    obox = oracle.make_box([0, 0, 0], box_len, ifpd=(1, 1, 0))
+    st = np.ones(n, np.int32)
+    ox, ov, of, ost, _ = oracle.md(pos, vel, np.ones(n, np.int32), st, obox, t, np.array([lt.CU_MASS]),
+                                   1.0, 40, lt.CU_RC_NL, skin_trigger=0.15, mxkvois=96)
+    e = Engine(n, lt.CU_RC_NL, mxkvois=64)
+    e.init_forcetable(ForceTable.cleri_rosato(**lt.CU_CR, rc=lt.CU_RC))
+    e.set_masses([lt.CU_MASS])
+    e.copyin([(n, (0, 0, 0), tuple(box_len), (1, 1, 0))], pos, vel)
+    e.run_steps(40, 1.0)
+    gx, gv, gst, _ = e.get_state()
+    assert np.array_equal(gst, ost)
+    assert (ost & L.STATU_OUTOFBOX).sum() > 0
+    act = (ost & L.STATU_ACTIVE) == L.STATU_ACTIVE
+    dx = gx - ox
+    dx[:, :2] -= np.round(dx[:, :2] / box_len[:2]) * box_len[:2]
+    assert np.abs(dx[act]).max() < 1e-8
+    e.close()
+
+
+def test_fixpos_fixvel_bits(oracle):
+    pos, vel, L_ = lt.cu_config(6, 0.05, 600.0, 51)
+    n = len(pos)
+    st = np.ones(n, np.int32)
+    st[::5] |= L.STATU_FIXPOSX | L.STATU_FIXPOSY | L.STATU_FIXPOSZ
+    st[1::7] |= L.STATU_FIXVELZ
+    t = cu_tables(oracle)
+    box = oracle.make_box([0, 0, 0], L_)
+    ox, ov, _, ost, _ = oracle.md(pos, vel, np.ones(n, np.int32), st, box, t, np.array([lt.CU_MASS]),
+                                  1.0, 30, lt.CU_RC_NL, skin_trigger=0.15, mxkvois=96)
+    e = Engine(n, lt.CU_RC_NL, mxkvois=64)
+    e.init_forcetable(ForceTable.cleri_rosato(**lt.CU_CR, rc=lt.CU_RC))
+    e.set_masses([lt.CU_MASS])
+    e.copyin([(n, (0, 0, 0), tuple(L_), (1, 1, 1))], pos, vel, statu=st)
+    e.run_steps(30, 1.0)
+    gx, gv, gst, _ = e.get_state()
+    assert np.array_equal(gst, ost)
+    assert np.array_equal(gx[::5], pos[::5])                 # fixed atoms did not move
+    assert np.array_equal(gv[1::7, 2], vel[1::7, 2])         # fixed z-velocities unchanged
+    dx = gx - ox
+    dx -= np.round(dx / L_) * L_
+    assert np.abs(dx).max() < 1e-8
+    e.close()
