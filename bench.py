@@ -148,7 +148,7 @@ def precision_compare(e, box, pos, vel, steps):
     return err_norm, err_max, len(pos) * steps / (ms64 / 1e3)
 
 
-def batched_c3(steps, steps_perbox, device=0):
+def batched_uneven_boxes(steps, steps_perbox, device=0):
     """512 independent periodic Cu boxes, edge uniform in 4..12 fcc cells, 0-3 vacancies,
     300-1200 K: all boxes in one context (one launch per pass over every box, the whole step
     one CUDA graph) against one context per box (512 graphs per step, each on its own
@@ -200,7 +200,7 @@ def batched_c3(steps, steps_perbox, device=0):
     return out
 
 
-def hvp_c4(device=0):
+def hvp_w_dumbbell(device=0):
     """bcc W 20^3 cells + <111> dumbbell (16,001 atoms), Marinica EAM2: device time of one
     HVP against one FP64 force call on the same state."""
     from msmpscu_gb300 import Engine, ForceTable, lattice as lt
@@ -216,7 +216,7 @@ def hvp_c4(device=0):
             "hvp_cost_force_calls": ms_hvp / ms_force}
 
 
-def adjoint_c5(device=0):
+def adjoint_cu_snapshots(device=0):
     """64 fcc Cu snapshots of 4,000 atoms (sigma 0.1 A), targets from parameters x 1.02:
     wall time of one adjoint call (FP64 forces + adjoint passes + host derivative tables)
     against one FP64 force call with copy-out."""
@@ -407,9 +407,9 @@ def run_ours(args):
     extras = {}
     if not args.no_extras:
         e.close()
-        extras["batched_c3"] = batched_c3(max(10, min(args.steps, 100)), 20, device)
-        extras["hvp_c4"] = hvp_c4(device)
-        extras["adjoint_c5"] = adjoint_c5(device)
+        extras["batched_boxes"] = batched_uneven_boxes(max(10, min(args.steps, 100)), 20, device)
+        extras["hvp"] = hvp_w_dumbbell(device)
+        extras["adjoint"] = adjoint_cu_snapshots(device)
         e = None
 
     cpu = None

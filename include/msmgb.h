@@ -128,13 +128,20 @@ int  msmgb_clear_forcetable(msmgb_ctx *ctx);
 int  msmgb_calforce(msmgb_ctx *ctx);
 /* pCalPTensor: CALPTENSOR_*_Force_Table2A_DEV (MD_FS_ForceTable_GPU.F90:1348-1411):
  * forces plus the 3x3 virial of every box; vtensor receives 9*nbox values (row-major per
- * box), NOT divided by the number of boxes (reference quirk Q9, :1462-1463). */
+ * box), NOT divided by the number of boxes as the reference's copy-out does (:1462-1463). */
 int  msmgb_calptensor(msmgb_ctx *ctx, double *vtensor);
 /* pCalEpot: CALEPOT_*_Force_Table2A_DEV (MD_FS_ForceTable_GPU.F90:1720-1742): per-atom
  * potential energy, kept on the device (msmgb_copyout_epot). */
 int  msmgb_calepot(msmgb_ctx *ctx);
 /* pCalEDen: CALDEN_*_Force_Table2A_DEV (MD_FS_ForceTable_GPU.F90:875-930): F'(rho) only */
 int  msmgb_calden(msmgb_ctx *ctx);
+/* pCalAVStress: Cal_FS/EAM_AtomicStressTensor_DEV (MD_FS_ForceTable_GPU.F90:2044-2076,
+ * MD_EAM_ForceTable_GPU.F90:2073-2106; kernels :1746-1965 / :1775-1994): per-atom virial
+ * tensor AP_i(a,b) = sum_j FORTOT s_a s_b (cubic boxes; zero on inactive atoms).  Unlike the
+ * reference, which reads the F'(rho) of an earlier force call, this runs its own FP64
+ * density pass first.  ap receives 9 slabs of N doubles, component 3a+b (the reference's
+ * AP(NAPDEV, 9) layout), in the caller's order (MSMGB_ORDER_ORIGINAL) or sorted order. */
+int  msmgb_cal_atomic_stress(msmgb_ctx *ctx, double *ap, int order);
 
 /* ---- state transfer (MD_Globle_Variables_GPU.F90 CopyIn/CopyOut_SimBox_DEV) -------------- */
 /* Uploads a batch of boxes (nbox >= 1, boxes concatenated in order).  xp and xp1 are

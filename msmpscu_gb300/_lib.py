@@ -69,6 +69,7 @@ SIGNATURES = [
     ("msmgb_calptensor", C.c_int, [C.c_void_p, _dp]),
     ("msmgb_calepot", C.c_int, [C.c_void_p]),
     ("msmgb_calden", C.c_int, [C.c_void_p]),
+    ("msmgb_cal_atomic_stress", C.c_int, [C.c_void_p, _dp, C.c_int]),
     ("msmgb_copyin_simbox", C.c_int, [C.c_void_p, C.c_int, C.POINTER(Box), _ip, _ip, _dp, _dp]),
     ("msmgb_set_masses", C.c_int, [C.c_void_p, C.c_int, _dp]),
     ("msmgb_copyout_simbox", C.c_int, [C.c_void_p, _dp, _dp, _ip, _dp, C.c_int]),

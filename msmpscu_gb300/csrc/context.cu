@@ -329,7 +329,7 @@ extern "C" int msmgb_init_forcetable(msmgb_ctx *c, const msmgb_forcetable *ft)
             if (id < 1 || id > ft->nkind1) return set_err(c, MSMGB_ERR_ARG, "KEMBD id out of range");
             t.kembd[i] = id - 1;
         }
-    // padded rows: index 0 -> 0, 1..NTAB -> table, NTAB+1 -> T(NTAB) (quirk Q6)
+    // padded rows: index 0 -> 0, 1..NTAB -> table, NTAB+1 -> T(NTAB) (read with DK = 0 when r = Rmax)
     const size_t rowp = (size_t)t.ntp, nk = (size_t)t.nkind, nk1 = (size_t)t.nkind1, nep = (size_t)t.nep;
     const size_t nd = 4 * nk * rowp + (eam ? 2 * nk1 * nep : 0);
     std::vector<double> hd(nd, 0.0);
@@ -742,6 +742,19 @@ extern "C" int msmgb_calden(msmgb_ctx *c)
     return poll_flags(c);
 }
 
+extern "C" int msmgb_cal_atomic_stress(msmgb_ctx *c, double *ap, int order)
+{
+    if (!c || !ap) return MSMGB_ERR_ARG;
+    RET(ready_for_force(c));
+    // 72 B per atom fit in the 100 B per atom of the scratch buffer
+    const size_t bytes = sizeof(double) * 9 * (size_t)c->n;
+    double *tmp = (double *)c->scratch;
+    RET(launch_density(c, false));
+    RET(launch_stress(c, order == MSMGB_ORDER_SORTED, tmp));
+    CK(cudaMemcpyAsync(ap, tmp, bytes, cudaMemcpyDeviceToHost, c->stream), "stress copy-out");
+    return poll_flags(c);
+}
+
 // ---- integrator -------------------------------------------------------------------------------
 extern "C" int msmgb_predictor(msmgb_ctx *c, double h)
 {
@@ -785,7 +798,7 @@ static int capture_step(msmgb_ctx *c, double h)
     c->graph_h = h;
     c->graph_prec = c->p.precision;
     c->graph_n = c->n;
-    c->graph_tune = c->tune_dens_unroll * 16 + c->tune_force_unroll;
+    c->graph_tune = c->tune_dens_unroll * 64 + c->tune_force_unroll;
     return MSMGB_OK;
 }
 
@@ -872,7 +885,7 @@ static int capture_fused(msmgb_ctx *c, double h)
     c->launches = l_start;            // capturing launches nothing; graph launches are counted
     c->fg_h = h;
     c->fg_n = c->n;
-    c->fg_tune = c->tune_dens_unroll * 16 + c->tune_force_unroll;
+    c->fg_tune = c->tune_dens_unroll * 64 + c->tune_force_unroll;
     return MSMGB_OK;
 }
 
@@ -880,12 +893,12 @@ static int ensure_graphs(msmgb_ctx *c, double h)
 {
     if (fused_mixed(c)) {
         if (!c->g_pre || c->fg_h != h || c->fg_n != c->n ||
-            c->fg_tune != c->tune_dens_unroll * 16 + c->tune_force_unroll)
+            c->fg_tune != c->tune_dens_unroll * 64 + c->tune_force_unroll)
             return capture_fused(c, h);
         return MSMGB_OK;
     }
     if (!c->step_graph || c->graph_h != h || c->graph_prec != c->p.precision || c->graph_n != c->n ||
-        c->graph_tune != c->tune_dens_unroll * 16 + c->tune_force_unroll)
+        c->graph_tune != c->tune_dens_unroll * 64 + c->tune_force_unroll)
         return capture_step(c, h);
     return MSMGB_OK;
 }

@@ -111,7 +111,7 @@ __device__ __forceinline__ unsigned pair_index(const PosFF &pi, const PosFF &pj,
     return ((unsigned)kk << kDkBits) | q;
 }
 
-template <int POT, bool MULTI, int UNR, int MINB>
+template <int POT, bool MULTI, int UNR, int MINB, bool PF>
 __global__ void __launch_bounds__(kBlock, MINB) k_density32(DevAtoms a, DevTables t)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -130,39 +130,72 @@ __global__ void __launch_bounds__(kBlock, MINB) k_density32(DevAtoms a, DevTable
     const int *__restrict__ nb = a.indi + i;
     const float2 *__restrict__ row0 = t.dens2;
     float rho = 0.0f;
-    int w = 0;
-    // UNR neighbours per iteration keep UNR independent gathers in flight
-    for (; w + UNR <= kn; w += UNR) {
-        int j[UNR];
-        PosFF p[UNR];
+    if (PF) {
+        // list entries of the next UNR slots are loaded one iteration ahead (slots past
+        // KVOIS are marked -1), so the stream of ELL columns overlaps the position gathers
+        int jn[UNR];
 #pragma unroll
-        for (int u = 0; u < UNR; ++u) j[u] = __ldg(nb + (w + u) * ld);
+        for (int u = 0; u < UNR; ++u) jn[u] = u < kn ? __ldg(nb + u * ld) : -1;
+        for (int w = 0; w < kn; w += UNR) {
+            int j[UNR];
 #pragma unroll
-        for (int u = 0; u < UNR; ++u) p[u] = a.posff[j[u]];
+            for (int u = 0; u < UNR; ++u) j[u] = jn[u];
 #pragma unroll
-        for (int u = 0; u < UNR; ++u) {
+            for (int u = 0; u < UNR; ++u) {
+                const int sl = w + UNR + u;
+                jn[u] = sl < kn ? __ldg(nb + sl * ld) : -1;
+            }
+#pragma unroll
+            for (int u = 0; u < UNR; ++u) {
+                if (j[u] >= 0) {
+                    const PosFF pu = a.posff[j[u]];
+                    float dk;
+                    int kk;
+                    const unsigned c = pair_index(pi, pu, b, t, rej, dk, kk);
+                    pk[(w + u) * ld] = c;
+                    if (c != kSkip) {
+                        const int k = MULTI ? t.kpair[(a.ityp[j[u]] - 1) * t.ngroup + ti] : 0;
+                        const float2 e = __ldg(row0 + k * t.ntp + kk);
+                        rho += fmaf(dk, e.y, e.x);
+                    }
+                }
+            }
+        }
+    } else {
+        int w = 0;
+        // UNR neighbours per iteration keep UNR independent gathers in flight
+        for (; w + UNR <= kn; w += UNR) {
+            int j[UNR];
+            PosFF p[UNR];
+#pragma unroll
+            for (int u = 0; u < UNR; ++u) j[u] = __ldg(nb + (w + u) * ld);
+#pragma unroll
+            for (int u = 0; u < UNR; ++u) p[u] = a.posff[j[u]];
+#pragma unroll
+            for (int u = 0; u < UNR; ++u) {
+                float dk;
+                int kk;
+                const unsigned c = pair_index(pi, p[u], b, t, rej, dk, kk);
+                pk[(w + u) * ld] = c;
+                if (c != kSkip) {
+                    const int k = MULTI ? t.kpair[(a.ityp[j[u]] - 1) * t.ngroup + ti] : 0;
+                    const float2 e = __ldg(row0 + k * t.ntp + kk);
+                    rho += fmaf(dk, e.y, e.x);
+                }
+            }
+        }
+        for (; w < kn; ++w) {
+            const int j0 = __ldg(nb + w * ld);
+            const PosFF p0 = a.posff[j0];
             float dk;
             int kk;
-            const unsigned c = pair_index(pi, p[u], b, t, rej, dk, kk);
-            pk[(w + u) * ld] = c;
+            const unsigned c = pair_index(pi, p0, b, t, rej, dk, kk);
+            pk[w * ld] = c;
             if (c != kSkip) {
-                const int k = MULTI ? t.kpair[(a.ityp[j[u]] - 1) * t.ngroup + ti] : 0;
+                const int k = MULTI ? t.kpair[(a.ityp[j0] - 1) * t.ngroup + ti] : 0;
                 const float2 e = __ldg(row0 + k * t.ntp + kk);
                 rho += fmaf(dk, e.y, e.x);
             }
-        }
-    }
-    for (; w < kn; ++w) {
-        const int j0 = __ldg(nb + w * ld);
-        const PosFF p0 = a.posff[j0];
-        float dk;
-        int kk;
-        const unsigned c = pair_index(pi, p0, b, t, rej, dk, kk);
-        pk[w * ld] = c;
-        if (c != kSkip) {
-            const int k = MULTI ? t.kpair[(a.ityp[j0] - 1) * t.ngroup + ti] : 0;
-            const float2 e = __ldg(row0 + k * t.ntp + kk);
-            rho += fmaf(dk, e.y, e.x);
         }
     }
     float d = rho;
@@ -220,21 +253,40 @@ __device__ __forceinline__ void force_pair(const PosFF &pi, const PosFF &pj, uns
     fz = fmaf(ft, sz, fz);
 }
 
-template <bool MULTI, int UNR, int MINB>
-__global__ void __launch_bounds__(kBlock, MINB) k_force32(DevAtoms a, DevTables t)
+// Walks the ELL list of atom i, UNR slots per iteration, and calls body(j, c) for every slot
+// whose packed index c is not kSkip.  With PF the slots of the next iteration are loaded
+// before the current ones are processed (slots past KVOIS read as kSkip).
+template <int UNR, bool PF, class Body>
+__device__ __forceinline__ void walk_pairs(const int *__restrict__ nb, const unsigned *__restrict__ pk,
+                                           size_t ld, int kn, Body body)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= a.n) return;
-    float fx = 0.0f, fy = 0.0f, fz = 0.0f;
-    if ((a.statu[i] & MSMGB_STATU_ACTIVE) == MSMGB_STATU_ACTIVE) {
-        const BoxF b = load_boxf(a.box[a.boxid[i]]);
-        const PosFF pi = a.posff[i];
-        const int ti = MULTI ? a.ityp[i] - 1 : 0;
-        const float di = a.den32[i];
-        const int kn = a.kvois[i];
-        const size_t ld = (size_t)a.ld;
-        const int *__restrict__ nb = a.indi + i;
-        const unsigned *__restrict__ pk = a.pk + i;
+    if (PF) {
+        unsigned cn[UNR];
+        int jn[UNR];
+#pragma unroll
+        for (int u = 0; u < UNR; ++u) {
+            cn[u] = u < kn ? __ldg(pk + u * ld) : kSkip;
+            jn[u] = u < kn ? __ldg(nb + u * ld) : 0;
+        }
+        for (int w = 0; w < kn; w += UNR) {
+            unsigned c[UNR];
+            int j[UNR];
+#pragma unroll
+            for (int u = 0; u < UNR; ++u) {
+                c[u] = cn[u];
+                j[u] = jn[u];
+            }
+#pragma unroll
+            for (int u = 0; u < UNR; ++u) {
+                const int sl = w + UNR + u;
+                cn[u] = sl < kn ? __ldg(pk + sl * ld) : kSkip;
+                jn[u] = sl < kn ? __ldg(nb + sl * ld) : 0;
+            }
+#pragma unroll
+            for (int u = 0; u < UNR; ++u)
+                if (c[u] != kSkip) body(j[u], c[u]);
+        }
+    } else {
         int w = 0;
         for (; w + UNR <= kn; w += UNR) {
             unsigned c[UNR];
@@ -245,23 +297,32 @@ __global__ void __launch_bounds__(kBlock, MINB) k_force32(DevAtoms a, DevTables 
                 j[u] = __ldg(nb + (w + u) * ld);
             }
 #pragma unroll
-            for (int u = 0; u < UNR; ++u) {
-                if (c[u] != kSkip) {
-                    const PosFF pj = a.posff[j[u]];
-                    force_pair<MULTI>(pi, pj, c[u], di, __ldg(a.den32 + j[u]), ti,
-                                      MULTI ? a.ityp[j[u]] - 1 : 0, b, t, fx, fy, fz);
-                }
-            }
+            for (int u = 0; u < UNR; ++u)
+                if (c[u] != kSkip) body(j[u], c[u]);
         }
         for (; w < kn; ++w) {
             const unsigned c0 = __ldg(pk + w * ld);
-            if (c0 != kSkip) {
-                const int j0 = __ldg(nb + w * ld);
-                const PosFF p0 = a.posff[j0];
-                force_pair<MULTI>(pi, p0, c0, di, __ldg(a.den32 + j0), ti, MULTI ? a.ityp[j0] - 1 : 0, b, t,
-                                  fx, fy, fz);
-            }
+            if (c0 != kSkip) body(__ldg(nb + w * ld), c0);
         }
+    }
+}
+
+template <bool MULTI, int UNR, int MINB, bool PF>
+__global__ void __launch_bounds__(kBlock, MINB) k_force32(DevAtoms a, DevTables t)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    float fx = 0.0f, fy = 0.0f, fz = 0.0f;
+    if ((a.statu[i] & MSMGB_STATU_ACTIVE) == MSMGB_STATU_ACTIVE) {
+        const BoxF b = load_boxf(a.box[a.boxid[i]]);
+        const PosFF pi = a.posff[i];
+        const int ti = MULTI ? a.ityp[i] - 1 : 0;
+        const float di = a.den32[i];
+        walk_pairs<UNR, PF>(a.indi + i, a.pk + i, (size_t)a.ld, a.kvois[i], [&](int j, unsigned c) {
+            const PosFF pj = a.posff[j];
+            force_pair<MULTI>(pi, pj, c, di, __ldg(a.den32 + j), ti, MULTI ? a.ityp[j] - 1 : 0, b, t, fx, fy,
+                              fz);
+        });
     }
     a.fx[i] = (double)fx;
     a.fy[i] = (double)fy;
@@ -400,7 +461,7 @@ __global__ void __launch_bounds__(kBlock) k_force32s(DevAtoms a, DevTables t, in
 // still gathering.  The integrator's FP64 work then runs on the FP64 pipe while other warps
 // of the same kernel keep the FP32 pipes busy, and one pass over x, v and F disappears.
 // Single species only (the multi-species mixed step keeps the separate integrator).
-template <int UNR, int MINB>
+template <int UNR, int MINB, bool PF>
 __global__ void __launch_bounds__(kBlock, MINB) k_force32_vv(DevAtoms a, DevTables t, double th)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -413,35 +474,10 @@ __global__ void __launch_bounds__(kBlock, MINB) k_force32_vv(DevAtoms a, DevTabl
             const BoxF b = load_boxf(bb);
             const PosFF pi = a.posff[i];
             const float di = a.den32[i];
-            const int kn = a.kvois[i];
-            const size_t ld = (size_t)a.ld;
-            const int *__restrict__ nb = a.indi + i;
-            const unsigned *__restrict__ pk = a.pk + i;
-            int w = 0;
-            for (; w + UNR <= kn; w += UNR) {
-                unsigned c[UNR];
-                int j[UNR];
-#pragma unroll
-                for (int u = 0; u < UNR; ++u) {
-                    c[u] = __ldg(pk + (w + u) * ld);
-                    j[u] = __ldg(nb + (w + u) * ld);
-                }
-#pragma unroll
-                for (int u = 0; u < UNR; ++u) {
-                    if (c[u] != kSkip) {
-                        const PosFF pj = a.posff[j[u]];
-                        force_pair<false>(pi, pj, c[u], di, __ldg(a.den32 + j[u]), 0, 0, b, t, fx, fy, fz);
-                    }
-                }
-            }
-            for (; w < kn; ++w) {
-                const unsigned c0 = __ldg(pk + w * ld);
-                if (c0 != kSkip) {
-                    const int j0 = __ldg(nb + w * ld);
-                    const PosFF p0 = a.posff[j0];
-                    force_pair<false>(pi, p0, c0, di, __ldg(a.den32 + j0), 0, 0, b, t, fx, fy, fz);
-                }
-            }
+            walk_pairs<UNR, PF>(a.indi + i, a.pk + i, (size_t)a.ld, a.kvois[i], [&](int j, unsigned c) {
+                const PosFF pj = a.posff[j];
+                force_pair<false>(pi, pj, c, di, __ldg(a.den32 + j), 0, 0, b, t, fx, fy, fz);
+            });
         }
         const double Fx = (double)fx, Fy = (double)fy, Fz = (double)fz;
         a.fx[i] = Fx;
@@ -460,17 +496,26 @@ __global__ void __launch_bounds__(kBlock, MINB) k_force32_vv(DevAtoms a, DevTabl
 
 static inline int nblk(long n, int b) { return (int)((n + b - 1) / b); }
 
-// variant codes of the fused kernel: (neighbours in flight, minimum resident blocks)
+// variant codes of the fused kernel: (neighbours in flight, minimum resident blocks), codes
+// 6-11 the same six with the next slots of the list loaded one iteration ahead
+constexpr int kFusedVariants = 12;
+
 static void fused_variant(msmgb_ctx *c, int code, double h)
 {
     const int g = nblk(c->n, kBlock);
     switch (code) {
-    case 1: k_force32_vv<4, 1><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
-    case 2: k_force32_vv<2, 4><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
-    case 3: k_force32_vv<4, 4><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
-    case 4: k_force32_vv<2, 5><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
-    case 5: k_force32_vv<4, 5><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
-    default: k_force32_vv<2, 1><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
+    case 1: k_force32_vv<4, 1, false><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
+    case 2: k_force32_vv<2, 4, false><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
+    case 3: k_force32_vv<4, 4, false><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
+    case 4: k_force32_vv<2, 5, false><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
+    case 5: k_force32_vv<4, 5, false><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
+    case 6: k_force32_vv<2, 1, true><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
+    case 7: k_force32_vv<4, 1, true><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
+    case 8: k_force32_vv<2, 4, true><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
+    case 9: k_force32_vv<4, 4, true><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
+    case 10: k_force32_vv<2, 5, true><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
+    case 11: k_force32_vv<4, 5, true><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
+    default: k_force32_vv<2, 1, false><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
     }
 }
 
@@ -491,7 +536,7 @@ int autotune_fused(msmgb_ctx *c)
     if (err != cudaSuccess) return cuda_err(c, err, "autotune events");
     float best = 1e30f;
     int bestc = 0;
-    for (int code = 0; code < 6; ++code) {
+    for (int code = 0; code < kFusedVariants; ++code) {
         for (int r = 0; r < 4; ++r) {
             if (r == 1) cudaEventRecord(e0, c->stream);
             fused_variant(c, code, 0.0);
@@ -533,7 +578,7 @@ template <int POT, bool MULTI>
 static void dens_variant(msmgb_ctx *c, int unr)
 {
     const int g = nblk(c->n, kBlock);
-    if (!MULTI && unr >= 8) {
+    if (!MULTI && (unr & 8)) {
         int kmin, cnt;
         smem_window(c, (int)sizeof(float2), &kmin, &cnt);
         const int smem = cnt * (int)sizeof(float2);
@@ -544,12 +589,21 @@ static void dens_variant(msmgb_ctx *c, int unr)
         }
         return;
     }
+    if (unr & 16) {
+        switch (unr & 7) {
+        case 4: k_density32<POT, MULTI, 4, 1, true><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
+        case 5: k_density32<POT, MULTI, 4, 6, true><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
+        case 3: k_density32<POT, MULTI, 2, 6, true><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
+        default: k_density32<POT, MULTI, 2, 1, true><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
+        }
+        return;
+    }
     switch (unr & 7) {
-    case 1: k_density32<POT, MULTI, 1, 1><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
-    case 4: k_density32<POT, MULTI, 4, 1><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
-    case 5: k_density32<POT, MULTI, 4, 6><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
-    case 3: k_density32<POT, MULTI, 2, 6><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
-    default: k_density32<POT, MULTI, 2, 1><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
+    case 1: k_density32<POT, MULTI, 1, 1, false><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
+    case 4: k_density32<POT, MULTI, 4, 1, false><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
+    case 5: k_density32<POT, MULTI, 4, 6, false><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
+    case 3: k_density32<POT, MULTI, 2, 6, false><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
+    default: k_density32<POT, MULTI, 2, 1, false><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
     }
 }
 
@@ -557,7 +611,7 @@ template <bool MULTI>
 static void force_variant(msmgb_ctx *c, int unr)
 {
     const int g = nblk(c->n, kBlock);
-    if (!MULTI && unr >= 8) {
+    if (!MULTI && (unr & 8)) {
         int kmin, cnt;
         smem_window(c, (int)sizeof(float4), &kmin, &cnt);
         const int smem = cnt * (int)sizeof(float4);
@@ -568,12 +622,21 @@ static void force_variant(msmgb_ctx *c, int unr)
         }
         return;
     }
+    if (unr & 16) {
+        switch (unr & 7) {
+        case 4: k_force32<MULTI, 4, 1, true><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
+        case 5: k_force32<MULTI, 4, 6, true><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
+        case 3: k_force32<MULTI, 2, 6, true><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
+        default: k_force32<MULTI, 2, 1, true><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
+        }
+        return;
+    }
     switch (unr & 7) {
-    case 1: k_force32<MULTI, 1, 1><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
-    case 4: k_force32<MULTI, 4, 1><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
-    case 5: k_force32<MULTI, 4, 6><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
-    case 3: k_force32<MULTI, 2, 6><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
-    default: k_force32<MULTI, 2, 1><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
+    case 1: k_force32<MULTI, 1, 1, false><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
+    case 4: k_force32<MULTI, 4, 1, false><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
+    case 5: k_force32<MULTI, 4, 6, false><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
+    case 3: k_force32<MULTI, 2, 6, false><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
+    default: k_force32<MULTI, 2, 1, false><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
     }
 }
 
@@ -610,10 +673,11 @@ int launch_force32(msmgb_ctx *c)
 int autotune_mixed(msmgb_ctx *c)
 {
     // code & 7: 1, 2, 4 = neighbours in flight per thread; 3 = 2 and 5 = 4 with registers
-    // capped for 6 blocks (75% occupancy); +8: persistent grid with the table in shared memory
+    // capped for 6 blocks (75% occupancy); +16: list slots loaded one iteration ahead;
+    // +8: persistent grid with the table in shared memory (single kind only)
     const bool single = c->tab.ngroup == 1;
-    const int cands[7] = {1, 2, 4, 3, 5, 9, 10};
-    const int ncand = single ? 7 : 5;
+    const int cands[11] = {1, 2, 4, 3, 5, 18, 20, 19, 21, 9, 10};
+    const int ncand = single ? 11 : 9;
     cudaEvent_t e0, e1;
     cudaError_t err = cudaEventCreate(&e0);
     if (err == cudaSuccess) err = cudaEventCreate(&e1);

@@ -8,6 +8,9 @@
 //   k_force64    CALFORCE_KERNEL / CALPTENSOR_KERNEL (:623-806, :998-1272 and EAM twins)
 //                FORTOT = FPOTR/R^2 + (FPOTB(k_ij) F'_i + FPOTB(k_ji) F'_j)/R,
 //                F_i = sum_j FORTOT s_ij, virial P_ab += FORTOT/2 s_a s_b per box.
+//   k_stress64   CAL_FS_AtomicStress_KERNEL / CAL_EAM_AtomicStress_KERNEL
+//                (MD_FS_ForceTable_GPU.F90:1746-1965, MD_EAM_ForceTable_GPU.F90:1775-1994)
+//                AP_i(a,b) = sum_j FORTOT s_a s_b, written straight into the caller's order.
 //
 // One thread per atom over the cell-sorted order, so the 32 atoms of a warp share most of
 // their neighbours and the double4_32a position gathers hit L1/L2.  The two square roots and
@@ -183,6 +186,53 @@ __global__ void __launch_bounds__(kBlock) k_force64(DevAtoms a, DevTables t)
     if (VIRIAL) virial_flush(a, box, v);
 }
 
+// Per-atom virial tensor from the F'(rho) of the last FP64 density pass.  ap holds 9 slabs
+// of n doubles (component 3a+b, the reference's AP(NAPDEV, 9)); atom i goes to row gid[i]
+// (caller order) or i (sorted order).
+template <bool MULTI>
+__global__ void __launch_bounds__(kBlock) k_stress64(DevAtoms a, DevTables t, int sorted, double *ap)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    double p[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    if ((a.statu[i] & MSMGB_STATU_ACTIVE) == MSMGB_STATU_ACTIVE) {
+        const DevBox &b = a.box[a.boxid[i]];
+        const double4_32a pi = a.pos[i];
+        const int ti = MULTI ? a.ityp[i] - 1 : 0;
+        const double di = a.den[i];
+        const int kn = a.kvois[i];
+        const size_t ld = (size_t)a.ld;
+        for (int w = 0; w < kn; ++w) {
+            const int j = __ldg(a.indi + i + w * ld);
+            const double4_32a q = a.pos[j];
+            double s[3];
+            s[0] = mi(pi.x - q.x, b.len[0], b.half[0], b.ifpd[0]);
+            s[1] = mi(pi.y - q.y, b.len[1], b.half[1], b.ifpd[1]);
+            s[2] = mi(pi.z - q.z, b.len[2], b.half[2], b.ifpd[2]);
+            const double r2 = s[0] * s[0] + s[1] * s[1] + s[2] * s[2];
+            if (r2 > t.ru2) continue;
+            const int tj = MULTI ? a.ityp[j] - 1 : 0;
+            const int k = pair_kind<MULTI>(t, ti, tj);
+            const int k1 = pair_kind<MULTI>(t, tj, ti);
+            const double y = rsqrt(r2);
+            const double sk = rsqrt(y) * t.csi;
+            const int kk = min((int)sk, t.ntab);
+            const double dk = sk - kk;
+            const double P = lerp_row(t.fpotr + (size_t)k * t.ntp, kk, dk);
+            const double B = lerp_row(t.fpotb + (size_t)k * t.ntp, kk, dk);
+            const double B1 = (MULTI && k1 != k) ? lerp_row(t.fpotb + (size_t)k1 * t.ntp, kk, dk) : B;
+            const double ft = P * (y * y) + (B * di + B1 * a.den[j]) * y;
+#pragma unroll
+            for (int u = 0; u < 3; ++u)
+#pragma unroll
+                for (int v = 0; v < 3; ++v) p[3 * u + v] += s[u] * s[v] * ft;
+        }
+    }
+    const size_t row = sorted ? (size_t)i : (size_t)a.gid[i];
+#pragma unroll
+    for (int m = 0; m < 9; ++m) ap[(size_t)m * a.n + row] = p[m];
+}
+
 static inline int nblk(long n, int b) { return (int)((n + b - 1) / b); }
 
 template <int POT, bool MULTI>
@@ -214,6 +264,15 @@ int launch_density(msmgb_ctx *c, bool want_epot)
     c->launches += 1;
     c->den_is32 = false;
     return check_launch(c, "density pass");
+}
+
+int launch_stress(msmgb_ctx *c, int sorted, double *ap)
+{
+    const int bs = block_for(c->n), g = nblk(c->n, bs);
+    if (c->tab.ngroup > 1) k_stress64<true><<<g, bs, 0, c->stream>>>(c->a, c->tab, sorted, ap);
+    else k_stress64<false><<<g, bs, 0, c->stream>>>(c->a, c->tab, sorted, ap);
+    c->launches += 1;
+    return check_launch(c, "atomic stress pass");
 }
 
 int launch_force(msmgb_ctx *c, bool want_virial)

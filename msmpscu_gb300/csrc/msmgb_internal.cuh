@@ -14,7 +14,7 @@
 //   ityp, statu, gid (sorted -> original), boxid
 //   kvois    int32    neighbour count, INDI column-major int32 [mxkvois][cap] (reference
 //                     layout INDI(NAPDEV,MXKVOIS), MD_NeighborsList_GPU.F90:75-85)
-//   tables   double   per kind, NTAB+2 entries (index 0 and NTAB+1 padded, quirk Q6)
+//   tables   double   per kind, NTAB+2 entries (index 0 and NTAB+1 padded: the reference reads NTAB+1 when r = Rmax)
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -313,6 +313,7 @@ int build_list(msmgb_ctx *c, bool predicated);
 // force passes (force64.cu / force32.cu)
 int launch_density(msmgb_ctx *c, bool want_epot);
 int launch_force(msmgb_ctx *c, bool want_virial);
+int launch_stress(msmgb_ctx *c, int sorted, double *ap);
 int launch_density32(msmgb_ctx *c);
 int launch_force32(msmgb_ctx *c);
 int launch_force32_vv(msmgb_ctx *c, double h);

@@ -184,6 +184,12 @@ class Engine:
     def calden(self):
         self._ck(self.lib.msmgb_calden(self.ctx))
 
+    def atomic_stress(self, order=L.ORDER_ORIGINAL):
+        """Per-atom virial tensors sum_j FORTOT s_a s_b, shape (N, 3, 3) (pCalAVStress)."""
+        ap = np.zeros(9 * self.n)
+        self._ck(self.lib.msmgb_cal_atomic_stress(self.ctx, _d(ap), order))
+        return ap.reshape(9, self.n).T.reshape(self.n, 3, 3).copy()
+
     # ---- state ---------------------------------------------------------------------------------
     def copyin(self, boxes, pos, vel=None, ityp=None, statu=None):
         """boxes: list of (natom, lo[3], len[3], ifpd[3]); pos/vel: (N,3) arrays."""

@@ -10,11 +10,11 @@
  * restatement without reference golden vectors ("parity unpinned" beyond the tables).
  *
  * Deliberate deviations from the reference, each cited where it happens:
- *   Q5  the cell list uses minimum-image distances, so boxes whose cells are smaller than
+ *   - the cell list uses minimum-image distances, so boxes whose cells are smaller than
  *       the list cutoff (NCELL forced to 3) still find every neighbour;
- *   Q6  the tables are read as if padded: index NTAB+1 returns T(NTAB) (only ever hit with
+ *   - the tables are read as if padded: index NTAB+1 returns T(NTAB) (only ever hit with
  *       DK = 0), index 0 returns 0;
- *   Q8  the full-list force pairs FPOTB(KPAIR(I,J)) with DEN(I), as the GPU kernels do.
+ *   - the full-list force pairs FPOTB(KPAIR(I,J)) with DEN(I), as the GPU kernels do.
  * Compile with -ffp-contract=off so x86 and Arm give identical results.
  */
 #include "msm_oracle.h"
@@ -222,8 +222,8 @@ int orc_make_tables(int pot, const double *prm, double rmax, int ntab, int nembd
 
 static inline double tab(const double *T, int nkind, int ntab, int k, int i)
 {
-    if (i < 1) return 0.0;          /* Q6: never reached for r > CSIV^2 */
-    if (i > ntab) i = ntab;         /* Q6: r == Rmax exactly reads NTAB+1 with DK = 0 */
+    if (i < 1) return 0.0;          /* padding: never reached for r > CSIV^2 */
+    if (i > ntab) i = ntab;         /* padding: r == Rmax exactly reads NTAB+1 with DK = 0 */
     return T[(size_t)(i - 1) * (size_t)nkind + (size_t)k];
 }
 
@@ -549,7 +549,7 @@ void orc_predictor(int n, double *x, double *y, double *z, double *vx, double *v
             xn[k] = xv;
             dp[k][i] = dp[k][i] + dis;
         }
-        /* Q10: PASSBOUND stays local; only the out-of-box flags are stored (:372-378) */
+        /* PASSBOUND stays local; only the out-of-box flags are stored (:372-378) */
         if (xn[0] > ub[0] || xn[1] > ub[1] || xn[2] > ub[2])
             statu[i] = ORC_STATU_OUTOFBOX | ORC_STATU_REFLECT;
         else if (xn[0] < lb[0] || xn[1] < lb[1] || xn[2] < lb[2])
@@ -613,6 +613,53 @@ int orc_md(int n, double *x, double *y, double *z, double *vx, double *vy, doubl
 done:
     free(kvois); free(indi); free(dsb);
     return rc;
+}
+
+/* ------------------------------------------------------------------------------------ */
+/* Per-atom virial tensor (MD_FS_ForceTable_GPU.F90:1746-1965; EAM :1775-1994)           */
+/* ------------------------------------------------------------------------------------ */
+void orc_atomic_stress(int n, const double *x, const double *y, const double *z, const int *ityp,
+                       const int *statu, const orc_box *box, const int *kvois, const int *indi,
+                       int ldi, const orc_tables *t, const double *den, double *ap, int nthreads)
+{
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#else
+    (void)nthreads;
+#endif
+    const double bx = box->len[0], by = box->len[1], bz = box->len[2];
+    const int px = box->ifpd[0], py = box->ifpd[1], pz = box->ifpd[2];
+    const int nk = t->nkind, nt = t->ntab, ng = t->ngroup;
+#pragma omp parallel for schedule(static)
+    for (int ic = 0; ic < n; ++ic) {
+        double p[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+        if ((statu[ic] & ORC_STATU_ACTIVE) == ORC_STATU_ACTIVE) {
+            const int ityi = ityp[ic];
+            const double denki = den[ic];
+            for (int iw = 0; iw < kvois[ic]; ++iw) {
+                int j = indi[(size_t)iw * (size_t)ldi + (size_t)ic];
+                double s[3];
+                s[0] = min_image(x[ic] - x[j], bx, 0.5 * bx, px);
+                s[1] = min_image(y[ic] - y[j], by, 0.5 * by, py);
+                s[2] = min_image(z[ic] - z[j], bz, 0.5 * bz, pz);
+                double r2 = s[0] * s[0] + s[1] * s[1] + s[2] * s[2];
+                if (r2 > t->ru2) continue;
+                int ityj = ityp[j];
+                int ktab = t->kpair[(ityj - 1) * ng + (ityi - 1)] - 1;
+                int ktab1 = t->kpair[(ityi - 1) * ng + (ityj - 1)] - 1;
+                double r = sqrt(r2);
+                double sk = sqrt(r) * t->csi;
+                int kk = (int)sk;
+                double dk = sk - kk;
+                double fortot = interp(t->fpotr, nk, nt, ktab, kk, dk) / r2 +
+                                (interp(t->fpotb, nk, nt, ktab, kk, dk) * denki +
+                                 interp(t->fpotb, nk, nt, ktab1, kk, dk) * den[j]) / r;
+                for (int a = 0; a < 3; ++a)
+                    for (int b = 0; b < 3; ++b) p[3 * a + b] += s[a] * s[b] * fortot;
+            }
+        }
+        for (int m = 0; m < 9; ++m) ap[(size_t)m * (size_t)n + (size_t)ic] = p[m];
+    }
 }
 
 /* ------------------------------------------------------------------------------------ */

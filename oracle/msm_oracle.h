@@ -96,6 +96,14 @@ int  orc_force(int n, const double *x, const double *y, const double *z, const i
                const orc_tables *t, double *den, double *fx, double *fy, double *fz,
                double *epot, double *vir9, int nthreads);
 
+/* per-atom virial tensor, CAL_FS_AtomicStress_KERNEL (MD_FS_ForceTable_GPU.F90:1746-1965) and
+ * CAL_EAM_AtomicStress_KERNEL (MD_EAM_ForceTable_GPU.F90:1775-1994), cubic box:
+ * AP(i, 3a+b) = sum_j FORTOT s_a s_b (no 1/2), zero on inactive atoms.  den = F'(rho) from
+ * orc_force; ap has 9 slabs of n (the reference's AP(NAPDEV, 9) column-major). */
+void orc_atomic_stress(int n, const double *x, const double *y, const double *z, const int *ityp,
+                       const int *statu, const orc_box *box, const int *kvois, const int *indi,
+                       int ldi, const orc_tables *t, const double *den, double *ap, int nthreads);
+
 /* Swope velocity Verlet (MD_DiffScheme_GPU.F90:242-384 predictor, 686-760 corrector) */
 void orc_predictor(int n, double *x, double *y, double *z, double *vx, double *vy, double *vz,
                    const double *fx, const double *fy, const double *fz, double *dx, double *dy,

@@ -45,6 +45,7 @@ def lib():
         _lib.orc_md.restype = C.c_int
         _lib.orc_hvp.restype = C.c_int
         _lib.orc_adjoint_cr.restype = C.c_int
+        _lib.orc_atomic_stress.restype = None
         _lib.orc_pot_eval.restype = C.c_int
         _lib.orc_embed_eval.restype = C.c_int
     return _lib
@@ -187,6 +188,18 @@ def force(pos, ityp, statu, box, kvois, indi, tables, want_virial=True, want_epo
                            nthreads)
     return dict(den=den, f=np.stack([fx, fy, fz], 1), epot=epot,
                 vir=vir.reshape(3, 3) if want_virial else None, nbad=nbad)
+
+
+def atomic_stress(pos, ityp, statu, box, kvois, indi, tables, den, nthreads=0):
+    """Per-atom virial tensors, shape (N, 3, 3); den = F'(rho) from force()."""
+    n = pos.shape[0]
+    x, y, z = (f64(pos[:, k]) for k in range(3))
+    kv, ind = i32(kvois), i32(indi)
+    ap = np.zeros(9 * n)
+    lib().orc_atomic_stress(n, _d(x), _d(y), _d(z), _i(i32(ityp)), _i(i32(statu)), C.byref(box),
+                            _i(kv), _i(ind), ind.shape[1] if ind.ndim == 2 else n, C.byref(tables.s),
+                            _d(f64(den)), _d(ap), nthreads)
+    return ap.reshape(9, n).T.reshape(n, 3, 3).copy()
 
 
 def hvp(pos, ityp, statu, box, kvois, indi, tables, v, nthreads=0):

@@ -1,11 +1,11 @@
 """GPU tests of the differentiation kernels at the benchmark sizes:
-C4  bcc W 20^3 cells + one <111> dumbbell (16,001 atoms), Marinica EAM2: HVP against central
-    finite differences of the device forces (delta = 1e-4 A, unit probes) at <= 1e-8, against
-    the oracle's HVP at 1e-10, and the lowest curvature of 50 Lanczos iterations agreeing
-    with a Lanczos run on the oracle's HVP;
-C5  64 Cu snapshots of 4,000 atoms (sigma 0.1 A): force-matching gradient w.r.t. the five
-    Cleri-Rosato parameters (targets from parameters x 1.02) against central FD (relative
-    step 1e-6) of the device FP64 loss;
+* bcc W 20^3 cells + one <111> dumbbell (16,001 atoms), Marinica EAM2: HVP against central
+  finite differences of the device forces (delta = 1e-4 A, unit probes) at <= 1e-8, against
+  the oracle's HVP at 1e-10, and the lowest curvature of 50 Lanczos iterations agreeing
+  with a Lanczos run on the oracle's HVP;
+* 64 Cu snapshots of 4,000 atoms (sigma 0.1 A): force-matching gradient w.r.t. the five
+  Cleri-Rosato parameters (targets from parameters x 1.02) against central FD (relative
+  step 1e-6) of the device FP64 loss;
 and the torch.autograd harness around both."""
 import numpy as np
 import pytest

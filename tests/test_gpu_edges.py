@@ -120,3 +120,58 @@ def test_fixpos_fixvel_bits(oracle):
     dx -= np.round(dx / L_) * L_
     assert np.abs(dx).max() < 1e-8
     e.close()
+
+
+@pytest.mark.parametrize("kind", ["cu", "w", "two_species"])
+def test_atomic_stress_parity(oracle, kind):
+    """pCalAVStress: per-atom virial tensors against the oracle (FP64, 1e-10), both orders."""
+    from tests.helpers import w_tables
+    if kind == "w":
+        pos, L_ = lt.w_sia_config(6, 0.02, 12)
+        vel = np.zeros_like(pos)
+        t = w_tables(oracle)
+        rc_nl, ityp = lt.W_RC_NL, np.ones(len(pos), np.int32)
+    else:
+        pos, vel, L_ = lt.cu_config(8, 0.05, 300.0, 33)
+        rc_nl = lt.CU_RC_NL
+        ityp = np.ones(len(pos), np.int32)
+        t = cu_tables(oracle)
+    n = len(pos)
+    st = np.ones(n, np.int32)
+    box = oracle.make_box([0, 0, 0], L_)
+    e = Engine(n, rc_nl, mxkvois=96)
+    if kind == "two_species":
+        ityp = (np.random.default_rng(8).random(n) < 0.4).astype(np.int32) + 1
+        arr, kpair = _two_species_tables(oracle)
+        t = oracle.RawTables(oracle.FS, 10000, 4, lt.CU_RC, lt.CU_RC, arr["potr"], arr["fpotr"],
+                             arr["potb"], arr["fpotb"], kpair)
+        e.init_forcetable_raw(L.FS_TYPE, 10000, 4, lt.CU_RC, lt.CU_RC, arr["potr"], arr["fpotr"],
+                              arr["potb"], arr["fpotb"], 2, kpair)
+    elif kind == "w":
+        e.init_forcetable(ForceTable.marinica_eam2(rc=lt.W_RC))
+    else:
+        e.init_forcetable(ForceTable.cleri_rosato(**lt.CU_CR, rc=lt.CU_RC))
+    kv, ind = oracle.nlist(pos, st, box, rc_nl, 128)
+    ref = oracle.force(pos, ityp, st, box, kv, ind, t)
+    ap_ref = oracle.atomic_stress(pos, ityp, st, box, kv, ind, t, ref["den"])
+    e.copyin([(n, (0, 0, 0), tuple(L_), (1, 1, 1))], pos, vel, ityp=ityp)
+    ap = e.atomic_stress()
+    assert rel_err(ap, ap_ref) < TOL
+    aps = e.atomic_stress(order=L.ORDER_SORTED)
+    gid = e.get_gid()
+    assert np.array_equal(aps, ap[gid])
+    e.close()
+
+
+def test_atomic_stress_sum_is_twice_virial_large():
+    """256,000 atoms: the per-atom tensors add up to twice the box virial of calptensor."""
+    pos, vel, L_ = lt.cu_config(40, 0.05, 600.0, 7)
+    n = len(pos)
+    e = Engine(n, lt.CU_RC_NL, mxkvois=64)
+    e.init_forcetable(ForceTable.cleri_rosato(**lt.CU_CR, rc=lt.CU_RC))
+    e.copyin([(n, (0, 0, 0), tuple(L_), (1, 1, 1))], pos, vel)
+    vir = e.calptensor()[0]
+    ap = e.atomic_stress()
+    assert np.allclose(ap, ap.transpose(0, 2, 1), rtol=0, atol=1e-9 * np.abs(ap).max())
+    assert rel_err(ap.sum(0), 2.0 * vir) < 1e-9
+    e.close()

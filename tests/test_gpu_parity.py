@@ -52,7 +52,7 @@ def test_neighbour_sets_identical(oracle, ncell, sigma, seed):
 
 
 def test_small_box_neighbours_complete(oracle):
-    """edge 4 cells: NCELL forced to 3 (cells narrower than the cutoff, quirk Q5)."""
+    """edge 4 cells: NCELL forced to 3 (cells narrower than the cutoff, the reference's NCELL >= 3 rule)."""
     pos, vel, L_ = lt.cu_config(4, 0.05, 300.0, 9)
     e = _cu_engine(len(pos))
     e.copyin(_box(len(pos), L_), pos, vel)
@@ -144,7 +144,7 @@ def test_predictor_corrector_parity(oracle):
 
 
 @pytest.mark.parametrize("precision_steps", [("fp64", 100)])
-def test_md_trajectory_parity_c1(oracle, precision_steps):
+def test_md_trajectory_parity_cu4000(oracle, precision_steps):
     """Cu 4,000 atoms, 300 K, sigma 0.02 A, 100 NVE steps of 1 fs with the skin trigger."""
     prec, nsteps = precision_steps
     pos, vel, L_ = lt.cu_config(10, 0.02, 300.0, 1)

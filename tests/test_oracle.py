@@ -56,7 +56,7 @@ def test_cell_list_equals_brute_force(oracle):
 
 
 def test_small_box_minimum_image_list(oracle):
-    """4-cell box: NCELL is forced to 3 with cells narrower than the cutoff (quirk Q5);
+    """4-cell box: NCELL is forced to 3 with cells narrower than the cutoff (the reference's NCELL >= 3 rule);
     the minimum-image rule still finds every neighbour."""
     pos, _, L = lt.cu_config(4, 0.05, 300.0, 7)
     box = oracle.make_box([0, 0, 0], L)
@@ -115,6 +115,30 @@ def test_virial_trace_matches_sum_r_dot_f(oracle):
     vir = out["vir"]
     assert np.allclose(vir, vir.T)
     assert abs(np.trace(vir)) > 0
+
+
+def test_atomic_stress_sums_to_virial_and_strain_derivative(oracle):
+    """Per-atom tensors (pCalAVStress) are symmetric, sum to twice the box virial, and the
+    virial is minus the derivative of the energy under a homogeneous strain of the box."""
+    pos, _, L = _cu_small(seed=6)
+    t = cu_tables(oracle)
+    box = oracle.make_box([0, 0, 0], L)
+    n = len(pos)
+    st, ty = np.ones(n, np.int32), np.ones(n, np.int32)
+    kv, ind = oracle.nlist(pos, st, box, lt.CU_RC_NL, 96)
+    out = oracle.force(pos, ty, st, box, kv, ind, t)
+    ap = oracle.atomic_stress(pos, ty, st, box, kv, ind, t, out["den"])
+    assert np.allclose(ap, ap.transpose(0, 2, 1), rtol=0, atol=1e-12)
+    assert np.allclose(ap.sum(0), 2.0 * out["vir"], rtol=1e-12, atol=1e-9)
+    for a in (0, 2):
+        e = []
+        for sgn in (1.0, -1.0):
+            scale = np.ones(3)
+            scale[a] += sgn * 1e-6
+            bx = oracle.make_box([0, 0, 0], L * scale)
+            e.append(oracle.force(pos * scale, ty, st, bx, kv, ind, t)["epot"].sum())
+        dE = (e[0] - e[1]) / 2e-6
+        assert dE == pytest.approx(-out["vir"][a, a], rel=2e-3)
 
 
 def test_eam_w_force_and_hvp_finite_difference(oracle):
