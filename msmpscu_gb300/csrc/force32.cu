@@ -145,20 +145,20 @@ __global__ void __launch_bounds__(kBlock, MINB) k_density32(DevAtoms a, DevTable
                 const int sl = w + UNR + u;
                 jn[u] = sl < kn ? __ldg(nb + sl * ld) : -1;
             }
+            // all gathers first (slots past KVOIS read atom i itself and are discarded)
+            PosFF p[UNR];
+#pragma unroll
+            for (int u = 0; u < UNR; ++u) p[u] = a.posff[j[u] >= 0 ? j[u] : i];
 #pragma unroll
             for (int u = 0; u < UNR; ++u) {
-                if (j[u] >= 0) {
-                    const PosFF pu = a.posff[j[u]];
-                    float dk;
-                    int kk;
-                    const unsigned c = pair_index(pi, pu, b, t, rej, dk, kk);
-                    pk[(w + u) * ld] = c;
-                    if (c != kSkip) {
-                        const int k = MULTI ? t.kpair[(a.ityp[j[u]] - 1) * t.ngroup + ti] : 0;
-                        const float2 e = __ldg(row0 + k * t.ntp + kk);
-                        rho += fmaf(dk, e.y, e.x);
-                    }
-                }
+                float dk = 0.0f;
+                int kk = 0;
+                const unsigned c = pair_index(pi, p[u], b, t, rej, dk, kk);
+                if (j[u] >= 0) pk[(w + u) * ld] = c;
+                const bool ok = j[u] >= 0 && c != kSkip;
+                const int k = MULTI ? t.kpair[(a.ityp[j[u] >= 0 ? j[u] : i] - 1) * t.ngroup + ti] : 0;
+                const float2 e = __ldg(row0 + k * t.ntp + (ok ? kk : 0));
+                rho += ok ? fmaf(dk, e.y, e.x) : 0.0f;
             }
         }
     } else {
@@ -307,7 +307,75 @@ __device__ __forceinline__ void walk_pairs(const int *__restrict__ nb, const uns
     }
 }
 
-template <bool MULTI, int UNR, int MINB, bool PF>
+// Single-kind pair term with the table row e = {P, P', B, B'} (at KK) already loaded.
+__device__ __forceinline__ void force_pair_e(const PosFF &pi, const PosFF &pj, unsigned c, float di, float dj,
+                                             const float4 &e, const BoxF &b, float &fx, float &fy, float &fz)
+{
+    const float sx = sep1(pi.hx, pi.lx, pj.hx, pj.lx, b.lh[0], b.ll[0], b.half[0], b.pd[0]);
+    const float sy = sep1(pi.hy, pi.ly, pj.hy, pj.ly, b.lh[1], b.ll[1], b.half[1], b.pd[1]);
+    const float sz = sep1(pi.hz, pi.lz, pj.hz, pj.lz, b.lh[2], b.ll[2], b.half[2], b.pd[2]);
+    const float y = rsqrtf(fmaf(sx, sx, fmaf(sy, sy, sz * sz)));
+    const float dk = (float)(c & ((1u << kDkBits) - 1)) * kDkInv;
+    const float P = fmaf(dk, e.y, e.x);
+    const float B = fmaf(dk, e.w, e.z);
+    const float ft = fmaf(P, y, B * (di + dj)) * y;
+    fx = fmaf(ft, sx, fx);
+    fy = fmaf(ft, sy, fy);
+    fz = fmaf(ft, sz, fz);
+}
+
+// Single-kind force loop over the ELL list of atom i with every load of a batch issued
+// before any of its arithmetic: list slots one iteration ahead, then for all UNR slots the
+// neighbour position, its F'(rho) and the table row.  Slots beyond RU (kSkip) and past
+// KVOIS gather row 0 / atom i itself, which are always valid addresses, and are then not
+// accumulated.  The loads are thereby unconditional and overlap, instead of one dependent
+// gather chain per slot.
+template <int UNR>
+__device__ __forceinline__ void force_loop_batched(const DevAtoms &a, const DevTables &t, int i, const PosFF &pi,
+                                                   float di, const BoxF &b, float &fx, float &fy, float &fz)
+{
+    const int *__restrict__ nb = a.indi + i;
+    const unsigned *__restrict__ pk = a.pk + i;
+    const size_t ld = (size_t)a.ld;
+    const int kn = a.kvois[i];
+    unsigned cn[UNR];
+    int jn[UNR];
+#pragma unroll
+    for (int u = 0; u < UNR; ++u) {
+        cn[u] = u < kn ? __ldg(pk + u * ld) : kSkip;
+        jn[u] = u < kn ? __ldg(nb + u * ld) : i;
+    }
+    for (int w = 0; w < kn; w += UNR) {
+        unsigned c[UNR];
+        int j[UNR];
+#pragma unroll
+        for (int u = 0; u < UNR; ++u) {
+            c[u] = cn[u];
+            j[u] = jn[u];
+        }
+#pragma unroll
+        for (int u = 0; u < UNR; ++u) {
+            const int sl = w + UNR + u;
+            cn[u] = sl < kn ? __ldg(pk + sl * ld) : kSkip;
+            jn[u] = sl < kn ? __ldg(nb + sl * ld) : i;
+        }
+        PosFF pj[UNR];
+        float dj[UNR];
+        float4 e[UNR];
+#pragma unroll
+        for (int u = 0; u < UNR; ++u) {
+            const unsigned row = c[u] == kSkip ? 0u : (c[u] >> kDkBits);
+            pj[u] = a.posff[j[u]];
+            dj[u] = __ldg(a.den32 + j[u]);
+            e[u] = __ldg(t.force4 + row);
+        }
+#pragma unroll
+        for (int u = 0; u < UNR; ++u)
+            if (c[u] != kSkip) force_pair_e(pi, pj[u], c[u], di, dj[u], e[u], b, fx, fy, fz);
+    }
+}
+
+template <bool MULTI, int UNR, int MINB, int PF>
 __global__ void __launch_bounds__(kBlock, MINB) k_force32(DevAtoms a, DevTables t)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -318,11 +386,15 @@ __global__ void __launch_bounds__(kBlock, MINB) k_force32(DevAtoms a, DevTables 
         const PosFF pi = a.posff[i];
         const int ti = MULTI ? a.ityp[i] - 1 : 0;
         const float di = a.den32[i];
-        walk_pairs<UNR, PF>(a.indi + i, a.pk + i, (size_t)a.ld, a.kvois[i], [&](int j, unsigned c) {
-            const PosFF pj = a.posff[j];
-            force_pair<MULTI>(pi, pj, c, di, __ldg(a.den32 + j), ti, MULTI ? a.ityp[j] - 1 : 0, b, t, fx, fy,
-                              fz);
-        });
+        if (PF == 2 && !MULTI) {
+            force_loop_batched<UNR>(a, t, i, pi, di, b, fx, fy, fz);
+        } else {
+            walk_pairs<UNR, (PF != 0)>(a.indi + i, a.pk + i, (size_t)a.ld, a.kvois[i], [&](int j, unsigned c) {
+                const PosFF pj = a.posff[j];
+                force_pair<MULTI>(pi, pj, c, di, __ldg(a.den32 + j), ti, MULTI ? a.ityp[j] - 1 : 0, b, t, fx, fy,
+                                  fz);
+            });
+        }
     }
     a.fx[i] = (double)fx;
     a.fy[i] = (double)fy;
@@ -461,7 +533,7 @@ __global__ void __launch_bounds__(kBlock) k_force32s(DevAtoms a, DevTables t, in
 // still gathering.  The integrator's FP64 work then runs on the FP64 pipe while other warps
 // of the same kernel keep the FP32 pipes busy, and one pass over x, v and F disappears.
 // Single species only (the multi-species mixed step keeps the separate integrator).
-template <int UNR, int MINB, bool PF>
+template <int UNR, int MINB, int PF>
 __global__ void __launch_bounds__(kBlock, MINB) k_force32_vv(DevAtoms a, DevTables t, double th)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -474,10 +546,14 @@ __global__ void __launch_bounds__(kBlock, MINB) k_force32_vv(DevAtoms a, DevTabl
             const BoxF b = load_boxf(bb);
             const PosFF pi = a.posff[i];
             const float di = a.den32[i];
-            walk_pairs<UNR, PF>(a.indi + i, a.pk + i, (size_t)a.ld, a.kvois[i], [&](int j, unsigned c) {
-                const PosFF pj = a.posff[j];
-                force_pair<false>(pi, pj, c, di, __ldg(a.den32 + j), 0, 0, b, t, fx, fy, fz);
-            });
+            if (PF == 2) {
+                force_loop_batched<UNR>(a, t, i, pi, di, b, fx, fy, fz);
+            } else {
+                walk_pairs<UNR, (PF != 0)>(a.indi + i, a.pk + i, (size_t)a.ld, a.kvois[i], [&](int j, unsigned c) {
+                    const PosFF pj = a.posff[j];
+                    force_pair<false>(pi, pj, c, di, __ldg(a.den32 + j), 0, 0, b, t, fx, fy, fz);
+                });
+            }
         }
         const double Fx = (double)fx, Fy = (double)fy, Fz = (double)fz;
         a.fx[i] = Fx;
@@ -497,25 +573,32 @@ __global__ void __launch_bounds__(kBlock, MINB) k_force32_vv(DevAtoms a, DevTabl
 static inline int nblk(long n, int b) { return (int)((n + b - 1) / b); }
 
 // variant codes of the fused kernel: (neighbours in flight, minimum resident blocks), codes
-// 6-11 the same six with the next slots of the list loaded one iteration ahead
-constexpr int kFusedVariants = 12;
+// 6-11 the same six with the next slots of the list loaded one iteration ahead, 12-17 with
+// in addition every gather of a batch issued before its arithmetic (force_loop_batched)
+constexpr int kFusedVariants = 18;
 
 static void fused_variant(msmgb_ctx *c, int code, double h)
 {
     const int g = nblk(c->n, kBlock);
     switch (code) {
-    case 1: k_force32_vv<4, 1, false><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
-    case 2: k_force32_vv<2, 4, false><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
-    case 3: k_force32_vv<4, 4, false><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
-    case 4: k_force32_vv<2, 5, false><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
-    case 5: k_force32_vv<4, 5, false><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
-    case 6: k_force32_vv<2, 1, true><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
-    case 7: k_force32_vv<4, 1, true><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
-    case 8: k_force32_vv<2, 4, true><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
-    case 9: k_force32_vv<4, 4, true><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
-    case 10: k_force32_vv<2, 5, true><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
-    case 11: k_force32_vv<4, 5, true><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
-    default: k_force32_vv<2, 1, false><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
+    case 1: k_force32_vv<4, 1, 0><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
+    case 2: k_force32_vv<2, 4, 0><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
+    case 3: k_force32_vv<4, 4, 0><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
+    case 4: k_force32_vv<2, 5, 0><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
+    case 5: k_force32_vv<4, 5, 0><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
+    case 6: k_force32_vv<2, 1, 1><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
+    case 7: k_force32_vv<4, 1, 1><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
+    case 8: k_force32_vv<2, 4, 1><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
+    case 9: k_force32_vv<4, 4, 1><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
+    case 10: k_force32_vv<2, 5, 1><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
+    case 11: k_force32_vv<4, 5, 1><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
+    case 12: k_force32_vv<2, 1, 2><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
+    case 13: k_force32_vv<4, 1, 2><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
+    case 14: k_force32_vv<2, 4, 2><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
+    case 15: k_force32_vv<4, 4, 2><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
+    case 16: k_force32_vv<2, 5, 2><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
+    case 17: k_force32_vv<4, 5, 2><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
+    default: k_force32_vv<2, 1, 0><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
     }
 }
 
@@ -622,21 +705,30 @@ static void force_variant(msmgb_ctx *c, int unr)
         }
         return;
     }
+    if (!MULTI && (unr & 32)) {
+        switch (unr & 7) {
+        case 4: k_force32<MULTI, 4, 1, 2><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
+        case 5: k_force32<MULTI, 4, 6, 2><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
+        case 3: k_force32<MULTI, 2, 6, 2><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
+        default: k_force32<MULTI, 2, 1, 2><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
+        }
+        return;
+    }
     if (unr & 16) {
         switch (unr & 7) {
-        case 4: k_force32<MULTI, 4, 1, true><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
-        case 5: k_force32<MULTI, 4, 6, true><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
-        case 3: k_force32<MULTI, 2, 6, true><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
-        default: k_force32<MULTI, 2, 1, true><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
+        case 4: k_force32<MULTI, 4, 1, 1><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
+        case 5: k_force32<MULTI, 4, 6, 1><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
+        case 3: k_force32<MULTI, 2, 6, 1><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
+        default: k_force32<MULTI, 2, 1, 1><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
         }
         return;
     }
     switch (unr & 7) {
-    case 1: k_force32<MULTI, 1, 1, false><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
-    case 4: k_force32<MULTI, 4, 1, false><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
-    case 5: k_force32<MULTI, 4, 6, false><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
-    case 3: k_force32<MULTI, 2, 6, false><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
-    default: k_force32<MULTI, 2, 1, false><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
+    case 1: k_force32<MULTI, 1, 1, 0><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
+    case 4: k_force32<MULTI, 4, 1, 0><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
+    case 5: k_force32<MULTI, 4, 6, 0><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
+    case 3: k_force32<MULTI, 2, 6, 0><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
+    default: k_force32<MULTI, 2, 1, 0><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
     }
 }
 
@@ -674,10 +766,13 @@ int autotune_mixed(msmgb_ctx *c)
 {
     // code & 7: 1, 2, 4 = neighbours in flight per thread; 3 = 2 and 5 = 4 with registers
     // capped for 6 blocks (75% occupancy); +16: list slots loaded one iteration ahead;
+    // +32 (force, single kind): and all gathers of a batch before its arithmetic;
     // +8: persistent grid with the table in shared memory (single kind only)
     const bool single = c->tab.ngroup == 1;
-    const int cands[11] = {1, 2, 4, 3, 5, 18, 20, 19, 21, 9, 10};
-    const int ncand = single ? 11 : 9;
+    const int dcands[11] = {1, 2, 4, 3, 5, 18, 20, 19, 21, 9, 10};
+    const int fcands[15] = {1, 2, 4, 3, 5, 18, 20, 19, 21, 50, 52, 51, 53, 9, 10};
+    const int *cands = dcands;
+    int ncand = single ? 11 : 9;
     cudaEvent_t e0, e1;
     cudaError_t err = cudaEventCreate(&e0);
     if (err == cudaSuccess) err = cudaEventCreate(&e1);
@@ -700,6 +795,8 @@ int autotune_mixed(msmgb_ctx *c)
     c->tune_dens_unroll = bd;
     int rc = launch_density32(c);
     if (rc) return rc;
+    cands = fcands;
+    ncand = single ? 15 : 9;
     for (int k = 0; k < ncand; ++k) {
         c->tune_force_unroll = cands[k];
         for (int r = 0; r < 4; ++r) {
