@@ -1095,6 +1095,9 @@ extern "C" int msmgb_time_passes(msmgb_ctx *c, int reps, float *out)
     out[4] = 0.0f;
     for (int which = 0; which < 5; ++which) {
         if (which == 4 && !fused) break;
+        // the integrator pass rewrote the float-float positions, whose records also carry
+        // F'(rho) for the fused kernel: refresh it (untimed)
+        if (which == 4) RET(launch_density32(c));
         double total = 0.0;
         for (int r = 0; r < reps + 1; ++r) {
             CK(cudaStreamSynchronize(c->stream), "synchronize");

@@ -121,6 +121,7 @@ __global__ void __launch_bounds__(kBlock, MINB) k_density32(DevAtoms a, DevTable
     const size_t ld = (size_t)a.ld;
     if ((a.statu[i] & MSMGB_STATU_ACTIVE) != MSMGB_STATU_ACTIVE) {   // the force pass skips it
         a.den32[i] = 0.0f;
+        a.posff[i].d = 0.0f;
         return;
     }
     const BoxF b = load_boxf(a.box[a.boxid[i]]);
@@ -213,6 +214,7 @@ __global__ void __launch_bounds__(kBlock, MINB) k_density32(DevAtoms a, DevTable
         d = fmaf(sk - (float)kk, e.y, e.x);
     }
     a.den32[i] = d;
+    a.posff[i].d = d;
 }
 
 // FP32 separation for the force direction (dh exact, dl small)
@@ -326,7 +328,7 @@ __device__ __forceinline__ void force_pair_e(const PosFF &pi, const PosFF &pj, u
 
 // Single-kind force loop over the ELL list of atom i with every load of a batch issued
 // before any of its arithmetic: list slots one iteration ahead, then for all UNR slots the
-// neighbour position, its F'(rho) and the table row.  Slots beyond RU (kSkip) and past
+// neighbour position with its F'(rho) (one 32 B record) and the table row.  Slots beyond RU (kSkip) and past
 // KVOIS gather row 0 / atom i itself, which are always valid addresses, and are then not
 // accumulated.  The loads are thereby unconditional and overlap, instead of one dependent
 // gather chain per slot.
@@ -360,18 +362,16 @@ __device__ __forceinline__ void force_loop_batched(const DevAtoms &a, const DevT
             jn[u] = sl < kn ? __ldg(nb + sl * ld) : i;
         }
         PosFF pj[UNR];
-        float dj[UNR];
         float4 e[UNR];
 #pragma unroll
         for (int u = 0; u < UNR; ++u) {
             const unsigned row = c[u] == kSkip ? 0u : (c[u] >> kDkBits);
             pj[u] = a.posff[j[u]];
-            dj[u] = __ldg(a.den32 + j[u]);
             e[u] = __ldg(t.force4 + row);
         }
 #pragma unroll
         for (int u = 0; u < UNR; ++u)
-            if (c[u] != kSkip) force_pair_e(pi, pj[u], c[u], di, dj[u], e[u], b, fx, fy, fz);
+            if (c[u] != kSkip) force_pair_e(pi, pj[u], c[u], di, pj[u].d, e[u], b, fx, fy, fz);
     }
 }
 
@@ -385,14 +385,13 @@ __global__ void __launch_bounds__(kBlock, MINB) k_force32(DevAtoms a, DevTables 
         const BoxF b = load_boxf(a.box[a.boxid[i]]);
         const PosFF pi = a.posff[i];
         const int ti = MULTI ? a.ityp[i] - 1 : 0;
-        const float di = a.den32[i];
+        const float di = pi.d;
         if (PF == 2 && !MULTI) {
             force_loop_batched<UNR>(a, t, i, pi, di, b, fx, fy, fz);
         } else {
             walk_pairs<UNR, (PF != 0)>(a.indi + i, a.pk + i, (size_t)a.ld, a.kvois[i], [&](int j, unsigned c) {
                 const PosFF pj = a.posff[j];
-                force_pair<MULTI>(pi, pj, c, di, __ldg(a.den32 + j), ti, MULTI ? a.ityp[j] - 1 : 0, b, t, fx, fy,
-                                  fz);
+                force_pair<MULTI>(pi, pj, c, di, pj.d, ti, MULTI ? a.ityp[j] - 1 : 0, b, t, fx, fy, fz);
             });
         }
     }
@@ -419,6 +418,7 @@ __global__ void __launch_bounds__(kBlock) k_density32s(DevAtoms a, DevTables t, 
         unsigned *__restrict__ pk = a.pk + i;
         if ((a.statu[i] & MSMGB_STATU_ACTIVE) != MSMGB_STATU_ACTIVE) {
             a.den32[i] = 0.0f;
+            a.posff[i].d = 0.0f;
             continue;
         }
         const BoxF b = load_boxf(a.box[a.boxid[i]]);
@@ -472,6 +472,7 @@ __global__ void __launch_bounds__(kBlock) k_density32s(DevAtoms a, DevTables t, 
             d = fmaf(sk - (float)kk, e.y, e.x);
         }
         a.den32[i] = d;
+        a.posff[i].d = d;
     }
 }
 
@@ -487,7 +488,7 @@ __global__ void __launch_bounds__(kBlock) k_force32s(DevAtoms a, DevTables t, in
         if ((a.statu[i] & MSMGB_STATU_ACTIVE) == MSMGB_STATU_ACTIVE) {
             const BoxF b = load_boxf(a.box[a.boxid[i]]);
             const PosFF pi = a.posff[i];
-            const float di = a.den32[i];
+            const float di = pi.d;
             const int kn = a.kvois[i];
             const int *__restrict__ nb = a.indi + i;
             const unsigned *__restrict__ pk = a.pk + i;
@@ -503,7 +504,7 @@ __global__ void __launch_bounds__(kBlock) k_force32s(DevAtoms a, DevTables t, in
                 for (int u = 0; u < UNR; ++u) {
                     if (c[u] == kSkip) continue;
                     const PosFF pj = a.posff[j[u]];
-                    const float dj = __ldg(a.den32 + j[u]);
+                    const float dj = pj.d;
                     const float sx = sep1(pi.hx, pi.lx, pj.hx, pj.lx, b.lh[0], b.ll[0], b.half[0], b.pd[0]);
                     const float sy = sep1(pi.hy, pi.ly, pj.hy, pj.ly, b.lh[1], b.ll[1], b.half[1], b.pd[1]);
                     const float sz = sep1(pi.hz, pi.lz, pj.hz, pj.lz, b.lh[2], b.ll[2], b.half[2], b.pd[2]);
@@ -545,13 +546,13 @@ __global__ void __launch_bounds__(kBlock, MINB) k_force32_vv(DevAtoms a, DevTabl
         if ((stat & MSMGB_STATU_ACTIVE) == MSMGB_STATU_ACTIVE) {
             const BoxF b = load_boxf(bb);
             const PosFF pi = a.posff[i];
-            const float di = a.den32[i];
+            const float di = pi.d;
             if (PF == 2) {
                 force_loop_batched<UNR>(a, t, i, pi, di, b, fx, fy, fz);
             } else {
                 walk_pairs<UNR, (PF != 0)>(a.indi + i, a.pk + i, (size_t)a.ld, a.kvois[i], [&](int j, unsigned c) {
                     const PosFF pj = a.posff[j];
-                    force_pair<false>(pi, pj, c, di, __ldg(a.den32 + j), 0, 0, b, t, fx, fy, fz);
+                    force_pair<false>(pi, pj, c, di, pj.d, 0, 0, b, t, fx, fy, fz);
                 });
             }
         }
@@ -613,6 +614,10 @@ int launch_force32_vv(msmgb_ctx *c, double h)
 // (the next-step buffer receives the current positions), on the atom view c->a.
 int autotune_fused(msmgb_ctx *c)
 {
+    // F'(rho) of the current positions (carried in the float-float records) first, so that
+    // the forces the variants write are those of the current state
+    int rc = launch_density32(c);
+    if (rc) return rc;
     cudaEvent_t e0, e1;
     cudaError_t err = cudaEventCreate(&e0);
     if (err == cudaSuccess) err = cudaEventCreate(&e1);

@@ -44,8 +44,11 @@ enum {
     kFlagWords = 8
 };
 
+// float-float position (hi, lo parts of u = x + ushift).  d carries the atom's FP32
+// F'(rho) from the mixed density pass, so the force pass gets a neighbour's position and
+// F'(rho) with one 32 B gather.
 struct __align__(32) PosFF {
-    float hx, hy, hz, hw;
+    float hx, hy, hz, d;
     float lx, ly, lz, lw;
 };
 
@@ -133,7 +136,7 @@ __device__ __forceinline__ PosFF make_posff(double x, double y, double z, const 
     split_ff(x + b.ushift[0], p.hx, p.lx);
     split_ff(y + b.ushift[1], p.hy, p.ly);
     split_ff(z + b.ushift[2], p.hz, p.lz);
-    p.hw = 0.0f;
+    p.d = 0.0f;
     p.lw = 0.0f;
     return p;
 }
