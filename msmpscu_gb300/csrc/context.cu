@@ -209,6 +209,8 @@ extern "C" int msmgb_create(msmgb_ctx **out, const msmgb_params *p)
     if ((e = cudaMemsetAsync(c->maxdisp, 0, sizeof(unsigned long long), c->stream)) != cudaSuccess) return fail(e, "memset");
     if (p->precision == MSMGB_PREC_MIXED && (e = dalloc(&a.pk, N * (size_t)p->mxkvois)) != cudaSuccess)
         return fail(e, "cudaMalloc pair index");
+    if (p->precision == MSMGB_PREC_MIXED && (e = dalloc(&a.rec, N)) != cudaSuccess)
+        return fail(e, "cudaMalloc records");
     a.flags = c->flags;
     a.maxdisp = c->maxdisp;
     a.virial = c->virial;
@@ -229,7 +231,7 @@ extern "C" int msmgb_destroy(msmgb_ctx *c)
     DevAtoms &a = c->a;
     void *ptrs[] = {a.pos, a.posff, a.pos_bld, a.vx, a.vy, a.vz, a.fx, a.fy, a.fz,
                     a.dx, a.dy, a.dz, a.ityp, a.statu, a.gid, a.boxid, a.den, a.epot,
-                    a.den32, a.kvois, a.indi, a.pk, c->cell_of, c->perm, c->dbox, c->cm, c->icm,
+                    a.den32, a.kvois, a.indi, a.pk, a.rec, c->cell_of, c->perm, c->dbox, c->cm, c->icm,
                     c->flags, c->maxdisp, c->virial, c->scratch, c->cell_start,
                     c->cell_cursor, c->scan_tmp, c->tab_mem, c->adj_mem, c->hvp_pair, c->pos2, c->posff2};
     for (void *q : ptrs)
@@ -254,6 +256,10 @@ extern "C" int msmgb_set_precision(msmgb_ctx *c, int precision)
         RET(use_device(c));
         CK(cudaStreamSynchronize(c->stream), "synchronize");
         CK(dalloc(&c->a.pk, (size_t)c->cap_atoms * (size_t)c->p.mxkvois), "cudaMalloc pair index");
+    }
+    if (precision == MSMGB_PREC_MIXED && !c->a.rec) {
+        RET(use_device(c));
+        CK(dalloc(&c->a.rec, (size_t)c->cap_atoms), "cudaMalloc records");
     }
     if (precision != c->p.precision) {
         c->p.precision = precision;
@@ -1095,8 +1101,8 @@ extern "C" int msmgb_time_passes(msmgb_ctx *c, int reps, float *out)
     out[4] = 0.0f;
     for (int which = 0; which < 5; ++which) {
         if (which == 4 && !fused) break;
-        // the integrator pass rewrote the float-float positions, whose records also carry
-        // F'(rho) for the fused kernel: refresh it (untimed)
+        // the fused kernel reads the {position, F'(rho)} records of the density pass:
+        // refresh them for the current positions (untimed)
         if (which == 4) RET(launch_density32(c));
         double total = 0.0;
         for (int r = 0; r < reps + 1; ++r) {

@@ -32,6 +32,18 @@ constexpr int kDkBits = 18;
 constexpr float kDkScale = 262144.0f;       // 2^18
 constexpr float kDkInv = 1.0f / 262144.0f;
 
+// read-only gather of a 32 B record (the arrays read this way are not written by the
+// kernel that reads them)
+__device__ __forceinline__ PosFF ldg_ff(const PosFF *p)
+{
+    const float4 *q = reinterpret_cast<const float4 *>(p);
+    const float4 a = __ldg(q), b = __ldg(q + 1);
+    PosFF r;
+    r.hx = a.x; r.hy = a.y; r.hz = a.z; r.d = a.w;
+    r.lx = b.x; r.ly = b.y; r.lz = b.z; r.lw = b.w;
+    return r;
+}
+
 struct BoxF {
     float lh[3], ll[3], half[3];
     int pd[3];
@@ -121,7 +133,7 @@ __global__ void __launch_bounds__(kBlock, MINB) k_density32(DevAtoms a, DevTable
     const size_t ld = (size_t)a.ld;
     if ((a.statu[i] & MSMGB_STATU_ACTIVE) != MSMGB_STATU_ACTIVE) {   // the force pass skips it
         a.den32[i] = 0.0f;
-        a.posff[i].d = 0.0f;
+        a.rec[i] = a.posff[i];          // d = 0
         return;
     }
     const BoxF b = load_boxf(a.box[a.boxid[i]]);
@@ -149,7 +161,7 @@ __global__ void __launch_bounds__(kBlock, MINB) k_density32(DevAtoms a, DevTable
             // all gathers first (slots past KVOIS read atom i itself and are discarded)
             PosFF p[UNR];
 #pragma unroll
-            for (int u = 0; u < UNR; ++u) p[u] = a.posff[j[u] >= 0 ? j[u] : i];
+            for (int u = 0; u < UNR; ++u) p[u] = ldg_ff(a.posff + (j[u] >= 0 ? j[u] : i));
 #pragma unroll
             for (int u = 0; u < UNR; ++u) {
                 float dk = 0.0f;
@@ -171,7 +183,7 @@ __global__ void __launch_bounds__(kBlock, MINB) k_density32(DevAtoms a, DevTable
 #pragma unroll
             for (int u = 0; u < UNR; ++u) j[u] = __ldg(nb + (w + u) * ld);
 #pragma unroll
-            for (int u = 0; u < UNR; ++u) p[u] = a.posff[j[u]];
+            for (int u = 0; u < UNR; ++u) p[u] = ldg_ff(a.posff + j[u]);
 #pragma unroll
             for (int u = 0; u < UNR; ++u) {
                 float dk;
@@ -187,7 +199,7 @@ __global__ void __launch_bounds__(kBlock, MINB) k_density32(DevAtoms a, DevTable
         }
         for (; w < kn; ++w) {
             const int j0 = __ldg(nb + w * ld);
-            const PosFF p0 = a.posff[j0];
+            const PosFF p0 = ldg_ff(a.posff + j0);
             float dk;
             int kk;
             const unsigned c = pair_index(pi, p0, b, t, rej, dk, kk);
@@ -214,7 +226,9 @@ __global__ void __launch_bounds__(kBlock, MINB) k_density32(DevAtoms a, DevTable
         d = fmaf(sk - (float)kk, e.y, e.x);
     }
     a.den32[i] = d;
-    a.posff[i].d = d;
+    PosFF r = pi;
+    r.d = d;
+    a.rec[i] = r;
 }
 
 // FP32 separation for the force direction (dh exact, dl small)
@@ -366,7 +380,7 @@ __device__ __forceinline__ void force_loop_batched(const DevAtoms &a, const DevT
 #pragma unroll
         for (int u = 0; u < UNR; ++u) {
             const unsigned row = c[u] == kSkip ? 0u : (c[u] >> kDkBits);
-            pj[u] = a.posff[j[u]];
+            pj[u] = ldg_ff(a.rec + j[u]);
             e[u] = __ldg(t.force4 + row);
         }
 #pragma unroll
@@ -383,14 +397,14 @@ __global__ void __launch_bounds__(kBlock, MINB) k_force32(DevAtoms a, DevTables 
     float fx = 0.0f, fy = 0.0f, fz = 0.0f;
     if ((a.statu[i] & MSMGB_STATU_ACTIVE) == MSMGB_STATU_ACTIVE) {
         const BoxF b = load_boxf(a.box[a.boxid[i]]);
-        const PosFF pi = a.posff[i];
+        const PosFF pi = a.rec[i];
         const int ti = MULTI ? a.ityp[i] - 1 : 0;
         const float di = pi.d;
         if (PF == 2 && !MULTI) {
             force_loop_batched<UNR>(a, t, i, pi, di, b, fx, fy, fz);
         } else {
             walk_pairs<UNR, (PF != 0)>(a.indi + i, a.pk + i, (size_t)a.ld, a.kvois[i], [&](int j, unsigned c) {
-                const PosFF pj = a.posff[j];
+                const PosFF pj = ldg_ff(a.rec + j);
                 force_pair<MULTI>(pi, pj, c, di, pj.d, ti, MULTI ? a.ityp[j] - 1 : 0, b, t, fx, fy, fz);
             });
         }
@@ -418,7 +432,7 @@ __global__ void __launch_bounds__(kBlock) k_density32s(DevAtoms a, DevTables t, 
         unsigned *__restrict__ pk = a.pk + i;
         if ((a.statu[i] & MSMGB_STATU_ACTIVE) != MSMGB_STATU_ACTIVE) {
             a.den32[i] = 0.0f;
-            a.posff[i].d = 0.0f;
+            a.rec[i] = a.posff[i];
             continue;
         }
         const BoxF b = load_boxf(a.box[a.boxid[i]]);
@@ -433,7 +447,7 @@ __global__ void __launch_bounds__(kBlock) k_density32s(DevAtoms a, DevTables t, 
 #pragma unroll
             for (int u = 0; u < UNR; ++u) j[u] = __ldg(nb + (w + u) * ld);
 #pragma unroll
-            for (int u = 0; u < UNR; ++u) p[u] = a.posff[j[u]];
+            for (int u = 0; u < UNR; ++u) p[u] = ldg_ff(a.posff + j[u]);
 #pragma unroll
             for (int u = 0; u < UNR; ++u) {
                 float dk;
@@ -448,7 +462,7 @@ __global__ void __launch_bounds__(kBlock) k_density32s(DevAtoms a, DevTables t, 
         }
         for (; w < kn; ++w) {
             const int j0 = __ldg(nb + w * ld);
-            const PosFF p0 = a.posff[j0];
+            const PosFF p0 = ldg_ff(a.posff + j0);
             float dk;
             int kk;
             const unsigned c = pair_index(pi, p0, b, t, rej, dk, kk);
@@ -472,7 +486,9 @@ __global__ void __launch_bounds__(kBlock) k_density32s(DevAtoms a, DevTables t, 
             d = fmaf(sk - (float)kk, e.y, e.x);
         }
         a.den32[i] = d;
-        a.posff[i].d = d;
+        PosFF r = pi;
+        r.d = d;
+        a.rec[i] = r;
     }
 }
 
@@ -487,7 +503,7 @@ __global__ void __launch_bounds__(kBlock) k_force32s(DevAtoms a, DevTables t, in
         float fx = 0.0f, fy = 0.0f, fz = 0.0f;
         if ((a.statu[i] & MSMGB_STATU_ACTIVE) == MSMGB_STATU_ACTIVE) {
             const BoxF b = load_boxf(a.box[a.boxid[i]]);
-            const PosFF pi = a.posff[i];
+            const PosFF pi = a.rec[i];
             const float di = pi.d;
             const int kn = a.kvois[i];
             const int *__restrict__ nb = a.indi + i;
@@ -503,7 +519,7 @@ __global__ void __launch_bounds__(kBlock) k_force32s(DevAtoms a, DevTables t, in
 #pragma unroll
                 for (int u = 0; u < UNR; ++u) {
                     if (c[u] == kSkip) continue;
-                    const PosFF pj = a.posff[j[u]];
+                    const PosFF pj = ldg_ff(a.rec + j[u]);
                     const float dj = pj.d;
                     const float sx = sep1(pi.hx, pi.lx, pj.hx, pj.lx, b.lh[0], b.ll[0], b.half[0], b.pd[0]);
                     const float sy = sep1(pi.hy, pi.ly, pj.hy, pj.ly, b.lh[1], b.ll[1], b.half[1], b.pd[1]);
@@ -545,13 +561,13 @@ __global__ void __launch_bounds__(kBlock, MINB) k_force32_vv(DevAtoms a, DevTabl
         const DevBox &bb = a.box[a.boxid[i]];
         if ((stat & MSMGB_STATU_ACTIVE) == MSMGB_STATU_ACTIVE) {
             const BoxF b = load_boxf(bb);
-            const PosFF pi = a.posff[i];
+            const PosFF pi = a.rec[i];
             const float di = pi.d;
             if (PF == 2) {
                 force_loop_batched<UNR>(a, t, i, pi, di, b, fx, fy, fz);
             } else {
                 walk_pairs<UNR, (PF != 0)>(a.indi + i, a.pk + i, (size_t)a.ld, a.kvois[i], [&](int j, unsigned c) {
-                    const PosFF pj = a.posff[j];
+                    const PosFF pj = ldg_ff(a.rec + j);
                     force_pair<false>(pi, pj, c, di, pj.d, 0, 0, b, t, fx, fy, fz);
                 });
             }

@@ -44,9 +44,9 @@ enum {
     kFlagWords = 8
 };
 
-// float-float position (hi, lo parts of u = x + ushift).  d carries the atom's FP32
-// F'(rho) from the mixed density pass, so the force pass gets a neighbour's position and
-// F'(rho) with one 32 B gather.
+// float-float position (hi, lo parts of u = x + ushift).  In the record buffer `rec` the
+// mixed density pass writes d = the atom's FP32 F'(rho) next to its position, so the force
+// pass gets a neighbour's position and F'(rho) with one 32 B gather.
 struct __align__(32) PosFF {
     float hx, hy, hz, d;
     float lx, ly, lz, lw;
@@ -109,6 +109,7 @@ struct DevAtoms {
     const double *cm;    // masses per type (0-based type index)
     const double *icm;   // reciprocal masses per type
     unsigned *pk;        // mixed passes: per-pair table index (KK << 18 | DK * 2^18), ELL layout
+    PosFF *rec;          // mixed passes: {position, F'(rho)} records written by the density pass
     int *flags;
     unsigned long long *maxdisp;
     double *virial;      // [nbox][6]
