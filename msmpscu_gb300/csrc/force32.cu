@@ -32,16 +32,23 @@ constexpr int kDkBits = 18;
 constexpr float kDkScale = 262144.0f;       // 2^18
 constexpr float kDkInv = 1.0f / 262144.0f;
 
-// read-only gather of a 32 B record (the arrays read this way are not written by the
-// kernel that reads them)
-__device__ __forceinline__ PosFF ldg_ff(const PosFF *p)
+// One 256-bit load / store per 32 B record (sm_100+ vector width): a gather of 32 lanes'
+// records then touches each sector once instead of once per 16 B half.  The records are
+// 32 B aligned (PosFF is __align__(32), buffers come from cudaMalloc).
+__device__ __forceinline__ PosFF ld_ff(const PosFF *p)
 {
-    const float4 *q = reinterpret_cast<const float4 *>(p);
-    const float4 a = __ldg(q), b = __ldg(q + 1);
     PosFF r;
-    r.hx = a.x; r.hy = a.y; r.hz = a.z; r.d = a.w;
-    r.lx = b.x; r.ly = b.y; r.lz = b.z; r.lw = b.w;
+    asm("ld.global.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=f"(r.hx), "=f"(r.hy), "=f"(r.hz), "=f"(r.d), "=f"(r.lx), "=f"(r.ly), "=f"(r.lz), "=f"(r.lw)
+        : "l"(p));
     return r;
+}
+
+__device__ __forceinline__ void st_ff(PosFF *p, const PosFF &r)
+{
+    asm volatile("st.global.v8.f32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"l"(p), "f"(r.hx), "f"(r.hy),
+                 "f"(r.hz), "f"(r.d), "f"(r.lx), "f"(r.ly), "f"(r.lz), "f"(r.lw)
+                 : "memory");
 }
 
 struct BoxF {
@@ -133,12 +140,12 @@ __global__ void __launch_bounds__(kBlock, MINB) k_density32(DevAtoms a, DevTable
     const size_t ld = (size_t)a.ld;
     if ((a.statu[i] & MSMGB_STATU_ACTIVE) != MSMGB_STATU_ACTIVE) {   // the force pass skips it
         a.den32[i] = 0.0f;
-        a.rec[i] = a.posff[i];          // d = 0
+        st_ff(a.rec + i, ld_ff(a.posff + i));          // d = 0
         return;
     }
     const BoxF b = load_boxf(a.box[a.boxid[i]]);
     const float rej = t.ru2h + 4.0f * sqrtf(t.ru2h) * b.dlmax + 1e-5f * t.ru2h;
-    const PosFF pi = a.posff[i];
+    const PosFF pi = ld_ff(a.posff + i);
     const int ti = MULTI ? a.ityp[i] - 1 : 0;
     const int *__restrict__ nb = a.indi + i;
     const float2 *__restrict__ row0 = t.dens2;
@@ -161,7 +168,7 @@ __global__ void __launch_bounds__(kBlock, MINB) k_density32(DevAtoms a, DevTable
             // all gathers first (slots past KVOIS read atom i itself and are discarded)
             PosFF p[UNR];
 #pragma unroll
-            for (int u = 0; u < UNR; ++u) p[u] = ldg_ff(a.posff + (j[u] >= 0 ? j[u] : i));
+            for (int u = 0; u < UNR; ++u) p[u] = ld_ff(a.posff + (j[u] >= 0 ? j[u] : i));
 #pragma unroll
             for (int u = 0; u < UNR; ++u) {
                 float dk = 0.0f;
@@ -183,7 +190,7 @@ __global__ void __launch_bounds__(kBlock, MINB) k_density32(DevAtoms a, DevTable
 #pragma unroll
             for (int u = 0; u < UNR; ++u) j[u] = __ldg(nb + (w + u) * ld);
 #pragma unroll
-            for (int u = 0; u < UNR; ++u) p[u] = ldg_ff(a.posff + j[u]);
+            for (int u = 0; u < UNR; ++u) p[u] = ld_ff(a.posff + j[u]);
 #pragma unroll
             for (int u = 0; u < UNR; ++u) {
                 float dk;
@@ -199,7 +206,7 @@ __global__ void __launch_bounds__(kBlock, MINB) k_density32(DevAtoms a, DevTable
         }
         for (; w < kn; ++w) {
             const int j0 = __ldg(nb + w * ld);
-            const PosFF p0 = ldg_ff(a.posff + j0);
+            const PosFF p0 = ld_ff(a.posff + j0);
             float dk;
             int kk;
             const unsigned c = pair_index(pi, p0, b, t, rej, dk, kk);
@@ -228,7 +235,7 @@ __global__ void __launch_bounds__(kBlock, MINB) k_density32(DevAtoms a, DevTable
     a.den32[i] = d;
     PosFF r = pi;
     r.d = d;
-    a.rec[i] = r;
+    st_ff(a.rec + i, r);
 }
 
 // FP32 separation for the force direction (dh exact, dl small)
@@ -380,7 +387,7 @@ __device__ __forceinline__ void force_loop_batched(const DevAtoms &a, const DevT
 #pragma unroll
         for (int u = 0; u < UNR; ++u) {
             const unsigned row = c[u] == kSkip ? 0u : (c[u] >> kDkBits);
-            pj[u] = ldg_ff(a.rec + j[u]);
+            pj[u] = ld_ff(a.rec + j[u]);
             e[u] = __ldg(t.force4 + row);
         }
 #pragma unroll
@@ -397,14 +404,14 @@ __global__ void __launch_bounds__(kBlock, MINB) k_force32(DevAtoms a, DevTables 
     float fx = 0.0f, fy = 0.0f, fz = 0.0f;
     if ((a.statu[i] & MSMGB_STATU_ACTIVE) == MSMGB_STATU_ACTIVE) {
         const BoxF b = load_boxf(a.box[a.boxid[i]]);
-        const PosFF pi = a.rec[i];
+        const PosFF pi = ld_ff(a.rec + i);
         const int ti = MULTI ? a.ityp[i] - 1 : 0;
         const float di = pi.d;
         if (PF == 2 && !MULTI) {
             force_loop_batched<UNR>(a, t, i, pi, di, b, fx, fy, fz);
         } else {
             walk_pairs<UNR, (PF != 0)>(a.indi + i, a.pk + i, (size_t)a.ld, a.kvois[i], [&](int j, unsigned c) {
-                const PosFF pj = ldg_ff(a.rec + j);
+                const PosFF pj = ld_ff(a.rec + j);
                 force_pair<MULTI>(pi, pj, c, di, pj.d, ti, MULTI ? a.ityp[j] - 1 : 0, b, t, fx, fy, fz);
             });
         }
@@ -432,12 +439,12 @@ __global__ void __launch_bounds__(kBlock) k_density32s(DevAtoms a, DevTables t, 
         unsigned *__restrict__ pk = a.pk + i;
         if ((a.statu[i] & MSMGB_STATU_ACTIVE) != MSMGB_STATU_ACTIVE) {
             a.den32[i] = 0.0f;
-            a.rec[i] = a.posff[i];
+            st_ff(a.rec + i, ld_ff(a.posff + i));
             continue;
         }
         const BoxF b = load_boxf(a.box[a.boxid[i]]);
         const float rej = t.ru2h + 4.0f * sqrtf(t.ru2h) * b.dlmax + 1e-5f * t.ru2h;
-        const PosFF pi = a.posff[i];
+        const PosFF pi = ld_ff(a.posff + i);
         const int *__restrict__ nb = a.indi + i;
         float rho = 0.0f;
         int w = 0;
@@ -447,7 +454,7 @@ __global__ void __launch_bounds__(kBlock) k_density32s(DevAtoms a, DevTables t, 
 #pragma unroll
             for (int u = 0; u < UNR; ++u) j[u] = __ldg(nb + (w + u) * ld);
 #pragma unroll
-            for (int u = 0; u < UNR; ++u) p[u] = ldg_ff(a.posff + j[u]);
+            for (int u = 0; u < UNR; ++u) p[u] = ld_ff(a.posff + j[u]);
 #pragma unroll
             for (int u = 0; u < UNR; ++u) {
                 float dk;
@@ -462,7 +469,7 @@ __global__ void __launch_bounds__(kBlock) k_density32s(DevAtoms a, DevTables t, 
         }
         for (; w < kn; ++w) {
             const int j0 = __ldg(nb + w * ld);
-            const PosFF p0 = ldg_ff(a.posff + j0);
+            const PosFF p0 = ld_ff(a.posff + j0);
             float dk;
             int kk;
             const unsigned c = pair_index(pi, p0, b, t, rej, dk, kk);
@@ -488,7 +495,7 @@ __global__ void __launch_bounds__(kBlock) k_density32s(DevAtoms a, DevTables t, 
         a.den32[i] = d;
         PosFF r = pi;
         r.d = d;
-        a.rec[i] = r;
+        st_ff(a.rec + i, r);
     }
 }
 
@@ -503,7 +510,7 @@ __global__ void __launch_bounds__(kBlock) k_force32s(DevAtoms a, DevTables t, in
         float fx = 0.0f, fy = 0.0f, fz = 0.0f;
         if ((a.statu[i] & MSMGB_STATU_ACTIVE) == MSMGB_STATU_ACTIVE) {
             const BoxF b = load_boxf(a.box[a.boxid[i]]);
-            const PosFF pi = a.rec[i];
+            const PosFF pi = ld_ff(a.rec + i);
             const float di = pi.d;
             const int kn = a.kvois[i];
             const int *__restrict__ nb = a.indi + i;
@@ -519,7 +526,7 @@ __global__ void __launch_bounds__(kBlock) k_force32s(DevAtoms a, DevTables t, in
 #pragma unroll
                 for (int u = 0; u < UNR; ++u) {
                     if (c[u] == kSkip) continue;
-                    const PosFF pj = ldg_ff(a.rec + j[u]);
+                    const PosFF pj = ld_ff(a.rec + j[u]);
                     const float dj = pj.d;
                     const float sx = sep1(pi.hx, pi.lx, pj.hx, pj.lx, b.lh[0], b.ll[0], b.half[0], b.pd[0]);
                     const float sy = sep1(pi.hy, pi.ly, pj.hy, pj.ly, b.lh[1], b.ll[1], b.half[1], b.pd[1]);
@@ -561,13 +568,13 @@ __global__ void __launch_bounds__(kBlock, MINB) k_force32_vv(DevAtoms a, DevTabl
         const DevBox &bb = a.box[a.boxid[i]];
         if ((stat & MSMGB_STATU_ACTIVE) == MSMGB_STATU_ACTIVE) {
             const BoxF b = load_boxf(bb);
-            const PosFF pi = a.rec[i];
+            const PosFF pi = ld_ff(a.rec + i);
             const float di = pi.d;
             if (PF == 2) {
                 force_loop_batched<UNR>(a, t, i, pi, di, b, fx, fy, fz);
             } else {
                 walk_pairs<UNR, (PF != 0)>(a.indi + i, a.pk + i, (size_t)a.ld, a.kvois[i], [&](int j, unsigned c) {
-                    const PosFF pj = ldg_ff(a.rec + j);
+                    const PosFF pj = ld_ff(a.rec + j);
                     force_pair<false>(pi, pj, c, di, pj.d, 0, 0, b, t, fx, fy, fz);
                 });
             }
