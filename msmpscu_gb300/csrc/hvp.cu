@@ -44,7 +44,11 @@ __global__ void __launch_bounds__(kBlock) k_hvp_density(DevAtoms a, DevTables t,
         dd[i] = make_double2(0.0, 0.0);
         return;
     }
+    // box parameters in registers: the per-pair stores below could alias the box array
     const DevBox &b = a.box[a.boxid[i]];
+    const double lx = b.len[0], ly = b.len[1], lz = b.len[2];
+    const double hx = b.half[0], hy = b.half[1], hz = b.half[2];
+    const int px = b.ifpd[0], py = b.ifpd[1], pz = b.ifpd[2];
     const double4_32a p = a.pos[i];
     const double4_32a vi = v[i];
     const int ti = a.ityp[i] - 1;
@@ -54,9 +58,9 @@ __global__ void __launch_bounds__(kBlock) k_hvp_density(DevAtoms a, DevTables t,
     for (int w = 0; w < kn; ++w) {
         int j = __ldg(a.indi + i + w * ld);
         double4_32a q = a.pos[j];
-        double sx = mi(p.x - q.x, b.len[0], b.half[0], b.ifpd[0]);
-        double sy = mi(p.y - q.y, b.len[1], b.half[1], b.ifpd[1]);
-        double sz = mi(p.z - q.z, b.len[2], b.half[2], b.ifpd[2]);
+        double sx = mi(p.x - q.x, lx, hx, px);
+        double sy = mi(p.y - q.y, ly, hy, py);
+        double sz = mi(p.z - q.z, lz, hz, pz);
         double r2 = sx * sx + sy * sy + sz * sz;
         if (r2 > t.ru2) {
             pg[w * ld + i] = make_double4_32a(0.0, 0.0, 0.0, 0.0);   // beyond RU: skipped later

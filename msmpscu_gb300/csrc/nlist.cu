@@ -227,57 +227,77 @@ __device__ __forceinline__ float mi32(float s, float len, float half, int pd)
     return (pd && fabsf(s) > half) ? s - copysignf(len, s) : s;
 }
 
-// Full neighbour list, one thread per (sorted) atom.
+// Full neighbour list, one thread per (sorted) atom.  The box parameters are copied into
+// registers first: the list stores in the loop could alias the box array, so reading them
+// through a reference would reload them for every candidate.
 __global__ void __launch_bounds__(kBlock) k_build(DevAtoms a, const int *cell_of, const int *start,
                                                   double rc2, float d2lo, float d2hi, int predicated)
 {
     if (skip_rebuild(a.flags, predicated)) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
-    double4_32a p = a.pos[i];
+    const double4_32a p = a.pos[i];
     const PosFF pf = a.posff[i];
     a.pos_bld[i] = make_float4(pf.hx, pf.hy, pf.hz, 0.0f);
     if (a.statu[i] & MSMGB_STATU_OUTOFBOX) { a.kvois[i] = 0; return; }
-    const DevBox &b = a.box[a.boxid[i]];
-    int c = cell_of[i] - b.cell0;
-    int ix = c % b.nc[0], iy = (c / b.nc[0]) % b.nc[1], iz = c / (b.nc[0] * b.nc[1]);
+    const DevBox &bref = a.box[a.boxid[i]];
+    int nc[3], pd[3];
+    float lf[3], hf[3];
+    double ld64[3], hd64[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        nc[k] = bref.nc[k];
+        pd[k] = bref.ifpd[k];
+        lf[k] = bref.lenf[k];
+        hf[k] = bref.halff[k];
+        ld64[k] = bref.len[k];
+        hd64[k] = bref.half[k];
+    }
+    const int cell0 = bref.cell0;
+    const int c = cell_of[i] - cell0;
+    const int ix = c % nc[0], iy = (c / nc[0]) % nc[1], iz = c / (nc[0] * nc[1]);
     int nn = 0;
-    const int ld = a.ld, mxk = a.mxk;
+    const size_t ld = (size_t)a.ld;
+    const int mxk = a.mxk;
+    int *const indi = a.indi + i;
+    const PosFF *const posff = a.posff;
+    const double4_32a *const pos = a.pos;
     for (int s = 0; s < 27; ++s) {
         int j3[3] = {ix + c_nix[s], iy + c_niy[s], iz + c_niz[s]};
         bool skip = false;
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
-            if (b.ifpd[k]) {
-                if (j3[k] >= b.nc[k]) j3[k] = 0;
-                else if (j3[k] < 0) j3[k] = b.nc[k] - 1;
+            if (pd[k]) {
+                if (j3[k] >= nc[k]) j3[k] = 0;
+                else if (j3[k] < 0) j3[k] = nc[k] - 1;
             }
-            if (j3[k] < 0 || j3[k] >= b.nc[k]) skip = true;
+            if (j3[k] < 0 || j3[k] >= nc[k]) skip = true;
         }
         if (skip) continue;
-        int g = b.cell0 + j3[0] + b.nc[0] * (j3[1] + b.nc[1] * j3[2]);
-        int e = start[g + 1];
+        const int g = cell0 + j3[0] + nc[0] * (j3[1] + nc[1] * j3[2]);
+        const int e = start[g + 1];
         for (int j = start[g]; j < e; ++j) {
             if (j == i) continue;
-            const PosFF q = a.posff[j];
-            float sx = mi32(pf.hx - q.hx, b.lenf[0], b.halff[0], b.ifpd[0]);
-            float sy = mi32(pf.hy - q.hy, b.lenf[1], b.halff[1], b.ifpd[1]);
-            float sz = mi32(pf.hz - q.hz, b.lenf[2], b.halff[2], b.ifpd[2]);
-            float d2f = sx * sx + sy * sy + sz * sz;
+            // hi parts only (first 16 B of the record)
+            const float4 q = *reinterpret_cast<const float4 *>(posff + j);
+            const float sx = mi32(pf.hx - q.x, lf[0], hf[0], pd[0]);
+            const float sy = mi32(pf.hy - q.y, lf[1], hf[1], pd[1]);
+            const float sz = mi32(pf.hz - q.z, lf[2], hf[2], pd[2]);
+            const float d2f = sx * sx + sy * sy + sz * sz;
             bool in;
             if (d2f < d2lo) {
                 in = true;
             } else if (d2f > d2hi) {
                 in = false;
             } else {        // narrow band: the exact FP64 rule of the oracle
-                double4_32a qd = a.pos[j];
-                double dx = mi64(p.x - qd.x, b.len[0], b.half[0], b.ifpd[0]);
-                double dy = mi64(p.y - qd.y, b.len[1], b.half[1], b.ifpd[1]);
-                double dz = mi64(p.z - qd.z, b.len[2], b.half[2], b.ifpd[2]);
+                const double4_32a qd = pos[j];
+                const double dx = mi64(p.x - qd.x, ld64[0], hd64[0], pd[0]);
+                const double dy = mi64(p.y - qd.y, ld64[1], hd64[1], pd[1]);
+                const double dz = mi64(p.z - qd.z, ld64[2], hd64[2], pd[2]);
                 in = (dx * dx + dy * dy + dz * dz) < rc2;
             }
             if (in) {
-                if (nn < mxk) a.indi[(size_t)nn * (size_t)ld + (size_t)i] = j;
+                if (nn < mxk) indi[(size_t)nn * ld] = j;
                 ++nn;
             }
         }
