@@ -227,78 +227,96 @@ __device__ __forceinline__ float mi32(float s, float len, float half, int pd)
     return (pd && fabsf(s) > half) ? s - copysignf(len, s) : s;
 }
 
-// Full neighbour list, one thread per (sorted) atom.  The box parameters are copied into
-// registers first: the list stores in the loop could alias the box array, so reading them
-// through a reference would reload them for every candidate.
+// Records a candidate that passed the FP32 test or, inside the narrow band around the
+// cutoff, the exact FP64 rule of the oracle.
+__device__ __forceinline__ bool accept(float d2f, float d2lo, float d2hi, const DevAtoms &a, int i, int j,
+                                       const DevBox &b, double rc2)
+{
+    if (d2f < d2lo) return true;
+    if (d2f > d2hi) return false;
+    const double4_32a p = a.pos[i];
+    const double4_32a qd = a.pos[j];
+    const double dx = mi64(p.x - qd.x, b.len[0], b.half[0], b.ifpd[0]);
+    const double dy = mi64(p.y - qd.y, b.len[1], b.half[1], b.ifpd[1]);
+    const double dz = mi64(p.z - qd.z, b.len[2], b.half[2], b.ifpd[2]);
+    return (dx * dx + dy * dy + dz * dz) < rc2;
+}
+
+// Full neighbour list, one thread per (sorted) atom.  Cells of a box are at least rc_nl
+// wide unless the box forced NCELL to 3 (the reference's rule for small boxes); in the wide
+// case the periodic image of every candidate is the one of its stencil cell, so the
+// separation is the exact hi-part difference plus a per-cell shift of -L, 0 or +L, with no
+// per-candidate minimum-image test.  Narrow boxes take the minimum image per candidate.
 __global__ void __launch_bounds__(kBlock) k_build(DevAtoms a, const int *cell_of, const int *start,
                                                   double rc2, float d2lo, float d2hi, int predicated)
 {
     if (skip_rebuild(a.flags, predicated)) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
-    const double4_32a p = a.pos[i];
     const PosFF pf = a.posff[i];
     a.pos_bld[i] = make_float4(pf.hx, pf.hy, pf.hz, 0.0f);
     if (a.statu[i] & MSMGB_STATU_OUTOFBOX) { a.kvois[i] = 0; return; }
-    const DevBox &bref = a.box[a.boxid[i]];
+    const DevBox &b = a.box[a.boxid[i]];
     int nc[3], pd[3];
-    float lf[3], hf[3];
-    double ld64[3], hd64[3];
+    float lf[3];
+    bool wide = true;
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-        nc[k] = bref.nc[k];
-        pd[k] = bref.ifpd[k];
-        lf[k] = bref.lenf[k];
-        hf[k] = bref.halff[k];
-        ld64[k] = bref.len[k];
-        hd64[k] = bref.half[k];
+        nc[k] = b.nc[k];
+        pd[k] = b.ifpd[k];
+        lf[k] = b.lenf[k];
+        const double w = b.len[k] / nc[k];
+        if (pd[k] && w * w < rc2) wide = false;
     }
-    const int cell0 = bref.cell0;
+    const int cell0 = b.cell0;
     const int c = cell_of[i] - cell0;
     const int ix = c % nc[0], iy = (c / nc[0]) % nc[1], iz = c / (nc[0] * nc[1]);
     int nn = 0;
     const size_t ld = (size_t)a.ld;
     const int mxk = a.mxk;
     int *const indi = a.indi + i;
-    const PosFF *const posff = a.posff;
-    const double4_32a *const pos = a.pos;
+    const float4 *const hi = reinterpret_cast<const float4 *>(a.posff);   // record = 2 float4
     for (int s = 0; s < 27; ++s) {
         int j3[3] = {ix + c_nix[s], iy + c_niy[s], iz + c_niz[s]};
+        float sh[3];
         bool skip = false;
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
+            sh[k] = 0.0f;
             if (pd[k]) {
-                if (j3[k] >= nc[k]) j3[k] = 0;
-                else if (j3[k] < 0) j3[k] = nc[k] - 1;
+                // candidate cell wrapped to the other end: its image lies one box length away
+                if (j3[k] >= nc[k]) { j3[k] = 0; sh[k] = -lf[k]; }
+                else if (j3[k] < 0) { j3[k] = nc[k] - 1; sh[k] = lf[k]; }
             }
             if (j3[k] < 0 || j3[k] >= nc[k]) skip = true;
         }
         if (skip) continue;
         const int g = cell0 + j3[0] + nc[0] * (j3[1] + nc[1] * j3[2]);
-        const int e = start[g + 1];
-        for (int j = start[g]; j < e; ++j) {
-            if (j == i) continue;
-            // hi parts only (first 16 B of the record)
-            const float4 q = *reinterpret_cast<const float4 *>(posff + j);
-            const float sx = mi32(pf.hx - q.x, lf[0], hf[0], pd[0]);
-            const float sy = mi32(pf.hy - q.y, lf[1], hf[1], pd[1]);
-            const float sz = mi32(pf.hz - q.z, lf[2], hf[2], pd[2]);
-            const float d2f = sx * sx + sy * sy + sz * sz;
-            bool in;
-            if (d2f < d2lo) {
-                in = true;
-            } else if (d2f > d2hi) {
-                in = false;
-            } else {        // narrow band: the exact FP64 rule of the oracle
-                const double4_32a qd = pos[j];
-                const double dx = mi64(p.x - qd.x, ld64[0], hd64[0], pd[0]);
-                const double dy = mi64(p.y - qd.y, ld64[1], hd64[1], pd[1]);
-                const double dz = mi64(p.z - qd.z, ld64[2], hd64[2], pd[2]);
-                in = (dx * dx + dy * dy + dz * dz) < rc2;
+        const int j0 = start[g], e = start[g + 1];
+        if (wide) {
+            for (int j = j0; j < e; ++j) {
+                const float4 q = hi[2 * (size_t)j];
+                const float sx = (pf.hx - q.x) + sh[0];      // hi difference exact (Sterbenz)
+                const float sy = (pf.hy - q.y) + sh[1];
+                const float sz = (pf.hz - q.z) + sh[2];
+                const float d2f = fmaf(sx, sx, fmaf(sy, sy, sz * sz));
+                if (j != i && accept(d2f, d2lo, d2hi, a, i, j, b, rc2)) {
+                    if (nn < mxk) indi[(size_t)nn * ld] = j;
+                    ++nn;
+                }
             }
-            if (in) {
-                if (nn < mxk) indi[(size_t)nn * ld] = j;
-                ++nn;
+        } else {
+            const float h0 = b.halff[0], h1 = b.halff[1], h2 = b.halff[2];
+            for (int j = j0; j < e; ++j) {
+                const float4 q = hi[2 * (size_t)j];
+                const float sx = mi32(pf.hx - q.x, lf[0], h0, pd[0]);
+                const float sy = mi32(pf.hy - q.y, lf[1], h1, pd[1]);
+                const float sz = mi32(pf.hz - q.z, lf[2], h2, pd[2]);
+                const float d2f = fmaf(sx, sx, fmaf(sy, sy, sz * sz));
+                if (j != i && accept(d2f, d2lo, d2hi, a, i, j, b, rc2)) {
+                    if (nn < mxk) indi[(size_t)nn * ld] = j;
+                    ++nn;
+                }
             }
         }
     }
