@@ -5,7 +5,7 @@ TB-SMA, sigma 0.05 A, 600 K, NVE velocity Verlet dt = 1 fs, skin trigger 0.15 A.
 One step = fused corrector/predictor + skin check (+ device list rebuild when triggered) +
 density pass + force pass, all on one GPU.  Prints one JSON line (see the keys below).
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--precision mixed|fp64]
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--precision mixed|fp64|ff]
                   [--impl ours|reference]
 
 --impl reference times the CPU restatement of the reference's serial path (the oracle, the
@@ -128,24 +128,29 @@ def workload(ncell=NCELL):
 
 
 def precision_compare(e, box, pos, vel, steps):
-    """FP64 form on the same state: its atom-steps/s and the mixed force error against it
-    (norm-wise and max-abs, relative).  The FP64 form is itself parity-checked against the
-    oracle at 1e-10 by the GPU tests."""
+    """FP64 form and float-float form on the same state: their atom-steps/s, and the mixed
+    and float-float force errors against the FP64 forces (norm-wise and max-abs, relative).
+    Both are parity-checked against the oracle at 1e-10 by the GPU tests."""
     e.copyin(box, pos, vel)
     e.set_precision("fp64")
     e.calforce()
     f64 = e.get_force()
+    out = {}
+    for prec in ("mixed", "ff"):
+        e.set_precision(prec)
+        e.calforce()
+        d = e.get_force() - f64
+        out[prec + "_force_err_norm"] = float(np.linalg.norm(d) / np.linalg.norm(f64))
+        out[prec + "_force_err_max"] = float(np.abs(d).max() / np.abs(f64).max())
+    for prec in ("fp64", "ff"):
+        e.copyin(box, pos, vel)
+        e.set_precision(prec)
+        e.run_steps(3, DT)
+        ms, _ = e.time_steps(steps, DT)
+        out[prec + "_value"] = len(pos) * steps / (ms / 1e3)
     e.set_precision("mixed")
-    e.calforce()
-    f32 = e.get_force()
-    d = f32 - f64
-    err_norm = float(np.linalg.norm(d) / np.linalg.norm(f64))
-    err_max = float(np.abs(d).max() / np.abs(f64).max())
-    e.set_precision("fp64")
-    e.run_steps(3, DT)
-    ms64, _ = e.time_steps(steps, DT)
-    e.set_precision("mixed")
-    return err_norm, err_max, len(pos) * steps / (ms64 / 1e3)
+    e.copyin(box, pos, vel)
+    return out
 
 
 def batched_uneven_boxes(steps, steps_perbox, device=0):
@@ -400,9 +405,12 @@ def run_ours(args):
 
     cmp = None
     if prec == "mixed" and not args.no_compare:
-        en, em, v64 = precision_compare(e, box, pos, vel, max(3, min(args.steps, 40)))
-        cmp = {"fp64_value": v64, "mixed_value": value / ws, "speedup": value / ws / v64,
-               "mixed_force_err_norm": en, "mixed_force_err_max": em}
+        pc = precision_compare(e, box, pos, vel, max(3, min(args.steps, 40)))
+        cmp = {"fp64_value": pc["fp64_value"], "mixed_value": value / ws,
+               "speedup": value / ws / pc["fp64_value"],
+               "mixed_force_err_norm": pc["mixed_force_err_norm"], "mixed_force_err_max": pc["mixed_force_err_max"],
+               "ff_value": pc["ff_value"], "ff_speedup_vs_fp64": pc["ff_value"] / pc["fp64_value"],
+               "ff_force_err_norm": pc["ff_force_err_norm"], "ff_force_err_max": pc["ff_force_err_max"]}
 
     extras = {}
     if not args.no_extras:

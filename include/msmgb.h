@@ -42,8 +42,12 @@ extern "C" {
 
 /* ---- arithmetic of the force passes ---------------------------------------------------- */
 #define MSMGB_PREC_FP64  0   /* plain FP64, the reference's arithmetic                   */
-#define MSMGB_PREC_MIXED 1   /* FP32 pair/density/table terms, FP64 accumulation,
+#define MSMGB_PREC_MIXED 1   /* FP32 pair, density and table terms and sums on an exact
+                                float-float table index (force error <= 1e-6 relative);
                                 FP64 positions and integration                           */
+#define MSMGB_PREC_FF    2   /* float-float (two FP32 numbers per value) force passes:
+                                FP64 parity (<= 1e-10 relative) on the FP32 pipe; the
+                                virial and per-atom energy calls use the FP64 passes     */
 
 /* ---- atom status bits (MD_Const.F90:78-96) ---------------------------------------------- */
 #define MSMGB_STATU_ACTIVE    1
@@ -74,7 +78,7 @@ typedef struct {
     double skin_trigger;  /* rebuild when max displacement since the last build exceeds
                              this (> 0); <= 0 selects the reference's fixed interval      */
     int    nb_uptab;      /* NB_UPTAB: rebuild interval when skin_trigger <= 0            */
-    int    precision;     /* MSMGB_PREC_FP64 or MSMGB_PREC_MIXED                          */
+    int    precision;     /* MSMGB_PREC_FP64, MSMGB_PREC_MIXED or MSMGB_PREC_FF           */
     void  *stream;        /* cudaStream_t to issue on; NULL = the context makes its own   */
 } msmgb_params;
 

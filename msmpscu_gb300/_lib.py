@@ -10,7 +10,8 @@ OK = 0
 ERR_ARG, ERR_CUDA, ERR_NL_OVERFLOW, ERR_OUT_OF_BOX = -1, -2, -3, -4
 ERR_RHO_RANGE, ERR_BOX_TOO_SMALL, ERR_NO_DEVICE, ERR_CAPACITY = -5, -6, -7, -8
 FS_TYPE, EAM_TYPE = 0, 1
-PREC_FP64, PREC_MIXED = 0, 1
+PREC_FP64, PREC_MIXED, PREC_FF = 0, 1, 2
+PRECISIONS = {"fp64": PREC_FP64, "mixed": PREC_MIXED, "ff": PREC_FF}
 ORDER_ORIGINAL, ORDER_SORTED = 0, 1
 POT_CR, POT_MARINICA2, POT_ACKLAND_WW = 1, 2, 3
 STATU_ACTIVE = 1

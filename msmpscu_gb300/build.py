@@ -10,7 +10,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libmsmgb.so")
-CU_SOURCES = ["context.cu", "nlist.cu", "force64.cu", "force32.cu", "vv.cu", "hvp.cu", "adjoint.cu", "noalloc.cu"]
+CU_SOURCES = ["context.cu", "nlist.cu", "force64.cu", "force32.cu", "forceff.cu", "vv.cu", "hvp.cu", "adjoint.cu", "noalloc.cu"]
 CPP_SOURCES = ["tables.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

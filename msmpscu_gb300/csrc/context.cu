@@ -9,6 +9,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdint>
 #include <cstring>
 
 #include "msmgb_internal.cuh"
@@ -155,7 +156,8 @@ extern "C" int msmgb_create(msmgb_ctx **out, const msmgb_params *p)
     *out = nullptr;
     if (p->max_atoms <= 0 || p->max_boxes <= 0 || p->mxkvois <= 0 || p->rc_nl <= 0.0)
         return MSMGB_ERR_ARG;
-    if (p->precision != MSMGB_PREC_FP64 && p->precision != MSMGB_PREC_MIXED) return MSMGB_ERR_ARG;
+    if (p->precision != MSMGB_PREC_FP64 && p->precision != MSMGB_PREC_MIXED && p->precision != MSMGB_PREC_FF)
+        return MSMGB_ERR_ARG;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= p->device || p->device < 0) {
         cudaGetLastError();
@@ -209,8 +211,10 @@ extern "C" int msmgb_create(msmgb_ctx **out, const msmgb_params *p)
     if ((e = cudaMemsetAsync(c->maxdisp, 0, sizeof(unsigned long long), c->stream)) != cudaSuccess) return fail(e, "memset");
     if (p->precision == MSMGB_PREC_MIXED && (e = dalloc(&a.pk, N * (size_t)p->mxkvois)) != cudaSuccess)
         return fail(e, "cudaMalloc pair index");
-    if (p->precision == MSMGB_PREC_MIXED && (e = dalloc(&a.rec, N)) != cudaSuccess)
+    if (p->precision != MSMGB_PREC_FP64 && (e = dalloc(&a.rec, N)) != cudaSuccess)
         return fail(e, "cudaMalloc records");
+    if (p->precision == MSMGB_PREC_FF && ((e = dalloc(&a.posfx, N)) != cudaSuccess || (e = dalloc(&a.recfx, N)) != cudaSuccess))
+        return fail(e, "cudaMalloc float-float records");
     a.flags = c->flags;
     a.maxdisp = c->maxdisp;
     a.virial = c->virial;
@@ -231,7 +235,7 @@ extern "C" int msmgb_destroy(msmgb_ctx *c)
     DevAtoms &a = c->a;
     void *ptrs[] = {a.pos, a.posff, a.pos_bld, a.vx, a.vy, a.vz, a.fx, a.fy, a.fz,
                     a.dx, a.dy, a.dz, a.ityp, a.statu, a.gid, a.boxid, a.den, a.epot,
-                    a.den32, a.kvois, a.indi, a.pk, a.rec, c->cell_of, c->perm, c->dbox, c->cm, c->icm,
+                    a.den32, a.kvois, a.indi, a.pk, a.rec, a.posfx, a.recfx, c->cell_of, c->perm, c->dbox, c->cm, c->icm,
                     c->flags, c->maxdisp, c->virial, c->scratch, c->cell_start,
                     c->cell_cursor, c->scan_tmp, c->tab_mem, c->adj_mem, c->hvp_pair, c->pos2, c->posff2};
     for (void *q : ptrs)
@@ -250,14 +254,20 @@ extern "C" int64_t msmgb_launch_count(const msmgb_ctx *c) { return c ? c->launch
 extern "C" int msmgb_set_precision(msmgb_ctx *c, int precision)
 {
     if (!c) return MSMGB_ERR_ARG;
-    if (precision != MSMGB_PREC_FP64 && precision != MSMGB_PREC_MIXED)
-        return set_err(c, MSMGB_ERR_ARG, "precision must be MSMGB_PREC_FP64 or MSMGB_PREC_MIXED");
+    if (precision != MSMGB_PREC_FP64 && precision != MSMGB_PREC_MIXED && precision != MSMGB_PREC_FF)
+        return set_err(c, MSMGB_ERR_ARG, "precision must be MSMGB_PREC_FP64, MSMGB_PREC_MIXED or MSMGB_PREC_FF");
     if (precision == MSMGB_PREC_MIXED && !c->a.pk) {
         RET(use_device(c));
         CK(cudaStreamSynchronize(c->stream), "synchronize");
         CK(dalloc(&c->a.pk, (size_t)c->cap_atoms * (size_t)c->p.mxkvois), "cudaMalloc pair index");
     }
-    if (precision == MSMGB_PREC_MIXED && !c->a.rec) {
+    if (precision == MSMGB_PREC_FF && !c->a.posfx) {
+        RET(use_device(c));
+        CK(cudaStreamSynchronize(c->stream), "synchronize");
+        CK(dalloc(&c->a.posfx, (size_t)c->cap_atoms), "cudaMalloc float-float records");
+        CK(dalloc(&c->a.recfx, (size_t)c->cap_atoms), "cudaMalloc float-float records");
+    }
+    if (precision != MSMGB_PREC_FP64 && !c->a.rec) {
         RET(use_device(c));
         CK(dalloc(&c->a.rec, (size_t)c->cap_atoms), "cudaMalloc records");
     }
@@ -378,16 +388,51 @@ extern "C" int msmgb_init_forcetable(msmgb_ctx *c, const msmgb_forcetable *ft)
                 e2[2 * o + 1] = (float)(hdf[o1] - hdf[o]);
             }
     }
+    // float-float tables: value and FP64 slope, each split into hi + lo
+    auto split = [](double v, float *o) {
+        o[0] = (float)v;
+        o[1] = (float)(v - (double)o[0]);
+    };
+    std::vector<float> fd((size_t)4 * nk * rowp), ff8((size_t)8 * nk * rowp), fe((size_t)4 * nk1 * nep);
+    for (size_t k = 0; k < nk; ++k)
+        for (size_t i = 0; i < rowp; ++i) {
+            size_t o = k * rowp + i, o1 = i + 1 < rowp ? o + 1 : o;
+            split(hpotb[o], &fd[4 * o]);
+            split(hpotb[o1] - hpotb[o], &fd[4 * o + 2]);
+            split(hfpotr[o], &ff8[8 * o]);
+            split(hfpotr[o1] - hfpotr[o], &ff8[8 * o + 2]);
+            split(hfpotb[o], &ff8[8 * o + 4]);
+            split(hfpotb[o1] - hfpotb[o], &ff8[8 * o + 6]);
+        }
+    if (eam) {
+        const double *hdf = hpotr + 4 * nk * rowp + nk1 * nep;
+        for (size_t k = 0; k < nk1; ++k)
+            for (size_t i = 0; i < nep; ++i) {
+                size_t o = k * nep + i, o1 = i + 1 < nep ? o + 1 : o;
+                split(hdf[o], &fe[4 * o]);
+                split(hdf[o1] - hdf[o], &fe[4 * o + 2]);
+            }
+    }
     CK(cudaStreamSynchronize(c->stream), "synchronize");
     if (c->tab_mem) { cudaFree(c->tab_mem); c->tab_mem = nullptr; }
-    const size_t bytes = nd * sizeof(double) + (f2.size() + f4.size() + e2.size()) * sizeof(float) + 1024;
+    const size_t bytes = nd * sizeof(double) +
+                         (f2.size() + f4.size() + e2.size() + fd.size() + ff8.size() + fe.size()) * sizeof(float) +
+                         2048;
     CK(cudaMalloc(&c->tab_mem, bytes), "table alloc");
     char *base = (char *)c->tab_mem;
     double *dd = (double *)base;
     float *df4 = (float *)(base + ((nd * sizeof(double) + 255) / 256) * 256);
     float *df2 = df4 + f4.size();
     float *de2 = df2 + f2.size();
+    // float4 rows: 16-byte aligned offsets
+    const uintptr_t a16 = ((uintptr_t)(de2 + e2.size()) + 15) & ~(uintptr_t)15;
+    float *dfd = (float *)a16;
+    float *dff8 = dfd + fd.size();
+    float *dfe = dff8 + ff8.size();
     CK(cudaMemcpy(dd, hd.data(), nd * sizeof(double), cudaMemcpyHostToDevice), "table upload");
+    CK(cudaMemcpy(dfd, fd.data(), fd.size() * sizeof(float), cudaMemcpyHostToDevice), "table upload");
+    CK(cudaMemcpy(dff8, ff8.data(), ff8.size() * sizeof(float), cudaMemcpyHostToDevice), "table upload");
+    if (eam) CK(cudaMemcpy(dfe, fe.data(), fe.size() * sizeof(float), cudaMemcpyHostToDevice), "table upload");
     CK(cudaMemcpy(df4, f4.data(), f4.size() * sizeof(float), cudaMemcpyHostToDevice), "table upload");
     CK(cudaMemcpy(df2, f2.data(), f2.size() * sizeof(float), cudaMemcpyHostToDevice), "table upload");
     if (eam) CK(cudaMemcpy(de2, e2.data(), e2.size() * sizeof(float), cudaMemcpyHostToDevice), "table upload");
@@ -399,6 +444,14 @@ extern "C" int msmgb_init_forcetable(msmgb_ctx *c, const msmgb_forcetable *ft)
     t.force4 = (const float4 *)df4;
     t.dens2 = (const float2 *)df2;
     t.embd2 = eam ? (const float2 *)de2 : nullptr;
+    t.densff = (const float4 *)dfd;
+    t.forceff = (const float4 *)dff8;
+    t.embff = eam ? (const float4 *)dfe : nullptr;
+    {
+        const double ir = 1.0 / t.rhod;
+        t.irhodh = (float)ir;
+        t.irhodl = (float)(ir - (double)t.irhodh);
+    }
     t.csih = (float)t.csi;
     t.csil = (float)(t.csi - (double)t.csih);
     t.ru2h = (float)t.ru2;
@@ -466,6 +519,12 @@ extern "C" int msmgb_copyin_simbox(msmgb_ctx *c, int nbox, const msmgb_box *boxe
         {   // |lo_i - lo_j| <= ulp(2L) (u in [L, 2L]) and |L - float(L)| <= ulp(L)/2
             double ext = 2.0 * std::max(d.len[0], std::max(d.len[1], d.len[2]));
             d.dlmax = (float)(2.0 * ldexp(1.0, ilogb(ext) - 23));
+            // float-float passes: remainders u - float(u) (|.| <= ulp(2L)/2) in units of
+            // 2^-30 ulp(2L), i.e. |q| <= 2^29
+            const double ulp2l = ldexp(1.0, ilogb(ext) - 23);
+            d.fxq = (float)ldexp(ulp2l, -30);
+            d.fxinv = ldexp(1.0, 30) / ulp2l;
+            for (int k = 0; k < 3; ++k) d.lq[k] = (int)llrint((d.len[k] - (double)d.lenf[k]) * d.fxinv);
         }
         long nb = (long)d.nc[0] * d.nc[1] * d.nc[2];
         if ((long)cells + nb > (1L << 24) - 2) return set_err(c, MSMGB_ERR_CAPACITY, "too many cells");
@@ -695,6 +754,9 @@ static int force_passes(msmgb_ctx *c, bool virial, bool epot)
         }
         RET(launch_density32(c));
         RET(launch_force32(c));
+    } else if (c->p.precision == MSMGB_PREC_FF && !virial && !epot) {
+        RET(launch_density_ff(c));
+        RET(launch_force_ff(c));
     } else {
         RET(launch_density(c, epot));
         RET(launch_force(c, virial));
@@ -1094,6 +1156,7 @@ extern "C" int msmgb_time_passes(msmgb_ctx *c, int reps, float *out)
     RET(ready_for_force(c));
     if (!c->have_masses) return set_err(c, MSMGB_ERR_ARG, "no masses: call msmgb_set_masses");
     const bool mixed = c->p.precision == MSMGB_PREC_MIXED;
+    const bool ffp = c->p.precision == MSMGB_PREC_FF;
     const bool fused = fused_mixed(c) && c->pos2;
     cudaEvent_t ev[2];
     CK(cudaEventCreate(&ev[0]), "event");
@@ -1109,8 +1172,8 @@ extern "C" int msmgb_time_passes(msmgb_ctx *c, int reps, float *out)
             CK(cudaStreamSynchronize(c->stream), "synchronize");
             CK(cudaEventRecord(ev[0], c->stream), "event");
             int rc = MSMGB_OK;
-            if (which == 0) rc = mixed ? launch_density32(c) : launch_density(c, false);
-            else if (which == 1) rc = mixed ? launch_force32(c) : launch_force(c, false);
+            if (which == 0) rc = mixed ? launch_density32(c) : (ffp ? launch_density_ff(c) : launch_density(c, false));
+            else if (which == 1) rc = mixed ? launch_force32(c) : (ffp ? launch_force_ff(c) : launch_force(c, false));
             else if (which == 2) rc = build_list(c, false);
             else if (which == 3) rc = launch_vv(c, 0.0, 2);
             else {

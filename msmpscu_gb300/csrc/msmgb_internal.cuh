@@ -52,6 +52,16 @@ struct __align__(32) PosFF {
     float lx, ly, lz, lw;
 };
 
+// Position record of the float-float passes: hi = float(u) of u = x + ushift and the exact
+// remainder u - hi as an integer multiple of the box's quantum (fxq = 2^-30 of the largest
+// ulp of hi), so separations and image shifts are exact integer differences; dh, dl carry
+// F'(rho) in the records written by the float-float density pass.
+struct __align__(32) PosFX {
+    float hx, hy, hz;
+    int qx, qy, qz;
+    float dh, dl;
+};
+
 struct DevBox {
     double lo[3];
     double len[3];
@@ -62,6 +72,9 @@ struct DevBox {
     float lenlo[3];
     float halff[3];
     float dlmax;         // bound on the low part of a float-float separation component
+    float fxq;           // float-float passes: quantum of the integer remainders (power of 2)
+    double fxinv;        // 1 / fxq
+    int lq[3];           // (L - float(L)) / fxq, exact
     int ifpd[3];
     int nc[3];
     int cell0;           // first global cell id of this box
@@ -77,6 +90,11 @@ struct DevTables {
     const float2 *dens2;           // [nkind][ntp] {POTB(k), POTB(k+1)-POTB(k)}
     const float4 *force4;          // [nkind][ntp] {FPOTR, dFPOTR, FPOTB, dFPOTB}
     const float2 *embd2;           // [nkind1][nep] {DFEMBD, dDFEMBD}
+    // float-float tables: {value hi, lo, slope hi, lo} (slope to the next grid point in FP64)
+    const float4 *densff;          // [nkind][ntp] POTB
+    const float4 *forceff;         // [nkind][ntp][2] FPOTR, FPOTB
+    const float4 *embff;           // [nkind1][nep] DFEMBD
+    float irhodh, irhodl;          // 1 / RHOD as float-float
     float csih, csil;              // CSI as float-float
     float ru2h, ru2l;              // RU^2 as float-float
     float rhodf;
@@ -110,6 +128,8 @@ struct DevAtoms {
     const double *icm;   // reciprocal masses per type
     unsigned *pk;        // mixed passes: per-pair table index (KK << 18 | DK * 2^18), ELL layout
     PosFF *rec;          // mixed passes: {position, F'(rho)} records written by the density pass
+    PosFX *posfx;        // float-float passes: positions (k_fix) ...
+    PosFX *recfx;        // ... and {position, F'(rho)} records written by the density pass
     int *flags;
     unsigned long long *maxdisp;
     double *virial;      // [nbox][6]
@@ -321,6 +341,8 @@ int launch_stress(msmgb_ctx *c, int sorted, double *ap);
 int launch_density32(msmgb_ctx *c);
 int launch_force32(msmgb_ctx *c);
 int launch_force32_vv(msmgb_ctx *c, double h);
+int launch_density_ff(msmgb_ctx *c);
+int launch_force_ff(msmgb_ctx *c);
 int autotune_fused(msmgb_ctx *c);
 int autotune_mixed(msmgb_ctx *c);
 int launch_hvp(msmgb_ctx *c, const double *dv, double *dhv, double *v4buf, double *ddbuf);
