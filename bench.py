@@ -493,7 +493,7 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed", "ff"])
     ap.add_argument("--ncell", type=int, default=NCELL,
                     help="fcc cells per edge (80 = the benchmark; smaller for profiling captures)")
     ap.add_argument("--no-compare", action="store_true")
