@@ -148,6 +148,7 @@ def precision_compare(e, box, pos, vel, steps):
         e.run_steps(3, DT)
         ms, _ = e.time_steps(steps, DT)
         out[prec + "_value"] = len(pos) * steps / (ms / 1e3)
+        out[prec + "_pass_ms"] = {k: v for k, v in e.time_passes(3).items() if k != "fused"}
     e.set_precision("mixed")
     e.copyin(box, pos, vel)
     return out
@@ -410,7 +411,8 @@ def run_ours(args):
                "speedup": value / ws / pc["fp64_value"],
                "mixed_force_err_norm": pc["mixed_force_err_norm"], "mixed_force_err_max": pc["mixed_force_err_max"],
                "ff_value": pc["ff_value"], "ff_speedup_vs_fp64": pc["ff_value"] / pc["fp64_value"],
-               "ff_force_err_norm": pc["ff_force_err_norm"], "ff_force_err_max": pc["ff_force_err_max"]}
+               "ff_force_err_norm": pc["ff_force_err_norm"], "ff_force_err_max": pc["ff_force_err_max"],
+               "fp64_pass_ms": pc["fp64_pass_ms"], "ff_pass_ms": pc["ff_pass_ms"]}
 
     extras = {}
     if not args.no_extras:
