@@ -870,10 +870,25 @@ static int capture_step(msmgb_ctx *c, double h)
     return MSMGB_OK;
 }
 
-// ---- fused mixed step (single species): force pass + integrator in one kernel ----------
+// ---- fused step: force pass + integrator in one kernel (mixed single species, float-float)
 static bool fused_mixed(const msmgb_ctx *c)
 {
-    return c->p.precision == MSMGB_PREC_MIXED && c->tab.ngroup == 1;
+    return (c->p.precision == MSMGB_PREC_MIXED && c->tab.ngroup == 1) || c->p.precision == MSMGB_PREC_FF;
+}
+
+static int step_density(msmgb_ctx *c)
+{
+    return c->p.precision == MSMGB_PREC_FF ? launch_density_ff(c) : launch_density32(c);
+}
+
+static int step_force_vv(msmgb_ctx *c, double h)
+{
+    return c->p.precision == MSMGB_PREC_FF ? launch_force_ff_vv(c, h) : launch_force32_vv(c, h);
+}
+
+static int step_force(msmgb_ctx *c)
+{
+    return c->p.precision == MSMGB_PREC_FF ? launch_force_ff(c) : launch_force32(c);
 }
 
 // atom view whose positions are buffer p (0: c->a's own, 1: the second buffer) and whose
@@ -913,11 +928,13 @@ static int capture_fused(msmgb_ctx *c, double h)
     }
     const DevAtoms base = c->a;
     int rc = MSMGB_OK;
-    // tune the fused kernel on the current state (h = 0 changes nothing), outside capture
-    c->a = atoms_on(c, base, 0);
-    rc = autotune_fused(c);
-    c->a = base;
-    RET(rc);
+    // tune the fused mixed kernel on the current state (h = 0 changes nothing), outside capture
+    if (c->p.precision == MSMGB_PREC_MIXED) {
+        c->a = atoms_on(c, base, 0);
+        rc = autotune_fused(c);
+        c->a = base;
+        RET(rc);
+    }
     const int64_t l_start = c->launches;
     int64_t l0 = c->launches;
     CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "graph capture");
@@ -932,8 +949,8 @@ static int capture_fused(msmgb_ctx *c, double h)
         l0 = c->launches;
         CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "graph capture");
         c->a = atoms_on(c, base, p);
-        rc = launch_density32(c);
-        if (!rc) rc = launch_force32_vv(c, h);
+        rc = step_density(c);
+        if (!rc) rc = step_force_vv(c, h);
         if (!rc) rc = launch_decide(c, c->p.skin_trigger, c->p.nb_uptab);
         c->a = atoms_on(c, base, 1 - p);
         if (!rc) rc = build_list(c, true);
@@ -943,8 +960,8 @@ static int capture_fused(msmgb_ctx *c, double h)
         l0 = c->launches;
         CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "graph capture");
         c->a = atoms_on(c, base, p);
-        rc = launch_density32(c);
-        if (!rc) rc = launch_force32(c);
+        rc = step_density(c);
+        if (!rc) rc = step_force(c);
         if (!rc) rc = launch_correct(c, h, false);
         c->a = base;
         RET(end_capture(c, rc, &c->g_final[p]));
@@ -953,6 +970,7 @@ static int capture_fused(msmgb_ctx *c, double h)
     c->launches = l_start;            // capturing launches nothing; graph launches are counted
     c->fg_h = h;
     c->fg_n = c->n;
+    c->fg_prec = c->p.precision;
     c->fg_tune = c->tune_dens_unroll * 64 + c->tune_force_unroll;
     return MSMGB_OK;
 }
@@ -960,7 +978,7 @@ static int capture_fused(msmgb_ctx *c, double h)
 static int ensure_graphs(msmgb_ctx *c, double h)
 {
     if (fused_mixed(c)) {
-        if (!c->g_pre || c->fg_h != h || c->fg_n != c->n ||
+        if (!c->g_pre || c->fg_h != h || c->fg_n != c->n || c->fg_prec != c->p.precision ||
             c->fg_tune != c->tune_dens_unroll * 64 + c->tune_force_unroll)
             return capture_fused(c, h);
         return MSMGB_OK;
@@ -1166,7 +1184,7 @@ extern "C" int msmgb_time_passes(msmgb_ctx *c, int reps, float *out)
         if (which == 4 && !fused) break;
         // the fused kernel reads the {position, F'(rho)} records of the density pass:
         // refresh them for the current positions (untimed)
-        if (which == 4) RET(launch_density32(c));
+        if (which == 4) RET(step_density(c));
         double total = 0.0;
         for (int r = 0; r < reps + 1; ++r) {
             CK(cudaStreamSynchronize(c->stream), "synchronize");
@@ -1179,7 +1197,7 @@ extern "C" int msmgb_time_passes(msmgb_ctx *c, int reps, float *out)
             else {
                 const DevAtoms base = c->a;
                 c->a = atoms_on(c, base, 0);
-                rc = launch_force32_vv(c, 0.0);
+                rc = step_force_vv(c, 0.0);
                 c->a = base;
             }
             if (rc) return rc;

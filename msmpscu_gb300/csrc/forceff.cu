@@ -20,6 +20,8 @@
 //                 {position, F'(rho) hi, lo} of atom i for the force pass and F'(rho) as FP64.
 //   k_force_ff    recomputes the pair index, 1/R and the FORTOT of every pair in float-float
 //                 and accumulates F_i in float-float; writes F as FP64.
+//   k_force_ff_vv the same followed by the FP64 corrector / predictor of the atom (the MD step
+//                 kernel of this mode, like k_force32_vv of the mixed passes).
 #include "msmgb_internal.cuh"
 
 namespace msmgb {
@@ -59,6 +61,23 @@ __device__ __forceinline__ ff ff_mul_f(ff x, float f)
     const float p = x.h * f;
     const float e = fmaf(x.h, f, -p);
     return quick_two_sum(p, fmaf(x.l, f, e));
+}
+
+// Accumulation of a float-float sum without renormalising each term: F.l collects the exact
+// rounding errors of the hi additions and the low parts (tiny against F.h), the sum is
+// F.h + F.l at the end.
+__device__ __forceinline__ void acc_add(ff &F, float ph, float pl)
+{
+    const ff s = two_sum(F.h, ph);
+    F.h = s.h;
+    F.l += s.l + pl;
+}
+
+// product x*y as an unnormalised pair (p, e) with p + e = x*y to ~2^-46
+__device__ __forceinline__ void mul_pair(ff x, ff y, float &p, float &e)
+{
+    p = x.h * y.h;
+    e = fmaf(x.h, y.l, fmaf(x.l, y.h, fmaf(x.h, y.h, -p)));
 }
 
 // x + dk * s for a table row {x.h, x.l, s.h, s.l} and dk = dkh + dkl (dkh holds few bits)
@@ -247,8 +266,10 @@ __global__ void __launch_bounds__(kBlock) k_density_ff(DevAtoms a, DevTables t)
         if (!pair_ff(pi, pj, b, t, rej, q)) continue;
         const int k = MULTI ? t.kpair[(a.ityp[j] - 1) * t.ngroup + ti] : 0;
         const float4 row = __ldg(t.densff + (size_t)k * t.ntp + q.kk);
-        rho = ff_add(rho, lerp_ff(row, q.dkh, q.dkl));
+        const ff v = lerp_ff(row, q.dkh, q.dkl);
+        acc_add(rho, v.h, v.l);
     }
+    rho = quick_two_sum(rho.h, rho.l);
     ff d = rho;
     if (POT == MSMGB_FS_TYPE) {
         if (rho.h > 0.0f) {
@@ -282,54 +303,92 @@ __global__ void __launch_bounds__(kBlock) k_density_ff(DevAtoms a, DevTables t)
     a.den[i] = (double)d.h + (double)d.l;
 }
 
+// F_i of one atom in float-float (FORTOT of every pair recomputed from the records)
+template <bool MULTI>
+__device__ __forceinline__ void force_atom_ff(const DevAtoms &a, const DevTables &t, int i, ff F[3])
+{
+    const PosFX pi = ld_rec(a.recfx + i);
+    const BoxFF b = load_boxff(a.box[a.boxid[i]]);
+    const float rej = t.ru2h + 4.0f * sqrtf(t.ru2h) * b.dlmax + 1e-5f * t.ru2h;
+    const int ti = MULTI ? a.ityp[i] - 1 : 0;
+    const ff di = {pi.dh, pi.dl};
+    const int kn = a.kvois[i];
+    const int *__restrict__ nb = a.indi + i;
+    const size_t ld = (size_t)a.ld;
+    for (int w = 0; w < kn; ++w) {
+        const int j = __ldg(nb + w * ld);
+        const PosFX pj = ld_rec(a.recfx + j);
+        PairFF q;
+        if (!pair_ff(pi, pj, b, t, rej, q)) continue;
+        const ff dj = {pj.dh, pj.dl};
+        const ff y = ff_rsqrt(q.r2);                              // 1/R
+        const float4 *rows = t.forceff;
+        int k = 0, k1 = 0;
+        if (MULTI) {
+            const int tj = a.ityp[j] - 1;
+            k = t.kpair[tj * t.ngroup + ti];
+            k1 = t.kpair[ti * t.ngroup + tj];
+        }
+        const float4 *rk = rows + 2 * ((size_t)k * t.ntp + q.kk);
+        const ff P = lerp_ff(__ldg(rk), q.dkh, q.dkl);
+        const ff B = lerp_ff(__ldg(rk + 1), q.dkh, q.dkl);
+        ff emb;
+        if (MULTI && k1 != k) {
+            const ff B1 = lerp_ff(__ldg(rows + 2 * ((size_t)k1 * t.ntp + q.kk) + 1), q.dkh, q.dkl);
+            emb = ff_add(ff_mul(B, di), ff_mul(B1, dj));
+        } else {
+            emb = ff_mul(B, ff_add(di, dj));
+        }
+        // FORTOT = (FPOTR / R + (FPOTB_k D_i + FPOTB_k1 D_j)) / R
+        const ff ft = ff_mul(ff_add(ff_mul(P, y), emb), y);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            float ph, pl;
+            mul_pair(ft, q.s[c], ph, pl);
+            acc_add(F[c], ph, pl);
+        }
+    }
+}
+
 template <bool MULTI>
 __global__ void __launch_bounds__(kBlock) k_force_ff(DevAtoms a, DevTables t)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
     ff F[3] = {{0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}};
-    if ((a.statu[i] & MSMGB_STATU_ACTIVE) == MSMGB_STATU_ACTIVE) {
-        const PosFX pi = ld_rec(a.recfx + i);
-        const BoxFF b = load_boxff(a.box[a.boxid[i]]);
-        const float rej = t.ru2h + 4.0f * sqrtf(t.ru2h) * b.dlmax + 1e-5f * t.ru2h;
-        const int ti = MULTI ? a.ityp[i] - 1 : 0;
-        const ff di = {pi.dh, pi.dl};
-        const int kn = a.kvois[i];
-        const int *__restrict__ nb = a.indi + i;
-        const size_t ld = (size_t)a.ld;
-        for (int w = 0; w < kn; ++w) {
-            const int j = __ldg(nb + w * ld);
-            const PosFX pj = ld_rec(a.recfx + j);
-            PairFF q;
-            if (!pair_ff(pi, pj, b, t, rej, q)) continue;
-            const ff dj = {pj.dh, pj.dl};
-            const ff y = ff_rsqrt(q.r2);                              // 1/R
-            const float4 *rows = t.forceff;
-            int k = 0, k1 = 0;
-            if (MULTI) {
-                const int tj = a.ityp[j] - 1;
-                k = t.kpair[tj * t.ngroup + ti];
-                k1 = t.kpair[ti * t.ngroup + tj];
-            }
-            const float4 *rk = rows + 2 * ((size_t)k * t.ntp + q.kk);
-            const ff P = lerp_ff(__ldg(rk), q.dkh, q.dkl);
-            const ff B = lerp_ff(__ldg(rk + 1), q.dkh, q.dkl);
-            ff emb;
-            if (MULTI && k1 != k) {
-                const ff B1 = lerp_ff(__ldg(rows + 2 * ((size_t)k1 * t.ntp + q.kk) + 1), q.dkh, q.dkl);
-                emb = ff_add(ff_mul(B, di), ff_mul(B1, dj));
-            } else {
-                emb = ff_mul(B, ff_add(di, dj));
-            }
-            // FORTOT = (FPOTR / R + (FPOTB_k D_i + FPOTB_k1 D_j)) / R
-            const ff ft = ff_mul(ff_add(ff_mul(P, y), emb), y);
-#pragma unroll
-            for (int c = 0; c < 3; ++c) F[c] = ff_add(F[c], ff_mul(ft, q.s[c]));
-        }
-    }
+    if ((a.statu[i] & MSMGB_STATU_ACTIVE) == MSMGB_STATU_ACTIVE) force_atom_ff<MULTI>(a, t, i, F);
     a.fx[i] = (double)F[0].h + (double)F[0].l;
     a.fy[i] = (double)F[1].h + (double)F[1].l;
     a.fz[i] = (double)F[2].h + (double)F[2].l;
+}
+
+// The float-float MD step kernel: force pass, then corrector of step n and predictor of step
+// n+1 of the same atom (vv_atom, FP64), positions of step n+1 into the second buffer.
+template <bool MULTI>
+__global__ void __launch_bounds__(kBlock) k_force_ff_vv(DevAtoms a, DevTables t, double th)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double dmax = 0.0;
+    if (i < a.n) {
+        const int stat = a.statu[i];
+        ff F[3] = {{0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}};
+        const bool act = (stat & MSMGB_STATU_ACTIVE) == MSMGB_STATU_ACTIVE;
+        if (act) force_atom_ff<MULTI>(a, t, i, F);
+        const double Fx = (double)F[0].h + (double)F[0].l;
+        const double Fy = (double)F[1].h + (double)F[1].l;
+        const double Fz = (double)F[2].h + (double)F[2].l;
+        a.fx[i] = Fx;
+        a.fy[i] = Fy;
+        a.fz[i] = Fz;
+        const double4_32a p = a.pos[i];
+        if (act) {
+            dmax = vv_atom(a, i, stat, a.box[a.boxid[i]], th, true, Fx, Fy, Fz, p, a.pos_nxt, a.posff_nxt);
+        } else {
+            a.pos_nxt[i] = p;
+            a.posff_nxt[i] = a.posff[i];
+        }
+    }
+    block_max_flush(dmax, a.maxdisp);
 }
 
 static inline int nblk(long n, int b) { return (int)((n + b - 1) / b); }
@@ -350,6 +409,15 @@ int launch_density_ff(msmgb_ctx *c)
     c->launches += 2;
     c->den_is32 = false;
     return check_launch(c, "float-float density pass");
+}
+
+int launch_force_ff_vv(msmgb_ctx *c, double h)
+{
+    const int g = nblk(c->n, kBlock);
+    if (c->tab.ngroup > 1) k_force_ff_vv<true><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h);
+    else k_force_ff_vv<false><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h);
+    c->launches += 1;
+    return check_launch(c, "float-float force pass + integrator");
 }
 
 int launch_force_ff(msmgb_ctx *c)

@@ -313,7 +313,7 @@ struct msmgb_ctx {
     cudaGraphExec_t g_pre = nullptr, g_loop[2] = {nullptr, nullptr}, g_final[2] = {nullptr, nullptr};
     int64_t gk_pre = 0, gk_loop = 0, gk_final = 0;
     double fg_h = 0.0;
-    int fg_n = -1, fg_tune = -1;
+    int fg_n = -1, fg_tune = -1, fg_prec = -1;
 
     // CUDA graph of one MD step
     cudaGraphExec_t step_graph = nullptr;
@@ -343,6 +343,7 @@ int launch_force32(msmgb_ctx *c);
 int launch_force32_vv(msmgb_ctx *c, double h);
 int launch_density_ff(msmgb_ctx *c);
 int launch_force_ff(msmgb_ctx *c);
+int launch_force_ff_vv(msmgb_ctx *c, double h);
 int autotune_fused(msmgb_ctx *c);
 int autotune_mixed(msmgb_ctx *c);
 int launch_hvp(msmgb_ctx *c, const double *dv, double *dhv, double *v4buf, double *ddbuf);
