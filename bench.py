@@ -168,7 +168,7 @@ def batched_uneven_boxes(steps, steps_perbox, device=0):
     out = {"boxes": len(boxes), "atoms": int(len(pos)),
            "box_atoms_min": int(min(len(b[0]) for b in boxes)),
            "box_atoms_max": int(max(len(b[0]) for b in boxes))}
-    for prec in ("mixed", "fp64"):
+    for prec in ("mixed", "ff", "fp64"):
         e = Engine(len(pos), lt.CU_RC_NL, max_boxes=len(boxes), mxkvois=MXKVOIS, skin_trigger=0.15,
                    precision=prec, device=device)
         e.init_forcetable(table)
