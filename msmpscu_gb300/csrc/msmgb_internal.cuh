@@ -314,7 +314,6 @@ struct msmgb_ctx {
     int64_t gk_pre = 0, gk_loop = 0, gk_final = 0;
     double fg_h = 0.0;
     int fg_n = -1, fg_tune = -1, fg_prec = -1;
-    bool build_cells = true;     // list build: warp per cell (true) or thread per atom
 
     // CUDA graph of one MD step
     cudaGraphExec_t step_graph = nullptr;

@@ -328,142 +328,6 @@ __global__ void __launch_bounds__(kBlock) k_build(DevAtoms a, const int *cell_of
     atomicMax(&a.flags[kFlagMaxK], nn);
 }
 
-// Warp-per-cell variant of the same list (identical sets and order).  One warp owns one cell:
-// it stages the candidates of the 27 stencil cells, in stencil order, in shared memory (hi
-// parts with the cell's image shift already applied: q - L is exact by Sterbenz, q + L is
-// off by at most one ulp of 2L, inside the prefilter band), then tests each atom of its cell
-// against 32 candidates per step, one per lane, and appends the accepted ones in candidate
-// order with a ballot.  Lane l keeps the list length of atom l of the current group of 32.
-constexpr int kCellWarps = 4;
-constexpr int kCandCap = 448;
-
-__global__ void __launch_bounds__(kCellWarps * 32) k_build_cells(DevAtoms a, const int *start, int ncell, double rc2,
-                                                                 float d2lo, float d2hi, int predicated)
-{
-    if (skip_rebuild(a.flags, predicated)) return;
-    __shared__ float4 cand[kCellWarps][kCandCap];
-    const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
-    const int g = blockIdx.x * kCellWarps + wl;
-    if (g > ncell) return;                           // whole warp
-    const int a0 = start[g], a1 = start[g + 1];
-    if (a0 == a1) return;
-    const float4 *const hi = reinterpret_cast<const float4 *>(a.posff);   // record = 2 float4
-    for (int i = a0 + lane; i < a1; i += 32) {
-        const float4 q = hi[2 * (size_t)i];
-        a.pos_bld[i] = make_float4(q.x, q.y, q.z, 0.0f);
-        if (g == ncell) a.kvois[i] = 0;              // sentinel cell: out-of-box atoms
-    }
-    if (g == ncell) return;
-    const DevBox &b = a.box[a.boxid[a0]];
-    int nc[3], pd[3];
-    float lf[3], hf[3];
-    bool wide = true;
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        nc[k] = b.nc[k];
-        pd[k] = b.ifpd[k];
-        lf[k] = b.lenf[k];
-        hf[k] = b.halff[k];
-        const double w = b.len[k] / nc[k];
-        if (pd[k] && w * w < rc2) wide = false;
-    }
-    const int cell0 = b.cell0;
-    const int c = g - cell0;
-    const int ix = c % nc[0], iy = (c / nc[0]) % nc[1], iz = c / (nc[0] * nc[1]);
-    const size_t ld = (size_t)a.ld;
-    const int mxk = a.mxk;
-    const unsigned lt_mask = (1u << lane) - 1u;
-    float4 *const cw = cand[wl];
-    for (int gs = a0; gs < a1; gs += 32) {          // atoms of the cell in groups of 32
-        const int grp = min(32, a1 - gs);
-        float4 mine = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        if (lane < grp) mine = hi[2 * (size_t)(gs + lane)];
-        int nn_own = 0;
-        int s = 0, sub = 0;                         // next stencil cell / offset inside it
-        while (s < 27) {
-            // ---- stage a batch of candidates (warp-uniform control flow)
-            int cnt = 0;
-            while (s < 27 && cnt < kCandCap) {
-                int j3[3] = {ix + c_nix[s], iy + c_niy[s], iz + c_niz[s]};
-                float sh[3];
-                bool skip = false;
-#pragma unroll
-                for (int k = 0; k < 3; ++k) {
-                    sh[k] = 0.0f;
-                    if (pd[k]) {
-                        if (j3[k] >= nc[k]) { j3[k] = 0; sh[k] = -lf[k]; }
-                        else if (j3[k] < 0) { j3[k] = nc[k] - 1; sh[k] = lf[k]; }
-                    }
-                    if (j3[k] < 0 || j3[k] >= nc[k]) skip = true;
-                }
-                if (skip) { ++s; sub = 0; continue; }
-                const int gc = cell0 + j3[0] + nc[0] * (j3[1] + nc[1] * j3[2]);
-                const int c0 = start[gc] + sub, c1 = start[gc + 1];
-                const int take = min(c1 - c0, kCandCap - cnt);
-                for (int t = lane; t < take; t += 32) {
-                    const int j = c0 + t;
-                    const float4 q = hi[2 * (size_t)j];
-                    // staged value v with separation p - v: v = q - sh in the wide case
-                    cw[cnt + t] = wide ? make_float4(q.x - sh[0], q.y - sh[1], q.z - sh[2], __int_as_float(j))
-                                       : make_float4(q.x, q.y, q.z, __int_as_float(j));
-                }
-                cnt += take;
-                if (c0 + take < c1) { sub += take; break; }   // rest of this cell in the next batch
-                ++s;
-                sub = 0;
-            }
-            __syncwarp();
-            // ---- every atom of the group against the batch
-            for (int t = 0; t < grp; ++t) {
-                const int i = gs + t;
-                const float px = __shfl_sync(0xffffffffu, mine.x, t);
-                const float py = __shfl_sync(0xffffffffu, mine.y, t);
-                const float pz = __shfl_sync(0xffffffffu, mine.z, t);
-                int nn = __shfl_sync(0xffffffffu, nn_own, t);
-                for (int base = 0; base < cnt; base += 32) {
-                    const int k = base + lane;
-                    bool in = false;
-                    int j = i;
-                    if (k < cnt) {
-                        const float4 v = cw[k];
-                        j = __float_as_int(v.w);
-                        float sx, sy, sz;
-                        if (wide) {
-                            sx = px - v.x;
-                            sy = py - v.y;
-                            sz = pz - v.z;
-                        } else {
-                            sx = mi32(px - v.x, lf[0], hf[0], pd[0]);
-                            sy = mi32(py - v.y, lf[1], hf[1], pd[1]);
-                            sz = mi32(pz - v.z, lf[2], hf[2], pd[2]);
-                        }
-                        const float d2f = fmaf(sx, sx, fmaf(sy, sy, sz * sz));
-                        in = j != i && accept(d2f, d2lo, d2hi, a, i, j, b, rc2);
-                    }
-                    const unsigned m = __ballot_sync(0xffffffffu, in);
-                    if (in) {
-                        const int slot = nn + __popc(m & lt_mask);
-                        if (slot < mxk) a.indi[(size_t)slot * ld + i] = j;
-                    }
-                    nn += __popc(m);
-                }
-                if (lane == t) nn_own = nn;
-            }
-            __syncwarp();
-        }
-        if (lane < grp) {
-            const int i = gs + lane;
-            int nn = nn_own;
-            if (nn > mxk) {
-                atomicOr(&a.flags[kFlagErr], kErrOverflow);
-                nn = mxk;
-            }
-            a.kvois[i] = nn;
-            atomicMax(&a.flags[kFlagMaxK], nn);
-        }
-    }
-}
-
 static inline int nblk(long n, int b) { return (int)((n + b - 1) / b); }
 
 // Margin of the FP32 prefilter: it uses the hi parts of the shifted coordinates
@@ -513,11 +377,7 @@ int build_list(msmgb_ctx *c, bool predicated)
     double rc2 = c->p.rc_nl * c->p.rc_nl;
     float d2lo, d2hi;
     prefilter_band(c, rc2, &d2lo, &d2hi);
-    if (c->build_cells)
-        k_build_cells<<<nblk(ncs, kCellWarps), kCellWarps * 32, 0, s>>>(a, c->cell_start, c->ncell_total, rc2, d2lo,
-                                                                        d2hi, pr);
-    else
-        k_build<<<nblk(n, kBlock), kBlock, 0, s>>>(a, c->cell_of, c->cell_start, rc2, d2lo, d2hi, pr);
+    k_build<<<nblk(n, kBlock), kBlock, 0, s>>>(a, c->cell_of, c->cell_start, rc2, d2lo, d2hi, pr);
     c->launches += 6;
     return check_launch(c, "neighbour list");
 }
