@@ -279,6 +279,22 @@ int  msmgb_create_forcetable(int pot, const double *prm, double rmax, int ntab, 
                              double rhoscal, double *potr, double *fpotr, double *potb,
                              double *fpotb, double *fembd, double *dfembd, double *rhod);
 
+/* ---- tabulated EAM potentials in setfl layout (Register_ForceTableProc_Setfl,
+ *      Filedatas_Func_Setfl.F90:499-541; reader get_filedatas_setfl :119-253) ------------- */
+/* Element count, grid sizes and cutoff of a setfl file (Angstrom / eV, LAMMPS layout). */
+int  msmgb_setfl_info(const char *path, int *nelem, int *nrho, int *nr, double *cutoff);
+/* Tables of a setfl file on the sqrt(r) grid of ntab points up to Rmax = cutoff, EAM type:
+ * NKIND = NE^2 pair tables (id (I-1)*NE + J for an I atom with a J neighbour: the pair
+ * phi_IJ and the density of element J) in the (NKIND, NTAB) column-major layout of
+ * msmgb_forcetable with POTR = 0.5 r phi, FPOTR = -r phi', POTB = rho_J, FPOTB = -rho_J';
+ * NKIND1 = NE embedding tables F, F' on the file's rho grid (NEMBD = Nrho, RHOD = drho),
+ * (NKIND1, NEMBD) column-major; KPAIR (NE, NE) column-major, KEMBD (NE), masses (NE, amu).
+ * Interpolation: natural cubic spline through the file's data (the reference's SLATEC
+ * DBINT4/DBVALU settings, :25-34, 256-276).  Host only. */
+int  msmgb_setfl_tables(const char *path, int ntab, double *potr, double *fpotr, double *potb,
+                        double *fpotb, double *fembd, double *dfembd, int *kpair, int *kembd,
+                        double *rhod, double *masses);
+
 #ifdef __cplusplus
 }
 #endif

@@ -92,6 +92,8 @@ SIGNATURES = [
     ("msmgb_hvp", C.c_int, [C.c_void_p, _dp, _dp]),
     ("msmgb_time_hvp", C.c_int, [C.c_void_p, _dp, C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
     ("msmgb_param_adjoint", C.c_int, [C.c_void_p, C.c_int, _dp, _dp, _dp, _dp]),
+    ("msmgb_setfl_info", C.c_int, [C.c_char_p, _ip, _ip, _ip, _dp]),
+    ("msmgb_setfl_tables", C.c_int, [C.c_char_p, C.c_int, _dp, _dp, _dp, _dp, _dp, _dp, _ip, _ip, _dp, _dp]),
     ("msmgb_cr_param_tables", C.c_int, [_dp, C.c_double, C.c_int, _dp]),
     ("msmgb_calforce_noalloc", C.c_int, [C.POINTER(ForceNoAlloc)]),
     ("msmgb_create_forcetable", C.c_int, [C.c_int, _dp, C.c_double, C.c_int, C.c_int, C.c_double,

@@ -12,6 +12,11 @@
 // POTR = f1(R)*R, FPOTR = f2(R)*R, POTB = rho(R), FPOTB = -rho'(R);
 // RHOMX = RHOSCAL * max POTB, RHOD = RHOMX/NEMBD; F, F' at rho = (i-1)*RHOD (:1040-1048).
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
 
 #include "../../include/msmgb.h"
 
@@ -183,5 +188,195 @@ extern "C" int msmgb_cr_param_tables(const double *prm, double rmax, int ntab, d
         for (int m = 0; m < 5; ++m)
             for (int k = 0; k < 3; ++k) d[(size_t)(m * 3 + k) * ntab + (i - 1)] = v[m][k];
     }
+    return MSMGB_OK;
+}
+
+// ---- tabulated EAM potentials in setfl layout -------------------------------------------
+// Register_ForceTableProc_Setfl (Filedatas_Func_Setfl.F90:499-541) with the reader
+// get_filedatas_setfl (:119-253): three comment lines; "NE el1 el2 ..."; "Nrho drho Nr dr
+// cutoff"; per element a line "Z mass a lattice", Nrho values of F(rho) and Nr values of
+// rho(r); then r*phi(r) for every pair I >= J.  The r grid is R_i = i cutoff/Nr, the rho grid
+// i drho.  A leading "INF" / "NAN" token stands for the r = 0 value, which takes the next one.
+// Interpolation: the reference uses SLATEC DBINT4/DBVALU with IBCL = IBCR = 2, FBCL = FBCR
+// = 0 and KNTOPT = 1 (:25-34, 256-276), i.e. the natural cubic spline through the data.
+namespace {
+
+struct Setfl {
+    int ne = 0, nrho = 0, nr = 0;
+    double drho = 0.0, dr = 0.0, cutoff = 0.0;
+    std::vector<double> mass;
+    std::vector<std::vector<double>> frho, rhor;   // [element][point]
+    std::vector<std::vector<double>> rphi;         // [I*(I+1)/2 + J], J <= I
+};
+
+bool next_token(FILE *f, std::string &t)
+{
+    t.clear();
+    int c;
+    while ((c = fgetc(f)) != EOF && (c == ' ' || c == '\t' || c == '\n' || c == '\r')) {}
+    if (c == EOF) return false;
+    do { t.push_back((char)c); } while ((c = fgetc(f)) != EOF && c != ' ' && c != '\t' && c != '\n' && c != '\r');
+    return true;
+}
+
+bool read_block(FILE *f, int n, std::vector<double> &v)
+{
+    v.assign((size_t)n, 0.0);
+    std::string t;
+    bool first_special = false;
+    for (int i = 0; i < n; ++i) {
+        if (!next_token(f, t)) return false;
+        if (i == 0 && (t == "INF" || t == "inf" || t == "NAN" || t == "nan")) {
+            first_special = true;
+            continue;
+        }
+        char *end = nullptr;
+        v[(size_t)i] = strtod(t.c_str(), &end);
+        if (end == t.c_str()) return false;
+    }
+    if (first_special) v[0] = n > 1 ? v[1] : 0.0;
+    return true;
+}
+
+int read_setfl(const char *path, Setfl &s)
+{
+    FILE *f = fopen(path, "r");
+    if (!f) return MSMGB_ERR_ARG;
+    char line[4096];
+    int rc = MSMGB_ERR_ARG;
+    for (int k = 0; k < 3; ++k)
+        if (!fgets(line, sizeof(line), f)) goto done;
+    if (!fgets(line, sizeof(line), f) || sscanf(line, "%d", &s.ne) != 1 || s.ne < 1 || s.ne > 4) goto done;
+    if (!fgets(line, sizeof(line), f) ||
+        sscanf(line, "%d %lf %d %lf %lf", &s.nrho, &s.drho, &s.nr, &s.dr, &s.cutoff) != 5 || s.nrho < 3 ||
+        s.nr < 3 || s.drho <= 0.0 || s.cutoff <= 0.0)
+        goto done;
+    s.mass.assign((size_t)s.ne, 0.0);
+    s.frho.resize((size_t)s.ne);
+    s.rhor.resize((size_t)s.ne);
+    for (int e = 0; e < s.ne; ++e) {
+        std::string t;
+        if (!next_token(f, t)) goto done;                     // atomic number
+        if (!next_token(f, t)) goto done;
+        s.mass[(size_t)e] = strtod(t.c_str(), nullptr);
+        if (!next_token(f, t) || !next_token(f, t)) goto done;   // lattice constant, structure
+        if (!read_block(f, s.nrho, s.frho[(size_t)e]) || !read_block(f, s.nr, s.rhor[(size_t)e])) goto done;
+    }
+    s.rphi.resize((size_t)(s.ne * (s.ne + 1) / 2));
+    for (int i = 0; i < s.ne; ++i)
+        for (int j = 0; j <= i; ++j)
+            if (!read_block(f, s.nr, s.rphi[(size_t)(i * (i + 1) / 2 + j)])) goto done;
+    rc = MSMGB_OK;
+done:
+    fclose(f);
+    return rc;
+}
+
+// natural cubic spline on x_i = i h: second derivatives (Thomas algorithm)
+std::vector<double> spline_m(const std::vector<double> &y, double h)
+{
+    const size_t n = y.size();
+    std::vector<double> m(n, 0.0), cp(n, 0.0);
+    const double s = 6.0 / (h * h);
+    for (size_t i = 1; i + 1 < n; ++i) {
+        const double den = 4.0 - cp[i - 1];
+        cp[i] = 1.0 / den;
+        m[i] = (s * (y[i + 1] - 2.0 * y[i] + y[i - 1]) - m[i - 1]) / den;
+    }
+    m[n - 1] = 0.0;
+    for (size_t i = n - 2; i >= 1; --i) m[i] -= cp[i] * m[i + 1];
+    return m;
+}
+
+double spline_at(const std::vector<double> &y, const std::vector<double> &m, double h, double x, double *dy)
+{
+    const int n = (int)y.size();
+    int k = (int)std::floor(x / h);
+    if (k < 0) k = 0;
+    if (k > n - 2) k = n - 2;
+    const double b = (x - k * h) / h, a = 1.0 - b;
+    if (dy)
+        *dy = (y[(size_t)k + 1] - y[(size_t)k]) / h +
+              h * ((1.0 - 3.0 * a * a) * m[(size_t)k] + (3.0 * b * b - 1.0) * m[(size_t)k + 1]) / 6.0;
+    return a * y[(size_t)k] + b * y[(size_t)k + 1] +
+           ((a * a * a - a) * m[(size_t)k] + (b * b * b - b) * m[(size_t)k + 1]) * (h * h / 6.0);
+}
+
+}  // namespace
+
+extern "C" int msmgb_setfl_info(const char *path, int *nelem, int *nrho, int *nr, double *cutoff)
+{
+    if (!path) return MSMGB_ERR_ARG;
+    Setfl s;
+    int rc = read_setfl(path, s);
+    if (rc) return rc;
+    if (nelem) *nelem = s.ne;
+    if (nrho) *nrho = s.nrho;
+    if (nr) *nr = s.nr;
+    if (cutoff) *cutoff = s.cutoff;
+    return MSMGB_OK;
+}
+
+extern "C" int msmgb_setfl_tables(const char *path, int ntab, double *potr, double *fpotr, double *potb,
+                                  double *fpotb, double *fembd, double *dfembd, int *kpair, int *kembd,
+                                  double *rhod, double *masses)
+{
+    if (!path || ntab < 2 || !potr || !fpotr || !potb || !fpotb || !fembd || !dfembd || !kpair || !kembd)
+        return MSMGB_ERR_ARG;
+    Setfl s;
+    int rc = read_setfl(path, s);
+    if (rc) return rc;
+    const int ne = s.ne, nk = ne * ne;
+    const double dr = s.cutoff / s.nr;                 // R(I) = (I-1) cutoff/Nr
+    const double rimax = (s.nr - 1) * dr, fimax = (s.nrho - 1) * s.drho;
+    std::vector<std::vector<double>> mr((size_t)ne), mf((size_t)ne), mp(s.rphi.size());
+    std::vector<int> fzero((size_t)ne, 1);
+    for (int e = 0; e < ne; ++e) {
+        mr[(size_t)e] = spline_m(s.rhor[(size_t)e], dr);
+        mf[(size_t)e] = spline_m(s.frho[(size_t)e], s.drho);
+        for (double v : s.frho[(size_t)e])
+            if (v != 0.0) fzero[(size_t)e] = 0;
+    }
+    for (size_t q = 0; q < s.rphi.size(); ++q) mp[q] = spline_m(s.rphi[q], dr);
+    const double csiv = std::sqrt(s.cutoff) / ntab;
+    // table (I, J), 1-based id (I-1)*NE + J: pair phi_{max(I,J),min(I,J)}; density of a J atom
+    // at an I atom (zero when element I has no embedding energy)
+    for (int I = 0; I < ne; ++I)
+        for (int J = 0; J < ne; ++J) {
+            const int k = I * ne + J;
+            const int a = I > J ? I : J, b = I > J ? J : I;
+            const std::vector<double> &yp = s.rphi[(size_t)(a * (a + 1) / 2 + b)];
+            const std::vector<double> &mpk = mp[(size_t)(a * (a + 1) / 2 + b)];
+            for (int i = 1; i <= ntab; ++i) {
+                const double t = i * csiv, r = t * t;
+                double f = 0.0, df = 0.0, rho = 0.0, drh = 0.0;
+                if (r <= rimax) {
+                    f = spline_at(yp, mpk, dr, r, &df);
+                    if (!fzero[(size_t)I]) rho = spline_at(s.rhor[(size_t)J], mr[(size_t)J], dr, r, &drh);
+                }
+                const double phi = f / r, dphi = (df - phi) / r;
+                const size_t o = (size_t)(i - 1) * nk + k;  // (NKIND, NTAB) column-major
+                potr[o] = 0.5 * phi * r;
+                fpotr[o] = -dphi * r;
+                potb[o] = rho;
+                fpotb[o] = -drh;
+            }
+            kpair[J * ne + I] = k + 1;                      // KPAIR(I,J), column-major
+        }
+    for (int e = 0; e < ne; ++e) {
+        kembd[e] = e + 1;
+        for (int i = 1; i <= s.nrho; ++i) {
+            const double rho = (i - 1) * s.drho;
+            double d = 0.0, f;
+            if (rho <= fimax) f = spline_at(s.frho[(size_t)e], mf[(size_t)e], s.drho, rho, &d);
+            else f = spline_at(s.frho[(size_t)e], mf[(size_t)e], s.drho, fimax, nullptr);
+            const size_t o = (size_t)(i - 1) * ne + e;      // (NKIND1, NEMBD) column-major
+            fembd[o] = f;
+            dfembd[o] = d;
+        }
+    }
+    if (rhod) *rhod = s.drho;
+    if (masses)
+        for (int e = 0; e < ne; ++e) masses[e] = s.mass[(size_t)e];
     return MSMGB_OK;
 }

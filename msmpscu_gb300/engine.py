@@ -9,6 +9,7 @@ the C ABI of libmsmgb.so; there is no CPU path.
 Units: Angstrom, eV, fs, masses in eV*fs^2/A^2 (``lattice.AMU`` per amu).
 """
 import ctypes as C
+import os
 
 import numpy as np
 
@@ -51,6 +52,39 @@ class ForceTable:
         self.rhod = rhod.value
         self._kpair = np.array([1], np.int32)
         self._kembd = np.array([1], np.int32)
+        self.nkind = self.nkind1 = self.ngroup = 1
+        self.masses = None
+
+    @classmethod
+    def setfl(cls, path, ntab=10000):
+        """Tabulated EAM potential from a setfl file (Register_ForceTableProc_Setfl): NE^2
+        pair tables on the sqrt(r) grid up to the file's cutoff, NE embedding tables on the
+        file's rho grid; masses (amu) from the file."""
+        lib = L.load()
+        ne, nrho, nr, cut = C.c_int(), C.c_int(), C.c_int(), C.c_double()
+        bpath = os.fsencode(path)
+        rc = lib.msmgb_setfl_info(bpath, C.byref(ne), C.byref(nrho), C.byref(nr), C.byref(cut))
+        if rc != L.OK:
+            raise MSMError(rc, "cannot read setfl file %s" % path)
+        self = cls.__new__(cls)
+        ne, nrho = ne.value, nrho.value
+        self.pot, self.pottype, self.prm = None, L.EAM_TYPE, np.zeros(5)
+        self.rmax = self.ru = cut.value
+        self.ntab, self.nembd = int(ntab), nrho
+        self.nkind, self.nkind1, self.ngroup = ne * ne, ne, ne
+        self.potr, self.fpotr, self.potb, self.fpotb = (np.zeros(self.ntab * self.nkind) for _ in range(4))
+        self.fembd, self.dfembd = np.zeros(nrho * ne), np.zeros(nrho * ne)
+        self._kpair = np.zeros(ne * ne, np.int32)
+        self._kembd = np.zeros(ne, np.int32)
+        self.masses = np.zeros(ne)
+        rhod = C.c_double()
+        rc = lib.msmgb_setfl_tables(bpath, self.ntab, _d(self.potr), _d(self.fpotr), _d(self.potb),
+                                    _d(self.fpotb), _d(self.fembd), _d(self.dfembd), _i(self._kpair),
+                                    _i(self._kembd), C.byref(rhod), _d(self.masses))
+        if rc != L.OK:
+            raise MSMError(rc, "setfl table generation failed")
+        self.rhod = rhod.value
+        return self
 
     @classmethod
     def cleri_rosato(cls, A, xi, p, q, r0, rc, ntab=10000):
@@ -69,14 +103,14 @@ class ForceTable:
 
     def struct(self):
         t = L.ForceTable()
-        t.pottype, t.ntab, t.nkind, t.rmax = self.pottype, self.ntab, 1, self.rmax
+        t.pottype, t.ntab, t.nkind, t.rmax = self.pottype, self.ntab, self.nkind, self.rmax
         t.potr, t.fpotr, t.potb, t.fpotb = (_d(a) for a in (self.potr, self.fpotr, self.potb, self.fpotb))
         eam = self.pottype == L.EAM_TYPE
         t.nembd = self.nembd if eam else 0
-        t.nkind1 = 1 if eam else 0
+        t.nkind1 = self.nkind1 if eam else 0
         t.rhod = self.rhod
         t.fembd, t.dfembd = (_d(self.fembd), _d(self.dfembd)) if eam else (None, None)
-        t.ngroup = 1
+        t.ngroup = self.ngroup
         t.kpair = _i(self._kpair)
         t.kembd = _i(self._kembd)
         t.ru = self.ru

@@ -888,3 +888,93 @@ int orc_adjoint_cr(int n, const double *x, const double *y, const double *z, con
     free(fx); free(fy); free(fz); free(dn); free(rho); free(drho);
     return 0;
 }
+
+/* ------------------------------------------------------------------------------------ */
+/* Natural cubic spline (the interpolant of SLATEC DBINT4 with IBCL = IBCR = 2, FBCL =    */
+/* FBCR = 0, KNTOPT = 1, used by Filedatas_Func_Setfl.F90:256-276), uniform grid           */
+/* ------------------------------------------------------------------------------------ */
+void orc_spline_natural(int n, double h, const double *y, double *m)
+{
+    /* m_{i-1} + 4 m_i + m_{i+1} = 6 (y_{i+1} - 2 y_i + y_{i-1}) / h^2, m_0 = m_{n-1} = 0,
+     * solved by forward elimination / back substitution (Thomas) */
+    if (n < 3) {
+        for (int i = 0; i < n; ++i) m[i] = 0.0;
+        return;
+    }
+    double *cp = (double *)malloc(sizeof(double) * (size_t)n);
+    const double s = 6.0 / (h * h);
+    m[0] = 0.0;
+    cp[0] = 0.0;
+    for (int i = 1; i < n - 1; ++i) {
+        const double rhs = s * (y[i + 1] - 2.0 * y[i] + y[i - 1]);
+        const double den = 4.0 - cp[i - 1];
+        cp[i] = 1.0 / den;
+        m[i] = (rhs - m[i - 1]) / den;
+    }
+    m[n - 1] = 0.0;
+    for (int i = n - 2; i >= 1; --i) m[i] -= cp[i] * m[i + 1];
+    free(cp);
+}
+
+double orc_spline_eval(int n, double x0, double h, const double *y, const double *m, double x,
+                       double *dy)
+{
+    int k = (int)floor((x - x0) / h);
+    if (k < 0) k = 0;
+    if (k > n - 2) k = n - 2;
+    const double xk = x0 + k * h;
+    const double b = (x - xk) / h, a = 1.0 - b;
+    const double h26 = h * h / 6.0;
+    if (dy)
+        *dy = (y[k + 1] - y[k]) / h + h * ((1.0 - 3.0 * a * a) * m[k] + (3.0 * b * b - 1.0) * m[k + 1]) / 6.0;
+    return a * y[k] + b * y[k + 1] + ((a * a * a - a) * m[k] + (b * b * b - b) * m[k + 1]) * h26;
+}
+
+int orc_setfl_tables(int nrho, double drho, int nr, double cutoff, const double *frho,
+                     const double *rhor, const double *rphi, int ntab, double *potr, double *fpotr,
+                     double *potb, double *fpotb, double *fembd, double *dfembd)
+{
+    if (nrho < 3 || nr < 3 || ntab < 2) return -1;
+    const double dr = cutoff / nr;              /* R(I) = (I-1) cutoff/Nr (:166-169) */
+    const double rimax = (nr - 1) * dr, fimax = (nrho - 1) * drho;
+    double *m1 = (double *)malloc(sizeof(double) * (size_t)nr);
+    double *m2 = (double *)malloc(sizeof(double) * (size_t)nr);
+    double *m3 = (double *)malloc(sizeof(double) * (size_t)nrho);
+    orc_spline_natural(nr, dr, rphi, m1);
+    orc_spline_natural(nr, dr, rhor, m2);
+    orc_spline_natural(nrho, drho, frho, m3);
+    int fzero = 1;
+    for (int i = 0; i < nrho; ++i)
+        if (frho[i] != 0.0) fzero = 0;
+    const double csiv = sqrt(cutoff) / ntab;
+    for (int i = 1; i <= ntab; ++i) {
+        const double t = i * csiv, r = t * t;
+        double f = 0.0, df = 0.0, rho = 0.0, drh = 0.0;
+        if (r <= rimax) {                       /* Vr_Spline / Rhor_Spline; zero beyond */
+            f = orc_spline_eval(nr, 0.0, dr, rphi, m1, r, &df);
+            if (!fzero) rho = orc_spline_eval(nr, 0.0, dr, rhor, m2, r, &drh);
+        }
+        const double phi = f / r;               /* NN_Spline: V = (r phi)/r, V' = (F' - V)/r */
+        const double dphi = (df - phi) / r;
+        potr[i - 1] = 0.5 * phi * r;
+        fpotr[i - 1] = -dphi * r;
+        potb[i - 1] = rho;
+        fpotb[i - 1] = -drh;
+    }
+    for (int i = 1; i <= nrho; ++i) {           /* EMBED_Spline on RHO_i = (i-1) RHOD, RHOD = drho */
+        const double rho = (i - 1) * drho;
+        double d = 0.0, f;
+        if (rho <= fimax) {
+            f = orc_spline_eval(nrho, 0.0, drho, frho, m3, rho, &d);
+        } else {
+            f = orc_spline_eval(nrho, 0.0, drho, frho, m3, fimax, NULL);
+            d = 0.0;
+        }
+        fembd[i - 1] = f;
+        dfembd[i - 1] = d;
+    }
+    free(m1);
+    free(m2);
+    free(m3);
+    return 0;
+}

@@ -77,7 +77,27 @@ int  orc_make_tables(int pot, const double *prm, double rmax, int ntab, int nemb
                      double *potr, double *fpotr, double *potb, double *fpotb,
                      double *fembd, double *dfembd, double *rhod);
 
-/* neighbour list (MD_NeighborsList.F90:396-633, cut rule d^2 < rc^2 in FP64, minimum image).
+/* Tabulated EAM potentials in LAMMPS setfl layout (Filedatas_Func_Setfl.F90:119-253).  The
+ * reference interpolates the file's arrays with SLATEC DBINT4/DBVALU (LIB/sor/f/MATH90A) with
+ * IBCL = IBCR = 2, FBCL = FBCR = 0, KNTOPT = 1 (:25-34): the cubic interpolating spline with
+ * knots at the data points and zero second derivative at both ends, i.e. the natural cubic
+ * spline, restated here on the uniform grid x_i = x0 + i h.
+ *   orc_spline_natural: second derivatives m[0..n-1] (m[0] = m[n-1] = 0)
+ *   orc_spline_eval:    value (and derivative through *dy) at x in [x0, x0 + (n-1) h]   */
+void   orc_spline_natural(int n, double h, const double *y, double *m);
+double orc_spline_eval(int n, double x0, double h, const double *y, const double *m, double x,
+                       double *dy);
+/* One element's pair and embedding tables from setfl arrays (r grid R_i = i cutoff/nr,
+ * rho grid (i) drho, rphi = r*phi(r)), on the sqrt(r) grid of ntab points up to
+ * Rmax = cutoff and the rho grid RHOD = drho of nrho points (the file's own grid):
+ *   POTR = 0.5 r phi, FPOTR = -r dphi/dr (NN_Spline, :440-458), POTB = rho(r),
+ *   FPOTB = -drho/dr (RHO_Spline, :461-476), FEMBD/DFEMBD = F, dF/drho (EMBED_Spline,
+ *   :479-496), with the reference's clamping outside the data range (:292-437). */
+int    orc_setfl_tables(int nrho, double drho, int nr, double cutoff, const double *frho,
+                        const double *rhor, const double *rphi, int ntab, double *potr, double *fpotr,
+                        double *potb, double *fpotb, double *fembd, double *dfembd);
+
+/* neighbour list (MD_NeighborsList.F90:396-633/* neighbour list (MD_NeighborsList.F90:396-633, cut rule d^2 < rc^2 in FP64, minimum image).
  * indi is ELL column-major: neighbour k of atom i at indi[k*n + i]; 0-based atom ids.
  * Returns 0, or -1 on neighbour overflow, -2 on an atom outside the box. */
 int  orc_nlist(int n, const double *x, const double *y, const double *z, const int *statu,

@@ -46,6 +46,8 @@ def lib():
         _lib.orc_hvp.restype = C.c_int
         _lib.orc_adjoint_cr.restype = C.c_int
         _lib.orc_atomic_stress.restype = None
+        _lib.orc_spline_eval.restype = C.c_double
+        _lib.orc_setfl_tables.restype = C.c_int
         _lib.orc_pot_eval.restype = C.c_int
         _lib.orc_embed_eval.restype = C.c_int
     return _lib
@@ -125,22 +127,79 @@ class RawTables:
     """Multi-kind tables in the reference layout: arrays (NTAB, NKIND) C-order = Fortran
     (NKIND, NTAB); kpair (NGROUP, NGROUP) with KPAIR(i, j) at kpair[i-1, j-1]."""
 
-    def __init__(self, pottype, ntab, nkind, rmax, ru, potr, fpotr, potb, fpotb, kpair):
-        self.keep = [f64(a) for a in (potr, fpotr, potb, fpotb)] + [np.zeros(1), np.zeros(1)]
+    def __init__(self, pottype, ntab, nkind, rmax, ru, potr, fpotr, potb, fpotb, kpair, fembd=None,
+                 dfembd=None, kembd=None, rhod=1.0):
+        """EAM: fembd/dfembd (NEMBD, NKIND1) C-order = Fortran (NKIND1, NEMBD), kembd 1-based."""
+        emb = [f64(fembd), f64(dfembd)] if fembd is not None else [np.zeros(1), np.zeros(1)]
+        self.keep = [f64(a) for a in (potr, fpotr, potb, fpotb)] + emb
         ng = np.asarray(kpair).shape[0]
         self.kpair = i32(np.asarray(kpair, np.int32).T)
-        self.kembd = i32(np.ones(ng))
+        self.kembd = i32(kembd if kembd is not None else np.ones(ng))
         s = OrcTables()
         s.pottype, s.ntab, s.nkind = pottype, ntab, nkind
         s.csi = float(ntab) / np.sqrt(rmax)
         s.ru2 = ru * ru
         s.potr, s.fpotr, s.potb, s.fpotb = (_d(a) for a in self.keep[:4])
-        s.nembd, s.nkind1, s.rhod = 1, 1, 1.0
+        if fembd is not None:
+            fe = np.asarray(fembd)
+            s.nembd, s.nkind1, s.rhod = fe.shape[0], (fe.shape[1] if fe.ndim == 2 else 1), float(rhod)
+        else:
+            s.nembd, s.nkind1, s.rhod = 1, 1, 1.0
         s.fembd, s.dfembd = _d(self.keep[4]), _d(self.keep[5])
         s.ngroup = ng
         s.kpair = _i(self.kpair)
         s.kembd = _i(self.kembd)
         self.s = s
+
+
+def read_setfl(path):
+    """Setfl file (Filedatas_Func_Setfl.F90:119-253): elements, grids, and per element F(rho)
+    and rho(r), then r*phi(r) for every pair i >= j.  'INF' / 'NAN' as the first value of a
+    rho / r*phi block stand for the r = 0 entry, which takes the next value."""
+    lines = open(path).read().split("\n")
+    el = lines[3].split()
+    ne = int(float(el[0]))
+    g = lines[4].split()
+    nrho, drho, nr, dr, cutoff = int(g[0]), float(g[1]), int(g[2]), float(g[3]), float(g[4])
+    toks = " ".join(lines[5:]).split()
+    pos = 0
+    out = dict(elements=el[1:1 + ne], nrho=nrho, drho=drho, nr=nr, dr=dr, cutoff=cutoff,
+               mass=[], frho=[], rhor=[], rphi={})
+
+    def block(n):
+        nonlocal pos
+        v = toks[pos:pos + n]
+        pos += n
+        vals = np.array([np.nan if x.upper() in ("INF", "NAN") else float(x) for x in v])
+        if np.isnan(vals[0]):
+            vals[0] = vals[1]
+        return vals
+
+    for _ in range(ne):
+        out["mass"].append(float(toks[pos + 1]))
+        pos += 4
+        out["frho"].append(block(nrho))
+        out["rhor"].append(block(nr))
+    for i in range(ne):
+        for j in range(i + 1):
+            out["rphi"][(i, j)] = block(nr)
+    return out
+
+
+def setfl_tables(d, ntab=10000, i=0, j=None):
+    """Tables of an element-i atom with an element-j neighbour (default j = i) from
+    read_setfl output: pair phi_ij, density of element j, embedding of element i; RHOD = drho."""
+    j = i if j is None else j
+    potr, fpotr, potb, fpotb = (np.zeros(ntab) for _ in range(4))
+    fe, dfe = np.zeros(d["nrho"]), np.zeros(d["nrho"])
+    rc = lib().orc_setfl_tables(d["nrho"], C.c_double(d["drho"]), d["nr"], C.c_double(d["cutoff"]),
+                                _d(f64(d["frho"][i])), _d(f64(d["rhor"][j])),
+                                _d(f64(d["rphi"][(max(i, j), min(i, j))])),
+                                ntab, _d(potr), _d(fpotr), _d(potb), _d(fpotb), _d(fe), _d(dfe))
+    if rc != 0:
+        raise RuntimeError("oracle setfl tables failed")
+    return dict(potr=potr, fpotr=fpotr, potb=potb, fpotb=fpotb, fembd=fe, dfembd=dfe, rhod=d["drho"],
+                ntab=ntab, nembd=d["nrho"], rmax=d["cutoff"])
 
 
 def make_box(lo, length, ifpd=(1, 1, 1)):
