@@ -175,11 +175,12 @@ def batched_uneven_boxes(steps, steps_perbox, device=0):
         e.set_masses([lt.CU_MASS])
         e.copyin(desc, pos, vel)
         e.run_steps(3, DT)
+        l0 = e.launches
         ms, reb = e.time_steps(steps, DT)
         out["batched_%s_box_steps_per_s" % prec] = len(boxes) * steps / (ms / 1e3)
         out["batched_%s_atom_steps_per_s" % prec] = len(pos) * steps / (ms / 1e3)
         out["batched_%s_ms_per_step" % prec] = ms / steps
-        out["batched_%s_launches_per_step" % prec] = None
+        out["batched_%s_launches_per_step" % prec] = (e.launches - l0) / steps
         e.close()
     engines = []
     for (p, v, L), d in zip(boxes, desc):
