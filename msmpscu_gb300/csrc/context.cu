@@ -928,8 +928,9 @@ static int capture_fused(msmgb_ctx *c, double h)
     }
     const DevAtoms base = c->a;
     int rc = MSMGB_OK;
-    // tune the fused mixed kernel on the current state (h = 0 changes nothing), outside capture
-    if (c->p.precision == MSMGB_PREC_MIXED) {
+    // tune the fused mixed kernel on the current state (h = 0 changes nothing), outside
+    // capture, once per atom count (a new state of the same size keeps the choice)
+    if (c->p.precision == MSMGB_PREC_MIXED && c->tuned_fused_n != c->n) {
         c->a = atoms_on(c, base, 0);
         rc = autotune_fused(c);
         c->a = base;

@@ -660,6 +660,7 @@ int autotune_fused(msmgb_ctx *c)
     }
     c->tune_fused = bestc;
     c->tune_ms_fused = best / 3.0f;
+    c->tuned_fused_n = c->n;
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     cudaMemsetAsync(c->a.maxdisp, 0, sizeof(unsigned long long), c->stream);

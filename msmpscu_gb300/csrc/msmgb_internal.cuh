@@ -304,6 +304,7 @@ struct msmgb_ctx {
     // autotuned launch variants of the mixed passes (neighbours in flight per thread)
     int tune_dens_unroll = 2, tune_force_unroll = 2, tune_fused = 0;
     float tune_ms_fused = 0.f;
+    int tuned_fused_n = -1;      // atom count the fused kernel was tuned for
     int tuned_n = -1;
     float tune_ms[2] = {0.f, 0.f};
 
