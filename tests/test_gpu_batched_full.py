@@ -43,10 +43,12 @@ def test_512_uneven_boxes_forces_all_precisions(oracle):
         e.calforce()
         f = e.get_force()
         off, worst = 0, 0.0
-        for (p, v, L_), ref in zip(boxes, refs):
+        for k, ((p, v, L_), ref) in enumerate(zip(boxes, refs)):
             sl = slice(off, off + len(p))
             worst = max(worst, rel_err(f[sl], ref))
-            assert np.abs(f[sl].sum(0)).max() < 1e-9 * len(p) * np.abs(ref).max()
+            # momentum: FP64-class passes to rounding, the mixed passes to FP32 rounding
+            mtol = (1e-6 if precision == "mixed" else 1e-9) * len(p) * np.abs(ref).max()
+            assert np.abs(f[sl].sum(0)).max() < mtol, (precision, k)
             off += len(p)
         assert worst < tol, (precision, worst)
         e.close()
