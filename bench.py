@@ -274,6 +274,42 @@ def bytes_model(kmean):
     return dict(density=dens, force=force, vv=vv, fused=force + vv - 24.0, step=dens + force + vv)
 
 
+def nve_drift(device=0, steps=20000, every=2000):
+    """Total-energy drift of NVE runs (Cu 10^3 cells, 4,000 atoms, 600 K, sigma 0.05 A,
+    dt = 1 fs, skin trigger) in each precision: (E(end) - E(0)) per atom per ns and the largest
+    excursion |E(t) - E(0)| per atom seen at the checkpoints.  Energies from the FP64 passes."""
+    from msmpscu_gb300 import Engine, ForceTable, lattice as lt
+    pos, vel, L = lt.cu_config(10, SIGMA, TEMP, 7)
+    n = len(pos)
+    box = [(n, (0, 0, 0), tuple(L), (1, 1, 1))]
+    out = {"atoms": n, "steps": steps, "dt_fs": DT}
+
+    def energy(e):
+        _, v, _, _ = e.get_state()
+        prec = e.precision
+        e.set_precision("fp64")
+        e.calepot()
+        pe = float(e.get_epot().sum())
+        e.set_precision(prec)
+        return pe + 0.5 * lt.CU_MASS * float((v * v).sum())
+
+    for prec in ("fp64", "ff", "mixed"):
+        e = Engine(n, lt.CU_RC_NL, mxkvois=MXKVOIS, skin_trigger=0.15, precision=prec, device=device)
+        e.init_forcetable(ForceTable.cleri_rosato(**lt.CU_CR, rc=lt.CU_RC))
+        e.set_masses([lt.CU_MASS])
+        e.copyin(box, pos, vel)
+        e0 = energy(e)
+        excursion = 0.0
+        for _ in range(steps // every):
+            e.run_steps(every, DT)
+            excursion = max(excursion, abs(energy(e) - e0))
+        e1 = energy(e)
+        out[prec + "_drift_eV_per_atom_per_ns"] = (e1 - e0) / n / (steps * DT * 1e-6)
+        out[prec + "_max_excursion_eV_per_atom"] = excursion / n
+        e.close()
+    return out
+
+
 def cpu_baseline(pos, vel, L, nthreads, sample_steps=2):
     """Oracle (C restatement of the reference's serial CPU path) on the full workload:
     per-step time = (T(k steps) - T(0 steps)) / k, both runs including the initial list
@@ -421,15 +457,20 @@ def run_ours(args):
         extras["batched_boxes"] = batched_uneven_boxes(max(10, min(args.steps, 100)), 20, device)
         extras["hvp"] = hvp_w_dumbbell(device)
         extras["adjoint"] = adjoint_cu_snapshots(device)
+        extras["nve_drift"] = nve_drift(device)
         e = None
 
     cpu = None
     if rank == 0 and not args.no_cpu:
         threads = os.cpu_count() or 1
         cv, per = cpu_baseline(pos, vel, L, threads, sample_steps=args.cpu_steps)
+        # the reference's CPU path is serial: the same sample on one thread
+        cv1, per1 = cpu_baseline(pos, vel, L, 1, sample_steps=1)
         cpu = {"value": cv, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": "%d NVE steps of the full 2,048,000-atom system (oracle, OpenMP over "
-                         "atoms), per-step time %.2f s" % (args.cpu_steps, per)}
+                         "atoms), per-step time %.2f s" % (args.cpu_steps, per),
+               "serial_value": cv1, "serial_sample": "1 NVE step of the same system on one thread, "
+                                                     "per-step time %.2f s" % per1}
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,

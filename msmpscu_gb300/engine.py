@@ -131,6 +131,7 @@ class Engine:
         p.device, p.max_atoms, p.max_boxes, p.mxkvois = device, int(max_atoms), int(max_boxes), int(mxkvois)
         p.rc_nl, p.skin_trigger, p.nb_uptab = float(rc_nl), float(skin_trigger), int(nb_uptab)
         p.precision = L.PRECISIONS[precision]
+        self.precision = precision
         p.stream = stream
         self.ctx = C.c_void_p()
         rc = self.lib.msmgb_create(C.byref(self.ctx), C.byref(p))
@@ -172,6 +173,7 @@ class Engine:
 
     def set_precision(self, precision):
         self._ck(self.lib.msmgb_set_precision(self.ctx, L.PRECISIONS[precision]))
+        self.precision = precision
 
     # ---- force class ---------------------------------------------------------------------------
     def init_forcetable(self, table: ForceTable):
