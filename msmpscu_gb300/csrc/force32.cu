@@ -138,7 +138,7 @@ __device__ __forceinline__ unsigned pair_index(const PosFF &pi, const PosFF &pj,
 __device__ __forceinline__ void ld_comb(const float4 *comb, int kk, float4 &r0, float4 &r1)
 {
     const float4 *q = comb + 2 * (size_t)kk;
-    asm("ld.global.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+    asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
         : "=f"(r0.x), "=f"(r0.y), "=f"(r0.z), "=f"(r0.w), "=f"(r1.x), "=f"(r1.y), "=f"(r1.z), "=f"(r1.w)
         : "l"(q));
 }
