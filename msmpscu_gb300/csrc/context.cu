@@ -209,9 +209,8 @@ extern "C" int msmgb_create(msmgb_ctx **out, const msmgb_params *p)
     if ((e = cudaMallocHost((void **)&c->h_virial, sizeof(double) * 6 * c->cap_boxes)) != cudaSuccess) return fail(e, "pinned");
     if ((e = cudaMemsetAsync(c->flags, 0, sizeof(int) * kFlagWords, c->stream)) != cudaSuccess) return fail(e, "memset");
     if ((e = cudaMemsetAsync(c->maxdisp, 0, sizeof(unsigned long long), c->stream)) != cudaSuccess) return fail(e, "memset");
-    if (p->precision == MSMGB_PREC_MIXED && ((e = dalloc(&a.pk, N * (size_t)p->mxkvois)) != cudaSuccess ||
-                                            (e = dalloc(&a.pb, N * (size_t)p->mxkvois)) != cudaSuccess))
-        return fail(e, "cudaMalloc pair buffers");
+    if (p->precision == MSMGB_PREC_MIXED && (e = dalloc(&a.pk, N * (size_t)p->mxkvois)) != cudaSuccess)
+        return fail(e, "cudaMalloc pair index");
     if (p->precision != MSMGB_PREC_FP64 && (e = dalloc(&a.rec, N)) != cudaSuccess)
         return fail(e, "cudaMalloc records");
     if (p->precision == MSMGB_PREC_FF && ((e = dalloc(&a.posfx, N)) != cudaSuccess || (e = dalloc(&a.recfx, N)) != cudaSuccess))
@@ -236,7 +235,7 @@ extern "C" int msmgb_destroy(msmgb_ctx *c)
     DevAtoms &a = c->a;
     void *ptrs[] = {a.pos, a.posff, a.pos_bld, a.vx, a.vy, a.vz, a.fx, a.fy, a.fz,
                     a.dx, a.dy, a.dz, a.ityp, a.statu, a.gid, a.boxid, a.den, a.epot,
-                    a.den32, a.kvois, a.indi, a.pk, a.pb, a.rec, a.posfx, a.recfx, c->cell_of, c->perm, c->dbox, c->cm, c->icm,
+                    a.den32, a.kvois, a.indi, a.pk, a.rec, a.posfx, a.recfx, c->cell_of, c->perm, c->dbox, c->cm, c->icm,
                     c->flags, c->maxdisp, c->virial, c->scratch, c->cell_start,
                     c->cell_cursor, c->scan_tmp, c->tab_mem, c->adj_mem, c->hvp_pair, c->pos2, c->posff2};
     for (void *q : ptrs)
@@ -261,7 +260,6 @@ extern "C" int msmgb_set_precision(msmgb_ctx *c, int precision)
         RET(use_device(c));
         CK(cudaStreamSynchronize(c->stream), "synchronize");
         CK(dalloc(&c->a.pk, (size_t)c->cap_atoms * (size_t)c->p.mxkvois), "cudaMalloc pair index");
-        CK(dalloc(&c->a.pb, (size_t)c->cap_atoms * (size_t)c->p.mxkvois), "cudaMalloc pair terms");
     }
     if (precision == MSMGB_PREC_FF && !c->a.posfx) {
         RET(use_device(c));
@@ -390,17 +388,6 @@ extern "C" int msmgb_init_forcetable(msmgb_ctx *c, const msmgb_forcetable *ft)
                 e2[2 * o + 1] = (float)(hdf[o1] - hdf[o]);
             }
     }
-    // combined single-kind row of the mixed density pass (kind 0): 32 B per grid point
-    std::vector<float> fc((size_t)8 * rowp, 0.0f);
-    for (size_t i = 0; i < rowp; ++i) {
-        const size_t o = i, o1 = i + 1 < rowp ? i + 1 : i;
-        fc[8 * i + 0] = (float)hpotb[o];
-        fc[8 * i + 1] = (float)(hpotb[o1] - hpotb[o]);
-        fc[8 * i + 2] = (float)hfpotr[o];
-        fc[8 * i + 3] = (float)(hfpotr[o1] - hfpotr[o]);
-        fc[8 * i + 4] = (float)hfpotb[o];
-        fc[8 * i + 5] = (float)(hfpotb[o1] - hfpotb[o]);
-    }
     // float-float tables: value and FP64 slope, each split into hi + lo
     auto split = [](double v, float *o) {
         o[0] = (float)v;
@@ -429,8 +416,7 @@ extern "C" int msmgb_init_forcetable(msmgb_ctx *c, const msmgb_forcetable *ft)
     CK(cudaStreamSynchronize(c->stream), "synchronize");
     if (c->tab_mem) { cudaFree(c->tab_mem); c->tab_mem = nullptr; }
     const size_t bytes = nd * sizeof(double) +
-                         (f2.size() + f4.size() + e2.size() + fd.size() + ff8.size() + fe.size() + fc.size()) *
-                             sizeof(float) +
+                         (f2.size() + f4.size() + e2.size() + fd.size() + ff8.size() + fe.size()) * sizeof(float) +
                          2048;
     CK(cudaMalloc(&c->tab_mem, bytes), "table alloc");
     char *base = (char *)c->tab_mem;
@@ -443,9 +429,6 @@ extern "C" int msmgb_init_forcetable(msmgb_ctx *c, const msmgb_forcetable *ft)
     float *dfd = (float *)a16;
     float *dff8 = dfd + fd.size();
     float *dfe = dff8 + ff8.size();
-    // combined rows are read with 256-bit loads: 32-byte aligned
-    float *dfc = (float *)((((uintptr_t)(dfe + fe.size())) + 31) & ~(uintptr_t)31);
-    CK(cudaMemcpy(dfc, fc.data(), fc.size() * sizeof(float), cudaMemcpyHostToDevice), "table upload");
     CK(cudaMemcpy(dd, hd.data(), nd * sizeof(double), cudaMemcpyHostToDevice), "table upload");
     CK(cudaMemcpy(dfd, fd.data(), fd.size() * sizeof(float), cudaMemcpyHostToDevice), "table upload");
     CK(cudaMemcpy(dff8, ff8.data(), ff8.size() * sizeof(float), cudaMemcpyHostToDevice), "table upload");
@@ -462,7 +445,6 @@ extern "C" int msmgb_init_forcetable(msmgb_ctx *c, const msmgb_forcetable *ft)
     t.dens2 = (const float2 *)df2;
     t.embd2 = eam ? (const float2 *)de2 : nullptr;
     t.densff = (const float4 *)dfd;
-    t.comb = (const float4 *)dfc;
     t.forceff = (const float4 *)dff8;
     t.embff = eam ? (const float4 *)dfe : nullptr;
     {

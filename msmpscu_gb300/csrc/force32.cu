@@ -14,16 +14,13 @@
 //     FP64 rule up to ~1e-13 relative;
 //   * SK = CSI r2^(1/4): two MUFU reciprocal square roots and one Newton correction
 //     evaluated in float-float give DK to ~1e-7.
-// Hand-over between the passes (one table kind, the common case): the density pass reads one
-// 32 B table row {POTB, slope, FPOTR, slope, FPOTB, slope} per pair and hands the force pass
-// the interpolated pair terms {FPOTR(r), FPOTB(r)} (8 B per pair, ELL layout; zero beyond RU),
-// so the force pass streams them coalesced and gathers no table row; it only forms the FP32
-// separation for the force direction and 1/R.  With several table kinds the density pass
-// stores the table index of every pair instead (KK << 18 | DK * 2^18, DK quantised to 4e-6,
-// a table-value error below 1e-8), because the force pass then needs FPOTB of both KPAIR(i,j)
-// and KPAIR(j,i).  Table values come from interleaved {value, slope} FP32 rows; rho and F
-// accumulate in FP32 (measured error ~3e-7 of the FP64 forces).  Positions, the integrator
-// and the list stay FP64.
+// The density pass stores the table index of every pair it accepts (KK << 18 | DK * 2^18,
+// DK quantised to 4e-6, i.e. a table-value error below 1e-8) in the ELL layout of the
+// list; the force pass reads it back instead of recomputing the separation in float-float
+// and only forms the FP32 separation for the force direction and 1/R.
+// Table values come from interleaved {value, slope} FP32 rows (one 8 B or 16 B load per
+// pair); rho and F accumulate in FP32 (measured error ~3e-7 of the FP64 forces).
+// Positions, the integrator and the list stay FP64.
 #include <algorithm>
 
 #include "msmgb_internal.cuh"
@@ -133,38 +130,6 @@ __device__ __forceinline__ unsigned pair_index(const PosFF &pi, const PosFF &pj,
     return ((unsigned)kk << kDkBits) | q;
 }
 
-
-// combined single-kind table row at index kk: {POTB, dPOTB, FPOTR, dFPOTR}, {FPOTB, dFPOTB, -, -}
-__device__ __forceinline__ void ld_comb(const float4 *comb, int kk, float4 &r0, float4 &r1)
-{
-    const float4 *q = comb + 2 * (size_t)kk;
-    asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
-        : "=f"(r0.x), "=f"(r0.y), "=f"(r0.z), "=f"(r0.w), "=f"(r1.x), "=f"(r1.y), "=f"(r1.z), "=f"(r1.w)
-        : "l"(q));
-}
-
-// One list slot of the density pass.  Single kind: rho contribution and the handed-over pair
-// terms {FPOTR(r), FPOTB(r)} (zero beyond RU); several kinds: the packed table index.
-template <bool MULTI>
-__device__ __forceinline__ float density_slot(const PosFF &pi, const PosFF &pj, const BoxF &b, const DevTables &t,
-                                              float rej, int k, bool valid, unsigned *pk, float2 *pb)
-{
-    float dk = 0.0f;
-    int kk = 0;
-    const unsigned c = pair_index(pi, pj, b, t, rej, dk, kk);
-    const bool ok = valid && c != kSkip;
-    if (MULTI) {
-        if (valid) *pk = c;
-        const float2 e = __ldg(t.dens2 + k * t.ntp + (ok ? kk : 0));
-        return ok ? fmaf(dk, e.y, e.x) : 0.0f;
-    }
-    float4 r0, r1;
-    ld_comb(t.comb, ok ? kk : 0, r0, r1);
-    if (valid)
-        *pb = ok ? make_float2(fmaf(dk, r0.w, r0.z), fmaf(dk, r1.y, r1.x)) : make_float2(0.0f, 0.0f);
-    return ok ? fmaf(dk, r0.y, r0.x) : 0.0f;
-}
-
 template <int POT, bool MULTI, int UNR, int MINB, bool PF>
 __global__ void __launch_bounds__(kBlock, MINB) k_density32(DevAtoms a, DevTables t)
 {
@@ -172,7 +137,6 @@ __global__ void __launch_bounds__(kBlock, MINB) k_density32(DevAtoms a, DevTable
     if (i >= a.n) return;
     const int kn = a.kvois[i];
     unsigned *__restrict__ pk = a.pk + i;
-    float2 *__restrict__ pb = a.pb + i;
     const size_t ld = (size_t)a.ld;
     if ((a.statu[i] & MSMGB_STATU_ACTIVE) != MSMGB_STATU_ACTIVE) {   // the force pass skips it
         a.den32[i] = 0.0f;
@@ -184,6 +148,7 @@ __global__ void __launch_bounds__(kBlock, MINB) k_density32(DevAtoms a, DevTable
     const PosFF pi = ld_ff(a.posff + i);
     const int ti = MULTI ? a.ityp[i] - 1 : 0;
     const int *__restrict__ nb = a.indi + i;
+    const float2 *__restrict__ row0 = t.dens2;
     float rho = 0.0f;
     if (PF) {
         // list entries of the next UNR slots are loaded one iteration ahead (slots past
@@ -206,9 +171,14 @@ __global__ void __launch_bounds__(kBlock, MINB) k_density32(DevAtoms a, DevTable
             for (int u = 0; u < UNR; ++u) p[u] = ld_ff(a.posff + (j[u] >= 0 ? j[u] : i));
 #pragma unroll
             for (int u = 0; u < UNR; ++u) {
-                const int jj = j[u] >= 0 ? j[u] : i;
-                const int k = MULTI ? t.kpair[(a.ityp[jj] - 1) * t.ngroup + ti] : 0;
-                rho += density_slot<MULTI>(pi, p[u], b, t, rej, k, j[u] >= 0, pk + (w + u) * ld, pb + (w + u) * ld);
+                float dk = 0.0f;
+                int kk = 0;
+                const unsigned c = pair_index(pi, p[u], b, t, rej, dk, kk);
+                if (j[u] >= 0) pk[(w + u) * ld] = c;
+                const bool ok = j[u] >= 0 && c != kSkip;
+                const int k = MULTI ? t.kpair[(a.ityp[j[u] >= 0 ? j[u] : i] - 1) * t.ngroup + ti] : 0;
+                const float2 e = __ldg(row0 + k * t.ntp + (ok ? kk : 0));
+                rho += ok ? fmaf(dk, e.y, e.x) : 0.0f;
             }
         }
     } else {
@@ -223,15 +193,29 @@ __global__ void __launch_bounds__(kBlock, MINB) k_density32(DevAtoms a, DevTable
             for (int u = 0; u < UNR; ++u) p[u] = ld_ff(a.posff + j[u]);
 #pragma unroll
             for (int u = 0; u < UNR; ++u) {
-                const int k = MULTI ? t.kpair[(a.ityp[j[u]] - 1) * t.ngroup + ti] : 0;
-                rho += density_slot<MULTI>(pi, p[u], b, t, rej, k, true, pk + (w + u) * ld, pb + (w + u) * ld);
+                float dk;
+                int kk;
+                const unsigned c = pair_index(pi, p[u], b, t, rej, dk, kk);
+                pk[(w + u) * ld] = c;
+                if (c != kSkip) {
+                    const int k = MULTI ? t.kpair[(a.ityp[j[u]] - 1) * t.ngroup + ti] : 0;
+                    const float2 e = __ldg(row0 + k * t.ntp + kk);
+                    rho += fmaf(dk, e.y, e.x);
+                }
             }
         }
         for (; w < kn; ++w) {
             const int j0 = __ldg(nb + w * ld);
             const PosFF p0 = ld_ff(a.posff + j0);
-            const int k = MULTI ? t.kpair[(a.ityp[j0] - 1) * t.ngroup + ti] : 0;
-            rho += density_slot<MULTI>(pi, p0, b, t, rej, k, true, pk + w * ld, pb + w * ld);
+            float dk;
+            int kk;
+            const unsigned c = pair_index(pi, p0, b, t, rej, dk, kk);
+            pk[w * ld] = c;
+            if (c != kSkip) {
+                const int k = MULTI ? t.kpair[(a.ityp[j0] - 1) * t.ngroup + ti] : 0;
+                const float2 e = __ldg(row0 + k * t.ntp + kk);
+                rho += fmaf(dk, e.y, e.x);
+            }
         }
     }
     float d = rho;
@@ -263,10 +247,10 @@ __device__ __forceinline__ float sep1(float hi, float lo, float hj, float lj, fl
     return dh + dl;
 }
 
-// Pair term with several table kinds: table index c from the density pass.
-__device__ __forceinline__ void force_pair_multi(const PosFF &pi, const PosFF &pj, unsigned c, float di,
-                                                 float dj, int ti, int tj, const BoxF &b, const DevTables &t,
-                                                 float &fx, float &fy, float &fz)
+template <bool MULTI>
+__device__ __forceinline__ void force_pair(const PosFF &pi, const PosFF &pj, unsigned c, float di,
+                                           float dj, int ti, int tj, const BoxF &b, const DevTables &t,
+                                           float &fx, float &fy, float &fz)
 {
     const float sx = sep1(pi.hx, pi.lx, pj.hx, pj.lx, b.lh[0], b.ll[0], b.half[0], b.pd[0]);
     const float sy = sep1(pi.hy, pi.ly, pj.hy, pj.ly, b.lh[1], b.ll[1], b.half[1], b.pd[1]);
@@ -274,15 +258,17 @@ __device__ __forceinline__ void force_pair_multi(const PosFF &pi, const PosFF &p
     const float y = rsqrtf(fmaf(sx, sx, fmaf(sy, sy, sz * sz)));
     const int kk = (int)(c >> kDkBits);
     const float dk = (float)(c & ((1u << kDkBits) - 1)) * kDkInv;
-    const int k = t.kpair[tj * t.ngroup + ti];
+    const int k = MULTI ? t.kpair[tj * t.ngroup + ti] : 0;
     const float4 e = __ldg(t.force4 + k * t.ntp + kk);
     const float P = fmaf(dk, e.y, e.x);
     const float B = fmaf(dk, e.w, e.z);
     float emb = B * (di + dj);
-    const int k1 = t.kpair[ti * t.ngroup + tj];
-    if (k1 != k) {
-        const float4 e1 = __ldg(t.force4 + k1 * t.ntp + kk);
-        emb = B * di + fmaf(dk, e1.w, e1.z) * dj;
+    if (MULTI) {
+        const int k1 = t.kpair[ti * t.ngroup + tj];
+        if (k1 != k) {
+            const float4 e1 = __ldg(t.force4 + k1 * t.ntp + kk);
+            emb = B * di + fmaf(dk, e1.w, e1.z) * dj;
+        }
     }
     const float ft = fmaf(P, y, emb) * y;
     fx = fmaf(ft, sx, fx);
@@ -290,39 +276,23 @@ __device__ __forceinline__ void force_pair_multi(const PosFF &pi, const PosFF &p
     fz = fmaf(ft, sz, fz);
 }
 
-// Pair term with one table kind: the interpolated FPOTR, FPOTB handed over by the density
-// pass (both zero beyond RU, so such slots add exactly zero).
-__device__ __forceinline__ void force_pair_pb(const PosFF &pi, const PosFF &pj, float2 pbv, float di,
-                                              const BoxF &b, float &fx, float &fy, float &fz)
-{
-    const float sx = sep1(pi.hx, pi.lx, pj.hx, pj.lx, b.lh[0], b.ll[0], b.half[0], b.pd[0]);
-    const float sy = sep1(pi.hy, pi.ly, pj.hy, pj.ly, b.lh[1], b.ll[1], b.half[1], b.pd[1]);
-    const float sz = sep1(pi.hz, pi.lz, pj.hz, pj.lz, b.lh[2], b.ll[2], b.half[2], b.pd[2]);
-    const float y = rsqrtf(fmaf(sx, sx, fmaf(sy, sy, sz * sz)));
-    const float ft = fmaf(pbv.x, y, pbv.y * (di + pj.d)) * y;
-    fx = fmaf(ft, sx, fx);
-    fy = fmaf(ft, sy, fy);
-    fz = fmaf(ft, sz, fz);
-}
-
-// Walks the ELL list of atom i, UNR slots per iteration, and calls body(j, v) for every slot
-// (v = the slot's entry of `pv`, a packed index or handed-over pair terms) for which
-// keep(v) holds.  With PF the slots of the next iteration are loaded before the current ones
-// are processed (slots past KVOIS read as `none` and are not kept).
-template <int UNR, bool PF, class V, class Keep, class Body>
-__device__ __forceinline__ void walk_pairs(const int *__restrict__ nb, const V *__restrict__ pv, size_t ld,
-                                           int kn, V none, Keep keep, Body body)
+// Walks the ELL list of atom i, UNR slots per iteration, and calls body(j, c) for every slot
+// whose packed index c is not kSkip.  With PF the slots of the next iteration are loaded
+// before the current ones are processed (slots past KVOIS read as kSkip).
+template <int UNR, bool PF, class Body>
+__device__ __forceinline__ void walk_pairs(const int *__restrict__ nb, const unsigned *__restrict__ pk,
+                                           size_t ld, int kn, Body body)
 {
     if (PF) {
-        V cn[UNR];
+        unsigned cn[UNR];
         int jn[UNR];
 #pragma unroll
         for (int u = 0; u < UNR; ++u) {
-            cn[u] = u < kn ? __ldg(pv + u * ld) : none;
+            cn[u] = u < kn ? __ldg(pk + u * ld) : kSkip;
             jn[u] = u < kn ? __ldg(nb + u * ld) : 0;
         }
         for (int w = 0; w < kn; w += UNR) {
-            V c[UNR];
+            unsigned c[UNR];
             int j[UNR];
 #pragma unroll
             for (int u = 0; u < UNR; ++u) {
@@ -332,63 +302,74 @@ __device__ __forceinline__ void walk_pairs(const int *__restrict__ nb, const V *
 #pragma unroll
             for (int u = 0; u < UNR; ++u) {
                 const int sl = w + UNR + u;
-                cn[u] = sl < kn ? __ldg(pv + sl * ld) : none;
+                cn[u] = sl < kn ? __ldg(pk + sl * ld) : kSkip;
                 jn[u] = sl < kn ? __ldg(nb + sl * ld) : 0;
             }
 #pragma unroll
             for (int u = 0; u < UNR; ++u)
-                if (keep(c[u])) body(j[u], c[u]);
+                if (c[u] != kSkip) body(j[u], c[u]);
         }
     } else {
         int w = 0;
         for (; w + UNR <= kn; w += UNR) {
-            V c[UNR];
+            unsigned c[UNR];
             int j[UNR];
 #pragma unroll
             for (int u = 0; u < UNR; ++u) {
-                c[u] = __ldg(pv + (w + u) * ld);
+                c[u] = __ldg(pk + (w + u) * ld);
                 j[u] = __ldg(nb + (w + u) * ld);
             }
 #pragma unroll
             for (int u = 0; u < UNR; ++u)
-                if (keep(c[u])) body(j[u], c[u]);
+                if (c[u] != kSkip) body(j[u], c[u]);
         }
         for (; w < kn; ++w) {
-            const V c0 = __ldg(pv + w * ld);
-            if (keep(c0)) body(__ldg(nb + w * ld), c0);
+            const unsigned c0 = __ldg(pk + w * ld);
+            if (c0 != kSkip) body(__ldg(nb + w * ld), c0);
         }
     }
 }
 
-struct KeepIndex {
-    __device__ bool operator()(unsigned c) const { return c != kSkip; }
-};
-// slots with zero pair terms (beyond RU, or past KVOIS in the prefetching walk) add nothing
-struct KeepTerms {
-    __device__ bool operator()(float2 v) const { return v.x != 0.0f || v.y != 0.0f; }
-};
+// Single-kind pair term with the table row e = {P, P', B, B'} (at KK) already loaded.
+__device__ __forceinline__ void force_pair_e(const PosFF &pi, const PosFF &pj, unsigned c, float di, float dj,
+                                             const float4 &e, const BoxF &b, float &fx, float &fy, float &fz)
+{
+    const float sx = sep1(pi.hx, pi.lx, pj.hx, pj.lx, b.lh[0], b.ll[0], b.half[0], b.pd[0]);
+    const float sy = sep1(pi.hy, pi.ly, pj.hy, pj.ly, b.lh[1], b.ll[1], b.half[1], b.pd[1]);
+    const float sz = sep1(pi.hz, pi.lz, pj.hz, pj.lz, b.lh[2], b.ll[2], b.half[2], b.pd[2]);
+    const float y = rsqrtf(fmaf(sx, sx, fmaf(sy, sy, sz * sz)));
+    const float dk = (float)(c & ((1u << kDkBits) - 1)) * kDkInv;
+    const float P = fmaf(dk, e.y, e.x);
+    const float B = fmaf(dk, e.w, e.z);
+    const float ft = fmaf(P, y, B * (di + dj)) * y;
+    fx = fmaf(ft, sx, fx);
+    fy = fmaf(ft, sy, fy);
+    fz = fmaf(ft, sz, fz);
+}
 
-// Single-kind force loop with every load of a batch issued before any of its arithmetic: the
-// handed-over pair terms and list entries one iteration ahead, then the UNR neighbour records
-// {position, F'(rho)} of the batch (slots past KVOIS read atom i itself with zero pair terms).
+// Single-kind force loop over the ELL list of atom i with every load of a batch issued
+// before any of its arithmetic: list slots one iteration ahead, then for all UNR slots the
+// neighbour position with its F'(rho) (one 32 B record) and the table row.  Slots beyond RU (kSkip) and past
+// KVOIS gather row 0 / atom i itself, which are always valid addresses, and are then not
+// accumulated.  The loads are thereby unconditional and overlap, instead of one dependent
+// gather chain per slot.
 template <int UNR>
-__device__ __forceinline__ void force_loop_batched(const DevAtoms &a, int i, const PosFF &pi, float di,
-                                                   const BoxF &b, float &fx, float &fy, float &fz)
+__device__ __forceinline__ void force_loop_batched(const DevAtoms &a, const DevTables &t, int i, const PosFF &pi,
+                                                   float di, const BoxF &b, float &fx, float &fy, float &fz)
 {
     const int *__restrict__ nb = a.indi + i;
-    const float2 *__restrict__ pb = a.pb + i;
+    const unsigned *__restrict__ pk = a.pk + i;
     const size_t ld = (size_t)a.ld;
     const int kn = a.kvois[i];
-    const float2 zero = make_float2(0.0f, 0.0f);
-    float2 cn[UNR];
+    unsigned cn[UNR];
     int jn[UNR];
 #pragma unroll
     for (int u = 0; u < UNR; ++u) {
-        cn[u] = u < kn ? __ldg(pb + u * ld) : zero;
+        cn[u] = u < kn ? __ldg(pk + u * ld) : kSkip;
         jn[u] = u < kn ? __ldg(nb + u * ld) : i;
     }
     for (int w = 0; w < kn; w += UNR) {
-        float2 c[UNR];
+        unsigned c[UNR];
         int j[UNR];
 #pragma unroll
         for (int u = 0; u < UNR; ++u) {
@@ -398,42 +379,20 @@ __device__ __forceinline__ void force_loop_batched(const DevAtoms &a, int i, con
 #pragma unroll
         for (int u = 0; u < UNR; ++u) {
             const int sl = w + UNR + u;
-            cn[u] = sl < kn ? __ldg(pb + sl * ld) : zero;
+            cn[u] = sl < kn ? __ldg(pk + sl * ld) : kSkip;
             jn[u] = sl < kn ? __ldg(nb + sl * ld) : i;
         }
         PosFF pj[UNR];
+        float4 e[UNR];
 #pragma unroll
-        for (int u = 0; u < UNR; ++u) pj[u] = ld_ff(a.rec + j[u]);
+        for (int u = 0; u < UNR; ++u) {
+            const unsigned row = c[u] == kSkip ? 0u : (c[u] >> kDkBits);
+            pj[u] = ld_ff(a.rec + j[u]);
+            e[u] = __ldg(t.force4 + row);
+        }
 #pragma unroll
         for (int u = 0; u < UNR; ++u)
-            if (j[u] != i) force_pair_pb(pi, pj[u], c[u], di, b, fx, fy, fz);
-    }
-}
-
-// F_i of one atom of the mixed force pass (PF: 0 plain, 1 list prefetch, 2 prefetch + batched
-// gathers; the last only with one table kind)
-template <bool MULTI, int UNR, int PF>
-__device__ __forceinline__ void force_atom32(const DevAtoms &a, const DevTables &t, int i, float &fx, float &fy,
-                                             float &fz)
-{
-    const BoxF b = load_boxf(a.box[a.boxid[i]]);
-    const PosFF pi = ld_ff(a.rec + i);
-    const float di = pi.d;
-    if (MULTI) {
-        const int ti = a.ityp[i] - 1;
-        walk_pairs<UNR, (PF != 0)>(a.indi + i, a.pk + i, (size_t)a.ld, a.kvois[i], kSkip, KeepIndex(),
-                                   [&](int j, unsigned c) {
-                                       const PosFF pj = ld_ff(a.rec + j);
-                                       force_pair_multi(pi, pj, c, di, pj.d, ti, a.ityp[j] - 1, b, t, fx, fy, fz);
-                                   });
-    } else if (PF == 2) {
-        force_loop_batched<UNR>(a, i, pi, di, b, fx, fy, fz);
-    } else {
-        walk_pairs<UNR, (PF != 0)>(a.indi + i, a.pb + i, (size_t)a.ld, a.kvois[i], make_float2(0.0f, 0.0f),
-                                   KeepTerms(), [&](int j, float2 v) {
-                                       const PosFF pj = ld_ff(a.rec + j);
-                                       force_pair_pb(pi, pj, v, di, b, fx, fy, fz);
-                                   });
+            if (c[u] != kSkip) force_pair_e(pi, pj[u], c[u], di, pj[u].d, e[u], b, fx, fy, fz);
     }
 }
 
@@ -443,15 +402,161 @@ __global__ void __launch_bounds__(kBlock, MINB) k_force32(DevAtoms a, DevTables 
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
     float fx = 0.0f, fy = 0.0f, fz = 0.0f;
-    if ((a.statu[i] & MSMGB_STATU_ACTIVE) == MSMGB_STATU_ACTIVE) force_atom32<MULTI, UNR, PF>(a, t, i, fx, fy, fz);
+    if ((a.statu[i] & MSMGB_STATU_ACTIVE) == MSMGB_STATU_ACTIVE) {
+        const BoxF b = load_boxf(a.box[a.boxid[i]]);
+        const PosFF pi = ld_ff(a.rec + i);
+        const int ti = MULTI ? a.ityp[i] - 1 : 0;
+        const float di = pi.d;
+        if (PF == 2 && !MULTI) {
+            force_loop_batched<UNR>(a, t, i, pi, di, b, fx, fy, fz);
+        } else {
+            walk_pairs<UNR, (PF != 0)>(a.indi + i, a.pk + i, (size_t)a.ld, a.kvois[i], [&](int j, unsigned c) {
+                const PosFF pj = ld_ff(a.rec + j);
+                force_pair<MULTI>(pi, pj, c, di, pj.d, ti, MULTI ? a.ityp[j] - 1 : 0, b, t, fx, fy, fz);
+            });
+        }
+    }
     a.fx[i] = (double)fx;
     a.fy[i] = (double)fy;
     a.fz[i] = (double)fz;
 }
 
-// The mixed MD step kernel (one table kind): force pass, then the corrector of step n and the
-// predictor of step n+1 of the same atom (vv_atom), positions of step n+1 into the second
-// buffer (neighbours still read step n's records).
+// ---- persistent variants with the used table range in shared memory -----------------
+// One block per SM slot (grid = resident blocks x SMs), grid-stride over the atoms.  The
+// last `cnt` rows of the single-kind table (the short-distance end is rarely reached) are
+// copied to shared memory once per block, so the divergent per-lane table reads of a warp
+// hit shared memory banks instead of distinct L1 lines; rows below `kmin` fall back to the
+// global table.
+template <int POT, int UNR>
+__global__ void __launch_bounds__(kBlock) k_density32s(DevAtoms a, DevTables t, int kmin, int cnt)
+{
+    extern __shared__ float2 sdens[];
+    for (int k = threadIdx.x; k < cnt; k += blockDim.x) sdens[k] = t.dens2[kmin + k];
+    __syncthreads();
+    const size_t ld = (size_t)a.ld;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += gridDim.x * blockDim.x) {
+        const int kn = a.kvois[i];
+        unsigned *__restrict__ pk = a.pk + i;
+        if ((a.statu[i] & MSMGB_STATU_ACTIVE) != MSMGB_STATU_ACTIVE) {
+            a.den32[i] = 0.0f;
+            st_ff(a.rec + i, ld_ff(a.posff + i));
+            continue;
+        }
+        const BoxF b = load_boxf(a.box[a.boxid[i]]);
+        const float rej = t.ru2h + 4.0f * sqrtf(t.ru2h) * b.dlmax + 1e-5f * t.ru2h;
+        const PosFF pi = ld_ff(a.posff + i);
+        const int *__restrict__ nb = a.indi + i;
+        float rho = 0.0f;
+        int w = 0;
+        for (; w + UNR <= kn; w += UNR) {
+            int j[UNR];
+            PosFF p[UNR];
+#pragma unroll
+            for (int u = 0; u < UNR; ++u) j[u] = __ldg(nb + (w + u) * ld);
+#pragma unroll
+            for (int u = 0; u < UNR; ++u) p[u] = ld_ff(a.posff + j[u]);
+#pragma unroll
+            for (int u = 0; u < UNR; ++u) {
+                float dk;
+                int kk;
+                const unsigned c = pair_index(pi, p[u], b, t, rej, dk, kk);
+                pk[(w + u) * ld] = c;
+                if (c != kSkip) {
+                    const float2 e = kk >= kmin ? sdens[kk - kmin] : __ldg(t.dens2 + kk);
+                    rho += fmaf(dk, e.y, e.x);
+                }
+            }
+        }
+        for (; w < kn; ++w) {
+            const int j0 = __ldg(nb + w * ld);
+            const PosFF p0 = ld_ff(a.posff + j0);
+            float dk;
+            int kk;
+            const unsigned c = pair_index(pi, p0, b, t, rej, dk, kk);
+            pk[w * ld] = c;
+            if (c != kSkip) {
+                const float2 e = kk >= kmin ? sdens[kk - kmin] : __ldg(t.dens2 + kk);
+                rho += fmaf(dk, e.y, e.x);
+            }
+        }
+        float d = rho;
+        if (POT == MSMGB_FS_TYPE) {
+            if (rho > 0.0f) d = -0.5f * rsqrtf(rho);
+        } else if (rho > 0.0f) {
+            const float sk = rho / t.rhodf + 1.0f;
+            int kk = (int)(sk + 0.000001f);
+            if (kk + 1 > t.nembd) {
+                atomicOr(&a.flags[kFlagErr], kErrRho);
+                kk = t.nembd;
+            }
+            const float2 e = __ldg(t.embd2 + kk);
+            d = fmaf(sk - (float)kk, e.y, e.x);
+        }
+        a.den32[i] = d;
+        PosFF r = pi;
+        r.d = d;
+        st_ff(a.rec + i, r);
+    }
+}
+
+template <int UNR>
+__global__ void __launch_bounds__(kBlock) k_force32s(DevAtoms a, DevTables t, int kmin, int cnt)
+{
+    extern __shared__ float4 sforce[];
+    for (int k = threadIdx.x; k < cnt; k += blockDim.x) sforce[k] = t.force4[kmin + k];
+    __syncthreads();
+    const size_t ld = (size_t)a.ld;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += gridDim.x * blockDim.x) {
+        float fx = 0.0f, fy = 0.0f, fz = 0.0f;
+        if ((a.statu[i] & MSMGB_STATU_ACTIVE) == MSMGB_STATU_ACTIVE) {
+            const BoxF b = load_boxf(a.box[a.boxid[i]]);
+            const PosFF pi = ld_ff(a.rec + i);
+            const float di = pi.d;
+            const int kn = a.kvois[i];
+            const int *__restrict__ nb = a.indi + i;
+            const unsigned *__restrict__ pk = a.pk + i;
+            for (int w = 0; w < kn; w += UNR) {
+                unsigned c[UNR];
+                int j[UNR];
+#pragma unroll
+                for (int u = 0; u < UNR; ++u) {
+                    c[u] = (w + u < kn) ? __ldg(pk + (w + u) * ld) : kSkip;
+                    j[u] = (w + u < kn) ? __ldg(nb + (w + u) * ld) : 0;
+                }
+#pragma unroll
+                for (int u = 0; u < UNR; ++u) {
+                    if (c[u] == kSkip) continue;
+                    const PosFF pj = ld_ff(a.rec + j[u]);
+                    const float dj = pj.d;
+                    const float sx = sep1(pi.hx, pi.lx, pj.hx, pj.lx, b.lh[0], b.ll[0], b.half[0], b.pd[0]);
+                    const float sy = sep1(pi.hy, pi.ly, pj.hy, pj.ly, b.lh[1], b.ll[1], b.half[1], b.pd[1]);
+                    const float sz = sep1(pi.hz, pi.lz, pj.hz, pj.lz, b.lh[2], b.ll[2], b.half[2], b.pd[2]);
+                    const float y = rsqrtf(fmaf(sx, sx, fmaf(sy, sy, sz * sz)));
+                    const int kk = (int)(c[u] >> kDkBits);
+                    const float dk = (float)(c[u] & ((1u << kDkBits) - 1)) * kDkInv;
+                    const float4 e = kk >= kmin ? sforce[kk - kmin] : __ldg(t.force4 + kk);
+                    const float P = fmaf(dk, e.y, e.x);
+                    const float B = fmaf(dk, e.w, e.z);
+                    const float ft = fmaf(P, y, B * (di + dj)) * y;
+                    fx = fmaf(ft, sx, fx);
+                    fy = fmaf(ft, sy, fy);
+                    fz = fmaf(ft, sz, fz);
+                }
+            }
+        }
+        a.fx[i] = (double)fx;
+        a.fy[i] = (double)fy;
+        a.fz[i] = (double)fz;
+    }
+}
+
+// ---- fused force pass + integrator (mixed step) ---------------------------------------
+// The force pass of step n followed, per atom, by the corrector of step n and the predictor
+// of step n+1 (vv_atom): positions are read from a.pos / a.posff (neighbours of step n) and
+// written to a.pos_nxt / a.posff_nxt, so no thread overwrites a position another thread is
+// still gathering.  The integrator's FP64 work then runs on the FP64 pipe while other warps
+// of the same kernel keep the FP32 pipes busy, and one pass over x, v and F disappears.
+// Single species only (the multi-species mixed step keeps the separate integrator).
 template <int UNR, int MINB, int PF>
 __global__ void __launch_bounds__(kBlock, MINB) k_force32_vv(DevAtoms a, DevTables t, double th)
 {
@@ -460,15 +565,27 @@ __global__ void __launch_bounds__(kBlock, MINB) k_force32_vv(DevAtoms a, DevTabl
     if (i < a.n) {
         const int stat = a.statu[i];
         float fx = 0.0f, fy = 0.0f, fz = 0.0f;
-        const bool act = (stat & MSMGB_STATU_ACTIVE) == MSMGB_STATU_ACTIVE;
-        if (act) force_atom32<false, UNR, PF>(a, t, i, fx, fy, fz);
+        const DevBox &bb = a.box[a.boxid[i]];
+        if ((stat & MSMGB_STATU_ACTIVE) == MSMGB_STATU_ACTIVE) {
+            const BoxF b = load_boxf(bb);
+            const PosFF pi = ld_ff(a.rec + i);
+            const float di = pi.d;
+            if (PF == 2) {
+                force_loop_batched<UNR>(a, t, i, pi, di, b, fx, fy, fz);
+            } else {
+                walk_pairs<UNR, (PF != 0)>(a.indi + i, a.pk + i, (size_t)a.ld, a.kvois[i], [&](int j, unsigned c) {
+                    const PosFF pj = ld_ff(a.rec + j);
+                    force_pair<false>(pi, pj, c, di, pj.d, 0, 0, b, t, fx, fy, fz);
+                });
+            }
+        }
         const double Fx = (double)fx, Fy = (double)fy, Fz = (double)fz;
         a.fx[i] = Fx;
         a.fy[i] = Fy;
         a.fz[i] = Fz;
         const double4_32a p = a.pos[i];
-        if (act) {
-            dmax = vv_atom(a, i, stat, a.box[a.boxid[i]], th, true, Fx, Fy, Fz, p, a.pos_nxt, a.posff_nxt);
+        if ((stat & MSMGB_STATU_ACTIVE) == MSMGB_STATU_ACTIVE) {
+            dmax = vv_atom(a, i, stat, bb, th, true, Fx, Fy, Fz, p, a.pos_nxt, a.posff_nxt);
         } else {
             a.pos_nxt[i] = p;
             a.posff_nxt[i] = a.posff[i];
@@ -550,10 +667,40 @@ int autotune_fused(msmgb_ctx *c)
     return check_launch(c, "autotune fused");
 }
 
+
+
+// shared-memory table window of the persistent variants (rows [kmin, ntp))
+static void smem_window(const msmgb_ctx *c, int bytes_per_row, int *kmin, int *cnt)
+{
+    const int budget = 48 * 1024 / bytes_per_row;
+    *cnt = std::min(budget, c->tab.ntp);
+    *kmin = c->tab.ntp - *cnt;
+}
+
+static int persistent_grid(const void *kernel, int smem)
+{
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, kBlock, smem);
+    return std::max(1, per) * std::max(1, sms);
+}
+
 template <int POT, bool MULTI>
 static void dens_variant(msmgb_ctx *c, int unr)
 {
     const int g = nblk(c->n, kBlock);
+    if (!MULTI && (unr & 8)) {
+        int kmin, cnt;
+        smem_window(c, (int)sizeof(float2), &kmin, &cnt);
+        const int smem = cnt * (int)sizeof(float2);
+        if ((unr & 7) == 1) {
+            k_density32s<POT, 1><<<persistent_grid((const void *)k_density32s<POT, 1>, smem), kBlock, smem, c->stream>>>(c->a, c->tab, kmin, cnt);
+        } else {
+            k_density32s<POT, 2><<<persistent_grid((const void *)k_density32s<POT, 2>, smem), kBlock, smem, c->stream>>>(c->a, c->tab, kmin, cnt);
+        }
+        return;
+    }
     if (unr & 16) {
         switch (unr & 7) {
         case 4: k_density32<POT, MULTI, 4, 1, true><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
@@ -576,6 +723,17 @@ template <bool MULTI>
 static void force_variant(msmgb_ctx *c, int unr)
 {
     const int g = nblk(c->n, kBlock);
+    if (!MULTI && (unr & 8)) {
+        int kmin, cnt;
+        smem_window(c, (int)sizeof(float4), &kmin, &cnt);
+        const int smem = cnt * (int)sizeof(float4);
+        if ((unr & 7) == 1) {
+            k_force32s<1><<<persistent_grid((const void *)k_force32s<1>, smem), kBlock, smem, c->stream>>>(c->a, c->tab, kmin, cnt);
+        } else {
+            k_force32s<2><<<persistent_grid((const void *)k_force32s<2>, smem), kBlock, smem, c->stream>>>(c->a, c->tab, kmin, cnt);
+        }
+        return;
+    }
     if (!MULTI && (unr & 32)) {
         switch (unr & 7) {
         case 4: k_force32<MULTI, 4, 1, 2><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
@@ -605,8 +763,7 @@ static void force_variant(msmgb_ctx *c, int unr)
 
 int launch_density32(msmgb_ctx *c)
 {
-    if (!c->a.pk || !c->a.pb)
-        return set_err(c, MSMGB_ERR_ARG, "mixed passes need the pair buffers (set MIXED precision)");
+    if (!c->a.pk) return set_err(c, MSMGB_ERR_ARG, "mixed passes need the pair-index buffer (set MIXED precision)");
     if (c->tab.ntab >= (1 << (32 - kDkBits)) - 1)
         return set_err(c, MSMGB_ERR_ARG, "mixed passes support NTAB < 16383");
     const bool multi = c->tab.ngroup > 1;
@@ -638,12 +795,13 @@ int autotune_mixed(msmgb_ctx *c)
 {
     // code & 7: 1, 2, 4 = neighbours in flight per thread; 3 = 2 and 5 = 4 with registers
     // capped for 6 blocks (75% occupancy); +16: list slots loaded one iteration ahead;
-    // +32 (force, single kind): and all gathers of a batch before its arithmetic
+    // +32 (force, single kind): and all gathers of a batch before its arithmetic;
+    // +8: persistent grid with the table in shared memory (single kind only)
     const bool single = c->tab.ngroup == 1;
-    const int dcands[9] = {1, 2, 4, 3, 5, 18, 20, 19, 21};
-    const int fcands[13] = {1, 2, 4, 3, 5, 18, 20, 19, 21, 50, 52, 51, 53};
+    const int dcands[11] = {1, 2, 4, 3, 5, 18, 20, 19, 21, 9, 10};
+    const int fcands[15] = {1, 2, 4, 3, 5, 18, 20, 19, 21, 50, 52, 51, 53, 9, 10};
     const int *cands = dcands;
-    int ncand = 9;
+    int ncand = single ? 11 : 9;
     cudaEvent_t e0, e1;
     cudaError_t err = cudaEventCreate(&e0);
     if (err == cudaSuccess) err = cudaEventCreate(&e1);
@@ -667,7 +825,7 @@ int autotune_mixed(msmgb_ctx *c)
     int rc = launch_density32(c);
     if (rc) return rc;
     cands = fcands;
-    ncand = single ? 13 : 9;
+    ncand = single ? 15 : 9;
     for (int k = 0; k < ncand; ++k) {
         c->tune_force_unroll = cands[k];
         for (int r = 0; r < 4; ++r) {

@@ -89,7 +89,6 @@ struct DevTables {
     // mixed-precision tables: value and slope to the next grid point, interleaved
     const float2 *dens2;           // [nkind][ntp] {POTB(k), POTB(k+1)-POTB(k)}
     const float4 *force4;          // [nkind][ntp] {FPOTR, dFPOTR, FPOTB, dFPOTB}
-    const float4 *comb;            // kind 0, [ntp][2] {POTB, dPOTB, FPOTR, dFPOTR}, {FPOTB, dFPOTB, 0, 0}
     const float2 *embd2;           // [nkind1][nep] {DFEMBD, dDFEMBD}
     // float-float tables: {value hi, lo, slope hi, lo} (slope to the next grid point in FP64)
     const float4 *densff;          // [nkind][ntp] POTB
@@ -129,7 +128,6 @@ struct DevAtoms {
     const double *icm;   // reciprocal masses per type
     unsigned *pk;        // mixed passes: per-pair table index (KK << 18 | DK * 2^18), ELL layout
     PosFF *rec;          // mixed passes: {position, F'(rho)} records written by the density pass
-    float2 *pb;          // mixed passes, one table kind: pair terms {FPOTR(r), FPOTB(r)}, ELL layout
     PosFX *posfx;        // float-float passes: positions (k_fix) ...
     PosFX *recfx;        // ... and {position, F'(rho)} records written by the density pass
     int *flags;
