@@ -845,23 +845,101 @@ extern "C" int msmgb_correction(msmgb_ctx *c, double h)
     return poll_flags(c);
 }
 
+// ---- step graphs with a conditional rebuild ---------------------------------------------
+// A step graph is captured into a graph that owns an IF node: k_decide sets its condition on
+// the device, and the node's body holds the list rebuild, so a step without a rebuild runs
+// none of the rebuild kernels.
+static int begin_step_capture(msmgb_ctx *c, cudaGraph_t *g, cudaGraphConditionalHandle *cond)
+{
+    *g = nullptr;
+    CK(cudaGraphCreate(g, 0), "graph create");
+    cudaError_t e = cudaGraphConditionalHandleCreate(cond, *g, 0, cudaGraphCondAssignDefault);
+    if (e == cudaSuccess)
+        e = cudaStreamBeginCaptureToGraph(c->stream, *g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) {
+        cudaGraphDestroy(*g);
+        *g = nullptr;
+        return cuda_err(c, e, "graph capture");
+    }
+    return MSMGB_OK;
+}
+
+// IF node at the current position of the capture; its body graph is returned for later filling
+static int add_rebuild_node(msmgb_ctx *c, cudaGraphConditionalHandle cond, cudaGraph_t *body)
+{
+    cudaStreamCaptureStatus st;
+    unsigned long long id = 0;
+    cudaGraph_t cg = nullptr;
+    const cudaGraphNode_t *deps = nullptr;
+    const cudaGraphEdgeData *edges = nullptr;
+    size_t nd = 0;
+    CK(cudaStreamGetCaptureInfo(c->stream, &st, &id, &cg, &deps, &edges, &nd), "capture info");
+    cudaGraphNodeParams p = {};
+    p.type = cudaGraphNodeTypeConditional;
+    p.conditional.handle = cond;
+    p.conditional.type = cudaGraphCondTypeIf;
+    p.conditional.size = 1;
+    cudaGraphNode_t node;
+    CK(cudaGraphAddNode(&node, cg, deps, edges, nd, &p), "conditional node");
+    *body = p.conditional.phGraph_out[0];
+    CK(cudaStreamUpdateCaptureDependencies(c->stream, &node, nullptr, 1, cudaStreamSetCaptureDependencies),
+       "capture dependencies");
+    return MSMGB_OK;
+}
+
+// the rebuild of the current atom view c->a into a conditional body (kernels counted apart)
+static int fill_rebuild_body(msmgb_ctx *c, cudaGraph_t body)
+{
+    CK(cudaStreamBeginCaptureToGraph(c->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal),
+       "graph capture");
+    const int64_t l0 = c->launches;
+    const int rc = build_list(c, false);
+    cudaGraph_t out = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(c->stream, &out);
+    c->gk_body = c->launches - l0;
+    c->launches = l0;
+    if (rc) return rc;
+    if (e != cudaSuccess) return cuda_err(c, e, "graph capture");
+    return MSMGB_OK;
+}
+
+static int finish_step_graph(msmgb_ctx *c, int rc, cudaGraph_t g, cudaGraph_t body, cudaGraphExec_t *out,
+                             const DevAtoms &body_view)
+{
+    cudaGraph_t ended = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(c->stream, &ended);
+    if (!rc && e != cudaSuccess) rc = cuda_err(c, e, "graph capture");
+    if (!rc && body) {
+        const DevAtoms keep = c->a;
+        c->a = body_view;
+        rc = fill_rebuild_body(c, body);
+        c->a = keep;
+    }
+    if (!rc) {
+        const cudaError_t ie = cudaGraphInstantiate(out, g, 0);
+        if (ie != cudaSuccess) {
+            *out = nullptr;
+            rc = cuda_err(c, ie, "graph instantiate");
+        }
+    }
+    cudaGraphDestroy(g);
+    return rc;
+}
+
 static int capture_step(msmgb_ctx *c, double h)
 {
     free_graph(c);
-    cudaGraph_t g = nullptr;
-    CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "graph capture");
+    cudaGraph_t g = nullptr, body = nullptr;
+    cudaGraphConditionalHandle cond = 0;
+    RET(begin_step_capture(c, &g, &cond));
     int64_t l0 = c->launches;
     int rc = launch_vv(c, h, 1);
-    if (!rc) rc = launch_decide(c, c->p.skin_trigger, c->p.nb_uptab);
-    if (!rc) rc = build_list(c, true);
+    if (!rc) rc = launch_decide(c, c->p.skin_trigger, c->p.nb_uptab, cond, true);
+    if (!rc) rc = add_rebuild_node(c, cond, &body);
     if (!rc) rc = force_passes(c, false, false);
-    cudaError_t e = cudaStreamEndCapture(c->stream, &g);
-    if (rc) { if (g) cudaGraphDestroy(g); return rc; }
-    if (e != cudaSuccess) return cuda_err(c, e, "graph capture");
-    e = cudaGraphInstantiate(&c->step_graph, g, 0);
-    cudaGraphDestroy(g);
-    if (e != cudaSuccess) { c->step_graph = nullptr; return cuda_err(c, e, "graph instantiate"); }
-    c->graph_kernels = c->launches - l0;
+    const int64_t nk = c->launches - l0;
+    RET(finish_step_graph(c, rc, g, body, &c->step_graph, c->a));
+    c->graph_kernels = nk;
     c->launches = l0;
     c->graph_h = h;
     c->graph_prec = c->p.precision;
@@ -938,26 +1016,33 @@ static int capture_fused(msmgb_ctx *c, double h)
     }
     const int64_t l_start = c->launches;
     int64_t l0 = c->launches;
-    CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "graph capture");
-    c->a = atoms_on(c, base, 0);
-    rc = launch_vv(c, h, 0);
-    if (!rc) rc = launch_decide(c, c->p.skin_trigger, c->p.nb_uptab);
-    if (!rc) rc = build_list(c, true);
-    c->a = base;
-    RET(end_capture(c, rc, &c->g_pre));
-    c->gk_pre = c->launches - l0;
+    {
+        cudaGraph_t g = nullptr, body = nullptr;
+        cudaGraphConditionalHandle cond = 0;
+        RET(begin_step_capture(c, &g, &cond));
+        c->a = atoms_on(c, base, 0);
+        rc = launch_vv(c, h, 0);
+        if (!rc) rc = launch_decide(c, c->p.skin_trigger, c->p.nb_uptab, cond, true);
+        if (!rc) rc = add_rebuild_node(c, cond, &body);
+        c->gk_pre = c->launches - l0;
+        rc = finish_step_graph(c, rc, g, body, &c->g_pre, atoms_on(c, base, 0));
+        c->a = base;
+        RET(rc);
+    }
     for (int p = 0; p < 2; ++p) {
         l0 = c->launches;
-        CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "graph capture");
+        cudaGraph_t g = nullptr, body = nullptr;
+        cudaGraphConditionalHandle cond = 0;
+        RET(begin_step_capture(c, &g, &cond));
         c->a = atoms_on(c, base, p);
         rc = step_density(c);
         if (!rc) rc = step_force_vv(c, h);
-        if (!rc) rc = launch_decide(c, c->p.skin_trigger, c->p.nb_uptab);
-        c->a = atoms_on(c, base, 1 - p);
-        if (!rc) rc = build_list(c, true);
-        c->a = base;
-        RET(end_capture(c, rc, &c->g_loop[p]));
+        if (!rc) rc = launch_decide(c, c->p.skin_trigger, c->p.nb_uptab, cond, true);
+        if (!rc) rc = add_rebuild_node(c, cond, &body);
         c->gk_loop = c->launches - l0;
+        rc = finish_step_graph(c, rc, g, body, &c->g_loop[p], atoms_on(c, base, 1 - p));
+        c->a = base;
+        RET(rc);
         l0 = c->launches;
         CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "graph capture");
         c->a = atoms_on(c, base, p);
@@ -1035,6 +1120,8 @@ extern "C" int msmgb_run_steps(msmgb_ctx *c, int nsteps, double h, int *rebuilds
     RET(launch_correct(c, h, true));          // no-op unless the last step left a pending half-kick
     int rc = poll_flags(c);
     if (rebuilds) *rebuilds = c->h_flags[kFlagRebuilds];
+    c->launches += (int64_t)c->h_flags[kFlagRebuilds] * c->gk_body;   // conditional rebuild bodies run
+    CK(cudaMemsetAsync(c->flags + kFlagRebuilds, 0, sizeof(int), c->stream), "flag clear");
     return rc;
 }
 
@@ -1060,6 +1147,7 @@ extern "C" int msmgb_finish_steps(msmgb_ctx *c, double h, int *rebuilds)
     RET(launch_correct(c, h, true));
     int rc = poll_flags(c);
     if (rebuilds) *rebuilds = c->h_flags[kFlagRebuilds];
+    c->launches += (int64_t)c->h_flags[kFlagRebuilds] * c->gk_body;   // conditional rebuild bodies run
     CK(cudaMemsetAsync(c->flags + kFlagRebuilds, 0, sizeof(int), c->stream), "flag clear");
     return rc;
 }

@@ -313,6 +313,7 @@ struct msmgb_ctx {
     msmgb::PosFF *posff2 = nullptr;
     cudaGraphExec_t g_pre = nullptr, g_loop[2] = {nullptr, nullptr}, g_final[2] = {nullptr, nullptr};
     int64_t gk_pre = 0, gk_loop = 0, gk_final = 0;
+    int64_t gk_body = 0;         // kernels of the conditional rebuild body of a step graph
     double fg_h = 0.0;
     int fg_n = -1, fg_tune = -1, fg_prec = -1;
 
@@ -354,6 +355,7 @@ int launch_adjoint(msmgb_ctx *c, const double *ft, const double *dtab, double *w
 // integrator (vv.cu)
 int launch_vv(msmgb_ctx *c, double h, int mode);   // mode 0: predictor; 1: fused; 2: fused if pending
 int launch_correct(msmgb_ctx *c, double h, bool only_if_pending);
-int launch_decide(msmgb_ctx *c, double skin_trigger, int nb_uptab);
+int launch_decide(msmgb_ctx *c, double skin_trigger, int nb_uptab, cudaGraphConditionalHandle cond = 0,
+                  bool use_cond = false);
 
 }  // namespace msmgb

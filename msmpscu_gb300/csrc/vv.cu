@@ -11,7 +11,8 @@
 //              the fused mixed force kernel.
 //   k_correct  Correction_KERNEL alone (end of a run, or msmgb_correction()).
 //   k_decide   one thread: rebuild flag for this step from the skin trigger (or the
-//              reference's fixed NB_UPTAB interval, MD_Method_GenericMD_GPU.F90:599-601).
+//              reference's fixed NB_UPTAB interval, MD_Method_GenericMD_GPU.F90:599-601);
+//              in a step graph it also sets the conditional node that runs the rebuild.
 #include "msmgb_internal.cuh"
 
 namespace msmgb {
@@ -50,7 +51,9 @@ __global__ void __launch_bounds__(kBlock) k_correct(DevAtoms a, double th, int o
 
 __global__ void k_clear_pending(int *flags) { flags[kFlagPending] = 0; }
 
-__global__ void k_decide(int *flags, unsigned long long *maxdisp, double thr2, int nb_uptab)
+// Inside a step graph the decision also switches the graph's conditional rebuild node.
+__global__ void k_decide(int *flags, unsigned long long *maxdisp, double thr2, int nb_uptab,
+                         cudaGraphConditionalHandle cond, int use_cond)
 {
     int rebuild = 0;
     if (thr2 > 0.0) {
@@ -61,6 +64,7 @@ __global__ void k_decide(int *flags, unsigned long long *maxdisp, double thr2, i
     }
     flags[kFlagRebuild] = rebuild;
     if (rebuild) flags[kFlagRebuilds] += 1;
+    if (use_cond) cudaGraphSetConditional(cond, rebuild ? 1u : 0u);
     *maxdisp = 0ull;
     flags[kFlagPending] = 1;
 }
@@ -84,10 +88,10 @@ int launch_correct(msmgb_ctx *c, double h, bool only_if_pending)
     return check_launch(c, "corrector");
 }
 
-int launch_decide(msmgb_ctx *c, double skin_trigger, int nb_uptab)
+int launch_decide(msmgb_ctx *c, double skin_trigger, int nb_uptab, cudaGraphConditionalHandle cond, bool use_cond)
 {
     double thr2 = skin_trigger > 0.0 ? skin_trigger * skin_trigger : 0.0;
-    k_decide<<<1, 1, 0, c->stream>>>(c->a.flags, c->a.maxdisp, thr2, nb_uptab);
+    k_decide<<<1, 1, 0, c->stream>>>(c->a.flags, c->a.maxdisp, thr2, nb_uptab, cond, use_cond ? 1 : 0);
     c->launches += 1;
     return check_launch(c, "rebuild decision");
 }
