@@ -692,7 +692,7 @@ extern "C" int msmgb_cal_neighborelist(msmgb_ctx *c)
     RET(need_state(c));
     RET(use_device(c));
     CK(cudaMemsetAsync(c->flags + kFlagMaxK, 0, sizeof(int), c->stream), "flag clear");
-    RET(build_list(c, false));
+    RET(build_list(c));
     CK(cudaMemsetAsync(c->maxdisp, 0, sizeof(unsigned long long), c->stream), "flag clear");
     RET(poll_flags(c));
     c->list_valid = true;
@@ -737,7 +737,7 @@ static int ready_for_force(msmgb_ctx *c)
     RET(use_device(c));
     if (!c->list_valid) {
         CK(cudaMemsetAsync(c->flags + kFlagMaxK, 0, sizeof(int), c->stream), "flag clear");
-        RET(build_list(c, false));
+        RET(build_list(c));
         CK(cudaMemsetAsync(c->maxdisp, 0, sizeof(unsigned long long), c->stream), "flag clear");
         c->list_valid = true;
     }
@@ -893,7 +893,7 @@ static int fill_rebuild_body(msmgb_ctx *c, cudaGraph_t body)
     CK(cudaStreamBeginCaptureToGraph(c->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal),
        "graph capture");
     const int64_t l0 = c->launches;
-    const int rc = build_list(c, false);
+    const int rc = build_list(c);
     cudaGraph_t out = nullptr;
     const cudaError_t e = cudaStreamEndCapture(c->stream, &out);
     c->gk_body = c->launches - l0;
@@ -1281,7 +1281,7 @@ extern "C" int msmgb_time_passes(msmgb_ctx *c, int reps, float *out)
             int rc = MSMGB_OK;
             if (which == 0) rc = mixed ? launch_density32(c) : (ffp ? launch_density_ff(c) : launch_density(c, false));
             else if (which == 1) rc = mixed ? launch_force32(c) : (ffp ? launch_force_ff(c) : launch_force(c, false));
-            else if (which == 2) rc = build_list(c, false);
+            else if (which == 2) rc = build_list(c);
             else if (which == 3) rc = launch_vv(c, 0.0, 2);
             else {
                 const DevAtoms base = c->a;

@@ -334,7 +334,7 @@ int set_err(msmgb_ctx *c, int code, const std::string &msg);
 int cuda_err(msmgb_ctx *c, cudaError_t e, const char *what);
 
 // neighbour list (nlist.cu)
-int build_list(msmgb_ctx *c, bool predicated);
+int build_list(msmgb_ctx *c);
 
 // force passes (force64.cu / force32.cu)
 int launch_density(msmgb_ctx *c, bool want_epot);

@@ -14,8 +14,8 @@
 //               distance test decides every pair outside a narrow band around the cutoff,
 //               pairs inside the band get the exact FP64 rule d^2 < rc^2
 //               (MD_NeighborsList.F90:605), so the sets equal the FP64 oracle's.
-// Every kernel can be predicated on flags[kFlagRebuild] so the whole rebuild sits inside
-// the captured MD-step graph and costs a few empty launches when the trigger is off.
+// In an MD-step graph the rebuild is the body of a conditional node that the step's
+// decision kernel switches on (context.cu), so steps without a rebuild launch none of these.
 #include "msmgb_internal.cuh"
 
 namespace msmgb {
@@ -24,21 +24,14 @@ __constant__ int c_nix[27] = {0, -1, -1, -1, 0, 0, -1, 1, -1, 0, 1, -1, 0, 1, 1,
 __constant__ int c_niy[27] = {0, 0, -1, 1, 1, 0, 0, 0, -1, -1, -1, 1, 1, 1, 0, 1, -1, -1, 0, 0, 0, -1, -1, -1, 1, 1, 1};
 __constant__ int c_niz[27] = {0, 0, 0, 0, 0, 1, 1, 1, 1, 1, 1, 1, 1, 1, 0, 0, 0, 0, -1, -1, -1, -1, -1, -1, -1, -1, -1};
 
-__device__ __forceinline__ bool skip_rebuild(const int *flags, int predicated)
+__global__ void k_zero_int(int *p, int n)
 {
-    return predicated && flags[kFlagRebuild] == 0;
-}
-
-__global__ void k_zero_int(int *p, int n, const int *flags, int predicated)
-{
-    if (skip_rebuild(flags, predicated)) return;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) p[i] = 0;
 }
 
 // cell index per atom: int((x - lo)/L * NC - 1e-4), MD_NeighborsList_GPU.F90:800-811
-__global__ void k_bin(DevAtoms a, int sentinel, int *cell_of, int *count, int predicated)
+__global__ void k_bin(DevAtoms a, int sentinel, int *cell_of, int *count)
 {
-    if (skip_rebuild(a.flags, predicated)) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
     int st = a.statu[i];
@@ -98,10 +91,8 @@ __device__ __forceinline__ int block_exclusive_scan(int v, int *total)
     return excl;
 }
 
-__global__ void __launch_bounds__(kScanThreads) k_scan_tile(const int *in, int *out, int n, int *sums,
-                                                            const int *flags, int predicated)
+__global__ void __launch_bounds__(kScanThreads) k_scan_tile(const int *in, int *out, int n, int *sums)
 {
-    if (skip_rebuild(flags, predicated)) return;
     int base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
     int v[kScanItems];
     int s = 0;
@@ -120,10 +111,8 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_tile(const int *in, int *
     if (threadIdx.x == 0 && sums) sums[blockIdx.x] = total;
 }
 
-__global__ void __launch_bounds__(kScanThreads) k_scan_add(int *out, int n, const int *sums,
-                                                           const int *flags, int predicated)
+__global__ void __launch_bounds__(kScanThreads) k_scan_add(int *out, int n, const int *sums)
 {
-    if (skip_rebuild(flags, predicated)) return;
     if (blockIdx.x == 0) return;
     int add = sums[blockIdx.x];
     int base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
@@ -133,10 +122,8 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_add(int *out, int n, cons
 }
 
 // ---- counting-sort scatter and deterministic per-cell order --------------------------
-__global__ void k_scatter(DevAtoms a, const int *cell_of, const int *start, int *cursor, int *perm,
-                          int predicated)
+__global__ void k_scatter(DevAtoms a, const int *cell_of, const int *start, int *cursor, int *perm)
 {
-    if (skip_rebuild(a.flags, predicated)) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
     int c = cell_of[i];
@@ -144,9 +131,8 @@ __global__ void k_scatter(DevAtoms a, const int *cell_of, const int *start, int 
     perm[slot] = i;
 }
 
-__global__ void k_cellsort(int ncs, const int *start, int *perm, const int *flags, int predicated)
+__global__ void k_cellsort(int ncs, const int *start, int *perm)
 {
-    if (skip_rebuild(flags, predicated)) return;
     int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= ncs) return;
     int b = start[c], e = start[c + 1];
@@ -184,9 +170,8 @@ __host__ __device__ inline Stage stage_of(void *scratch, int cap)
     return s;
 }
 
-__global__ void k_permute(DevAtoms a, Stage s, const int *perm, const int *cell_of, int predicated)
+__global__ void k_permute(DevAtoms a, Stage s, const int *perm, const int *cell_of)
 {
-    if (skip_rebuild(a.flags, predicated)) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
     int o = perm[i];
@@ -200,9 +185,8 @@ __global__ void k_permute(DevAtoms a, Stage s, const int *perm, const int *cell_
     s.cell[i] = cell_of[o];
 }
 
-__global__ void k_copyback(DevAtoms a, Stage s, int *cell_of, int predicated)
+__global__ void k_copyback(DevAtoms a, Stage s, int *cell_of)
 {
-    if (skip_rebuild(a.flags, predicated)) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
     double4_32a p = s.pos[i];
@@ -248,9 +232,8 @@ __device__ __forceinline__ bool accept(float d2f, float d2lo, float d2hi, const 
 // separation is the exact hi-part difference plus a per-cell shift of -L, 0 or +L, with no
 // per-candidate minimum-image test.  Narrow boxes take the minimum image per candidate.
 __global__ void __launch_bounds__(kBlock) k_build(DevAtoms a, const int *cell_of, const int *start,
-                                                  double rc2, float d2lo, float d2hi, int predicated)
+                                                  double rc2, float d2lo, float d2hi)
 {
-    if (skip_rebuild(a.flags, predicated)) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
     const PosFF pf = a.posff[i];
@@ -348,36 +331,35 @@ static void prefilter_band(const msmgb_ctx *c, double rc2, float *lo, float *hi)
     *hi = (float)(rc2 + m);
 }
 
-int build_list(msmgb_ctx *c, bool predicated)
+int build_list(msmgb_ctx *c)
 {
     const int n = c->n;
     const int ncs = c->ncell_total + 1;   // + sentinel cell for out-of-box atoms
-    const int pr = predicated ? 1 : 0;
     int *count = c->cell_cursor;          // histogram, then re-zeroed as scatter cursor
     cudaStream_t s = c->stream;
     DevAtoms a = c->a;
 
-    k_zero_int<<<nblk(ncs + 1, kBlock), kBlock, 0, s>>>(count, ncs + 1, a.flags, pr);
-    k_bin<<<nblk(n, kBlock), kBlock, 0, s>>>(a, c->ncell_total, c->cell_of, count, pr);
+    k_zero_int<<<nblk(ncs + 1, kBlock), kBlock, 0, s>>>(count, ncs + 1);
+    k_bin<<<nblk(n, kBlock), kBlock, 0, s>>>(a, c->ncell_total, c->cell_of, count);
     // exclusive scan over ncs + 1 entries: start[ncs] = n
     int ntile = nblk(ncs + 1, kScanTile);
-    k_scan_tile<<<ntile, kScanThreads, 0, s>>>(count, c->cell_start, ncs + 1, c->scan_tmp, a.flags, pr);
+    k_scan_tile<<<ntile, kScanThreads, 0, s>>>(count, c->cell_start, ncs + 1, c->scan_tmp);
     c->launches += 3;
     if (ntile > 1) {
-        k_scan_tile<<<1, kScanThreads, 0, s>>>(c->scan_tmp, c->scan_tmp, ntile, nullptr, a.flags, pr);
-        k_scan_add<<<ntile, kScanThreads, 0, s>>>(c->cell_start, ncs + 1, c->scan_tmp, a.flags, pr);
+        k_scan_tile<<<1, kScanThreads, 0, s>>>(c->scan_tmp, c->scan_tmp, ntile, nullptr);
+        k_scan_add<<<ntile, kScanThreads, 0, s>>>(c->cell_start, ncs + 1, c->scan_tmp);
         c->launches += 2;
     }
-    k_zero_int<<<nblk(ncs + 1, kBlock), kBlock, 0, s>>>(count, ncs + 1, a.flags, pr);
-    k_scatter<<<nblk(n, kBlock), kBlock, 0, s>>>(a, c->cell_of, c->cell_start, count, c->perm, pr);
-    k_cellsort<<<nblk(ncs, kBlock), kBlock, 0, s>>>(ncs, c->cell_start, c->perm, a.flags, pr);
+    k_zero_int<<<nblk(ncs + 1, kBlock), kBlock, 0, s>>>(count, ncs + 1);
+    k_scatter<<<nblk(n, kBlock), kBlock, 0, s>>>(a, c->cell_of, c->cell_start, count, c->perm);
+    k_cellsort<<<nblk(ncs, kBlock), kBlock, 0, s>>>(ncs, c->cell_start, c->perm);
     Stage st = stage_of(c->scratch, c->cap_atoms);
-    k_permute<<<nblk(n, kBlock), kBlock, 0, s>>>(a, st, c->perm, c->cell_of, pr);
-    k_copyback<<<nblk(n, kBlock), kBlock, 0, s>>>(a, st, c->cell_of, pr);
+    k_permute<<<nblk(n, kBlock), kBlock, 0, s>>>(a, st, c->perm, c->cell_of);
+    k_copyback<<<nblk(n, kBlock), kBlock, 0, s>>>(a, st, c->cell_of);
     double rc2 = c->p.rc_nl * c->p.rc_nl;
     float d2lo, d2hi;
     prefilter_band(c, rc2, &d2lo, &d2hi);
-    k_build<<<nblk(n, kBlock), kBlock, 0, s>>>(a, c->cell_of, c->cell_start, rc2, d2lo, d2hi, pr);
+    k_build<<<nblk(n, kBlock), kBlock, 0, s>>>(a, c->cell_of, c->cell_start, rc2, d2lo, d2hi);
     c->launches += 6;
     return check_launch(c, "neighbour list");
 }
