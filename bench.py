@@ -121,6 +121,13 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def workload_config(ncell, n):
+    """The workload entry of `config`, identical in both arms."""
+    return {"workload": "fcc Cu %dx%dx%d cells, %d atoms, Cleri-Rosato, sigma 0.05 A, 600 K, NVE dt=1fs, "
+                        "skin 0.3 A (rebuild at 0.15 A)" % (ncell, ncell, ncell, n),
+            "atoms": n}
+
+
 def workload(ncell=NCELL):
     from msmpscu_gb300 import lattice as lt
     pos, vel, L = lt.cu_config(ncell, SIGMA, TEMP, SEED)
@@ -338,7 +345,7 @@ def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
         return
-    pos, vel, L = workload()
+    pos, vel, L = workload(args.ncell)
     n = len(pos)
     threads = os.cpu_count() or 1
     from msmpscu_gb300 import lattice as lt
@@ -377,11 +384,10 @@ def run_reference(args):
             "steps": done, "warmup": args.warmup, "ms_per_step": 1e3 * t_total / done,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded fcc Cu lattice)",
-            "config": {"workload": "fcc Cu 80x80x80 cells, 2,048,000 atoms, Cleri-Rosato, NVE dt=1fs, skin 0.3 A",
-                       "atoms": n, "parallelism": "replicas"},
+            "config": dict(workload_config(args.ncell, n), parallelism="host threads (OpenMP over atoms)"),
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": "%d of %d NVE steps of the full 2,048,000-atom system "
-                                       "(oracle, OpenMP over atoms)" % (done, args.steps)},
+                             "sample": "%d of %d NVE steps of the full %d-atom system "
+                                       "(oracle, OpenMP over atoms)" % (done, args.steps, n)},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -476,10 +482,7 @@ def run_ours(args):
                 "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64" if prec == "fp64" else "f32+f64",
                 "data": "synthetic (seeded fcc Cu lattice, Gaussian displacements, Maxwell-Boltzmann velocities)",
-                "config": {"workload": "fcc Cu %dx%dx%d cells, %d atoms, Cleri-Rosato, sigma 0.05 A, "
-                                       "600 K, NVE dt=1fs, skin 0.3 A (rebuild at 0.15 A)"
-                                       % (args.ncell, args.ncell, args.ncell, n),
-                           "atoms": n, "precision": prec, "parallelism": "replicas" if ws > 1 else "single GPU",
+                "config": {**workload_config(args.ncell, n), "precision": prec, "parallelism": "replicas" if ws > 1 else "single GPU",
                            "l2": "inputs larger than L2 (~0.9 GB touched per step)",
                            "rebuilds_in_timed_steps": rebuilds, "mean_neighbours": kmean,
                            "max_neighbours": kmax},
