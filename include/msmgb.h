@@ -35,6 +35,8 @@ extern "C" {
 #define MSMGB_ERR_BOX_TOO_SMALL -6   /* box edge < 2 * list cutoff (minimum image ambiguous)*/
 #define MSMGB_ERR_NO_DEVICE     -7   /* no CUDA device / extension unusable                */
 #define MSMGB_ERR_CAPACITY      -8   /* more atoms / boxes than the context was sized for  */
+#define MSMGB_ERR_TIMEOUT       -9   /* a bounded device-side wait ran out (asynchronous copy
+                                        not completed); the context stays usable            */
 
 /* ---- potential types (MDForceTable%PotType) ------------------------------------------- */
 #define MSMGB_FS_TYPE  0
@@ -202,6 +204,16 @@ int  msmgb_time_passes(msmgb_ctx *ctx, int reps, float *out);
  * time per launch.  Tuning runs at the first mixed force call / step graph for a given
  * atom count. */
 int  msmgb_get_tuning(const msmgb_ctx *ctx, int *out, float *ms);
+/* Pins the kernel variants of the mixed passes (codes as returned by msmgb_get_tuning:
+ * codes[0] density, codes[1] force, codes[2] fused step kernel; a negative code leaves that
+ * choice to the tuner).  Pinned choices are kept for the context's atom count and skip the
+ * tuning runs; the step graphs are recaptured.  No counterpart in the reference. */
+int  msmgb_set_tuning(msmgb_ctx *ctx, const int *codes);
+/* Failure-path self-test of the bounded device waits (the TMA-streamed step kernel's
+ * mbarrier waits give up after 0.5 s): runs one block that waits on a barrier nothing
+ * completes and returns MSMGB_ERR_TIMEOUT; the context stays usable.  No counterpart in the
+ * reference. */
+int  msmgb_selftest_wait(msmgb_ctx *ctx);
 /* Largest and mean neighbour count of the current list. */
 int  msmgb_list_stats(msmgb_ctx *ctx, int *maxk, double *meank);
 

@@ -8,7 +8,7 @@ LIB_PATH = os.path.join(HERE, "_build", "libmsmgb.so")
 
 OK = 0
 ERR_ARG, ERR_CUDA, ERR_NL_OVERFLOW, ERR_OUT_OF_BOX = -1, -2, -3, -4
-ERR_RHO_RANGE, ERR_BOX_TOO_SMALL, ERR_NO_DEVICE, ERR_CAPACITY = -5, -6, -7, -8
+ERR_RHO_RANGE, ERR_BOX_TOO_SMALL, ERR_NO_DEVICE, ERR_CAPACITY, ERR_TIMEOUT = -5, -6, -7, -8, -9
 FS_TYPE, EAM_TYPE = 0, 1
 PREC_FP64, PREC_MIXED, PREC_FF = 0, 1, 2
 PRECISIONS = {"fp64": PREC_FP64, "mixed": PREC_MIXED, "ff": PREC_FF}
@@ -89,6 +89,8 @@ SIGNATURES = [
     ("msmgb_time_passes", C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_float)]),
     ("msmgb_list_stats", C.c_int, [C.c_void_p, _ip, _dp]),
     ("msmgb_get_tuning", C.c_int, [C.c_void_p, _ip, C.POINTER(C.c_float)]),
+    ("msmgb_set_tuning", C.c_int, [C.c_void_p, _ip]),
+    ("msmgb_selftest_wait", C.c_int, [C.c_void_p]),
     ("msmgb_hvp", C.c_int, [C.c_void_p, _dp, _dp]),
     ("msmgb_time_hvp", C.c_int, [C.c_void_p, _dp, C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
     ("msmgb_param_adjoint", C.c_int, [C.c_void_p, C.c_int, _dp, _dp, _dp, _dp]),

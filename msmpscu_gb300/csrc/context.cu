@@ -185,7 +185,10 @@ extern "C" int msmgb_create(msmgb_ctx **out, const msmgb_params *p)
     const size_t N = (size_t)c->cap_atoms;
     DevAtoms &a = c->a;
     a.mxk = p->mxkvois;
-    a.ld = c->cap_atoms;
+    // ELL leading dimension: a multiple of 256 atoms, so a block's tile of the list (256 atoms x
+    // some slots) never leaves the allocation and a row is a multiple of 16 bytes (TMA)
+    a.ld = (int)((((size_t)c->cap_atoms + 255) / 256) * 256);
+    const size_t LD = (size_t)a.ld;
 #define AL(ptr, cnt)                                            \
     if ((e = dalloc(&(ptr), (cnt))) != cudaSuccess) return fail(e, "cudaMalloc " #ptr);
     AL(a.pos, N) AL(a.posff, N) AL(a.pos_bld, N)
@@ -194,7 +197,7 @@ extern "C" int msmgb_create(msmgb_ctx **out, const msmgb_params *p)
     AL(a.dx, N) AL(a.dy, N) AL(a.dz, N)
     AL(a.ityp, N) AL(a.statu, N) AL(a.gid, N) AL(a.boxid, N)
     AL(a.den, N) AL(a.epot, N) AL(a.den32, N)
-    AL(a.kvois, N) AL(a.indi, N * (size_t)p->mxkvois)
+    AL(a.kvois, N) AL(a.indi, LD * (size_t)p->mxkvois)
     AL(c->cell_of, N) AL(c->perm, N)
     AL(c->dbox, (size_t)c->cap_boxes)
     AL(c->cm, (size_t)kMaxGroups)
@@ -209,7 +212,7 @@ extern "C" int msmgb_create(msmgb_ctx **out, const msmgb_params *p)
     if ((e = cudaMallocHost((void **)&c->h_virial, sizeof(double) * 6 * c->cap_boxes)) != cudaSuccess) return fail(e, "pinned");
     if ((e = cudaMemsetAsync(c->flags, 0, sizeof(int) * kFlagWords, c->stream)) != cudaSuccess) return fail(e, "memset");
     if ((e = cudaMemsetAsync(c->maxdisp, 0, sizeof(unsigned long long), c->stream)) != cudaSuccess) return fail(e, "memset");
-    if (p->precision == MSMGB_PREC_MIXED && (e = dalloc(&a.pk, N * (size_t)p->mxkvois)) != cudaSuccess)
+    if (p->precision == MSMGB_PREC_MIXED && (e = dalloc(&a.pk, LD * (size_t)p->mxkvois)) != cudaSuccess)
         return fail(e, "cudaMalloc pair index");
     if (p->precision != MSMGB_PREC_FP64 && (e = dalloc(&a.rec, N)) != cudaSuccess)
         return fail(e, "cudaMalloc records");
@@ -259,7 +262,7 @@ extern "C" int msmgb_set_precision(msmgb_ctx *c, int precision)
     if (precision == MSMGB_PREC_MIXED && !c->a.pk) {
         RET(use_device(c));
         CK(cudaStreamSynchronize(c->stream), "synchronize");
-        CK(dalloc(&c->a.pk, (size_t)c->cap_atoms * (size_t)c->p.mxkvois), "cudaMalloc pair index");
+        CK(dalloc(&c->a.pk, (size_t)c->a.ld * (size_t)c->p.mxkvois), "cudaMalloc pair index");
     }
     if (precision == MSMGB_PREC_FF && !c->a.posfx) {
         RET(use_device(c));
@@ -303,6 +306,8 @@ static int poll_flags(msmgb_ctx *c)
         }
         if (e & kErrOutOfBox) return set_err(c, MSMGB_ERR_OUT_OF_BOX, "an active atom lies outside its box");
         if (e & kErrRho) return set_err(c, MSMGB_ERR_RHO_RANGE, "electron density beyond the F(rho) table");
+        if (e & kErrTimeout)
+            return set_err(c, MSMGB_ERR_TIMEOUT, "a bounded wait for an asynchronous list copy ran out");
     }
     return MSMGB_OK;
 }
@@ -713,7 +718,7 @@ extern "C" int msmgb_copyout_neighborelist(msmgb_ctx *c, int *kvois, int *indi, 
     CK(cudaMemcpy(gid.data(), c->a.gid, sizeof(int) * (size_t)n, cudaMemcpyDeviceToHost), "copy-out");
     std::vector<int> ind;
     if (indi) {
-        ind.resize((size_t)mxk * (size_t)c->cap_atoms);
+        ind.resize((size_t)mxk * (size_t)c->a.ld);
         CK(cudaMemcpy(ind.data(), c->a.indi, sizeof(int) * ind.size(), cudaMemcpyDeviceToHost), "copy-out");
     }
     const bool sorted = order == MSMGB_ORDER_SORTED;
@@ -722,7 +727,7 @@ extern "C" int msmgb_copyout_neighborelist(msmgb_ctx *c, int *kvois, int *indi, 
         kvois[g] = kv[(size_t)s];
         if (indi)
             for (int k = 0; k < kv[(size_t)s]; ++k) {
-                int j = ind[(size_t)k * (size_t)c->cap_atoms + (size_t)s];
+                int j = ind[(size_t)k * (size_t)c->a.ld + (size_t)s];
                 indi[(size_t)k * (size_t)ld + (size_t)g] = sorted ? j : gid[(size_t)j];
             }
     }
@@ -1157,7 +1162,7 @@ static int ensure_hvp_pair(msmgb_ctx *c)
 {
     if (c->hvp_pair) return MSMGB_OK;
     CK(cudaStreamSynchronize(c->stream), "synchronize");
-    CK(cudaMalloc(&c->hvp_pair, sizeof(double) * 5 * (size_t)c->cap_atoms * (size_t)c->p.mxkvois),
+    CK(cudaMalloc(&c->hvp_pair, sizeof(double) * 5 * (size_t)c->a.ld * (size_t)c->p.mxkvois),
        "HVP pair buffer");
     return MSMGB_OK;
 }
@@ -1362,6 +1367,44 @@ extern "C" int msmgb_time_hvp(msmgb_ctx *c, const double *v, int reps, float *ms
 
 // Launch variants chosen by the autotuner: out[0] density unroll, out[1] force unroll;
 // ms[0], ms[1]: their measured time per launch (0 before tuning).
+extern "C" int msmgb_selftest_wait(msmgb_ctx *c)
+{
+    if (!c) return MSMGB_ERR_ARG;
+    RET(use_device(c));
+    RET(launch_wait_selftest(c));
+    return poll_flags(c);
+}
+
+extern "C" int msmgb_set_tuning(msmgb_ctx *c, const int *codes)
+{
+    if (!c || !codes) return MSMGB_ERR_ARG;
+    static const int valid_d[] = {1, 2, 3, 4, 5, 9, 10, 18, 19, 20, 21};
+    static const int valid_f[] = {1, 2, 3, 4, 5, 9, 10, 18, 19, 20, 21, 50, 51, 52, 53};
+    auto in = [](int v, const int *set, int n) {
+        for (int k = 0; k < n; ++k)
+            if (set[k] == v) return true;
+        return false;
+    };
+    if ((codes[0] >= 0 && !in(codes[0], valid_d, 11)) || (codes[1] >= 0 && !in(codes[1], valid_f, 15)) ||
+        codes[2] >= 20)
+        return set_err(c, MSMGB_ERR_ARG, "unknown kernel variant code");
+    if (codes[2] >= 18) {
+        RET(use_device(c));
+        if (ensure_list_maps(c) != 1) return set_err(c, MSMGB_ERR_ARG, "TMA list descriptors unavailable");
+    }
+    if (codes[0] >= 0 || codes[1] >= 0) {
+        if (codes[0] >= 0) c->tune_dens_unroll = codes[0];
+        if (codes[1] >= 0) c->tune_force_unroll = codes[1];
+        c->tuned_n = c->n;
+    }
+    if (codes[2] >= 0) {
+        c->tune_fused = codes[2];
+        c->tuned_fused_n = c->n;
+    }
+    free_graph(c);
+    return MSMGB_OK;
+}
+
 extern "C" int msmgb_get_tuning(const msmgb_ctx *c, int *out, float *ms)
 {
     if (!c || !out) return MSMGB_ERR_ARG;

@@ -594,12 +594,226 @@ __global__ void __launch_bounds__(kBlock, MINB) k_force32_vv(DevAtoms a, DevTabl
     block_max_flush(dmax, a.maxdisp);
 }
 
+// ---- TMA-streamed variant of the step kernel ----------------------------------------------
+// The block's 256 atoms read their list slots from shared memory: one thread issues a 2D
+// tensor copy (cp.async.bulk.tensor) of the (256 atoms x kTmaSlots slots) tile of INDI and of
+// the packed indices per stage, double-buffered behind two mbarriers, so the coalesced list
+// stream leaves the load/store path of the SM that the neighbour gathers keep busy.  Every
+// wait is bounded: on expiry the block records kErrTimeout, waits (bounded again) for the
+// copies it issued and skips its atoms' work.
+constexpr int kTmaSlots = 8;
+constexpr unsigned long long kWaitNs = 500000000ull;   // 0.5 s per wait
+constexpr long kWaitSpinCap = 1L << 26;                // fallback bound on the polls
+
+__device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long *bar, unsigned bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, unsigned parity)
+{
+    unsigned ok;
+    asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                 "selp.u32 %0, 1, 0, p;\n\t}"
+                 : "=r"(ok)
+                 : "r"(smem_u32(bar)), "r"(parity)
+                 : "memory");
+    return ok != 0;
+}
+
+__device__ __forceinline__ unsigned long long global_ns()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// waits for the phase of `parity` to complete, for at most kWaitNs of wall time
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *bar, unsigned parity)
+{
+    const unsigned long long t0 = global_ns();
+    for (long it = 0; it < kWaitSpinCap; ++it) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if (global_ns() - t0 > kWaitNs) return false;
+    }
+    return false;
+}
+
+// Self-test of the bounded wait: one block waits on a barrier whose phase nothing completes;
+// the wait runs out, the kernel records kErrTimeout and returns.
+__global__ void k_wait_selftest(int *flags)
+{
+    __shared__ alignas(8) unsigned long long bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    const bool ok = mbar_wait_bounded(&bar, 0);
+    if (__syncthreads_or(!ok) && threadIdx.x == 0) atomicOr(&flags[kFlagErr], kErrTimeout);
+}
+
+int launch_wait_selftest(msmgb_ctx *c)
+{
+    k_wait_selftest<<<1, 32, 0, c->stream>>>(c->a.flags);
+    c->launches += 1;
+    return check_launch(c, "wait self-test");
+}
+
+__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *tm, int x, int y, unsigned long long *bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::
+            "r"(smem_u32(dst)),
+        "l"(reinterpret_cast<unsigned long long>(tm)), "r"(x), "r"(y), "r"(smem_u32(bar))
+        : "memory");
+}
+
+template <int UNR>
+__global__ void __launch_bounds__(kBlock, 4)
+    k_force32_vv_tma(DevAtoms a, DevTables t, double th, const __grid_constant__ CUtensorMap tm_indi,
+                     const __grid_constant__ CUtensorMap tm_pk)
+{
+    __shared__ alignas(128) int s_indi[2][kTmaSlots][kBlock];
+    __shared__ alignas(128) unsigned s_pk[2][kTmaSlots][kBlock];
+    __shared__ alignas(8) unsigned long long bar[2];
+    __shared__ int s_maxkn;
+    const int tid = threadIdx.x;
+    const int i0 = blockIdx.x * kBlock, i = i0 + tid;
+    const bool in = i < a.n;
+    const int stat = in ? a.statu[i] : 0;
+    const bool act = in && (stat & MSMGB_STATU_ACTIVE) == MSMGB_STATU_ACTIVE;
+    const int kn = act ? a.kvois[i] : 0;
+    if (tid == 0) {
+        s_maxkn = 0;
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    atomicMax(&s_maxkn, kn);
+    __syncthreads();
+    const int nstage = (s_maxkn + kTmaSlots - 1) / kTmaSlots;
+    constexpr unsigned kStageBytes = 2u * kTmaSlots * kBlock * sizeof(int);
+    if (tid == 0)
+        for (int st = 0; st < 2 && st < nstage; ++st) {
+            mbar_expect_tx(&bar[st], kStageBytes);
+            tma_load_2d(&s_indi[st][0][0], &tm_indi, i0, st * kTmaSlots, &bar[st]);
+            tma_load_2d(&s_pk[st][0][0], &tm_pk, i0, st * kTmaSlots, &bar[st]);
+        }
+    float fx = 0.0f, fy = 0.0f, fz = 0.0f;
+    PosFF pi;
+    BoxF b;
+    if (act) {
+        pi = ld_ff(a.rec + i);
+        b = load_boxf(a.box[a.boxid[i]]);
+    }
+    bool bail = false;
+    int st = 0;
+    for (; st < nstage; ++st) {
+        const int buf = st & 1;
+        const bool ok = mbar_wait_bounded(&bar[buf], (unsigned)((st >> 1) & 1));
+        bail = __syncthreads_or(!ok) != 0;
+        if (bail) break;
+#pragma unroll
+        for (int u0 = 0; u0 < kTmaSlots; u0 += UNR) {
+            unsigned c[UNR];
+            int j[UNR];
+#pragma unroll
+            for (int u = 0; u < UNR; ++u) {
+                const int w = st * kTmaSlots + u0 + u;
+                c[u] = w < kn ? s_pk[buf][u0 + u][tid] : kSkip;
+                j[u] = c[u] != kSkip ? s_indi[buf][u0 + u][tid] : i;
+            }
+            PosFF pj[UNR];
+            float4 e[UNR];
+#pragma unroll
+            for (int u = 0; u < UNR; ++u) {
+                pj[u] = ld_ff(a.rec + (c[u] != kSkip ? j[u] : (act ? i : 0)));
+                e[u] = __ldg(t.force4 + (c[u] != kSkip ? (c[u] >> kDkBits) : 0u));
+            }
+#pragma unroll
+            for (int u = 0; u < UNR; ++u)
+                if (c[u] != kSkip) force_pair_e(pi, pj[u], c[u], pi.d, pj[u].d, e[u], b, fx, fy, fz);
+        }
+        __syncthreads();                              // every thread is done with this buffer
+        if (tid == 0 && st + 2 < nstage) {
+            mbar_expect_tx(&bar[buf], kStageBytes);
+            tma_load_2d(&s_indi[buf][0][0], &tm_indi, i0, (st + 2) * kTmaSlots, &bar[buf]);
+            tma_load_2d(&s_pk[buf][0][0], &tm_pk, i0, (st + 2) * kTmaSlots, &bar[buf]);
+        }
+    }
+    if (bail) {
+        // copies issued for stages st and st + 1 may still be in flight: wait for them
+        // (bounded) before the block's shared memory goes away, record the timeout, skip the work
+        for (int s2 = st; s2 < st + 2 && s2 < nstage; ++s2) mbar_wait_bounded(&bar[s2 & 1], (unsigned)((s2 >> 1) & 1));
+        if (tid == 0) atomicOr(&a.flags[kFlagErr], kErrTimeout);
+        return;
+    }
+    double dmax = 0.0;
+    if (in) {
+        const double Fx = (double)fx, Fy = (double)fy, Fz = (double)fz;
+        a.fx[i] = Fx;
+        a.fy[i] = Fy;
+        a.fz[i] = Fz;
+        const double4_32a p = a.pos[i];
+        if (act) {
+            dmax = vv_atom(a, i, stat, a.box[a.boxid[i]], th, true, Fx, Fy, Fz, p, a.pos_nxt, a.posff_nxt);
+        } else {
+            a.pos_nxt[i] = p;
+            a.posff_nxt[i] = a.posff[i];
+        }
+    }
+    block_max_flush(dmax, a.maxdisp);
+}
+
+// Builds the two TMA descriptors once per context (driver entry point fetched at run time,
+// no link-time dependency on the driver library).  Unavailable -> the variants are skipped.
+int ensure_list_maps(msmgb_ctx *c)
+{
+    if (c->tm_state) return c->tm_state;
+    c->tm_state = -1;
+    if (!c->a.pk || (c->a.ld % 256) != 0) return -1;
+    void *fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !fn) {
+        cudaGetLastError();
+        return -1;
+    }
+    typedef CUresult (*Encode)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                               const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                               CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+    Encode enc = (Encode)fn;
+    const cuuint64_t dims[2] = {(cuuint64_t)c->a.ld, (cuuint64_t)c->p.mxkvois};
+    const cuuint64_t strides[1] = {(cuuint64_t)c->a.ld * sizeof(int)};
+    const cuuint32_t box[2] = {(cuuint32_t)kBlock, (cuuint32_t)kTmaSlots};
+    const cuuint32_t estr[2] = {1, 1};
+    CUresult r1 = enc(&c->tm_indi, CU_TENSOR_MAP_DATA_TYPE_INT32, 2, (void *)c->a.indi, dims, strides, box, estr,
+                      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    CUresult r2 = enc(&c->tm_pk, CU_TENSOR_MAP_DATA_TYPE_UINT32, 2, (void *)c->a.pk, dims, strides, box, estr,
+                      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    c->tm_state = (r1 == CUDA_SUCCESS && r2 == CUDA_SUCCESS) ? 1 : -1;
+    return c->tm_state;
+}
+
 static inline int nblk(long n, int b) { return (int)((n + b - 1) / b); }
 
 // variant codes of the fused kernel: (neighbours in flight, minimum resident blocks), codes
 // 6-11 the same six with the next slots of the list loaded one iteration ahead, 12-17 with
-// in addition every gather of a batch issued before its arithmetic (force_loop_batched)
-constexpr int kFusedVariants = 18;
+// in addition every gather of a batch issued before its arithmetic (force_loop_batched),
+// 18-19 the TMA-streamed list (2 and 4 neighbours per batch; skipped without descriptors)
+constexpr int kFusedVariants = 20;
 
 static void fused_variant(msmgb_ctx *c, int code, double h)
 {
@@ -622,6 +836,8 @@ static void fused_variant(msmgb_ctx *c, int code, double h)
     case 15: k_force32_vv<4, 4, 2><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
     case 16: k_force32_vv<2, 5, 2><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
     case 17: k_force32_vv<4, 5, 2><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
+    case 18: k_force32_vv_tma<2><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h, c->tm_indi, c->tm_pk); break;
+    case 19: k_force32_vv_tma<4><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h, c->tm_indi, c->tm_pk); break;
     default: k_force32_vv<2, 1, 0><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
     }
 }
@@ -647,7 +863,9 @@ int autotune_fused(msmgb_ctx *c)
     if (err != cudaSuccess) return cuda_err(c, err, "autotune events");
     float best = 1e30f;
     int bestc = 0;
+    const bool tma = ensure_list_maps(c) == 1;
     for (int code = 0; code < kFusedVariants; ++code) {
+        if (code >= 18 && !tma) continue;
         for (int r = 0; r < 4; ++r) {
             if (r == 1) cudaEventRecord(e0, c->stream);
             fused_variant(c, code, 0.0);

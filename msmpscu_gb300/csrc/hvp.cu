@@ -191,7 +191,7 @@ int launch_hvp(msmgb_ctx *c, const double *dv, double *dhv, double *v4buf, doubl
 {
     if (!c->hvp_pair) return set_err(c, MSMGB_ERR_ARG, "HVP pair buffer not allocated");
     double4_32a *pg = (double4_32a *)c->hvp_pair;
-    double *psk = (double *)(pg + (size_t)c->cap_atoms * (size_t)c->p.mxkvois);
+    double *psk = (double *)(pg + (size_t)c->a.ld * (size_t)c->p.mxkvois);
     const int n = c->n;
     const int bs = block_for(n), g = nblk(n, bs);
     const bool multi = c->tab.ngroup > 1;

@@ -16,6 +16,7 @@
 //                     layout INDI(NAPDEV,MXKVOIS), MD_NeighborsList_GPU.F90:75-85)
 //   tables   double   per kind, NTAB+2 entries (index 0 and NTAB+1 padded: the reference reads NTAB+1 when r = Rmax)
 #pragma once
+#include <cuda.h>            // CUtensorMap (type only; the encoder is fetched at run time)
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <string>
@@ -32,6 +33,7 @@ constexpr int kMaxGroups = 16;          // mp_MXGROUP, MD_Const.F90:77
 constexpr int kErrOverflow = 1;
 constexpr int kErrOutOfBox = 2;
 constexpr int kErrRho = 4;
+constexpr int kErrTimeout = 8;
 
 // device flag words
 enum {
@@ -305,6 +307,9 @@ struct msmgb_ctx {
     int tune_dens_unroll = 2, tune_force_unroll = 2, tune_fused = 0;
     float tune_ms_fused = 0.f;
     int tuned_fused_n = -1;      // atom count the fused kernel was tuned for
+    // TMA descriptors of the list (INDI) and packed-index (pk) ELL arrays, 2D {ld, mxkvois}
+    alignas(64) CUtensorMap tm_indi, tm_pk;
+    int tm_state = 0;            // 0 not built, 1 ready, -1 unavailable
     int tuned_n = -1;
     float tune_ms[2] = {0.f, 0.f};
 
@@ -347,6 +352,8 @@ int launch_density_ff(msmgb_ctx *c);
 int launch_force_ff(msmgb_ctx *c);
 int launch_force_ff_vv(msmgb_ctx *c, double h);
 int autotune_fused(msmgb_ctx *c);
+int ensure_list_maps(msmgb_ctx *c);
+int launch_wait_selftest(msmgb_ctx *c);
 int autotune_mixed(msmgb_ctx *c);
 int launch_hvp(msmgb_ctx *c, const double *dv, double *dhv, double *v4buf, double *ddbuf);
 int launch_adjoint(msmgb_ctx *c, const double *ft, const double *dtab, double *w4buf, double *ddbuf,

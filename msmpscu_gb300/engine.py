@@ -351,6 +351,11 @@ class Engine:
         return {"density_variant": out[0], "force_variant": out[1], "fused_variant": out[2],
                 "density_ms": ms[0], "force_ms": ms[1], "fused_ms": ms[2]}
 
+    def set_tuning(self, density=-1, force=-1, fused=-1):
+        """Pins kernel variants of the mixed passes (-1 leaves a choice to the tuner)."""
+        codes = (C.c_int * 3)(density, force, fused)
+        self._ck(self.lib.msmgb_set_tuning(self.ctx, codes))
+
     def list_stats(self):
         mk = C.c_int()
         mean = C.c_double()
