@@ -466,6 +466,7 @@ extern "C" int msmgb_init_forcetable(msmgb_ctx *c, const msmgb_forcetable *ft)
     c->tab_rmax = ft->rmax;
     c->have_tables = true;
     c->force_valid = false;
+    c->tuned_n = c->tuned_fused_n = -1;   // kernel variants are tuned per table kind count
     free_graph(c);
     return MSMGB_OK;
 }
@@ -956,7 +957,7 @@ static int capture_step(msmgb_ctx *c, double h)
 // ---- fused step: force pass + integrator in one kernel (mixed single species, float-float)
 static bool fused_mixed(const msmgb_ctx *c)
 {
-    return (c->p.precision == MSMGB_PREC_MIXED && c->tab.ngroup == 1) || c->p.precision == MSMGB_PREC_FF;
+    return c->p.precision == MSMGB_PREC_MIXED || c->p.precision == MSMGB_PREC_FF;
 }
 
 static int step_density(msmgb_ctx *c)
@@ -1386,9 +1387,9 @@ extern "C" int msmgb_set_tuning(msmgb_ctx *c, const int *codes)
         return false;
     };
     if ((codes[0] >= 0 && !in(codes[0], valid_d, 11)) || (codes[1] >= 0 && !in(codes[1], valid_f, 15)) ||
-        codes[2] >= 20)
+        codes[2] >= (c->tab.ngroup > 1 ? 4 : 20))
         return set_err(c, MSMGB_ERR_ARG, "unknown kernel variant code");
-    if (codes[2] >= 18) {
+    if (codes[2] >= 18 && c->tab.ngroup == 1) {
         RET(use_device(c));
         if (ensure_list_maps(c) != 1) return set_err(c, MSMGB_ERR_ARG, "TMA list descriptors unavailable");
     }

@@ -556,8 +556,8 @@ __global__ void __launch_bounds__(kBlock) k_force32s(DevAtoms a, DevTables t, in
 // written to a.pos_nxt / a.posff_nxt, so no thread overwrites a position another thread is
 // still gathering.  The integrator's FP64 work then runs on the FP64 pipe while other warps
 // of the same kernel keep the FP32 pipes busy, and one pass over x, v and F disappears.
-// Single species only (the multi-species mixed step keeps the separate integrator).
-template <int UNR, int MINB, int PF>
+// MULTI: several table kinds (FPOTB of KPAIR(i,j) and KPAIR(j,i)); PF 0 or 1 then.
+template <int UNR, int MINB, int PF, bool MULTI = false>
 __global__ void __launch_bounds__(kBlock, MINB) k_force32_vv(DevAtoms a, DevTables t, double th)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -570,7 +570,13 @@ __global__ void __launch_bounds__(kBlock, MINB) k_force32_vv(DevAtoms a, DevTabl
             const BoxF b = load_boxf(bb);
             const PosFF pi = ld_ff(a.rec + i);
             const float di = pi.d;
-            if (PF == 2) {
+            if (MULTI) {
+                const int ti = a.ityp[i] - 1;
+                walk_pairs<UNR, (PF != 0)>(a.indi + i, a.pk + i, (size_t)a.ld, a.kvois[i], [&](int j, unsigned c) {
+                    const PosFF pj = ld_ff(a.rec + j);
+                    force_pair<true>(pi, pj, c, di, pj.d, ti, a.ityp[j] - 1, b, t, fx, fy, fz);
+                });
+            } else if (PF == 2) {
                 force_loop_batched<UNR>(a, t, i, pi, di, b, fx, fy, fz);
             } else {
                 walk_pairs<UNR, (PF != 0)>(a.indi + i, a.pk + i, (size_t)a.ld, a.kvois[i], [&](int j, unsigned c) {
@@ -812,12 +818,24 @@ static inline int nblk(long n, int b) { return (int)((n + b - 1) / b); }
 // variant codes of the fused kernel: (neighbours in flight, minimum resident blocks), codes
 // 6-11 the same six with the next slots of the list loaded one iteration ahead, 12-17 with
 // in addition every gather of a batch issued before its arithmetic (force_loop_batched),
-// 18-19 the TMA-streamed list (2 and 4 neighbours per batch; skipped without descriptors)
+// 18-19 the TMA-streamed list (2 and 4 neighbours per batch; skipped without descriptors);
+// with several table kinds codes 0-3: 2/4 in flight x {plain, list prefetch}
 constexpr int kFusedVariants = 20;
+
+constexpr int kFusedVariantsMulti = 4;
 
 static void fused_variant(msmgb_ctx *c, int code, double h)
 {
     const int g = nblk(c->n, kBlock);
+    if (c->tab.ngroup > 1) {      // several table kinds: codes 0-3
+        switch (code) {
+        case 1: k_force32_vv<4, 1, 0, true><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
+        case 2: k_force32_vv<2, 1, 1, true><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
+        case 3: k_force32_vv<4, 1, 1, true><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
+        default: k_force32_vv<2, 1, 0, true><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
+        }
+        return;
+    }
     switch (code) {
     case 1: k_force32_vv<4, 1, 0><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
     case 2: k_force32_vv<2, 4, 0><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
@@ -863,8 +881,9 @@ int autotune_fused(msmgb_ctx *c)
     if (err != cudaSuccess) return cuda_err(c, err, "autotune events");
     float best = 1e30f;
     int bestc = 0;
-    const bool tma = ensure_list_maps(c) == 1;
-    for (int code = 0; code < kFusedVariants; ++code) {
+    const bool multi = c->tab.ngroup > 1;
+    const bool tma = !multi && ensure_list_maps(c) == 1;
+    for (int code = 0; code < (multi ? kFusedVariantsMulti : kFusedVariants); ++code) {
         if (code >= 18 && !tma) continue;
         for (int r = 0; r < 4; ++r) {
             if (r == 1) cudaEventRecord(e0, c->stream);
