@@ -281,6 +281,40 @@ def bytes_model(kmean):
     return dict(density=dens, force=force, vv=vv, fused=force + vv - 24.0, step=dens + force + vv)
 
 
+def oracle_parity(pos, vel, L, device=0, sample=200000):
+    """Full 2,048,000-atom system against the oracle (OpenMP): relative force error of each
+    precision (max abs difference over the max magnitude, and norm-wise), and the neighbour
+    sets of a random sample of atoms compared as sets."""
+    from msmpscu_gb300 import Engine, ForceTable, lattice as lt
+    from oracle import pyoracle as po
+    n = len(pos)
+    tabs = po.make_tables(po.POT_CR, [lt.CU_CR[k] for k in ("A", "xi", "p", "q", "r0")],
+                          lt.CU_RC, 10000, 10000, 20.0, want_embed=False)
+    t = po.Tables(tabs, po.FS, lt.CU_RC)
+    box = po.make_box([0, 0, 0], L)
+    ones = np.ones(n, np.int32)
+    okv, oind = po.nlist(pos, ones, box, lt.CU_RC_NL, 80)
+    ref = po.force(pos, ones, ones, box, okv, oind, t, want_virial=False, want_epot=False)["f"]
+    out = {"atoms": n}
+    for prec in ("fp64", "ff", "mixed"):
+        e = Engine(n, lt.CU_RC_NL, mxkvois=MXKVOIS, precision=prec, device=device)
+        e.init_forcetable(ForceTable.cleri_rosato(**lt.CU_CR, rc=lt.CU_RC))
+        e.copyin([(n, (0, 0, 0), tuple(L), (1, 1, 1))], pos, vel)
+        e.calforce()
+        d = e.get_force() - ref
+        out[prec + "_force_err_max"] = float(np.abs(d).max() / np.abs(ref).max())
+        out[prec + "_force_err_norm"] = float(np.linalg.norm(d) / np.linalg.norm(ref))
+        if prec == "fp64":
+            kv, ind = e.get_neighborelist()
+            rng = np.random.default_rng(1)
+            idx = rng.choice(n, min(sample, n), replace=False)
+            same = sum(1 for i in idx if np.array_equal(np.sort(ind[:kv[i], i]), np.sort(oind[:okv[i], i])))
+            out["nl_atoms_checked"] = int(len(idx))
+            out["nl_sets_identical"] = int(same)
+        e.close()
+    return out
+
+
 def nve_drift(device=0, steps=20000, every=2000):
     """Total-energy drift of NVE runs (Cu 10^3 cells, 4,000 atoms, 600 K, sigma 0.05 A,
     dt = 1 fs, skin trigger) in each precision: (E(end) - E(0)) per atom per ns and the largest
@@ -464,6 +498,7 @@ def run_ours(args):
         extras["hvp"] = hvp_w_dumbbell(device)
         extras["adjoint"] = adjoint_cu_snapshots(device)
         extras["nve_drift"] = nve_drift(device)
+        extras["oracle_parity"] = oracle_parity(pos, vel, L, device)
         e = None
 
     cpu = None
