@@ -4,7 +4,7 @@ FIXPOS / FIXVEL status bits of the integrator."""
 import numpy as np
 import pytest
 
-from msmpscu_gb300 import Engine, ForceTable, lattice as lt
+from msmpscu_gb300 import Engine, ForceTable, MSMError, lattice as lt
 from msmpscu_gb300 import _lib as L
 from tests.helpers import cu_tables, rel_err, sorted_sets, CR_PRM
 
@@ -174,4 +174,23 @@ def test_atomic_stress_sum_is_twice_virial_large():
     ap = e.atomic_stress()
     assert np.allclose(ap, ap.transpose(0, 2, 1), rtol=0, atol=1e-9 * np.abs(ap).max())
     assert rel_err(ap.sum(0), 2.0 * vir) < 1e-9
+    e.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "ff", "mixed"])
+def test_embedding_density_beyond_table_reported(precision):
+    """EAM: an F(rho) table that ends below the crystal's electron density (RHOMX = 0.5 max
+    POTB) is reported as MSMGB_ERR_RHO_RANGE by every precision; with a proper table the same
+    context then computes forces."""
+    pos, L_ = lt.w_sia_config(6, 0.02, 4)
+    n = len(pos)
+    e = Engine(n, lt.W_RC_NL, mxkvois=96, precision=precision)
+    e.init_forcetable(ForceTable.marinica_eam2(rhoscal=0.5))
+    e.copyin([(n, (0, 0, 0), tuple(L_), (1, 1, 1))], pos)
+    with pytest.raises(MSMError) as ei:
+        e.calforce()
+    assert ei.value.code == L.ERR_RHO_RANGE
+    e.init_forcetable(ForceTable.marinica_eam2())
+    e.calforce()
+    assert np.isfinite(e.get_force()).all()
     e.close()
