@@ -4,8 +4,11 @@
 // (dm_WorkSpace, dm_FTableWS, dm_Neighbors; MD_Globle_Variables_GPU.F90:158-194).  All
 // work is issued on the context's stream; the per-step sequence of For_One_Step
 // (MD_Method_GenericMD_GPU.F90:596-627: Predictor_DEV, Cal_NeighBoreList_DEV every
-// NB_UPTAB steps, CalForce, Correction_DEV) is captured once as a CUDA graph with the list
-// rebuild predicated on a device flag, so a step costs one graph launch and no host sync.
+// NB_UPTAB steps, CalForce, Correction_DEV) is captured once as a CUDA graph whose list
+// rebuild sits in a conditional node that the step's decision kernel switches on the
+// device, so a step costs one graph launch and no host synchronisation.  In the mixed and
+// float-float modes the force pass and the integrator are one kernel and the graphs
+// alternate two position buffers.
 #include <algorithm>
 #include <cmath>
 #include <cstdio>

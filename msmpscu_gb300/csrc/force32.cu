@@ -20,7 +20,11 @@
 // and only forms the FP32 separation for the force direction and 1/R.
 // Table values come from interleaved {value, slope} FP32 rows (one 8 B or 16 B load per
 // pair); rho and F accumulate in FP32 (measured error ~3e-7 of the FP64 forces).
-// Positions, the integrator and the list stay FP64.
+// Positions, the integrator and the list stay FP64.  The density pass also writes each
+// atom's {position, F'(rho)} record, so the force pass gets both with one 32 B gather.
+// Every pass exists in several variants (neighbours in flight, register caps, list
+// prefetch, batched gathers, TMA-streamed list tiles, shared-memory table windows) that
+// the autotuner times once per atom count.
 #include <algorithm>
 
 #include "msmgb_internal.cuh"

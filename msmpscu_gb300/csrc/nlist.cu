@@ -13,7 +13,9 @@
 //               (own cell first, then NIX/NIY/NIZ, MD_NeighborsList.F90:423-425); an FP32
 //               distance test decides every pair outside a narrow band around the cutoff,
 //               pairs inside the band get the exact FP64 rule d^2 < rc^2
-//               (MD_NeighborsList.F90:605), so the sets equal the FP64 oracle's.
+//               (MD_NeighborsList.F90:605), so the sets equal the FP64 oracle's.  Boxes
+//               whose cells are at least rc_nl wide take the image shift of the stencil
+//               cell; boxes with NCELL forced to 3 the minimum image of every candidate.
 // In an MD-step graph the rebuild is the body of a conditional node that the step's
 // decision kernel switches on (context.cu), so steps without a rebuild launch none of these.
 #include "msmgb_internal.cuh"
