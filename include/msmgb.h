@@ -157,7 +157,14 @@ int  msmgb_copyin_simbox(msmgb_ctx *ctx, int nbox, const msmgb_box *boxes, const
                          const int *statu, const double *xp, const double *xp1);
 /* masses CM(NGROUP) per atom type */
 int  msmgb_set_masses(msmgb_ctx *ctx, int ngroup, const double *cm);
-/* any pointer may be NULL; order = MSMGB_ORDER_ORIGINAL or MSMGB_ORDER_SORTED */
+/* New positions for the atoms already loaded (XP(N,3), caller order; host or device memory),
+ * as a minimiser or saddle search moves them: types, status, velocities and boxes stay;
+ * periodic directions are wrapped into the box; the neighbour list is kept while no atom has
+ * moved more than the skin trigger since the last build.  No counterpart in the reference
+ * (its drivers rewrite XP on the host and copy the whole box in again). */
+int  msmgb_update_positions(msmgb_ctx *ctx, const double *xp);
+/* any pointer may be NULL; order = MSMGB_ORDER_ORIGINAL or MSMGB_ORDER_SORTED.  The
+ * destination arrays of the copy-out calls may be host or device memory. */
 int  msmgb_copyout_simbox(msmgb_ctx *ctx, double *xp, double *xp1, int *statu, double *dis,
                           int order);
 int  msmgb_copyout_force(msmgb_ctx *ctx, double *fp, int order);       /* FP(N,3)          */

@@ -73,6 +73,7 @@ SIGNATURES = [
     ("msmgb_cal_atomic_stress", C.c_int, [C.c_void_p, _dp, C.c_int]),
     ("msmgb_copyin_simbox", C.c_int, [C.c_void_p, C.c_int, C.POINTER(Box), _ip, _ip, _dp, _dp]),
     ("msmgb_set_masses", C.c_int, [C.c_void_p, C.c_int, _dp]),
+    ("msmgb_update_positions", C.c_int, [C.c_void_p, C.c_void_p]),
     ("msmgb_copyout_simbox", C.c_int, [C.c_void_p, _dp, _dp, _ip, _dp, C.c_int]),
     ("msmgb_copyout_force", C.c_int, [C.c_void_p, _dp, C.c_int]),
     ("msmgb_copyout_epot", C.c_int, [C.c_void_p, _dp, C.c_int]),

@@ -128,6 +128,31 @@ __global__ void k_unpack3(const double *s0, const double *s1, const double *s2, 
     if (s2) dst[2 * n + g] = s2[s];
 }
 
+// caller-order positions -> sorted state (periodic directions wrapped into the box); the
+// largest displacement since the last list build goes to maxdisp (skin check)
+__global__ void __launch_bounds__(kBlock) k_update_pos(DevAtoms a, const double *xp)
+{
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    double d2 = 0.0;
+    if (s < a.n) {
+        const int n = a.n, g = a.gid[s];
+        const DevBox &b = a.box[a.boxid[s]];
+        double x[3] = {xp[g], xp[n + g], xp[2 * n + g]};
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+            if (b.ifpd[k]) x[k] -= floor((x[k] - b.lo[k]) / b.len[k]) * b.len[k];
+        a.pos[s] = make_double4_32a(x[0], x[1], x[2], 0.0);
+        const PosFF f = make_posff(x[0], x[1], x[2], b);
+        a.posff[s] = f;
+        const float4 q = a.pos_bld[s];
+        const float ex = mi32f(f.hx - q.x, b.lenf[0], b.halff[0], b.ifpd[0]);
+        const float ey = mi32f(f.hy - q.y, b.lenf[1], b.halff[1], b.ifpd[1]);
+        const float ez = mi32f(f.hz - q.z, b.lenf[2], b.halff[2], b.ifpd[2]);
+        d2 = (double)(ex * ex + ey * ey + ez * ez);
+    }
+    block_max_flush(d2, a.maxdisp);
+}
+
 __global__ void k_unpack_pos(const double4_32a *pos, const int *gid, int n, int sorted, double *dst)
 {
     int s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -618,7 +643,7 @@ static int copy_out_doubles(msmgb_ctx *c, const double *s0, const double *s1, co
     c->launches += 1;
     RET(check_launch(c, "copy-out"));
     int m = s1 ? 3 : 1;
-    CK(cudaMemcpyAsync(host, tmp, sizeof(double) * (size_t)m * n, cudaMemcpyDeviceToHost, c->stream), "copy-out");
+    CK(cudaMemcpyAsync(host, tmp, sizeof(double) * (size_t)m * n, cudaMemcpyDefault, c->stream), "copy-out");
     CK(cudaStreamSynchronize(c->stream), "synchronize");
     return MSMGB_OK;
 }
@@ -636,7 +661,7 @@ extern "C" int msmgb_copyout_simbox(msmgb_ctx *c, double *xp, double *xp1, int *
         k_unpack_pos<<<nblk(n, kBlock), kBlock, 0, c->stream>>>(c->a.pos, c->a.gid, n, sorted, tmp);
         c->launches += 1;
         RET(check_launch(c, "copy-out"));
-        CK(cudaMemcpyAsync(xp, tmp, sizeof(double) * 3 * (size_t)n, cudaMemcpyDeviceToHost, c->stream), "copy-out");
+        CK(cudaMemcpyAsync(xp, tmp, sizeof(double) * 3 * (size_t)n, cudaMemcpyDefault, c->stream), "copy-out");
         CK(cudaStreamSynchronize(c->stream), "synchronize");
     }
     if (xp1) RET(copy_out_doubles(c, c->a.vx, c->a.vy, c->a.vz, xp1, order));
@@ -649,6 +674,30 @@ extern "C" int msmgb_copyout_simbox(msmgb_ctx *c, double *xp, double *xp1, int *
         CK(cudaMemcpyAsync(statu, tmp, sizeof(int) * (size_t)n, cudaMemcpyDeviceToHost, c->stream), "copy-out");
         CK(cudaStreamSynchronize(c->stream), "synchronize");
     }
+    return MSMGB_OK;
+}
+
+extern "C" int msmgb_update_positions(msmgb_ctx *c, const double *xp)
+{
+    if (!c || !xp) return MSMGB_ERR_ARG;
+    RET(need_state(c));
+    RET(use_device(c));
+    const int n = c->n;
+    double *tmp = (double *)c->scratch;
+    CK(cudaMemcpyAsync(tmp, xp, sizeof(double) * 3 * (size_t)n, cudaMemcpyDefault, c->stream), "position copy-in");
+    CK(cudaMemsetAsync(c->maxdisp, 0, sizeof(unsigned long long), c->stream), "flag clear");
+    k_update_pos<<<nblk(n, kBlock), kBlock, 0, c->stream>>>(c->a, tmp);
+    c->launches += 1;
+    RET(check_launch(c, "position update"));
+    unsigned long long md = 0;
+    CK(cudaMemcpyAsync(&md, c->maxdisp, sizeof(md), cudaMemcpyDeviceToHost, c->stream), "flag read");
+    CK(cudaStreamSynchronize(c->stream), "synchronize");
+    double d2;
+    memcpy(&d2, &md, sizeof(d2));
+    const double thr = c->p.skin_trigger > 0.0 ? c->p.skin_trigger : 0.0;
+    if (!(d2 <= thr * thr)) c->list_valid = false;   // moved beyond the skin: rebuild at the next call
+    CK(cudaMemsetAsync(c->maxdisp, 0, sizeof(unsigned long long), c->stream), "flag clear");
+    c->force_valid = false;
     return MSMGB_OK;
 }
 

@@ -268,6 +268,15 @@ class Engine:
         if fp is not None:
             self._ck(self.lib.msmgb_copyout_force(self.ctx, _d(fp), order))
 
+    def update_positions(self, x):
+        """New positions (N,3) of the loaded atoms: a numpy array, or a CUDA tensor in the
+        XP layout (3N contiguous, x block then y then z) whose device memory is read directly."""
+        if hasattr(x, "data_ptr"):
+            self._ck(self.lib.msmgb_update_positions(self.ctx, C.c_void_p(x.data_ptr())))
+        else:
+            xp = np.ascontiguousarray(np.asarray(x, np.float64).T).reshape(-1)
+            self._ck(self.lib.msmgb_update_positions(self.ctx, xp.ctypes.data_as(C.c_void_p)))
+
     def set_masses(self, cm):
         cm = np.ascontiguousarray(np.atleast_1d(cm), dtype=np.float64)
         self._ck(self.lib.msmgb_set_masses(self.ctx, int(cm.size), _d(cm)))

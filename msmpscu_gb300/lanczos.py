@@ -15,11 +15,12 @@ def _project_translations(x):
     return (x - x.mean(axis=0, keepdims=True)).reshape(-1)
 
 
-def lanczos_lowest(matvec, n_atoms, iters=50, seed=0, project=True):
+def lanczos_lowest(matvec, n_atoms, iters=50, seed=0, project=True, v0=None):
     """matvec(v[N,3]) -> H v [N,3].  Returns (lowest Ritz value, its unit mode [N,3],
-    all Ritz values, per-iteration list of Krylov vectors used)."""
+    all Ritz values, per-iteration list of Krylov vectors used).  v0 (N,3) starts the Krylov
+    space (e.g. the previous mode of a saddle search), else a seeded random vector."""
     rng = np.random.default_rng(seed)
-    q = rng.normal(size=3 * n_atoms)
+    q = rng.normal(size=3 * n_atoms) if v0 is None else np.asarray(v0, np.float64).reshape(-1).copy()
     if project:
         q = _project_translations(q)
     q /= np.linalg.norm(q)
