@@ -160,8 +160,9 @@ int  msmgb_set_masses(msmgb_ctx *ctx, int ngroup, const double *cm);
 /* New positions for the atoms already loaded (XP(N,3), caller order; host or device memory),
  * as a minimiser or saddle search moves them: types, status, velocities and boxes stay;
  * periodic directions are wrapped into the box; the neighbour list is kept while no atom has
- * moved more than the skin trigger since the last build.  No counterpart in the reference
- * (its drivers rewrite XP on the host and copy the whole box in again). */
+ * moved more than the skin trigger since the last build.  Replaces CopyXPFrom_Host_to_Devices
+ * (MDLIB/sor/CommonGPU/MD_Globle_Variables_GPU.F90:349-353,2044), which the ART driver calls after
+ * moving XP on the host (MDLIB/sor/Appshell/MD_Method_ART_GPU.F90:630). */
 int  msmgb_update_positions(msmgb_ctx *ctx, const double *xp);
 /* any pointer may be NULL; order = MSMGB_ORDER_ORIGINAL or MSMGB_ORDER_SORTED.  The
  * destination arrays of the copy-out calls may be host or device memory. */
