@@ -315,6 +315,26 @@ int  msmgb_setfl_tables(const char *path, int ntab, double *potr, double *fpotr,
                         double *fpotb, double *fembd, double *dfembd, int *kpair, int *kembd,
                         double *rhod, double *masses);
 
+/* ---- tabulated EAM potentials in lspt layout (Register_ForceTableProc_SPT,
+ *      MDLIB/sor/Potentials/EAM_NIST/Filedatas_Func_Lspt.F90:560-604; reader
+ *      get_filedatas_lspt :118-301) ------------------------------------------------------- */
+/* flags: the reference reads the first file named on each pair line for every pair of that
+ * line (:263); MSMGB_LSPT_EACH_VR_FILE reads each named file instead. */
+#define MSMGB_LSPT_EACH_VR_FILE 1
+/* Element count, largest pair-file r (Angstrom) and largest F(rho)-file rho of an lspt
+ * control file and the ".spt" files it names. */
+int  msmgb_lspt_info(const char *path, int flags, int *nelem, double *rmax, double *rhomax);
+/* Tables of an lspt potential, EAM type, in the layouts of msmgb_setfl_tables: NKIND = NE^2
+ * pair tables on the sqrt(r) grid of ntab points up to rmax (<= 0: the files' largest r),
+ * POTR = 0.5 V r, FPOTR = -V' r, POTB = rho_J, FPOTB = -rho_J'; NKIND1 = NE embedding tables
+ * of nembd points, RHOD = max(largest F(rho)-file rho, rhoscal * max POTB) / nembd
+ * (rhoscal <= 0: 20, the reference's RHOSCAL default).  Natural cubic splines through the
+ * data with the reader's range rules (Vr_Spline, Rhor_Spline, Frho_Spline :340-500).
+ * Host only.  Returns MSMGB_ERR_ARG for a missing or malformed file. */
+int  msmgb_lspt_tables(const char *path, int flags, int ntab, int nembd, double rmax, double rhoscal,
+                       double *potr, double *fpotr, double *potb, double *fpotb, double *fembd,
+                       double *dfembd, int *kpair, int *kembd, double *rhod);
+
 #ifdef __cplusplus
 }
 #endif

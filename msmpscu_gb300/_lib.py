@@ -13,6 +13,7 @@ FS_TYPE, EAM_TYPE = 0, 1
 PREC_FP64, PREC_MIXED, PREC_FF = 0, 1, 2
 PRECISIONS = {"fp64": PREC_FP64, "mixed": PREC_MIXED, "ff": PREC_FF}
 ORDER_ORIGINAL, ORDER_SORTED = 0, 1
+LSPT_EACH_VR_FILE = 1
 POT_CR, POT_MARINICA2, POT_ACKLAND_WW = 1, 2, 3
 STATU_ACTIVE = 1
 STATU_FIXPOSX, STATU_FIXPOSY, STATU_FIXPOSZ = 2, 4, 8
@@ -97,6 +98,9 @@ SIGNATURES = [
     ("msmgb_param_adjoint", C.c_int, [C.c_void_p, C.c_int, _dp, _dp, _dp, _dp]),
     ("msmgb_setfl_info", C.c_int, [C.c_char_p, _ip, _ip, _ip, _dp]),
     ("msmgb_setfl_tables", C.c_int, [C.c_char_p, C.c_int, _dp, _dp, _dp, _dp, _dp, _dp, _ip, _ip, _dp, _dp]),
+    ("msmgb_lspt_info", C.c_int, [C.c_char_p, C.c_int, _ip, _dp, _dp]),
+    ("msmgb_lspt_tables", C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
+                                    _dp, _dp, _dp, _dp, _dp, _dp, _ip, _ip, _dp]),
     ("msmgb_cr_param_tables", C.c_int, [_dp, C.c_double, C.c_int, _dp]),
     ("msmgb_calforce_noalloc", C.c_int, [C.POINTER(ForceNoAlloc)]),
     ("msmgb_create_forcetable", C.c_int, [C.c_int, _dp, C.c_double, C.c_int, C.c_int, C.c_double,

@@ -380,3 +380,269 @@ extern "C" int msmgb_setfl_tables(const char *path, int ntab, double *potr, doub
         for (int e = 0; e < ne; ++e) masses[e] = s.mass[(size_t)e];
     return MSMGB_OK;
 }
+
+// ---- tabulated EAM potentials in lspt layout ----------------------------------------------
+// Register_ForceTableProc_SPT (Filedatas_Func_Lspt.F90:560-604) with the reader
+// get_filedatas_lspt (:118-301).  The control file, read line by line with comment lines
+// ('!') and blank lines skipped (GETINPUTSTRLINE.F): a line starting "&LSPT"; a line whose
+// first number is the element count NE; a line of NE quoted element symbols; per element a
+// line quoting its F(rho) file and one quoting its rho(r) file ("NA" = none); then for
+// I = 1..NE a line quoting I pair files V(r) of element I with elements 1..I.  Quoted means
+// between a pair of " or ' (EXSUBSTR.F).  Data files (".spt") hold '#' comment lines, then
+// "x f(x)" lines; their paths are relative to the control file's folder.
+// The reference opens the FIRST file named on each pair line for every pair of that line
+// (:263, SUBSTR(1) inside the loop over J); msmgb_lspt_tables does the same unless it is
+// given MSMGB_LSPT_EACH_VR_FILE.
+// Evaluation (Vr_Spline :340-385, Rhor_Spline :388-443, Frho_Spline :446-500): natural cubic
+// spline through the data (DBINT4 with IBCL = IBCR = 2, FBCL = FBCR = 0, KNTOPT = 1, :24-34);
+// below the first x the value at the first x with zero derivative; above the last x zero for
+// V(r) and rho(r), and F(x_last) with zero derivative for F(rho).  Tables take POTR = 0.5 V r,
+// FPOTR = -V' r, POTB = rho, FPOTB = -rho' (NN_Spline, RHO_Spline :503-537).  The density at
+// a host element without an F(rho) file is zero (the integer flag test at :406 read as "the
+// host has an F(rho) file"; no force or energy depends on it).
+// RMAX = the largest x of the pair files read (:291); RHOMX = max(largest x of the F(rho)
+// files (:290), RHOSCAL * max POTB over all tables (MD_TypeDef_ForceTable.F90:965)),
+// RHOD = RHOMX / NEMBD.
+namespace {
+
+struct Spt {
+    bool na = true;
+    std::vector<double> x, y, m;
+};
+
+struct Lspt {
+    int ne = 0;
+    std::vector<Spt> frho, rhor;
+    std::vector<Spt> vr;        // [I*(I+1)/2 + J], J <= I
+    double rmax = 0.0, rhomax = 0.0;
+};
+
+// one input line as GETINPUTSTRLINE returns it: printable characters only, left-adjusted;
+// false at end of file
+bool ctl_line(FILE *f, const char *skip, std::string &s)
+{
+    char buf[4096];
+    while (fgets(buf, sizeof(buf), f)) {
+        s.clear();
+        for (const char *p = buf; *p; ++p)
+            if ((unsigned char)*p >= 20 && (unsigned char)*p <= 126) s.push_back(*p);
+        size_t b = s.find_first_not_of(' ');
+        if (b == std::string::npos) continue;
+        s.erase(0, b);
+        if (strchr(skip, s[0])) continue;
+        return true;
+    }
+    return false;
+}
+
+std::vector<std::string> quoted(const std::string &s)
+{
+    std::vector<std::string> out;
+    size_t i = 0;
+    while (i < s.size()) {
+        if (s[i] == '"' || s[i] == '\'') {
+            size_t e = s.find(s[i], i + 1);
+            if (e == std::string::npos) break;
+            out.push_back(s.substr(i + 1, e - i - 1));
+            i = e + 1;
+        } else {
+            ++i;
+        }
+    }
+    return out;
+}
+
+std::string trim(const std::string &s)
+{
+    size_t b = s.find_first_not_of(' '), e = s.find_last_not_of(' ');
+    return b == std::string::npos ? std::string() : s.substr(b, e - b + 1);
+}
+
+bool is_na(const std::string &name)
+{
+    std::string t = trim(name);
+    return t.size() == 2 && toupper((unsigned char)t[0]) == 'N' && toupper((unsigned char)t[1]) == 'A';
+}
+
+// natural cubic spline through (x_i, y_i), x strictly increasing: second derivatives
+void spline_nu(Spt &s)
+{
+    const size_t n = s.x.size();
+    s.m.assign(n, 0.0);
+    if (n < 3) return;
+    std::vector<double> c(n, 0.0);
+    for (size_t i = 1; i + 1 < n; ++i) {
+        const double h0 = s.x[i] - s.x[i - 1], h1 = s.x[i + 1] - s.x[i];
+        const double rhs = 6.0 * ((s.y[i + 1] - s.y[i]) / h1 - (s.y[i] - s.y[i - 1]) / h0);
+        const double den = 2.0 * (h0 + h1) - h0 * c[i - 1];
+        c[i] = h1 / den;
+        s.m[i] = (rhs - h0 * s.m[i - 1]) / den;
+    }
+    for (size_t i = n - 2; i >= 1; --i) s.m[i] -= c[i] * s.m[i + 1];
+}
+
+double spline_nu_at(const Spt &s, double t, double *dy)
+{
+    const size_t n = s.x.size();
+    size_t lo = 0, hi = n - 1;                   // x[lo] <= t < x[hi]
+    while (hi - lo > 1) {
+        const size_t mid = (lo + hi) / 2;
+        if (s.x[mid] <= t) lo = mid; else hi = mid;
+    }
+    const double h = s.x[hi] - s.x[lo], b = (t - s.x[lo]) / h, a = 1.0 - b;
+    if (dy)
+        *dy = (s.y[hi] - s.y[lo]) / h + h * ((1.0 - 3.0 * a * a) * s.m[lo] + (3.0 * b * b - 1.0) * s.m[hi]) / 6.0;
+    return a * s.y[lo] + b * s.y[hi] + ((a * a * a - a) * s.m[lo] + (b * b * b - b) * s.m[hi]) * (h * h / 6.0);
+}
+
+// value and derivative with the reader's range rules; above_keep: F(rho) keeps its last value
+double spt_eval(const Spt &s, double t, bool above_keep, double *dy)
+{
+    *dy = 0.0;
+    if (s.na) return 0.0;
+    if (t < s.x.front()) return spline_nu_at(s, s.x.front(), nullptr);
+    if (t <= s.x.back()) return spline_nu_at(s, t, dy);
+    return above_keep ? spline_nu_at(s, s.x.back(), nullptr) : 0.0;
+}
+
+int read_spt(const std::string &path, Spt &s)
+{
+    FILE *f = fopen(path.c_str(), "r");
+    if (!f) return MSMGB_ERR_ARG;
+    std::string line;
+    int rc = MSMGB_OK;
+    s.x.clear();
+    s.y.clear();
+    while (ctl_line(f, "#", line)) {
+        char *e1 = nullptr, *e2 = nullptr;
+        const double x = strtod(line.c_str(), &e1);
+        const double y = strtod(e1, &e2);
+        if (e1 == line.c_str() || e2 == e1) { rc = MSMGB_ERR_ARG; break; }
+        if (!s.x.empty() && !(x > s.x.back())) { rc = MSMGB_ERR_ARG; break; }
+        s.x.push_back(x);
+        s.y.push_back(y);
+    }
+    fclose(f);
+    if (rc == MSMGB_OK && s.x.size() < 2) rc = MSMGB_ERR_ARG;
+    if (rc == MSMGB_OK) {
+        s.na = false;
+        spline_nu(s);
+    }
+    return rc;
+}
+
+int read_lspt(const char *path, int flags, Lspt &L)
+{
+    FILE *f = fopen(path, "r");
+    if (!f) return MSMGB_ERR_ARG;
+    std::string dir(path);
+    const size_t slash = dir.find_last_of('/');
+    dir = slash == std::string::npos ? std::string() : dir.substr(0, slash + 1);
+    std::string s;
+    int rc = MSMGB_ERR_ARG;
+    std::vector<std::string> q;
+    if (!ctl_line(f, "!", s)) goto done;
+    {
+        std::string kw = s.substr(0, s.find(' '));
+        for (char &c : kw) c = (char)toupper((unsigned char)c);
+        if (kw != "&LSPT") goto done;
+    }
+    if (!ctl_line(f, "!", s)) goto done;
+    {
+        size_t i = s.find_first_of("0123456789");
+        if (i == std::string::npos) goto done;
+        L.ne = atoi(s.c_str() + i);
+        if (L.ne < 1 || L.ne > 4) goto done;
+    }
+    if (!ctl_line(f, "!", s) || (int)quoted(s).size() != L.ne) goto done;
+    L.frho.resize((size_t)L.ne);
+    L.rhor.resize((size_t)L.ne);
+    L.vr.resize((size_t)(L.ne * (L.ne + 1) / 2));
+    for (int e = 0; e < L.ne; ++e)
+        for (int w = 0; w < 2; ++w) {
+            if (!ctl_line(f, "!", s) || (q = quoted(s)).empty()) goto done;
+            Spt &t = w == 0 ? L.frho[(size_t)e] : L.rhor[(size_t)e];
+            if (is_na(q[0])) continue;
+            if (read_spt(dir + trim(q[0]), t) != MSMGB_OK) goto done;
+            if (w == 0 && t.x.back() > L.rhomax) L.rhomax = t.x.back();
+        }
+    for (int i = 0; i < L.ne; ++i) {
+        if (!ctl_line(f, "!", s) || (int)(q = quoted(s)).size() != i + 1) goto done;
+        for (int j = 0; j <= i; ++j) {
+            Spt &t = L.vr[(size_t)(i * (i + 1) / 2 + j)];
+            const std::string &name = (flags & MSMGB_LSPT_EACH_VR_FILE) ? q[(size_t)j] : q[0];
+            if (read_spt(dir + trim(name), t) != MSMGB_OK) goto done;
+            if (t.x.back() > L.rmax) L.rmax = t.x.back();
+        }
+    }
+    rc = MSMGB_OK;
+done:
+    fclose(f);
+    return rc;
+}
+
+}  // namespace
+
+extern "C" int msmgb_lspt_info(const char *path, int flags, int *nelem, double *rmax, double *rhomax)
+{
+    if (!path) return MSMGB_ERR_ARG;
+    Lspt L;
+    int rc = read_lspt(path, flags, L);
+    if (rc) return rc;
+    if (nelem) *nelem = L.ne;
+    if (rmax) *rmax = L.rmax;
+    if (rhomax) *rhomax = L.rhomax;
+    return MSMGB_OK;
+}
+
+extern "C" int msmgb_lspt_tables(const char *path, int flags, int ntab, int nembd, double rmax,
+                                 double rhoscal, double *potr, double *fpotr, double *potb, double *fpotb,
+                                 double *fembd, double *dfembd, int *kpair, int *kembd, double *rhod)
+{
+    if (!path || ntab < 2 || nembd < 2 || !potr || !fpotr || !potb || !fpotb || !fembd || !dfembd || !kpair ||
+        !kembd)
+        return MSMGB_ERR_ARG;
+    Lspt L;
+    int rc = read_lspt(path, flags, L);
+    if (rc) return rc;
+    const int ne = L.ne, nk = ne * ne;
+    if (!(rmax > 0.0)) rmax = L.rmax;
+    if (!(rhoscal > 0.0)) rhoscal = 20.0;
+    const double csiv = std::sqrt(rmax) / ntab;
+    double rhomx = L.rhomax;
+    // table (I, J), 1-based id (I-1)*NE + J (Notify_func :327-337): pair V of elements
+    // max(I,J), min(I,J); density of element J at an element-I host
+    for (int I = 0; I < ne; ++I)
+        for (int J = 0; J < ne; ++J) {
+            const int k = I * ne + J;
+            const int a = I > J ? I : J, b = I > J ? J : I;
+            const Spt &v = L.vr[(size_t)(a * (a + 1) / 2 + b)];
+            const bool no_density = L.frho[(size_t)I].na;
+            for (int i = 1; i <= ntab; ++i) {
+                const double t = i * csiv, r = t * t;
+                double dv = 0.0, drh = 0.0;
+                const double vv = spt_eval(v, r, false, &dv);
+                const double rho = no_density ? 0.0 : spt_eval(L.rhor[(size_t)J], r, false, &drh);
+                const size_t o = (size_t)(i - 1) * nk + k;  // (NKIND, NTAB) column-major
+                potr[o] = 0.5 * vv * r;
+                fpotr[o] = -dv * r;
+                potb[o] = rho;
+                fpotb[o] = -drh;
+                if (rho * rhoscal > rhomx) rhomx = rho * rhoscal;
+            }
+            kpair[J * ne + I] = k + 1;                      // KPAIR(I,J), column-major
+        }
+    const double d = rhomx / nembd;
+    for (int e = 0; e < ne; ++e) {
+        kembd[e] = e + 1;
+        for (int i = 1; i <= nembd; ++i) {
+            double df = 0.0;
+            const double f = spt_eval(L.frho[(size_t)e], (i - 1) * d, true, &df);
+            const size_t o = (size_t)(i - 1) * ne + e;      // (NKIND1, NEMBD) column-major
+            fembd[o] = f;
+            dfembd[o] = df;
+        }
+    }
+    if (rhod) *rhod = d;
+    return MSMGB_OK;
+}

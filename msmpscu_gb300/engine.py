@@ -87,6 +87,41 @@ class ForceTable:
         return self
 
     @classmethod
+    def lspt(cls, path, ntab=10000, nembd=10000, rmax=None, rhoscal=20.0, each_vr_file=False):
+        """Tabulated EAM potential from an lspt control file and the ".spt" files it names
+        (Register_ForceTableProc_SPT): NE^2 pair tables on the sqrt(r) grid up to the largest
+        pair-file r (or rmax), NE embedding tables of nembd points.  each_vr_file=False reads,
+        like the reference, the first file named on each pair line for all pairs of that
+        line.  The files carry no masses: set them with Engine.set_masses."""
+        lib = L.load()
+        flags = L.LSPT_EACH_VR_FILE if each_vr_file else 0
+        bpath = os.fsencode(path)
+        ne, rfile, rhofile = C.c_int(), C.c_double(), C.c_double()
+        rc = lib.msmgb_lspt_info(bpath, flags, C.byref(ne), C.byref(rfile), C.byref(rhofile))
+        if rc != L.OK:
+            raise MSMError(rc, "cannot read lspt potential %s" % path)
+        self = cls.__new__(cls)
+        ne = ne.value
+        self.pot, self.pottype, self.prm = None, L.EAM_TYPE, np.zeros(5)
+        self.rmax = self.ru = float(rmax) if rmax else rfile.value
+        self.ntab, self.nembd = int(ntab), int(nembd)
+        self.nkind, self.nkind1, self.ngroup = ne * ne, ne, ne
+        self.potr, self.fpotr, self.potb, self.fpotb = (np.zeros(self.ntab * self.nkind) for _ in range(4))
+        self.fembd, self.dfembd = np.zeros(self.nembd * ne), np.zeros(self.nembd * ne)
+        self._kpair = np.zeros(ne * ne, np.int32)
+        self._kembd = np.zeros(ne, np.int32)
+        self.masses = None
+        rhod = C.c_double()
+        rc = lib.msmgb_lspt_tables(bpath, flags, self.ntab, self.nembd, self.rmax, float(rhoscal),
+                                   _d(self.potr), _d(self.fpotr), _d(self.potb), _d(self.fpotb),
+                                   _d(self.fembd), _d(self.dfembd), _i(self._kpair), _i(self._kembd),
+                                   C.byref(rhod))
+        if rc != L.OK:
+            raise MSMError(rc, "lspt table generation failed")
+        self.rhod = rhod.value
+        return self
+
+    @classmethod
     def cleri_rosato(cls, A, xi, p, q, r0, rc, ntab=10000):
         """Cleri-Rosato TB-SMA (FS type) with a hard cutoff rc (Rmax = RU = rc)."""
         return cls(L.POT_CR, [A, xi, p, q, r0], rc, rc, L.FS_TYPE, ntab=ntab, nembd=ntab)

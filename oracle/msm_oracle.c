@@ -930,6 +930,41 @@ double orc_spline_eval(int n, double x0, double h, const double *y, const double
     return a * y[k] + b * y[k + 1] + ((a * a * a - a) * m[k] + (b * b * b - b) * m[k + 1]) * h26;
 }
 
+void orc_spline_knots(int n, const double *x, const double *y, double *m)
+{
+    /* mu_i m_{i-1} + 2 m_i + lam_i m_{i+1} = d_i with mu_i = h_{i-1}/(h_{i-1}+h_i),
+     * lam_i = 1 - mu_i, d_i = 6 [x_{i-1}, x_i, x_{i+1}] (second divided difference) */
+    double *c = (double *)calloc((size_t)n, sizeof(double));
+    for (int i = 0; i < n; ++i) m[i] = 0.0;
+    for (int i = 1; i < n - 1; ++i) {
+        const double h0 = x[i] - x[i - 1], h1 = x[i + 1] - x[i];
+        const double mu = h0 / (h0 + h1), lam = 1.0 - mu;
+        const double d = 6.0 * ((y[i + 1] - y[i]) / h1 - (y[i] - y[i - 1]) / h0) / (h0 + h1);
+        const double piv = 2.0 - mu * c[i - 1];
+        c[i] = lam / piv;
+        m[i] = (d - mu * m[i - 1]) / piv;
+    }
+    for (int i = n - 2; i > 0; --i) m[i] -= c[i] * m[i + 1];
+    free(c);
+}
+
+void orc_spline_knots_eval(int n, const double *x, const double *y, const double *m, int nt,
+                           const double *t, double *f, double *df)
+{
+    for (int k = 0; k < nt; ++k) {
+        int lo = 0, hi = n - 1;
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (t[k] >= x[mid]) lo = mid; else hi = mid;
+        }
+        const double h = x[hi] - x[lo];
+        const double u = x[hi] - t[k], v = t[k] - x[lo];
+        f[k] = (m[lo] * u * u * u + m[hi] * v * v * v) / (6.0 * h) + (y[lo] / h - m[lo] * h / 6.0) * u +
+               (y[hi] / h - m[hi] * h / 6.0) * v;
+        df[k] = (m[hi] * v * v - m[lo] * u * u) / (2.0 * h) + (y[hi] - y[lo]) / h - (m[hi] - m[lo]) * h / 6.0;
+    }
+}
+
 int orc_setfl_tables(int nrho, double drho, int nr, double cutoff, const double *frho,
                      const double *rhor, const double *rphi, int ntab, double *potr, double *fpotr,
                      double *potb, double *fpotb, double *fembd, double *dfembd)

@@ -97,6 +97,14 @@ int    orc_setfl_tables(int nrho, double drho, int nr, double cutoff, const doub
                         const double *rhor, const double *rphi, int ntab, double *potr, double *fpotr,
                         double *potb, double *fpotb, double *fembd, double *dfembd);
 
+/* The same natural cubic spline on arbitrary increasing knots x_0 < ... < x_{n-1} (the lspt
+ * ".spt" files, Filedatas_Func_Lspt.F90:304-324 with the settings of :24-34):
+ *   orc_spline_knots:      second derivatives m (m[0] = m[n-1] = 0)
+ *   orc_spline_knots_eval: value f[k] and derivative df[k] at each t[k] in [x_0, x_{n-1}] */
+void   orc_spline_knots(int n, const double *x, const double *y, double *m);
+void   orc_spline_knots_eval(int n, const double *x, const double *y, const double *m, int nt,
+                             const double *t, double *f, double *df);
+
 /* neighbour list (MD_NeighborsList.F90:396-633/* neighbour list (MD_NeighborsList.F90:396-633, cut rule d^2 < rc^2 in FP64, minimum image).
  * indi is ELL column-major: neighbour k of atom i at indi[k*n + i]; 0-based atom ids.
  * Returns 0, or -1 on neighbour overflow, -2 on an atom outside the box. */

@@ -5,6 +5,7 @@ module, and only as the checker.  The product (``msmpscu_gb300``) never imports 
 """
 import ctypes as C
 import os
+import re
 
 import numpy as np
 
@@ -48,6 +49,8 @@ def lib():
         _lib.orc_atomic_stress.restype = None
         _lib.orc_spline_eval.restype = C.c_double
         _lib.orc_setfl_tables.restype = C.c_int
+        _lib.orc_spline_knots.restype = None
+        _lib.orc_spline_knots_eval.restype = None
         _lib.orc_pot_eval.restype = C.c_int
         _lib.orc_embed_eval.restype = C.c_int
     return _lib
@@ -200,6 +203,115 @@ def setfl_tables(d, ntab=10000, i=0, j=None):
         raise RuntimeError("oracle setfl tables failed")
     return dict(potr=potr, fpotr=fpotr, potb=potb, fpotb=fpotb, fembd=fe, dfembd=dfe, rhod=d["drho"],
                 ntab=ntab, nembd=d["nrho"], rmax=d["cutoff"])
+
+
+def _ctl_lines(path, skip):
+    """Non-comment lines as GETINPUTSTRLINE returns them (LIB/sor/f/MiniUtilities/
+    GETINPUTSTRLINE.F): printable characters (codes 20..126), left-adjusted, blank lines and
+    lines starting with a character of `skip` dropped."""
+    out = []
+    for raw in open(path, "rb").read().split(b"\n"):
+        s = "".join(chr(c) for c in raw if 20 <= c <= 126).lstrip(" ")
+        if s and s[0] not in skip:
+            out.append(s)
+    return out
+
+
+def _quoted(s):
+    """Substrings between matching quotes (LIB/sor/f/MiniUtilities/EXSUBSTR.F)."""
+    out, i = [], 0
+    while i < len(s):
+        if s[i] in "\"'":
+            e = s.find(s[i], i + 1)
+            if e < 0:
+                break
+            out.append(s[i + 1:e])
+            i = e + 1
+        else:
+            i += 1
+    return out
+
+
+def _read_spt(path):
+    rows = [ln.split() for ln in _ctl_lines(path, "#")]
+    a = np.array([[float(r[0]), float(r[1])] for r in rows])
+    return a[:, 0].copy(), a[:, 1].copy()
+
+
+def read_lspt(path, each_vr_file=False):
+    """lspt control file and its ".spt" files (get_filedatas_lspt, Filedatas_Func_Lspt.F90:
+    118-301).  Pair line I quotes I files; the reference opens the first of them for every
+    pair of the line (:263), which each_vr_file=False reproduces."""
+    folder = os.path.dirname(path)
+    ln = _ctl_lines(path, "!")
+    if not ln[0].split()[0].upper().startswith("&LSPT"):
+        raise ValueError("no &LSPT block")
+    ne = int(re.search(r"\d+", ln[1]).group(0))
+    el = [q.strip() for q in _quoted(ln[2])]
+    assert len(el) == ne
+    d = dict(elements=el, frho=[], rhor=[], vr={})
+    k = 3
+    for e in range(ne):
+        for key in ("frho", "rhor"):
+            name = _quoted(ln[k])[0].strip()
+            k += 1
+            d[key].append(None if name.upper() == "NA" else _read_spt(os.path.join(folder, name)))
+    for i in range(ne):
+        q = _quoted(ln[k])
+        k += 1
+        assert len(q) == i + 1
+        for j in range(i + 1):
+            d["vr"][(i, j)] = _read_spt(os.path.join(folder, (q[j] if each_vr_file else q[0]).strip()))
+    d["rmax"] = max(v[0][-1] for v in d["vr"].values())
+    d["rhomax"] = max([0.0] + [f[0][-1] for f in d["frho"] if f is not None])
+    return d
+
+
+def _spt_eval(xy, t, keep_above):
+    """Vr_Spline / Rhor_Spline / Frho_Spline range rules (Filedatas_Func_Lspt.F90:340-500):
+    natural spline inside the data, the first value with zero slope below it, and above it
+    zero (V, rho) or the last value with zero slope (F)."""
+    t = np.asarray(t, np.float64)
+    f, df = np.zeros_like(t), np.zeros_like(t)
+    if xy is None:
+        return f, df
+    x, y = f64(xy[0]), f64(xy[1])
+    m = np.zeros_like(x)
+    lib().orc_spline_knots(len(x), _d(x), _d(y), _d(m))
+    tc = np.clip(t, x[0], x[-1])
+    lib().orc_spline_knots_eval(len(x), _d(x), _d(y), _d(m), len(tc), _d(f64(tc)), _d(f), _d(df))
+    inside = (t >= x[0]) & (t <= x[-1])
+    df = np.where(inside, df, 0.0)
+    if not keep_above:
+        f = np.where(t > x[-1], 0.0, f)
+    return f, df
+
+
+def lspt_tables(d, ntab=10000, nembd=10000, rhoscal=20.0, rmax=None):
+    """All NE^2 pair tables (column (I, J) = I * NE + J: V of the pair, density of element J at
+    an element-I host, zero when element I has no F(rho)) on the sqrt(r) grid up to rmax (the
+    pair files' largest r) and the NE embedding tables on RHOD = max(largest F(rho) knot,
+    rhoscal * max POTB) / nembd (MD_TypeDef_ForceTable.F90:949-976, 1040-1048)."""
+    ne = len(d["elements"])
+    rmax = d["rmax"] if rmax is None else rmax
+    r = (np.arange(1, ntab + 1) * (np.sqrt(rmax) / ntab)) ** 2
+    potr, fpotr, potb, fpotb = (np.zeros((ntab, ne * ne)) for _ in range(4))
+    for i in range(ne):
+        for j in range(ne):
+            c = i * ne + j
+            v, dv = _spt_eval(d["vr"][(max(i, j), min(i, j))], r, False)
+            potr[:, c], fpotr[:, c] = 0.5 * v * r, -dv * r
+            if d["frho"][i] is not None:
+                rho, drho = _spt_eval(d["rhor"][j], r, False)
+                potb[:, c], fpotb[:, c] = rho, -drho
+    rhod = max(d["rhomax"], rhoscal * potb.max()) / nembd
+    fembd, dfembd = np.zeros((nembd, ne)), np.zeros((nembd, ne))
+    for e in range(ne):
+        fembd[:, e], dfembd[:, e] = _spt_eval(d["frho"][e], np.arange(nembd) * rhod, True)
+    kpair = np.arange(1, ne * ne + 1, dtype=np.int32).reshape(ne, ne)   # KPAIR(I, J) at [I-1, J-1]
+    return dict(potr=potr, fpotr=fpotr, potb=potb, fpotb=fpotb, fembd=fembd, dfembd=dfembd,
+                rhod=rhod, kpair=kpair, kembd=np.arange(1, ne + 1, dtype=np.int32), ntab=ntab,
+                nembd=nembd, rmax=rmax)
 
 
 def make_box(lo, length, ifpd=(1, 1, 1)):
