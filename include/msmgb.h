@@ -292,6 +292,10 @@ int  msmgb_calforce_noalloc(const msmgb_force_noalloc *args);
 #define MSMGB_POT_CR          1   /* Cleri-Rosato TB-SMA, FS form; prm = A, xi, p, q, r0     */
 #define MSMGB_POT_MARINICA2   2   /* Marinica EAM2 for W (EAM form); prm unused              */
 #define MSMGB_POT_ACKLAND_WW  3   /* Ackland-Thetford W, FS form; prm unused                 */
+/* the rest of the W-He library EM_TB_WangJun_W-HE_2010 (EM_TB_ForceTable_WangJun_W_HE_2010.F90:68-121) */
+#define MSMGB_POT_DERLET_WW   4   /* Derlet-Nguyen-Manh-Dudarev W, FS form (FS_PM_WW.F90)      */
+#define MSMGB_POT_HEHE_EXP6   5   /* He-He ZBL / cubic / EXP6, no density (ZBL_EXP6_HeHe.F90)  */
+#define MSMGB_POT_HEW_ZBL     6   /* He-W ZBL / cubics / EXP6, no density (ZBL_ABINTIO_He_W_930.F90) */
 /* Fills POTR/FPOTR/POTB/FPOTB (ntab each) and, if fembd/dfembd are non-NULL, F/F' (nembd
  * each); returns RHOD = rhoscal * max(POTB) / nembd through *rhod.  Lengths in Angstrom,
  * energies in eV. */

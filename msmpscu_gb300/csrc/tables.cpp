@@ -114,6 +114,150 @@ PairVal ackland_ww(double r)
     return o;
 }
 
+// The W-He library of the reference (EM_TB_WangJun_W-HE_2010, registered by
+// EM_TB_ForceTable_WangJun_W_HE_2010.F90:68-121).  These three are evaluated in the reference's
+// CGS units (cm, erg) exactly as written there and converted to Angstrom / eV on return.
+const double kEVERG = 1.60219e-12;      // eV -> erg (MSM_Const.F90:83)
+const double kBOHR = 5.291772108e-9;    // cm (MSM_Const.F90:99)
+const double kPI = 3.141592654;         // CP_PI (MSM_Const.F90:56), as the reference states it
+
+PairVal to_ev(double potr_erg, double fpotr_erg_cm)
+{
+    return PairVal{potr_erg / kEVERG, fpotr_erg_cm / kEVERG * 1e-8, 0.0, 0.0};
+}
+
+// Derlet, Nguyen-Manh, Dudarev W (FS form), FS_PM_WW.F90:7-204: V = sum_k v_k (rv_k - r)^3,
+// rho = A^2 sum_k f_k (rf_k - r)^3 over the knots with r <= knot.  A is written without an
+// exponent letter (:13), i.e. as a single-precision literal, so its value is that float.
+PairVal derlet_ww(double r_a)
+{
+    static const double rv[9] = {4.2689e-8, 3.98568e-8, 3.70246e-8, 3.41924e-8, 3.13602e-8,
+                                 2.8528e-8, 2.74110e-8, 2.604045e-8, 2.46699e-8};
+    static const double v[9] = {-0.1036435865158945e24, -0.2912948318493851e24, -2.096765499656263e24,
+                                19.1604545270101e24, -41.01619862085917e24, 46.05205617244703e24,
+                                26.42203930654883e24, 15.35211507804088e24, 14.12806259323987e24};
+    static const double rf[7] = {3.3216e-8, 3.165333333333333e-8, 3.009066666666667e-8, 2.8528e-8,
+                                 2.7411e-8, 2.604045e-8, 2.46699e-8};
+    static const double f[7] = {1.677334871575606e24, -1.673137509507131e24, -4.737051994974169e24,
+                                7.870789420780674e24, -3.7924230525563378e20, 6.190816158916646e24,
+                                -0.9565713891199151e24};
+    const double A = (double)10.84238200368439f * kEVERG;
+    const double r = r_a * 1e-8;
+    double pv = 0.0, dv = 0.0, pb = 0.0, db = 0.0;
+    for (int k = 0; k < 9; ++k)
+        if (!(r > rv[k])) {
+            const double t = rv[k] - r;
+            pv += v[k] * kEVERG * t * t * t;
+            dv += 3.0 * v[k] * kEVERG * t * t;
+        }
+    for (int k = 0; k < 7; ++k)
+        if (!(r > rf[k])) {
+            const double t = rf[k] - r;
+            pb += f[k] * t * t * t;
+            db += 3.0 * f[k] * t * t;
+        }
+    PairVal o = to_ev(0.5 * pv, dv);
+    o.potb = pb * A * A / (kEVERG * kEVERG);          // eV^2
+    o.fpotb = db * A * A / (kEVERG * kEVERG) * 1e-8;  // eV^2 / A
+    return o;
+}
+
+// universal ZBL screened Coulomb pair, MD_CorePotent.F90:24-75 (CGS): POTR = V/2, FPOTR = -V'
+void zbl_cgs(double z1, double z2, double r, double *potr, double *fpotr)
+{
+    const double ke2 = 9.0e9 * 1.60219e-19 * 1.60219e-19 * 1.0e7 * 1.0e2;
+    const double as = 0.88534 * kBOHR / (std::pow(z1, 0.23) + std::pow(z2, 0.23));
+    const double x = r / as, zz = z1 * z2 * ke2;
+    const double e1 = std::exp(-3.1998 * x), e2 = std::exp(-0.94229 * x), e3 = std::exp(-0.4029 * x),
+                 e4 = std::exp(-0.20162 * x);
+    const double phi = zz * (0.18175 * e1 + 0.50986 * e2 + 0.28022 * e3 + 0.028171 * e4) / r;
+    const double dphi = zz * (3.1998 * 0.18175 * e1 + 0.94229 * 0.50986 * e2 + 0.4029 * 0.28022 * e3 +
+                              0.20162 * 0.028171 * e4) / as;
+    *potr = 0.5 * phi;
+    *fpotr = (phi + dphi) / r;
+}
+
+// He-He, ZBL_EXP6_HeHe.F90:7-86: ZBL below 1.0 A, a cubic bridge to 1.3 A, EXP6 beyond; no
+// density.  The bridge's last two coefficients (:9-12) are written without an exponent letter,
+// i.e. as single-precision literals, so they take their float values.
+PairVal hehe_exp6(double r_a)
+{
+    static const double sc[4] = {3.5443059983603055e-11, -4.8619762395294636e-3, (double)200609.6243721997f,
+                                 (double)-2069784026620.333f};
+    const double r = r_a * 1e-8;
+    double p, f;
+    if (r < 1.0e-8) {
+        zbl_cgs(2.0, 2.0, r, &p, &f);
+    } else if (r < 1.3e-8) {
+        p = (sc[0] + sc[1] * r + sc[2] * r * r + sc[3] * r * r * r) * 0.5;
+        f = -(sc[1] + 2.0 * sc[2] * r + 3.0 * sc[3] * r * r);
+    } else {
+        const double ce = 0.000930644 * kEVERG, r0 = 0.29673e-7, alpha = 13.1;
+        const double redx = r0 / r, ex = std::exp(alpha * (1.0 - 1.0 / redx));
+        p = 0.5 * ce * (6.0 / (alpha - 6.0) * ex - (alpha / (alpha - 6.0)) * std::pow(redx, 6.0));
+        f = ce * (6.0 / (alpha - 6.0) * ex * alpha / r0 -
+                  (alpha / (alpha - 6.0)) * 6.0 * std::pow(redx, 5.0) * r0 / r / r);
+    }
+    return to_ev(p, f);
+}
+
+// He-W, ZBL_ABINTIO_He_W_930.F90:58-176: ZBL (SI constants) below 1.578 A, six cubic pieces in
+// A / eV to 3.5 A, then an EXP6 form times a sine switch between 4.3 and 7.3 A.  The switch's
+// derivative is taken as -cos(phase)/2 without the phase's own derivative (:147), and is kept so.
+PairVal hew_zbl(double r_a)
+{
+    const double ep0 = 8.854187817e-12, qe = 1.60219e-19, z1 = 2.0, z2 = 74.0, a0 = 5.291772108e-11;
+    static const double mid[7] = {1.57783601880074, 1.94810507446527, 2.10799896717072, 2.22277348041534,
+                                  2.32289959788322, 3.05974050760269, 3.5};
+    static const double cub[6][4] = {
+        {-54.6920134504158, 147.764553002780, -106.604073601512, 23.3457856042901},
+        {8.13894099222489, -6.77821270976276, 2.38825082778931, -0.378954410552979},
+        {11.8316959842284, -9.92672851472125, 2.88240909576416, -0.299054384231567},
+        {18.5956897803305, -18.0913941109865, 6.12169742584229, -0.719758272171021},
+        {11.5965650160971, -9.38901671011024, 2.52039670944214, -0.223789215087891},
+        {11.0095425643702, -9.03994004997097, 2.48033046722412, -0.227488279342651}};
+    const double r = r_a * 1e-8, rr = r * 1.0e8;
+    double p = 0.0, f = 0.0;
+    if (r < mid[0] * 1.0e-8) {
+        const double a = 0.88534 * a0 / (std::pow(z1, 0.23) + std::pow(z2, 0.23));
+        const double x = r * 1.0e-2 / a;
+        const double e1 = std::exp(-3.1998 * x), e2 = std::exp(-0.94229 * x), e3 = std::exp(-0.4029 * x),
+                     e4 = std::exp(-0.20162 * x);
+        const double faix = 0.18175 * e1 + 0.50986 * e2 + 0.28022 * e3 + 0.028171 * e4;
+        const double dfaix = (0.18175 * e1 * (-3.1998) + 0.50986 * e2 * (-0.94229) + 0.28022 * e3 * (-0.4029) +
+                              0.028171 * e4 * (-0.20162)) / a;
+        p = 0.5 * (qe * z1 * z2 * faix / (4.0 * kPI * ep0 * r * 1.0e-2)) * kEVERG;
+        f = -kEVERG * (qe * z1 * z2 / (4.0 * kPI * ep0) * (dfaix * r - faix * 1.0e2) / r / r);
+    } else if (r < 3.5e-8) {
+        int k = 0;
+        while (k < 5 && !(r < mid[k + 1] * 1.0e-8)) ++k;
+        const double *c = cub[k];
+        p = kEVERG * 0.5 * (c[0] + c[1] * rr + c[2] * std::pow(rr, 2.0) + c[3] * std::pow(rr, 3.0));
+        f = -kEVERG * (c[1] + 2.0 * c[2] * rr + 3.0 * c[3] * std::pow(rr, 2.0)) * 1.0e8;
+    } else {
+        const double cutrr = 5.8, cutorin = 1.5, ea = 0.0084600, eb = 9.6004204435, ec = 4.135;
+        double fc, dfc;
+        if (rr <= cutrr - cutorin) {
+            fc = 1.0;
+            dfc = 0.0;
+        } else if (cutrr + cutorin <= rr) {
+            fc = 0.0;
+            dfc = 0.0;
+        } else {
+            const double ph = 3.141592654 * 0.5 * (rr - cutrr) / cutorin;
+            dfc = -0.5 * std::cos(ph);
+            fc = 0.5 * (1.0 - std::sin(ph));
+        }
+        const double zb = 6.0 / (eb - 6.0) * std::exp(eb * (1.0 - rr / ec));
+        const double pm = ea * (zb - eb / (eb - 6.0) * std::pow(ec / rr, 6.0));
+        double fp = -zb * eb / ec + eb / (eb - 6.0) * 6.0 * std::pow(ec / rr, 5.0) * ec / rr / rr;
+        fp = ea * fp * fc + pm * dfc;
+        p = kEVERG * 0.5 * (pm * fc);
+        f = -kEVERG * fp * 1.0e8;
+    }
+    return to_ev(p, f);
+}
+
 }  // namespace
 
 extern "C" int msmgb_create_forcetable(int pot, const double *prm, double rmax, int ntab,
@@ -123,16 +267,22 @@ extern "C" int msmgb_create_forcetable(int pot, const double *prm, double rmax, 
 {
     if (ntab < 2 || rmax <= 0.0 || !potr || !fpotr || !potb || !fpotb) return MSMGB_ERR_ARG;
     if (pot == MSMGB_POT_CR && !prm) return MSMGB_ERR_ARG;
-    if (pot != MSMGB_POT_CR && pot != MSMGB_POT_MARINICA2 && pot != MSMGB_POT_ACKLAND_WW)
-        return MSMGB_ERR_ARG;
+    if (pot < MSMGB_POT_CR || pot > MSMGB_POT_HEW_ZBL) return MSMGB_ERR_ARG;
     const double csi = (double)ntab / std::sqrt(rmax);
     const double csiv = 1.0 / csi;
     double rhomx = -1.0;
     for (int i = 1; i <= ntab; ++i) {
         double t = (double)i * csiv;
         double r = t * t;
-        PairVal v = pot == MSMGB_POT_CR ? cleri_rosato(r, prm)
-                  : pot == MSMGB_POT_MARINICA2 ? marinica2(r) : ackland_ww(r);
+        PairVal v;
+        switch (pot) {
+        case MSMGB_POT_CR: v = cleri_rosato(r, prm); break;
+        case MSMGB_POT_MARINICA2: v = marinica2(r); break;
+        case MSMGB_POT_ACKLAND_WW: v = ackland_ww(r); break;
+        case MSMGB_POT_DERLET_WW: v = derlet_ww(r); break;
+        case MSMGB_POT_HEHE_EXP6: v = hehe_exp6(r); break;
+        default: v = hew_zbl(r); break;
+        }
         potr[i - 1] = v.potr * r;
         fpotr[i - 1] = v.fpotr * r;
         potb[i - 1] = v.potb;

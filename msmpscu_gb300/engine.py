@@ -136,6 +136,27 @@ class ForceTable:
     def ackland_ww(cls, rmax, ru=None, ntab=10000):
         return cls(L.POT_ACKLAND_WW, None, rmax, ru if ru else rmax, L.FS_TYPE, ntab=ntab)
 
+    @classmethod
+    def wangjun_w_he(cls, rmax=10.0, ru=None, ww="ackland", ntab=10000):
+        """The reference's W-He FS library EM_TB_WangJun_W-HE_2010
+        (EM_TB_ForceTable_WangJun_W_HE_2010.F90:68-121): tables #1 W-W (Ackland-Thetford),
+        #2 He-He (ZBL/EXP6), #3 He-W and #4 W-He (ZBL/ab-initio/EXP6), #5 W-W (Derlet et al.).
+        Groups W = 1, He = 2: KPAIR(1,1) = 1 (ww="ackland") or 5 (ww="derlet"),
+        KPAIR(2,2) = 2, KPAIR(2,1) = 3, KPAIR(1,2) = 4."""
+        pots = [L.POT_ACKLAND_WW, L.POT_HEHE_EXP6, L.POT_HEW_ZBL, L.POT_HEW_ZBL, L.POT_DERLET_WW]
+        parts = [cls(p, None, rmax, ru if ru else rmax, L.FS_TYPE, ntab=ntab) for p in pots]
+        self = parts[0]
+        nk = len(pots)
+        for key in ("potr", "fpotr", "potb", "fpotb"):
+            setattr(self, key, np.stack([getattr(t, key) for t in parts], 1).reshape(-1).copy())
+        self.pot = None
+        self.nkind, self.ngroup, self.nkind1 = nk, 2, 1
+        ww_id = {"ackland": 1, "derlet": 5}[ww]
+        kp = np.array([[ww_id, 4], [3, 2]], np.int32)       # KPAIR(I, J) at kp[I-1, J-1]
+        self._kpair = np.ascontiguousarray(kp.T).reshape(-1)
+        self._kembd = np.ones(2, np.int32)
+        return self
+
     def struct(self):
         t = L.ForceTable()
         t.pottype, t.ntab, t.nkind, t.rmax = self.pottype, self.ntab, self.nkind, self.rmax

@@ -160,6 +160,143 @@ static void ack_ne(double r, double *potb, double *fpotb)
     }
 }
 
+/* Derlet-Nguyen-Manh-Dudarev W (FS form), EM_TB_WangJun_W-HE_2010/FS_PM_WW.F90:7-204, restated
+ * in Angstrom / eV: knots x1e8, pair coefficients (erg/cm^3 / CP_EVERG) x1e-24 eV/A^3, density
+ * coefficients x1e-24 /A^3.  The prefactor A (:13) has no exponent letter in the source, so the
+ * reference holds it as a single-precision number: (float)10.84238200368439 eV. */
+static void der_nn(double r, double *potr, double *fpotr)
+{
+    static const double kn[9] = {4.2689, 3.98568, 3.70246, 3.41924, 3.13602, 2.8528, 2.74110,
+                                 2.604045, 2.46699};
+    static const double cv[9] = {-0.1036435865158945, -0.2912948318493851, -2.096765499656263,
+                                 19.1604545270101, -41.01619862085917, 46.05205617244703,
+                                 26.42203930654883, 15.35211507804088, 14.12806259323987};
+    double v = 0.0, dv = 0.0;
+    for (int k = 0; k < 9; ++k) {
+        if (r > kn[k]) continue;
+        v += cv[k] * pow(kn[k] - r, 3.0);
+        dv += 3.0 * cv[k] * pow(kn[k] - r, 2.0);
+    }
+    *potr = 0.5 * v;
+    *fpotr = dv;
+}
+
+static void der_ne(double r, double *potb, double *fpotb)
+{
+    static const double kn[7] = {3.3216, 3.165333333333333, 3.009066666666667, 2.8528, 2.7411,
+                                 2.604045, 2.46699};
+    static const double cf[7] = {1.677334871575606, -1.673137509507131, -4.737051994974169,
+                                 7.870789420780674, -3.7924230525563378e-4, 6.190816158916646,
+                                 -0.9565713891199151};
+    const double a = (double)(float)10.84238200368439;
+    double p = 0.0, d = 0.0;
+    for (int k = 0; k < 7; ++k) {
+        if (r > kn[k]) continue;
+        p += cf[k] * pow(kn[k] - r, 3.0);
+        d += 3.0 * cf[k] * pow(kn[k] - r, 2.0);
+    }
+    *potb = a * a * p;
+    *fpotb = a * a * d;
+}
+
+/* ZBL universal screening phi(x) and -dphi/dx */
+static void zbl_phi(double x, double *phi, double *mdphi)
+{
+    static const double c[4] = {0.18175, 0.50986, 0.28022, 0.028171};
+    static const double b[4] = {3.1998, 0.94229, 0.4029, 0.20162};
+    *phi = 0.0;
+    *mdphi = 0.0;
+    for (int k = 0; k < 4; ++k) {
+        *phi += c[k] * exp(-b[k] * x);
+        *mdphi += b[k] * c[k] * exp(-b[k] * x);
+    }
+}
+
+/* He-He, ZBL_EXP6_HeHe.F90:7-86 (ZBL of MD_CorePotent.F90:24-75 below 1 A, its fitted cubic to
+ * 1.3 A, EXP6 beyond), in Angstrom / eV.  The ZBL Coulomb constant 9e9 qe^2 (SI, :37-39) is
+ * 9 x 1.60219 eV*A with the reference's qe = 1.60219e-19 and eV = 1.60219e-12 erg. */
+static void hehe_nn(double r, double *potr, double *fpotr)
+{
+    if (r < 1.0) {
+        const double ke = 9.0 * 1.60219 * 4.0;                       /* Z1 Z2 e^2 / (4 pi eps0) */
+        const double as = 0.88534 * 0.5291772108 / (2.0 * pow(2.0, 0.23));
+        double phi, mdphi;
+        zbl_phi(r / as, &phi, &mdphi);
+        const double v = ke * phi / r;
+        *potr = 0.5 * v;
+        *fpotr = v / r + ke * mdphi / (as * r);
+    } else if (r < 1.3) {
+        /* the cubic's CGS coefficients (:9-12) in eV, eV/A, eV/A^2, eV/A^3; the last two are
+         * single-precision literals in the source (no exponent letter) */
+        const double e = 1.60219e-12;
+        const double c0 = 3.5443059983603055e-11 / e, c1 = -4.8619762395294636e-3 * 1e-8 / e;
+        const double c2 = (double)(float)200609.6243721997 * 1e-16 / e;
+        const double c3 = (double)(float)-2069784026620.333 * 1e-24 / e;
+        *potr = 0.5 * (c0 + r * (c1 + r * (c2 + r * c3)));
+        *fpotr = -(c1 + r * (2.0 * c2 + 3.0 * c3 * r));
+    } else {
+        const double ce = 0.000930644, r0 = 2.9673, al = 13.1;
+        const double ex = exp(al * (1.0 - r / r0)), s6 = pow(r0 / r, 6.0);
+        *potr = 0.5 * ce * (6.0 / (al - 6.0) * ex - al / (al - 6.0) * s6);
+        *fpotr = ce * (6.0 * al / ((al - 6.0) * r0) * ex - 6.0 * al / (al - 6.0) * s6 / r);
+    }
+}
+
+/* He-W, ZBL_ABINTIO_He_W_930.F90:58-176, in Angstrom / eV: ZBL with SI constants below
+ * 1.5778 A (4 pi with the reference's pi = 3.141592654), six cubics to 3.5 A, then an EXP6 form
+ * times the switch s = (1 - sin(pi (r - 5.8)/3))/2 on [4.3, 7.3] A whose derivative the
+ * reference takes as -cos(pi (r - 5.8)/3)/2 (no factor pi/3), reproduced here. */
+static void hew_nn(double r, double *potr, double *fpotr)
+{
+    static const double edge[7] = {1.57783601880074, 1.94810507446527, 2.10799896717072,
+                                   2.22277348041534, 2.32289959788322, 3.05974050760269, 3.5};
+    static const double c[6][4] = {
+        {-54.6920134504158, 147.764553002780, -106.604073601512, 23.3457856042901},
+        {8.13894099222489, -6.77821270976276, 2.38825082778931, -0.378954410552979},
+        {11.8316959842284, -9.92672851472125, 2.88240909576416, -0.299054384231567},
+        {18.5956897803305, -18.0913941109865, 6.12169742584229, -0.719758272171021},
+        {11.5965650160971, -9.38901671011024, 2.52039670944214, -0.223789215087891},
+        {11.0095425643702, -9.03994004997097, 2.48033046722412, -0.227488279342651}};
+    if (r < edge[0]) {
+        /* q Z1 Z2 / (4 pi eps0 r[m]) volts = eV per elementary charge; a in m */
+        const double k = 1.60219e-19 * 2.0 * 74.0 / (4.0 * 3.141592654 * 8.854187817e-12) * 1e10;
+        const double a = 0.88534 * 5.291772108e-11 / (pow(2.0, 0.23) + pow(74.0, 0.23)) * 1e10;
+        double phi, mdphi;
+        zbl_phi(r / a, &phi, &mdphi);
+        *potr = 0.5 * k * phi / r;
+        *fpotr = k * (phi / (r * r) + mdphi / (a * r));
+        return;
+    }
+    if (r < 3.5) {
+        int s = 5;
+        for (int q = 0; q < 6; ++q)
+            if (r < edge[q + 1]) { s = q; break; }
+        *potr = 0.5 * (c[s][0] + r * (c[s][1] + r * (c[s][2] + r * c[s][3])));
+        *fpotr = -(c[s][1] + r * (2.0 * c[s][2] + 3.0 * c[s][3] * r));
+        return;
+    }
+    const double ea = 0.0084600, eb = 9.6004204435, ec = 4.135;
+    double sw = 1.0, dsw = 0.0;
+    if (r >= 7.3) { sw = 0.0; }
+    else if (r > 4.3) {
+        const double ph = 3.141592654 * (r - 5.8) / 3.0;
+        sw = 0.5 * (1.0 - sin(ph));
+        dsw = -0.5 * cos(ph);
+    }
+    const double ex = 6.0 / (eb - 6.0) * exp(eb * (1.0 - r / ec));
+    const double v = ea * (ex - eb / (eb - 6.0) * pow(ec / r, 6.0));
+    const double mdv = ea * (ex * eb / ec - 6.0 * eb / (eb - 6.0) * pow(ec / r, 6.0) / r);
+    *potr = 0.5 * v * sw;
+    *fpotr = mdv * sw - v * dsw;
+}
+
+static void zero_ne(double r, double *potb, double *fpotb)
+{
+    (void)r;
+    *potb = 0.0;
+    *fpotb = 0.0;
+}
+
 int orc_pot_eval(int pot, const double *prm, double r, double *potr, double *fpotr,
                  double *potb, double *fpotb)
 {
@@ -167,6 +304,9 @@ int orc_pot_eval(int pot, const double *prm, double r, double *potr, double *fpo
     case ORC_POT_CR: cr_nn(r, prm, potr, fpotr); cr_ne(r, prm, potb, fpotb); return 0;
     case ORC_POT_MARINICA2: mar_nn(r, potr, fpotr); mar_ne(r, potb, fpotb); return 0;
     case ORC_POT_ACKLAND_WW: ack_nn(r, potr, fpotr); ack_ne(r, potb, fpotb); return 0;
+    case ORC_POT_DERLET_WW: der_nn(r, potr, fpotr); der_ne(r, potb, fpotb); return 0;
+    case ORC_POT_HEHE_EXP6: hehe_nn(r, potr, fpotr); zero_ne(r, potb, fpotb); return 0;
+    case ORC_POT_HEW_ZBL: hew_nn(r, potr, fpotr); zero_ne(r, potb, fpotb); return 0;
     default: return -1;
     }
 }

@@ -41,6 +41,9 @@ extern "C" {
 #define ORC_POT_CR          1   /* Cleri-Rosato TB-SMA (FS form); prm = A, xi, p, q, r0 */
 #define ORC_POT_MARINICA2   2   /* Marinica EAM2 W (EAM form); prm unused */
 #define ORC_POT_ACKLAND_WW  3   /* Ackland-Thetford W (FS form); prm unused; Angstrom/eV units */
+#define ORC_POT_DERLET_WW   4   /* Derlet-Nguyen-Manh-Dudarev W (FS form), FS_PM_WW.F90 */
+#define ORC_POT_HEHE_EXP6   5   /* He-He ZBL / cubic / EXP6 (no density), ZBL_EXP6_HeHe.F90 */
+#define ORC_POT_HEW_ZBL     6   /* He-W ZBL / cubics / EXP6 (no density), ZBL_ABINTIO_He_W_930.F90 */
 
 #define ORC_FS  0
 #define ORC_EAM 1

@@ -216,3 +216,27 @@ def test_force_matching_gradient_vs_central_fd(oracle):
         pm[m] -= h
         fd = (_loss(oracle, pp, pos, box, kv, ind, ft) - _loss(oracle, pm, pos, box, kv, ind, ft)) / (2 * h)
         assert grad[m] == pytest.approx(fd, rel=1e-6), m
+
+
+WANGJUN = os.path.join(os.path.dirname(__file__), "golden", "wangjun_pair_rows.txt")
+
+
+@pytest.mark.parametrize("col,pot", [(0, "POT_HEHE_EXP6"), (1, "POT_HEW_ZBL"), (2, "POT_HEW_ZBL"),
+                                     (3, "POT_DERLET_WW")])
+def test_wangjun_library_tables_match_reference_export(oracle, col, pot):
+    """Tables #2-#5 of EM_TB_WANGJUN_W-HE_2010.pair (He-He, He-W, W-He, Derlet W-W), with the
+    rows around every piece boundary: the oracle's Angstrom/eV restatement and the library's
+    CGS evaluation both reproduce the export's 10 printed digits (this also pins the
+    single-precision literals of the reference source and its switch derivative)."""
+    from msmpscu_gb300 import ForceTable, _lib as L
+    d = np.loadtxt(WANGJUN)
+    idx = d[:, 0].astype(int)
+    ref = d[:, 2 + 4 * col:6 + 4 * col]
+    t = oracle.make_tables(getattr(oracle, pot), None, 10.0, 10000, 10000, 20.0, want_embed=False)
+    lib = ForceTable(getattr(L, pot), None, 10.0, 10.0, L.FS_TYPE)
+    assert np.allclose((idx * np.sqrt(10.0) / 10000) ** 2, d[:, 1], rtol=1e-9)
+    for src in ((t["potr"], t["fpotr"], t["potb"], t["fpotb"]), (lib.potr, lib.fpotr, lib.potb, lib.fpotb)):
+        mine = np.stack([2.0 * src[0][idx - 1], src[1][idx - 1], src[2][idx - 1], src[3][idx - 1]], 1)
+        nz = ref != 0
+        assert (np.abs(mine[nz] - ref[nz]) / np.abs(ref[nz])).max() < 6e-10
+        assert not mine[~nz].any()
