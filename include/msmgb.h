@@ -319,6 +319,18 @@ int  msmgb_setfl_tables(const char *path, int ntab, double *potr, double *fpotr,
                         double *fpotb, double *fembd, double *dfembd, int *kpair, int *kembd,
                         double *rhod, double *masses);
 
+/* ---- Bonny, Grigorev, Terentyev W-H-He EAM (EAM_WHeH_Bonny_JPCM26_2014;
+ *      EAM_ForceTable_Bonny_JPCM26_2014.F90:17-121) ---------------------------------------- */
+/* subtype 1 = EAM1 (H and He pair-only), 2 = EAM2 (H embedded in the W density).  Writes
+ * *nkind = 9 (EAM1) or 10 (EAM2, table #10 zero) tables in the reference's registration order,
+ * (NKIND, NTAB) column-major (caller allocates 10*ntab), on the sqrt(r) grid up to rmax; the
+ * embedding tables of W, H, He (3, NEMBD) column-major with RHOD = rhoscal * max POTB / nembd
+ * (rhoscal <= 0: 20); KPAIR (3,3) column-major for groups W = 1, H = 2, He = 3 with the host
+ * first, KEMBD = 1, 2, 3.  Host only. */
+int  msmgb_bonny_wheh_tables(int subtype, double rmax, int ntab, int nembd, double rhoscal,
+                             double *potr, double *fpotr, double *potb, double *fpotb, double *fembd,
+                             double *dfembd, int *kpair, int *kembd, int *nkind, double *rhod);
+
 /* ---- tabulated EAM potentials in lspt layout (Register_ForceTableProc_SPT,
  *      MDLIB/sor/Potentials/EAM_NIST/Filedatas_Func_Lspt.F90:560-604; reader
  *      get_filedatas_lspt :118-301) ------------------------------------------------------- */

@@ -99,6 +99,8 @@ SIGNATURES = [
     ("msmgb_param_adjoint", C.c_int, [C.c_void_p, C.c_int, _dp, _dp, _dp, _dp]),
     ("msmgb_setfl_info", C.c_int, [C.c_char_p, _ip, _ip, _ip, _dp]),
     ("msmgb_setfl_tables", C.c_int, [C.c_char_p, C.c_int, _dp, _dp, _dp, _dp, _dp, _dp, _ip, _ip, _dp, _dp]),
+    ("msmgb_bonny_wheh_tables", C.c_int, [C.c_int, C.c_double, C.c_int, C.c_int, C.c_double,
+                                          _dp, _dp, _dp, _dp, _dp, _dp, _ip, _ip, _ip, _dp]),
     ("msmgb_lspt_info", C.c_int, [C.c_char_p, C.c_int, _ip, _dp, _dp]),
     ("msmgb_lspt_tables", C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
                                     _dp, _dp, _dp, _dp, _dp, _dp, _ip, _ip, _dp]),

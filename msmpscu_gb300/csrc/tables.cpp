@@ -258,6 +258,85 @@ PairVal hew_zbl(double r_a)
     return to_ev(p, f);
 }
 
+// Bonny, Grigorev, Terentyev W-H-He EAM (EAM_WHeH_Bonny_JPCM26_2014), subtypes EAM1 and EAM2
+// (EAM1_WHeH_Bonny_JPCM26_2014.F90).  W-W is Marinica EAM2 under a gauge transformation
+// (:15-104); the other pairs are sums of cubic knots (NN_FuncPoly3,
+// MD_Pot_EAM_Utilities.F90:48-85: POTR = V/2, FPOTR = -V').
+PairVal poly3_pair(double r, const double *a, const double *ri, int n)
+{
+    double p = 0.0, d = 0.0;
+    for (int i = 0; i < n; ++i)
+        if (ri[i] - r >= 0.0) {
+            p += a[i] * (ri[i] - r) * (ri[i] - r) * (ri[i] - r);
+            d += a[i] * (ri[i] - r) * (ri[i] - r);
+        }
+    return PairVal{0.5 * p, 3.0 * d, 0.0, 0.0};
+}
+
+const double kBonC = 1.848055990, kBonS = 2.232322602e-1;
+
+PairVal bonny_ww(double r)
+{
+    const PairVal m = marinica2(r);
+    return PairVal{m.potr - kBonC * m.potb, m.fpotr - 2.0 * kBonC * m.fpotb, m.potb * kBonS, m.fpotb * kBonS};
+}
+
+void bonny_w_embed(double rho, double *f, double *df)
+{
+    const double is = 1.0 / kBonS, cos_ = kBonC * is;
+    if (rho <= 1.359141225) {
+        const double t = rho * is;
+        double tf, tdf;
+        marinica2_embed(t, &tf, &tdf);
+        *f = tf + kBonC * t;
+        *df = tdf * is + cos_;
+    } else {
+        const double a0 = -5.524855802, a1 = 2.317313103e-1, a2 = -3.665345949e-2, a3 = 8.989367404e-3;
+        *f = a0 + rho * (a1 + rho * (a2 + rho * a3));
+        *df = a1 + rho * (2.0 * a2 + 3.0 * a3 * rho);
+    }
+}
+
+// EMBED_HH_Func2 through EMBED_FS_PLOY_Func (MD_Pot_EAM_Utilities.F90:332-368)
+void bonny_h_embed(double rho, double *f, double *df)
+{
+    if (rho <= 0.0) { *f = 0.0; *df = 0.0; return; }
+    const double a1 = -2.610066441e+01, a2 = 4.688963869e-01;
+    *f = a1 * std::sqrt(rho) + a2 * rho * rho;
+    *df = 0.5 * a1 / std::sqrt(rho) + 2.0 * a2 * rho;
+}
+
+// pair functions NN_*_Func1 (EAM1) and NN_*_Func2 (EAM2) for W-H, W-He, H-H, H-He, He-He
+PairVal bonny_pair(int sub, int which, double r)
+{
+    static const double wh1a[2] = {1.375733214e+01, 1.296071475e-01}, wh1r[2] = {2.0, 3.0};
+    static const double whe1a[3] = {2.100000000e+01, 8.565323293e-01, 2.750099819e-01}, whe1r[3] = {1.9, 2.2, 3.5};
+    static const double hh1a[2] = {4.862785907e-01, 1.018797872e-01}, hh1r[2] = {2.0, 3.0};
+    static const double hhe1a[3] = {1.500000000e+01, 2.563700119e-01, -4.489510592e-02}, hhe1r[3] = {1.8, 2.0, 3.0};
+    static const double hehe1a[2] = {2.106615791e+00, -2.217639348e-01}, hehe1r[2] = {2.0, 3.0};
+    static const double wh2a[3] = {4.424459079e+01, -4.993477782e+00, 1.461712984e+00},
+                        wh2r[3] = {2.0, 2.6475, 3.295};
+    static const double whe2a[4] = {0.0, 1.400000000e+01, -3.712116187e+00, 3.105031456e-01},
+                        whe2r[4] = {1.9, 2.0, 2.2, 3.5};
+    static const double hh2a[4] = {4.000000000e+01, 2.315124670e-01, -2.000000000e-01, 5.180584543e-02},
+                        hh2r[4] = {1.6, 2.0, 2.2, 3.0};
+    static const double hhe2a[3] = {3.256370012e+00, -4.000000000e-01, -4.489510592e-02}, hhe2r[3] = {2.0, 2.5, 3.0};
+    static const double hehe2a[4] = {2.000000000e+01, 1.051327582e+00, -4.000000000e+00, 3.203322671e-02},
+                        hehe2r[4] = {1.8, 2.0, 2.1, 3.0};
+    switch (which * 2 + (sub == 2)) {
+    case 0: return poly3_pair(r, wh1a, wh1r, 2);
+    case 1: return poly3_pair(r, wh2a, wh2r, 3);
+    case 2: return poly3_pair(r, whe1a, whe1r, 3);
+    case 3: return poly3_pair(r, whe2a, whe2r, 4);
+    case 4: return poly3_pair(r, hh1a, hh1r, 2);
+    case 5: return poly3_pair(r, hh2a, hh2r, 4);
+    case 6: return poly3_pair(r, hhe1a, hhe1r, 3);
+    case 7: return poly3_pair(r, hhe2a, hhe2r, 3);
+    case 8: return poly3_pair(r, hehe1a, hehe1r, 2);
+    default: return poly3_pair(r, hehe2a, hehe2r, 4);
+    }
+}
+
 }  // namespace
 
 extern "C" int msmgb_create_forcetable(int pot, const double *prm, double rmax, int ntab,
@@ -793,6 +872,69 @@ extern "C" int msmgb_lspt_tables(const char *path, int flags, int ntab, int nemb
             dfembd[o] = df;
         }
     }
+    if (rhod) *rhod = d;
+    return MSMGB_OK;
+}
+
+// Register_Interaction_Table of EAM_ForceTable_Bonny_JPCM26_2014.F90 (:17-121): tables in the
+// order the reference registers them, (source, target) = (W,W) (H,W) (He,W) (W,H) (H,H) (He,H)
+// (W,He) (H,He) (He,He), plus a zero table #10 for EAM2.  The target is the host
+// (Create_Interaction_ForceTable, MD_TypeDef_ForceTable.F90:1168-1178), so with groups
+// W = 1, H = 2, He = 3 the host-I / neighbour-J table is KPAIR(I,J) = (I-1)*3 + J.
+extern "C" int msmgb_bonny_wheh_tables(int subtype, double rmax, int ntab, int nembd, double rhoscal,
+                                       double *potr, double *fpotr, double *potb, double *fpotb,
+                                       double *fembd, double *dfembd, int *kpair, int *kembd, int *nkind,
+                                       double *rhod)
+{
+    if ((subtype != 1 && subtype != 2) || rmax <= 0.0 || ntab < 2 || nembd < 2 || !potr || !fpotr || !potb ||
+        !fpotb || !fembd || !dfembd || !kpair || !kembd)
+        return MSMGB_ERR_ARG;
+    if (!(rhoscal > 0.0)) rhoscal = 20.0;
+    const int nk = subtype == 2 ? 10 : 9;
+    // pair function per table: -1 W-W, else bonny_pair index (0 WH, 1 WHe, 2 HH, 3 HHe, 4 HeHe)
+    static const int pairfn[10] = {-1, 0, 1, 0, 2, 3, 1, 3, 4, -2};
+    const double csiv = std::sqrt(rmax) / ntab;
+    double rhomx = 0.0;
+    for (int k = 0; k < nk; ++k)
+        for (int i = 1; i <= ntab; ++i) {
+            const double t = i * csiv, r = t * t;
+            PairVal v{0.0, 0.0, 0.0, 0.0};
+            if (pairfn[k] == -1) {
+                v = bonny_ww(r);
+            } else if (pairfn[k] >= 0) {
+                v = bonny_pair(subtype, pairfn[k], r);
+                if (subtype == 2 && k == 3) {                // (W,H): the W density at an H host
+                    const PairVal w = bonny_ww(r);
+                    v.potb = w.potb;
+                    v.fpotb = w.fpotb;
+                }
+            }
+            const size_t o = (size_t)(i - 1) * nk + k;
+            potr[o] = v.potr * r;
+            fpotr[o] = v.fpotr * r;
+            potb[o] = v.potb;
+            fpotb[o] = v.fpotb;
+            if (rhomx < v.potb * rhoscal) rhomx = v.potb * rhoscal;
+        }
+    const double d = rhomx / nembd;
+    for (int i = 1; i <= nembd; ++i) {
+        const double rho = (i - 1) * d;
+        double f = 0.0, df = 0.0;
+        bonny_w_embed(rho, &f, &df);
+        fembd[(size_t)(i - 1) * 3 + 0] = f;
+        dfembd[(size_t)(i - 1) * 3 + 0] = df;
+        f = df = 0.0;
+        if (subtype == 2) bonny_h_embed(rho, &f, &df);
+        fembd[(size_t)(i - 1) * 3 + 1] = f;
+        dfembd[(size_t)(i - 1) * 3 + 1] = df;
+        fembd[(size_t)(i - 1) * 3 + 2] = 0.0;
+        dfembd[(size_t)(i - 1) * 3 + 2] = 0.0;
+    }
+    for (int I = 0; I < 3; ++I) {
+        kembd[I] = I + 1;
+        for (int J = 0; J < 3; ++J) kpair[J * 3 + I] = I * 3 + J + 1;   // column-major
+    }
+    if (nkind) *nkind = nk;
     if (rhod) *rhod = d;
     return MSMGB_OK;
 }

@@ -157,6 +157,33 @@ class ForceTable:
         self._kembd = np.ones(2, np.int32)
         return self
 
+    @classmethod
+    def bonny_wheh(cls, subtype="EAM1", rmax=5.4604375, ntab=10000, nembd=10000, rhoscal=20.0):
+        """The reference's W-H-He EAM of Bonny, Grigorev, Terentyev (EAM_WHeH_Bonny_JPCM26_2014),
+        subtype "EAM1" (H, He pair-only) or "EAM2" (H embedded in the W density); groups
+        W = 1, H = 2, He = 3."""
+        lib = L.load()
+        sub = {"EAM1": 1, "EAM2": 2}[subtype.upper()]
+        self = cls.__new__(cls)
+        self.pot, self.pottype, self.prm = None, L.EAM_TYPE, np.zeros(5)
+        self.rmax = self.ru = float(rmax)
+        self.ntab, self.nembd = int(ntab), int(nembd)
+        arrs = [np.zeros(10 * self.ntab) for _ in range(4)]
+        self.fembd, self.dfembd = np.zeros(3 * self.nembd), np.zeros(3 * self.nembd)
+        self._kpair = np.zeros(9, np.int32)
+        self._kembd = np.zeros(3, np.int32)
+        nk, rhod = C.c_int(), C.c_double()
+        rc = lib.msmgb_bonny_wheh_tables(sub, self.rmax, self.ntab, self.nembd, float(rhoscal),
+                                         *[_d(a) for a in arrs], _d(self.fembd), _d(self.dfembd),
+                                         _i(self._kpair), _i(self._kembd), C.byref(nk), C.byref(rhod))
+        if rc != L.OK:
+            raise MSMError(rc, "Bonny W-H-He table generation failed")
+        self.nkind, self.nkind1, self.ngroup = nk.value, 3, 3
+        self.potr, self.fpotr, self.potb, self.fpotb = (a[:self.nkind * self.ntab].copy() for a in arrs)
+        self.rhod = rhod.value
+        self.masses = None
+        return self
+
     def struct(self):
         t = L.ForceTable()
         t.pottype, t.ntab, t.nkind, t.rmax = self.pottype, self.ntab, self.nkind, self.rmax

@@ -297,6 +297,90 @@ static void zero_ne(double r, double *potb, double *fpotb)
     *fpotb = 0.0;
 }
 
+/* Bonny, Grigorev, Terentyev W-H-He EAM (EAM1_WHeH_Bonny_JPCM26_2014.F90), Angstrom / eV.
+ * Knot sums V = sum a_k (r_k - r)^3 for r <= r_k (NN_FuncPoly3, MD_Pot_EAM_Utilities.F90:48-85). */
+typedef struct { int n; double a[4], k[4]; } knots_t;
+
+static void knot_pair(const knots_t *p, double r, double *potr, double *fpotr)
+{
+    double v = 0.0, d = 0.0;
+    for (int i = 0; i < p->n; ++i) {
+        const double x = p->k[i] - r;
+        if (x < 0.0) continue;
+        v += p->a[i] * x * x * x;
+        d += p->a[i] * x * x;
+    }
+    *potr = 0.5 * v;
+    *fpotr = 3.0 * d;
+}
+
+/* table t (1-based, registration order) of subtype sub (1 = EAM1, 2 = EAM2):
+ * (W,W) (H,W) (He,W) (W,H) (H,H) (He,H) (W,He) (H,He) (He,He) [+ a zero #10 for EAM2] as
+ * (source, target); returns -1 for an unknown table */
+int orc_bonny_pair(int sub, int t, double r, double *potr, double *fpotr, double *potb, double *fpotb)
+{
+    static const knots_t k1[5] = {                        /* WH, WHe, HH, HHe, HeHe of EAM1 */
+        {2, {13.75733214, 0.1296071475}, {2.0, 3.0}},
+        {3, {21.0, 0.8565323293, 0.2750099819}, {1.9, 2.2, 3.5}},
+        {2, {0.4862785907, 0.1018797872}, {2.0, 3.0}},
+        {3, {15.0, 0.2563700119, -0.04489510592}, {1.8, 2.0, 3.0}},
+        {2, {2.106615791, -0.2217639348}, {2.0, 3.0}}};
+    static const knots_t k2[5] = {                        /* the same for EAM2 */
+        {3, {44.24459079, -4.993477782, 1.461712984}, {2.0, 2.6475, 3.295}},
+        {4, {0.0, 14.0, -3.712116187, 0.3105031456}, {1.9, 2.0, 2.2, 3.5}},
+        {4, {40.0, 0.2315124670, -0.2, 0.05180584543}, {1.6, 2.0, 2.2, 3.0}},
+        {3, {3.256370012, -0.4, -0.04489510592}, {2.0, 2.5, 3.0}},
+        {4, {20.0, 1.051327582, -4.0, 0.03203322671}, {1.8, 2.0, 2.1, 3.0}}};
+    static const int fn[10] = {-1, 0, 1, 0, 2, 3, 1, 3, 4, -2};
+    const double gc = 1.848055990, gs = 2.232322602e-1;
+    if (t < 1 || t > (sub == 2 ? 10 : 9)) return -1;
+    *potr = *fpotr = *potb = *fpotb = 0.0;
+    const int f = fn[t - 1];
+    if (f == -2) return 0;
+    double rho = 0.0, mdrho = 0.0;
+    if (f == -1 || (sub == 2 && t == 4)) {               /* the gauge-transformed Marinica density */
+        mar_ne(r, &rho, &mdrho);
+        *potb = gs * rho;
+        *fpotb = gs * mdrho;
+    }
+    if (f == -1) {                                       /* W-W: Marinica pair minus 2C rho */
+        double v2, mdv;
+        mar_nn(r, &v2, &mdv);
+        *potr = v2 - gc * rho;
+        *fpotr = mdv - 2.0 * gc * mdrho;
+    } else {
+        knot_pair(sub == 2 ? &k2[f] : &k1[f], r, potr, fpotr);
+    }
+    return 0;
+}
+
+/* embedding of group g (1 W, 2 H, 3 He): W the gauge-transformed Marinica F below
+ * rho_I = 1.359141225 and a cubic above; H (EAM2 only) -26.10066441 sqrt(rho) + 0.4688963869 rho^2 */
+int orc_bonny_embed(int sub, int g, double rho, double *f, double *df)
+{
+    *f = *df = 0.0;
+    if (g == 1) {
+        const double gc = 1.848055990, gs = 2.232322602e-1;
+        if (rho <= 1.359141225) {
+            double tf, tdf;
+            const double tr = rho * (1.0 / gs);
+            mar_embed(tr, &tf, &tdf);
+            *f = tf + gc * tr;
+            *df = tdf * (1.0 / gs) + gc * (1.0 / gs);
+        } else {
+            const double c[4] = {-5.524855802, 2.317313103e-1, -3.665345949e-2, 8.989367404e-3};
+            *f = c[0] + c[1] * rho + c[2] * rho * rho + c[3] * rho * rho * rho;
+            *df = c[1] + 2.0 * c[2] * rho + 3.0 * c[3] * rho * rho;
+        }
+        return 0;
+    }
+    if (g == 2 && sub == 2 && rho > 0.0) {
+        *f = -26.10066441 * sqrt(rho) + 0.4688963869 * rho * rho;
+        *df = -13.050332205 / sqrt(rho) + 2.0 * 0.4688963869 * rho;
+    }
+    return 0;
+}
+
 int orc_pot_eval(int pot, const double *prm, double r, double *potr, double *fpotr,
                  double *potb, double *fpotb)
 {

@@ -100,6 +100,12 @@ int    orc_setfl_tables(int nrho, double drho, int nr, double cutoff, const doub
                         const double *rhor, const double *rphi, int ntab, double *potr, double *fpotr,
                         double *potb, double *fpotb, double *fembd, double *dfembd);
 
+/* Bonny W-H-He EAM (EAM1_WHeH_Bonny_JPCM26_2014.F90, EAM_ForceTable_Bonny_JPCM26_2014.F90):
+ * pair/density functions of table t (registration order, 1-based) and the embedding of group g
+ * (1 W, 2 H, 3 He) for subtype sub (1 EAM1, 2 EAM2), Angstrom / eV, POTR = V/2 conventions. */
+int    orc_bonny_pair(int sub, int t, double r, double *potr, double *fpotr, double *potb, double *fpotb);
+int    orc_bonny_embed(int sub, int g, double rho, double *f, double *df);
+
 /* The same natural cubic spline on arbitrary increasing knots x_0 < ... < x_{n-1} (the lspt
  * ".spt" files, Filedatas_Func_Lspt.F90:304-324 with the settings of :24-34):
  *   orc_spline_knots:      second derivatives m (m[0] = m[n-1] = 0)

@@ -51,6 +51,8 @@ def lib():
         _lib.orc_spline_eval.restype = C.c_double
         _lib.orc_setfl_tables.restype = C.c_int
         _lib.orc_spline_knots.restype = None
+        _lib.orc_bonny_pair.restype = C.c_int
+        _lib.orc_bonny_embed.restype = C.c_int
         _lib.orc_spline_knots_eval.restype = None
         _lib.orc_pot_eval.restype = C.c_int
         _lib.orc_embed_eval.restype = C.c_int
@@ -313,6 +315,33 @@ def lspt_tables(d, ntab=10000, nembd=10000, rhoscal=20.0, rmax=None):
     return dict(potr=potr, fpotr=fpotr, potb=potb, fpotb=fpotb, fembd=fembd, dfembd=dfembd,
                 rhod=rhod, kpair=kpair, kembd=np.arange(1, ne + 1, dtype=np.int32), ntab=ntab,
                 nembd=nembd, rmax=rmax)
+
+
+def bonny_tables(sub, rmax=5.4604375, ntab=10000, nembd=10000, rhoscal=20.0):
+    """Bonny W-H-He EAM tables (sub 1 = EAM1, 2 = EAM2): NKIND = 9 (10) pair/density tables on
+    the sqrt(r) grid up to rmax, POTR = (V/2) r, FPOTR = -V' r, POTB = rho, FPOTB = -rho'
+    (Create_Pairwise_ForceTable, MD_TypeDef_ForceTable.F90:949-976); embedding tables of W, H,
+    He on RHOD = rhoscal * max POTB / nembd (:965, 1040-1048); KPAIR(I, J) = (I-1)*3 + J with
+    I the host (groups W, H, He)."""
+    nk = 10 if sub == 2 else 9
+    r = (np.arange(1, ntab + 1) * (np.sqrt(rmax) / ntab)) ** 2
+    out = {k: np.zeros((ntab, nk)) for k in ("potr", "fpotr", "potb", "fpotb")}
+    a, b, c, d = C.c_double(), C.c_double(), C.c_double(), C.c_double()
+    for t in range(nk):
+        for i, ri in enumerate(r):
+            if lib().orc_bonny_pair(sub, t + 1, C.c_double(ri), C.byref(a), C.byref(b), C.byref(c), C.byref(d)):
+                raise RuntimeError("unknown Bonny table")
+            out["potr"][i, t], out["fpotr"][i, t] = a.value * ri, b.value * ri
+            out["potb"][i, t], out["fpotb"][i, t] = c.value, d.value
+    rhod = rhoscal * out["potb"].max() / nembd
+    fe, dfe = np.zeros((nembd, 3)), np.zeros((nembd, 3))
+    for g in range(3):
+        for i in range(nembd):
+            lib().orc_bonny_embed(sub, g + 1, C.c_double(i * rhod), C.byref(a), C.byref(b))
+            fe[i, g], dfe[i, g] = a.value, b.value
+    out.update(fembd=fe, dfembd=dfe, rhod=rhod, nkind=nk, rmax=rmax,
+               kpair=np.arange(1, 10, dtype=np.int32).reshape(3, 3), kembd=np.arange(1, 4, dtype=np.int32))
+    return out
 
 
 def make_box(lo, length, ifpd=(1, 1, 1)):
