@@ -296,6 +296,9 @@ int  msmgb_calforce_noalloc(const msmgb_force_noalloc *args);
 #define MSMGB_POT_DERLET_WW   4   /* Derlet-Nguyen-Manh-Dudarev W, FS form (FS_PM_WW.F90)      */
 #define MSMGB_POT_HEHE_EXP6   5   /* He-He ZBL / cubic / EXP6, no density (ZBL_EXP6_HeHe.F90)  */
 #define MSMGB_POT_HEW_ZBL     6   /* He-W ZBL / cubics / EXP6, no density (ZBL_ABINTIO_He_W_930.F90) */
+/* the other subtypes of EAM_WW_Marinica_JPCM25_2013 (EAM_ForceTable_Marinica_JPCM25_2013.F90:31-44) */
+#define MSMGB_POT_MARINICA3   7   /* Marinica EAM3 for W (EAM form); prm unused              */
+#define MSMGB_POT_MARINICA4   8   /* Marinica EAM4 for W (EAM form); prm unused              */
 /* Fills POTR/FPOTR/POTB/FPOTB (ntab each) and, if fembd/dfembd are non-NULL, F/F' (nembd
  * each); returns RHOD = rhoscal * max(POTB) / nembd through *rhod.  Lengths in Angstrom,
  * energies in eV. */

@@ -39,27 +39,55 @@ PairVal cleri_rosato(double r, const double *prm)
     return o;
 }
 
-// Marinica EAM2.  The knot radii are single-precision literals in the reference source, so
-// their values are the float roundings of the printed decimals.
-const double kMarA[15] = {0.960851701343041e2, -0.184410923895214e3, 0.935784079613550e2,
-                          -0.798358265041677e1, 0.747034092936229e1, -0.152756043708453e1,
-                          0.125205932634393e1, 0.163082162159425e1, -0.141854775352260e1,
-                          -0.819936046256149e0, 0.198013514305908e1, -0.696430179520267e0,
-                          0.304546909722160e-1, -0.163131143161660e1, 0.138409896486177e1};
-const float kMarR[15] = {2.5648975f, 2.629795f, 2.6946925f, 2.8663175f, 2.973045f,
-                         3.0797725f, 3.5164725f, 3.846445f, 4.1764175f, 4.700845f,
-                         4.8953f, 5.089755f, 5.3429525f, 5.401695f, 5.4604375f};
-const double kMarB[4] = {-0.420429107805055e1, 0.518217702261442e0, 0.562720834534370e-1,
-                         0.344164178842340e-1};
-const float kMarRB[4] = {2.5f, 3.1f, 3.5f, 4.9f};
-const double kMarRC = 2.002970124727;
-const double kMarF[2] = {-5.946454472402710, -0.049477376935239};
+// Marinica EAM2, EAM3, EAM4 for W (EAM2/3/4_WW_Marinica_JPCM25_2013.F90): V a sum of 14-15
+// cubic knots, rho of 4 knots frozen below RC = 2.002970124727 A, F = f1 sqrt(rho) + f2 rho^2.
+// Literals without an exponent letter in those files are single precision and are written
+// here as float literals: EAM2's knot radii, EAM3's knot radii and embedding coefficients,
+// EAM4's pair knot radii.
+struct MarSet {
+    int nv;
+    double a[15], r[15], b[4], rb[4], f[2];
+};
 
-void cubic_knots(double rt, const double *a, const float *ri, int n, double *v, double *f)
+const MarSet kMar[3] = {
+    {15,
+     {0.960851701343041e2, -0.184410923895214e3, 0.935784079613550e2, -0.798358265041677e1,
+      0.747034092936229e1, -0.152756043708453e1, 0.125205932634393e1, 0.163082162159425e1,
+      -0.141854775352260e1, -0.819936046256149e0, 0.198013514305908e1, -0.696430179520267e0,
+      0.304546909722160e-1, -0.163131143161660e1, 0.138409896486177e1},
+     {2.5648975f, 2.629795f, 2.6946925f, 2.8663175f, 2.973045f, 3.0797725f, 3.5164725f, 3.846445f,
+      4.1764175f, 4.700845f, 4.8953f, 5.089755f, 5.3429525f, 5.401695f, 5.4604375f},
+     {-0.420429107805055e1, 0.518217702261442e0, 0.562720834534370e-1, 0.344164178842340e-1},
+     {2.5f, 3.1f, 3.5f, 4.9f},
+     {-5.946454472402710, -0.049477376935239}},
+    {14,
+     {0.335180090207171e3, -0.630187843239795e3, 0.351436490059390e3, -0.187104554936536e-1,
+      0.599698179163370e-1, -0.210635074070024e-1, 0.258575483268791e-1, 0.389896994857220e-1,
+      -0.139737073858817e-1, 0.184785876328131e-1, -0.505971175928021e0, -0.890738292956047e1,
+      0.495992901621487e-1, 0.377639491131043e-1},
+     {2.61f, 2.68f, 2.71816025391593f, 2.75852291093924f, 2.89242768139096f, 3.4015171088841f,
+      3.67528316716263f, 4.24839261315764f, 4.63102917008654f, 4.82264509508677f, 5.02121483593414f,
+      5.2828858486271f, 5.28302924730536f, 5.29092563021923f},
+     {-0.420429107805055e-1, 0.518217702261442e0, 0.562720834534370e-1, 0.344164178842340e-1},
+     {2.5f, 3.1f, 3.5f, 4.9f},
+     {-5.0732379057085f, -0.039263610952181f}},
+    {15,
+     {0.954071477542914e2, -0.181161004448916e3, 0.930215233132627e2, -0.108428907515182e2,
+      0.112027468539573e2, -0.312459176640227e1, 0.123028140617302e1, 0.154767467307454e1,
+      -0.128861387780439e1, -0.843327493551467e0, 0.214009882965042e1, -0.102898314532388e1,
+      0.138163259601912e1, -0.360872433001551e1, 0.217655968740690e1},
+     {2.5648975f, 2.629795f, 2.6946925f, 2.8663175f, 2.973045f, 3.0797725f, 3.5164725f, 3.846445f,
+      4.1764175f, 4.700845f, 4.8953f, 5.089755f, 5.3429525f, 5.401695f, 5.4604375f},
+     {-0.420429107805055e-1, 0.518217702261442e0, 0.562720834534370e-1, 0.344164178842340e-1},
+     {2.5, 3.1, 3.5, 4.9},
+     {-5.553986589859130, -0.045691157657292}}};
+const double kMarRC = 2.002970124727;
+
+void cubic_knots(double rt, const double *a, const double *ri, int n, double *v, double *f)
 {
     double p = 0.0, d = 0.0;
     for (int i = 0; i < n; ++i) {
-        double r = (double)ri[i];
+        double r = ri[i];
         double stp = (r - rt) >= 0.0 ? 1.0 : 0.0;
         p = p + a[i] * (r - rt) * (r - rt) * (r - rt) * stp;
         d = d + a[i] * (r - rt) * (r - rt) * stp;
@@ -68,28 +96,31 @@ void cubic_knots(double rt, const double *a, const float *ri, int n, double *v, 
     *f = 3.0 * d;
 }
 
-PairVal marinica2(double r)
+PairVal marinica(const MarSet &m, double r)
 {
     PairVal o;
     double v, f;
-    cubic_knots(r, kMarA, kMarR, 15, &v, &f);
+    cubic_knots(r, m.a, m.r, m.nv, &v, &f);
     o.potr = 0.5 * v;            // NN_FuncPoly3 returns 0.5 V and -V'
     o.fpotr = f;
     if (r <= kMarRC) {           // density frozen inside RC
-        cubic_knots(kMarRC, kMarB, kMarRB, 4, &o.potb, &o.fpotb);
+        cubic_knots(kMarRC, m.b, m.rb, 4, &o.potb, &o.fpotb);
         o.fpotb = 0.0;
     } else {
-        cubic_knots(r, kMarB, kMarRB, 4, &o.potb, &o.fpotb);
+        cubic_knots(r, m.b, m.rb, 4, &o.potb, &o.fpotb);
     }
     return o;
 }
 
-void marinica2_embed(double rho, double *f, double *df)
+void marinica_embed(const MarSet &m, double rho, double *f, double *df)
 {
     if (rho <= 0.0) { *f = 0.0; *df = 0.0; return; }
-    *f = kMarF[0] * std::sqrt(rho) + kMarF[1] * rho * rho;
-    *df = 0.5 * kMarF[0] / std::sqrt(rho) + 2.0 * kMarF[1] * rho;
+    *f = m.f[0] * std::sqrt(rho) + m.f[1] * rho * rho;
+    *df = 0.5 * m.f[0] / std::sqrt(rho) + 2.0 * m.f[1] * rho;
 }
+
+PairVal marinica2(double r) { return marinica(kMar[0], r); }
+void marinica2_embed(double rho, double *f, double *df) { marinica_embed(kMar[0], rho, f, df); }
 
 PairVal ackland_ww(double r)
 {
@@ -346,7 +377,7 @@ extern "C" int msmgb_create_forcetable(int pot, const double *prm, double rmax, 
 {
     if (ntab < 2 || rmax <= 0.0 || !potr || !fpotr || !potb || !fpotb) return MSMGB_ERR_ARG;
     if (pot == MSMGB_POT_CR && !prm) return MSMGB_ERR_ARG;
-    if (pot < MSMGB_POT_CR || pot > MSMGB_POT_HEW_ZBL) return MSMGB_ERR_ARG;
+    if (pot < MSMGB_POT_CR || pot > MSMGB_POT_MARINICA4) return MSMGB_ERR_ARG;
     const double csi = (double)ntab / std::sqrt(rmax);
     const double csiv = 1.0 / csi;
     double rhomx = -1.0;
@@ -357,6 +388,8 @@ extern "C" int msmgb_create_forcetable(int pot, const double *prm, double rmax, 
         switch (pot) {
         case MSMGB_POT_CR: v = cleri_rosato(r, prm); break;
         case MSMGB_POT_MARINICA2: v = marinica2(r); break;
+        case MSMGB_POT_MARINICA3: v = marinica(kMar[1], r); break;
+        case MSMGB_POT_MARINICA4: v = marinica(kMar[2], r); break;
         case MSMGB_POT_ACKLAND_WW: v = ackland_ww(r); break;
         case MSMGB_POT_DERLET_WW: v = derlet_ww(r); break;
         case MSMGB_POT_HEHE_EXP6: v = hehe_exp6(r); break;
@@ -373,8 +406,9 @@ extern "C" int msmgb_create_forcetable(int pot, const double *prm, double rmax, 
     if (fembd && dfembd && nembd > 0) {
         for (int i = 1; i <= nembd; ++i) {
             double rho = (double)(i - 1) * rd;
-            if (pot == MSMGB_POT_MARINICA2) {
-                marinica2_embed(rho, &fembd[i - 1], &dfembd[i - 1]);
+            if (pot == MSMGB_POT_MARINICA2 || pot == MSMGB_POT_MARINICA3 || pot == MSMGB_POT_MARINICA4) {
+                const int set = pot == MSMGB_POT_MARINICA2 ? 0 : pot == MSMGB_POT_MARINICA3 ? 1 : 2;
+                marinica_embed(kMar[set], rho, &fembd[i - 1], &dfembd[i - 1]);
             } else {
                 fembd[i - 1] = 0.0;
                 dfembd[i - 1] = 0.0;

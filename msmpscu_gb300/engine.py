@@ -127,10 +127,11 @@ class ForceTable:
         return cls(L.POT_CR, [A, xi, p, q, r0], rc, rc, L.FS_TYPE, ntab=ntab, nembd=ntab)
 
     @classmethod
-    def marinica_eam2(cls, rc=5.4604375, ntab=10000, nembd=10000, rhoscal=20.0):
-        """Marinica EAM2 for W (EAM type)."""
-        return cls(L.POT_MARINICA2, None, rc, rc, L.EAM_TYPE, ntab=ntab, nembd=nembd,
-                   rhoscal=rhoscal)
+    def marinica_eam2(cls, rc=5.4604375, ntab=10000, nembd=10000, rhoscal=20.0, subtype="EAM2"):
+        """Marinica W (EAM type), subtype EAM2 (the reference's default), EAM3 or EAM4
+        (EAM_ForceTable_Marinica_JPCM25_2013.F90:31-44)."""
+        pot = {"EAM2": L.POT_MARINICA2, "EAM3": L.POT_MARINICA3, "EAM4": L.POT_MARINICA4}[subtype.upper()]
+        return cls(pot, None, rc, rc, L.EAM_TYPE, ntab=ntab, nembd=nembd, rhoscal=rhoscal)
 
     @classmethod
     def ackland_ww(cls, rmax, ru=None, ntab=10000):

@@ -52,77 +52,112 @@ static void cr_ne(double r, const double *prm, double *potb, double *fpotb)
     *fpotb = rho * qsr0 * 2.0;
 }
 
-/* Marinica EAM2 W, EAM2_WW_Marinica_JPCM25_2013.F90:17-116 through the cubic-knot helpers
- * of MD_Pot_EAM_Utilities.F90:48-85 (returns 0.5 V and -V') and 259-290 (rho, -rho').
- * The knot radii are written in the reference as default-REAL literals (no D exponent),
- * so their values are the single-precision roundings; that is reproduced with (float). */
-static const double mar_afai[15] = {
-    0.960851701343041e2, -0.184410923895214e3, 0.935784079613550e2, -0.798358265041677e1,
-    0.747034092936229e1, -0.152756043708453e1, 0.125205932634393e1, 0.163082162159425e1,
-    -0.141854775352260e1, -0.819936046256149e0, 0.198013514305908e1, -0.696430179520267e0,
-    0.304546909722160e-1, -0.163131143161660e1, 0.138409896486177e1};
-static const float mar_afair[15] = {
-    2.564897500000000f, 2.629795000000000f, 2.694692500000000f, 2.866317500000000f,
-    2.973045000000000f, 3.079772500000000f, 3.516472500000000f, 3.846445000000000f,
-    4.176417500000000f, 4.700845000000000f, 4.895300000000000f, 5.089755000000000f,
-    5.342952500000000f, 5.401695000000000f, 5.460437500000000f};
-static const double mar_arho[4] = {-0.420429107805055e1, 0.518217702261442e0,
-                                   0.562720834534370e-1, 0.344164178842340e-1};
-static const float mar_arhor[4] = {2.500000000000000f, 3.100000000000000f,
-                                   3.500000000000000f, 4.900000000000000f};
+/* Marinica EAM2/EAM3/EAM4 W (EAM2_WW_Marinica_JPCM25_2013.F90:17-116 and the EAM3, EAM4
+ * files of the same folder) through the cubic-knot helpers of MD_Pot_EAM_Utilities.F90:48-85
+ * (returns 0.5 V and -V') and 259-290 (rho, -rho').  Literals written without a D exponent
+ * in the reference are default REAL, i.e. single precision; those are given here as float
+ * literals (f suffix) and widened: EAM2's knot radii, EAM3's knot radii and embedding
+ * coefficients, EAM4's pair knot radii. */
+typedef struct {
+    int nv;
+    double a[15], r[15];      /* pair knots */
+    double b[4], rb[4];       /* density knots */
+    double f[2];              /* embedding: f1 sqrt(rho) + f2 rho^2 */
+} mar_set_t;
+
 static const double mar_rc = 2.002970124727;
-static const double mar_af[2] = {-5.946454472402710, -0.049477376935239};
+
+static const mar_set_t mar_sets[3] = {
+    {15,
+     {0.960851701343041e2, -0.184410923895214e3, 0.935784079613550e2, -0.798358265041677e1,
+      0.747034092936229e1, -0.152756043708453e1, 0.125205932634393e1, 0.163082162159425e1,
+      -0.141854775352260e1, -0.819936046256149e0, 0.198013514305908e1, -0.696430179520267e0,
+      0.304546909722160e-1, -0.163131143161660e1, 0.138409896486177e1},
+     {2.564897500000000f, 2.629795000000000f, 2.694692500000000f, 2.866317500000000f,
+      2.973045000000000f, 3.079772500000000f, 3.516472500000000f, 3.846445000000000f,
+      4.176417500000000f, 4.700845000000000f, 4.895300000000000f, 5.089755000000000f,
+      5.342952500000000f, 5.401695000000000f, 5.460437500000000f},
+     {-0.420429107805055e1, 0.518217702261442e0, 0.562720834534370e-1, 0.344164178842340e-1},
+     {2.500000000000000f, 3.100000000000000f, 3.500000000000000f, 4.900000000000000f},
+     {-5.946454472402710, -0.049477376935239}},
+    {14,
+     {0.335180090207171e3, -0.630187843239795e3, 0.351436490059390e3, -0.187104554936536e-1,
+      0.599698179163370e-1, -0.210635074070024e-1, 0.258575483268791e-1, 0.389896994857220e-1,
+      -0.139737073858817e-1, 0.184785876328131e-1, -0.505971175928021e0, -0.890738292956047e1,
+      0.495992901621487e-1, 0.377639491131043e-1},
+     {2.610000000000000f, 2.680000000000000f, 2.718160253915930f, 2.758522910939240f,
+      2.892427681390960f, 3.401517108884100f, 3.675283167162630f, 4.248392613157640f,
+      4.631029170086540f, 4.822645095086770f, 5.021214835934140f, 5.282885848627100f,
+      5.283029247305360f, 5.290925630219230f},
+     {-0.420429107805055e-1, 0.518217702261442e0, 0.562720834534370e-1, 0.344164178842340e-1},
+     {2.500000000000000f, 3.100000000000000f, 3.500000000000000f, 4.900000000000000f},
+     {-5.073237905708500f, -0.039263610952181f}},
+    {15,
+     {0.954071477542914e2, -0.181161004448916e3, 0.930215233132627e2, -0.108428907515182e2,
+      0.112027468539573e2, -0.312459176640227e1, 0.123028140617302e1, 0.154767467307454e1,
+      -0.128861387780439e1, -0.843327493551467e0, 0.214009882965042e1, -0.102898314532388e1,
+      0.138163259601912e1, -0.360872433001551e1, 0.217655968740690e1},
+     {2.564897500000000f, 2.629795000000000f, 2.694692500000000f, 2.866317500000000f,
+      2.973045000000000f, 3.079772500000000f, 3.516472500000000f, 3.846445000000000f,
+      4.176417500000000f, 4.700845000000000f, 4.895300000000000f, 5.089755000000000f,
+      5.342952500000000f, 5.401695000000000f, 5.460437500000000f},
+     {-0.420429107805055e-1, 0.518217702261442e0, 0.562720834534370e-1, 0.344164178842340e-1},
+     {2.5, 3.1, 3.5, 4.9},
+     {-5.553986589859130, -0.045691157657292}}};
 
 static double step_h(double x) { return x >= 0.0 ? 1.0 : 0.0; }   /* MD_Pot_EAM_Utilities.F90:35-44 */
 
-static void mar_nn(double rt, double *potr, double *fpotr)
+static void mar_set_nn(const mar_set_t *m, double rt, double *potr, double *fpotr)
 {
     double p = 0.0, f = 0.0;
-    for (int i = 0; i < 15; ++i) {
-        double ri = (double)mar_afair[i];
-        double stp = step_h(ri - rt);
-        p = p + mar_afai[i] * (ri - rt) * (ri - rt) * (ri - rt) * stp;
-        f = f + mar_afai[i] * (ri - rt) * (ri - rt) * stp;
+    for (int i = 0; i < m->nv; ++i) {
+        const double ri = m->r[i], stp = step_h(ri - rt);
+        p = p + m->a[i] * (ri - rt) * (ri - rt) * (ri - rt) * stp;
+        f = f + m->a[i] * (ri - rt) * (ri - rt) * stp;
     }
     *potr = 0.5 * p;
     *fpotr = 3.0 * f;
 }
 
-static void mar_rho_poly(double rt, double *potb, double *fpotb)
+static void mar_set_rho(const mar_set_t *m, double rt, double *potb, double *fpotb)
 {
     double p = 0.0, f = 0.0;
     for (int i = 0; i < 4; ++i) {
-        double ri = (double)mar_arhor[i];
-        double stp = step_h(ri - rt);
-        p = p + mar_arho[i] * (ri - rt) * (ri - rt) * (ri - rt) * stp;
-        f = f + mar_arho[i] * (ri - rt) * (ri - rt) * stp;
+        const double ri = m->rb[i], stp = step_h(ri - rt);
+        p = p + m->b[i] * (ri - rt) * (ri - rt) * (ri - rt) * stp;
+        f = f + m->b[i] * (ri - rt) * (ri - rt) * stp;
     }
     *potb = p;
     *fpotb = 3.0 * f;
 }
 
-static void mar_ne(double r, double *potb, double *fpotb)
+/* density frozen inside RC (EAM2_WW_Marinica_JPCM25_2013.F90:83-88, the same in EAM3/EAM4) */
+static void mar_set_ne(const mar_set_t *m, double r, double *potb, double *fpotb)
 {
-    if (r <= mar_rc) {            /* density frozen inside RC, EAM2_WW_Marinica_JPCM25_2013.F90:83-88 */
-        mar_rho_poly(mar_rc, potb, fpotb);
+    if (r <= mar_rc) {
+        mar_set_rho(m, mar_rc, potb, fpotb);
         *fpotb = 0.0;
     } else {
-        mar_rho_poly(r, potb, fpotb);
+        mar_set_rho(m, r, potb, fpotb);
     }
 }
 
 /* EMBED_FS_PLOY_Func, MD_Pot_EAM_Utilities.F90:332-368: F = a1 sqrt(rho) + a2 rho^2 */
-static void mar_embed(double rho, double *f, double *df)
+static void mar_set_embed(const mar_set_t *m, double rho, double *f, double *df)
 {
     if (rho <= 0.0) { *f = 0.0; *df = 0.0; return; }
     double trho = rho;
-    double fr = mar_af[0] * sqrt(trho);
-    double dfr = 0.5 * mar_af[0] / sqrt(trho);
-    fr = fr + mar_af[1] * rho * trho;
-    dfr = dfr + 2.0 * mar_af[1] * trho;
+    double fr = m->f[0] * sqrt(trho);
+    double dfr = 0.5 * m->f[0] / sqrt(trho);
+    fr = fr + m->f[1] * rho * trho;
+    dfr = dfr + 2.0 * m->f[1] * trho;
     *f = fr;
     *df = dfr;
 }
+
+static void mar_nn(double r, double *potr, double *fpotr) { mar_set_nn(&mar_sets[0], r, potr, fpotr); }
+static void mar_ne(double r, double *potb, double *fpotb) { mar_set_ne(&mar_sets[0], r, potb, fpotb); }
+static void mar_embed(double rho, double *f, double *df) { mar_set_embed(&mar_sets[0], rho, f, df); }
 
 /* Ackland-Thetford W-W (FS form), EM_TB_WangJun_W-HE_2010/FS_Ackland_WW.F90:23-88, restated
  * in Angstrom / eV (the reference's CGS constants divided out). */
@@ -387,6 +422,13 @@ int orc_pot_eval(int pot, const double *prm, double r, double *potr, double *fpo
     switch (pot) {
     case ORC_POT_CR: cr_nn(r, prm, potr, fpotr); cr_ne(r, prm, potb, fpotb); return 0;
     case ORC_POT_MARINICA2: mar_nn(r, potr, fpotr); mar_ne(r, potb, fpotb); return 0;
+    case ORC_POT_MARINICA3:
+    case ORC_POT_MARINICA4: {
+        const mar_set_t *m = &mar_sets[pot == ORC_POT_MARINICA3 ? 1 : 2];
+        mar_set_nn(m, r, potr, fpotr);
+        mar_set_ne(m, r, potb, fpotb);
+        return 0;
+    }
     case ORC_POT_ACKLAND_WW: ack_nn(r, potr, fpotr); ack_ne(r, potb, fpotb); return 0;
     case ORC_POT_DERLET_WW: der_nn(r, potr, fpotr); der_ne(r, potb, fpotb); return 0;
     case ORC_POT_HEHE_EXP6: hehe_nn(r, potr, fpotr); zero_ne(r, potb, fpotb); return 0;
@@ -399,6 +441,8 @@ int orc_embed_eval(int pot, const double *prm, double rho, double *f, double *df
 {
     (void)prm;
     if (pot == ORC_POT_MARINICA2) { mar_embed(rho, f, df); return 0; }
+    if (pot == ORC_POT_MARINICA3) { mar_set_embed(&mar_sets[1], rho, f, df); return 0; }
+    if (pot == ORC_POT_MARINICA4) { mar_set_embed(&mar_sets[2], rho, f, df); return 0; }
     *f = 0.0; *df = 0.0;
     return -1;
 }

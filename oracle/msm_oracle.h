@@ -44,6 +44,8 @@ extern "C" {
 #define ORC_POT_DERLET_WW   4   /* Derlet-Nguyen-Manh-Dudarev W (FS form), FS_PM_WW.F90 */
 #define ORC_POT_HEHE_EXP6   5   /* He-He ZBL / cubic / EXP6 (no density), ZBL_EXP6_HeHe.F90 */
 #define ORC_POT_HEW_ZBL     6   /* He-W ZBL / cubics / EXP6 (no density), ZBL_ABINTIO_He_W_930.F90 */
+#define ORC_POT_MARINICA3   7   /* Marinica EAM3 W (EAM form), EAM3_WW_Marinica_JPCM25_2013.F90 */
+#define ORC_POT_MARINICA4   8   /* Marinica EAM4 W (EAM form), EAM4_WW_Marinica_JPCM25_2013.F90 */
 
 #define ORC_FS  0
 #define ORC_EAM 1

@@ -61,6 +61,12 @@ def test_table_generator_matches_oracle(lib, oracle):
     for k in ("potr", "fpotr", "potb", "fpotb", "fembd", "dfembd"):
         np.testing.assert_allclose(getattr(w, k), o[k], rtol=1e-15, atol=1e-300)
     assert w.rhod == o["rhod"]
+    for sub, pot in (("EAM3", oracle.POT_MARINICA3), ("EAM4", oracle.POT_MARINICA4)):
+        w = ForceTable.marinica_eam2(subtype=sub)
+        o = oracle.make_tables(pot, None, lt.W_RC, 10000, 10000, 20.0)
+        for k in ("potr", "fpotr", "potb", "fpotb", "fembd", "dfembd"):
+            np.testing.assert_allclose(getattr(w, k), o[k], rtol=1e-13, atol=1e-13 * np.abs(o[k]).max())
+        assert w.rhod == pytest.approx(o["rhod"], rel=1e-15)
 
 
 def test_table_generator_rejects_unknown_potential(lib):

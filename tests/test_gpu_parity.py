@@ -82,12 +82,15 @@ def test_fs_force_energy_virial_parity(oracle):
     e.close()
 
 
-def test_eam_force_parity_w_sia(oracle):
+@pytest.mark.parametrize("subtype", ["EAM2", "EAM3", "EAM4"])
+def test_eam_force_parity_w_sia(oracle, subtype):
     pos, L_ = lt.w_sia_config(8, 0.02, 3)                # 1,025 atoms with a <111> dumbbell
-    t = w_tables(oracle)
+    pot = {"EAM2": oracle.POT_MARINICA2, "EAM3": oracle.POT_MARINICA3, "EAM4": oracle.POT_MARINICA4}[subtype]
+    t = oracle.Tables(oracle.make_tables(pot, None, lt.W_RC, 10000, 10000, 20.0, want_embed=True),
+                      oracle.EAM, lt.W_RC)
     ref, _, _ = _oracle_force(oracle, pos, L_, t, rc_nl=lt.W_RC_NL, mxk=128)
     e = Engine(len(pos), lt.W_RC_NL, mxkvois=96)
-    e.init_forcetable(ForceTable.marinica_eam2())
+    e.init_forcetable(ForceTable.marinica_eam2(subtype=subtype))
     e.copyin(_box(len(pos), L_), pos)
     vir = e.calptensor()[0]
     assert rel_err(e.get_force(), ref["f"]) < TOL
