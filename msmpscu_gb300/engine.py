@@ -127,6 +127,28 @@ class ForceTable:
         return cls(L.POT_CR, [A, xi, p, q, r0], rc, rc, L.FS_TYPE, ntab=ntab, nembd=ntab)
 
     @classmethod
+    def cleri_rosato_element(cls, element, rc, ntab=10000):
+        """The reference's Cleri-Rosato library EM_TB_Cleri_Rosato_PRB48_22 (Al, Au, Ti;
+        EM_TB_ForcetTable_CR_2014.F90:31-36), FS type with a hard cutoff rc.  Parameters as
+        the reference holds them: Al's lattice constant 4.050 (TB_CR_AlAl.F90:13) and all of
+        Ti's constants (TB_CR_TiTi.F90:10-16) are single-precision literals, and Ti's
+        r0 = 2.951 A * sqrt(1/3 + beta^2/4) is evaluated in single precision."""
+        f32 = np.float32
+        halfrsq2 = 0.707106781187                                  # CP_HALFRSQ2
+        if element == "Al":
+            prm = [0.1221, 1.316, 8.612, 2.516, float(f32(4.050)) * halfrsq2]
+        elif element == "Au":
+            prm = [0.2061, 1.790, 10.229, 4.036, 4.079 * halfrsq2]
+        elif element == "Ti":
+            beta = f32(1.5874)
+            fac = np.sqrt(f32(1.0) / f32(3.0) + beta * beta / f32(4.0), dtype=np.float32)
+            prm = [float(f32(0.1519)), float(f32(1.8112)), float(f32(8.620)), float(f32(2.390)),
+                   2.951 * float(fac)]
+        else:
+            raise ValueError("the Cleri-Rosato library holds Al, Au and Ti")
+        return cls(L.POT_CR, prm, rc, rc, L.FS_TYPE, ntab=ntab, nembd=ntab)
+
+    @classmethod
     def marinica_eam2(cls, rc=5.4604375, ntab=10000, nembd=10000, rhoscal=20.0, subtype="EAM2"):
         """Marinica W (EAM type), subtype EAM2 (the reference's default), EAM3 or EAM4
         (EAM_ForceTable_Marinica_JPCM25_2013.F90:31-44)."""

@@ -73,3 +73,31 @@ def test_table_generator_rejects_unknown_potential(lib):
     z = np.zeros(10)
     d = z.ctypes.data_as(C.POINTER(C.c_double))
     assert lib.msmgb_create_forcetable(99, None, 5.0, 10, 10, 20.0, d, d, d, d, None, None, None) == L.ERR_ARG
+
+
+@pytest.mark.parametrize("element,a,ecoh", [("Al", 4.05, -3.317), ("Au", 4.079, -3.778)])
+def test_cleri_rosato_library_elements(oracle, element, a, ecoh):
+    """Al and Au of the reference's Cleri-Rosato library: library tables equal the oracle's
+    CR restatement with the same parameters, and the perfect fcc lattice has zero force and
+    the Cleri-Rosato cohesive energy at a three-shell cutoff."""
+    ft = ForceTable.cleri_rosato_element(element, rc=1.3 * a)
+    o = oracle.make_tables(oracle.POT_CR, list(ft.prm), ft.rmax, 10000, 10000, 20.0, want_embed=False)
+    for k in ("potr", "fpotr", "potb", "fpotb"):
+        np.testing.assert_allclose(getattr(ft, k), o[k], rtol=1e-15, atol=0)
+    pos, L_ = lt.fcc(5, 5, 5, a)
+    n = len(pos)
+    t = oracle.Tables(o, oracle.FS, ft.rmax)
+    box = oracle.make_box([0, 0, 0], L_)
+    st = np.ones(n, np.int32)
+    kv, ind = oracle.nlist(pos, st, box, ft.rmax + 0.3, 128)
+    r = oracle.force(pos, np.ones(n, np.int32), st, box, kv, ind, t)
+    assert np.abs(r["f"]).max() < 1e-10
+    assert r["epot"].mean() == pytest.approx(ecoh, abs=2e-3)
+
+
+def test_cleri_rosato_library_ti_single_precision_constants():
+    ft = ForceTable.cleri_rosato_element("Ti", rc=5.0)
+    assert ft.prm[0] == float(np.float32(0.1519)) and ft.prm[2] == float(np.float32(8.620))
+    assert ft.prm[4] == pytest.approx(2.951 * np.sqrt(1 / 3 + 1.5874 ** 2 / 4), rel=1e-6)
+    with pytest.raises(ValueError):
+        ForceTable.cleri_rosato_element("Cu", rc=5.0)
