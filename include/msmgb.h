@@ -299,6 +299,10 @@ int  msmgb_calforce_noalloc(const msmgb_force_noalloc *args);
 /* the other subtypes of EAM_WW_Marinica_JPCM25_2013 (EAM_ForceTable_Marinica_JPCM25_2013.F90:31-44) */
 #define MSMGB_POT_MARINICA3   7   /* Marinica EAM3 for W (EAM form); prm unused              */
 #define MSMGB_POT_MARINICA4   8   /* Marinica EAM4 for W (EAM form); prm unused              */
+/* EM_TB_Ackland_Vitek_PRB41_10324 (EM_TB_ForceTable_Ackland_Vitek_PRB41_10324.F90), FS form */
+#define MSMGB_POT_AV_CU       9   /* Cu-Cu                                                   */
+#define MSMGB_POT_AV_AU      10   /* Au-Au                                                   */
+#define MSMGB_POT_AV_CUAU    11   /* Cu-Au cross pair and density sqrt(rho_Cu rho_Au)        */
 /* Fills POTR/FPOTR/POTB/FPOTB (ntab each) and, if fembd/dfembd are non-NULL, F/F' (nembd
  * each); returns RHOD = rhoscal * max(POTB) / nembd through *rhod.  Lengths in Angstrom,
  * energies in eV. */

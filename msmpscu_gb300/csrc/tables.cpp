@@ -289,6 +289,154 @@ PairVal hew_zbl(double r_a)
     return to_ev(p, f);
 }
 
+// Ackland-Vitek Cu, Au and Cu-Au (EM_TB_Ackland_Vitek_PRB41_10324, FS form), evaluated in the
+// reference's CGS units as written and converted on return.  Pair: Moliere screened Coulomb
+// below R11, a fitted cubic to R21, then V/2 = sum_k AR_k (RCR_k - r)^3 over the knots above r;
+// density: sum_k AT_k (RCT_k - r)^3 (Cu, Au) or the geometric mean sqrt(rho_Cu rho_Au) of the
+// two (Cu-Au).  Single-precision literals of the source (Cu and Au knot coefficients and
+// radii, Cu's screening length, the 0.3 of every Moliere derivative) are float literals here.
+// The Cu-Au density derivative is written as 1.5 sum A A (X + Y) (X Y)^2 without the division
+// by sqrt(P) (EM_TB_CuAu_Ackland_Vitek_PRB41_10324.F90:180-197); in CGS that is ~1e-24 of the
+// true derivative, and it is kept so.
+struct AVSet {
+    double rrfit, ar[6], rcr[6], at[2], rct[2], r11, r21, as, z1, z2, ca[4];
+};
+
+AVSet av_cu()
+{
+    const double rr = 3.615e-08, e = kEVERG;
+    const float a[6] = {61.73525861f, -108.1846780f, 57.00053948f, -12.88796578f, 39.163819010f, 0.0f};
+    const float m[6] = {1.225f, 1.202f, 1.154f, 1.050f, 0.866f, 0.707f};
+    AVSet s{};
+    s.rrfit = rr;
+    for (int k = 0; k < 6; ++k) {
+        s.ar[k] = (double)a[k] * e * 0.5 / (rr * rr * rr);
+        s.rcr[k] = (double)m[k] * rr;
+    }
+    s.at[0] = (double)10.03718305f * (e * e) / (rr * rr * rr);
+    s.at[1] = (double)17.06363299f * (e * e) / (rr * rr * rr);
+    s.rct[0] = (double)1.225f * rr;
+    s.rct[1] = (double)0.990f * rr;
+    s.r11 = 1.65e-8;
+    s.r21 = 1.90e-8;
+    s.as = (double)0.0738f * 1.0e-8;
+    s.z1 = s.z2 = 29.0;
+    s.ca[0] = 0.825015e-09; s.ca[1] = -0.130825; s.ca[2] = 0.696400e+07; s.ca[3] = -0.124069e+15;
+    return s;
+}
+
+AVSet av_au()
+{
+    const double rr = 4.078e-08, e = kEVERG;
+    const float a[6] = {29.059066f, -153.14779f, 148.17881f, -22.20508f, 72.71465f, 199.26269f};
+    const float m[6] = {1.2247449f, 1.1547054f, 1.1180065f, 1.0000000f, 0.8660254f, 0.7071068f};
+    AVSet s{};
+    s.rrfit = rr;
+    for (int k = 0; k < 6; ++k) {
+        s.ar[k] = (double)a[k] * e * 0.5 / (rr * rr * rr);
+        s.rcr[k] = (double)m[k] * rr;
+    }
+    s.at[0] = (double)21.930125f * (e * e) / (rr * rr * rr);
+    s.at[1] = (double)284.99631f * (e * e) / (rr * rr * rr);
+    s.rct[0] = (double)1.1180065f * rr;
+    s.rct[1] = (double)0.8660254f * rr;
+    s.r11 = 1.85e-8;
+    s.r21 = 2.10e-8;
+    s.as = 0.0752 * 1.0e-8;
+    s.z1 = s.z2 = 79.0;
+    s.ca[0] = 0.333482e-08; s.ca[1] = -0.476248; s.ca[2] = 0.228187e+08; s.ca[3] = -0.365939e+15;
+    return s;
+}
+
+AVSet av_cuau()
+{
+    const double e = kEVERG;
+    AVSet s{};
+    const double a[3] = {-0.0855455166e24, 0.1928358800e24, 0.7593228600e24};
+    const double rc[3] = {4.3098160e-08, 4.0474790e-08, 3.2979464e-08};
+    for (int k = 0; k < 3; ++k) {
+        s.ar[k] = a[k] * e * 0.5;
+        s.rcr[k] = rc[k];
+    }
+    s.r11 = 1.85e-8;
+    s.r21 = 2.05e-8;
+    s.as = 0.0745 * 1.0e-8;
+    s.z1 = 29.0;
+    s.z2 = 79.0;
+    s.ca[0] = 0.172724e-08; s.ca[1] = -0.253573; s.ca[2] = 0.124675e+08; s.ca[3] = -0.204896e+15;
+    return s;
+}
+
+void av_pair_cgs(const AVSet &s, double r, double *potr, double *fpotr)
+{
+    if (r < s.r11) {
+        const double zze2 = 9.0e9 * s.z1 * s.z2 * 1.6029e-19 * 1.6029e-19 * 1.0e9;
+        const double be1 = std::exp(-0.3 * r / s.as), be2 = std::pow(be1, 4.0), be3 = std::pow(be2, 5.0);
+        const double tp = zze2 * (0.35 * be1 + 0.55 * be2 + 0.1 * be3) / r;
+        *potr = tp / 2.0;
+        *fpotr = tp / r + zze2 * (0.35 * (double)0.3f * be1 + 0.55 * 1.2 * be2 + 0.1 * 6.0 * be3) / (r * s.as);
+    } else if (r < s.r21) {
+        *potr = (s.ca[0] + s.ca[1] * r + s.ca[2] * r * r + s.ca[3] * r * r * r) / 2.0;
+        *fpotr = -(s.ca[1] + 2.0 * s.ca[2] * r + 3.0 * s.ca[3] * r * r);
+    } else {
+        double p = 0.0, f = 0.0;
+        for (int k = 0; k < 6; ++k)
+            if (r < s.rcr[k]) {
+                p += s.ar[k] * std::pow(s.rcr[k] - r, 3.0);
+                f += 6.0 * s.ar[k] * std::pow(s.rcr[k] - r, 2.0);
+            }
+        *potr = p;
+        *fpotr = f;
+    }
+}
+
+void av_rho_cgs(const AVSet &s, double r, double *potb, double *fpotb)
+{
+    *potb = 0.0;
+    *fpotb = 0.0;
+    for (int k = 0; k < 2; ++k)
+        if (r > 0.0 && r < s.rct[k]) {
+            *potb += s.at[k] * std::pow(s.rct[k] - r, 3.0);
+            *fpotb += 3.0 * s.at[k] * std::pow(s.rct[k] - r, 2.0);
+        }
+}
+
+PairVal ackland_vitek(int which, double r_a)
+{
+    const double r = r_a * 1e-8;
+    const AVSet s = which == 0 ? av_cu() : which == 1 ? av_au() : av_cuau();
+    double p, f, b = 0.0, db = 0.0;
+    av_pair_cgs(s, r, &p, &f);
+    if (which < 2) {
+        av_rho_cgs(s, r, &b, &db);
+    } else {
+        const AVSet cu = av_cu(), au = av_au();
+        const double x1 = cu.rct[0] - r, y1 = cu.rct[1] - r, x2 = au.rct[0] - r, y2 = au.rct[1] - r;
+        double q = 0.0, dq = 0.0;
+        if (r > 0.0 && r < au.rct[1]) {
+            q = au.at[0] * cu.at[0] * std::pow(x2 * x1, 3.0) + au.at[0] * cu.at[1] * std::pow(x2 * y1, 3.0) +
+                au.at[1] * cu.at[0] * std::pow(y2 * x1, 3.0) + au.at[1] * cu.at[1] * std::pow(y2 * y1, 3.0);
+            dq = 1.5 * au.at[0] * cu.at[0] * (x2 + x1) * std::pow(x2 * x1, 2.0) +
+                 1.5 * au.at[0] * cu.at[1] * (x2 + y1) * std::pow(x2 * y1, 2.0) +
+                 1.5 * au.at[1] * cu.at[0] * (y2 + x1) * std::pow(y2 * x1, 2.0) +
+                 1.5 * au.at[1] * cu.at[1] * (y2 + y1) * std::pow(y2 * y1, 2.0);
+        } else if (r >= au.rct[1] && r < cu.rct[1]) {
+            q = au.at[0] * cu.at[0] * std::pow(x2 * x1, 3.0) + au.at[0] * cu.at[1] * std::pow(x2 * y1, 3.0);
+            dq = 1.5 * au.at[0] * cu.at[0] * (x2 + x1) * std::pow(x2 * x1, 2.0) +
+                 1.5 * au.at[0] * cu.at[1] * (x2 + y1) * std::pow(x2 * y1, 2.0);
+        } else if (r >= cu.rct[1] && r < cu.rct[0]) {
+            q = au.at[0] * cu.at[0] * std::pow(x2 * x1, 3.0);
+            dq = 1.5 * au.at[0] * cu.at[0] * (x2 + x1) * std::pow(x2 * x1, 2.0);
+        }
+        b = q > 0.0 ? std::sqrt(q) : 0.0;
+        db = dq;
+    }
+    PairVal o = to_ev(p, f);
+    o.potb = b / (kEVERG * kEVERG);
+    o.fpotb = db / (kEVERG * kEVERG) * 1e-8;
+    return o;
+}
+
 // Bonny, Grigorev, Terentyev W-H-He EAM (EAM_WHeH_Bonny_JPCM26_2014), subtypes EAM1 and EAM2
 // (EAM1_WHeH_Bonny_JPCM26_2014.F90).  W-W is Marinica EAM2 under a gauge transformation
 // (:15-104); the other pairs are sums of cubic knots (NN_FuncPoly3,
@@ -377,7 +525,7 @@ extern "C" int msmgb_create_forcetable(int pot, const double *prm, double rmax, 
 {
     if (ntab < 2 || rmax <= 0.0 || !potr || !fpotr || !potb || !fpotb) return MSMGB_ERR_ARG;
     if (pot == MSMGB_POT_CR && !prm) return MSMGB_ERR_ARG;
-    if (pot < MSMGB_POT_CR || pot > MSMGB_POT_MARINICA4) return MSMGB_ERR_ARG;
+    if (pot < MSMGB_POT_CR || pot > MSMGB_POT_AV_CUAU) return MSMGB_ERR_ARG;
     const double csi = (double)ntab / std::sqrt(rmax);
     const double csiv = 1.0 / csi;
     double rhomx = -1.0;
@@ -390,6 +538,9 @@ extern "C" int msmgb_create_forcetable(int pot, const double *prm, double rmax, 
         case MSMGB_POT_MARINICA2: v = marinica2(r); break;
         case MSMGB_POT_MARINICA3: v = marinica(kMar[1], r); break;
         case MSMGB_POT_MARINICA4: v = marinica(kMar[2], r); break;
+        case MSMGB_POT_AV_CU: v = ackland_vitek(0, r); break;
+        case MSMGB_POT_AV_AU: v = ackland_vitek(1, r); break;
+        case MSMGB_POT_AV_CUAU: v = ackland_vitek(2, r); break;
         case MSMGB_POT_ACKLAND_WW: v = ackland_ww(r); break;
         case MSMGB_POT_DERLET_WW: v = derlet_ww(r); break;
         case MSMGB_POT_HEHE_EXP6: v = hehe_exp6(r); break;

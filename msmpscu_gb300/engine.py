@@ -181,6 +181,25 @@ class ForceTable:
         return self
 
     @classmethod
+    def ackland_vitek(cls, rmax, ru=None, ntab=10000):
+        """The reference's Cu-Au FS library EM_TB_Ackland_Vitek_PRB41_10324
+        (EM_TB_ForceTable_Ackland_Vitek_PRB41_10324.F90): tables #1 Cu-Cu, #2 Au-Au,
+        #3 (Au neighbour of a Cu host) and #4 (Cu neighbour of an Au host), both the Cu-Au
+        cross functions.  Groups Cu = 1, Au = 2: KPAIR(1,1) = 1, KPAIR(2,2) = 2,
+        KPAIR(1,2) = 3, KPAIR(2,1) = 4."""
+        pots = [L.POT_AV_CU, L.POT_AV_AU, L.POT_AV_CUAU, L.POT_AV_CUAU]
+        parts = [cls(p, None, rmax, ru if ru else rmax, L.FS_TYPE, ntab=ntab) for p in pots]
+        self = parts[0]
+        for key in ("potr", "fpotr", "potb", "fpotb"):
+            setattr(self, key, np.stack([getattr(t, key) for t in parts], 1).reshape(-1).copy())
+        self.pot = None
+        self.nkind, self.ngroup, self.nkind1 = 4, 2, 1
+        kp = np.array([[1, 3], [4, 2]], np.int32)           # KPAIR(I, J) at kp[I-1, J-1]
+        self._kpair = np.ascontiguousarray(kp.T).reshape(-1)
+        self._kembd = np.ones(2, np.int32)
+        return self
+
+    @classmethod
     def bonny_wheh(cls, subtype="EAM1", rmax=5.4604375, ntab=10000, nembd=10000, rhoscal=20.0):
         """The reference's W-H-He EAM of Bonny, Grigorev, Terentyev (EAM_WHeH_Bonny_JPCM26_2014),
         subtype "EAM1" (H, He pair-only) or "EAM2" (H embedded in the W density); groups

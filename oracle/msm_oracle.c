@@ -416,12 +416,114 @@ int orc_bonny_embed(int sub, int g, double rho, double *f, double *df)
     return 0;
 }
 
+/* Ackland-Vitek Cu, Au, Cu-Au (EM_TB_{CuCu,AuAu,CuAu}_Ackland_Vitek_PRB41_10324.F90), FS form,
+ * restated in Angstrom / eV.  Source literals without a D exponent are single precision
+ * (float literals here).  The Cu-Au density derivative of the reference (:180-197) is
+ * 1.5 sum A A (X+Y) (XY)^2 in its CGS units, i.e. 1.5 EVERG^2 sum A A (X+Y) (XY)^2 in eV / A
+ * with A in eV^2/A^3; reproduced as such. */
+typedef struct {
+    double ar[6], rcr[6], at[2], rct[2], r11, r21, as, zz, c[4];
+} av_t;
+
+static av_t av_params(int which)
+{
+    const double ev = 1.60219e-12;
+    av_t p;
+    memset(&p, 0, sizeof(p));
+    if (which == 0) {
+        const double rr = 3.615;
+        const float a[6] = {61.73525861f, -108.1846780f, 57.00053948f, -12.88796578f, 39.163819010f, 0.0f};
+        const float m[6] = {1.225f, 1.202f, 1.154f, 1.050f, 0.866f, 0.707f};
+        for (int k = 0; k < 6; ++k) { p.ar[k] = 0.5 * a[k] / (rr * rr * rr); p.rcr[k] = m[k] * rr; }
+        p.at[0] = 10.03718305f / (rr * rr * rr); p.rct[0] = 1.225f * rr;
+        p.at[1] = 17.06363299f / (rr * rr * rr); p.rct[1] = 0.990f * rr;
+        p.r11 = 1.65; p.r21 = 1.90; p.as = 0.0738f; p.zz = 29.0 * 29.0;
+        p.c[0] = 0.825015e-09; p.c[1] = -0.130825; p.c[2] = 0.696400e+07; p.c[3] = -0.124069e+15;
+    } else if (which == 1) {
+        const double rr = 4.078;
+        const float a[6] = {29.059066f, -153.14779f, 148.17881f, -22.20508f, 72.71465f, 199.26269f};
+        const float m[6] = {1.2247449f, 1.1547054f, 1.1180065f, 1.0000000f, 0.8660254f, 0.7071068f};
+        for (int k = 0; k < 6; ++k) { p.ar[k] = 0.5 * a[k] / (rr * rr * rr); p.rcr[k] = m[k] * rr; }
+        p.at[0] = 21.930125f / (rr * rr * rr); p.rct[0] = 1.1180065f * rr;
+        p.at[1] = 284.99631f / (rr * rr * rr); p.rct[1] = 0.8660254f * rr;
+        p.r11 = 1.85; p.r21 = 2.10; p.as = 0.0752; p.zz = 79.0 * 79.0;
+        p.c[0] = 0.333482e-08; p.c[1] = -0.476248; p.c[2] = 0.228187e+08; p.c[3] = -0.365939e+15;
+    } else {
+        p.ar[0] = -0.0855455166 * 0.5; p.rcr[0] = 4.3098160;
+        p.ar[1] = 0.1928358800 * 0.5;  p.rcr[1] = 4.0474790;
+        p.ar[2] = 0.7593228600 * 0.5;  p.rcr[2] = 3.2979464;
+        p.r11 = 1.85; p.r21 = 2.05; p.as = 0.0745; p.zz = 29.0 * 79.0;
+        p.c[0] = 0.172724e-08; p.c[1] = -0.253573; p.c[2] = 0.124675e+08; p.c[3] = -0.204896e+15;
+    }
+    /* the cubic bridge's CGS coefficients in eV, eV/A, eV/A^2, eV/A^3 */
+    p.c[0] /= ev; p.c[1] *= 1e-8 / ev; p.c[2] *= 1e-16 / ev; p.c[3] *= 1e-24 / ev;
+    return p;
+}
+
+static void av_nn(int which, double r, double *potr, double *fpotr)
+{
+    const av_t p = av_params(which);
+    if (r < p.r11) {
+        /* Moliere: k e^2 with k = 9e9, e = 1.6029e-19 C (the source's values), in eV*A */
+        const double ke2 = 9.0e9 * 1.6029e-19 * 1.6029e-19 * 1e9 / 1.60219e-12 * 1e8 * p.zz;
+        const double x = r / p.as;
+        const double s = 0.35 * exp(-0.3 * x) + 0.55 * exp(-1.2 * x) + 0.1 * exp(-6.0 * x);
+        const double ds = 0.35 * (double)0.3f * exp(-0.3 * x) + 0.55 * 1.2 * exp(-1.2 * x) + 0.1 * 6.0 * exp(-6.0 * x);
+        *potr = 0.5 * ke2 * s / r;
+        *fpotr = ke2 * s / (r * r) + ke2 * ds / (r * p.as);
+    } else if (r < p.r21) {
+        *potr = 0.5 * (p.c[0] + r * (p.c[1] + r * (p.c[2] + r * p.c[3])));
+        *fpotr = -(p.c[1] + r * (2.0 * p.c[2] + 3.0 * p.c[3] * r));
+    } else {
+        double v = 0.0, d = 0.0;
+        for (int k = 0; k < 6; ++k) {
+            if (!(r < p.rcr[k])) continue;
+            const double t = p.rcr[k] - r;
+            v += p.ar[k] * t * t * t;
+            d += 6.0 * p.ar[k] * t * t;
+        }
+        *potr = v;
+        *fpotr = d;
+    }
+}
+
+static void av_ne(int which, double r, double *potb, double *fpotb)
+{
+    *potb = *fpotb = 0.0;
+    if (which < 2) {
+        const av_t p = av_params(which);
+        for (int k = 0; k < 2; ++k) {
+            if (!(r > 0.0 && r < p.rct[k])) continue;
+            const double t = p.rct[k] - r;
+            *potb += p.at[k] * t * t * t;
+            *fpotb += 3.0 * p.at[k] * t * t;
+        }
+        return;
+    }
+    const av_t cu = av_params(0), au = av_params(1);
+    const double xc[2] = {cu.rct[0] - r, cu.rct[1] - r}, xa[2] = {au.rct[0] - r, au.rct[1] - r};
+    double q = 0.0, dq = 0.0;
+    for (int a = 0; a < 2; ++a)
+        for (int c = 0; c < 2; ++c) {
+            if (!(r > 0.0 && xa[a] > 0.0 && xc[c] > 0.0)) continue;
+            const double pr = xa[a] * xc[c];
+            q += au.at[a] * cu.at[c] * pr * pr * pr;
+            dq += 1.5 * au.at[a] * cu.at[c] * (xa[a] + xc[c]) * pr * pr;
+        }
+    if (r >= cu.rct[0]) { q = 0.0; dq = 0.0; }    /* no branch of the source beyond Cu's RCT1 */
+    *potb = sqrt(q);
+    *fpotb = dq * 1.60219e-12 * 1.60219e-12;
+}
+
 int orc_pot_eval(int pot, const double *prm, double r, double *potr, double *fpotr,
                  double *potb, double *fpotb)
 {
     switch (pot) {
     case ORC_POT_CR: cr_nn(r, prm, potr, fpotr); cr_ne(r, prm, potb, fpotb); return 0;
     case ORC_POT_MARINICA2: mar_nn(r, potr, fpotr); mar_ne(r, potb, fpotb); return 0;
+    case ORC_POT_AV_CU: av_nn(0, r, potr, fpotr); av_ne(0, r, potb, fpotb); return 0;
+    case ORC_POT_AV_AU: av_nn(1, r, potr, fpotr); av_ne(1, r, potb, fpotb); return 0;
+    case ORC_POT_AV_CUAU: av_nn(2, r, potr, fpotr); av_ne(2, r, potb, fpotb); return 0;
     case ORC_POT_MARINICA3:
     case ORC_POT_MARINICA4: {
         const mar_set_t *m = &mar_sets[pot == ORC_POT_MARINICA3 ? 1 : 2];

@@ -46,6 +46,9 @@ extern "C" {
 #define ORC_POT_HEW_ZBL     6   /* He-W ZBL / cubics / EXP6 (no density), ZBL_ABINTIO_He_W_930.F90 */
 #define ORC_POT_MARINICA3   7   /* Marinica EAM3 W (EAM form), EAM3_WW_Marinica_JPCM25_2013.F90 */
 #define ORC_POT_MARINICA4   8   /* Marinica EAM4 W (EAM form), EAM4_WW_Marinica_JPCM25_2013.F90 */
+#define ORC_POT_AV_CU       9   /* Ackland-Vitek Cu (FS form), EM_TB_CuCu_Ackland_Vitek_PRB41_10324.F90 */
+#define ORC_POT_AV_AU      10   /* Ackland-Vitek Au (FS form), EM_TB_AuAu_Ackland_Vitek_PRB41_10324.F90 */
+#define ORC_POT_AV_CUAU    11   /* Ackland-Vitek Cu-Au (FS form), EM_TB_CuAu_Ackland_Vitek_PRB41_10324.F90 */
 
 #define ORC_FS  0
 #define ORC_EAM 1

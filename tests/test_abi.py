@@ -101,3 +101,28 @@ def test_cleri_rosato_library_ti_single_precision_constants():
     assert ft.prm[4] == pytest.approx(2.951 * np.sqrt(1 / 3 + 1.5874 ** 2 / 4), rel=1e-6)
     with pytest.raises(ValueError):
         ForceTable.cleri_rosato_element("Cu", rc=5.0)
+
+
+@pytest.mark.parametrize("pot,a,ecoh", [("POT_AV_CU", 3.615, -3.518), ("POT_AV_AU", 4.078, -3.789),
+                                        ("POT_AV_CUAU", None, None)])
+def test_ackland_vitek_tables(oracle, pot, a, ecoh):
+    """Ackland-Vitek Cu, Au and Cu-Au: the library's CGS evaluation equals the oracle's
+    Angstrom/eV restatement; the pure metals have zero force and their cohesive energy on the
+    perfect fcc lattice."""
+    ft = ForceTable(getattr(L, pot), None, 6.0, 6.0, L.FS_TYPE)
+    o = oracle.make_tables(getattr(oracle, pot), None, 6.0, 10000, 10000, 20.0, want_embed=False)
+    for k in ("potr", "fpotr", "potb", "fpotb"):
+        assert np.max(np.abs(getattr(ft, k) - o[k])) <= 1e-14 * np.max(np.abs(o[k])), k
+    if a is None:
+        # the cross density's derivative of the reference carries a factor EVERG^2 (CGS)
+        assert 0.0 < np.max(np.abs(o["fpotb"])) < 1e-18 < np.max(o["potb"])
+        return
+    pos, L_ = lt.fcc(5, 5, 5, a)
+    n = len(pos)
+    t = oracle.Tables(o, oracle.FS, 6.0)
+    box = oracle.make_box([0, 0, 0], L_)
+    st = np.ones(n, np.int32)
+    kv, ind = oracle.nlist(pos, st, box, 6.3, 200)
+    r = oracle.force(pos, np.ones(n, np.int32), st, box, kv, ind, t)
+    assert np.abs(r["f"]).max() < 1e-10
+    assert r["epot"].mean() == pytest.approx(ecoh, abs=2e-3)

@@ -1,0 +1,52 @@
+"""GPU parity for the remaining potential libraries of the reference on multi-species boxes:
+Ackland-Vitek Cu-Au (FS, four tables, geometric-mean cross density) on an L1_2 Cu3Au
+crystal with displacements.  The oracle tabulates the functions independently."""
+import numpy as np
+import pytest
+
+from msmpscu_gb300 import Engine, ForceTable, lattice as lt
+from tests.helpers import rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+def _cu3au(ncell, a, sigma, seed):
+    pos, L_ = lt.fcc(ncell, ncell, ncell, a)
+    # in each cubic cell the corner site is Au, the three face centres Cu (L1_2)
+    ityp = np.ones(len(pos), np.int32)
+    frac = (pos / a) % 1.0
+    ityp[np.all(np.abs(frac) < 1e-6, axis=1)] = 2
+    pos = pos + np.random.default_rng(seed).normal(scale=sigma, size=pos.shape)
+    return pos - np.floor(pos / L_) * L_, ityp, L_
+
+
+def test_ackland_vitek_cu3au_force_parity(oracle):
+    rc = 5.5
+    ft = ForceTable.ackland_vitek(rmax=rc)
+    pots = [oracle.POT_AV_CU, oracle.POT_AV_AU, oracle.POT_AV_CUAU, oracle.POT_AV_CUAU]
+    ts = [oracle.make_tables(p, None, rc, 10000, 10000, 20.0, want_embed=False) for p in pots]
+    arr = {k: np.stack([t[k] for t in ts], 1) for k in ("potr", "fpotr", "potb", "fpotb")}
+    t = oracle.RawTables(oracle.FS, 10000, 4, rc, rc, arr["potr"], arr["fpotr"], arr["potb"], arr["fpotb"],
+                         np.array([[1, 3], [4, 2]]))
+    pos, ityp, L_ = _cu3au(7, 3.75, 0.05, 4)
+    assert (ityp == 2).sum() * 4 == len(pos)
+    n = len(pos)
+    rc_nl = rc + 0.3
+    box = oracle.make_box([0, 0, 0], L_)
+    st = np.ones(n, np.int32)
+    kv, ind = oracle.nlist(pos, st, box, rc_nl, 200)
+    ref = oracle.force(pos, ityp, st, box, kv, ind, t)
+    for precision in ("fp64", "ff", "mixed"):
+        e = Engine(n, rc_nl, mxkvois=128, precision=precision)
+        e.init_forcetable(ft)
+        e.set_masses(np.array([63.546, 196.97]) * lt.AMU)
+        e.copyin([(n, (0, 0, 0), tuple(L_), (1, 1, 1))], pos, ityp=ityp)
+        e.calforce()
+        f = e.get_force()
+        if precision == "mixed":
+            assert np.abs(f - ref["f"]).max() / np.abs(ref["f"]).max() < 1e-6
+        else:
+            assert rel_err(f, ref["f"]) < 1e-10, precision
+            e.calepot()
+            assert rel_err(e.get_epot(), ref["epot"]) < 1e-10, precision
+        e.close()
