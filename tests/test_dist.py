@@ -29,7 +29,7 @@ def _worker(rank, world, port, out):
 def test_replica_aggregation_two_ranks():
     import random
     port = 29500 + random.randint(0, 2000)
-    mgr = mp.Manager()
+    mgr = mp.get_context("spawn").Manager()          # no fork of a threaded process
     out = mgr.dict()
     mp.spawn(_worker, args=(2, port, out), nprocs=2, join=True)
     for r in range(2):
