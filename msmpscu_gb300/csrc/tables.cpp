@@ -437,6 +437,83 @@ PairVal ackland_vitek(int which, double r_a)
     return o;
 }
 
+// Mendelev-Ackland Zr EAM (EAM_ZrZr_Mendelev_Phil_Mag_L87_2007.F90:18-150), in Angstrom / eV
+// like the source: a screened Coulomb pair below 1 A, exp(cubic) to 2.3 A, then sums of
+// (r_k - r)^n knots (n = 4..8); density knots at 5.6 A; F = -sqrt(rho) + sum_k c_k (rho - rho_k)^4.
+// Single-precision literals of the source (the four screening weights and the knot radii
+// 2.3, 5.6, 7.6) are float literals here.  H(x) = [x >= 0], H0(x) = [x > 0] (:172-192).
+// F'(0) is -0.5/sqrt(0) = -inf in the first embedding row, as in the reference.
+PairVal mendelev_zr(double r)
+{
+    auto H = [](double x) { return x >= 0.0 ? 1.0 : 0.0; };
+    auto H0 = [](double x) { return x > 0.0 ? 1.0 : 0.0; };
+    const double w[4] = {0.1818f, 0.5099f, 0.2802f, 0.02817f};
+    const double b[4] = {3.3035595072498e+01, 9.7279503865046e+00, 4.1593878920967e+00, 2.0812424895674e+00};
+    const double k23 = 2.3000f, k56 = 5.6f, k76 = 7.6f;
+    const double kn[3] = {3.5, 6.0, k76};
+    const double c[3][5] = {
+        {-1.4261501929757e+01, 1.5850036758176e+01, -1.1325102264291e+01, -4.0971114831366e+00, 3.6739378016909e+00},
+        {1.3066813393823e+00, -6.0542710718094e-01, 1.0055527194350e+00, -1.4918186777562e-01, 3.2773112059590e-02},
+        {1.1433120304691e-02, -2.1982172508973e-02, -1.2542439692607e-02, 2.5062673874258e-02, -7.5442887837418e-03}};
+    double v = 0.0, f = 0.0;
+    if (H0(1.0 - r) > 0.0) {
+        double s = 0.0, ds = 0.0;
+        for (int k = 0; k < 4; ++k) {
+            s += w[k] * std::exp(-b[k] * r);
+            ds += (1.0 / r + b[k]) * w[k] * std::exp(-b[k] * r);
+        }
+        v += 2.3039613229091e+04 / r * s;
+        f += 2.3039613229091e+04 / r * ds;
+    }
+    if (H(r - 1.0) * H0(k23 - r) > 0.0) {
+        const double e = std::exp(1.2333392307614e+01 - 1.0847321969086e+01 * r + 4.5733524424508e+00 * r * r -
+                                  8.5266291445935e-01 * r * r * r);
+        v += e;
+        f -= (-1.0847321969086e+01 + 9.1467048849017e+00 * r - 2.5579887433781e+00 * r * r) * e;
+    }
+    if (H(r - k23) > 0.0) {
+        for (int g = 0; g < 3; ++g) {
+            const double x = kn[g] - r;
+            if (H(x) == 0.0) continue;
+            double p = x * x * x;                       // x^3
+            for (int n = 4; n <= 8; ++n) {
+                f += c[g][n - 4] * n * p;
+                p *= x;
+                v += c[g][n - 4] * p;
+            }
+        }
+    }
+    PairVal o{0.5 * v, f, 0.0, 0.0};
+    const double cr[5] = {7.7718711248373e-01, -4.8102928454986e-01, 1.4501312593993e-01, -2.1292226813959e-02,
+                          1.2209217625670e-03};
+    const double x = k56 - r;
+    if (H(x) > 0.0) {
+        double p = x * x * x;
+        for (int n = 4; n <= 8; ++n) {
+            o.fpotb += cr[n - 4] * n * p;
+            p *= x;
+            o.potb += cr[n - 4] * p;
+        }
+    }
+    return o;
+}
+
+void mendelev_zr_embed(double rho, double *f, double *df)
+{
+    const double kr[5] = {60.0, 70.0, 80.0, 85.0, 90.0};
+    const double kc[5] = {-1.9162462126235e-07, 4.6418727035037e-07, 6.6448294272955e-07, -2.0680252960229e-06,
+                          1.1387131464983e-06};
+    double a = -std::pow(rho, 0.5), d = -0.5 / std::pow(rho, 0.5);
+    for (int k = 0; k < 5; ++k) {
+        const double x = rho - kr[k];
+        if (x < 0.0) continue;
+        a += kc[k] * x * x * x * x;
+        d += 4.0 * kc[k] * x * x * x;
+    }
+    *f = a;
+    *df = d;
+}
+
 // Bonny, Grigorev, Terentyev W-H-He EAM (EAM_WHeH_Bonny_JPCM26_2014), subtypes EAM1 and EAM2
 // (EAM1_WHeH_Bonny_JPCM26_2014.F90).  W-W is Marinica EAM2 under a gauge transformation
 // (:15-104); the other pairs are sums of cubic knots (NN_FuncPoly3,
@@ -525,7 +602,7 @@ extern "C" int msmgb_create_forcetable(int pot, const double *prm, double rmax, 
 {
     if (ntab < 2 || rmax <= 0.0 || !potr || !fpotr || !potb || !fpotb) return MSMGB_ERR_ARG;
     if (pot == MSMGB_POT_CR && !prm) return MSMGB_ERR_ARG;
-    if (pot < MSMGB_POT_CR || pot > MSMGB_POT_AV_CUAU) return MSMGB_ERR_ARG;
+    if (pot < MSMGB_POT_CR || pot > MSMGB_POT_MENDELEV_ZR) return MSMGB_ERR_ARG;
     const double csi = (double)ntab / std::sqrt(rmax);
     const double csiv = 1.0 / csi;
     double rhomx = -1.0;
@@ -541,6 +618,7 @@ extern "C" int msmgb_create_forcetable(int pot, const double *prm, double rmax, 
         case MSMGB_POT_AV_CU: v = ackland_vitek(0, r); break;
         case MSMGB_POT_AV_AU: v = ackland_vitek(1, r); break;
         case MSMGB_POT_AV_CUAU: v = ackland_vitek(2, r); break;
+        case MSMGB_POT_MENDELEV_ZR: v = mendelev_zr(r); break;
         case MSMGB_POT_ACKLAND_WW: v = ackland_ww(r); break;
         case MSMGB_POT_DERLET_WW: v = derlet_ww(r); break;
         case MSMGB_POT_HEHE_EXP6: v = hehe_exp6(r); break;
@@ -560,6 +638,8 @@ extern "C" int msmgb_create_forcetable(int pot, const double *prm, double rmax, 
             if (pot == MSMGB_POT_MARINICA2 || pot == MSMGB_POT_MARINICA3 || pot == MSMGB_POT_MARINICA4) {
                 const int set = pot == MSMGB_POT_MARINICA2 ? 0 : pot == MSMGB_POT_MARINICA3 ? 1 : 2;
                 marinica_embed(kMar[set], rho, &fembd[i - 1], &dfembd[i - 1]);
+            } else if (pot == MSMGB_POT_MENDELEV_ZR) {
+                mendelev_zr_embed(rho, &fembd[i - 1], &dfembd[i - 1]);
             } else {
                 fembd[i - 1] = 0.0;
                 dfembd[i - 1] = 0.0;

@@ -181,6 +181,12 @@ class ForceTable:
         return self
 
     @classmethod
+    def mendelev_zr(cls, rc=7.6, ntab=10000, nembd=10000, rhoscal=20.0):
+        """Mendelev-Ackland Zr (EAM type), the reference's EAM_Zr_Mendelev_Phil_Mag_L87_2007;
+        its pair knots end at 7.6 A."""
+        return cls(L.POT_MENDELEV_ZR, None, rc, rc, L.EAM_TYPE, ntab=ntab, nembd=nembd, rhoscal=rhoscal)
+
+    @classmethod
     def ackland_vitek(cls, rmax, ru=None, ntab=10000):
         """The reference's Cu-Au FS library EM_TB_Ackland_Vitek_PRB41_10324
         (EM_TB_ForceTable_Ackland_Vitek_PRB41_10324.F90): tables #1 Cu-Cu, #2 Au-Au,

@@ -37,6 +37,15 @@ def bcc(nx, ny, nz, a):
     return pos, np.array([nx * a, ny * a, nz * a])
 
 
+def hcp(nx, ny, nz, a, c):
+    """hcp in its orthorhombic cell (a, a sqrt(3), c) of four atoms."""
+    base = np.array([[0, 0, 0], [0.5, 0.5, 0], [0.5, 5.0 / 6.0, 0.5], [0, 1.0 / 3.0, 0.5]])
+    cell = np.array([a, a * np.sqrt(3.0), c])
+    g = np.stack(np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing="ij"), -1).reshape(-1, 1, 3)
+    pos = ((g + base[None]) * cell).reshape(-1, 3)
+    return pos, cell * np.array([nx, ny, nz])
+
+
 def wrap(pos, lo, length):
     return lo + np.mod(pos - lo, length)
 

@@ -515,6 +515,75 @@ static void av_ne(int which, double r, double *potb, double *fpotb)
     *fpotb = dq * 1.60219e-12 * 1.60219e-12;
 }
 
+/* Mendelev-Ackland Zr EAM, EAM_ZrZr_Mendelev_Phil_Mag_L87_2007.F90:18-150 (Angstrom / eV in the
+ * source itself).  Float literals: the source's default-REAL constants (0.1818, 0.5099, 0.2802,
+ * 0.02817, 2.3000, 5.6, 7.6).  Step functions: [x >= 0] and, at 1 A and 2.3 A upper ends, [x > 0]. */
+static double zr_knots(const double *c, double k, double r, double *mdv)
+{
+    double v = 0.0, d = 0.0;
+    if (k - r >= 0.0)
+        for (int n = 4; n <= 8; ++n) {
+            v += c[n - 4] * pow(k - r, (double)n);
+            d += c[n - 4] * n * pow(k - r, (double)(n - 1));
+        }
+    *mdv = d;
+    return v;
+}
+
+static void zr_nn(double r, double *potr, double *fpotr)
+{
+    static const double c35[5] = {-1.4261501929757e+01, 1.5850036758176e+01, -1.1325102264291e+01,
+                                  -4.0971114831366e+00, 3.6739378016909e+00};
+    static const double c60[5] = {1.3066813393823e+00, -6.0542710718094e-01, 1.0055527194350e+00,
+                                  -1.4918186777562e-01, 3.2773112059590e-02};
+    static const double c76[5] = {1.1433120304691e-02, -2.1982172508973e-02, -1.2542439692607e-02,
+                                  2.5062673874258e-02, -7.5442887837418e-03};
+    const double r23 = 2.3000f;
+    double v = 0.0, d = 0.0;
+    if (1.0 - r > 0.0) {
+        const double q = 2.3039613229091e+04;
+        const double t1 = 0.1818f * exp(-3.3035595072498e+01 * r), t2 = 0.5099f * exp(-9.7279503865046e+00 * r);
+        const double t3 = 0.2802f * exp(-4.1593878920967e+00 * r), t4 = 0.02817f * exp(-2.0812424895674e+00 * r);
+        v += q / r * (t1 + t2 + t3 + t4);
+        d += q / r * ((1.0 / r + 3.3035595072498e+01) * t1 + (1.0 / r + 9.7279503865046e+00) * t2 +
+                      (1.0 / r + 4.1593878920967e+00) * t3 + (1.0 / r + 2.0812424895674e+00) * t4);
+    }
+    if (r - 1.0 >= 0.0 && r23 - r > 0.0) {
+        const double pe = 1.2333392307614e+01 - 1.0847321969086e+01 * r + 4.5733524424508e+00 * r * r -
+                          8.5266291445935e-01 * r * r * r;
+        v += exp(pe);
+        d -= (-1.0847321969086e+01 + 9.1467048849017e+00 * r - 2.5579887433781e+00 * r * r) * exp(pe);
+    }
+    if (r - r23 >= 0.0) {
+        double d1, d2, d3;
+        v += zr_knots(c35, 3.5, r, &d1) + zr_knots(c60, 6.0, r, &d2) + zr_knots(c76, (double)7.6f, r, &d3);
+        d += d1 + d2 + d3;
+    }
+    *potr = 0.5 * v;
+    *fpotr = d;
+}
+
+static void zr_ne(double r, double *potb, double *fpotb)
+{
+    static const double cr[5] = {7.7718711248373e-01, -4.8102928454986e-01, 1.4501312593993e-01,
+                                 -2.1292226813959e-02, 1.2209217625670e-03};
+    *potb = zr_knots(cr, (double)5.6f, r, fpotb);
+}
+
+static void zr_embed(double rho, double *f, double *df)
+{
+    static const double rk[5] = {60.0, 70.0, 80.0, 85.0, 90.0};
+    static const double ck[5] = {-1.9162462126235e-07, 4.6418727035037e-07, 6.6448294272955e-07,
+                                 -2.0680252960229e-06, 1.1387131464983e-06};
+    *f = -pow(rho, 0.5);
+    *df = -0.5 / pow(rho, 0.5);                 /* -inf at rho = 0, as in the reference */
+    for (int k = 0; k < 5; ++k) {
+        if (rho - rk[k] < 0.0) continue;
+        *f += ck[k] * pow(rho - rk[k], 4.0);
+        *df += 4.0 * ck[k] * pow(rho - rk[k], 3.0);
+    }
+}
+
 int orc_pot_eval(int pot, const double *prm, double r, double *potr, double *fpotr,
                  double *potb, double *fpotb)
 {
@@ -524,6 +593,7 @@ int orc_pot_eval(int pot, const double *prm, double r, double *potr, double *fpo
     case ORC_POT_AV_CU: av_nn(0, r, potr, fpotr); av_ne(0, r, potb, fpotb); return 0;
     case ORC_POT_AV_AU: av_nn(1, r, potr, fpotr); av_ne(1, r, potb, fpotb); return 0;
     case ORC_POT_AV_CUAU: av_nn(2, r, potr, fpotr); av_ne(2, r, potb, fpotb); return 0;
+    case ORC_POT_MENDELEV_ZR: zr_nn(r, potr, fpotr); zr_ne(r, potb, fpotb); return 0;
     case ORC_POT_MARINICA3:
     case ORC_POT_MARINICA4: {
         const mar_set_t *m = &mar_sets[pot == ORC_POT_MARINICA3 ? 1 : 2];
@@ -545,6 +615,7 @@ int orc_embed_eval(int pot, const double *prm, double rho, double *f, double *df
     if (pot == ORC_POT_MARINICA2) { mar_embed(rho, f, df); return 0; }
     if (pot == ORC_POT_MARINICA3) { mar_set_embed(&mar_sets[1], rho, f, df); return 0; }
     if (pot == ORC_POT_MARINICA4) { mar_set_embed(&mar_sets[2], rho, f, df); return 0; }
+    if (pot == ORC_POT_MENDELEV_ZR) { zr_embed(rho, f, df); return 0; }
     *f = 0.0; *df = 0.0;
     return -1;
 }

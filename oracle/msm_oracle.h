@@ -49,6 +49,7 @@ extern "C" {
 #define ORC_POT_AV_CU       9   /* Ackland-Vitek Cu (FS form), EM_TB_CuCu_Ackland_Vitek_PRB41_10324.F90 */
 #define ORC_POT_AV_AU      10   /* Ackland-Vitek Au (FS form), EM_TB_AuAu_Ackland_Vitek_PRB41_10324.F90 */
 #define ORC_POT_AV_CUAU    11   /* Ackland-Vitek Cu-Au (FS form), EM_TB_CuAu_Ackland_Vitek_PRB41_10324.F90 */
+#define ORC_POT_MENDELEV_ZR 12  /* Mendelev-Ackland Zr (EAM form), EAM_ZrZr_Mendelev_Phil_Mag_L87_2007.F90 */
 
 #define ORC_FS  0
 #define ORC_EAM 1

@@ -126,3 +126,25 @@ def test_ackland_vitek_tables(oracle, pot, a, ecoh):
     r = oracle.force(pos, np.ones(n, np.int32), st, box, kv, ind, t)
     assert np.abs(r["f"]).max() < 1e-10
     assert r["epot"].mean() == pytest.approx(ecoh, abs=2e-3)
+
+
+def test_mendelev_zr_tables_and_hcp_energy(oracle):
+    """Mendelev-Ackland Zr: library equals oracle (the first F' row is -inf in both, as in the
+    reference); the perfect hcp crystal has zero force and E = -6.467 eV/atom."""
+    ft = ForceTable.mendelev_zr()
+    o = oracle.make_tables(oracle.POT_MENDELEV_ZR, None, 7.6, 10000, 10000, 20.0)
+    for k in ("potr", "fpotr", "potb", "fpotb", "fembd", "dfembd"):
+        a, b = getattr(ft, k), o[k]
+        fin = np.isfinite(b)
+        assert np.array_equal(np.isfinite(a), fin), k
+        assert np.max(np.abs(a[fin] - b[fin])) <= 1e-12 * np.max(np.abs(b[fin])), k
+    assert np.isneginf(ft.dfembd[0]) and ft.rhod == pytest.approx(o["rhod"], rel=1e-14)
+    pos, L_ = lt.hcp(6, 4, 4, 3.232, 3.232 * 1.593)
+    n = len(pos)
+    t = oracle.Tables(o, oracle.EAM, 7.6)
+    box = oracle.make_box([0, 0, 0], L_)
+    st = np.ones(n, np.int32)
+    kv, ind = oracle.nlist(pos, st, box, 7.9, 200)
+    r = oracle.force(pos, np.ones(n, np.int32), st, box, kv, ind, t)
+    assert r["nbad"] == 0 and np.abs(r["f"]).max() < 1e-10
+    assert r["epot"].mean() == pytest.approx(-6.467, abs=2e-3)

@@ -50,3 +50,31 @@ def test_ackland_vitek_cu3au_force_parity(oracle):
             e.calepot()
             assert rel_err(e.get_epot(), ref["epot"]) < 1e-10, precision
         e.close()
+
+
+def test_mendelev_zr_hcp_force_parity(oracle):
+    ft = ForceTable.mendelev_zr()
+    t = oracle.Tables(oracle.make_tables(oracle.POT_MENDELEV_ZR, None, 7.6, 10000, 10000, 20.0),
+                      oracle.EAM, 7.6)
+    pos, L_ = lt.hcp(8, 5, 5, 3.232, 3.232 * 1.593)          # every edge above 3 rc_nl
+    pos = pos + np.random.default_rng(6).normal(scale=0.05, size=pos.shape)
+    pos -= np.floor(pos / L_) * L_
+    n = len(pos)
+    rc_nl = 7.9
+    box = oracle.make_box([0, 0, 0], L_)
+    st = np.ones(n, np.int32)
+    kv, ind = oracle.nlist(pos, st, box, rc_nl, 200)
+    ref = oracle.force(pos, np.ones(n, np.int32), st, box, kv, ind, t)
+    assert ref["nbad"] == 0
+    for precision in ("fp64", "ff", "mixed"):
+        e = Engine(n, rc_nl, mxkvois=160, precision=precision)
+        e.init_forcetable(ft)
+        e.copyin([(n, (0, 0, 0), tuple(L_), (1, 1, 1))], pos)
+        e.calforce()
+        f = e.get_force()
+        if precision == "mixed":
+            assert np.abs(f - ref["f"]).max() / np.abs(ref["f"]).max() < 1e-6
+        else:
+            assert rel_err(f, ref["f"]) < 1e-10, precision
+            assert rel_err(e.get_den(), ref["den"]) < 1e-10, precision
+        e.close()
