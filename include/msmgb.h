@@ -304,6 +304,8 @@ int  msmgb_calforce_noalloc(const msmgb_force_noalloc *args);
 #define MSMGB_POT_AV_AU      10   /* Au-Au                                                   */
 #define MSMGB_POT_AV_CUAU    11   /* Cu-Au cross pair and density sqrt(rho_Cu rho_Au)        */
 #define MSMGB_POT_MENDELEV_ZR 12  /* Mendelev-Ackland Zr, EAM form (EAM_ZrZr_Mendelev_Phil_Mag_L87_2007.F90) */
+#define MSMGB_POT_AWB_ZR     13   /* Ackland-Wooding-Bacon Zr, FS form (EM_TB_AWB_Phil_Mag_A71_1995_553.F90) */
+#define MSMGB_POT_HETI_LJ    14   /* He-Ti pair, no density (EM_TB_WangJun_Ti-HE_2007/LJ_He_Ti.F90) */
 /* Fills POTR/FPOTR/POTB/FPOTB (ntab each) and, if fembd/dfembd are non-NULL, F/F' (nembd
  * each); returns RHOD = rhoscal * max(POTB) / nembd through *rhod.  Lengths in Angstrom,
  * energies in eV. */

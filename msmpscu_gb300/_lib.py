@@ -19,6 +19,8 @@ POT_DERLET_WW, POT_HEHE_EXP6, POT_HEW_ZBL = 4, 5, 6
 POT_MARINICA3, POT_MARINICA4 = 7, 8
 POT_AV_CU, POT_AV_AU, POT_AV_CUAU = 9, 10, 11
 POT_MENDELEV_ZR = 12
+POT_AWB_ZR = 13
+POT_HETI_LJ = 14
 STATU_ACTIVE = 1
 STATU_FIXPOSX, STATU_FIXPOSY, STATU_FIXPOSZ = 2, 4, 8
 STATU_FIXVELX, STATU_FIXVELY, STATU_FIXVELZ = 16, 32, 64

@@ -514,6 +514,73 @@ void mendelev_zr_embed(double rho, double *f, double *df)
     *df = d;
 }
 
+// Ackland-Wooding-Bacon Zr (EM_TB_AWB_Phil_Mag_A71_1995_553.F90, FS form), evaluated in CGS as
+// written and converted on return: ZBL (Z = 40) below 1.2 A, exp(cubic in A) to 2.55 A, a cubic
+// in cm to RCR7, then V = sum_k AR_k (RCR_k - r)^3 (7 knots) with POTR = V/2; density
+// AT2 (RCT2 - r)^3 + AT1 (RCT1 - r)^3.  The knot coefficients and radii and B1..B4 are
+// single-precision literals in the source.  Beyond RCR1 (pair) and RCT1 (density) the source
+// assigns nothing, leaving the zero-initialised table entries (MD_TypeDef_ForceTable.F90:586).
+PairVal awb_zr(double r_a)
+{
+    const double e = kEVERG, rr = 3.249e-08 * 1.414213562;     // RRFIT * CP_RSQ2
+    const float ar[7] = {-58.480671f, 83.692945f, -20.958026f, -1.309533f, 65.726356f, 139.411255f, 443.442749f};
+    const float mr[7] = {1.22f, 1.20f, 1.14f, 0.95f, 0.80f, 0.70f, 0.63f};
+    const double r = r_a * 1e-8;
+    double p = 0.0, f = 0.0;
+    const double rcr7 = (double)mr[6] * rr;
+    if (r < 1.20e-8) {
+        zbl_cgs(40.0, 40.0, r, &p, &f);
+    } else if (r <= 2.55e-8) {
+        const double b1 = 13.4037f, b2 = -12.2190f, b3 = 5.0261f, b4 = -0.8435f;
+        const double ra = r * 1e8;
+        const double tp = e * std::exp(b1 + b2 * ra + b3 * ra * ra + b4 * ra * ra * ra);
+        p = tp / 2.0;
+        f = -(b2 + 2.0 * b3 * ra + 3.0 * b4 * ra * ra) * 1e8 * tp;
+    } else if (r <= rcr7) {
+        const double c3 = -19388949878932.86, c2 = 1706444.034874689, c1 = -5.0454065151782766e-002,
+                     c0 = 5.0256487041006336e-010;
+        p = (c0 + c1 * r + c2 * std::pow(r, 2.0) + c3 * std::pow(r, 3.0)) * 0.5;
+        f = -(c1 + 2.0 * c2 * r + 3.0 * c3 * std::pow(r, 2.0));
+    } else {
+        for (int k = 0; k < 7; ++k) {
+            const double rk = (double)mr[k] * rr, a = (double)ar[k] * e / (rr * rr * rr);
+            if (r < rk) {
+                p += a * std::pow(rk - r, 3.0);
+                f += 3.0 * a * std::pow(rk - r, 2.0);
+            }
+        }
+        p *= 0.5;
+    }
+    PairVal o = to_ev(p, f);
+    const double rct1 = (double)1.22f * rr, rct2 = (double)1.05f * rr;
+    const double at1 = (double)48.288836f * (e * e) / (rr * rr * rr), at2 = (double)-0.850556f * (e * e) / (rr * rr * rr);
+    double b = 0.0, db = 0.0;
+    if (r > 0.0 && r < rct2) {
+        b = at2 * std::pow(rct2 - r, 3.0) + at1 * std::pow(rct1 - r, 3.0);
+        db = 3.0 * at2 * std::pow(rct2 - r, 2.0) + 3.0 * at1 * std::pow(rct1 - r, 2.0);
+    } else if (r >= rct2 && r < rct1) {
+        b = at1 * std::pow(rct1 - r, 3.0);
+        db = 3.0 * at1 * std::pow(rct1 - r, 2.0);
+    }
+    o.potb = b / (e * e);
+    o.fpotb = db / (e * e) * 1e-8;
+    return o;
+}
+
+// He-Ti of the reference's Ti-He library (LJ_He_Ti.F90:10-28, NN_HeTi_Interaction; no density),
+// in CGS as written: V = pha0 ((r0/r)^4.35 - 3.211829 (r0/r)^1.4).  Both exponents are
+// single-precision literals while the derivative's factors 4.35D0 and 1.4D0 are double, so
+// -V' differs from the derivative of V in the eighth digit; kept so.
+PairVal heti_lj(double r_a)
+{
+    const double pha0 = 0.02617 * kEVERG, r0 = 4.72879e-8;
+    const double r = r_a * 1e-8, x = r0 / r;
+    const double e1 = (double)4.35f, e2 = (double)1.4f;
+    const double p = 0.5 * pha0 * (std::pow(x, e1) - 3.211829 * std::pow(x, e2));
+    const double f = 0.5 * 2.0 * pha0 * (4.35 * std::pow(x, e1) / r - 3.211829 * 1.4 * std::pow(x, e2) / r);
+    return to_ev(p, f);
+}
+
 // Bonny, Grigorev, Terentyev W-H-He EAM (EAM_WHeH_Bonny_JPCM26_2014), subtypes EAM1 and EAM2
 // (EAM1_WHeH_Bonny_JPCM26_2014.F90).  W-W is Marinica EAM2 under a gauge transformation
 // (:15-104); the other pairs are sums of cubic knots (NN_FuncPoly3,
@@ -602,7 +669,7 @@ extern "C" int msmgb_create_forcetable(int pot, const double *prm, double rmax, 
 {
     if (ntab < 2 || rmax <= 0.0 || !potr || !fpotr || !potb || !fpotb) return MSMGB_ERR_ARG;
     if (pot == MSMGB_POT_CR && !prm) return MSMGB_ERR_ARG;
-    if (pot < MSMGB_POT_CR || pot > MSMGB_POT_MENDELEV_ZR) return MSMGB_ERR_ARG;
+    if (pot < MSMGB_POT_CR || pot > MSMGB_POT_HETI_LJ) return MSMGB_ERR_ARG;
     const double csi = (double)ntab / std::sqrt(rmax);
     const double csiv = 1.0 / csi;
     double rhomx = -1.0;
@@ -619,6 +686,8 @@ extern "C" int msmgb_create_forcetable(int pot, const double *prm, double rmax, 
         case MSMGB_POT_AV_AU: v = ackland_vitek(1, r); break;
         case MSMGB_POT_AV_CUAU: v = ackland_vitek(2, r); break;
         case MSMGB_POT_MENDELEV_ZR: v = mendelev_zr(r); break;
+        case MSMGB_POT_AWB_ZR: v = awb_zr(r); break;
+        case MSMGB_POT_HETI_LJ: v = heti_lj(r); break;
         case MSMGB_POT_ACKLAND_WW: v = ackland_ww(r); break;
         case MSMGB_POT_DERLET_WW: v = derlet_ww(r); break;
         case MSMGB_POT_HEHE_EXP6: v = hehe_exp6(r); break;

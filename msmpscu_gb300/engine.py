@@ -30,6 +30,23 @@ def _i(a):
     return a.ctypes.data_as(C.POINTER(C.c_int)) if a is not None else None
 
 
+def _cr_element_prm(element):
+    """A, xi, p, q, r0 of the reference's Cleri-Rosato library (TB_CR_AlAl/AuAu/TiTi.F90) as it
+    holds them: Al's lattice constant 4.050 and all Ti constants are single-precision literals,
+    and Ti's r0 = 2.951 A * sqrt(1/3 + beta^2/4) is evaluated in single precision."""
+    f32 = np.float32
+    halfrsq2 = 0.707106781187                                  # CP_HALFRSQ2
+    if element == "Al":
+        return [0.1221, 1.316, 8.612, 2.516, float(f32(4.050)) * halfrsq2]
+    if element == "Au":
+        return [0.2061, 1.790, 10.229, 4.036, 4.079 * halfrsq2]
+    if element == "Ti":
+        beta = f32(1.5874)
+        fac = np.sqrt(f32(1.0) / f32(3.0) + beta * beta / f32(4.0), dtype=np.float32)
+        return [float(f32(0.1519)), float(f32(1.8112)), float(f32(8.620)), float(f32(2.390)), 2.951 * float(fac)]
+    raise ValueError("the Cleri-Rosato library holds Al, Au and Ti")
+
+
 class ForceTable:
     """Single-species force table in the reference's conventions (NKIND = NGROUP = 1)."""
 
@@ -127,25 +144,40 @@ class ForceTable:
         return cls(L.POT_CR, [A, xi, p, q, r0], rc, rc, L.FS_TYPE, ntab=ntab, nembd=ntab)
 
     @classmethod
+    def awb_zr(cls, rmax=5.6, ru=None, ntab=10000):
+        """Ackland-Wooding-Bacon Zr (FS type), the reference's EM_TB_AWB_Phil_Mag_A71_1995_553."""
+        return cls(L.POT_AWB_ZR, None, rmax, ru if ru else rmax, L.FS_TYPE, ntab=ntab)
+
+    @classmethod
+    def wangjun_ti_he(cls, rmax, ru=None, ntab=10000):
+        """The reference's Ti-He FS library EM_TB_WangJun_Ti-HE_2007
+        (EM_TB_ForcetTable_WangJun_Ti_He_2007.F90): #1 Ti-Ti (Cleri-Rosato Ti), #2 He-He
+        (ZBL/EXP6, the W-He library's), #3 (Ti neighbour of a He host) and #4 (He neighbour of a
+        Ti host), both He-Ti.  Groups Ti = 1, He = 2: KPAIR(1,1) = 1, KPAIR(2,2) = 2,
+        KPAIR(2,1) = 3, KPAIR(1,2) = 4."""
+        ru = ru if ru else rmax
+        parts = [cls(L.POT_CR, _cr_element_prm("Ti"), rmax, ru, L.FS_TYPE, ntab=ntab, nembd=ntab),
+                 cls(L.POT_HEHE_EXP6, None, rmax, ru, L.FS_TYPE, ntab=ntab),
+                 cls(L.POT_HETI_LJ, None, rmax, ru, L.FS_TYPE, ntab=ntab),
+                 cls(L.POT_HETI_LJ, None, rmax, ru, L.FS_TYPE, ntab=ntab)]
+        self = parts[0]
+        for key in ("potr", "fpotr", "potb", "fpotb"):
+            setattr(self, key, np.stack([getattr(t, key) for t in parts], 1).reshape(-1).copy())
+        self.pot = None
+        self.nkind, self.ngroup, self.nkind1 = 4, 2, 1
+        kp = np.array([[1, 4], [3, 2]], np.int32)           # KPAIR(I, J) at kp[I-1, J-1]
+        self._kpair = np.ascontiguousarray(kp.T).reshape(-1)
+        self._kembd = np.ones(2, np.int32)
+        return self
+
+    @classmethod
     def cleri_rosato_element(cls, element, rc, ntab=10000):
         """The reference's Cleri-Rosato library EM_TB_Cleri_Rosato_PRB48_22 (Al, Au, Ti;
         EM_TB_ForcetTable_CR_2014.F90:31-36), FS type with a hard cutoff rc.  Parameters as
         the reference holds them: Al's lattice constant 4.050 (TB_CR_AlAl.F90:13) and all of
         Ti's constants (TB_CR_TiTi.F90:10-16) are single-precision literals, and Ti's
         r0 = 2.951 A * sqrt(1/3 + beta^2/4) is evaluated in single precision."""
-        f32 = np.float32
-        halfrsq2 = 0.707106781187                                  # CP_HALFRSQ2
-        if element == "Al":
-            prm = [0.1221, 1.316, 8.612, 2.516, float(f32(4.050)) * halfrsq2]
-        elif element == "Au":
-            prm = [0.2061, 1.790, 10.229, 4.036, 4.079 * halfrsq2]
-        elif element == "Ti":
-            beta = f32(1.5874)
-            fac = np.sqrt(f32(1.0) / f32(3.0) + beta * beta / f32(4.0), dtype=np.float32)
-            prm = [float(f32(0.1519)), float(f32(1.8112)), float(f32(8.620)), float(f32(2.390)),
-                   2.951 * float(fac)]
-        else:
-            raise ValueError("the Cleri-Rosato library holds Al, Au and Ti")
+        prm = _cr_element_prm(element)
         return cls(L.POT_CR, prm, rc, rc, L.FS_TYPE, ntab=ntab, nembd=ntab)
 
     @classmethod

@@ -584,6 +584,72 @@ static void zr_embed(double rho, double *f, double *df)
     }
 }
 
+/* Ackland-Wooding-Bacon Zr, EM_TB_AWB_Phil_Mag_A71_1995_553.F90 (FS form), Angstrom / eV.  Scale
+ * length s = 3.249 A * 1.414213562 (CP_RSQ2); float literals for the source's default-REAL
+ * constants; zero beyond the last knot (the source leaves those zero-initialised entries). */
+static void awb_nn(double r, double *potr, double *fpotr)
+{
+    const double ev = 1.60219e-12, s = 3.249 * 1.414213562;
+    static const float ar[7] = {-58.480671f, 83.692945f, -20.958026f, -1.309533f, 65.726356f, 139.411255f,
+                                443.442749f};
+    static const float mr[7] = {1.22f, 1.20f, 1.14f, 0.95f, 0.80f, 0.70f, 0.63f};
+    if (r < 1.20) {
+        /* ZBL with Z1 = Z2 = 40: 9e9 qe^2 = 9 x 1.60219 eV*A (qe = 1.60219e-19, eV = qe 1e7 erg) */
+        const double ke = 9.0 * 1.60219 * 1600.0;
+        const double as = 0.88534 * 0.5291772108 / (2.0 * pow(40.0, 0.23));
+        double phi, mdphi;
+        zbl_phi(r / as, &phi, &mdphi);
+        *potr = 0.5 * ke * phi / r;
+        *fpotr = ke * phi / (r * r) + ke * mdphi / (as * r);
+    } else if (r <= 2.55) {
+        const double q = exp(13.4037f + r * (-12.2190f + r * (5.0261f + r * -0.8435f)));
+        *potr = 0.5 * q;
+        *fpotr = -(-12.2190f + 2.0 * 5.0261f * r + 3.0 * -0.8435f * r * r) * q;
+    } else if (r <= mr[6] * s) {
+        /* cubic with CGS coefficients: eV, eV/A, eV/A^2, eV/A^3 after conversion */
+        const double c0 = 5.0256487041006336e-010 / ev, c1 = -5.0454065151782766e-002 * 1e-8 / ev;
+        const double c2 = 1706444.034874689 * 1e-16 / ev, c3 = -19388949878932.86 * 1e-24 / ev;
+        *potr = 0.5 * (c0 + r * (c1 + r * (c2 + r * c3)));
+        *fpotr = -(c1 + r * (2.0 * c2 + 3.0 * c3 * r));
+    } else {
+        double v = 0.0, d = 0.0;
+        for (int k = 0; k < 7; ++k) {
+            const double kk = mr[k] * s;
+            if (!(r < kk)) continue;
+            v += ar[k] / (s * s * s) * pow(kk - r, 3.0);
+            d += 3.0 * ar[k] / (s * s * s) * pow(kk - r, 2.0);
+        }
+        *potr = 0.5 * v;
+        *fpotr = d;
+    }
+}
+
+static void awb_ne(double r, double *potb, double *fpotb)
+{
+    const double s = 3.249 * 1.414213562;
+    const double k1 = 1.22f * s, k2 = 1.05f * s, a1 = 48.288836f / (s * s * s), a2 = -0.850556f / (s * s * s);
+    *potb = *fpotb = 0.0;
+    if (r > 0.0 && r < k1) {
+        *potb = a1 * pow(k1 - r, 3.0);
+        *fpotb = 3.0 * a1 * pow(k1 - r, 2.0);
+        if (r < k2) {
+            *potb += a2 * pow(k2 - r, 3.0);
+            *fpotb += 3.0 * a2 * pow(k2 - r, 2.0);
+        }
+    }
+}
+
+/* He-Ti, EM_TB_WangJun_Ti-HE_2007/LJ_He_Ti.F90:10-28, Angstrom / eV: phi0 = 0.02617 eV,
+ * r0 = 4.72879 A; the exponents 4.35 and 1.4 are single-precision literals in the source, the
+ * derivative's factors double. */
+static void heti_nn(double r, double *potr, double *fpotr)
+{
+    const double phi0 = 0.02617, r0 = 4.72879;
+    const double a = pow(r0 / r, (double)4.35f), b = pow(r0 / r, (double)1.4f);
+    *potr = 0.5 * phi0 * (a - 3.211829 * b);
+    *fpotr = phi0 * (4.35 * a - 3.211829 * 1.4 * b) / r;
+}
+
 int orc_pot_eval(int pot, const double *prm, double r, double *potr, double *fpotr,
                  double *potb, double *fpotb)
 {
@@ -594,6 +660,8 @@ int orc_pot_eval(int pot, const double *prm, double r, double *potr, double *fpo
     case ORC_POT_AV_AU: av_nn(1, r, potr, fpotr); av_ne(1, r, potb, fpotb); return 0;
     case ORC_POT_AV_CUAU: av_nn(2, r, potr, fpotr); av_ne(2, r, potb, fpotb); return 0;
     case ORC_POT_MENDELEV_ZR: zr_nn(r, potr, fpotr); zr_ne(r, potb, fpotb); return 0;
+    case ORC_POT_AWB_ZR: awb_nn(r, potr, fpotr); awb_ne(r, potb, fpotb); return 0;
+    case ORC_POT_HETI_LJ: heti_nn(r, potr, fpotr); zero_ne(r, potb, fpotb); return 0;
     case ORC_POT_MARINICA3:
     case ORC_POT_MARINICA4: {
         const mar_set_t *m = &mar_sets[pot == ORC_POT_MARINICA3 ? 1 : 2];

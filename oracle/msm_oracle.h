@@ -50,6 +50,8 @@ extern "C" {
 #define ORC_POT_AV_AU      10   /* Ackland-Vitek Au (FS form), EM_TB_AuAu_Ackland_Vitek_PRB41_10324.F90 */
 #define ORC_POT_AV_CUAU    11   /* Ackland-Vitek Cu-Au (FS form), EM_TB_CuAu_Ackland_Vitek_PRB41_10324.F90 */
 #define ORC_POT_MENDELEV_ZR 12  /* Mendelev-Ackland Zr (EAM form), EAM_ZrZr_Mendelev_Phil_Mag_L87_2007.F90 */
+#define ORC_POT_AWB_ZR     13   /* Ackland-Wooding-Bacon Zr (FS form), EM_TB_AWB_Phil_Mag_A71_1995_553.F90 */
+#define ORC_POT_HETI_LJ    14   /* He-Ti pair (no density), EM_TB_WangJun_Ti-HE_2007/LJ_He_Ti.F90 */
 
 #define ORC_FS  0
 #define ORC_EAM 1

@@ -16,6 +16,8 @@ POT_DERLET_WW, POT_HEHE_EXP6, POT_HEW_ZBL = 4, 5, 6
 POT_MARINICA3, POT_MARINICA4 = 7, 8
 POT_AV_CU, POT_AV_AU, POT_AV_CUAU = 9, 10, 11
 POT_MENDELEV_ZR = 12
+POT_AWB_ZR = 13
+POT_HETI_LJ = 14
 FS, EAM = 0, 1
 
 _dp = C.POINTER(C.c_double)

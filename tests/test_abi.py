@@ -148,3 +148,36 @@ def test_mendelev_zr_tables_and_hcp_energy(oracle):
     r = oracle.force(pos, np.ones(n, np.int32), st, box, kv, ind, t)
     assert r["nbad"] == 0 and np.abs(r["f"]).max() < 1e-10
     assert r["epot"].mean() == pytest.approx(-6.467, abs=2e-3)
+
+
+@pytest.mark.parametrize("pot,typ", [("POT_AWB_ZR", "FS"), ("POT_HETI_LJ", "FS")])
+def test_awb_and_heti_tables(oracle, pot, typ):
+    """AWB Zr and the He-Ti pair: the library's CGS evaluation equals the oracle's Angstrom/eV
+    restatement."""
+    ft = ForceTable(getattr(L, pot), None, 6.0, 6.0, L.FS_TYPE)
+    o = oracle.make_tables(getattr(oracle, pot), None, 6.0, 10000, 10000, 20.0, want_embed=False)
+    for k in ("potr", "fpotr", "potb", "fpotb"):
+        assert np.max(np.abs(getattr(ft, k) - o[k])) <= 1e-14 * max(np.max(np.abs(o[k])), 1e-300), k
+
+
+def test_awb_zr_hcp_energy(oracle):
+    ft = ForceTable.awb_zr(rmax=6.0)
+    t = oracle.Tables(oracle.make_tables(oracle.POT_AWB_ZR, None, 6.0, 10000, 10000, 20.0, want_embed=False),
+                      oracle.FS, 6.0)
+    pos, L_ = lt.hcp(8, 5, 5, 3.249, 3.249 * 1.593)
+    n = len(pos)
+    box = oracle.make_box([0, 0, 0], L_)
+    st = np.ones(n, np.int32)
+    kv, ind = oracle.nlist(pos, st, box, 6.3, 200)
+    r = oracle.force(pos, np.ones(n, np.int32), st, box, kv, ind, t)
+    assert np.abs(r["f"]).max() < 1e-10
+    assert r["epot"].mean() == pytest.approx(-6.243, abs=2e-3)
+    assert ft.nkind == 1
+
+
+def test_wangjun_ti_he_kpair():
+    ft = ForceTable.wangjun_ti_he(rmax=6.0)
+    kp = ft._kpair.reshape(2, 2).T
+    assert kp.tolist() == [[1, 4], [3, 2]]
+    p = ft.potr.reshape(ft.ntab, 4)
+    assert np.array_equal(p[:, 2], p[:, 3]) and not ft.potb.reshape(ft.ntab, 4)[:, 1:].any()

@@ -78,3 +78,58 @@ def test_mendelev_zr_hcp_force_parity(oracle):
             assert rel_err(f, ref["f"]) < 1e-10, precision
             assert rel_err(e.get_den(), ref["den"]) < 1e-10, precision
         e.close()
+
+
+def _fs_parity(oracle, ft, t, pos, ityp, L_, rc_nl, masses):
+    n = len(pos)
+    box = oracle.make_box([0, 0, 0], L_)
+    st = np.ones(n, np.int32)
+    kv, ind = oracle.nlist(pos, st, box, rc_nl, 200)
+    ref = oracle.force(pos, ityp, st, box, kv, ind, t)
+    for precision in ("fp64", "ff", "mixed"):
+        e = Engine(n, rc_nl, mxkvois=160, precision=precision)
+        e.init_forcetable(ft)
+        e.set_masses(masses)
+        e.copyin([(n, (0, 0, 0), tuple(L_), (1, 1, 1))], pos, ityp=ityp)
+        e.calforce()
+        f = e.get_force()
+        if precision == "mixed":
+            assert np.abs(f - ref["f"]).max() / np.abs(ref["f"]).max() < 1e-6
+        else:
+            assert rel_err(f, ref["f"]) < 1e-10, precision
+            e.calepot()
+            assert rel_err(e.get_epot(), ref["epot"]) < 1e-10, precision
+        e.close()
+
+
+def test_awb_zr_hcp_force_parity(oracle):
+    ft = ForceTable.awb_zr(rmax=6.0)
+    t = oracle.Tables(oracle.make_tables(oracle.POT_AWB_ZR, None, 6.0, 10000, 10000, 20.0, want_embed=False),
+                      oracle.FS, 6.0)
+    pos, L_ = lt.hcp(8, 5, 5, 3.249, 3.249 * 1.593)
+    pos = pos + np.random.default_rng(8).normal(scale=0.05, size=pos.shape)
+    pos -= np.floor(pos / L_) * L_
+    _fs_parity(oracle, ft, t, pos, np.ones(len(pos), np.int32), L_, 6.3, np.array([91.224]) * lt.AMU)
+
+
+def test_wangjun_ti_he_force_parity(oracle):
+    rc = 6.0
+    ft = ForceTable.wangjun_ti_he(rmax=rc)
+    ti = ForceTable.cleri_rosato_element("Ti", rc=rc).prm
+    ts = [oracle.make_tables(oracle.POT_CR, list(ti), rc, 10000, 10000, 20.0, want_embed=False),
+          oracle.make_tables(oracle.POT_HEHE_EXP6, None, rc, 10000, 10000, 20.0, want_embed=False),
+          oracle.make_tables(oracle.POT_HETI_LJ, None, rc, 10000, 10000, 20.0, want_embed=False),
+          oracle.make_tables(oracle.POT_HETI_LJ, None, rc, 10000, 10000, 20.0, want_embed=False)]
+    arr = {k: np.stack([t[k] for t in ts], 1) for k in ("potr", "fpotr", "potb", "fpotb")}
+    t = oracle.RawTables(oracle.FS, 10000, 4, rc, rc, arr["potr"], arr["fpotr"], arr["potb"], arr["fpotb"],
+                         np.array([[1, 4], [3, 2]]))
+    a, c = 2.951, 2.951 * 1.5874
+    pos, L_ = lt.hcp(9, 5, 5, a, c)
+    rng = np.random.default_rng(9)
+    # He in octahedral sites of the first 12 orthorhombic cells
+    he = np.array([[a * (i % 9) + 0.5 * a, a * np.sqrt(3.0) * ((i // 9) % 5) + a * np.sqrt(3.0) / 6.0, 0.25 * c]
+                   for i in range(12)])
+    pos = np.vstack([pos, he]) + rng.normal(scale=0.03, size=(len(pos) + len(he), 3))
+    pos -= np.floor(pos / L_) * L_
+    ityp = np.concatenate([np.ones(len(pos) - len(he), np.int32), np.full(len(he), 2, np.int32)])
+    _fs_parity(oracle, ft, t, pos, ityp, L_, rc + 0.3, np.array([47.867, 4.0026]) * lt.AMU)
