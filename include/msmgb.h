@@ -341,6 +341,16 @@ int  msmgb_bonny_wheh_tables(int subtype, double rmax, int ntab, int nembd, doub
                              double *potr, double *fpotr, double *potb, double *fpotb, double *fembd,
                              double *dfembd, int *kpair, int *kembd, int *nkind, double *rhod);
 
+/* ---- Moldy potential files (Register_ForceTableProc_Moldy,
+ *      MDLIB/sor/Potentials/EAM_NIST/Filedatas_Func_Moldy.F90:27-77,116-131) ------------------ */
+/* One element, EAM type with F = -sqrt(rho): the pair and density knot sums of the file
+ * (knots times the lattice constant a0, coefficients over a0^3 and a0^6) on the sqrt(r) grid of
+ * ntab points up to rmax (the cutoff), the embedding table of nembd points on
+ * RHOD = rhoscal * max POTB / nembd (rhoscal <= 0: 20).  Host only. */
+int  msmgb_moldy_tables(const char *path, double rmax, int ntab, int nembd, double rhoscal,
+                        double *potr, double *fpotr, double *potb, double *fpotb, double *fembd,
+                        double *dfembd, double *rhod);
+
 /* ---- tabulated EAM potentials in lspt layout (Register_ForceTableProc_SPT,
  *      MDLIB/sor/Potentials/EAM_NIST/Filedatas_Func_Lspt.F90:560-604; reader
  *      get_filedatas_lspt :118-301) ------------------------------------------------------- */
@@ -351,13 +361,13 @@ int  msmgb_bonny_wheh_tables(int subtype, double rmax, int ntab, int nembd, doub
  * control file and the ".spt" files it names. */
 int  msmgb_lspt_info(const char *path, int flags, int *nelem, double *rmax, double *rhomax);
 /* Tables of an lspt potential, EAM type, in the layouts of msmgb_setfl_tables: NKIND = NE^2
- * pair tables on the sqrt(r) grid of ntab points up to rmax (<= 0: the files' largest r),
- * POTR = 0.5 V r, FPOTR = -V' r, POTB = rho_J, FPOTB = -rho_J'; NKIND1 = NE embedding tables
- * of nembd points, RHOD = max(largest F(rho)-file rho, rhoscal * max POTB) / nembd
- * (rhoscal <= 0: 20, the reference's RHOSCAL default).  Natural cubic splines through the
- * data with the reader's range rules (Vr_Spline, Rhor_Spline, Frho_Spline :340-500).
+ * pair tables on the sqrt(r) grid of ntab points up to rmax (<= 0: the files' largest r, the
+ * reader's RMAX), POTR = 0.5 V r, FPOTR = -V' r, POTB = rho_J, FPOTB = -rho_J'; NKIND1 = NE
+ * embedding tables of nembd points, RHOD = largest F(rho)-file rho / nembd (the reader's RHOMX,
+ * which the NIST generator keeps, NIST_ForceTable.F90:379-413).  Natural cubic splines through
+ * the data with the reader's range rules (Vr_Spline, Rhor_Spline, Frho_Spline :340-500).
  * Host only.  Returns MSMGB_ERR_ARG for a missing or malformed file. */
-int  msmgb_lspt_tables(const char *path, int flags, int ntab, int nembd, double rmax, double rhoscal,
+int  msmgb_lspt_tables(const char *path, int flags, int ntab, int nembd, double rmax,
                        double *potr, double *fpotr, double *potb, double *fpotb, double *fembd,
                        double *dfembd, int *kpair, int *kembd, double *rhod);
 

@@ -106,8 +106,10 @@ SIGNATURES = [
     ("msmgb_setfl_tables", C.c_int, [C.c_char_p, C.c_int, _dp, _dp, _dp, _dp, _dp, _dp, _ip, _ip, _dp, _dp]),
     ("msmgb_bonny_wheh_tables", C.c_int, [C.c_int, C.c_double, C.c_int, C.c_int, C.c_double,
                                           _dp, _dp, _dp, _dp, _dp, _dp, _ip, _ip, _ip, _dp]),
+    ("msmgb_moldy_tables", C.c_int, [C.c_char_p, C.c_double, C.c_int, C.c_int, C.c_double,
+                                     _dp, _dp, _dp, _dp, _dp, _dp, _dp]),
     ("msmgb_lspt_info", C.c_int, [C.c_char_p, C.c_int, _ip, _dp, _dp]),
-    ("msmgb_lspt_tables", C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
+    ("msmgb_lspt_tables", C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_double,
                                     _dp, _dp, _dp, _dp, _dp, _dp, _ip, _ip, _dp]),
     ("msmgb_cr_param_tables", C.c_int, [_dp, C.c_double, C.c_int, _dp]),
     ("msmgb_calforce_noalloc", C.c_int, [C.POINTER(ForceNoAlloc)]),

@@ -963,9 +963,10 @@ extern "C" int msmgb_setfl_tables(const char *path, int ntab, double *potr, doub
 // FPOTR = -V' r, POTB = rho, FPOTB = -rho' (NN_Spline, RHO_Spline :503-537).  The density at
 // a host element without an F(rho) file is zero (the integer flag test at :406 read as "the
 // host has an F(rho) file"; no force or energy depends on it).
-// RMAX = the largest x of the pair files read (:291); RHOMX = max(largest x of the F(rho)
-// files (:290), RHOSCAL * max POTB over all tables (MD_TypeDef_ForceTable.F90:965)),
-// RHOD = RHOMX / NEMBD.
+// RMAX = the largest x of the pair files read (:291), RHOMX = the largest x of the F(rho) files
+// (:290), RHOD = RHOMX / NEMBD: the NIST table generator restores the reader's RHOMX after
+// building the pair tables (Generate_NIST_ForceTalbe, NIST_ForceTable.F90:379-413), so the
+// RHOSCAL * max POTB rule of other libraries does not apply (RHOD = 1 when no F(rho) file).
 namespace {
 
 struct Spt {
@@ -1159,7 +1160,7 @@ extern "C" int msmgb_lspt_info(const char *path, int flags, int *nelem, double *
 }
 
 extern "C" int msmgb_lspt_tables(const char *path, int flags, int ntab, int nembd, double rmax,
-                                 double rhoscal, double *potr, double *fpotr, double *potb, double *fpotb,
+                                 double *potr, double *fpotr, double *potb, double *fpotb,
                                  double *fembd, double *dfembd, int *kpair, int *kembd, double *rhod)
 {
     if (!path || ntab < 2 || nembd < 2 || !potr || !fpotr || !potb || !fpotb || !fembd || !dfembd || !kpair ||
@@ -1170,9 +1171,7 @@ extern "C" int msmgb_lspt_tables(const char *path, int flags, int ntab, int nemb
     if (rc) return rc;
     const int ne = L.ne, nk = ne * ne;
     if (!(rmax > 0.0)) rmax = L.rmax;
-    if (!(rhoscal > 0.0)) rhoscal = 20.0;
     const double csiv = std::sqrt(rmax) / ntab;
-    double rhomx = L.rhomax;
     // table (I, J), 1-based id (I-1)*NE + J (Notify_func :327-337): pair V of elements
     // max(I,J), min(I,J); density of element J at an element-I host
     for (int I = 0; I < ne; ++I)
@@ -1191,11 +1190,10 @@ extern "C" int msmgb_lspt_tables(const char *path, int flags, int ntab, int nemb
                 fpotr[o] = -dv * r;
                 potb[o] = rho;
                 fpotb[o] = -drh;
-                if (rho * rhoscal > rhomx) rhomx = rho * rhoscal;
             }
             kpair[J * ne + I] = k + 1;                      // KPAIR(I,J), column-major
         }
-    const double d = rhomx / nembd;
+    const double d = L.rhomax > 0.0 ? L.rhomax / nembd : 1.0;
     for (int e = 0; e < ne; ++e) {
         kembd[e] = e + 1;
         for (int i = 1; i <= nembd; ++i) {
@@ -1269,6 +1267,91 @@ extern "C" int msmgb_bonny_wheh_tables(int subtype, double rmax, int ntab, int n
         for (int J = 0; J < 3; ++J) kpair[J * 3 + I] = I * 3 + J + 1;   // column-major
     }
     if (nkind) *nkind = nk;
+    if (rhod) *rhod = d;
+    return MSMGB_OK;
+}
+
+// ---- Moldy potential files ------------------------------------------------------------------
+// Register_ForceTableProc_Moldy with the reader get_filedatas_moldy (Filedatas_Func_Moldy.F90:
+// 27-77, 116-131): line 1 the element symbol; then four lines of numbers (pair coefficients
+// a_k, pair knots r_k, density coefficients A_k, density knots R_k) and a line of constants
+// whose first is the lattice constant a0; numbers are the tokens between blanks, commas,
+// brackets and '=' (EXNUMB.F).  Knots scale by a0, a_k by a0^-3, A_k by a0^-6.  Pair
+// V = sum a_k (r_k - r)^3 (NN_FuncPoly3: POTR = V/2, FPOTR = -V'), density
+// rho = sum A_k (R_k - r)^3 (RHO_FuncPoly3), embedding F = -sqrt(rho) (EMBED_FS_PLOY_Func with
+// A = -1, zero for rho <= 0).  The reader sets neither RMAX nor RHOMX, so the grid runs to the
+// cutoff and RHOD = RHOSCAL * max POTB / NEMBD (Create_Pairwise_ForceTable).
+namespace {
+
+bool moldy_numbers(FILE *f, std::vector<double> &v)
+{
+    char buf[8192];
+    if (!fgets(buf, sizeof(buf), f)) return false;
+    v.clear();
+    std::string tok;
+    for (const char *p = buf;; ++p) {
+        const char c = *p;
+        const bool sep = c == '\0' || c == ' ' || c == '\t' || c == ',' || c == '(' || c == ')' || c == '[' ||
+                         c == ']' || c == '{' || c == '}' || c == '=' || c == '\n' || c == '\r';
+        if (sep) {
+            if (!tok.empty()) {
+                char *end = nullptr;
+                const double x = strtod(tok.c_str(), &end);
+                if (end != tok.c_str() && *end == '\0') v.push_back(x);
+                tok.clear();
+            }
+            if (c == '\0') break;
+        } else {
+            tok.push_back(c);
+        }
+    }
+    return true;
+}
+
+}  // namespace
+
+extern "C" int msmgb_moldy_tables(const char *path, double rmax, int ntab, int nembd, double rhoscal,
+                                  double *potr, double *fpotr, double *potb, double *fpotb, double *fembd,
+                                  double *dfembd, double *rhod)
+{
+    if (!path || rmax <= 0.0 || ntab < 2 || nembd < 2 || !potr || !fpotr || !potb || !fpotb || !fembd ||
+        !dfembd)
+        return MSMGB_ERR_ARG;
+    if (!(rhoscal > 0.0)) rhoscal = 20.0;
+    FILE *f = fopen(path, "r");
+    if (!f) return MSMGB_ERR_ARG;
+    char sym[256];
+    std::vector<double> av, rv, ab, rb, cst;
+    const bool ok = fgets(sym, sizeof(sym), f) && moldy_numbers(f, av) && moldy_numbers(f, rv) &&
+                    moldy_numbers(f, ab) && moldy_numbers(f, rb) && moldy_numbers(f, cst);
+    fclose(f);
+    if (!ok || av.empty() || av.size() != rv.size() || ab.empty() || ab.size() != rb.size() || cst.empty() ||
+        !(cst[0] > 0.0))
+        return MSMGB_ERR_ARG;
+    const double a0 = cst[0];
+    for (double &x : rv) x *= a0;
+    for (double &x : rb) x *= a0;
+    for (double &x : av) x /= std::pow(a0, 3.0);
+    for (double &x : ab) x /= std::pow(a0, 6.0);
+    const double csiv = std::sqrt(rmax) / ntab;
+    double rhomx = 0.0;
+    for (int i = 1; i <= ntab; ++i) {
+        const double t = i * csiv, r = t * t;
+        double v, dv, b, db;
+        cubic_knots(r, av.data(), rv.data(), (int)av.size(), &v, &dv);
+        cubic_knots(r, ab.data(), rb.data(), (int)ab.size(), &b, &db);
+        potr[i - 1] = 0.5 * v * r;
+        fpotr[i - 1] = dv * r;
+        potb[i - 1] = b;
+        fpotb[i - 1] = db;
+        if (rhomx < b * rhoscal) rhomx = b * rhoscal;
+    }
+    const double d = rhomx / nembd;
+    for (int i = 1; i <= nembd; ++i) {
+        const double rho = (i - 1) * d;
+        fembd[i - 1] = rho > 0.0 ? -std::sqrt(rho) : 0.0;
+        dfembd[i - 1] = rho > 0.0 ? -0.5 / std::sqrt(rho) : 0.0;
+    }
     if (rhod) *rhod = d;
     return MSMGB_OK;
 }

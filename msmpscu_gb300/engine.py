@@ -104,12 +104,13 @@ class ForceTable:
         return self
 
     @classmethod
-    def lspt(cls, path, ntab=10000, nembd=10000, rmax=None, rhoscal=20.0, each_vr_file=False):
+    def lspt(cls, path, ntab=10000, nembd=10000, rmax=None, each_vr_file=False):
         """Tabulated EAM potential from an lspt control file and the ".spt" files it names
         (Register_ForceTableProc_SPT): NE^2 pair tables on the sqrt(r) grid up to the largest
-        pair-file r (or rmax), NE embedding tables of nembd points.  each_vr_file=False reads,
-        like the reference, the first file named on each pair line for all pairs of that
-        line.  The files carry no masses: set them with Engine.set_masses."""
+        pair-file r (or rmax), NE embedding tables of nembd points up to the largest F(rho)
+        knot.  each_vr_file=False reads, like the reference, the first file named on each pair
+        line for all pairs of that line.  The files carry no masses: set them with
+        Engine.set_masses."""
         lib = L.load()
         flags = L.LSPT_EACH_VR_FILE if each_vr_file else 0
         bpath = os.fsencode(path)
@@ -129,13 +130,36 @@ class ForceTable:
         self._kembd = np.zeros(ne, np.int32)
         self.masses = None
         rhod = C.c_double()
-        rc = lib.msmgb_lspt_tables(bpath, flags, self.ntab, self.nembd, self.rmax, float(rhoscal),
-                                   _d(self.potr), _d(self.fpotr), _d(self.potb), _d(self.fpotb),
+        rc = lib.msmgb_lspt_tables(bpath, flags, self.ntab, self.nembd, self.rmax, _d(self.potr), _d(self.fpotr), _d(self.potb), _d(self.fpotb),
                                    _d(self.fembd), _d(self.dfembd), _i(self._kpair), _i(self._kembd),
                                    C.byref(rhod))
         if rc != L.OK:
             raise MSMError(rc, "lspt table generation failed")
         self.rhod = rhod.value
+        return self
+
+    @classmethod
+    def moldy(cls, path, rmax, ntab=10000, nembd=10000, rhoscal=20.0):
+        """One-element EAM potential (F = -sqrt(rho)) from a Moldy file
+        (Register_ForceTableProc_Moldy), on the sqrt(r) grid up to the cutoff rmax."""
+        lib = L.load()
+        self = cls.__new__(cls)
+        self.pot, self.pottype, self.prm = None, L.EAM_TYPE, np.zeros(5)
+        self.rmax = self.ru = float(rmax)
+        self.ntab, self.nembd = int(ntab), int(nembd)
+        self.potr, self.fpotr, self.potb, self.fpotb = (np.zeros(self.ntab) for _ in range(4))
+        self.fembd, self.dfembd = np.zeros(self.nembd), np.zeros(self.nembd)
+        rhod = C.c_double()
+        rc = lib.msmgb_moldy_tables(os.fsencode(path), self.rmax, self.ntab, self.nembd, float(rhoscal),
+                                    _d(self.potr), _d(self.fpotr), _d(self.potb), _d(self.fpotb),
+                                    _d(self.fembd), _d(self.dfembd), C.byref(rhod))
+        if rc != L.OK:
+            raise MSMError(rc, "cannot read Moldy potential %s" % path)
+        self.rhod = rhod.value
+        self._kpair = np.array([1], np.int32)
+        self._kembd = np.array([1], np.int32)
+        self.nkind = self.nkind1 = self.ngroup = 1
+        self.masses = None
         return self
 
     @classmethod

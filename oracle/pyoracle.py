@@ -295,11 +295,11 @@ def _spt_eval(xy, t, keep_above):
     return f, df
 
 
-def lspt_tables(d, ntab=10000, nembd=10000, rhoscal=20.0, rmax=None):
+def lspt_tables(d, ntab=10000, nembd=10000, rmax=None):
     """All NE^2 pair tables (column (I, J) = I * NE + J: V of the pair, density of element J at
     an element-I host, zero when element I has no F(rho)) on the sqrt(r) grid up to rmax (the
-    pair files' largest r) and the NE embedding tables on RHOD = max(largest F(rho) knot,
-    rhoscal * max POTB) / nembd (MD_TypeDef_ForceTable.F90:949-976, 1040-1048)."""
+    pair files' largest r) and the NE embedding tables on RHOD = largest F(rho) knot / nembd,
+    the reader's RHOMX that Generate_NIST_ForceTalbe keeps (NIST_ForceTable.F90:379-413)."""
     ne = len(d["elements"])
     rmax = d["rmax"] if rmax is None else rmax
     r = (np.arange(1, ntab + 1) * (np.sqrt(rmax) / ntab)) ** 2
@@ -312,7 +312,7 @@ def lspt_tables(d, ntab=10000, nembd=10000, rhoscal=20.0, rmax=None):
             if d["frho"][i] is not None:
                 rho, drho = _spt_eval(d["rhor"][j], r, False)
                 potb[:, c], fpotb[:, c] = rho, -drho
-    rhod = max(d["rhomax"], rhoscal * potb.max()) / nembd
+    rhod = d["rhomax"] / nembd if d["rhomax"] > 0.0 else 1.0
     fembd, dfembd = np.zeros((nembd, ne)), np.zeros((nembd, ne))
     for e in range(ne):
         fembd[:, e], dfembd[:, e] = _spt_eval(d["frho"][e], np.arange(nembd) * rhod, True)
@@ -347,6 +347,47 @@ def bonny_tables(sub, rmax=5.4604375, ntab=10000, nembd=10000, rhoscal=20.0):
     out.update(fembd=fe, dfembd=dfe, rhod=rhod, nkind=nk, rmax=rmax,
                kpair=np.arange(1, 10, dtype=np.int32).reshape(3, 3), kembd=np.arange(1, 4, dtype=np.int32))
     return out
+
+
+def read_moldy(path):
+    """Moldy file (get_filedatas_moldy, Filedatas_Func_Moldy.F90:27-77): symbol, then the
+    numbers of four lines (pair a_k, pair r_k, density A_k, density R_k) and of a constants
+    line whose first entry is the lattice constant; knots scaled by it, a_k by its -3rd and
+    A_k by its -6th power."""
+    lines = open(path).read().split("\n")
+
+    def nums(s):
+        out = []
+        for tok in re.split(r"[ \t,()\[\]{}=]+", s.strip()):
+            try:
+                out.append(float(tok))
+            except ValueError:
+                pass
+        return np.array(out)
+
+    av, rv, ab, rb, c = (nums(lines[k]) for k in range(1, 6))
+    a0 = c[0]
+    return dict(symbol=lines[0].strip(), av=av / a0 ** 3, rv=rv * a0, ab=ab / a0 ** 6, rb=rb * a0, a0=a0)
+
+
+def moldy_tables(d, rmax, ntab=10000, nembd=10000, rhoscal=20.0):
+    """Moldy tables: V = sum a (r_k - r)^3 [r <= r_k] (POTR = V r / 2, FPOTR = -V' r),
+    rho = sum A (R_k - r)^3 [r <= R_k], F = -sqrt(rho) on RHOD = rhoscal max POTB / nembd."""
+    r = (np.arange(1, ntab + 1) * (np.sqrt(rmax) / ntab)) ** 2
+    x = d["rv"][None, :] - r[:, None]
+    h = (x >= 0.0)
+    v = (d["av"] * x ** 3 * h).sum(1)
+    mdv = 3.0 * (d["av"] * x ** 2 * h).sum(1)
+    y = d["rb"][None, :] - r[:, None]
+    g = (y >= 0.0)
+    rho = (d["ab"] * y ** 3 * g).sum(1)
+    mdrho = 3.0 * (d["ab"] * y ** 2 * g).sum(1)
+    rhod = rhoscal * rho.max() / nembd
+    q = np.arange(nembd) * rhod
+    safe = np.where(q > 0.0, q, 1.0)
+    return dict(potr=0.5 * v * r, fpotr=mdv * r, potb=rho, fpotb=mdrho, rhod=rhod, ntab=ntab, nembd=nembd,
+                rmax=rmax, fembd=np.where(q > 0.0, -np.sqrt(safe), 0.0),
+                dfembd=np.where(q > 0.0, -0.5 / np.sqrt(safe), 0.0))
 
 
 def make_box(lo, length, ifpd=(1, 1, 1)):

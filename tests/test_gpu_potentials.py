@@ -133,3 +133,28 @@ def test_wangjun_ti_he_force_parity(oracle):
     pos -= np.floor(pos / L_) * L_
     ityp = np.concatenate([np.ones(len(pos) - len(he), np.int32), np.full(len(he), 2, np.int32)])
     _fs_parity(oracle, ft, t, pos, ityp, L_, rc + 0.3, np.array([47.867, 4.0026]) * lt.AMU)
+
+
+def test_moldy_cu_force_parity(oracle, tmp_path):
+    from tests.test_moldy import write_moldy_cu
+    p = write_moldy_cu(str(tmp_path / "cu.moldy"))
+    ft = ForceTable.moldy(p, rmax=5.0)
+    t = oracle.Tables(oracle.moldy_tables(oracle.read_moldy(p), 5.0), oracle.EAM, 5.0)
+    pos, vel, L_ = lt.cu_config(8, 0.08, 300.0, 12)
+    n = len(pos)
+    box = oracle.make_box([0, 0, 0], L_)
+    st = np.ones(n, np.int32)
+    kv, ind = oracle.nlist(pos, st, box, 5.3, 200)
+    ref = oracle.force(pos, np.ones(n, np.int32), st, box, kv, ind, t)
+    for precision in ("fp64", "ff", "mixed"):
+        e = Engine(n, 5.3, mxkvois=128, precision=precision)
+        e.init_forcetable(ft)
+        e.copyin([(n, (0, 0, 0), tuple(L_), (1, 1, 1))], pos, vel)
+        e.calforce()
+        f = e.get_force()
+        if precision == "mixed":
+            assert np.abs(f - ref["f"]).max() / np.abs(ref["f"]).max() < 1e-6
+        else:
+            assert rel_err(f, ref["f"]) < 1e-10, precision
+            assert rel_err(e.get_den(), ref["den"]) < 1e-10, precision
+        e.close()

@@ -27,7 +27,7 @@ def test_oracle_lspt_embedding_matches_reference_export(oracle, tmp_path):
     d = oracle.read_lspt(whhe(str(tmp_path)))
     assert d["elements"] == ["W", "H", "He"] and d["rhomax"] == 10.0
     t = oracle.lspt_tables(d)
-    assert t["rhod"] == pytest.approx(1e-3, rel=1e-15)     # RHOMX = the F(rho) file's last knot
+    assert t["rhod"] == pytest.approx(1e-3, rel=1e-15)     # RHOD = the F(rho) file's last knot / NEMBD
     rows = _rows()
     assert len(rows) > 390
     for i, (rho, f, df) in rows.items():
