@@ -13,7 +13,10 @@
 #include <cmath>
 #include <cstdio>
 #include <cstdint>
+#include <cstdlib>
 #include <cstring>
+#include <utility>
+#include <vector>
 
 #include "msmgb_internal.cuh"
 
@@ -268,7 +271,7 @@ extern "C" int msmgb_destroy(msmgb_ctx *c)
                     a.dx, a.dy, a.dz, a.ityp, a.statu, a.gid, a.boxid, a.den, a.epot,
                     a.den32, a.kvois, a.indi, a.pk, a.rec, a.posfx, a.recfx, c->cell_of, c->perm, c->dbox, c->cm, c->icm,
                     c->flags, c->maxdisp, c->virial, c->scratch, c->cell_start,
-                    c->cell_cursor, c->scan_tmp, c->tab_mem, c->adj_mem, c->hvp_pair, c->pos2, c->posff2};
+                    c->cell_cursor, c->scan_tmp, c->cell_rank, c->tab_mem, c->adj_mem, c->hvp_pair, c->pos2, c->posff2};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     if (c->h_flags) cudaFreeHost(c->h_flags);
@@ -575,12 +578,42 @@ extern "C" int msmgb_copyin_simbox(msmgb_ctx *c, int nbox, const msmgb_box *boxe
         if (c->cell_start) cudaFree(c->cell_start);
         if (c->cell_cursor) cudaFree(c->cell_cursor);
         if (c->scan_tmp) cudaFree(c->scan_tmp);
-        c->cell_start = c->cell_cursor = c->scan_tmp = nullptr;
+        if (c->cell_rank) cudaFree(c->cell_rank);
+        c->cell_start = c->cell_cursor = c->scan_tmp = c->cell_rank = nullptr;
         int cap = cells + 2;
         CK(dalloc(&c->cell_start, (size_t)cap + 1), "cell alloc");
         CK(dalloc(&c->cell_cursor, (size_t)cap + 1), "cell alloc");
         CK(dalloc(&c->scan_tmp, (size_t)(cap / 4096 + 2) + 4096), "cell alloc");
+        CK(dalloc(&c->cell_rank, (size_t)cap + 1), "cell alloc");
         c->cap_cells = cap;
+    }
+    {   // storage order of the cells: per box, Morton order of (ix, iy, iz), so that atoms
+        // consecutive in memory (a warp, a CTA) occupy a compact brick of cells and their
+        // neighbour records overlap; the sentinel cell of out-of-box atoms stays last
+        const char *env = getenv("MSMGB_CELL_ORDER");
+        c->cell_row_order = env && strcmp(env, "row") == 0;
+        std::vector<int> rank((size_t)cells + 1);
+        std::vector<std::pair<unsigned long long, int>> key;
+        for (int b = 0; b < nbox; ++b) {
+            const DevBox &d = hb[(size_t)b];
+            const int nb = d.nc[0] * d.nc[1] * d.nc[2];
+            key.resize((size_t)nb);
+            for (int l = 0; l < nb; ++l) {
+                const unsigned x = (unsigned)(l % d.nc[0]), y = (unsigned)((l / d.nc[0]) % d.nc[1]),
+                               z = (unsigned)(l / (d.nc[0] * d.nc[1]));
+                unsigned long long m = 0;
+                for (int bit = 0; bit < 21; ++bit)
+                    m |= ((unsigned long long)((x >> bit) & 1u) << (3 * bit)) |
+                         ((unsigned long long)((y >> bit) & 1u) << (3 * bit + 1)) |
+                         ((unsigned long long)((z >> bit) & 1u) << (3 * bit + 2));
+                key[(size_t)l] = std::make_pair(c->cell_row_order ? (unsigned long long)l : m, l);
+            }
+            std::sort(key.begin(), key.end());
+            for (int q = 0; q < nb; ++q) rank[(size_t)(d.cell0 + key[(size_t)q].second)] = d.cell0 + q;
+        }
+        rank[(size_t)cells] = cells;
+        CK(cudaMemcpy(c->cell_rank, rank.data(), sizeof(int) * ((size_t)cells + 1), cudaMemcpyHostToDevice),
+           "cell order upload");
     }
     c->ncell_total = cells;
     c->nbox = nbox;

@@ -279,6 +279,8 @@ struct msmgb_ctx {
     msmgb::DevAtoms a{};
     msmgb::DevBox *dbox = nullptr;
     int *cell_of = nullptr, *cell_start = nullptr, *cell_cursor = nullptr, *perm = nullptr;
+    int *cell_rank = nullptr;   // storage position of each cell (cells of a box in Morton order)
+    bool cell_row_order = false;  // MSMGB_CELL_ORDER=row: x-fastest cell storage instead
     int *scan_tmp = nullptr;
     void *scratch = nullptr;           // permutation staging (size: 96 B per atom)
     double *cm = nullptr;

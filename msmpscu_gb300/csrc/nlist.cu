@@ -4,7 +4,8 @@
 // bins on the device, copies ~10 N-length arrays to the host, builds linked cells there,
 // gathers the atoms in cell order, copies them back and then runs one CTA per cell
 // (Cal_NeighboreList_Kernel2C, :907-1199).  Here every stage stays on the device:
-//   k_bin       cell id per atom (NeighboreList_IC_KERNEL formula, :759-819) + histogram
+//   k_bin       cell id per atom (NeighboreList_IC_KERNEL formula, :759-819) + histogram over
+//               the cells' storage positions (each box's cells in Morton order of (ix, iy, iz))
 //   scan        exclusive scan of the cell histogram (cell start offsets, hm_IA1th)
 //   k_scatter   counting-sort scatter, then k_cellsort orders each cell by previous index
 //               so the permutation is deterministic
@@ -32,7 +33,7 @@ __global__ void k_zero_int(int *p, int n)
 }
 
 // cell index per atom: int((x - lo)/L * NC - 1e-4), MD_NeighborsList_GPU.F90:800-811
-__global__ void k_bin(DevAtoms a, int sentinel, int *cell_of, int *count)
+__global__ void k_bin(DevAtoms a, int sentinel, int *cell_of, const int *rank, int *count)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
@@ -56,7 +57,7 @@ __global__ void k_bin(DevAtoms a, int sentinel, int *cell_of, int *count)
         c = b.cell0 + ix[0] + b.nc[0] * (ix[1] + b.nc[1] * ix[2]);
     }
     cell_of[i] = c;
-    atomicAdd(&count[c], 1);
+    atomicAdd(&count[rank[c]], 1);
 }
 
 // ---- exclusive scan (4096 items per block, block sums scanned by one block) ------------
@@ -124,11 +125,11 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_add(int *out, int n, cons
 }
 
 // ---- counting-sort scatter and deterministic per-cell order --------------------------
-__global__ void k_scatter(DevAtoms a, const int *cell_of, const int *start, int *cursor, int *perm)
+__global__ void k_scatter(DevAtoms a, const int *cell_of, const int *rank, const int *start, int *cursor, int *perm)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
-    int c = cell_of[i];
+    int c = rank[cell_of[i]];
     int slot = start[c] + atomicAdd(&cursor[c], 1);
     perm[slot] = i;
 }
@@ -233,8 +234,8 @@ __device__ __forceinline__ bool accept(float d2f, float d2lo, float d2hi, const 
 // case the periodic image of every candidate is the one of its stencil cell, so the
 // separation is the exact hi-part difference plus a per-cell shift of -L, 0 or +L, with no
 // per-candidate minimum-image test.  Narrow boxes take the minimum image per candidate.
-__global__ void __launch_bounds__(kBlock) k_build(DevAtoms a, const int *cell_of, const int *start,
-                                                  double rc2, float d2lo, float d2hi)
+__global__ void __launch_bounds__(kBlock) k_build(DevAtoms a, const int *cell_of, const int *rank,
+                                                  const int *start, double rc2, float d2lo, float d2hi)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
@@ -276,7 +277,7 @@ __global__ void __launch_bounds__(kBlock) k_build(DevAtoms a, const int *cell_of
             if (j3[k] < 0 || j3[k] >= nc[k]) skip = true;
         }
         if (skip) continue;
-        const int g = cell0 + j3[0] + nc[0] * (j3[1] + nc[1] * j3[2]);
+        const int g = rank[cell0 + j3[0] + nc[0] * (j3[1] + nc[1] * j3[2])];
         const int j0 = start[g], e = start[g + 1];
         if (wide) {
             for (int j = j0; j < e; ++j) {
@@ -342,7 +343,7 @@ int build_list(msmgb_ctx *c)
     DevAtoms a = c->a;
 
     k_zero_int<<<nblk(ncs + 1, kBlock), kBlock, 0, s>>>(count, ncs + 1);
-    k_bin<<<nblk(n, kBlock), kBlock, 0, s>>>(a, c->ncell_total, c->cell_of, count);
+    k_bin<<<nblk(n, kBlock), kBlock, 0, s>>>(a, c->ncell_total, c->cell_of, c->cell_rank, count);
     // exclusive scan over ncs + 1 entries: start[ncs] = n
     int ntile = nblk(ncs + 1, kScanTile);
     k_scan_tile<<<ntile, kScanThreads, 0, s>>>(count, c->cell_start, ncs + 1, c->scan_tmp);
@@ -353,7 +354,7 @@ int build_list(msmgb_ctx *c)
         c->launches += 2;
     }
     k_zero_int<<<nblk(ncs + 1, kBlock), kBlock, 0, s>>>(count, ncs + 1);
-    k_scatter<<<nblk(n, kBlock), kBlock, 0, s>>>(a, c->cell_of, c->cell_start, count, c->perm);
+    k_scatter<<<nblk(n, kBlock), kBlock, 0, s>>>(a, c->cell_of, c->cell_rank, c->cell_start, count, c->perm);
     k_cellsort<<<nblk(ncs, kBlock), kBlock, 0, s>>>(ncs, c->cell_start, c->perm);
     Stage st = stage_of(c->scratch, c->cap_atoms);
     k_permute<<<nblk(n, kBlock), kBlock, 0, s>>>(a, st, c->perm, c->cell_of);
@@ -361,7 +362,7 @@ int build_list(msmgb_ctx *c)
     double rc2 = c->p.rc_nl * c->p.rc_nl;
     float d2lo, d2hi;
     prefilter_band(c, rc2, &d2lo, &d2hi);
-    k_build<<<nblk(n, kBlock), kBlock, 0, s>>>(a, c->cell_of, c->cell_start, rc2, d2lo, d2hi);
+    k_build<<<nblk(n, kBlock), kBlock, 0, s>>>(a, c->cell_of, c->cell_rank, c->cell_start, rc2, d2lo, d2hi);
     c->launches += 6;
     return check_launch(c, "neighbour list");
 }
