@@ -57,7 +57,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
             jobs.append(ex.submit(_compile, src, obj, nvcc, extra))
         objs = [j.result() for j in jobs]
     tmp = LIB + ".tmp"
-    cmd = [nvcc, "-shared", *ARCH, "-o", tmp, *objs, "-cudart", "static"]
+    cmd = [nvcc, "-shared", *ARCH, "-o", tmp, *objs, "-cudart", "static", "-ldl"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n" + r.stdout + r.stderr)

@@ -137,10 +137,18 @@ __global__ void __launch_bounds__(kBlock) k_update_pos(DevAtoms a, const double 
 {
     int s = blockIdx.x * blockDim.x + threadIdx.x;
     double d2 = 0.0;
+    bool ok = false;
+    double x[3] = {0.0, 0.0, 0.0};
     if (s < a.n) {
         const int n = a.n, g = a.gid[s];
+        x[0] = xp[g];
+        x[1] = xp[n + g];
+        x[2] = xp[2 * n + g];
+        ok = isfinite(x[0]) && isfinite(x[1]) && isfinite(x[2]);
+        if (!ok) atomicOr(&a.flags[kFlagErr], kErrNonFinite);   // that atom keeps its old position
+    }
+    if (ok) {
         const DevBox &b = a.box[a.boxid[s]];
-        double x[3] = {xp[g], xp[n + g], xp[2 * n + g]};
 #pragma unroll
         for (int k = 0; k < 3; ++k)
             if (b.ifpd[k]) x[k] -= floor((x[k] - b.lo[k]) / b.len[k]) * b.len[k];
@@ -196,6 +204,10 @@ extern "C" int msmgb_create(msmgb_ctx **out, const msmgb_params *p)
     }
     msmgb_ctx *c = new msmgb_ctx();
     c->p = *p;
+    {
+        const char *chk = getenv("MSMGB_CHECK_LISTS");
+        c->check_lists = chk && chk[0] == '1';
+    }
     c->cap_atoms = p->max_atoms;
     c->cap_boxes = p->max_boxes;
     int rc = use_device(c);
@@ -339,6 +351,8 @@ static int poll_flags(msmgb_ctx *c)
         if (e & kErrRho) return set_err(c, MSMGB_ERR_RHO_RANGE, "electron density beyond the F(rho) table");
         if (e & kErrTimeout)
             return set_err(c, MSMGB_ERR_TIMEOUT, "a bounded wait for an asynchronous list copy ran out");
+        if (e & kErrNonFinite) return set_err(c, MSMGB_ERR_ARG, "a position is not a finite number");
+        if (e & kErrBadList) return set_err(c, MSMGB_ERR_CUDA, "neighbour list validation failed");
     }
     return MSMGB_OK;
 }
@@ -346,6 +360,7 @@ static int poll_flags(msmgb_ctx *c)
 // ---- force table ----------------------------------------------------------------------------
 extern "C" int msmgb_init_forcetable(msmgb_ctx *c, const msmgb_forcetable *ft)
 {
+    NvtxRange nvtx_range("msmgb_init_forcetable");
     if (!c || !ft) return MSMGB_ERR_ARG;
     if (ft->pottype != MSMGB_FS_TYPE && ft->pottype != MSMGB_EAM_TYPE)
         return set_err(c, MSMGB_ERR_ARG, "unknown potential type");
@@ -519,6 +534,7 @@ extern "C" int msmgb_clear_forcetable(msmgb_ctx *c)
 extern "C" int msmgb_copyin_simbox(msmgb_ctx *c, int nbox, const msmgb_box *boxes, const int *ityp,
                                    const int *statu, const double *xp, const double *xp1)
 {
+    NvtxRange nvtx_range("msmgb_copyin_simbox");
     if (!c || !boxes || !ityp || !statu || !xp || nbox < 1) return MSMGB_ERR_ARG;
     if (nbox > c->cap_boxes) return set_err(c, MSMGB_ERR_CAPACITY, "more boxes than max_boxes");
     long total = 0;
@@ -528,6 +544,9 @@ extern "C" int msmgb_copyin_simbox(msmgb_ctx *c, int nbox, const msmgb_box *boxe
     }
     if (total > c->cap_atoms) return set_err(c, MSMGB_ERR_CAPACITY, "more atoms than max_atoms");
     if (total < 1) return set_err(c, MSMGB_ERR_ARG, "no atoms");
+    for (long q = 0; q < 3 * total; ++q)
+        if (!std::isfinite(xp[q]) || (xp1 && !std::isfinite(xp1[q])))
+            return set_err(c, MSMGB_ERR_ARG, "a position or velocity is not a finite number");
     RET(use_device(c));
     const int n = (int)total;
     std::vector<DevBox> hb((size_t)nbox);
@@ -684,6 +703,7 @@ static int copy_out_doubles(msmgb_ctx *c, const double *s0, const double *s1, co
 extern "C" int msmgb_copyout_simbox(msmgb_ctx *c, double *xp, double *xp1, int *statu, double *dis,
                                     int order)
 {
+    NvtxRange nvtx_range("msmgb_copyout_simbox");
     if (!c) return MSMGB_ERR_ARG;
     RET(need_state(c));
     RET(use_device(c));
@@ -712,6 +732,7 @@ extern "C" int msmgb_copyout_simbox(msmgb_ctx *c, double *xp, double *xp1, int *
 
 extern "C" int msmgb_update_positions(msmgb_ctx *c, const double *xp)
 {
+    NvtxRange nvtx_range("msmgb_update_positions");
     if (!c || !xp) return MSMGB_ERR_ARG;
     RET(need_state(c));
     RET(use_device(c));
@@ -725,6 +746,7 @@ extern "C" int msmgb_update_positions(msmgb_ctx *c, const double *xp)
     unsigned long long md = 0;
     CK(cudaMemcpyAsync(&md, c->maxdisp, sizeof(md), cudaMemcpyDeviceToHost, c->stream), "flag read");
     CK(cudaStreamSynchronize(c->stream), "synchronize");
+    RET(poll_flags(c));
     double d2;
     memcpy(&d2, &md, sizeof(d2));
     const double thr = c->p.skin_trigger > 0.0 ? c->p.skin_trigger : 0.0;
@@ -736,6 +758,7 @@ extern "C" int msmgb_update_positions(msmgb_ctx *c, const double *xp)
 
 extern "C" int msmgb_copyout_force(msmgb_ctx *c, double *fp, int order)
 {
+    NvtxRange nvtx_range("msmgb_copyout_force");
     if (!c || !fp) return MSMGB_ERR_ARG;
     RET(need_state(c));
     RET(use_device(c));
@@ -779,6 +802,7 @@ extern "C" int msmgb_copyout_gid(msmgb_ctx *c, int *gid)
 // ---- neighbour list ---------------------------------------------------------------------------
 extern "C" int msmgb_cal_neighborelist(msmgb_ctx *c)
 {
+    NvtxRange nvtx_range("msmgb_cal_neighborelist");
     if (!c) return MSMGB_ERR_ARG;
     RET(need_state(c));
     RET(use_device(c));
@@ -857,6 +881,7 @@ static int force_passes(msmgb_ctx *c, bool virial, bool epot)
 
 extern "C" int msmgb_calforce(msmgb_ctx *c)
 {
+    NvtxRange nvtx_range("msmgb_calforce");
     if (!c) return MSMGB_ERR_ARG;
     RET(ready_for_force(c));
     RET(force_passes(c, false, false));
@@ -867,6 +892,7 @@ extern "C" int msmgb_calforce(msmgb_ctx *c)
 
 extern "C" int msmgb_calptensor(msmgb_ctx *c, double *vt)
 {
+    NvtxRange nvtx_range("msmgb_calptensor");
     if (!c) return MSMGB_ERR_ARG;
     RET(ready_for_force(c));
     RET(force_passes(c, true, false));
@@ -887,6 +913,7 @@ extern "C" int msmgb_calptensor(msmgb_ctx *c, double *vt)
 
 extern "C" int msmgb_calepot(msmgb_ctx *c)
 {
+    NvtxRange nvtx_range("msmgb_calepot");
     if (!c) return MSMGB_ERR_ARG;
     RET(ready_for_force(c));
     RET(launch_density(c, true));
@@ -895,6 +922,7 @@ extern "C" int msmgb_calepot(msmgb_ctx *c)
 
 extern "C" int msmgb_calden(msmgb_ctx *c)
 {
+    NvtxRange nvtx_range("msmgb_calden");
     if (!c) return MSMGB_ERR_ARG;
     RET(ready_for_force(c));
     RET(launch_density(c, false));
@@ -903,6 +931,7 @@ extern "C" int msmgb_calden(msmgb_ctx *c)
 
 extern "C" int msmgb_cal_atomic_stress(msmgb_ctx *c, double *ap, int order)
 {
+    NvtxRange nvtx_range("msmgb_cal_atomic_stress");
     if (!c || !ap) return MSMGB_ERR_ARG;
     RET(ready_for_force(c));
     // 72 B per atom fit in the 100 B per atom of the scratch buffer
@@ -917,6 +946,7 @@ extern "C" int msmgb_cal_atomic_stress(msmgb_ctx *c, double *ap, int order)
 // ---- integrator -------------------------------------------------------------------------------
 extern "C" int msmgb_predictor(msmgb_ctx *c, double h)
 {
+    NvtxRange nvtx_range("msmgb_predictor");
     if (!c) return MSMGB_ERR_ARG;
     RET(need_state(c));
     if (!c->have_masses) return set_err(c, MSMGB_ERR_ARG, "no masses: call msmgb_set_masses");
@@ -928,6 +958,7 @@ extern "C" int msmgb_predictor(msmgb_ctx *c, double h)
 
 extern "C" int msmgb_correction(msmgb_ctx *c, double h)
 {
+    NvtxRange nvtx_range("msmgb_correction");
     if (!c) return MSMGB_ERR_ARG;
     RET(need_state(c));
     if (!c->have_masses) return set_err(c, MSMGB_ERR_ARG, "no masses: call msmgb_set_masses");
@@ -1198,6 +1229,7 @@ static int issue_steps(msmgb_ctx *c, int nsteps, double h)
 
 extern "C" int msmgb_run_steps(msmgb_ctx *c, int nsteps, double h, int *rebuilds)
 {
+    NvtxRange nvtx_range("msmgb_run_steps");
     if (!c || nsteps < 0) return MSMGB_ERR_ARG;
     if (!c->have_masses) return set_err(c, MSMGB_ERR_ARG, "no masses: call msmgb_set_masses");
     RET(ready_for_force(c));
@@ -1220,6 +1252,7 @@ extern "C" int msmgb_run_steps(msmgb_ctx *c, int nsteps, double h, int *rebuilds
 // the list, the forces and the step graphs
 extern "C" int msmgb_enqueue_steps(msmgb_ctx *c, int nsteps, double h)
 {
+    NvtxRange nvtx_range("msmgb_enqueue_steps");
     if (!c || nsteps < 0) return MSMGB_ERR_ARG;
     if (!c->have_masses) return set_err(c, MSMGB_ERR_ARG, "no masses: call msmgb_set_masses");
     RET(ready_for_force(c));
@@ -1233,6 +1266,7 @@ extern "C" int msmgb_enqueue_steps(msmgb_ctx *c, int nsteps, double h)
 
 extern "C" int msmgb_finish_steps(msmgb_ctx *c, double h, int *rebuilds)
 {
+    NvtxRange nvtx_range("msmgb_finish_steps");
     if (!c) return MSMGB_ERR_ARG;
     RET(use_device(c));
     RET(launch_correct(c, h, true));
@@ -1255,6 +1289,7 @@ static int ensure_hvp_pair(msmgb_ctx *c)
 
 extern "C" int msmgb_hvp(msmgb_ctx *c, const double *v, double *hv)
 {
+    NvtxRange nvtx_range("msmgb_hvp");
     if (!c || !v || !hv) return MSMGB_ERR_ARG;
     RET(ready_for_force(c));
     RET(ensure_hvp_pair(c));
@@ -1279,6 +1314,7 @@ extern "C" int msmgb_cr_param_tables(const double *prm, double rmax, int ntab, d
 extern "C" int msmgb_param_adjoint(msmgb_ctx *c, int pot, const double *prm, const double *ft,
                                    double *loss, double *grad)
 {
+    NvtxRange nvtx_range("msmgb_param_adjoint");
     if (!c || !prm || !ft || !grad) return MSMGB_ERR_ARG;
     if (pot != MSMGB_POT_CR) return set_err(c, MSMGB_ERR_ARG, "the adjoint supports the Cleri-Rosato parameters");
     RET(ready_for_force(c));

@@ -24,7 +24,18 @@
 
 #include "../../include/msmgb.h"
 
+#include <nvtx3/nvToolsExt.h>
+
 namespace msmgb {
+
+// NVTX range around an entry point of the C ABI (seen by nsys / ncu range filters; costs a
+// function-pointer test when no profiler is attached)
+struct NvtxRange {
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange &) = delete;
+    NvtxRange &operator=(const NvtxRange &) = delete;
+};
 
 constexpr int kBlock = 256;
 constexpr int kMaxGroups = 16;          // mp_MXGROUP, MD_Const.F90:77
@@ -34,6 +45,8 @@ constexpr int kErrOverflow = 1;
 constexpr int kErrOutOfBox = 2;
 constexpr int kErrRho = 4;
 constexpr int kErrTimeout = 8;
+constexpr int kErrNonFinite = 16;   // a position that is not a finite number
+constexpr int kErrBadList = 32;     // list validation (MSMGB_CHECK_LISTS=1) found a bad entry
 
 // device flag words
 enum {
@@ -281,6 +294,7 @@ struct msmgb_ctx {
     int *cell_of = nullptr, *cell_start = nullptr, *cell_cursor = nullptr, *perm = nullptr;
     int *cell_rank = nullptr;   // storage position of each cell (cells of a box in Morton order)
     bool cell_row_order = false;  // MSMGB_CELL_ORDER=row: x-fastest cell storage instead
+    bool check_lists = false;     // MSMGB_CHECK_LISTS=1: validate every list after its build
     int *scan_tmp = nullptr;
     void *scratch = nullptr;           // permutation staging (size: 96 B per atom)
     double *cm = nullptr;

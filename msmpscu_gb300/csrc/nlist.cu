@@ -45,6 +45,7 @@ __global__ void k_bin(DevAtoms a, int sentinel, int *cell_of, const int *rank, i
         const DevBox &b = a.box[a.boxid[i]];
         double4_32a p = a.pos[i];
         double xp[3] = {p.x, p.y, p.z};
+        if (!(isfinite(p.x) && isfinite(p.y) && isfinite(p.z))) atomicOr(&a.flags[kFlagErr], kErrNonFinite);
         int ix[3];
         bool bad = false;
         for (int k = 0; k < 3; ++k) {
@@ -314,6 +315,23 @@ __global__ void __launch_bounds__(kBlock) k_build(DevAtoms a, const int *cell_of
     atomicMax(&a.flags[kFlagMaxK], nn);
 }
 
+// Debug validation of a freshly built list (no trap): every stored neighbour index lies in
+// [0, n), differs from the atom itself and belongs to the same box; KVOIS lies in [0, MXKVOIS].
+__global__ void k_check_list(DevAtoms a)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    const int m = a.kvois[i];
+    bool bad = m < 0 || m > a.mxk;
+    const int mm = bad ? 0 : m;
+    const size_t ld = (size_t)a.ld;
+    for (int k = 0; k < mm && !bad; ++k) {
+        const int j = a.indi[(size_t)k * ld + i];
+        bad = j < 0 || j >= a.n || j == i || a.boxid[j] != a.boxid[i];
+    }
+    if (bad) atomicOr(&a.flags[kFlagErr], kErrBadList);
+}
+
 static inline int nblk(long n, int b) { return (int)((n + b - 1) / b); }
 
 // Margin of the FP32 prefilter: it uses the hi parts of the shifted coordinates
@@ -364,6 +382,10 @@ int build_list(msmgb_ctx *c)
     prefilter_band(c, rc2, &d2lo, &d2hi);
     k_build<<<nblk(n, kBlock), kBlock, 0, s>>>(a, c->cell_of, c->cell_rank, c->cell_start, rc2, d2lo, d2hi);
     c->launches += 6;
+    if (c->check_lists) {
+        k_check_list<<<nblk(n, kBlock), kBlock, 0, s>>>(a);
+        c->launches += 1;
+    }
     return check_launch(c, "neighbour list");
 }
 

@@ -194,3 +194,52 @@ def test_embedding_density_beyond_table_reported(precision):
     e.calforce()
     assert np.isfinite(e.get_force()).all()
     e.close()
+
+
+def test_non_finite_positions_rejected(oracle):
+    """A NaN or infinite coordinate is an argument error: at copy-in (host check, nothing is
+    uploaded) and in a position update (device check; the atom keeps its old position)."""
+    from msmpscu_gb300 import MSMError
+    from msmpscu_gb300 import _lib as L
+    pos, vel, L_ = lt.cu_config(5, 0.05, 300.0, 3)
+    n = len(pos)
+    e = Engine(n, lt.CU_RC_NL, mxkvois=64)
+    e.init_forcetable(ForceTable.cleri_rosato(**lt.CU_CR, rc=lt.CU_RC))
+    bad = pos.copy()
+    bad[7, 1] = np.nan
+    with pytest.raises(MSMError) as ex:
+        e.copyin([(n, (0, 0, 0), tuple(L_), (1, 1, 1))], bad)
+    assert ex.value.code == L.ERR_ARG
+    e.copyin([(n, (0, 0, 0), tuple(L_), (1, 1, 1))], pos)
+    e.calforce()
+    f0 = e.get_force()
+    upd = pos.copy()
+    upd[11, 2] = np.inf
+    with pytest.raises(MSMError) as ex:
+        e.update_positions(upd)
+    assert ex.value.code == L.ERR_ARG
+    e.update_positions(pos)                 # the context stays usable
+    e.calforce()
+    assert np.array_equal(e.get_force(), f0)
+    e.close()
+
+
+def test_list_validation_mode(oracle, monkeypatch):
+    """MSMGB_CHECK_LISTS=1 validates every list after its build (indices in range, not the atom
+    itself, same box, counts within MXKVOIS) with an extra kernel; a correct run passes it,
+    including the rebuilds inside the MD step graphs, and gives the same trajectory."""
+    pos, vel, L_ = lt.cu_config(6, 0.05, 900.0, 13)
+    n = len(pos)
+    out = []
+    for flag in ("0", "1"):
+        monkeypatch.setenv("MSMGB_CHECK_LISTS", flag)
+        e = Engine(n, lt.CU_RC_NL, mxkvois=64, skin_trigger=0.05)
+        e.init_forcetable(ForceTable.cleri_rosato(**lt.CU_CR, rc=lt.CU_RC))
+        e.set_masses([lt.CU_MASS])
+        e.copyin([(n, (0, 0, 0), tuple(L_), (1, 1, 1))], pos, vel)
+        l0 = e.launches
+        e.run_steps(40, 1.0)
+        out.append((e.get_state()[0], e.launches - l0))
+        e.close()
+    assert np.array_equal(out[0][0], out[1][0])
+    assert out[1][1] > out[0][1]           # the validation kernel ran
