@@ -102,6 +102,9 @@ __global__ void k_pack(DevAtoms a, const double *xp, const double *xp1, const in
     int n = a.n;
     if (i >= n) return;
     double x = xp[i], y = xp[n + i], z = xp[2 * n + i];
+    bool fin = isfinite(x) && isfinite(y) && isfinite(z);
+    if (xp1) fin = fin && isfinite(xp1[i]) && isfinite(xp1[n + i]) && isfinite(xp1[2 * n + i]);
+    if (!fin) atomicOr(&a.flags[kFlagErr], kErrNonFinite);
     a.pos[i] = make_double4_32a(x, y, z, 0.0);
     PosFF f = make_posff(x, y, z, a.box[boxid[i]]);
     a.posff[i] = f;
@@ -544,9 +547,6 @@ extern "C" int msmgb_copyin_simbox(msmgb_ctx *c, int nbox, const msmgb_box *boxe
     }
     if (total > c->cap_atoms) return set_err(c, MSMGB_ERR_CAPACITY, "more atoms than max_atoms");
     if (total < 1) return set_err(c, MSMGB_ERR_ARG, "no atoms");
-    for (long q = 0; q < 3 * total; ++q)
-        if (!std::isfinite(xp[q]) || (xp1 && !std::isfinite(xp1[q])))
-            return set_err(c, MSMGB_ERR_ARG, "a position or velocity is not a finite number");
     RET(use_device(c));
     const int n = (int)total;
     std::vector<DevBox> hb((size_t)nbox);
@@ -654,10 +654,18 @@ extern "C" int msmgb_copyin_simbox(msmgb_ctx *c, int nbox, const msmgb_box *boxe
     CK(cudaMemcpy(dty, ityp, sizeof(int) * (size_t)n, cudaMemcpyHostToDevice), "copyin");
     CK(cudaMemcpy(dst, statu, sizeof(int) * (size_t)n, cudaMemcpyHostToDevice), "copyin");
     CK(cudaMemcpy(dbx, boxid.data(), sizeof(int) * (size_t)n, cudaMemcpyHostToDevice), "copyin");
+    CK(cudaMemsetAsync(c->flags, 0, sizeof(int) * kFlagWords, c->stream), "flag clear");
     k_pack<<<nblk(n, kBlock), kBlock, 0, c->stream>>>(c->a, dxp, xp1 ? dxp1 : nullptr, dty, dst, dbx);
     c->launches += 1;
     RET(check_launch(c, "pack"));
-    CK(cudaMemsetAsync(c->flags, 0, sizeof(int) * kFlagWords, c->stream), "flag clear");
+    {   // a non-finite position or velocity leaves the context without a state
+        const int rc = poll_flags(c);
+        if (rc != MSMGB_OK) {
+            c->n = 0;
+            c->a.n = 0;
+            return rc;
+        }
+    }
     CK(cudaMemsetAsync(c->maxdisp, 0, sizeof(unsigned long long), c->stream), "flag clear");
     CK(cudaStreamSynchronize(c->stream), "synchronize");
     c->list_valid = false;

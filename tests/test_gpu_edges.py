@@ -197,8 +197,9 @@ def test_embedding_density_beyond_table_reported(precision):
 
 
 def test_non_finite_positions_rejected(oracle):
-    """A NaN or infinite coordinate is an argument error: at copy-in (host check, nothing is
-    uploaded) and in a position update (device check; the atom keeps its old position)."""
+    """A NaN or infinite coordinate is an argument error: at copy-in (checked in the pack
+    kernel; the context is left without a state until a valid copy-in) and in a position
+    update (the atom keeps its old position)."""
     from msmpscu_gb300 import MSMError
     from msmpscu_gb300 import _lib as L
     pos, vel, L_ = lt.cu_config(5, 0.05, 300.0, 3)
@@ -210,6 +211,8 @@ def test_non_finite_positions_rejected(oracle):
     with pytest.raises(MSMError) as ex:
         e.copyin([(n, (0, 0, 0), tuple(L_), (1, 1, 1))], bad)
     assert ex.value.code == L.ERR_ARG
+    with pytest.raises(MSMError):
+        e.calforce()                        # no state after the failed copy-in
     e.copyin([(n, (0, 0, 0), tuple(L_), (1, 1, 1))], pos)
     e.calforce()
     f0 = e.get_force()
