@@ -605,12 +605,20 @@ extern "C" int msmgb_copyin_simbox(msmgb_ctx *c, int nbox, const msmgb_box *boxe
         CK(dalloc(&c->scan_tmp, (size_t)(cap / 4096 + 2) + 4096), "cell alloc");
         CK(dalloc(&c->cell_rank, (size_t)cap + 1), "cell alloc");
         c->cap_cells = cap;
+        c->rank_layout.clear();
     }
-    {   // storage order of the cells: per box, Morton order of (ix, iy, iz), so that atoms
-        // consecutive in memory (a warp, a CTA) occupy a compact brick of cells and their
-        // neighbour records overlap; the sentinel cell of out-of-box atoms stays last
+    std::vector<int> layout;
+    {
         const char *env = getenv("MSMGB_CELL_ORDER");
         c->cell_row_order = env && strcmp(env, "row") == 0;
+        layout.push_back(c->cell_row_order ? 1 : 0);
+        for (int b = 0; b < nbox; ++b)
+            for (int k = 0; k < 3; ++k) layout.push_back(hb[(size_t)b].nc[k]);
+    }
+    if (layout != c->rank_layout) {   // storage order of the cells: per box, Morton order of
+        // (ix, iy, iz), so that atoms consecutive in memory (a warp, a CTA) occupy a compact
+        // brick of cells and their neighbour records overlap; the sentinel cell of out-of-box
+        // atoms stays last.  Made once per cell-grid layout.
         std::vector<int> rank((size_t)cells + 1);
         std::vector<std::pair<unsigned long long, int>> key;
         for (int b = 0; b < nbox; ++b) {
@@ -633,6 +641,7 @@ extern "C" int msmgb_copyin_simbox(msmgb_ctx *c, int nbox, const msmgb_box *boxe
         rank[(size_t)cells] = cells;
         CK(cudaMemcpy(c->cell_rank, rank.data(), sizeof(int) * ((size_t)cells + 1), cudaMemcpyHostToDevice),
            "cell order upload");
+        c->rank_layout = layout;
     }
     c->ncell_total = cells;
     c->nbox = nbox;

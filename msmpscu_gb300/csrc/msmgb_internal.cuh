@@ -295,6 +295,7 @@ struct msmgb_ctx {
     int *cell_rank = nullptr;   // storage position of each cell (cells of a box in Morton order)
     bool cell_row_order = false;  // MSMGB_CELL_ORDER=row: x-fastest cell storage instead
     bool check_lists = false;     // MSMGB_CHECK_LISTS=1: validate every list after its build
+    std::vector<int> rank_layout; // cell grids (and order) the uploaded cell_rank was made for
     int *scan_tmp = nullptr;
     void *scratch = nullptr;           // permutation staging (size: 96 B per atom)
     double *cm = nullptr;
