@@ -246,3 +246,82 @@ def test_list_validation_mode(oracle, monkeypatch):
         e.close()
     assert np.array_equal(out[0][0], out[1][0])
     assert out[1][1] > out[0][1]           # the validation kernel ran
+
+
+def _sparse_config():
+    """Isolated atoms (empty lists, rho = 0), a dimer and a 13-atom fcc cluster in a large
+    periodic box."""
+    L_ = np.array([40.0, 40.0, 40.0])
+    iso = np.array([[3.0, 3.0, 3.0], [35.0, 5.0, 20.0], [20.0, 35.0, 8.0]])
+    dimer = np.array([[10.0, 30.0, 30.0], [12.4, 30.3, 30.1]])
+    a = lt.CU_A
+    cl = np.array([[0, 0, 0], [0.5, 0.5, 0], [0.5, 0, 0.5], [0, 0.5, 0.5], [-0.5, 0.5, 0], [0.5, -0.5, 0],
+                   [-0.5, -0.5, 0], [-0.5, 0, 0.5], [0.5, 0, -0.5], [-0.5, 0, -0.5], [0, -0.5, 0.5],
+                   [0, 0.5, -0.5], [0, -0.5, -0.5]]) * a + np.array([20.0, 20.0, 20.0])
+    cl = cl + np.random.default_rng(4).normal(scale=0.05, size=cl.shape)
+    return np.vstack([iso, dimer, cl]), L_
+
+
+@pytest.mark.parametrize("kind", ["fs", "eam"])
+def test_isolated_atoms_dimer_cluster(oracle, kind):
+    pos, L_ = _sparse_config()
+    n = len(pos)
+    if kind == "fs":
+        ft, t, rc = ForceTable.cleri_rosato(**lt.CU_CR, rc=lt.CU_RC), cu_tables(oracle), lt.CU_RC_NL
+    else:
+        from tests.helpers import w_tables
+        ft, t, rc = ForceTable.marinica_eam2(), w_tables(oracle), lt.W_RC_NL
+    box = oracle.make_box([0, 0, 0], L_)
+    st = np.ones(n, np.int32)
+    kv, ind = oracle.nlist(pos, st, box, rc, 64)
+    assert (kv == 0).sum() == 3
+    ref = oracle.force(pos, np.ones(n, np.int32), st, box, kv, ind, t)
+    for precision in ("fp64", "ff", "mixed"):
+        e = Engine(n, rc, mxkvois=64, precision=precision)
+        e.init_forcetable(ft)
+        e.copyin([(n, (0, 0, 0), tuple(L_), (1, 1, 1))], pos)
+        e.calforce()
+        f = e.get_force()
+        assert np.all(f[:3] == 0.0), precision
+        tol = 1e-6 if precision == "mixed" else 1e-10
+        assert np.abs(f - ref["f"]).max() <= tol * np.abs(ref["f"]).max(), precision
+        if precision != "mixed":
+            e.calepot()
+            assert rel_err(e.get_epot(), ref["epot"]) < 1e-10, precision
+        e.close()
+
+
+def test_atoms_on_box_faces(oracle):
+    """Atoms exactly on the lower faces and on the upper faces (x = lo + L) of a periodic
+    box: binned inside (the reference's -1e-4 cell rule), same neighbour sets and forces as
+    the oracle."""
+    pos, vel, L_ = lt.cu_config(6, 0.0, 0.0, 1)              # the exact lattice
+    pos = pos.copy()
+    a = lt.CU_A
+
+    def site(p):
+        return int(np.nonzero(np.all(np.abs(pos - p) < 1e-9, axis=1))[0][0])
+
+    i1, i2, i3 = site([0.0, 0.5 * a, 0.5 * a]), site([0.5 * a, 0.0, 0.5 * a]), site([0.0, 0.0, 0.0])
+    i0 = site([0.0, 0.0, a])                                   # stays on the lower x and y faces
+    face = pos[[i0, i1, i2, i3]].copy()
+    face[1, 0] = L_[0]                                         # x = L face
+    face[2, 1] = L_[1]                                         # y = L face
+    face[3] = L_                                               # the far corner
+    pos = pos + np.random.default_rng(2).normal(scale=0.05, size=pos.shape)
+    pos -= np.floor(pos / L_) * L_
+    pos[[i0, i1, i2, i3]] = face
+    n = len(pos)
+    box = oracle.make_box([0, 0, 0], L_)
+    st = np.ones(n, np.int32)
+    kv, ind = oracle.nlist(pos, st, box, lt.CU_RC_NL, 96)
+    ref = oracle.force(pos, np.ones(n, np.int32), st, box, kv, ind, cu_tables(oracle))
+    e = Engine(n, lt.CU_RC_NL, mxkvois=96)
+    e.init_forcetable(ForceTable.cleri_rosato(**lt.CU_CR, rc=lt.CU_RC))
+    e.copyin([(n, (0, 0, 0), tuple(L_), (1, 1, 1))], pos)
+    e.cal_neighborelist()
+    gk, gi = e.get_neighborelist()
+    assert sorted_sets(gk, gi) == sorted_sets(kv, ind)
+    e.calforce()
+    assert rel_err(e.get_force(), ref["f"]) < 1e-10
+    e.close()
