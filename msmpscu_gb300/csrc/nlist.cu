@@ -235,7 +235,7 @@ __device__ __forceinline__ bool accept(float d2f, float d2lo, float d2hi, const 
 // case the periodic image of every candidate is the one of its stencil cell, so the
 // separation is the exact hi-part difference plus a per-cell shift of -L, 0 or +L, with no
 // per-candidate minimum-image test.  Narrow boxes take the minimum image per candidate.
-__global__ void __launch_bounds__(kBlock) k_build(DevAtoms a, const int *cell_of, const int *rank,
+__global__ void __launch_bounds__(kBlock, 6) k_build(DevAtoms a, const int *cell_of, const int *rank,
                                                   const int *start, double rc2, float d2lo, float d2hi)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
