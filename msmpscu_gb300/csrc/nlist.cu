@@ -195,7 +195,9 @@ __global__ void k_copyback(DevAtoms a, Stage s, int *cell_of)
     if (i >= a.n) return;
     double4_32a p = s.pos[i];
     a.pos[i] = p;
-    a.posff[i] = make_posff(p.x, p.y, p.z, a.box[s.boxid[i]]);
+    const PosFF f = make_posff(p.x, p.y, p.z, a.box[s.boxid[i]]);
+    a.posff[i] = f;
+    a.pos_bld[i] = make_float4(f.hx, f.hy, f.hz, 0.0f);   // skin reference and k_build candidates
     a.vx[i] = s.vx[i]; a.vy[i] = s.vy[i]; a.vz[i] = s.vz[i];
     a.dx[i] = s.dx[i]; a.dy[i] = s.dy[i]; a.dz[i] = s.dz[i];
     a.ityp[i] = s.ityp[i];
@@ -241,7 +243,6 @@ __global__ void __launch_bounds__(kBlock, 6) k_build(DevAtoms a, const int *cell
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
     const PosFF pf = a.posff[i];
-    a.pos_bld[i] = make_float4(pf.hx, pf.hy, pf.hz, 0.0f);
     if (a.statu[i] & MSMGB_STATU_OUTOFBOX) { a.kvois[i] = 0; return; }
     const DevBox &b = a.box[a.boxid[i]];
     int nc[3], pd[3];
@@ -262,7 +263,7 @@ __global__ void __launch_bounds__(kBlock, 6) k_build(DevAtoms a, const int *cell
     const size_t ld = (size_t)a.ld;
     const int mxk = a.mxk;
     int *const indi = a.indi + i;
-    const float4 *const hi = reinterpret_cast<const float4 *>(a.posff);   // record = 2 float4
+    const float4 *const hi = a.pos_bld;   // hi parts, 16 B per atom (written by k_copyback)
     for (int s = 0; s < 27; ++s) {
         int j3[3] = {ix + c_nix[s], iy + c_niy[s], iz + c_niz[s]};
         float sh[3];
@@ -282,7 +283,7 @@ __global__ void __launch_bounds__(kBlock, 6) k_build(DevAtoms a, const int *cell
         const int j0 = start[g], e = start[g + 1];
         if (wide) {
             for (int j = j0; j < e; ++j) {
-                const float4 q = hi[2 * (size_t)j];
+                const float4 q = hi[j];
                 const float sx = (pf.hx - q.x) + sh[0];      // hi difference exact (Sterbenz)
                 const float sy = (pf.hy - q.y) + sh[1];
                 const float sz = (pf.hz - q.z) + sh[2];
@@ -295,7 +296,7 @@ __global__ void __launch_bounds__(kBlock, 6) k_build(DevAtoms a, const int *cell
         } else {
             const float h0 = b.halff[0], h1 = b.halff[1], h2 = b.halff[2];
             for (int j = j0; j < e; ++j) {
-                const float4 q = hi[2 * (size_t)j];
+                const float4 q = hi[j];
                 const float sx = mi32(pf.hx - q.x, lf[0], h0, pd[0]);
                 const float sy = mi32(pf.hy - q.y, lf[1], h1, pd[1]);
                 const float sz = mi32(pf.hz - q.z, lf[2], h2, pd[2]);
