@@ -231,8 +231,9 @@ int  msmgb_list_stats(msmgb_ctx *ctx, int *maxk, double *meank);
  * stream).  v: 3*N probe, XP layout, caller order.  No counterpart in the reference. */
 int  msmgb_time_hvp(msmgb_ctx *ctx, const double *v, int reps, float *ms_hvp, float *ms_force);
 /* Hessian-vector product of the table-mode force (exact derivative of the interpolants):
- * hv = -dF/dx . v.  v and hv are 3*N arrays in XP layout, caller's order.  No counterpart in
- * the reference: it replaces finite-difference force pairs (MD_Method_ART_GPU.F90:454-576). */
+ * hv = -dF/dx . v.  v and hv are 3*N arrays in XP layout, caller's order, in host or device
+ * memory.  No counterpart in the reference: it replaces finite-difference force pairs
+ * (MD_Method_ART_GPU.F90:454-576). */
 int  msmgb_hvp(msmgb_ctx *ctx, const double *v, double *hv);
 
 /* Force-matching adjoint for the Cleri-Rosato parameters theta = (A, xi, p, q, r0) of the

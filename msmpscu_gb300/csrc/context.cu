@@ -1317,12 +1317,12 @@ extern "C" int msmgb_hvp(msmgb_ctx *c, const double *v, double *hv)
     double *dd = (double *)(s + 32 * N);      // 16 B: F'(rho) and its directional derivative
     double *hvs = (double *)(s + 48 * N);     // 24 B, sorted SoA result
     double *io = (double *)(s + 72 * N);      // 24 B, caller-order staging (input, then output)
-    CK(cudaMemcpyAsync(io, v, sizeof(double) * 3 * (size_t)n, cudaMemcpyHostToDevice, c->stream), "hvp copy-in");
+    CK(cudaMemcpyAsync(io, v, sizeof(double) * 3 * (size_t)n, cudaMemcpyDefault, c->stream), "hvp copy-in");
     RET(launch_hvp(c, io, hvs, v4, dd));
     k_unpack3<<<nblk(n, kBlock), kBlock, 0, c->stream>>>(hvs, hvs + n, hvs + 2 * (size_t)n, c->a.gid, n, 0, io);
     c->launches += 1;
     RET(check_launch(c, "hvp copy-out"));
-    CK(cudaMemcpyAsync(hv, io, sizeof(double) * 3 * (size_t)n, cudaMemcpyDeviceToHost, c->stream), "hvp copy-out");
+    CK(cudaMemcpyAsync(hv, io, sizeof(double) * 3 * (size_t)n, cudaMemcpyDefault, c->stream), "hvp copy-out");
     return poll_flags(c);
 }
 
@@ -1481,7 +1481,7 @@ extern "C" int msmgb_time_hvp(msmgb_ctx *c, const double *v, int reps, float *ms
     char *s = (char *)c->scratch;
     double *v4 = (double *)s, *dd = (double *)(s + 32 * N), *hvs = (double *)(s + 48 * N);
     double *io = (double *)(s + 72 * N);
-    CK(cudaMemcpyAsync(io, v, sizeof(double) * 3 * (size_t)n, cudaMemcpyHostToDevice, c->stream), "hvp copy-in");
+    CK(cudaMemcpyAsync(io, v, sizeof(double) * 3 * (size_t)n, cudaMemcpyDefault, c->stream), "hvp copy-in");
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0), "event");
     CK(cudaEventCreate(&e1), "event");

@@ -30,6 +30,21 @@ def _i(a):
     return a.ctypes.data_as(C.POINTER(C.c_int)) if a is not None else None
 
 
+def _tptr(t):
+    """double* of a contiguous float64 torch tensor (host or device memory)."""
+    if str(t.dtype) != "torch.float64" or not t.is_contiguous():
+        raise ValueError("expected a contiguous float64 tensor")
+    return C.cast(C.c_void_p(t.data_ptr()), C.POINTER(C.c_double))
+
+
+def _torch_ready(t):
+    """Orders the library's work after pending torch work on a CUDA tensor: the library runs
+    on its own stream and synchronises it before returning."""
+    if getattr(t, "is_cuda", False):
+        import torch
+        torch.cuda.current_stream(t.device).synchronize()
+
+
 def _cr_element_prm(element):
     """A, xi, p, q, r0 of the reference's Cleri-Rosato library (TB_CR_AlAl/AuAu/TiTi.F90) as it
     holds them: Al's lattice constant 4.050 and all Ti constants are single-precision literals,
@@ -456,9 +471,11 @@ class Engine:
             self._ck(self.lib.msmgb_copyout_force(self.ctx, _d(fp), order))
 
     def update_positions(self, x):
-        """New positions (N,3) of the loaded atoms: a numpy array, or a CUDA tensor in the
-        XP layout (3N contiguous, x block then y then z) whose device memory is read directly."""
+        """New positions (N,3) of the loaded atoms: a numpy array, or a float64 torch tensor in
+        the XP layout (shape (3, N) contiguous: x block, then y, then z) whose memory, host or
+        device, is read directly."""
         if hasattr(x, "data_ptr"):
+            _torch_ready(x)
             self._ck(self.lib.msmgb_update_positions(self.ctx, C.c_void_p(x.data_ptr())))
         else:
             xp = np.ascontiguousarray(np.asarray(x, np.float64).T).reshape(-1)
@@ -475,6 +492,20 @@ class Engine:
 
     def get_force(self, order=L.ORDER_ORIGINAL):
         return self._xp(self.lib.msmgb_copyout_force, order)
+
+    def force_into(self, out):
+        """Forces of the last force call into a float64 torch tensor of shape (3, N) (XP
+        layout, caller order), on the host or the device, with no staging through numpy."""
+        _torch_ready(out)
+        self._ck(self.lib.msmgb_copyout_force(self.ctx, _tptr(out), L.ORDER_ORIGINAL))
+        return out
+
+    def hvp_into(self, v, out):
+        """Hessian-vector product on float64 torch tensors of shape (3, N) (XP layout), host or
+        device memory."""
+        _torch_ready(v)
+        self._ck(self.lib.msmgb_hvp(self.ctx, _tptr(v), _tptr(out)))
+        return out
 
     def get_epot(self, order=L.ORDER_ORIGINAL):
         out = np.zeros(self.n)

@@ -51,6 +51,49 @@ def lanczos_lowest(matvec, n_atoms, iters=50, seed=0, project=True, v0=None):
     return float(ev[0]), mode.reshape(-1, 3), ev, Q
 
 
+def lanczos_lowest_t(matvec, like, iters=50, seed=0, project=True, v0=None):
+    """The same Lanczos iteration on torch tensors of shape (3, N) (the library's XP layout)
+    on like's device, so that a GPU-resident caller keeps every Krylov vector in device
+    memory; only the small tridiagonal problem goes to the host.  matvec(v) -> H v, same
+    shape.  Returns (lowest Ritz value, unit mode (3, N), all Ritz values)."""
+    import torch
+    if v0 is None:
+        g = torch.Generator().manual_seed(int(seed))
+        q = torch.randn(like.shape, generator=g, dtype=torch.float64).to(like.device)
+    else:
+        q = v0.detach().clone().to(like.device, torch.float64)
+    if project:
+        q = q - q.mean(dim=1, keepdim=True)
+    q = q / torch.linalg.norm(q)
+    Q, alpha, beta = [], [], []
+    q_prev = torch.zeros_like(q)
+    b_prev = 0.0
+    for _ in range(iters):
+        w = matvec(q)
+        if project:
+            w = w - w.mean(dim=1, keepdim=True)
+        a = float(torch.sum(q * w))
+        w = w - a * q - b_prev * q_prev
+        for qi in Q:                       # full reorthogonalisation
+            w = w - torch.sum(qi * w) * qi
+        w = w - torch.sum(q * w) * q
+        Q.append(q)
+        alpha.append(a)
+        b = float(torch.linalg.norm(w))
+        if b < 1e-12:
+            break
+        beta.append(b)
+        q_prev, q, b_prev = q, w / b, b
+    m = len(alpha)
+    T = np.diag(alpha) + np.diag(beta[:m - 1], 1) + np.diag(beta[:m - 1], -1)
+    ev, evec = np.linalg.eigh(T)
+    mode = torch.zeros_like(Q[0])
+    for k, qk in enumerate(Q):
+        mode = mode + float(evec[k, 0]) * qk
+    mode = mode / torch.linalg.norm(mode)
+    return float(ev[0]), mode, ev
+
+
 def fd_hvp(force, x, v, delta=1e-4):
     """Central finite difference of the force along the unit vector v (the reference-style
     curvature probe): H v ~ -(F(x + delta v) - F(x - delta v)) / (2 delta)."""

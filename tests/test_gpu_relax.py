@@ -61,3 +61,37 @@ def test_quench_and_vacancy_migration_saddle(oracle):
     # the unstable mode is dominated by the jumping atom, along the jump
     assert abs(float(mode[ib] @ (jump / np.linalg.norm(jump)))) > 0.5
     e.close()
+
+
+def test_quench_and_saddle_resident_on_device(oracle):
+    """The same vacancy quench and saddle search with every vector on the GPU (positions,
+    forces and HVPs passed to the library by device pointer): same saddle, same barrier."""
+    import torch
+    pos, L, site_a, site_b, ib = _vacancy_box()
+    n = len(pos)
+    e = Engine(n, lt.CU_RC_NL, mxkvois=96, precision="fp64")
+    e.init_forcetable(ForceTable.cleri_rosato(**lt.CU_CR, rc=lt.CU_RC))
+    e.set_masses([lt.CU_MASS])
+    rng = np.random.default_rng(1)
+    start = pos + rng.normal(scale=0.02, size=pos.shape)
+    e.copyin([(n, (0, 0, 0), tuple(L), (1, 1, 1))], start)
+    x0 = torch.tensor(start.T.copy(), device="cuda")
+    x_min, f_min, it = lbfgs_quench(e, x0, fmax=1e-4)
+    assert x_min.is_cuda and f_min.is_cuda and float(f_min.abs().max()) < 1e-4
+    xm = x_min.T.cpu().numpy()
+    e_min = energy(e, xm)
+    jump = site_a - site_b
+    jump -= np.round(jump / L) * L
+    xs0 = xm.copy()
+    xs0[ib] = site_b + 0.45 * jump
+    xs, fs, lam, mode, its = saddle_search(e, xs0, fmax=1e-3, device="cuda")
+    assert np.abs(fs).max() < 1e-3 and lam < 0.0
+    dmid = xs[ib] - (site_b + 0.5 * jump)
+    dmid -= np.round(dmid / L) * L
+    assert np.sqrt((dmid * dmid).sum()) < 0.02
+    barrier = energy(e, xs) - e_min
+    assert 0.2 < barrier < 2.0
+    # the host-driven search of the same start reaches the same barrier
+    xh, fh, lamh, _, _ = saddle_search(e, xs0, fmax=1e-3)
+    assert abs((energy(e, xh) - e_min) - barrier) < 1e-3
+    e.close()
