@@ -168,7 +168,11 @@ int  msmgb_update_positions(msmgb_ctx *ctx, const double *xp);
  * destination arrays of the copy-out calls may be host or device memory. */
 int  msmgb_copyout_simbox(msmgb_ctx *ctx, double *xp, double *xp1, int *statu, double *dis,
                           int order);
-int  msmgb_copyout_force(msmgb_ctx *ctx, double *fp, int order);       /* FP(N,3)          */
+int  msmgb_copyout_force(msmgb_ctx *ctx, double *fp, int order);       /* CALEKIN_DEV (MD_DiffScheme_GPU.F90:851-902, copied out in caller order as dbgEKIN): per-atom
+ * kinetic energy 0.5 m v^2, -1e32 for an inactive atom or one with a fixed position
+ * component; ekin (N) in host or device memory, order MSMGB_ORDER_ORIGINAL or _SORTED. */
+int  msmgb_calekin(msmgb_ctx *ctx, double *ekin, int order);
+/* FP(N,3)          */
 int  msmgb_copyout_epot(msmgb_ctx *ctx, double *epot, int order);     /* EPOT(N)          */
 int  msmgb_copyout_den(msmgb_ctx *ctx, double *den, int order);       /* F'(rho_i)        */
 /* sorted position -> original index map (hm_GID), N ints */

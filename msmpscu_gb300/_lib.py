@@ -84,6 +84,7 @@ SIGNATURES = [
     ("msmgb_copyout_simbox", C.c_int, [C.c_void_p, _dp, _dp, _ip, _dp, C.c_int]),
     ("msmgb_copyout_force", C.c_int, [C.c_void_p, _dp, C.c_int]),
     ("msmgb_copyout_epot", C.c_int, [C.c_void_p, _dp, C.c_int]),
+    ("msmgb_calekin", C.c_int, [C.c_void_p, _dp, C.c_int]),
     ("msmgb_copyout_den", C.c_int, [C.c_void_p, _dp, C.c_int]),
     ("msmgb_copyout_gid", C.c_int, [C.c_void_p, _ip]),
     ("msmgb_cal_neighborelist", C.c_int, [C.c_void_p]),

@@ -167,6 +167,21 @@ __global__ void __launch_bounds__(kBlock) k_update_pos(DevAtoms a, const double 
     block_max_flush(d2, a.maxdisp);
 }
 
+// per-atom kinetic energy in the sorted order (CALEKIN_KERNEL, MD_DiffScheme_GPU.F90:851-902):
+// 0.5 m v^2 for an active atom with no fixed position component, else -1e32
+__global__ void k_ekin(DevAtoms a, double *out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    const int st = a.statu[i];
+    double ek = -1.0e32;
+    if ((st & MSMGB_STATU_ACTIVE) && !(st & (MSMGB_STATU_FIXPOSX | MSMGB_STATU_FIXPOSY | MSMGB_STATU_FIXPOSZ))) {
+        const double m = a.cm[a.ityp[i] - 1];
+        ek = 0.5 * m * (a.vx[i] * a.vx[i] + a.vy[i] * a.vy[i] + a.vz[i] * a.vz[i]);
+    }
+    out[i] = ek;
+}
+
 __global__ void k_unpack_pos(const double4_32a *pos, const int *gid, int n, int sorted, double *dst)
 {
     int s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -789,6 +804,20 @@ extern "C" int msmgb_copyout_epot(msmgb_ctx *c, double *epot, int order)
     RET(need_state(c));
     RET(use_device(c));
     return copy_out_doubles(c, c->a.epot, nullptr, nullptr, epot, order);
+}
+
+extern "C" int msmgb_calekin(msmgb_ctx *c, double *ekin, int order)
+{
+    NvtxRange nvtx_range("msmgb_calekin");
+    if (!c || !ekin) return MSMGB_ERR_ARG;
+    RET(need_state(c));
+    if (!c->have_masses) return set_err(c, MSMGB_ERR_ARG, "no masses: call msmgb_set_masses");
+    RET(use_device(c));
+    double *tmp = (double *)c->scratch + 3 * (size_t)c->cap_atoms;   // past copy_out's staging
+    k_ekin<<<nblk(c->n, kBlock), kBlock, 0, c->stream>>>(c->a, tmp);
+    c->launches += 1;
+    RET(check_launch(c, "kinetic energy"));
+    return copy_out_doubles(c, tmp, nullptr, nullptr, ekin, order);
 }
 
 extern "C" int msmgb_copyout_den(msmgb_ctx *c, double *den, int order)

@@ -512,6 +512,12 @@ class Engine:
         self._ck(self.lib.msmgb_copyout_epot(self.ctx, _d(out), order))
         return out
 
+    def get_ekin(self, order=L.ORDER_ORIGINAL):
+        """Per-atom kinetic energy 0.5 m v^2 (-1e32 for inactive or position-fixed atoms)."""
+        out = np.zeros(self.n)
+        self._ck(self.lib.msmgb_calekin(self.ctx, _d(out), order))
+        return out
+
     def get_den(self, order=L.ORDER_ORIGINAL):
         out = np.zeros(self.n)
         self._ck(self.lib.msmgb_copyout_den(self.ctx, _d(out), order))

@@ -325,3 +325,34 @@ def test_atoms_on_box_faces(oracle):
     e.calforce()
     assert rel_err(e.get_force(), ref["f"]) < 1e-10
     e.close()
+
+
+def test_kinetic_energy_per_atom():
+    """msmgb_calekin (CALEKIN_DEV): 0.5 m v^2 per atom in caller order, -1e32 for inactive
+    atoms and atoms with a fixed position component; after MD steps it follows the state."""
+    pos, vel, L_ = lt.cu_config(6, 0.05, 600.0, 21)
+    n = len(pos)
+    ityp = np.ones(n, np.int32)
+    ityp[::7] = 2
+    statu = np.ones(n, np.int32)
+    statu[5] = 0                                             # inactive
+    statu[9] |= 4                                            # FIXPOSY
+    masses = np.array([lt.CU_MASS, 2.0 * lt.CU_MASS])
+    e = Engine(n, lt.CU_RC_NL, mxkvois=64)
+    t = ForceTable.cleri_rosato(**lt.CU_CR, rc=lt.CU_RC)
+    kp = np.array([[1, 1], [1, 1]], np.int32)
+    e.init_forcetable_raw(L.FS_TYPE, t.ntab, 1, t.rmax, t.ru, t.potr, t.fpotr, t.potb, t.fpotb, 2, kp)
+    e.set_masses(masses)
+    e.copyin([(n, (0, 0, 0), tuple(L_), (1, 1, 1))], pos, vel, ityp=ityp, statu=statu)
+
+    def expect(v):
+        ek = 0.5 * masses[ityp - 1] * (v * v).sum(axis=1)
+        ek[5] = ek[9] = -1.0e32
+        return ek
+
+    ek = e.get_ekin()
+    np.testing.assert_allclose(ek, expect(vel), rtol=1e-15)
+    e.run_steps(5, 1.0)
+    _, v, _, _ = e.get_state()
+    np.testing.assert_allclose(e.get_ekin(), expect(v), rtol=1e-15)
+    e.close()
