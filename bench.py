@@ -31,6 +31,7 @@ METRIC = "atom-steps/s FP64 vs mixed @1e-6 force err; batched boxes/s; HVP cost/
 UNIT = "atom-steps/s"
 NCELL, SIGMA, TEMP, SEED, DT = 80, 0.05, 600.0, 2024, 1.0
 MXKVOIS = 64
+OUTER_SKIN = 1.0      # two-level list: candidates within rc_nl + 1 A (lists are the same sets)
 
 
 def peaks():
@@ -263,7 +264,8 @@ def adjoint_cu_snapshots(device=0):
 
 def make_engine(n, precision, device=0):
     from msmpscu_gb300 import Engine, ForceTable, lattice as lt
-    e = Engine(n, lt.CU_RC_NL, mxkvois=MXKVOIS, skin_trigger=0.15, precision=precision, device=device)
+    e = Engine(n, lt.CU_RC_NL, mxkvois=MXKVOIS, skin_trigger=0.15, precision=precision, device=device,
+               outer_skin=OUTER_SKIN)
     e.init_forcetable(ForceTable.cleri_rosato(**lt.CU_CR, rc=lt.CU_RC))
     e.set_masses([lt.CU_MASS])
     return e
@@ -447,13 +449,17 @@ def run_ours(args):
     if dist:
         dist.barrier()
     l0 = e.launches
+    rc0 = e.rebuild_counts()
     with Clocks(device) as clk:
         ms, rebuilds = e.time_steps(args.steps, DT)
     launches = e.launches - l0
+    full_rebuilds = e.rebuild_counts()[1] - rc0[1]
     ms = reduce_max(ms, dist)
     value = replica_value(n, args.steps, ms, ws)
     kmax, kmean = e.list_stats()
     passes = e.time_passes(5)
+    rbt = e.time_rebuilds(3)
+    passes["nlist_full"], passes["nlist_reselect"] = rbt["full"], rbt["inner"]
     tune = e.tuning() if prec == "mixed" else None
     bm = bytes_model(kmean)
     hbm, peak_kind = peaks()
@@ -519,7 +525,8 @@ def run_ours(args):
                 "data": "synthetic (seeded fcc Cu lattice, Gaussian displacements, Maxwell-Boltzmann velocities)",
                 "config": {**workload_config(args.ncell, n), "precision": prec, "parallelism": "replicas" if ws > 1 else "single GPU",
                            "l2": "inputs larger than L2 (~0.9 GB touched per step)",
-                           "rebuilds_in_timed_steps": rebuilds, "mean_neighbours": kmean,
+                           "rebuilds_in_timed_steps": rebuilds, "full_rebuilds_in_timed_steps": full_rebuilds,
+                           "outer_skin": OUTER_SKIN, "mean_neighbours": kmean,
                            "max_neighbours": kmax},
                 "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm,
                              "unit": "GB/s", "frac": achieved / hbm, "traffic": traffic,

@@ -221,6 +221,20 @@ int  msmgb_get_tuning(const msmgb_ctx *ctx, int *out, float *ms);
  * choice to the tuner).  Pinned choices are kept for the context's atom count and skip the
  * tuning runs; the step graphs are recaptured.  No counterpart in the reference. */
 int  msmgb_set_tuning(msmgb_ctx *ctx, const int *codes);
+/* Two-level neighbour list: a full rebuild (cell binning, sort, 27-cell scan) also keeps, per
+ * atom, the candidates within rc_nl + skin; later rebuilds re-select the list from them with
+ * the same exact rule (the lists are the same sets) until the displacement since the full
+ * rebuild may exceed skin/2.  Cells are then sized by rc_nl + skin.  skin = 0 turns it off
+ * (every rebuild is full, cells sized by rc_nl as MD_NeighborsList_GPU.F90:289-292); the
+ * default is 1.0 A.  A new value applies from the next msmgb_copyin_simbox.  No counterpart
+ * in the reference (it rebuilds at a fixed interval, MD_Method_GenericMD_GPU.F90:599). */
+int  msmgb_set_outer_skin(msmgb_ctx *ctx, double skin);
+/* Device time (ms) of a full list rebuild and of a re-selection from the candidates (0 without
+ * a two-level list), averaged over reps launches.  No counterpart in the reference. */
+int  msmgb_time_rebuilds(msmgb_ctx *ctx, int reps, float *full_ms, float *inner_ms);
+/* List rebuilds done inside MD steps since the context was created, and how many of them
+ * were full rebuilds (all of them without a two-level list). */
+int  msmgb_rebuild_counts(const msmgb_ctx *ctx, int64_t *rebuilds, int64_t *full);
 /* Failure-path self-test of the bounded device waits (the TMA-streamed step kernel's
  * mbarrier waits give up after 0.5 s): runs one block that waits on a barrier nothing
  * completes and returns MSMGB_ERR_TIMEOUT; the context stays usable.  No counterpart in the
@@ -228,6 +242,11 @@ int  msmgb_set_tuning(msmgb_ctx *ctx, const int *codes);
 int  msmgb_selftest_wait(msmgb_ctx *ctx);
 /* Largest and mean neighbour count of the current list. */
 int  msmgb_list_stats(msmgb_ctx *ctx, int *maxk, double *meank);
+/* Cell tiles of the mixed passes for the current list (built after each list build while a
+ * selected variant reads them): blocks of 256 sorted atoms, blocks with a tile (a halo of at
+ * most 8192 atoms in at most 256 runs), mean and largest halo size over those.  All zero
+ * when no tiles are built.  No counterpart in the reference. */
+int  msmgb_tile_stats(msmgb_ctx *ctx, int *blocks, int *tiled, double *mean_halo, int *max_halo);
 
 /* ---- differentiation --------------------------------------------------------------------- */
 /* Device time of one Hessian-vector product and of one FP64 force call (density + force

@@ -153,8 +153,12 @@ __global__ void __launch_bounds__(kBlock) k_update_pos(DevAtoms a, const double 
     if (ok) {
         const DevBox &b = a.box[a.boxid[s]];
 #pragma unroll
-        for (int k = 0; k < 3; ++k)
+        bool out = false;
+        for (int k = 0; k < 3; ++k) {
             if (b.ifpd[k]) x[k] -= floor((x[k] - b.lo[k]) / b.len[k]) * b.len[k];
+            else out |= x[k] < b.lo[k] || x[k] > b.lo[k] + b.len[k];
+        }
+        if (out) atomicOr(&a.flags[kFlagOob], 1);   // the next list build re-bins every atom
         a.pos[s] = make_double4_32a(x[0], x[1], x[2], 0.0);
         const PosFF f = make_posff(x[0], x[1], x[2], b);
         a.posff[s] = f;
@@ -301,7 +305,8 @@ extern "C" int msmgb_destroy(msmgb_ctx *c)
                     a.dx, a.dy, a.dz, a.ityp, a.statu, a.gid, a.boxid, a.den, a.epot,
                     a.den32, a.kvois, a.indi, a.pk, a.rec, a.posfx, a.recfx, c->cell_of, c->perm, c->dbox, c->cm, c->icm,
                     c->flags, c->maxdisp, c->virial, c->scratch, c->cell_start,
-                    c->cell_cursor, c->scan_tmp, c->cell_rank, c->tab_mem, c->adj_mem, c->hvp_pair, c->pos2, c->posff2};
+                    c->cell_cursor, c->scan_tmp, c->cell_rank, c->cell_unrank, c->tab_mem, c->adj_mem, c->hvp_pair,
+                    c->pos2, c->posff2, a.lidx, a.hmeta, a.hruns, c->cand, c->kcand};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     if (c->h_flags) cudaFreeHost(c->h_flags);
@@ -363,6 +368,12 @@ static int poll_flags(msmgb_ctx *c)
         if (e & kErrOverflow) {
             char buf[160];
             snprintf(buf, sizeof(buf), "neighbour list overflow: an atom has more than MXKVOIS=%d neighbours", c->p.mxkvois);
+            return set_err(c, MSMGB_ERR_NL_OVERFLOW, buf);
+        }
+        if (e & kErrCandOverflow) {
+            char buf[200];
+            snprintf(buf, sizeof(buf), "candidate list overflow: an atom has more than %d candidates within "
+                     "rc_nl + outer skin (raise MXKVOIS or lower the outer skin)", c->mxo);
             return set_err(c, MSMGB_ERR_NL_OVERFLOW, buf);
         }
         if (e & kErrOutOfBox) return set_err(c, MSMGB_ERR_OUT_OF_BOX, "an active atom lies outside its box");
@@ -565,6 +576,7 @@ extern "C" int msmgb_copyin_simbox(msmgb_ctx *c, int nbox, const msmgb_box *boxe
     RET(use_device(c));
     const int n = (int)total;
     std::vector<DevBox> hb((size_t)nbox);
+    const double bin_rc = c->p.rc_nl + (c->outer_skin > 0.0 ? c->outer_skin : 0.0);
     std::vector<int> boxid((size_t)n);
     int cells = 0, atom0 = 0;
     for (int b = 0; b < nbox; ++b) {
@@ -584,7 +596,9 @@ extern "C" int msmgb_copyin_simbox(msmgb_ctx *c, int nbox, const msmgb_box *boxe
             if (d.len[k] <= 0.0) return set_err(c, MSMGB_ERR_ARG, "box length must be positive");
             if (d.ifpd[k] && d.len[k] <= 2.0 * c->p.rc_nl)
                 return set_err(c, MSMGB_ERR_BOX_TOO_SMALL, "periodic box edge must exceed twice the list cutoff");
-            int nc = (int)(d.len[k] / (1.0 * c->p.rc_nl) - 0.0001);   // MD_NeighborsList_GPU.F90:289-292
+            // MD_NeighborsList_GPU.F90:289-292 with the cell size rc_nl, or rc_nl + the outer
+            // skin for a two-level list (the candidates must lie in the 27-cell stencil)
+            int nc = (int)(d.len[k] / bin_rc - 0.0001);
             d.nc[k] = nc < 3 ? 3 : nc;
         }
         {   // |lo_i - lo_j| <= ulp(2L) (u in [L, 2L]) and |L - float(L)| <= ulp(L)/2
@@ -613,12 +627,14 @@ extern "C" int msmgb_copyin_simbox(msmgb_ctx *c, int nbox, const msmgb_box *boxe
         if (c->cell_cursor) cudaFree(c->cell_cursor);
         if (c->scan_tmp) cudaFree(c->scan_tmp);
         if (c->cell_rank) cudaFree(c->cell_rank);
-        c->cell_start = c->cell_cursor = c->scan_tmp = c->cell_rank = nullptr;
+        if (c->cell_unrank) cudaFree(c->cell_unrank);
+        c->cell_start = c->cell_cursor = c->scan_tmp = c->cell_rank = c->cell_unrank = nullptr;
         int cap = cells + 2;
         CK(dalloc(&c->cell_start, (size_t)cap + 1), "cell alloc");
         CK(dalloc(&c->cell_cursor, (size_t)cap + 1), "cell alloc");
         CK(dalloc(&c->scan_tmp, (size_t)(cap / 4096 + 2) + 4096), "cell alloc");
         CK(dalloc(&c->cell_rank, (size_t)cap + 1), "cell alloc");
+        CK(dalloc(&c->cell_unrank, (size_t)cap + 1), "cell alloc");
         c->cap_cells = cap;
         c->rank_layout.clear();
     }
@@ -654,11 +670,16 @@ extern "C" int msmgb_copyin_simbox(msmgb_ctx *c, int nbox, const msmgb_box *boxe
             for (int q = 0; q < nb; ++q) rank[(size_t)(d.cell0 + key[(size_t)q].second)] = d.cell0 + q;
         }
         rank[(size_t)cells] = cells;
+        std::vector<int> unrank((size_t)cells + 1);
+        for (int g = 0; g <= cells; ++g) unrank[(size_t)rank[(size_t)g]] = g;
         CK(cudaMemcpy(c->cell_rank, rank.data(), sizeof(int) * ((size_t)cells + 1), cudaMemcpyHostToDevice),
+           "cell order upload");
+        CK(cudaMemcpy(c->cell_unrank, unrank.data(), sizeof(int) * ((size_t)cells + 1), cudaMemcpyHostToDevice),
            "cell order upload");
         c->rank_layout = layout;
     }
     c->ncell_total = cells;
+    c->bin_rc = bin_rc;
     c->nbox = nbox;
     c->n = n;
     c->a.n = n;
@@ -1017,11 +1038,20 @@ extern "C" int msmgb_correction(msmgb_ctx *c, double h)
 // A step graph is captured into a graph that owns an IF node: k_decide sets its condition on
 // the device, and the node's body holds the list rebuild, so a step without a rebuild runs
 // none of the rebuild kernels.
-static int begin_step_capture(msmgb_ctx *c, cudaGraph_t *g, cudaGraphConditionalHandle *cond)
+// With a two-level list there are two IF nodes in sequence: the full rebuild (binning, sort,
+// candidates) and the list selection from the candidates, which runs on every rebuild.
+struct RebuildNodes {
+    cudaGraphConditionalHandle cond = 0, cond_inner = 0;
+    cudaGraph_t body = nullptr, body_inner = nullptr;
+};
+
+static int begin_step_capture(msmgb_ctx *c, cudaGraph_t *g, RebuildNodes *rn)
 {
     *g = nullptr;
     CK(cudaGraphCreate(g, 0), "graph create");
-    cudaError_t e = cudaGraphConditionalHandleCreate(cond, *g, 0, cudaGraphCondAssignDefault);
+    cudaError_t e = cudaGraphConditionalHandleCreate(&rn->cond, *g, 0, cudaGraphCondAssignDefault);
+    if (e == cudaSuccess && two_level(c))
+        e = cudaGraphConditionalHandleCreate(&rn->cond_inner, *g, 0, cudaGraphCondAssignDefault);
     if (e == cudaSuccess)
         e = cudaStreamBeginCaptureToGraph(c->stream, *g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) {
@@ -1055,32 +1085,48 @@ static int add_rebuild_node(msmgb_ctx *c, cudaGraphConditionalHandle cond, cudaG
     return MSMGB_OK;
 }
 
-// the rebuild of the current atom view c->a into a conditional body (kernels counted apart)
-static int fill_rebuild_body(msmgb_ctx *c, cudaGraph_t body)
+// the IF nodes of a rebuild at the current position of the capture
+static int add_rebuild_nodes(msmgb_ctx *c, RebuildNodes *rn)
+{
+    RET(add_rebuild_node(c, rn->cond, &rn->body));
+    if (rn->cond_inner) RET(add_rebuild_node(c, rn->cond_inner, &rn->body_inner));
+    return MSMGB_OK;
+}
+
+// the rebuild stage `stage` (0: the whole list build, 1: the full part of a two-level build,
+// 2: its list selection) of the current atom view c->a into a conditional body; its kernel
+// count is returned in *nk
+static int fill_rebuild_body(msmgb_ctx *c, cudaGraph_t body, int stage, int64_t *nk)
 {
     CK(cudaStreamBeginCaptureToGraph(c->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal),
        "graph capture");
     const int64_t l0 = c->launches;
-    const int rc = build_list(c);
+    const int rc = stage == 0 ? build_list(c) : (stage == 1 ? build_full(c) : build_inner(c));
     cudaGraph_t out = nullptr;
     const cudaError_t e = cudaStreamEndCapture(c->stream, &out);
-    c->gk_body = c->launches - l0;
+    *nk = c->launches - l0;
     c->launches = l0;
     if (rc) return rc;
     if (e != cudaSuccess) return cuda_err(c, e, "graph capture");
     return MSMGB_OK;
 }
 
-static int finish_step_graph(msmgb_ctx *c, int rc, cudaGraph_t g, cudaGraph_t body, cudaGraphExec_t *out,
+static int finish_step_graph(msmgb_ctx *c, int rc, cudaGraph_t g, const RebuildNodes &rn, cudaGraphExec_t *out,
                              const DevAtoms &body_view)
 {
     cudaGraph_t ended = nullptr;
     const cudaError_t e = cudaStreamEndCapture(c->stream, &ended);
     if (!rc && e != cudaSuccess) rc = cuda_err(c, e, "graph capture");
-    if (!rc && body) {
+    if (!rc && rn.body) {
         const DevAtoms keep = c->a;
         c->a = body_view;
-        rc = fill_rebuild_body(c, body);
+        c->gk_inner = 0;
+        if (rn.body_inner) {
+            rc = fill_rebuild_body(c, rn.body, 1, &c->gk_body);
+            if (!rc) rc = fill_rebuild_body(c, rn.body_inner, 2, &c->gk_inner);
+        } else {
+            rc = fill_rebuild_body(c, rn.body, 0, &c->gk_body);
+        }
         c->a = keep;
     }
     if (!rc) {
@@ -1097,16 +1143,16 @@ static int finish_step_graph(msmgb_ctx *c, int rc, cudaGraph_t g, cudaGraph_t bo
 static int capture_step(msmgb_ctx *c, double h)
 {
     free_graph(c);
-    cudaGraph_t g = nullptr, body = nullptr;
-    cudaGraphConditionalHandle cond = 0;
-    RET(begin_step_capture(c, &g, &cond));
+    cudaGraph_t g = nullptr;
+    RebuildNodes rn;
+    RET(begin_step_capture(c, &g, &rn));
     int64_t l0 = c->launches;
     int rc = launch_vv(c, h, 1);
-    if (!rc) rc = launch_decide(c, c->p.skin_trigger, c->p.nb_uptab, cond, true);
-    if (!rc) rc = add_rebuild_node(c, cond, &body);
+    if (!rc) rc = launch_decide(c, c->p.skin_trigger, c->p.nb_uptab, rn.cond, true, rn.cond_inner);
+    if (!rc) rc = add_rebuild_nodes(c, &rn);
     if (!rc) rc = force_passes(c, false, false);
     const int64_t nk = c->launches - l0;
-    RET(finish_step_graph(c, rc, g, body, &c->step_graph, c->a));
+    RET(finish_step_graph(c, rc, g, rn, &c->step_graph, c->a));
     c->graph_kernels = nk;
     c->launches = l0;
     c->graph_h = h;
@@ -1185,30 +1231,30 @@ static int capture_fused(msmgb_ctx *c, double h)
     const int64_t l_start = c->launches;
     int64_t l0 = c->launches;
     {
-        cudaGraph_t g = nullptr, body = nullptr;
-        cudaGraphConditionalHandle cond = 0;
-        RET(begin_step_capture(c, &g, &cond));
+        cudaGraph_t g = nullptr;
+        RebuildNodes rn;
+        RET(begin_step_capture(c, &g, &rn));
         c->a = atoms_on(c, base, 0);
         rc = launch_vv(c, h, 0);
-        if (!rc) rc = launch_decide(c, c->p.skin_trigger, c->p.nb_uptab, cond, true);
-        if (!rc) rc = add_rebuild_node(c, cond, &body);
+        if (!rc) rc = launch_decide(c, c->p.skin_trigger, c->p.nb_uptab, rn.cond, true, rn.cond_inner);
+        if (!rc) rc = add_rebuild_nodes(c, &rn);
         c->gk_pre = c->launches - l0;
-        rc = finish_step_graph(c, rc, g, body, &c->g_pre, atoms_on(c, base, 0));
+        rc = finish_step_graph(c, rc, g, rn, &c->g_pre, atoms_on(c, base, 0));
         c->a = base;
         RET(rc);
     }
     for (int p = 0; p < 2; ++p) {
         l0 = c->launches;
-        cudaGraph_t g = nullptr, body = nullptr;
-        cudaGraphConditionalHandle cond = 0;
-        RET(begin_step_capture(c, &g, &cond));
+        cudaGraph_t g = nullptr;
+        RebuildNodes rn;
+        RET(begin_step_capture(c, &g, &rn));
         c->a = atoms_on(c, base, p);
         rc = step_density(c);
         if (!rc) rc = step_force_vv(c, h);
-        if (!rc) rc = launch_decide(c, c->p.skin_trigger, c->p.nb_uptab, cond, true);
-        if (!rc) rc = add_rebuild_node(c, cond, &body);
+        if (!rc) rc = launch_decide(c, c->p.skin_trigger, c->p.nb_uptab, rn.cond, true, rn.cond_inner);
+        if (!rc) rc = add_rebuild_nodes(c, &rn);
         c->gk_loop = c->launches - l0;
-        rc = finish_step_graph(c, rc, g, body, &c->g_loop[p], atoms_on(c, base, 1 - p));
+        rc = finish_step_graph(c, rc, g, rn, &c->g_loop[p], atoms_on(c, base, 1 - p));
         c->a = base;
         RET(rc);
         l0 = c->launches;
@@ -1240,6 +1286,27 @@ static int ensure_graphs(msmgb_ctx *c, double h)
     if (!c->step_graph || c->graph_h != h || c->graph_prec != c->p.precision || c->graph_n != c->n ||
         c->graph_tune != c->tune_dens_unroll * 64 + c->tune_force_unroll)
         return capture_step(c, h);
+    return MSMGB_OK;
+}
+
+// kernels run by the conditional rebuild bodies since the rebuild counters were cleared
+// (h_flags freshly read): every rebuild runs the first body, or with a two-level list the
+// selection body, and the full rebuilds also the first one
+static void count_rebuild_kernels(msmgb_ctx *c)
+{
+    const int64_t nreb = c->h_flags[kFlagRebuilds];
+    const int64_t nfull = c->gk_inner > 0 ? (int64_t)c->h_flags[kFlagFull] : nreb;
+    if (c->gk_inner > 0) c->launches += nreb * c->gk_inner + nfull * c->gk_body;
+    else c->launches += nreb * c->gk_body;
+    c->step_rebuilds += nreb;
+    c->step_full += nfull;
+}
+
+extern "C" int msmgb_rebuild_counts(const msmgb_ctx *c, int64_t *rebuilds, int64_t *full)
+{
+    if (!c) return MSMGB_ERR_ARG;
+    if (rebuilds) *rebuilds = c->step_rebuilds;
+    if (full) *full = c->step_full;
     return MSMGB_OK;
 }
 
@@ -1284,13 +1351,15 @@ extern "C" int msmgb_run_steps(msmgb_ctx *c, int nsteps, double h, int *rebuilds
         c->force_valid = true;
     }
     CK(cudaMemsetAsync(c->flags + kFlagRebuilds, 0, sizeof(int) * 3, c->stream), "flag clear");  // rebuilds, pending, step
+    CK(cudaMemsetAsync(c->flags + kFlagFull, 0, sizeof(int), c->stream), "flag clear");
     RET(ensure_graphs(c, h));
     RET(issue_steps(c, nsteps, h));
     RET(launch_correct(c, h, true));          // no-op unless the last step left a pending half-kick
     int rc = poll_flags(c);
     if (rebuilds) *rebuilds = c->h_flags[kFlagRebuilds];
-    c->launches += (int64_t)c->h_flags[kFlagRebuilds] * c->gk_body;   // conditional rebuild bodies run
+    count_rebuild_kernels(c);
     CK(cudaMemsetAsync(c->flags + kFlagRebuilds, 0, sizeof(int), c->stream), "flag clear");
+    CK(cudaMemsetAsync(c->flags + kFlagFull, 0, sizeof(int), c->stream), "flag clear");
     return rc;
 }
 
@@ -1318,8 +1387,9 @@ extern "C" int msmgb_finish_steps(msmgb_ctx *c, double h, int *rebuilds)
     RET(launch_correct(c, h, true));
     int rc = poll_flags(c);
     if (rebuilds) *rebuilds = c->h_flags[kFlagRebuilds];
-    c->launches += (int64_t)c->h_flags[kFlagRebuilds] * c->gk_body;   // conditional rebuild bodies run
+    count_rebuild_kernels(c);
     CK(cudaMemsetAsync(c->flags + kFlagRebuilds, 0, sizeof(int), c->stream), "flag clear");
+    CK(cudaMemsetAsync(c->flags + kFlagFull, 0, sizeof(int), c->stream), "flag clear");
     return rc;
 }
 
@@ -1497,6 +1567,28 @@ extern "C" int msmgb_list_stats(msmgb_ctx *c, int *maxk, double *meank)
     return MSMGB_OK;
 }
 
+extern "C" int msmgb_tile_stats(msmgb_ctx *c, int *blocks, int *tiled, double *mean_halo, int *max_halo)
+{
+    if (!c) return MSMGB_ERR_ARG;
+    RET(need_state(c));
+    RET(use_device(c));
+    const int nb = (c->n + kBlock - 1) / kBlock;
+    int t = 0, mx = 0;
+    double s = 0.0;
+    if (c->halo_on && c->list_valid && c->a.hmeta) {
+        std::vector<int2> m((size_t)nb);
+        CK(cudaStreamSynchronize(c->stream), "synchronize");
+        CK(cudaMemcpy(m.data(), c->a.hmeta, sizeof(int2) * (size_t)nb, cudaMemcpyDeviceToHost), "copy-out");
+        for (const int2 &q : m)
+            if (q.x >= 0) { ++t; s += q.y; mx = std::max(mx, q.y); }
+    }
+    if (blocks) *blocks = nb;
+    if (tiled) *tiled = t;
+    if (mean_halo) *mean_halo = t ? s / t : 0.0;
+    if (max_halo) *max_halo = mx;
+    return MSMGB_OK;
+}
+
 // Device time of one Hessian-vector product (gather of v + the two HVP passes) and of one
 // FP64 force call (density + force pass) on the current state, averaged over `reps`
 // launches after a warm-up; v (caller order, XP layout) is uploaded once before timing.
@@ -1546,17 +1638,20 @@ extern "C" int msmgb_selftest_wait(msmgb_ctx *c)
 extern "C" int msmgb_set_tuning(msmgb_ctx *c, const int *codes)
 {
     if (!c || !codes) return MSMGB_ERR_ARG;
-    static const int valid_d[] = {1, 2, 3, 4, 5, 9, 10, 18, 19, 20, 21};
+    static const int valid_d[] = {1, 2, 3, 4, 5, 9, 10, 18, 19, 20, 21, 66, 68, 82, 84};
     static const int valid_f[] = {1, 2, 3, 4, 5, 9, 10, 18, 19, 20, 21, 50, 51, 52, 53};
     auto in = [](int v, const int *set, int n) {
         for (int k = 0; k < n; ++k)
             if (set[k] == v) return true;
         return false;
     };
-    if ((codes[0] >= 0 && !in(codes[0], valid_d, 11)) || (codes[1] >= 0 && !in(codes[1], valid_f, 15)) ||
-        codes[2] >= (c->tab.ngroup > 1 ? 4 : 20))
+    if ((codes[0] >= 0 && !in(codes[0], valid_d, 15)) || (codes[1] >= 0 && !in(codes[1], valid_f, 15)) ||
+        codes[2] >= (c->tab.ngroup > 1 ? 4 : 24))
         return set_err(c, MSMGB_ERR_ARG, "unknown kernel variant code");
-    if (codes[2] >= 18 && c->tab.ngroup == 1) {
+    if (((codes[0] >= 0 && (codes[0] & 64)) || codes[2] >= 20) &&
+        (c->tab.ngroup > 1 || c->p.precision != MSMGB_PREC_MIXED))
+        return set_err(c, MSMGB_ERR_ARG, "cell-tile variants need one table kind and MIXED precision");
+    if ((codes[2] == 18 || codes[2] == 19) && c->tab.ngroup == 1) {
         RET(use_device(c));
         if (ensure_list_maps(c) != 1) return set_err(c, MSMGB_ERR_ARG, "TMA list descriptors unavailable");
     }
@@ -1570,7 +1665,58 @@ extern "C" int msmgb_set_tuning(msmgb_ctx *c, const int *codes)
         c->tuned_fused_n = c->n;
     }
     free_graph(c);
+    if (uses_tiles(c)) {
+        RET(use_device(c));
+        RET(enable_halo(c));
+    } else {
+        c->halo_on = false;
+    }
     return MSMGB_OK;
+}
+
+extern "C" int msmgb_set_outer_skin(msmgb_ctx *c, double skin)
+{
+    if (!c) return MSMGB_ERR_ARG;
+    if (!(skin >= 0.0 && skin <= c->p.rc_nl))
+        return set_err(c, MSMGB_ERR_ARG, "the outer skin must lie in [0, rc_nl]");
+    if (skin != c->outer_skin) {
+        c->outer_skin = skin;
+        free_graph(c);
+        c->list_valid = false;        // the next list build is a full one (candidates included)
+    }
+    return MSMGB_OK;
+}
+
+// Device time of a full list rebuild and of a list selection from the candidates (two-level
+// list; 0 without one), averaged over `reps` launches after a warm-up.
+extern "C" int msmgb_time_rebuilds(msmgb_ctx *c, int reps, float *full_ms, float *inner_ms)
+{
+    if (!c || !full_ms || !inner_ms || reps < 1) return MSMGB_ERR_ARG;
+    RET(ready_for_force(c));
+    cudaEvent_t ev[2];
+    CK(cudaEventCreate(&ev[0]), "event");
+    CK(cudaEventCreate(&ev[1]), "event");
+    float out[2] = {0.0f, 0.0f};
+    for (int which = 0; which < 2; ++which) {
+        if (which == 1 && !two_level(c)) break;
+        double total = 0.0;
+        for (int r = 0; r < reps + 1; ++r) {
+            CK(cudaEventRecord(ev[0], c->stream), "event");
+            RET(which == 0 ? build_list(c) : build_inner(c));
+            CK(cudaEventRecord(ev[1], c->stream), "event");
+            CK(cudaEventSynchronize(ev[1]), "event");
+            float ms = 0.f;
+            CK(cudaEventElapsedTime(&ms, ev[0], ev[1]), "event");
+            if (r > 0) total += ms;
+        }
+        out[which] = (float)(total / reps);
+    }
+    cudaEventDestroy(ev[0]);
+    cudaEventDestroy(ev[1]);
+    c->force_valid = false;            // a full rebuild re-sorts the atoms
+    *full_ms = out[0];
+    *inner_ms = out[1];
+    return poll_flags(c);
 }
 
 extern "C" int msmgb_get_tuning(const msmgb_ctx *c, int *out, float *ms)

@@ -604,6 +604,239 @@ __global__ void __launch_bounds__(kBlock, MINB) k_force32_vv(DevAtoms a, DevTabl
     block_max_flush(dmax, a.maxdisp);
 }
 
+// ---- cell-tile variants (single kind) ----------------------------------------------------
+// The block's halo (built by k_halo after each list build: the atoms of every cell in the
+// 27-cell stencils of the block's cells, as runs of consecutive sorted atoms) is staged in
+// shared memory, one warp per run with coalesced loads, as two float4 arrays holding the
+// two halves of each 32 B record (consecutive records fall on consecutive 16 B bank
+// groups).  Every neighbour is then read from shared memory through its 16-bit halo
+// position instead of being gathered through L1 per lane.  A block without a tile, or whose
+// halo exceeds the launch's capacity `cap`, gathers from global memory as the other
+// variants do.  The arithmetic per pair and its order are those of the other variants, so
+// the results are bitwise the same.
+// 16 B global -> shared copy that completes asynchronously (cp.async, cached in L2 only)
+__device__ __forceinline__ void cp_async16(void *dst, const void *src)
+{
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((unsigned)__cvta_generic_to_shared(dst)),
+                 "l"(src)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool stage_halo(const DevAtoms &a, const PosFF *src, float4 *s_hi, float4 *s_lo, int cap)
+{
+    const int2 m = a.hmeta[blockIdx.x];
+    const bool tiled = m.x >= 0 && m.y <= cap;
+    if (tiled) {
+        // every copy of the block is in flight before any is waited for
+        const int2 *runs = a.hruns + (size_t)blockIdx.x * (kHaloRuns + 1);
+        const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+        for (int r = w; r < m.x; r += kBlock / 32) {
+            const int2 q = runs[r];
+            const int len = runs[r + 1].y - q.y;
+            for (int k = lane; k < len; k += 32) {
+                const float4 *p = reinterpret_cast<const float4 *>(src + q.x + k);
+                cp_async16(s_hi + q.y + k, p);
+                cp_async16(s_lo + q.y + k, p + 1);
+            }
+        }
+        asm volatile("cp.async.wait_all;" ::: "memory");
+    }
+    __syncthreads();
+    return tiled;
+}
+
+__device__ __forceinline__ PosFF smem_ff(const float4 *s_hi, const float4 *s_lo, int l)
+{
+    const float4 h = s_hi[l], o = s_lo[l];
+    PosFF p;
+    p.hx = h.x; p.hy = h.y; p.hz = h.z; p.d = h.w;
+    p.lx = o.x; p.ly = o.y; p.lz = o.z; p.lw = o.w;
+    return p;
+}
+
+// F'(rho) from rho (FS: -1/2 rho^-1/2; EAM: DFEMBD interpolated), single kind
+template <int POT>
+__device__ __forceinline__ float embed_slope32(const DevAtoms &a, const DevTables &t, float rho)
+{
+    float d = rho;
+    if (POT == MSMGB_FS_TYPE) {
+        if (rho > 0.0f) d = -0.5f * rsqrtf(rho);
+    } else if (rho > 0.0f) {
+        const float sk = rho / t.rhodf + 1.0f;
+        int kk = (int)(sk + 0.000001f);
+        if (kk + 1 > t.nembd) {
+            atomicOr(&a.flags[kFlagErr], kErrRho);
+            kk = t.nembd;
+        }
+        const float2 e = __ldg(t.embd2 + kk);
+        d = fmaf(sk - (float)kk, e.y, e.x);
+    }
+    return d;
+}
+
+// density sum over the list of atom i; idx: list entries (global atom or halo position),
+// load(v): the position record of entry v (v < 0: any valid record, not accumulated)
+template <int UNR, class Idx, class Load>
+__device__ __forceinline__ float density_loop(const DevTables &t, const Idx *__restrict__ nb, unsigned *__restrict__ pk,
+                                              size_t ld, int kn, const PosFF &pi, const BoxF &b, float rej, Load load)
+{
+    float rho = 0.0f;
+    int jn[UNR];
+#pragma unroll
+    for (int u = 0; u < UNR; ++u) jn[u] = u < kn ? (int)__ldg(nb + u * ld) : -1;
+    for (int w = 0; w < kn; w += UNR) {
+        int j[UNR];
+#pragma unroll
+        for (int u = 0; u < UNR; ++u) j[u] = jn[u];
+#pragma unroll
+        for (int u = 0; u < UNR; ++u) {
+            const int sl = w + UNR + u;
+            jn[u] = sl < kn ? (int)__ldg(nb + sl * ld) : -1;
+        }
+        PosFF p[UNR];
+#pragma unroll
+        for (int u = 0; u < UNR; ++u) p[u] = load(j[u]);
+#pragma unroll
+        for (int u = 0; u < UNR; ++u) {
+            float dk = 0.0f;
+            int kk = 0;
+            const unsigned c = pair_index(pi, p[u], b, t, rej, dk, kk);
+            if (j[u] >= 0) pk[(w + u) * ld] = c;
+            const bool ok = j[u] >= 0 && c != kSkip;
+            const float2 e = __ldg(t.dens2 + (ok ? kk : 0));
+            rho += ok ? fmaf(dk, e.y, e.x) : 0.0f;
+        }
+    }
+    return rho;
+}
+
+template <int POT, int UNR, int MINB>
+__global__ void __launch_bounds__(kBlock, MINB) k_density32t(DevAtoms a, DevTables t, int cap)
+{
+    extern __shared__ float4 s_halo[];
+    float4 *s_hi = s_halo, *s_lo = s_halo + cap;
+    const bool tiled = stage_halo(a, a.posff, s_hi, s_lo, cap);
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    const int kn = a.kvois[i];
+    unsigned *__restrict__ pk = a.pk + i;
+    const size_t ld = (size_t)a.ld;
+    if ((a.statu[i] & MSMGB_STATU_ACTIVE) != MSMGB_STATU_ACTIVE) {   // the force pass skips it
+        a.den32[i] = 0.0f;
+        st_ff(a.rec + i, ld_ff(a.posff + i));          // d = 0
+        return;
+    }
+    const BoxF b = load_boxf(a.box[a.boxid[i]]);
+    const float rej = t.ru2h + 4.0f * sqrtf(t.ru2h) * b.dlmax + 1e-5f * t.ru2h;
+    const PosFF pi = ld_ff(a.posff + i);
+    float rho;
+    if (tiled) {
+        rho = density_loop<UNR>(t, a.lidx + i, pk, ld, kn, pi, b, rej,
+                                [&](int v) { return smem_ff(s_hi, s_lo, v >= 0 ? v : 0); });
+    } else {
+        const PosFF *pf = a.posff;
+        rho = density_loop<UNR>(t, a.indi + i, pk, ld, kn, pi, b, rej,
+                                [&](int v) { return ld_ff(pf + (v >= 0 ? v : i)); });
+    }
+    const float d = embed_slope32<POT>(a, t, rho);
+    a.den32[i] = d;
+    PosFF r = pi;
+    r.d = d;
+    st_ff(a.rec + i, r);
+}
+
+// force loop of the fused tile kernel: force_loop_batched with the neighbour records read
+// from the staged halo
+template <int UNR>
+__device__ __forceinline__ void force_loop_tile(const DevAtoms &a, const DevTables &t, int i, const PosFF &pi,
+                                                float di, const BoxF &b, const float4 *s_hi, const float4 *s_lo,
+                                                float &fx, float &fy, float &fz)
+{
+    const unsigned short *__restrict__ nb = a.lidx + i;
+    const unsigned *__restrict__ pk = a.pk + i;
+    const size_t ld = (size_t)a.ld;
+    const int kn = a.kvois[i];
+    unsigned cn[UNR];
+    int jn[UNR];
+#pragma unroll
+    for (int u = 0; u < UNR; ++u) {
+        cn[u] = u < kn ? __ldg(pk + u * ld) : kSkip;
+        jn[u] = u < kn ? (int)__ldg(nb + u * ld) : 0;
+    }
+    for (int w = 0; w < kn; w += UNR) {
+        unsigned c[UNR];
+        int j[UNR];
+#pragma unroll
+        for (int u = 0; u < UNR; ++u) {
+            c[u] = cn[u];
+            j[u] = jn[u];
+        }
+#pragma unroll
+        for (int u = 0; u < UNR; ++u) {
+            const int sl = w + UNR + u;
+            cn[u] = sl < kn ? __ldg(pk + sl * ld) : kSkip;
+            jn[u] = sl < kn ? (int)__ldg(nb + sl * ld) : 0;
+        }
+        PosFF pj[UNR];
+        float4 e[UNR];
+#pragma unroll
+        for (int u = 0; u < UNR; ++u) {
+            const unsigned row = c[u] == kSkip ? 0u : (c[u] >> kDkBits);
+            pj[u] = smem_ff(s_hi, s_lo, j[u]);
+            e[u] = __ldg(t.force4 + row);
+        }
+#pragma unroll
+        for (int u = 0; u < UNR; ++u)
+            if (c[u] != kSkip) force_pair_e(pi, pj[u], c[u], di, pj[u].d, e[u], b, fx, fy, fz);
+    }
+}
+
+// the fused step kernel (k_force32_vv, single kind) on cell tiles
+template <int UNR, int MINB>
+__global__ void __launch_bounds__(kBlock, MINB) k_force32_vv_t(DevAtoms a, DevTables t, double th, int cap)
+{
+    extern __shared__ float4 s_halo[];
+    float4 *s_hi = s_halo, *s_lo = s_halo + cap;
+    const bool tiled = stage_halo(a, a.rec, s_hi, s_lo, cap);
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double dmax = 0.0;
+    if (i < a.n) {
+        const int stat = a.statu[i];
+        float fx = 0.0f, fy = 0.0f, fz = 0.0f;
+        const DevBox &bb = a.box[a.boxid[i]];
+        if ((stat & MSMGB_STATU_ACTIVE) == MSMGB_STATU_ACTIVE) {
+            const BoxF b = load_boxf(bb);
+            const PosFF pi = ld_ff(a.rec + i);
+            if (tiled) force_loop_tile<UNR>(a, t, i, pi, pi.d, b, s_hi, s_lo, fx, fy, fz);
+            else force_loop_batched<UNR>(a, t, i, pi, pi.d, b, fx, fy, fz);
+        }
+        const double Fx = (double)fx, Fy = (double)fy, Fz = (double)fz;
+        a.fx[i] = Fx;
+        a.fy[i] = Fy;
+        a.fz[i] = Fz;
+        const double4_32a p = a.pos[i];
+        if ((stat & MSMGB_STATU_ACTIVE) == MSMGB_STATU_ACTIVE) {
+            dmax = vv_atom(a, i, stat, bb, th, true, Fx, Fy, Fz, p, a.pos_nxt, a.posff_nxt);
+        } else {
+            a.pos_nxt[i] = p;
+            a.posff_nxt[i] = a.posff[i];
+        }
+    }
+    block_max_flush(dmax, a.maxdisp);
+}
+
+// launch shape of the tile variants: halo capacity (atoms) and its shared memory
+constexpr int kTileCapSmall = 2048;    // 64 KB: 3 blocks per SM
+constexpr int kTileCapLarge = 2560;    // 80 KB: 2 blocks per SM
+
+template <class K>
+static int tile_smem(K kernel, int cap)
+{
+    const int bytes = cap * 2 * (int)sizeof(float4);
+    cudaFuncSetAttribute((const void *)kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    return bytes;
+}
+
 // ---- TMA-streamed variant of the step kernel ----------------------------------------------
 // The block's 256 atoms read their list slots from shared memory: one thread issues a 2D
 // tensor copy (cp.async.bulk.tensor) of the (256 atoms x kTmaSlots slots) tile of INDI and of
@@ -819,12 +1052,26 @@ int ensure_list_maps(msmgb_ctx *c)
 
 static inline int nblk(long n, int b) { return (int)((n + b - 1) / b); }
 
+bool uses_tiles(const msmgb_ctx *c)
+{
+    return c->tab.ngroup == 1 && c->p.precision == MSMGB_PREC_MIXED &&
+           ((c->tune_dens_unroll & 64) != 0 || (c->tune_fused >= 20 && c->tune_fused < 24));
+}
+
 // variant codes of the fused kernel: (neighbours in flight, minimum resident blocks), codes
 // 6-11 the same six with the next slots of the list loaded one iteration ahead, 12-17 with
 // in addition every gather of a batch issued before its arithmetic (force_loop_batched),
-// 18-19 the TMA-streamed list (2 and 4 neighbours per batch; skipped without descriptors);
+// 18-19 the TMA-streamed list (2 and 4 neighbours per batch; skipped without descriptors),
+// 20-23 cell tiles (2/4 neighbours per batch x halo capacity 2048 / 2560 atoms);
 // with several table kinds codes 0-3: 2/4 in flight x {plain, list prefetch}
-constexpr int kFusedVariants = 20;
+constexpr int kFusedVariants = 24;
+
+template <int UNR, int MINB>
+static void fused_tile(msmgb_ctx *c, double h, int cap)
+{
+    const int smem = tile_smem(k_force32_vv_t<UNR, MINB>, cap);
+    k_force32_vv_t<UNR, MINB><<<nblk(c->n, kBlock), kBlock, smem, c->stream>>>(c->a, c->tab, h, cap);
+}
 
 constexpr int kFusedVariantsMulti = 4;
 
@@ -860,6 +1107,10 @@ static void fused_variant(msmgb_ctx *c, int code, double h)
     case 17: k_force32_vv<4, 5, 2><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
     case 18: k_force32_vv_tma<2><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h, c->tm_indi, c->tm_pk); break;
     case 19: k_force32_vv_tma<4><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h, c->tm_indi, c->tm_pk); break;
+    case 20: fused_tile<2, 3>(c, h, kTileCapSmall); break;
+    case 21: fused_tile<4, 3>(c, h, kTileCapSmall); break;
+    case 22: fused_tile<2, 2>(c, h, kTileCapLarge); break;
+    case 23: fused_tile<4, 2>(c, h, kTileCapLarge); break;
     default: k_force32_vv<2, 1, 0><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
     }
 }
@@ -887,8 +1138,10 @@ int autotune_fused(msmgb_ctx *c)
     int bestc = 0;
     const bool multi = c->tab.ngroup > 1;
     const bool tma = !multi && ensure_list_maps(c) == 1;
+    const bool tiles = !multi && enable_halo(c) == MSMGB_OK;
     for (int code = 0; code < (multi ? kFusedVariantsMulti : kFusedVariants); ++code) {
-        if (code >= 18 && !tma) continue;
+        if ((code == 18 || code == 19) && !tma) continue;
+        if (code >= 20 && !tiles) continue;
         for (int r = 0; r < 4; ++r) {
             if (r == 1) cudaEventRecord(e0, c->stream);
             fused_variant(c, code, 0.0);
@@ -902,6 +1155,7 @@ int autotune_fused(msmgb_ctx *c)
     c->tune_fused = bestc;
     c->tune_ms_fused = best / 3.0f;
     c->tuned_fused_n = c->n;
+    c->halo_on = uses_tiles(c);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     cudaMemsetAsync(c->a.maxdisp, 0, sizeof(unsigned long long), c->stream);
@@ -927,10 +1181,28 @@ static int persistent_grid(const void *kernel, int smem)
     return std::max(1, per) * std::max(1, sms);
 }
 
+template <int POT, int UNR, int MINB>
+static void dens_tile(msmgb_ctx *c, int cap)
+{
+    const int smem = tile_smem(k_density32t<POT, UNR, MINB>, cap);
+    k_density32t<POT, UNR, MINB><<<nblk(c->n, kBlock), kBlock, smem, c->stream>>>(c->a, c->tab, cap);
+}
+
 template <int POT, bool MULTI>
 static void dens_variant(msmgb_ctx *c, int unr)
 {
     const int g = nblk(c->n, kBlock);
+    if (!MULTI && (unr & 64)) {   // cell tiles: +16 the larger halo capacity
+        const bool large = (unr & 16) != 0;
+        if ((unr & 7) == 4) {
+            if (large) dens_tile<POT, 4, 2>(c, kTileCapLarge);
+            else dens_tile<POT, 4, 3>(c, kTileCapSmall);
+        } else {
+            if (large) dens_tile<POT, 2, 2>(c, kTileCapLarge);
+            else dens_tile<POT, 2, 3>(c, kTileCapSmall);
+        }
+        return;
+    }
     if (!MULTI && (unr & 8)) {
         int kmin, cnt;
         smem_window(c, (int)sizeof(float2), &kmin, &cnt);
@@ -1039,10 +1311,12 @@ int autotune_mixed(msmgb_ctx *c)
     // +32 (force, single kind): and all gathers of a batch before its arithmetic;
     // +8: persistent grid with the table in shared memory (single kind only)
     const bool single = c->tab.ngroup == 1;
-    const int dcands[11] = {1, 2, 4, 3, 5, 18, 20, 19, 21, 9, 10};
+    // +64 (density, single kind): cell tiles (+16: larger halo capacity)
+    const int dcands[15] = {1, 2, 4, 3, 5, 18, 20, 19, 21, 9, 10, 66, 68, 82, 84};
     const int fcands[15] = {1, 2, 4, 3, 5, 18, 20, 19, 21, 50, 52, 51, 53, 9, 10};
     const int *cands = dcands;
-    int ncand = single ? 11 : 9;
+    const bool tiles = single && enable_halo(c) == MSMGB_OK;
+    int ncand = single ? (tiles ? 15 : 11) : 9;
     cudaEvent_t e0, e1;
     cudaError_t err = cudaEventCreate(&e0);
     if (err == cudaSuccess) err = cudaEventCreate(&e1);
@@ -1084,6 +1358,7 @@ int autotune_mixed(msmgb_ctx *c)
     c->tune_ms[0] = best_d / 3.0f;
     c->tune_ms[1] = best_f / 3.0f;
     c->tuned_n = c->n;
+    c->halo_on = uses_tiles(c);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     return check_launch(c, "autotune");

@@ -40,6 +40,12 @@ struct NvtxRange {
 constexpr int kBlock = 256;
 constexpr int kMaxGroups = 16;          // mp_MXGROUP, MD_Const.F90:77
 
+// cell tiles (k_halo): a block of kBlock sorted atoms spanning at most kHaloCells cells,
+// whose halo has at most kHaloRuns runs and kHaloMax atoms, gets a tile; others none
+constexpr int kHaloCells = 64;
+constexpr int kHaloRuns = 256;
+constexpr int kHaloMax = 8192;
+
 // error bits in flags[kFlagErr]
 constexpr int kErrOverflow = 1;
 constexpr int kErrOutOfBox = 2;
@@ -47,6 +53,7 @@ constexpr int kErrRho = 4;
 constexpr int kErrTimeout = 8;
 constexpr int kErrNonFinite = 16;   // a position that is not a finite number
 constexpr int kErrBadList = 32;     // list validation (MSMGB_CHECK_LISTS=1) found a bad entry
+constexpr int kErrCandOverflow = 64;  // an atom has more candidates than the candidate list holds
 
 // device flag words
 enum {
@@ -56,7 +63,10 @@ enum {
     kFlagPending = 3,    // 1: a corrector half-kick is pending (fused integrator)
     kFlagStep = 4,       // step counter for the fixed-interval rebuild
     kFlagMaxK = 5,       // largest neighbour count seen by the last build
-    kFlagWords = 8
+    kFlagFull = 6,       // number of full rebuilds (two-level list) done by run_steps
+    kFlagAcc = 7,        // float bits: bound on the displacement since the last full rebuild
+    kFlagOob = 8,        // an atom left its box since the last full rebuild (next one is full)
+    kFlagWords = 16
 };
 
 // float-float position (hi, lo parts of u = x + ushift).  In the record buffer `rec` the
@@ -145,6 +155,12 @@ struct DevAtoms {
     PosFF *rec;          // mixed passes: {position, F'(rho)} records written by the density pass
     PosFX *posfx;        // float-float passes: positions (k_fix) ...
     PosFX *recfx;        // ... and {position, F'(rho)} records written by the density pass
+    // cell tiles of the mixed passes (k_halo, after each list build): for the 256 atoms of
+    // block b, the atoms of every cell in the 27-cell stencils of their cells ("halo") as runs
+    // of consecutive sorted atoms; lidx = each list slot's position in the block's halo
+    unsigned short *lidx;   // ELL layout like indi
+    int2 *hmeta;            // [block] {number of runs, halo atoms}; {-1, 0}: no tile
+    int2 *hruns;            // [block][kHaloRuns + 1] {first atom, offset in the halo}
     int *flags;
     unsigned long long *maxdisp;
     double *virial;      // [nbox][6]
@@ -247,6 +263,7 @@ __device__ __forceinline__ double vv_atom(const DevAtoms &a, int i, int stat, co
     // PASSBOUND is not stored (reference quirk, :372-378)
     if (hi) a.statu[i] = MSMGB_STATU_OUTOFBOX | MSMGB_STATU_REFLECT;
     else if (lo) a.statu[i] = MSMGB_STATU_OUTOFBOX | MSMGB_STATU_TRANSMIT;
+    if (hi | lo) atomicOr(&a.flags[kFlagOob], 1);
     // displacement since the last build from the exact FP32 hi parts (the trigger needs
     // ~1e-4 A, the hi parts are within 3e-5 A of the FP64 positions)
     const float4 q = a.pos_bld[i];
@@ -293,6 +310,14 @@ struct msmgb_ctx {
     msmgb::DevBox *dbox = nullptr;
     int *cell_of = nullptr, *cell_start = nullptr, *cell_cursor = nullptr, *perm = nullptr;
     int *cell_rank = nullptr;   // storage position of each cell (cells of a box in Morton order)
+    int *cell_unrank = nullptr; // global cell id at each storage position
+    bool halo_on = false;         // every list build also builds the cell tiles (k_halo)
+    // two-level list: candidates within rc_nl + outer_skin, kept between full rebuilds
+    double outer_skin = 1.0;      // 0: every rebuild bins, sorts and scans the cell stencil
+    double bin_rc = 0.0;          // cell-size radius of the current layout
+    int mxo = 0;                  // candidate slots per atom
+    int *cand = nullptr;          // candidates, ELL layout [mxo][ld]
+    int *kcand = nullptr;         // candidates per atom
     bool cell_row_order = false;  // MSMGB_CELL_ORDER=row: x-fastest cell storage instead
     bool check_lists = false;     // MSMGB_CHECK_LISTS=1: validate every list after its build
     std::vector<int> rank_layout; // cell grids (and order) the uploaded cell_rank was made for
@@ -336,6 +361,8 @@ struct msmgb_ctx {
     cudaGraphExec_t g_pre = nullptr, g_loop[2] = {nullptr, nullptr}, g_final[2] = {nullptr, nullptr};
     int64_t gk_pre = 0, gk_loop = 0, gk_final = 0;
     int64_t gk_body = 0;         // kernels of the conditional rebuild body of a step graph
+    int64_t gk_inner = 0;        // two-level list: kernels of the body that runs on every rebuild
+    int64_t step_rebuilds = 0, step_full = 0;   // list rebuilds inside MD steps, and the full ones
     double fg_h = 0.0;
     int fg_n = -1, fg_tune = -1, fg_prec = -1;
 
@@ -356,7 +383,12 @@ int set_err(msmgb_ctx *c, int code, const std::string &msg);
 int cuda_err(msmgb_ctx *c, cudaError_t e, const char *what);
 
 // neighbour list (nlist.cu)
-int build_list(msmgb_ctx *c);
+int build_list(msmgb_ctx *c);          // full build (both stages of a two-level list)
+bool two_level(const msmgb_ctx *c);     // the list keeps candidates between full rebuilds
+int build_full(msmgb_ctx *c);           // binning, sort, permutation, candidates (or the list)
+int build_inner(msmgb_ctx *c);          // the list from the candidates (two-level only)
+int build_halo(msmgb_ctx *c);
+int enable_halo(msmgb_ctx *c);      // allocates the tile buffers, builds them for the current list
 
 // force passes (force64.cu / force32.cu)
 int launch_density(msmgb_ctx *c, bool want_epot);
@@ -370,6 +402,7 @@ int launch_force_ff(msmgb_ctx *c);
 int launch_force_ff_vv(msmgb_ctx *c, double h);
 int autotune_fused(msmgb_ctx *c);
 int ensure_list_maps(msmgb_ctx *c);
+bool uses_tiles(const msmgb_ctx *c);  // a selected mixed variant reads the cell tiles
 int launch_wait_selftest(msmgb_ctx *c);
 int autotune_mixed(msmgb_ctx *c);
 int launch_hvp(msmgb_ctx *c, const double *dv, double *dhv, double *v4buf, double *ddbuf);
@@ -380,6 +413,6 @@ int launch_adjoint(msmgb_ctx *c, const double *ft, const double *dtab, double *w
 int launch_vv(msmgb_ctx *c, double h, int mode);   // mode 0: predictor; 1: fused; 2: fused if pending
 int launch_correct(msmgb_ctx *c, double h, bool only_if_pending);
 int launch_decide(msmgb_ctx *c, double skin_trigger, int nb_uptab, cudaGraphConditionalHandle cond = 0,
-                  bool use_cond = false);
+                  bool use_cond = false, cudaGraphConditionalHandle cond_inner = 0);
 
 }  // namespace msmgb

@@ -19,6 +19,8 @@
 //               cell; boxes with NCELL forced to 3 the minimum image of every candidate.
 // In an MD-step graph the rebuild is the body of a conditional node that the step's
 // decision kernel switches on (context.cu), so steps without a rebuild launch none of these.
+#include <climits>
+
 #include "msmgb_internal.cuh"
 
 namespace msmgb {
@@ -316,6 +318,142 @@ __global__ void __launch_bounds__(kBlock, 6) k_build(DevAtoms a, const int *cell
     atomicMax(&a.flags[kFlagMaxK], nn);
 }
 
+// ---- two-level list -----------------------------------------------------------------------
+// With an outer skin s_o > 0 a full rebuild (binning, sort, permutation) stores, per atom, the
+// candidates within rc_nl + s_o (k_build_cand, FP32 test with the prefilter margin: a superset
+// of the pairs whose exact distance is below rc_nl + s_o), and every list build, full or not,
+// selects from those candidates the pairs with d^2 < rc_nl^2 by the same FP32 prefilter and
+// FP64 band rule as k_build (k_inner).  Between full rebuilds no atom moves more than s_o / 2
+// (k_decide bounds the displacement since the full rebuild by the sum of the skin maxima of
+// the rebuild intervals), so a pair within rc_nl now was within rc_nl + s_o then and the
+// lists are the sets k_build would give.  The atoms keep their cell order between full
+// rebuilds.
+__global__ void __launch_bounds__(kBlock, 6) k_build_cand(DevAtoms a, const int *cell_of, const int *rank,
+                                                       const int *start, int *cand, int *kcand, int mxo, float d2o)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) {                          // displacement bound and box exits since this full rebuild
+        a.flags[kFlagAcc] = 0;
+        a.flags[kFlagOob] = 0;
+    }
+    if (i >= a.n) return;
+    if (a.statu[i] & MSMGB_STATU_OUTOFBOX) { kcand[i] = 0; return; }
+    const float4 pf = a.pos_bld[i];
+    const DevBox &b = a.box[a.boxid[i]];
+    int nc[3], pd[3];
+    float lf[3], hf[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        nc[k] = b.nc[k];
+        pd[k] = b.ifpd[k];
+        lf[k] = b.lenf[k];
+        hf[k] = b.halff[k];
+    }
+    const int cell0 = b.cell0;
+    const int c = cell_of[i] - cell0;
+    const int ix = c % nc[0], iy = (c / nc[0]) % nc[1], iz = c / (nc[0] * nc[1]);
+    int nn = 0;
+    const size_t ld = (size_t)a.ld;
+    int *const out = cand + i;
+    const float4 *const hi = a.pos_bld;
+    for (int s = 0; s < 27; ++s) {
+        int j3[3] = {ix + c_nix[s], iy + c_niy[s], iz + c_niz[s]};
+        bool skip = false;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            if (pd[k]) j3[k] = (j3[k] + nc[k]) % nc[k];
+            else if (j3[k] < 0 || j3[k] >= nc[k]) skip = true;
+        }
+        if (skip) continue;
+        const int g = rank[cell0 + j3[0] + nc[0] * (j3[1] + nc[1] * j3[2])];
+        const int j0 = start[g], e = start[g + 1];
+        for (int j = j0; j < e; ++j) {
+            const float4 q = hi[j];
+            const float sx = mi32(pf.x - q.x, lf[0], hf[0], pd[0]);
+            const float sy = mi32(pf.y - q.y, lf[1], hf[1], pd[1]);
+            const float sz = mi32(pf.z - q.z, lf[2], hf[2], pd[2]);
+            const float d2f = fmaf(sx, sx, fmaf(sy, sy, sz * sz));
+            if (j != i && d2f < d2o) {
+                if (nn < mxo) out[(size_t)nn * ld] = j;
+                ++nn;
+            }
+        }
+    }
+    if (nn > mxo) {
+        atomicOr(&a.flags[kFlagErr], kErrCandOverflow);
+        nn = mxo;
+    }
+    kcand[i] = nn;
+}
+
+// The list from the candidates at the current positions; also the skin reference pos_bld.
+// Candidates are taken kInnerUnr at a time, their indices one group ahead, so the position
+// gathers of a group overlap.  No candidate has left its box: an exit since the full rebuild
+// makes the next rebuild full (kFlagOob).
+constexpr int kInnerUnr = 4;
+
+__global__ void __launch_bounds__(kBlock) k_inner(DevAtoms a, const int *cand, const int *kcand, double rc2,
+                                                  float d2lo, float d2hi)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    const PosFF pf = a.posff[i];
+    a.pos_bld[i] = make_float4(pf.hx, pf.hy, pf.hz, 0.0f);
+    if (!(isfinite(pf.hx) && isfinite(pf.hy) && isfinite(pf.hz))) atomicOr(&a.flags[kFlagErr], kErrNonFinite);
+    // an atom outside its box neither has nor is a neighbour (the full rebuild puts it into
+    // the sentinel cell)
+    if (a.statu[i] & MSMGB_STATU_OUTOFBOX) { a.kvois[i] = 0; return; }
+    const int kc = kcand[i];
+    const DevBox &b = a.box[a.boxid[i]];
+    float lf[3], hf[3];
+    int pd[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        lf[k] = b.lenf[k];
+        hf[k] = b.halff[k];
+        pd[k] = b.ifpd[k];
+    }
+    const size_t ld = (size_t)a.ld;
+    const int mxk = a.mxk;
+    int *const indi = a.indi + i;
+    const int *const cd = cand + i;
+    const float4 *const hp = reinterpret_cast<const float4 *>(a.posff);   // hi halves: every 2nd float4
+    int nn = 0;
+    int jn[kInnerUnr];
+#pragma unroll
+    for (int u = 0; u < kInnerUnr; ++u) jn[u] = u < kc ? __ldg(cd + (size_t)u * ld) : i;
+    for (int s = 0; s < kc; s += kInnerUnr) {
+        int j[kInnerUnr];
+        float4 q[kInnerUnr];
+#pragma unroll
+        for (int u = 0; u < kInnerUnr; ++u) {
+            j[u] = jn[u];
+            const int sl = s + kInnerUnr + u;
+            jn[u] = sl < kc ? __ldg(cd + (size_t)sl * ld) : i;
+        }
+#pragma unroll
+        for (int u = 0; u < kInnerUnr; ++u) q[u] = __ldg(hp + 2 * (size_t)j[u]);
+#pragma unroll
+        for (int u = 0; u < kInnerUnr; ++u) {
+            if (s + u >= kc) break;
+            const float sx = mi32(pf.hx - q[u].x, lf[0], hf[0], pd[0]);
+            const float sy = mi32(pf.hy - q[u].y, lf[1], hf[1], pd[1]);
+            const float sz = mi32(pf.hz - q[u].z, lf[2], hf[2], pd[2]);
+            const float d2f = fmaf(sx, sx, fmaf(sy, sy, sz * sz));
+            if (accept(d2f, d2lo, d2hi, a, i, j[u], b, rc2)) {
+                if (nn < mxk) indi[(size_t)nn * ld] = j[u];
+                ++nn;
+            }
+        }
+    }
+    if (nn > mxk) {
+        atomicOr(&a.flags[kFlagErr], kErrOverflow);
+        nn = mxk;
+    }
+    a.kvois[i] = nn;
+    atomicMax(&a.flags[kFlagMaxK], nn);
+}
+
 // Debug validation of a freshly built list (no trap): every stored neighbour index lies in
 // [0, n), differs from the atom itself and belongs to the same box; KVOIS lies in [0, MXKVOIS].
 __global__ void k_check_list(DevAtoms a)
@@ -333,7 +471,164 @@ __global__ void k_check_list(DevAtoms a)
     if (bad) atomicOr(&a.flags[kFlagErr], kErrBadList);
 }
 
+// ---- cell tiles of the mixed passes -------------------------------------------------------
+// One block per kBlock sorted atoms (the blocks of the pass kernels).  Atoms are sorted by
+// cell storage position, so the block's atoms fill the cells of one range of storage
+// positions [r0, r1]; the halo is the union of the 27-cell stencils of those cells.  The
+// candidate cells are sorted and merged into runs of consecutive storage positions, which
+// are runs of consecutive atoms: the pass kernels stage a run with coalesced loads.  Each
+// list slot is then translated to its neighbour's position in the staged halo (a binary
+// search over the runs), so the passes gather neighbours from shared memory.
+constexpr int kHaloCand = 2048;   // >= 27 * kHaloCells, a power of two (bitonic sort)
+static_assert(kHaloCand >= 27 * kHaloCells, "candidate buffer");
+
+__global__ void __launch_bounds__(kBlock) k_halo(DevAtoms a, const int *cell_of, const int *rank, const int *unrank,
+                                                 const int *start, int sentinel)
+{
+    __shared__ int cand[kHaloCand];
+    __shared__ int r_first[kHaloRuns + 1], r_soff[kHaloRuns + 1], r_end[kHaloRuns];
+    __shared__ int s_cnt[kBlock];
+    __shared__ int s_bad, s_nrun;
+    const int t = threadIdx.x;
+    const int i0 = blockIdx.x * kBlock;
+    const int n = a.n;
+    const int i1 = min(i0 + kBlock, n) - 1;
+    const int r0 = rank[cell_of[i0]], r1 = rank[cell_of[i1]];
+    const int ncell = r1 - r0 + 1;
+    if (t == 0) s_bad = ncell > kHaloCells;
+    for (int k = t; k < kHaloCand; k += kBlock) cand[k] = INT_MAX;
+    __syncthreads();
+    if (!s_bad) {
+        for (int q = t; q < 27 * ncell; q += kBlock) {
+            const int r = r0 + q / 27, s = q % 27;
+            if (r == sentinel) continue;                 // out-of-box atoms have no neighbours
+            const int a0 = start[r];
+            if (start[r + 1] == a0) continue;            // no atom of the block in this cell
+            const DevBox &b = a.box[a.boxid[a0]];
+            const int l = unrank[r] - b.cell0;
+            int j3[3] = {l % b.nc[0] + c_nix[s], (l / b.nc[0]) % b.nc[1] + c_niy[s], l / (b.nc[0] * b.nc[1]) + c_niz[s]};
+            bool skip = false;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                if (b.ifpd[k]) j3[k] = (j3[k] + b.nc[k]) % b.nc[k];
+                else if (j3[k] < 0 || j3[k] >= b.nc[k]) skip = true;
+            }
+            if (!skip) cand[q] = rank[b.cell0 + j3[0] + b.nc[0] * (j3[1] + b.nc[1] * j3[2])];
+        }
+    }
+    __syncthreads();
+    if (s_bad) {
+        if (t == 0) a.hmeta[blockIdx.x] = make_int2(-1, 0);
+        return;
+    }
+    // bitonic sort of the candidate storage positions (ascending; INT_MAX pads)
+    for (int k = 2; k <= kHaloCand; k <<= 1) {
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int x = t; x < kHaloCand; x += kBlock) {
+                const int y = x ^ j;
+                if (y > x) {
+                    const int u = cand[x], v = cand[y];
+                    if ((u > v) == ((x & k) == 0)) { cand[x] = v; cand[y] = u; }
+                }
+            }
+            __syncthreads();
+        }
+    }
+    // runs: maximal sequences of storage positions with steps of 0 or 1
+    constexpr int kPer = kHaloCand / kBlock;
+    const int x0 = t * kPer;
+    int heads = 0;
+#pragma unroll
+    for (int m = 0; m < kPer; ++m) {
+        const int x = x0 + m, v = cand[x];
+        if (v != INT_MAX && (x == 0 || (cand[x - 1] != v && cand[x - 1] != v - 1))) ++heads;
+    }
+    s_cnt[t] = heads;
+    __syncthreads();
+    if (t == 0) {
+        int acc = 0;
+        for (int k = 0; k < kBlock; ++k) { const int h = s_cnt[k]; s_cnt[k] = acc; acc += h; }
+        s_nrun = acc;
+        if (acc > kHaloRuns) s_bad = 1;
+    }
+    __syncthreads();
+    const int nrun = s_nrun;
+    if (!s_bad) {
+        int id = s_cnt[t] - 1;
+#pragma unroll
+        for (int m = 0; m < kPer; ++m) {
+            const int x = x0 + m, v = cand[x];
+            if (v == INT_MAX) break;
+            if (x == 0 || (cand[x - 1] != v && cand[x - 1] != v - 1)) r_first[++id] = start[v];
+            const int w = x + 1 < kHaloCand ? cand[x + 1] : INT_MAX;
+            if (w != v && w != v + 1) r_end[id] = start[v + 1];
+        }
+    }
+    __syncthreads();
+    if (t == 0 && !s_bad) {
+        int acc = 0;
+        for (int r = 0; r < nrun; ++r) { r_soff[r] = acc; acc += r_end[r] - r_first[r]; }
+        r_soff[nrun] = acc;
+        if (acc > kHaloMax) s_bad = 1;
+    }
+    __syncthreads();
+    if (s_bad) {
+        if (t == 0) a.hmeta[blockIdx.x] = make_int2(-1, 0);
+        return;
+    }
+    // list slots -> halo positions
+    const int i = i0 + t;
+    if (i < n) {
+        const int kn = a.kvois[i];
+        const size_t ld = (size_t)a.ld;
+        bool miss = false;
+        for (int sl = 0; sl < kn; ++sl) {
+            const int j = a.indi[(size_t)sl * ld + i];
+            int lo = 0, hi = nrun - 1;          // last run whose first atom is <= j
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (r_first[mid] <= j) lo = mid;
+                else hi = mid - 1;
+            }
+            const int off = j - r_first[lo];
+            if (off < 0 || off >= r_soff[lo + 1] - r_soff[lo]) { miss = true; break; }
+            a.lidx[(size_t)sl * ld + i] = (unsigned short)(r_soff[lo] + off);
+        }
+        if (miss) s_bad = 1;                    // a neighbour outside the stencil cells: no tile
+    }
+    __syncthreads();
+    int2 *runs = a.hruns + (size_t)blockIdx.x * (kHaloRuns + 1);
+    for (int r = t; r <= nrun; r += kBlock) runs[r] = make_int2(r < nrun ? r_first[r] : 0, r_soff[r]);
+    if (t == 0) a.hmeta[blockIdx.x] = s_bad ? make_int2(-1, 0) : make_int2(nrun, r_soff[nrun]);
+}
+
 static inline int nblk(long n, int b) { return (int)((n + b - 1) / b); }
+
+int build_halo(msmgb_ctx *c)
+{
+    if (c->n <= 0) return MSMGB_OK;
+    k_halo<<<nblk(c->n, kBlock), kBlock, 0, c->stream>>>(c->a, c->cell_of, c->cell_rank, c->cell_unrank,
+                                                         c->cell_start, c->ncell_total);
+    c->launches += 1;
+    return check_launch(c, "cell tiles");
+}
+
+int enable_halo(msmgb_ctx *c)
+{
+    if (!c->a.lidx) {
+        cudaError_t e = cudaStreamSynchronize(c->stream);
+        const size_t nb = (size_t)c->a.ld / kBlock;
+        if (e == cudaSuccess) e = cudaMalloc((void **)&c->a.lidx, sizeof(unsigned short) * (size_t)c->a.ld * c->a.mxk);
+        if (e == cudaSuccess) e = cudaMalloc((void **)&c->a.hmeta, sizeof(int2) * nb);
+        if (e == cudaSuccess) e = cudaMalloc((void **)&c->a.hruns, sizeof(int2) * nb * (kHaloRuns + 1));
+        if (e != cudaSuccess) return cuda_err(c, e, "cudaMalloc cell tiles");
+    }
+    if (!c->halo_on) {
+        c->halo_on = true;
+        if (c->list_valid) return build_halo(c);
+    }
+    return MSMGB_OK;
+}
 
 // Margin of the FP32 prefilter: it uses the hi parts of the shifted coordinates
 // (u in [L, 2L]): hi_i - hi_j and the image shift by float(L) are exact (Sterbenz), so a
@@ -353,13 +648,40 @@ static void prefilter_band(const msmgb_ctx *c, double rc2, float *lo, float *hi)
     *hi = (float)(rc2 + m);
 }
 
-int build_list(msmgb_ctx *c)
+bool two_level(const msmgb_ctx *c)
+{
+    return c->outer_skin > 0.0 && c->bin_rc >= c->p.rc_nl + c->outer_skin;
+}
+
+static int ensure_candidates(msmgb_ctx *c)
+{
+    const double r = (c->p.rc_nl + c->outer_skin) / c->p.rc_nl;
+    const int mxo = (((int)ceil(c->p.mxkvois * r * r * r * 1.1) + 7) / 8) * 8;
+    if (c->cand && c->mxo == mxo) return MSMGB_OK;
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (c->cand) cudaFree(c->cand);
+    if (c->kcand) cudaFree(c->kcand);
+    c->cand = c->kcand = nullptr;
+    c->mxo = 0;
+    if (e == cudaSuccess) e = cudaMalloc((void **)&c->cand, sizeof(int) * (size_t)c->a.ld * (size_t)mxo);
+    if (e == cudaSuccess) e = cudaMalloc((void **)&c->kcand, sizeof(int) * (size_t)c->a.ld);
+    if (e != cudaSuccess) return cuda_err(c, e, "cudaMalloc candidate list");
+    c->mxo = mxo;
+    return MSMGB_OK;
+}
+
+int build_full(msmgb_ctx *c)
 {
     const int n = c->n;
     const int ncs = c->ncell_total + 1;   // + sentinel cell for out-of-box atoms
     int *count = c->cell_cursor;          // histogram, then re-zeroed as scatter cursor
     cudaStream_t s = c->stream;
     DevAtoms a = c->a;
+    const bool two = two_level(c);
+    if (two) {
+        const int rc = ensure_candidates(c);
+        if (rc) return rc;
+    }
 
     k_zero_int<<<nblk(ncs + 1, kBlock), kBlock, 0, s>>>(count, ncs + 1);
     k_bin<<<nblk(n, kBlock), kBlock, 0, s>>>(a, c->ncell_total, c->cell_of, c->cell_rank, count);
@@ -378,16 +700,49 @@ int build_list(msmgb_ctx *c)
     Stage st = stage_of(c->scratch, c->cap_atoms);
     k_permute<<<nblk(n, kBlock), kBlock, 0, s>>>(a, st, c->perm, c->cell_of);
     k_copyback<<<nblk(n, kBlock), kBlock, 0, s>>>(a, st, c->cell_of);
-    double rc2 = c->p.rc_nl * c->p.rc_nl;
-    float d2lo, d2hi;
-    prefilter_band(c, rc2, &d2lo, &d2hi);
-    k_build<<<nblk(n, kBlock), kBlock, 0, s>>>(a, c->cell_of, c->cell_rank, c->cell_start, rc2, d2lo, d2hi);
-    c->launches += 6;
+    c->launches += 5;
+    if (two) {
+        const double ro = c->p.rc_nl + c->outer_skin;
+        float d2lo, d2hi;
+        prefilter_band(c, ro * ro, &d2lo, &d2hi);
+        k_build_cand<<<nblk(n, kBlock), kBlock, 0, s>>>(a, c->cell_of, c->cell_rank, c->cell_start, c->cand,
+                                                        c->kcand, c->mxo, d2hi);
+    } else {
+        double rc2 = c->p.rc_nl * c->p.rc_nl;
+        float d2lo, d2hi;
+        prefilter_band(c, rc2, &d2lo, &d2hi);
+        k_build<<<nblk(n, kBlock), kBlock, 0, s>>>(a, c->cell_of, c->cell_rank, c->cell_start, rc2, d2lo, d2hi);
+    }
+    c->launches += 1;
+    return check_launch(c, "neighbour list");
+}
+
+static int finish_list(msmgb_ctx *c)
+{
     if (c->check_lists) {
-        k_check_list<<<nblk(n, kBlock), kBlock, 0, s>>>(a);
+        k_check_list<<<nblk(c->n, kBlock), kBlock, 0, c->stream>>>(c->a);
         c->launches += 1;
     }
-    return check_launch(c, "neighbour list");
+    const int rc = check_launch(c, "neighbour list");
+    if (rc || !c->halo_on) return rc;
+    return build_halo(c);
+}
+
+int build_inner(msmgb_ctx *c)
+{
+    const double rc2 = c->p.rc_nl * c->p.rc_nl;
+    float d2lo, d2hi;
+    prefilter_band(c, rc2, &d2lo, &d2hi);
+    k_inner<<<nblk(c->n, kBlock), kBlock, 0, c->stream>>>(c->a, c->cand, c->kcand, rc2, d2lo, d2hi);
+    c->launches += 1;
+    return finish_list(c);
+}
+
+int build_list(msmgb_ctx *c)
+{
+    const int rc = build_full(c);
+    if (rc) return rc;
+    return two_level(c) ? build_inner(c) : finish_list(c);
 }
 
 }  // namespace msmgb

@@ -52,19 +52,36 @@ __global__ void __launch_bounds__(kBlock) k_correct(DevAtoms a, double th, int o
 __global__ void k_clear_pending(int *flags) { flags[kFlagPending] = 0; }
 
 // Inside a step graph the decision also switches the graph's conditional rebuild node.
+// Two-level list (half_outer > 0): a rebuild is full (binning, sort, candidates) when the
+// displacement since the last full rebuild may exceed half the outer skin, bounded by the sum
+// of the interval maxima (each the largest displacement since the previous build); otherwise
+// only the list is re-selected from the candidates.  cond: the full body; cond_inner: the body
+// that runs on every rebuild.
 __global__ void k_decide(int *flags, unsigned long long *maxdisp, double thr2, int nb_uptab,
-                         cudaGraphConditionalHandle cond, int use_cond)
+                         cudaGraphConditionalHandle cond, int use_cond, float half_outer,
+                         cudaGraphConditionalHandle cond_inner)
 {
     int rebuild = 0;
+    const double md2 = __longlong_as_double((long long)*maxdisp);
     if (thr2 > 0.0) {
-        rebuild = __longlong_as_double((long long)*maxdisp) > thr2;
+        rebuild = md2 > thr2;
     } else if (nb_uptab > 0) {
         int step = ++flags[kFlagStep];
         rebuild = (step % nb_uptab) == 0;
     }
+    int full = rebuild;
+    if (rebuild && half_outer > 0.0f) {
+        const float acc = __int_as_float(flags[kFlagAcc]) + (float)sqrt(md2);
+        full = !(acc <= half_outer) || flags[kFlagOob] != 0;
+        flags[kFlagAcc] = __float_as_int(full ? 0.0f : acc);
+        if (full) flags[kFlagFull] += 1;
+    }
     flags[kFlagRebuild] = rebuild;
     if (rebuild) flags[kFlagRebuilds] += 1;
-    if (use_cond) cudaGraphSetConditional(cond, rebuild ? 1u : 0u);
+    if (use_cond) {
+        cudaGraphSetConditional(cond, full ? 1u : 0u);
+        if (half_outer > 0.0f) cudaGraphSetConditional(cond_inner, rebuild ? 1u : 0u);
+    }
     *maxdisp = 0ull;
     flags[kFlagPending] = 1;
 }
@@ -88,10 +105,14 @@ int launch_correct(msmgb_ctx *c, double h, bool only_if_pending)
     return check_launch(c, "corrector");
 }
 
-int launch_decide(msmgb_ctx *c, double skin_trigger, int nb_uptab, cudaGraphConditionalHandle cond, bool use_cond)
+int launch_decide(msmgb_ctx *c, double skin_trigger, int nb_uptab, cudaGraphConditionalHandle cond, bool use_cond,
+                  cudaGraphConditionalHandle cond_inner)
 {
     double thr2 = skin_trigger > 0.0 ? skin_trigger * skin_trigger : 0.0;
-    k_decide<<<1, 1, 0, c->stream>>>(c->a.flags, c->a.maxdisp, thr2, nb_uptab, cond, use_cond ? 1 : 0);
+    // the displacement bound comes from FP32 hi parts (within 3e-5 A of the positions): 1e-3 A margin
+    const float half_outer = (use_cond && two_level(c)) ? (float)(0.5 * c->outer_skin - 1e-3) : 0.0f;
+    k_decide<<<1, 1, 0, c->stream>>>(c->a.flags, c->a.maxdisp, thr2, nb_uptab, cond, use_cond ? 1 : 0, half_outer,
+                                     cond_inner);
     c->launches += 1;
     return check_launch(c, "rebuild decision");
 }

@@ -327,7 +327,7 @@ class Engine:
     """One device context: tables, a batch of boxes, neighbour list, force passes, MD steps."""
 
     def __init__(self, max_atoms, rc_nl, max_boxes=1, mxkvois=64, skin_trigger=0.15,
-                 nb_uptab=10, precision="fp64", device=0, stream=None):
+                 nb_uptab=10, precision="fp64", device=0, stream=None, outer_skin=None):
         self.lib = L.load()
         p = L.Params()
         p.device, p.max_atoms, p.max_boxes, p.mxkvois = device, int(max_atoms), int(max_boxes), int(mxkvois)
@@ -343,6 +343,8 @@ class Engine:
         self.n = 0
         self.nbox = 0
         self._table = None
+        if outer_skin is not None:
+            self.set_outer_skin(outer_skin)
 
     # ---- plumbing --------------------------------------------------------------------------
     def _ck(self, rc):
@@ -588,6 +590,29 @@ class Engine:
         """Pins kernel variants of the mixed passes (-1 leaves a choice to the tuner)."""
         codes = (C.c_int * 3)(density, force, fused)
         self._ck(self.lib.msmgb_set_tuning(self.ctx, codes))
+
+    def set_outer_skin(self, skin):
+        """Outer skin of the two-level list (0: off); applies from the next copyin."""
+        self._ck(self.lib.msmgb_set_outer_skin(self.ctx, float(skin)))
+
+    def rebuild_counts(self):
+        """(rebuilds, full rebuilds) done inside MD steps since the context was created."""
+        r, f = C.c_int64(), C.c_int64()
+        self._ck(self.lib.msmgb_rebuild_counts(self.ctx, C.byref(r), C.byref(f)))
+        return r.value, f.value
+
+    def time_rebuilds(self, reps=3):
+        """Device time (ms) of a full list rebuild and of a re-selection from the candidates."""
+        full, inner = C.c_float(), C.c_float()
+        self._ck(self.lib.msmgb_time_rebuilds(self.ctx, int(reps), C.byref(full), C.byref(inner)))
+        return dict(full=full.value, inner=inner.value)
+
+    def tile_stats(self):
+        """Cell tiles of the mixed passes: blocks, blocks with a tile, mean and largest halo."""
+        nb, nt, mx = C.c_int(), C.c_int(), C.c_int()
+        mean = C.c_double()
+        self._ck(self.lib.msmgb_tile_stats(self.ctx, C.byref(nb), C.byref(nt), C.byref(mean), C.byref(mx)))
+        return dict(blocks=nb.value, tiled=nt.value, mean_halo=mean.value, max_halo=mx.value)
 
     def list_stats(self):
         mk = C.c_int()

@@ -1,0 +1,109 @@
+"""Two-level neighbour list: a full rebuild keeps the candidates within rc_nl + outer skin and
+later rebuilds inside MD steps re-select the list from them.  The re-selected lists against the
+oracle's lists at the same positions (identical sets, MD_NeighborsList.F90:396-633 semantics),
+full rebuilds once the displacement bound passes half the outer skin, atoms leaving an open
+face, and two-level MD against single-level MD."""
+import numpy as np
+import pytest
+
+from msmpscu_gb300 import Engine, ForceTable, lattice as lt
+from helpers import sorted_sets
+
+pytestmark = pytest.mark.gpu
+
+
+def _engine(n, prec, outer_skin, nbox=1, skin=0.0, nb_uptab=5, mxk=96):
+    e = Engine(n, lt.CU_RC_NL, max_boxes=nbox, mxkvois=mxk, skin_trigger=skin, nb_uptab=nb_uptab,
+               precision=prec, outer_skin=outer_skin)
+    e.init_forcetable(ForceTable.cleri_rosato(**lt.CU_CR, rc=lt.CU_RC))
+    e.set_masses([lt.CU_MASS])
+    return e
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed", "ff"])
+def test_reselected_lists_equal_oracle(oracle, prec):
+    # a rebuild every 5 steps (fixed interval): after run_steps(5) the list belongs to the
+    # current positions; the hot lattice makes some rebuilds full and the others re-selections
+    pos, vel, L_ = lt.cu_config(8, 0.05, 1500.0, 4)
+    n = len(pos)
+    e = _engine(n, prec, 0.6)
+    e.copyin([(n, (0, 0, 0), tuple(L_), (1, 1, 1))], pos, vel)
+    box = oracle.make_box([0, 0, 0], L_)
+    for _ in range(8):
+        e.run_steps(5, 1.0)
+        kv, ind = e.get_neighborelist()
+        x = e.get_state()[0]
+        okv, oind = oracle.nlist(x, np.ones(n, np.int32), box, lt.CU_RC_NL, 96)
+        assert sorted_sets(kv, ind) == sorted_sets(okv, oind)
+    reb, full = e.rebuild_counts()
+    e.close()
+    assert reb == 8 and 0 < full < 8
+
+
+def test_reselection_small_box_and_open_face(oracle):
+    # 4-cell box (cells forced to 3 per edge, minimum image) with an open z face that atoms leave
+    rng = np.random.default_rng(3)
+    p, L_ = lt.fcc(4, 4, 4, lt.CU_A)
+    p = lt.displace(p, 0.05, rng, np.zeros(3), L_)
+    p[:, 2] = np.clip(p[:, 2], 0.05, L_[2] - 0.05)
+    n = len(p)
+    v = lt.velocities(n, lt.CU_MASS, 1500.0, rng)
+    v[:8, 2] = np.where(p[:8, 2] > L_[2] / 2, 0.05, -0.05)   # fast atoms toward the open faces
+    e = _engine(n, "fp64", 0.8)
+    e.copyin([(n, (0, 0, 0), tuple(L_), (1, 1, 0))], p, v)
+    box = oracle.make_box([0, 0, 0], L_, ifpd=(1, 1, 0))
+    for _ in range(6):
+        e.run_steps(5, 1.0)
+        kv, ind = e.get_neighborelist()
+        x, _, st, _ = e.get_state()
+        okv, oind = oracle.nlist(x, st, box, lt.CU_RC_NL, 96, brute=True)
+        assert sorted_sets(kv, ind) == sorted_sets(okv, oind)
+    e.close()
+
+
+def test_two_level_md_matches_single_level():
+    # same trajectory (FP64; only the summation order of a few lists differs) with the skin trigger
+    pos, vel, L_ = lt.cu_config(10, 0.05, 900.0, 8)
+    n = len(pos)
+    out = []
+    for skin in (0.0, 1.0):
+        e = _engine(n, "fp64", skin, skin=0.15, nb_uptab=10)
+        e.copyin([(n, (0, 0, 0), tuple(L_), (1, 1, 1))], pos, vel)
+        nr = e.run_steps(60, 1.0)
+        x, v, _, _ = e.get_state()
+        out.append((x, v, e.get_force(), nr, e.rebuild_counts()))
+        e.close()
+    (x0, v0, f0, n0, c0), (x1, v1, f1, n1, c1) = out
+    assert n0 == n1 and n0 > 1
+    assert c0 == (n0, n0) and c1[0] == n1 and c1[1] < n1
+    assert np.abs(x0 - x1).max() < 1e-9 and np.abs(v0 - v1).max() < 1e-12
+    assert np.abs(f0 - f1).max() < 1e-8 * np.abs(f0).max()
+
+
+def test_batched_boxes_reselection(oracle):
+    boxes, P, V = [], [], []
+    rng = np.random.default_rng(12)
+    for nc in (4, 7, 5, 9):
+        p, L_ = lt.fcc(nc, nc, nc, lt.CU_A)
+        P.append(lt.displace(p, 0.05, rng, np.zeros(3), L_))
+        V.append(lt.velocities(len(p), lt.CU_MASS, 1200.0, rng))
+        boxes.append((len(p), (0, 0, 0), tuple(L_), (1, 1, 1)))
+    pos, vel = np.vstack(P), np.vstack(V)
+    n = len(pos)
+    e = _engine(n, "mixed", 0.6, nbox=len(boxes))
+    e.copyin(boxes, pos, vel)
+    for _ in range(5):
+        e.run_steps(5, 1.0)
+    kv, ind = e.get_neighborelist()
+    x = e.get_state()[0]
+    off = 0
+    got = sorted_sets(kv, ind)
+    for (na, _, L_, _) in boxes:
+        box = oracle.make_box([0, 0, 0], L_)
+        okv, oind = oracle.nlist(x[off:off + na], np.ones(na, np.int32), box, lt.CU_RC_NL, 96)
+        want = [tuple(j + off for j in s) for s in sorted_sets(okv, oind)]
+        assert got[off:off + na] == want
+        off += na
+    reb, full = e.rebuild_counts()
+    e.close()
+    assert reb == 5 and full < 5
