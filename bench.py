@@ -262,10 +262,10 @@ def adjoint_cu_snapshots(device=0):
             "grad": [float(g) for g in grad]}
 
 
-def make_engine(n, precision, device=0):
+def make_engine(n, precision, device=0, outer_skin=None):
     from msmpscu_gb300 import Engine, ForceTable, lattice as lt
     e = Engine(n, lt.CU_RC_NL, mxkvois=MXKVOIS, skin_trigger=0.15, precision=precision, device=device,
-               outer_skin=OUTER_SKIN)
+               outer_skin=OUTER_SKIN if outer_skin is None else outer_skin)
     e.init_forcetable(ForceTable.cleri_rosato(**lt.CU_CR, rc=lt.CU_RC))
     e.set_masses([lt.CU_MASS])
     return e
@@ -442,9 +442,12 @@ def run_ours(args):
     pos, vel, L = workload(args.ncell)
     n = len(pos)
     prec = args.precision
-    e = make_engine(n, prec, device)
+    e = make_engine(n, prec, device, args.outer_skin)
     box = [(n, (0, 0, 0), tuple(L), (1, 1, 1))]
     e.copyin(box, pos, vel)
+    if args.pin:
+        d, f, u = (int(v) for v in args.pin.split(","))
+        e.set_tuning(density=d, force=f, fused=u)
     e.run_steps(args.warmup, DT)
     if dist:
         dist.barrier()
@@ -526,7 +529,7 @@ def run_ours(args):
                 "config": {**workload_config(args.ncell, n), "precision": prec, "parallelism": "replicas" if ws > 1 else "single GPU",
                            "l2": "inputs larger than L2 (~0.9 GB touched per step)",
                            "rebuilds_in_timed_steps": rebuilds, "full_rebuilds_in_timed_steps": full_rebuilds,
-                           "outer_skin": OUTER_SKIN, "mean_neighbours": kmean,
+                           "outer_skin": args.outer_skin, "pinned_variants": args.pin, "mean_neighbours": kmean,
                            "max_neighbours": kmax},
                 "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm,
                              "unit": "GB/s", "frac": achieved / hbm, "traffic": traffic,
@@ -589,6 +592,10 @@ def main():
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the batched-box, HVP and adjoint measurements")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--outer-skin", type=float, default=OUTER_SKIN,
+                    help="two-level list: candidates within rc_nl + this skin (0: single-level)")
+    ap.add_argument("--pin", default=None,
+                    help="mixed passes: kernel variant codes density,force,fused instead of the tuner's")
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--ref-budget-s", type=float, default=150.0)
     args = ap.parse_args()
