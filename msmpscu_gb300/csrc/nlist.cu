@@ -658,6 +658,11 @@ static int ensure_candidates(msmgb_ctx *c)
     const double r = (c->p.rc_nl + c->outer_skin) / c->p.rc_nl;
     const int mxo = (((int)ceil(c->p.mxkvois * r * r * r * 1.1) + 7) / 8) * 8;
     if (c->cand && c->mxo == mxo) return MSMGB_OK;
+    // allocated by the host-side full build that precedes every step-graph capture
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaStreamIsCapturing(c->stream, &cs);
+    if (cs != cudaStreamCaptureStatusNone)
+        return set_err(c, MSMGB_ERR_ARG, "candidate list allocation inside a graph capture");
     cudaError_t e = cudaStreamSynchronize(c->stream);
     if (c->cand) cudaFree(c->cand);
     if (c->kcand) cudaFree(c->kcand);

@@ -250,9 +250,11 @@ def test_hvp_parity_and_finite_difference(oracle):
     e.close()
 
 
-def test_neighbour_overflow_reported():
+@pytest.mark.parametrize("outer_skin", [0.0, 1.0])   # list overflow / candidate-list overflow
+def test_neighbour_overflow_reported(outer_skin):
     pos, vel, L_ = lt.cu_config(6, 0.02, 300.0, 1)
     e = _cu_engine(len(pos), mxk=16)
+    e.set_outer_skin(outer_skin)
     e.copyin(_box(len(pos), L_), pos, vel)
     with pytest.raises(MSMError) as ei:
         e.cal_neighborelist()
