@@ -621,7 +621,22 @@ extern "C" int msmgb_copyin_simbox(msmgb_ctx *c, int nbox, const msmgb_box *boxe
         atom0 += boxes[b].natom;
     }
     CK(cudaStreamSynchronize(c->stream), "synchronize");
-    free_graph(c);
+    {   // the step graphs hold the atom count, the cell grid and the prefilter band of the
+        // box extents: a state of the same layout keeps them
+        std::vector<double> gl = {(double)n, (double)nbox, bin_rc, (double)cells};
+        for (int b = 0; b < nbox; ++b) {
+            gl.push_back((double)boxes[b].natom);
+            for (int k = 0; k < 3; ++k) {
+                gl.push_back(boxes[b].lo[k]);
+                gl.push_back(boxes[b].len[k]);
+                gl.push_back((double)boxes[b].ifpd[k]);
+            }
+        }
+        if (gl != c->graph_layout || cells + 2 > c->cap_cells) {
+            free_graph(c);
+            c->graph_layout = gl;
+        }
+    }
     if (cells + 2 > c->cap_cells) {
         if (c->cell_start) cudaFree(c->cell_start);
         if (c->cell_cursor) cudaFree(c->cell_cursor);

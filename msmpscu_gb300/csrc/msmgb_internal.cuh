@@ -321,6 +321,7 @@ struct msmgb_ctx {
     bool cell_row_order = false;  // MSMGB_CELL_ORDER=row: x-fastest cell storage instead
     bool check_lists = false;     // MSMGB_CHECK_LISTS=1: validate every list after its build
     std::vector<int> rank_layout; // cell grids (and order) the uploaded cell_rank was made for
+    std::vector<double> graph_layout;  // atoms, boxes and cell size the step graphs were captured for
     int *scan_tmp = nullptr;
     void *scratch = nullptr;           // permutation staging (size: 96 B per atom)
     double *cm = nullptr;

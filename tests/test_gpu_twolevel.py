@@ -107,3 +107,29 @@ def test_batched_boxes_reselection(oracle):
     reb, full = e.rebuild_counts()
     e.close()
     assert reb == 5 and full < 5
+
+
+@pytest.mark.parametrize("prec", ["mixed", "fp64"])
+def test_new_state_of_same_layout_reuses_step_graphs(prec):
+    # a second copy-in of the same atom count and boxes keeps the captured step graphs; the
+    # trajectory equals that of a fresh context
+    p1, v1, L_ = lt.cu_config(12, 0.05, 900.0, 31)
+    p2, v2, _ = lt.cu_config(12, 0.08, 1200.0, 32)
+    n = len(p1)
+    box = [(n, (0, 0, 0), tuple(L_), (1, 1, 1))]
+    a = _engine(n, prec, 1.0, skin=0.15, nb_uptab=10)
+    a.copyin(box, p1, v1)
+    a.run_steps(30, 1.0)
+    a.copyin(box, p2, v2)
+    ra = a.run_steps(30, 1.0)
+    xa, va, _, _ = a.get_state()
+    fa = a.get_force()
+    a.close()
+    b = _engine(n, prec, 1.0, skin=0.15, nb_uptab=10)
+    b.copyin(box, p2, v2)
+    rb = b.run_steps(30, 1.0)
+    xb, vb, _, _ = b.get_state()
+    fb = b.get_force()
+    b.close()
+    assert ra == rb and ra > 0
+    assert np.array_equal(xa, xb) and np.array_equal(va, vb) and np.array_equal(fa, fb)
