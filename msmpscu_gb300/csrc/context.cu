@@ -371,6 +371,7 @@ static int poll_flags(msmgb_ctx *c)
             return set_err(c, MSMGB_ERR_NL_OVERFLOW, buf);
         }
         if (e & kErrCandOverflow) {
+            c->list_valid = false;     // the next host-side build grows the candidate buffer
             char buf[200];
             snprintf(buf, sizeof(buf), "candidate list overflow: an atom has more than %d candidates within "
                      "rc_nl + outer skin (raise MXKVOIS or lower the outer skin)", c->mxo);
@@ -695,6 +696,9 @@ extern "C" int msmgb_copyin_simbox(msmgb_ctx *c, int nbox, const msmgb_box *boxe
     }
     c->ncell_total = cells;
     c->bin_rc = bin_rc;
+    c->max_density = 0.0;
+    for (int b = 0; b < nbox; ++b)
+        c->max_density = std::max(c->max_density, boxes[b].natom / (boxes[b].len[0] * boxes[b].len[1] * boxes[b].len[2]));
     c->nbox = nbox;
     c->n = n;
     c->a.n = n;
@@ -1292,6 +1296,10 @@ static int capture_fused(msmgb_ctx *c, double h)
 
 static int ensure_graphs(msmgb_ctx *c, double h)
 {
+    if (c->graphs_stale) {
+        free_graph(c);
+        c->graphs_stale = false;
+    }
     if (fused_mixed(c)) {
         if (!c->g_pre || c->fg_h != h || c->fg_n != c->n || c->fg_prec != c->p.precision ||
             c->fg_tune != c->tune_dens_unroll * 64 + c->tune_force_unroll)

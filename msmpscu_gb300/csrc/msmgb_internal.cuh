@@ -66,6 +66,7 @@ enum {
     kFlagFull = 6,       // number of full rebuilds (two-level list) done by run_steps
     kFlagAcc = 7,        // float bits: bound on the displacement since the last full rebuild
     kFlagOob = 8,        // an atom left its box since the last full rebuild (next one is full)
+    kFlagMaxCand = 9,    // largest candidate count of the last full rebuild (two-level list)
     kFlagWords = 16
 };
 
@@ -315,9 +316,11 @@ struct msmgb_ctx {
     // two-level list: candidates within rc_nl + outer_skin, kept between full rebuilds
     double outer_skin = 1.0;      // 0: every rebuild bins, sorts and scans the cell stencil
     double bin_rc = 0.0;          // cell-size radius of the current layout
+    double max_density = 0.0;     // atoms per unit volume of the densest box
     int mxo = 0;                  // candidate slots per atom
     int *cand = nullptr;          // candidates, ELL layout [mxo][ld]
     int *kcand = nullptr;         // candidates per atom
+    bool graphs_stale = false;    // a buffer the step graphs hold was reallocated
     bool cell_row_order = false;  // MSMGB_CELL_ORDER=row: x-fastest cell storage instead
     bool check_lists = false;     // MSMGB_CHECK_LISTS=1: validate every list after its build
     std::vector<int> rank_layout; // cell grids (and order) the uploaded cell_rank was made for

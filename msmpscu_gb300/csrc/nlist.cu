@@ -19,6 +19,7 @@
 //               cell; boxes with NCELL forced to 3 the minimum image of every candidate.
 // In an MD-step graph the rebuild is the body of a conditional node that the step's
 // decision kernel switches on (context.cu), so steps without a rebuild launch none of these.
+#include <algorithm>
 #include <climits>
 
 #include "msmgb_internal.cuh"
@@ -336,6 +337,7 @@ __global__ void __launch_bounds__(kBlock, 6) k_build_cand(DevAtoms a, const int 
         a.flags[kFlagAcc] = 0;
         a.flags[kFlagOob] = 0;
     }
+    // (kFlagMaxCand is cleared by the host before a build it checks)
     if (i >= a.n) return;
     if (a.statu[i] & MSMGB_STATU_OUTOFBOX) { kcand[i] = 0; return; }
     const float4 pf = a.pos_bld[i];
@@ -379,6 +381,7 @@ __global__ void __launch_bounds__(kBlock, 6) k_build_cand(DevAtoms a, const int 
             }
         }
     }
+    atomicMax(&a.flags[kFlagMaxCand], nn);
     if (nn > mxo) {
         atomicOr(&a.flags[kFlagErr], kErrCandOverflow);
         nn = mxo;
@@ -653,10 +656,16 @@ bool two_level(const msmgb_ctx *c)
     return c->outer_skin > 0.0 && c->bin_rc >= c->p.rc_nl + c->outer_skin;
 }
 
-static int ensure_candidates(msmgb_ctx *c)
+static int ensure_candidates(msmgb_ctx *c, int need = 0)
 {
-    const double r = (c->p.rc_nl + c->outer_skin) / c->p.rc_nl;
-    const int mxo = (((int)ceil(c->p.mxkvois * r * r * r * 1.1) + 7) / 8) * 8;
+    // slots: MXKVOIS scaled by the volume ratio, at most twice the count the densest box
+    // gives for a sphere of rc_nl + skin (+32), so that a large MXKVOIS costs no memory
+    const double ro = c->p.rc_nl + c->outer_skin;
+    const double r = ro / c->p.rc_nl;
+    double by_mxk = ceil(c->p.mxkvois * r * r * r * 1.1);
+    double by_rho = 2.0 * (4.0 / 3.0) * 3.14159265358979 * ro * ro * ro * c->max_density + 32.0;
+    int mxo = (((int)std::min(by_mxk, by_rho) + 7) / 8) * 8;
+    mxo = std::max(mxo, std::max(need, c->mxo));      // never shrinks below a measured need
     if (c->cand && c->mxo == mxo) return MSMGB_OK;
     // allocated by the host-side full build that precedes every step-graph capture
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
@@ -743,11 +752,37 @@ int build_inner(msmgb_ctx *c)
     return finish_list(c);
 }
 
+// Host-side full build.  With a two-level list the largest candidate count is read back: a
+// candidate buffer that was too small (a denser region than the boxes' mean density) is
+// grown to 1.25 x that count + 16 and the build repeated, and the step graphs, which hold
+// the buffer's size, are recaptured.
 int build_list(msmgb_ctx *c)
 {
-    const int rc = build_full(c);
-    if (rc) return rc;
-    return two_level(c) ? build_inner(c) : finish_list(c);
+    if (!two_level(c)) {
+        const int rc = build_full(c);
+        return rc ? rc : finish_list(c);
+    }
+    for (int attempt = 0; attempt < 2; ++attempt) {
+        cudaError_t e = cudaMemsetAsync(c->a.flags + kFlagMaxCand, 0, sizeof(int), c->stream);
+        if (e != cudaSuccess) return cuda_err(c, e, "flag clear");
+        int rc = build_full(c);
+        if (rc) return rc;
+        int got[2] = {0, 0};     // error bits, largest candidate count
+        e = cudaMemcpyAsync(&got[0], c->a.flags + kFlagErr, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(&got[1], c->a.flags + kFlagMaxCand, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+        if (e != cudaSuccess) return cuda_err(c, e, "flag read");
+        if (got[1] <= c->mxo) break;
+        const int clear = got[0] & ~kErrCandOverflow;
+        e = cudaMemcpyAsync(c->a.flags + kFlagErr, &clear, sizeof(int), cudaMemcpyHostToDevice, c->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+        if (e != cudaSuccess) return cuda_err(c, e, "flag clear");
+        rc = ensure_candidates(c, (int)(1.25 * got[1]) + 16);
+        if (rc) return rc;
+        c->graphs_stale = true;
+    }
+    return build_inner(c);
 }
 
 }  // namespace msmgb

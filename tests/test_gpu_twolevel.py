@@ -133,3 +133,25 @@ def test_new_state_of_same_layout_reuses_step_graphs(prec):
     b.close()
     assert ra == rb and ra > 0
     assert np.array_equal(xa, xb) and np.array_equal(va, vb) and np.array_equal(fa, fb)
+
+
+def test_candidate_buffer_grows_for_a_dense_cluster(oracle):
+    # a bulk-density cluster in a box of 64x its volume: the candidate buffer sized from the
+    # box's mean density is too small at the first full build, is grown and the build redone
+    rng = np.random.default_rng(41)
+    p, Lc = lt.fcc(6, 6, 6, lt.CU_A)
+    L_ = 4.0 * Lc
+    pos = p + 1.5 * Lc + rng.normal(0.0, 0.03, p.shape)
+    n = len(pos)
+    vel = lt.velocities(n, lt.CU_MASS, 300.0, rng)
+    e = _engine(n, "mixed", 1.0, skin=0.15, nb_uptab=10)
+    e.copyin([(n, (0, 0, 0), tuple(L_), (0, 0, 0))], pos, vel)
+    e.cal_neighborelist()
+    kv, ind = e.get_neighborelist()
+    box = oracle.make_box([0, 0, 0], L_, ifpd=(0, 0, 0))
+    okv, oind = oracle.nlist(pos, np.ones(n, np.int32), box, lt.CU_RC_NL, 96)
+    assert sorted_sets(kv, ind) == sorted_sets(okv, oind)
+    e.run_steps(40, 1.0)
+    kv, ind = e.get_neighborelist()
+    assert kv.max() > 40
+    e.close()
