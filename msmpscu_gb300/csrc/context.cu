@@ -1668,10 +1668,17 @@ extern "C" int msmgb_set_tuning(msmgb_ctx *c, const int *codes)
             if (set[k] == v) return true;
         return false;
     };
-    if ((codes[0] >= 0 && !in(codes[0], valid_d, 15)) || (codes[1] >= 0 && !in(codes[1], valid_f, 15)) ||
-        codes[2] >= (c->tab.ngroup > 1 ? 4 : 24))
+    const bool multi = c->tab.ngroup > 1;
+    // density +128 (128-thread blocks) on the one-thread-per-atom families only
+    const int d = codes[0];
+    const bool d_ok = d < 0 || in(d, valid_d, 15) || ((d & 128) && (d & ~128) < 32 && (d & 8) == 0 &&
+                                                       in(d & ~128, valid_d, 15));
+    // fused: 0-23 (several kinds 0-3), + 32 for 0-17 (0-3) in 128-thread blocks
+    const int u = codes[2];
+    const bool u_ok = u < 0 || u < (multi ? 4 : 24) || (u >= 32 && u < 32 + (multi ? 4 : 18));
+    if (!d_ok || (codes[1] >= 0 && !in(codes[1], valid_f, 15)) || !u_ok)
         return set_err(c, MSMGB_ERR_ARG, "unknown kernel variant code");
-    if (((codes[0] >= 0 && (codes[0] & 64)) || codes[2] >= 20) &&
+    if (((codes[0] >= 0 && (codes[0] & 64)) || (codes[2] >= 20 && codes[2] < 24)) &&
         (c->tab.ngroup > 1 || c->p.precision != MSMGB_PREC_MIXED))
         return set_err(c, MSMGB_ERR_ARG, "cell-tile variants need one table kind and MIXED precision");
     if ((codes[2] == 18 || codes[2] == 19) && c->tab.ngroup == 1) {

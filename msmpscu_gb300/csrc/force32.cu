@@ -27,6 +27,8 @@
 // the autotuner times once per atom count.
 #include <algorithm>
 
+#include <vector>
+
 #include "msmgb_internal.cuh"
 
 namespace msmgb {
@@ -1063,7 +1065,8 @@ bool uses_tiles(const msmgb_ctx *c)
 // in addition every gather of a batch issued before its arithmetic (force_loop_batched),
 // 18-19 the TMA-streamed list (2 and 4 neighbours per batch; skipped without descriptors),
 // 20-23 cell tiles (2/4 neighbours per batch x halo capacity 2048 / 2560 atoms);
-// with several table kinds codes 0-3: 2/4 in flight x {plain, list prefetch}
+// with several table kinds codes 0-3: 2/4 in flight x {plain, list prefetch}.  Codes + 32:
+// codes 0-17 (several kinds: 0-3) in 128-thread blocks.
 constexpr int kFusedVariants = 24;
 
 template <int UNR, int MINB>
@@ -1077,41 +1080,45 @@ constexpr int kFusedVariantsMulti = 4;
 
 static void fused_variant(msmgb_ctx *c, int code, double h)
 {
-    const int g = nblk(c->n, kBlock);
+    // +32: the global-gather variants in 128-thread blocks (a finer last wave)
+    const int bs = (code & 32) ? 128 : kBlock;
+    code &= ~32;
+    const int g = nblk(c->n, bs);
+    const int g256 = nblk(c->n, kBlock);
     if (c->tab.ngroup > 1) {      // several table kinds: codes 0-3
         switch (code) {
-        case 1: k_force32_vv<4, 1, 0, true><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
-        case 2: k_force32_vv<2, 1, 1, true><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
-        case 3: k_force32_vv<4, 1, 1, true><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
-        default: k_force32_vv<2, 1, 0, true><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
+        case 1: k_force32_vv<4, 1, 0, true><<<g, bs, 0, c->stream>>>(c->a, c->tab, h); break;
+        case 2: k_force32_vv<2, 1, 1, true><<<g, bs, 0, c->stream>>>(c->a, c->tab, h); break;
+        case 3: k_force32_vv<4, 1, 1, true><<<g, bs, 0, c->stream>>>(c->a, c->tab, h); break;
+        default: k_force32_vv<2, 1, 0, true><<<g, bs, 0, c->stream>>>(c->a, c->tab, h); break;
         }
         return;
     }
     switch (code) {
-    case 1: k_force32_vv<4, 1, 0><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
-    case 2: k_force32_vv<2, 4, 0><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
-    case 3: k_force32_vv<4, 4, 0><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
-    case 4: k_force32_vv<2, 5, 0><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
-    case 5: k_force32_vv<4, 5, 0><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
-    case 6: k_force32_vv<2, 1, 1><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
-    case 7: k_force32_vv<4, 1, 1><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
-    case 8: k_force32_vv<2, 4, 1><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
-    case 9: k_force32_vv<4, 4, 1><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
-    case 10: k_force32_vv<2, 5, 1><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
-    case 11: k_force32_vv<4, 5, 1><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
-    case 12: k_force32_vv<2, 1, 2><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
-    case 13: k_force32_vv<4, 1, 2><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
-    case 14: k_force32_vv<2, 4, 2><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
-    case 15: k_force32_vv<4, 4, 2><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
-    case 16: k_force32_vv<2, 5, 2><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
-    case 17: k_force32_vv<4, 5, 2><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
-    case 18: k_force32_vv_tma<2><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h, c->tm_indi, c->tm_pk); break;
-    case 19: k_force32_vv_tma<4><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h, c->tm_indi, c->tm_pk); break;
+    case 1: k_force32_vv<4, 1, 0><<<g, bs, 0, c->stream>>>(c->a, c->tab, h); break;
+    case 2: k_force32_vv<2, 4, 0><<<g, bs, 0, c->stream>>>(c->a, c->tab, h); break;
+    case 3: k_force32_vv<4, 4, 0><<<g, bs, 0, c->stream>>>(c->a, c->tab, h); break;
+    case 4: k_force32_vv<2, 5, 0><<<g, bs, 0, c->stream>>>(c->a, c->tab, h); break;
+    case 5: k_force32_vv<4, 5, 0><<<g, bs, 0, c->stream>>>(c->a, c->tab, h); break;
+    case 6: k_force32_vv<2, 1, 1><<<g, bs, 0, c->stream>>>(c->a, c->tab, h); break;
+    case 7: k_force32_vv<4, 1, 1><<<g, bs, 0, c->stream>>>(c->a, c->tab, h); break;
+    case 8: k_force32_vv<2, 4, 1><<<g, bs, 0, c->stream>>>(c->a, c->tab, h); break;
+    case 9: k_force32_vv<4, 4, 1><<<g, bs, 0, c->stream>>>(c->a, c->tab, h); break;
+    case 10: k_force32_vv<2, 5, 1><<<g, bs, 0, c->stream>>>(c->a, c->tab, h); break;
+    case 11: k_force32_vv<4, 5, 1><<<g, bs, 0, c->stream>>>(c->a, c->tab, h); break;
+    case 12: k_force32_vv<2, 1, 2><<<g, bs, 0, c->stream>>>(c->a, c->tab, h); break;
+    case 13: k_force32_vv<4, 1, 2><<<g, bs, 0, c->stream>>>(c->a, c->tab, h); break;
+    case 14: k_force32_vv<2, 4, 2><<<g, bs, 0, c->stream>>>(c->a, c->tab, h); break;
+    case 15: k_force32_vv<4, 4, 2><<<g, bs, 0, c->stream>>>(c->a, c->tab, h); break;
+    case 16: k_force32_vv<2, 5, 2><<<g, bs, 0, c->stream>>>(c->a, c->tab, h); break;
+    case 17: k_force32_vv<4, 5, 2><<<g, bs, 0, c->stream>>>(c->a, c->tab, h); break;
+    case 18: k_force32_vv_tma<2><<<g256, kBlock, 0, c->stream>>>(c->a, c->tab, h, c->tm_indi, c->tm_pk); break;
+    case 19: k_force32_vv_tma<4><<<g256, kBlock, 0, c->stream>>>(c->a, c->tab, h, c->tm_indi, c->tm_pk); break;
     case 20: fused_tile<2, 3>(c, h, kTileCapSmall); break;
     case 21: fused_tile<4, 3>(c, h, kTileCapSmall); break;
     case 22: fused_tile<2, 2>(c, h, kTileCapLarge); break;
     case 23: fused_tile<4, 2>(c, h, kTileCapLarge); break;
-    default: k_force32_vv<2, 1, 0><<<g, kBlock, 0, c->stream>>>(c->a, c->tab, h); break;
+    default: k_force32_vv<2, 1, 0><<<g, bs, 0, c->stream>>>(c->a, c->tab, h); break;
     }
 }
 
@@ -1139,9 +1146,12 @@ int autotune_fused(msmgb_ctx *c)
     const bool multi = c->tab.ngroup > 1;
     const bool tma = !multi && ensure_list_maps(c) == 1;
     const bool tiles = !multi && enable_halo(c) == MSMGB_OK;
-    for (int code = 0; code < (multi ? kFusedVariantsMulti : kFusedVariants); ++code) {
+    std::vector<int> codes;
+    for (int code = 0; code < (multi ? kFusedVariantsMulti : kFusedVariants); ++code) codes.push_back(code);
+    for (int code = multi ? 0 : 6; code < (multi ? kFusedVariantsMulti : 18); ++code) codes.push_back(32 + code);
+    for (int code : codes) {
         if ((code == 18 || code == 19) && !tma) continue;
-        if (code >= 20 && !tiles) continue;
+        if (code >= 20 && code < 24 && !tiles) continue;
         for (int r = 0; r < 4; ++r) {
             if (r == 1) cudaEventRecord(e0, c->stream);
             fused_variant(c, code, 0.0);
@@ -1191,7 +1201,10 @@ static void dens_tile(msmgb_ctx *c, int cap)
 template <int POT, bool MULTI>
 static void dens_variant(msmgb_ctx *c, int unr)
 {
-    const int g = nblk(c->n, kBlock);
+    // +128: the one-thread-per-atom variants in 128-thread blocks (a finer last wave)
+    const int bs = (unr & 128) ? 128 : kBlock;
+    unr &= ~128;
+    const int g = nblk(c->n, bs);
     if (!MULTI && (unr & 64)) {   // cell tiles: +16 the larger halo capacity
         const bool large = (unr & 16) != 0;
         if ((unr & 7) == 4) {
@@ -1216,19 +1229,19 @@ static void dens_variant(msmgb_ctx *c, int unr)
     }
     if (unr & 16) {
         switch (unr & 7) {
-        case 4: k_density32<POT, MULTI, 4, 1, true><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
-        case 5: k_density32<POT, MULTI, 4, 6, true><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
-        case 3: k_density32<POT, MULTI, 2, 6, true><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
-        default: k_density32<POT, MULTI, 2, 1, true><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
+        case 4: k_density32<POT, MULTI, 4, 1, true><<<g, bs, 0, c->stream>>>(c->a, c->tab); break;
+        case 5: k_density32<POT, MULTI, 4, 6, true><<<g, bs, 0, c->stream>>>(c->a, c->tab); break;
+        case 3: k_density32<POT, MULTI, 2, 6, true><<<g, bs, 0, c->stream>>>(c->a, c->tab); break;
+        default: k_density32<POT, MULTI, 2, 1, true><<<g, bs, 0, c->stream>>>(c->a, c->tab); break;
         }
         return;
     }
     switch (unr & 7) {
-    case 1: k_density32<POT, MULTI, 1, 1, false><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
-    case 4: k_density32<POT, MULTI, 4, 1, false><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
-    case 5: k_density32<POT, MULTI, 4, 6, false><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
-    case 3: k_density32<POT, MULTI, 2, 6, false><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
-    default: k_density32<POT, MULTI, 2, 1, false><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
+    case 1: k_density32<POT, MULTI, 1, 1, false><<<g, bs, 0, c->stream>>>(c->a, c->tab); break;
+    case 4: k_density32<POT, MULTI, 4, 1, false><<<g, bs, 0, c->stream>>>(c->a, c->tab); break;
+    case 5: k_density32<POT, MULTI, 4, 6, false><<<g, bs, 0, c->stream>>>(c->a, c->tab); break;
+    case 3: k_density32<POT, MULTI, 2, 6, false><<<g, bs, 0, c->stream>>>(c->a, c->tab); break;
+    default: k_density32<POT, MULTI, 2, 1, false><<<g, bs, 0, c->stream>>>(c->a, c->tab); break;
     }
 }
 
@@ -1312,11 +1325,12 @@ int autotune_mixed(msmgb_ctx *c)
     // +8: persistent grid with the table in shared memory (single kind only)
     const bool single = c->tab.ngroup == 1;
     // +64 (density, single kind): cell tiles (+16: larger halo capacity)
-    const int dcands[15] = {1, 2, 4, 3, 5, 18, 20, 19, 21, 9, 10, 66, 68, 82, 84};
+    // +128: 128-thread blocks
+    const int dcands[19] = {1, 2, 4, 3, 5, 18, 20, 19, 21, 131, 133, 147, 149, 9, 10, 66, 68, 82, 84};
     const int fcands[15] = {1, 2, 4, 3, 5, 18, 20, 19, 21, 50, 52, 51, 53, 9, 10};
     const int *cands = dcands;
     const bool tiles = single && enable_halo(c) == MSMGB_OK;
-    int ncand = single ? (tiles ? 15 : 11) : 9;
+    int ncand = single ? (tiles ? 19 : 15) : 13;
     cudaEvent_t e0, e1;
     cudaError_t err = cudaEventCreate(&e0);
     if (err == cudaSuccess) err = cudaEventCreate(&e1);

@@ -116,3 +116,14 @@ def test_tile_variants_need_mixed_single_kind():
     with pytest.raises(MSMError):
         e.set_tuning(density=66)
     e.close()
+
+
+@pytest.mark.parametrize("d256,d128,u256,u128", [(3, 131, 14, 46), (19, 147, 12, 44), (5, 133, 17, 49)])
+def test_128_thread_block_variants_match(d256, d128, u256, u128):
+    # the block size changes only the grid, not the arithmetic of an atom
+    pos, vel, L_ = lt.cu_config(9, 0.08, 1200.0, 17)      # 2,916 atoms: partial last blocks
+    boxes = [(len(pos), (0, 0, 0), tuple(L_), (1, 1, 1))]
+    fa, xa, va, fa2, _ = _run(boxes, pos, vel, d256, u256, steps=30)
+    fb, xb, vb, fb2, _ = _run(boxes, pos, vel, d128, u128, steps=30)
+    assert np.array_equal(fa, fb)
+    assert np.array_equal(xa, xb) and np.array_equal(va, vb) and np.array_equal(fa2, fb2)
