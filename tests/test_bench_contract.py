@@ -40,6 +40,7 @@ def test_gpu_arm_json_line():
     assert d["n_gpus"] == 1 and d["steps"] == 5 and d["warmup"] == 3 and d["value"] > 0
     for k in ("bound", "achieved", "peak", "unit", "frac", "traffic"):
         assert k in d["roofline"], k
+    assert d["roofline"]["kernel"] in d["roofline_per_kernel"]
     for k in ("value", "unit", "h2d_bytes_per_step", "d2h_bytes_per_step"):
         assert k in d["e2e"], k
     assert d["e2e"]["h2d_bytes_per_step"] > 0 and d["e2e"]["d2h_bytes_per_step"] > 0
