@@ -38,6 +38,29 @@ constexpr int kDkBits = 18;
 constexpr float kDkScale = 262144.0f;       // 2^18
 constexpr float kDkInv = 1.0f / 262144.0f;
 
+// Compensated (Kahan) FP32 sum of the pair terms: s - c carries the sum of the rounded terms
+// to about twice FP32 precision, so the order and number of the ~46 terms do not add to the
+// error of a density or force component.
+struct KSum {
+    float s = 0.0f, c = 0.0f;       // running sum, its lost low part (negated)
+    __device__ __forceinline__ void add(float x)
+    {
+        const float y = x - c;
+        const float t = s + y;
+        c = (t - s) - y;
+        s = t;
+    }
+    __device__ __forceinline__ void fma_add(float a, float b)     // += a * b
+    {
+        const float y = fmaf(a, b, -c);
+        const float t = s + y;
+        c = (t - s) - y;
+        s = t;
+    }
+    __device__ __forceinline__ float value() const { return s - c; }
+    __device__ __forceinline__ double value64() const { return (double)s - (double)c; }
+};
+
 // One 256-bit load / store per 32 B record (sm_100+ vector width): a gather of 32 lanes'
 // records then touches each sector once instead of once per 16 B half.  The records are
 // 32 B aligned (PosFF is __align__(32), buffers come from cudaMalloc).
@@ -155,7 +178,7 @@ __global__ void __launch_bounds__(kBlock, MINB) k_density32(DevAtoms a, DevTable
     const int ti = MULTI ? a.ityp[i] - 1 : 0;
     const int *__restrict__ nb = a.indi + i;
     const float2 *__restrict__ row0 = t.dens2;
-    float rho = 0.0f;
+    KSum racc;
     if (PF) {
         // list entries of the next UNR slots are loaded one iteration ahead (slots past
         // KVOIS are marked -1), so the stream of ELL columns overlaps the position gathers
@@ -184,7 +207,7 @@ __global__ void __launch_bounds__(kBlock, MINB) k_density32(DevAtoms a, DevTable
                 const bool ok = j[u] >= 0 && c != kSkip;
                 const int k = MULTI ? t.kpair[(a.ityp[j[u] >= 0 ? j[u] : i] - 1) * t.ngroup + ti] : 0;
                 const float2 e = __ldg(row0 + k * t.ntp + (ok ? kk : 0));
-                rho += ok ? fmaf(dk, e.y, e.x) : 0.0f;
+                if (ok) racc.add(fmaf(dk, e.y, e.x));   // a skipped slot adds nothing (not even 0)
             }
         }
     } else {
@@ -206,7 +229,7 @@ __global__ void __launch_bounds__(kBlock, MINB) k_density32(DevAtoms a, DevTable
                 if (c != kSkip) {
                     const int k = MULTI ? t.kpair[(a.ityp[j[u]] - 1) * t.ngroup + ti] : 0;
                     const float2 e = __ldg(row0 + k * t.ntp + kk);
-                    rho += fmaf(dk, e.y, e.x);
+                    racc.add(fmaf(dk, e.y, e.x));
                 }
             }
         }
@@ -220,10 +243,11 @@ __global__ void __launch_bounds__(kBlock, MINB) k_density32(DevAtoms a, DevTable
             if (c != kSkip) {
                 const int k = MULTI ? t.kpair[(a.ityp[j0] - 1) * t.ngroup + ti] : 0;
                 const float2 e = __ldg(row0 + k * t.ntp + kk);
-                rho += fmaf(dk, e.y, e.x);
+                racc.add(fmaf(dk, e.y, e.x));
             }
         }
     }
+    const float rho = racc.value();
     float d = rho;
     if (POT == MSMGB_FS_TYPE) {
         if (rho > 0.0f) d = -0.5f * rsqrtf(rho);
@@ -256,7 +280,7 @@ __device__ __forceinline__ float sep1(float hi, float lo, float hj, float lj, fl
 template <bool MULTI>
 __device__ __forceinline__ void force_pair(const PosFF &pi, const PosFF &pj, unsigned c, float di,
                                            float dj, int ti, int tj, const BoxF &b, const DevTables &t,
-                                           float &fx, float &fy, float &fz)
+                                           KSum &fx, KSum &fy, KSum &fz)
 {
     const float sx = sep1(pi.hx, pi.lx, pj.hx, pj.lx, b.lh[0], b.ll[0], b.half[0], b.pd[0]);
     const float sy = sep1(pi.hy, pi.ly, pj.hy, pj.ly, b.lh[1], b.ll[1], b.half[1], b.pd[1]);
@@ -277,9 +301,9 @@ __device__ __forceinline__ void force_pair(const PosFF &pi, const PosFF &pj, uns
         }
     }
     const float ft = fmaf(P, y, emb) * y;
-    fx = fmaf(ft, sx, fx);
-    fy = fmaf(ft, sy, fy);
-    fz = fmaf(ft, sz, fz);
+    fx.fma_add(ft, sx);
+    fy.fma_add(ft, sy);
+    fz.fma_add(ft, sz);
 }
 
 // Walks the ELL list of atom i, UNR slots per iteration, and calls body(j, c) for every slot
@@ -338,7 +362,7 @@ __device__ __forceinline__ void walk_pairs(const int *__restrict__ nb, const uns
 
 // Single-kind pair term with the table row e = {P, P', B, B'} (at KK) already loaded.
 __device__ __forceinline__ void force_pair_e(const PosFF &pi, const PosFF &pj, unsigned c, float di, float dj,
-                                             const float4 &e, const BoxF &b, float &fx, float &fy, float &fz)
+                                             const float4 &e, const BoxF &b, KSum &fx, KSum &fy, KSum &fz)
 {
     const float sx = sep1(pi.hx, pi.lx, pj.hx, pj.lx, b.lh[0], b.ll[0], b.half[0], b.pd[0]);
     const float sy = sep1(pi.hy, pi.ly, pj.hy, pj.ly, b.lh[1], b.ll[1], b.half[1], b.pd[1]);
@@ -348,9 +372,9 @@ __device__ __forceinline__ void force_pair_e(const PosFF &pi, const PosFF &pj, u
     const float P = fmaf(dk, e.y, e.x);
     const float B = fmaf(dk, e.w, e.z);
     const float ft = fmaf(P, y, B * (di + dj)) * y;
-    fx = fmaf(ft, sx, fx);
-    fy = fmaf(ft, sy, fy);
-    fz = fmaf(ft, sz, fz);
+    fx.fma_add(ft, sx);
+    fy.fma_add(ft, sy);
+    fz.fma_add(ft, sz);
 }
 
 // Single-kind force loop over the ELL list of atom i with every load of a batch issued
@@ -361,7 +385,7 @@ __device__ __forceinline__ void force_pair_e(const PosFF &pi, const PosFF &pj, u
 // gather chain per slot.
 template <int UNR>
 __device__ __forceinline__ void force_loop_batched(const DevAtoms &a, const DevTables &t, int i, const PosFF &pi,
-                                                   float di, const BoxF &b, float &fx, float &fy, float &fz)
+                                                   float di, const BoxF &b, KSum &fx, KSum &fy, KSum &fz)
 {
     const int *__restrict__ nb = a.indi + i;
     const unsigned *__restrict__ pk = a.pk + i;
@@ -407,7 +431,7 @@ __global__ void __launch_bounds__(kBlock, MINB) k_force32(DevAtoms a, DevTables 
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
-    float fx = 0.0f, fy = 0.0f, fz = 0.0f;
+    KSum fx, fy, fz;
     if ((a.statu[i] & MSMGB_STATU_ACTIVE) == MSMGB_STATU_ACTIVE) {
         const BoxF b = load_boxf(a.box[a.boxid[i]]);
         const PosFF pi = ld_ff(a.rec + i);
@@ -422,9 +446,9 @@ __global__ void __launch_bounds__(kBlock, MINB) k_force32(DevAtoms a, DevTables 
             });
         }
     }
-    a.fx[i] = (double)fx;
-    a.fy[i] = (double)fy;
-    a.fz[i] = (double)fz;
+    a.fx[i] = fx.value64();
+    a.fy[i] = fy.value64();
+    a.fz[i] = fz.value64();
 }
 
 // ---- persistent variants with the used table range in shared memory -----------------
@@ -452,7 +476,7 @@ __global__ void __launch_bounds__(kBlock) k_density32s(DevAtoms a, DevTables t, 
         const float rej = t.ru2h + 4.0f * sqrtf(t.ru2h) * b.dlmax + 1e-5f * t.ru2h;
         const PosFF pi = ld_ff(a.posff + i);
         const int *__restrict__ nb = a.indi + i;
-        float rho = 0.0f;
+        KSum racc;
         int w = 0;
         for (; w + UNR <= kn; w += UNR) {
             int j[UNR];
@@ -469,7 +493,7 @@ __global__ void __launch_bounds__(kBlock) k_density32s(DevAtoms a, DevTables t, 
                 pk[(w + u) * ld] = c;
                 if (c != kSkip) {
                     const float2 e = kk >= kmin ? sdens[kk - kmin] : __ldg(t.dens2 + kk);
-                    rho += fmaf(dk, e.y, e.x);
+                    racc.add(fmaf(dk, e.y, e.x));
                 }
             }
         }
@@ -482,9 +506,10 @@ __global__ void __launch_bounds__(kBlock) k_density32s(DevAtoms a, DevTables t, 
             pk[w * ld] = c;
             if (c != kSkip) {
                 const float2 e = kk >= kmin ? sdens[kk - kmin] : __ldg(t.dens2 + kk);
-                rho += fmaf(dk, e.y, e.x);
+                racc.add(fmaf(dk, e.y, e.x));
             }
         }
+        const float rho = racc.value();
         float d = rho;
         if (POT == MSMGB_FS_TYPE) {
             if (rho > 0.0f) d = -0.5f * rsqrtf(rho);
@@ -513,7 +538,7 @@ __global__ void __launch_bounds__(kBlock) k_force32s(DevAtoms a, DevTables t, in
     __syncthreads();
     const size_t ld = (size_t)a.ld;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += gridDim.x * blockDim.x) {
-        float fx = 0.0f, fy = 0.0f, fz = 0.0f;
+        KSum fx, fy, fz;
         if ((a.statu[i] & MSMGB_STATU_ACTIVE) == MSMGB_STATU_ACTIVE) {
             const BoxF b = load_boxf(a.box[a.boxid[i]]);
             const PosFF pi = ld_ff(a.rec + i);
@@ -544,15 +569,15 @@ __global__ void __launch_bounds__(kBlock) k_force32s(DevAtoms a, DevTables t, in
                     const float P = fmaf(dk, e.y, e.x);
                     const float B = fmaf(dk, e.w, e.z);
                     const float ft = fmaf(P, y, B * (di + dj)) * y;
-                    fx = fmaf(ft, sx, fx);
-                    fy = fmaf(ft, sy, fy);
-                    fz = fmaf(ft, sz, fz);
+                    fx.fma_add(ft, sx);
+                    fy.fma_add(ft, sy);
+                    fz.fma_add(ft, sz);
                 }
             }
         }
-        a.fx[i] = (double)fx;
-        a.fy[i] = (double)fy;
-        a.fz[i] = (double)fz;
+        a.fx[i] = fx.value64();
+        a.fy[i] = fy.value64();
+        a.fz[i] = fz.value64();
     }
 }
 
@@ -570,7 +595,7 @@ __global__ void __launch_bounds__(kBlock, MINB) k_force32_vv(DevAtoms a, DevTabl
     double dmax = 0.0;
     if (i < a.n) {
         const int stat = a.statu[i];
-        float fx = 0.0f, fy = 0.0f, fz = 0.0f;
+        KSum fx, fy, fz;
         const DevBox &bb = a.box[a.boxid[i]];
         if ((stat & MSMGB_STATU_ACTIVE) == MSMGB_STATU_ACTIVE) {
             const BoxF b = load_boxf(bb);
@@ -591,7 +616,7 @@ __global__ void __launch_bounds__(kBlock, MINB) k_force32_vv(DevAtoms a, DevTabl
                 });
             }
         }
-        const double Fx = (double)fx, Fy = (double)fy, Fz = (double)fz;
+        const double Fx = fx.value64(), Fy = fy.value64(), Fz = fz.value64();
         a.fx[i] = Fx;
         a.fy[i] = Fy;
         a.fz[i] = Fz;
@@ -682,7 +707,7 @@ template <int UNR, class Idx, class Load>
 __device__ __forceinline__ float density_loop(const DevTables &t, const Idx *__restrict__ nb, unsigned *__restrict__ pk,
                                               size_t ld, int kn, const PosFF &pi, const BoxF &b, float rej, Load load)
 {
-    float rho = 0.0f;
+    KSum racc;
     int jn[UNR];
 #pragma unroll
     for (int u = 0; u < UNR; ++u) jn[u] = u < kn ? (int)__ldg(nb + u * ld) : -1;
@@ -706,10 +731,10 @@ __device__ __forceinline__ float density_loop(const DevTables &t, const Idx *__r
             if (j[u] >= 0) pk[(w + u) * ld] = c;
             const bool ok = j[u] >= 0 && c != kSkip;
             const float2 e = __ldg(t.dens2 + (ok ? kk : 0));
-            rho += ok ? fmaf(dk, e.y, e.x) : 0.0f;
+            if (ok) racc.add(fmaf(dk, e.y, e.x));   // a skipped slot adds nothing (not even 0)
         }
     }
-    return rho;
+    return racc.value();
 }
 
 template <int POT, int UNR, int MINB>
@@ -752,7 +777,7 @@ __global__ void __launch_bounds__(kBlock, MINB) k_density32t(DevAtoms a, DevTabl
 template <int UNR>
 __device__ __forceinline__ void force_loop_tile(const DevAtoms &a, const DevTables &t, int i, const PosFF &pi,
                                                 float di, const BoxF &b, const float4 *s_hi, const float4 *s_lo,
-                                                float &fx, float &fy, float &fz)
+                                                KSum &fx, KSum &fy, KSum &fz)
 {
     const unsigned short *__restrict__ nb = a.lidx + i;
     const unsigned *__restrict__ pk = a.pk + i;
@@ -804,7 +829,7 @@ __global__ void __launch_bounds__(kBlock, MINB) k_force32_vv_t(DevAtoms a, DevTa
     double dmax = 0.0;
     if (i < a.n) {
         const int stat = a.statu[i];
-        float fx = 0.0f, fy = 0.0f, fz = 0.0f;
+        KSum fx, fy, fz;
         const DevBox &bb = a.box[a.boxid[i]];
         if ((stat & MSMGB_STATU_ACTIVE) == MSMGB_STATU_ACTIVE) {
             const BoxF b = load_boxf(bb);
@@ -812,7 +837,7 @@ __global__ void __launch_bounds__(kBlock, MINB) k_force32_vv_t(DevAtoms a, DevTa
             if (tiled) force_loop_tile<UNR>(a, t, i, pi, pi.d, b, s_hi, s_lo, fx, fy, fz);
             else force_loop_batched<UNR>(a, t, i, pi, pi.d, b, fx, fy, fz);
         }
-        const double Fx = (double)fx, Fy = (double)fy, Fz = (double)fz;
+        const double Fx = fx.value64(), Fy = fy.value64(), Fz = fz.value64();
         a.fx[i] = Fx;
         a.fy[i] = Fy;
         a.fz[i] = Fz;
@@ -954,7 +979,7 @@ __global__ void __launch_bounds__(kBlock, 4)
             tma_load_2d(&s_indi[st][0][0], &tm_indi, i0, st * kTmaSlots, &bar[st]);
             tma_load_2d(&s_pk[st][0][0], &tm_pk, i0, st * kTmaSlots, &bar[st]);
         }
-    float fx = 0.0f, fy = 0.0f, fz = 0.0f;
+    KSum fx, fy, fz;
     PosFF pi;
     BoxF b;
     if (act) {
@@ -1005,7 +1030,7 @@ __global__ void __launch_bounds__(kBlock, 4)
     }
     double dmax = 0.0;
     if (in) {
-        const double Fx = (double)fx, Fy = (double)fy, Fz = (double)fz;
+        const double Fx = fx.value64(), Fy = fy.value64(), Fz = fz.value64();
         a.fx[i] = Fx;
         a.fy[i] = Fy;
         a.fz[i] = Fz;
