@@ -330,7 +330,8 @@ __global__ void __launch_bounds__(kBlock, 6) k_build(DevAtoms a, const int *cell
 // lists are the sets k_build would give.  The atoms keep their cell order between full
 // rebuilds.
 __global__ void __launch_bounds__(kBlock, 6) k_build_cand(DevAtoms a, const int *cell_of, const int *rank,
-                                                       const int *start, int *cand, int *kcand, int mxo, float d2o)
+                                                       const int *start, int *cand, int *kcand, int mxo, float d2o,
+                                                       double ro2)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i == 0) {                          // displacement bound and box exits since this full rebuild
@@ -344,12 +345,15 @@ __global__ void __launch_bounds__(kBlock, 6) k_build_cand(DevAtoms a, const int 
     const DevBox &b = a.box[a.boxid[i]];
     int nc[3], pd[3];
     float lf[3], hf[3];
+    bool wide = true;
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
         nc[k] = b.nc[k];
         pd[k] = b.ifpd[k];
         lf[k] = b.lenf[k];
         hf[k] = b.halff[k];
+        const double w = b.len[k] / nc[k];
+        if (pd[k] && w * w < ro2) wide = false;
     }
     const int cell0 = b.cell0;
     const int c = cell_of[i] - cell0;
@@ -360,24 +364,44 @@ __global__ void __launch_bounds__(kBlock, 6) k_build_cand(DevAtoms a, const int 
     const float4 *const hi = a.pos_bld;
     for (int s = 0; s < 27; ++s) {
         int j3[3] = {ix + c_nix[s], iy + c_niy[s], iz + c_niz[s]};
+        float sh[3];
         bool skip = false;
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
-            if (pd[k]) j3[k] = (j3[k] + nc[k]) % nc[k];
-            else if (j3[k] < 0 || j3[k] >= nc[k]) skip = true;
+            sh[k] = 0.0f;
+            if (pd[k]) {
+                // candidate cell wrapped to the other end: its image lies one box length away
+                if (j3[k] >= nc[k]) { j3[k] = 0; sh[k] = -lf[k]; }
+                else if (j3[k] < 0) { j3[k] = nc[k] - 1; sh[k] = lf[k]; }
+            }
+            if (j3[k] < 0 || j3[k] >= nc[k]) skip = true;
         }
         if (skip) continue;
         const int g = rank[cell0 + j3[0] + nc[0] * (j3[1] + nc[1] * j3[2])];
         const int j0 = start[g], e = start[g + 1];
-        for (int j = j0; j < e; ++j) {
-            const float4 q = hi[j];
-            const float sx = mi32(pf.x - q.x, lf[0], hf[0], pd[0]);
-            const float sy = mi32(pf.y - q.y, lf[1], hf[1], pd[1]);
-            const float sz = mi32(pf.z - q.z, lf[2], hf[2], pd[2]);
-            const float d2f = fmaf(sx, sx, fmaf(sy, sy, sz * sz));
-            if (j != i && d2f < d2o) {
-                if (nn < mxo) out[(size_t)nn * ld] = j;
-                ++nn;
+        if (wide) {   // cells of at least rc_nl + skin: the stencil cell's image is the nearest
+            for (int j = j0; j < e; ++j) {
+                const float4 q = hi[j];
+                const float sx = (pf.x - q.x) + sh[0];
+                const float sy = (pf.y - q.y) + sh[1];
+                const float sz = (pf.z - q.z) + sh[2];
+                const float d2f = fmaf(sx, sx, fmaf(sy, sy, sz * sz));
+                if (j != i && d2f < d2o) {
+                    if (nn < mxo) out[(size_t)nn * ld] = j;
+                    ++nn;
+                }
+            }
+        } else {
+            for (int j = j0; j < e; ++j) {
+                const float4 q = hi[j];
+                const float sx = mi32(pf.x - q.x, lf[0], hf[0], pd[0]);
+                const float sy = mi32(pf.y - q.y, lf[1], hf[1], pd[1]);
+                const float sz = mi32(pf.z - q.z, lf[2], hf[2], pd[2]);
+                const float d2f = fmaf(sx, sx, fmaf(sy, sy, sz * sz));
+                if (j != i && d2f < d2o) {
+                    if (nn < mxo) out[(size_t)nn * ld] = j;
+                    ++nn;
+                }
             }
         }
     }
@@ -720,7 +744,7 @@ int build_full(msmgb_ctx *c)
         float d2lo, d2hi;
         prefilter_band(c, ro * ro, &d2lo, &d2hi);
         k_build_cand<<<nblk(n, kBlock), kBlock, 0, s>>>(a, c->cell_of, c->cell_rank, c->cell_start, c->cand,
-                                                        c->kcand, c->mxo, d2hi);
+                                                        c->kcand, c->mxo, d2hi, ro * ro);
     } else {
         double rc2 = c->p.rc_nl * c->p.rc_nl;
         float d2lo, d2hi;
