@@ -155,3 +155,56 @@ def test_candidate_buffer_grows_for_a_dense_cluster(oracle):
     kv, ind = e.get_neighborelist()
     assert kv.max() > 40
     e.close()
+
+
+def test_reselection_bcc_w_eam(oracle):
+    # bcc W with a <111> dumbbell (Marinica EAM2, rc_nl = 5.76 A): re-selected lists equal the
+    # oracle's, FP64 forces at 1e-10 after the steps
+    from helpers import rel_err, w_tables
+    pos, L_ = lt.w_sia_config(8, 0.03, 5)
+    n = len(pos)
+    vel = lt.velocities(n, lt.W_MASS, 1500.0, np.random.default_rng(6))
+    e = Engine(n, lt.W_RC_NL, mxkvois=128, skin_trigger=0.0, nb_uptab=5, outer_skin=0.8)
+    e.init_forcetable(ForceTable.marinica_eam2(rc=lt.W_RC))
+    e.set_masses([lt.W_MASS])
+    e.copyin([(n, (0, 0, 0), tuple(L_), (1, 1, 1))], pos, vel)
+    box = oracle.make_box([0, 0, 0], L_)
+    t = w_tables(oracle)
+    st = np.ones(n, np.int32)
+    for _ in range(6):
+        e.run_steps(5, 1.0)
+        kv, ind = e.get_neighborelist()
+        x = e.get_state()[0]
+        okv, oind = oracle.nlist(x, st, box, lt.W_RC_NL, 128)
+        assert sorted_sets(kv, ind) == sorted_sets(okv, oind)
+    reb, full = e.rebuild_counts()
+    assert reb == 6 and full < 6
+    e.calforce()
+    ref = oracle.force(x, np.ones(n, np.int32), st, box, okv, oind, t)
+    assert rel_err(e.get_force(), ref["f"]) < 1e-10
+    e.close()
+
+
+@pytest.mark.parametrize("u256,u128", [(0, 32), (3, 35)])
+def test_two_species_fused_128_thread_blocks(oracle, u256, u128):
+    # several table kinds: the fused step kernel's 128-thread variants against the 256-thread
+    # ones (bitwise), with the two-level list
+    from test_gpu_edges import _two_species_tables
+    from msmpscu_gb300 import _lib as L
+    pos, vel, L_ = lt.cu_config(9, 0.05, 900.0, 44)
+    n = len(pos)
+    ityp = (np.random.default_rng(2).random(n) < 0.35).astype(np.int32) + 1
+    arr, kpair = _two_species_tables(oracle)
+    out = []
+    for code in (u256, u128):
+        e = Engine(n, lt.CU_RC_NL, mxkvois=80, precision="mixed")
+        e.init_forcetable_raw(L.FS_TYPE, 10000, 4, lt.CU_RC, lt.CU_RC, arr["potr"], arr["fpotr"],
+                              arr["potb"], arr["fpotb"], 2, kpair)
+        e.set_masses([lt.CU_MASS, 1.3 * lt.CU_MASS])
+        e.copyin([(n, (0, 0, 0), tuple(L_), (1, 1, 1))], pos, vel, ityp=ityp)
+        e.set_tuning(density=3, force=3, fused=code)
+        e.run_steps(25, 1.0)
+        x, v, _, _ = e.get_state()
+        out.append((x, v, e.get_force()))
+        e.close()
+    assert all(np.array_equal(a, b) for a, b in zip(out[0], out[1]))
