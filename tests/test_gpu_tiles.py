@@ -127,3 +127,26 @@ def test_128_thread_block_variants_match(d256, d128, u256, u128):
     fb, xb, vb, fb2, _ = _run(boxes, pos, vel, d128, u128, steps=30)
     assert np.array_equal(fa, fb)
     assert np.array_equal(xa, xb) and np.array_equal(va, vb) and np.array_equal(fa2, fb2)
+
+
+def test_tiles_eam_w_match_global_gathers():
+    # EAM (Marinica W, F'(rho) from the embedding table) on cell tiles against global gathers
+    pos, L_ = lt.w_sia_config(10, 0.03, 12)
+    n = len(pos)
+    vel = lt.velocities(n, lt.W_MASS, 900.0, np.random.default_rng(13))
+    out = []
+    for dens, fused in ((19, 12), (66, 20)):
+        e = Engine(n, lt.W_RC_NL, mxkvois=96, precision="mixed", outer_skin=0.0)
+        e.init_forcetable(ForceTable.marinica_eam2(rc=lt.W_RC))
+        e.set_masses([lt.W_MASS])
+        e.copyin([(n, (0, 0, 0), tuple(L_), (1, 1, 1))], pos, vel)
+        e.set_tuning(density=dens, force=20, fused=fused)
+        e.calforce()
+        f0 = e.get_force()
+        st = e.tile_stats()
+        e.run_steps(20, 1.0)
+        x, v, _, _ = e.get_state()
+        out.append((f0, x, v, e.get_force()))
+        e.close()
+    assert st["tiled"] > 0
+    assert all(np.array_equal(a, b) for a, b in zip(out[0], out[1]))
