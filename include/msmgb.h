@@ -229,6 +229,16 @@ int  msmgb_set_tuning(msmgb_ctx *ctx, const int *codes);
  * default is 1.0 A.  A new value applies from the next msmgb_copyin_simbox.  No counterpart
  * in the reference (it rebuilds at a fixed interval, MD_Method_GenericMD_GPU.F90:599). */
 int  msmgb_set_outer_skin(msmgb_ctx *ctx, double skin);
+/* Non-cubic box: BOXSHAPE of box ibox (SimBox%BOXSHAPE, MD_TypeDef_SimBox.F90:46), row K in
+ * bs[3K..3K+2]; the separation of two atoms in length units is BOXSHAPE . SEP, SEP the
+ * minimum-image difference of their positions (MD_FS_ForceTable.F90:235,333,
+ * MD_NeighborsList.F90:362-364).  Applies from the next msmgb_copyin_simbox; the identity is
+ * the default.  A state with a non-identity shape supports the FP64 calls (neighbour list,
+ * force, virial, energy, density, per-atom stress); MD, the mixed and float-float passes,
+ * the HVP and the adjoint return MSMGB_ERR_ARG for it.  Unlike the reference's GPU force
+ * pass (MD_FS_ForceTable_GPU.F90:775), the force pass applies the shape as its density pass
+ * and the reference's CPU force routine do. */
+int  msmgb_set_boxshape(msmgb_ctx *ctx, int ibox, const double *bs);
 /* Device time (ms) of a full list rebuild and of a re-selection from the candidates (0 without
  * a two-level list), averaged over reps launches.  No counterpart in the reference. */
 int  msmgb_time_rebuilds(msmgb_ctx *ctx, int reps, float *full_ms, float *inner_ms);

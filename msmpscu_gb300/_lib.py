@@ -99,6 +99,7 @@ SIGNATURES = [
     ("msmgb_list_stats", C.c_int, [C.c_void_p, _ip, _dp]),
     ("msmgb_tile_stats", C.c_int, [C.c_void_p, _ip, _ip, _dp, _ip]),
     ("msmgb_set_outer_skin", C.c_int, [C.c_void_p, C.c_double]),
+    ("msmgb_set_boxshape", C.c_int, [C.c_void_p, C.c_int, _dp]),
     ("msmgb_rebuild_counts", C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     ("msmgb_time_rebuilds", C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
     ("msmgb_get_tuning", C.c_int, [C.c_void_p, _ip, C.POINTER(C.c_float)]),

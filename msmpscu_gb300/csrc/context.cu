@@ -387,6 +387,14 @@ static int poll_flags(msmgb_ctx *c)
     return MSMGB_OK;
 }
 
+// a state with a non-cubic box supports the FP64 static calls only
+static int need_cubic(msmgb_ctx *c, const char *what)
+{
+    if (!c->any_shaped) return MSMGB_OK;
+    return set_err(c, MSMGB_ERR_ARG, std::string(what) + " needs cubic boxes (a BOXSHAPE is set; the FP64 "
+                                                         "force, energy, virial and stress calls support it)");
+}
+
 // ---- force table ----------------------------------------------------------------------------
 extern "C" int msmgb_init_forcetable(msmgb_ctx *c, const msmgb_forcetable *ft)
 {
@@ -580,9 +588,35 @@ extern "C" int msmgb_copyin_simbox(msmgb_ctx *c, int nbox, const msmgb_box *boxe
     const double bin_rc = c->p.rc_nl + (c->outer_skin > 0.0 ? c->outer_skin : 0.0);
     std::vector<int> boxid((size_t)n);
     int cells = 0, atom0 = 0;
+    bool any_shaped = false;
     for (int b = 0; b < nbox; ++b) {
         DevBox &d = hb[(size_t)b];
         memset(&d, 0, sizeof(d));
+        // BOXSHAPE (identity unless msmgb_set_boxshape gave one): a stencil cell must span
+        // rc_nl after the shape, i.e. rc_nl * |row k of BOXSHAPE^-1| along box direction k
+        double nrm[3] = {1.0, 1.0, 1.0};
+        {
+            double m[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+            if ((size_t)(b + 1) * 9 <= c->shapes.size()) memcpy(m, &c->shapes[(size_t)b * 9], sizeof(m));
+            memcpy(d.bs, m, sizeof(m));
+            d.shaped = 0;
+            for (int q = 0; q < 9; ++q)
+                if (m[q] != ((q % 4 == 0) ? 1.0 : 0.0)) d.shaped = 1;
+            if (d.shaped) {
+                const double det = m[0] * (m[4] * m[8] - m[5] * m[7]) - m[1] * (m[3] * m[8] - m[5] * m[6]) +
+                                   m[2] * (m[3] * m[7] - m[4] * m[6]);
+                if (!(fabs(det) > 1e-12)) return set_err(c, MSMGB_ERR_ARG, "BOXSHAPE is singular");
+                const double inv[9] = {(m[4] * m[8] - m[5] * m[7]) / det, (m[2] * m[7] - m[1] * m[8]) / det,
+                                       (m[1] * m[5] - m[2] * m[4]) / det, (m[5] * m[6] - m[3] * m[8]) / det,
+                                       (m[0] * m[8] - m[2] * m[6]) / det, (m[2] * m[3] - m[0] * m[5]) / det,
+                                       (m[3] * m[7] - m[4] * m[6]) / det, (m[1] * m[6] - m[0] * m[7]) / det,
+                                       (m[0] * m[4] - m[1] * m[3]) / det};
+                for (int k = 0; k < 3; ++k)
+                    nrm[k] = sqrt(inv[3 * k] * inv[3 * k] + inv[3 * k + 1] * inv[3 * k + 1] +
+                                  inv[3 * k + 2] * inv[3 * k + 2]);
+                any_shaped = true;
+            }
+        }
         for (int k = 0; k < 3; ++k) {
             d.lo[k] = boxes[b].lo[k];
             d.len[k] = boxes[b].len[k];
@@ -599,7 +633,7 @@ extern "C" int msmgb_copyin_simbox(msmgb_ctx *c, int nbox, const msmgb_box *boxe
                 return set_err(c, MSMGB_ERR_BOX_TOO_SMALL, "periodic box edge must exceed twice the list cutoff");
             // MD_NeighborsList_GPU.F90:289-292 with the cell size rc_nl, or rc_nl + the outer
             // skin for a two-level list (the candidates must lie in the 27-cell stencil)
-            int nc = (int)(d.len[k] / bin_rc - 0.0001);
+            int nc = (int)(d.len[k] / ((d.shaped ? c->p.rc_nl : bin_rc) * nrm[k]) - 0.0001);
             d.nc[k] = nc < 3 ? 3 : nc;
         }
         {   // |lo_i - lo_j| <= ulp(2L) (u in [L, 2L]) and |L - float(L)| <= ulp(L)/2
@@ -627,6 +661,7 @@ extern "C" int msmgb_copyin_simbox(msmgb_ctx *c, int nbox, const msmgb_box *boxe
         std::vector<double> gl = {(double)n, (double)nbox, bin_rc, (double)cells};
         for (int b = 0; b < nbox; ++b) {
             gl.push_back((double)boxes[b].natom);
+            for (int q = 0; q < 9; ++q) gl.push_back(hb[(size_t)b].bs[q]);
             for (int k = 0; k < 3; ++k) {
                 gl.push_back(boxes[b].lo[k]);
                 gl.push_back(boxes[b].len[k]);
@@ -696,6 +731,7 @@ extern "C" int msmgb_copyin_simbox(msmgb_ctx *c, int nbox, const msmgb_box *boxe
     }
     c->ncell_total = cells;
     c->bin_rc = bin_rc;
+    c->any_shaped = any_shaped;
     c->max_density = 0.0;
     for (int b = 0; b < nbox; ++b)
         c->max_density = std::max(c->max_density, boxes[b].natom / (boxes[b].len[0] * boxes[b].len[1] * boxes[b].len[2]));
@@ -823,6 +859,7 @@ extern "C" int msmgb_update_positions(msmgb_ctx *c, const double *xp)
     memcpy(&d2, &md, sizeof(d2));
     const double thr = c->p.skin_trigger > 0.0 ? c->p.skin_trigger : 0.0;
     if (!(d2 <= thr * thr)) c->list_valid = false;   // moved beyond the skin: rebuild at the next call
+    if (c->any_shaped) c->list_valid = false;         // the skin test is in box units: always rebuild
     CK(cudaMemsetAsync(c->maxdisp, 0, sizeof(unsigned long long), c->stream), "flag clear");
     c->force_valid = false;
     return MSMGB_OK;
@@ -947,6 +984,7 @@ static int ready_for_force(msmgb_ctx *c)
 
 static int force_passes(msmgb_ctx *c, bool virial, bool epot)
 {
+    if (c->p.precision != MSMGB_PREC_FP64 && !virial && !epot) RET(need_cubic(c, "a reduced-precision force pass"));
     if (c->p.precision == MSMGB_PREC_MIXED && !virial && !epot) {
         if (c->tuned_n != c->n) {
             cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
@@ -1034,6 +1072,7 @@ extern "C" int msmgb_predictor(msmgb_ctx *c, double h)
 {
     NvtxRange nvtx_range("msmgb_predictor");
     if (!c) return MSMGB_ERR_ARG;
+    RET(need_cubic(c, "the integrator"));
     RET(need_state(c));
     if (!c->have_masses) return set_err(c, MSMGB_ERR_ARG, "no masses: call msmgb_set_masses");
     RET(use_device(c));
@@ -1046,6 +1085,7 @@ extern "C" int msmgb_correction(msmgb_ctx *c, double h)
 {
     NvtxRange nvtx_range("msmgb_correction");
     if (!c) return MSMGB_ERR_ARG;
+    RET(need_cubic(c, "the integrator"));
     RET(need_state(c));
     if (!c->have_masses) return set_err(c, MSMGB_ERR_ARG, "no masses: call msmgb_set_masses");
     RET(use_device(c));
@@ -1367,6 +1407,7 @@ extern "C" int msmgb_run_steps(msmgb_ctx *c, int nsteps, double h, int *rebuilds
 {
     NvtxRange nvtx_range("msmgb_run_steps");
     if (!c || nsteps < 0) return MSMGB_ERR_ARG;
+    RET(need_cubic(c, "MD"));
     if (!c->have_masses) return set_err(c, MSMGB_ERR_ARG, "no masses: call msmgb_set_masses");
     RET(ready_for_force(c));
     if (!c->force_valid) {
@@ -1392,6 +1433,7 @@ extern "C" int msmgb_enqueue_steps(msmgb_ctx *c, int nsteps, double h)
 {
     NvtxRange nvtx_range("msmgb_enqueue_steps");
     if (!c || nsteps < 0) return MSMGB_ERR_ARG;
+    RET(need_cubic(c, "MD"));
     if (!c->have_masses) return set_err(c, MSMGB_ERR_ARG, "no masses: call msmgb_set_masses");
     RET(ready_for_force(c));
     if (!c->force_valid) {
@@ -1430,6 +1472,7 @@ extern "C" int msmgb_hvp(msmgb_ctx *c, const double *v, double *hv)
 {
     NvtxRange nvtx_range("msmgb_hvp");
     if (!c || !v || !hv) return MSMGB_ERR_ARG;
+    RET(need_cubic(c, "the Hessian-vector product"));
     RET(ready_for_force(c));
     RET(ensure_hvp_pair(c));
     const int n = c->n;
@@ -1455,6 +1498,7 @@ extern "C" int msmgb_param_adjoint(msmgb_ctx *c, int pot, const double *prm, con
 {
     NvtxRange nvtx_range("msmgb_param_adjoint");
     if (!c || !prm || !ft || !grad) return MSMGB_ERR_ARG;
+    RET(need_cubic(c, "the parameter adjoint"));
     if (pot != MSMGB_POT_CR) return set_err(c, MSMGB_ERR_ARG, "the adjoint supports the Cleri-Rosato parameters");
     RET(ready_for_force(c));
     if (c->tab.pottype != MSMGB_FS_TYPE || c->tab.nkind != 1 || c->tab.ngroup != 1)
@@ -1503,6 +1547,7 @@ extern "C" int msmgb_param_adjoint(msmgb_ctx *c, int pot, const double *prm, con
 extern "C" int msmgb_time_steps(msmgb_ctx *c, int nsteps, double h, float *ms, int *rebuilds)
 {
     if (!c || !ms || nsteps < 1) return MSMGB_ERR_ARG;
+    RET(need_cubic(c, "MD"));
     RET(msmgb_enqueue_steps(c, 0, h));           // list, forces and the step graph are ready
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0), "event");
@@ -1618,6 +1663,7 @@ extern "C" int msmgb_tile_stats(msmgb_ctx *c, int *blocks, int *tiled, double *m
 extern "C" int msmgb_time_hvp(msmgb_ctx *c, const double *v, int reps, float *ms_hvp, float *ms_force)
 {
     if (!c || !v || !ms_hvp || !ms_force || reps < 1) return MSMGB_ERR_ARG;
+    RET(need_cubic(c, "the Hessian-vector product"));
     RET(ready_for_force(c));
     RET(ensure_hvp_pair(c));
     const int n = c->n;
@@ -1714,6 +1760,21 @@ extern "C" int msmgb_set_outer_skin(msmgb_ctx *c, double skin)
         free_graph(c);
         c->list_valid = false;        // the next list build is a full one (candidates included)
     }
+    return MSMGB_OK;
+}
+
+extern "C" int msmgb_set_boxshape(msmgb_ctx *c, int ibox, const double *bs)
+{
+    if (!c || !bs || ibox < 0 || ibox >= c->cap_boxes) return MSMGB_ERR_ARG;
+    for (int q = 0; q < 9; ++q)
+        if (!std::isfinite(bs[q])) return set_err(c, MSMGB_ERR_ARG, "BOXSHAPE must be finite");
+    if (c->shapes.size() < (size_t)c->cap_boxes * 9) {
+        const size_t old = c->shapes.size() / 9;
+        c->shapes.resize((size_t)c->cap_boxes * 9, 0.0);
+        for (size_t b = old; b < (size_t)c->cap_boxes; ++b)
+            c->shapes[b * 9] = c->shapes[b * 9 + 4] = c->shapes[b * 9 + 8] = 1.0;
+    }
+    memcpy(&c->shapes[(size_t)ibox * 9], bs, sizeof(double) * 9);
     return MSMGB_OK;
 }
 

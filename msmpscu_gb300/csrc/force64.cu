@@ -81,6 +81,7 @@ __global__ void __launch_bounds__(kBlock) k_density64(DevAtoms a, DevTables t)
         double sx = mi(p.x - q.x, lx, hx, px);
         double sy = mi(p.y - q.y, ly, hy, py);
         double sz = mi(p.z - q.z, lz, hz, pz);
+        shape_sep(b, sx, sy, sz);
         double r2 = sx * sx + sy * sy + sz * sz;
         if (r2 <= t.ru2) {
             int k = pair_kind<MULTI>(t, ti, MULTI ? a.ityp[j] - 1 : 0);
@@ -151,6 +152,7 @@ __global__ void __launch_bounds__(kBlock) k_force64(DevAtoms a, DevTables t)
             double sx = mi(p.x - q.x, lx, hx, px);
             double sy = mi(p.y - q.y, ly, hy, py);
             double sz = mi(p.z - q.z, lz, hz, pz);
+            shape_sep(b, sx, sy, sz);
             double r2 = sx * sx + sy * sy + sz * sz;
             if (r2 <= t.ru2) {
                 int tj = MULTI ? a.ityp[j] - 1 : 0;
@@ -209,6 +211,7 @@ __global__ void __launch_bounds__(kBlock) k_stress64(DevAtoms a, DevTables t, in
             s[0] = mi(pi.x - q.x, b.len[0], b.half[0], b.ifpd[0]);
             s[1] = mi(pi.y - q.y, b.len[1], b.half[1], b.ifpd[1]);
             s[2] = mi(pi.z - q.z, b.len[2], b.half[2], b.ifpd[2]);
+            shape_sep(b, s[0], s[1], s[2]);
             const double r2 = s[0] * s[0] + s[1] * s[1] + s[2] * s[2];
             if (r2 > t.ru2) continue;
             const int tj = MULTI ? a.ityp[j] - 1 : 0;

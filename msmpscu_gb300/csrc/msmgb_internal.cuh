@@ -100,6 +100,8 @@ struct DevBox {
     float dlmax;         // bound on the low part of a float-float separation component
     float fxq;           // float-float passes: quantum of the integer remainders (power of 2)
     double fxinv;        // 1 / fxq
+    double bs[9];        // BOXSHAPE(K, 1:3) in row K: separations in length units are bs . SEP
+    int shaped;          // bs is not the identity (FP64 static calls only)
     int lq[3];           // (L - float(L)) / fxq, exact
     int ifpd[3];
     int nc[3];
@@ -192,6 +194,17 @@ __device__ __forceinline__ PosFF make_posff(double x, double y, double z, const 
     p.d = 0.0f;
     p.lw = 0.0f;
     return p;
+}
+
+// non-cubic box: DXYZ(K) = sum(BOXSHAPE(K,1:3)*SEP(1:3)) after the minimum image
+// (MD_FS_ForceTable.F90:235,333; MD_NeighborsList.F90:362-364)
+__device__ __forceinline__ void shape_sep(const DevBox &b, double &sx, double &sy, double &sz)
+{
+    if (!b.shaped) return;
+    const double x = sx, y = sy, z = sz;
+    sx = b.bs[0] * x + b.bs[1] * y + b.bs[2] * z;
+    sy = b.bs[3] * x + b.bs[4] * y + b.bs[5] * z;
+    sz = b.bs[6] * x + b.bs[7] * y + b.bs[8] * z;
 }
 
 __device__ __forceinline__ float mi32f(float s, float len, float half, int pd)
@@ -320,6 +333,8 @@ struct msmgb_ctx {
     int mxo = 0;                  // candidate slots per atom
     int *cand = nullptr;          // candidates, ELL layout [mxo][ld]
     int *kcand = nullptr;         // candidates per atom
+    std::vector<double> shapes;   // BOXSHAPE per box (9 each), applied at the next copy-in
+    bool any_shaped = false;      // a box of the current state is not cubic
     bool graphs_stale = false;    // a buffer the step graphs hold was reallocated
     bool cell_row_order = false;  // MSMGB_CELL_ORDER=row: x-fastest cell storage instead
     bool check_lists = false;     // MSMGB_CHECK_LISTS=1: validate every list after its build

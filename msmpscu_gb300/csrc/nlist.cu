@@ -319,6 +319,61 @@ __global__ void __launch_bounds__(kBlock, 6) k_build(DevAtoms a, const int *cell
     atomicMax(&a.flags[kFlagMaxK], nn);
 }
 
+// A state with a non-cubic box: every candidate by the FP64 rule on BOXSHAPE . SEP (cubic
+// boxes of the same state take the same path); cells were sized so that the stencil covers
+// rc_nl after the shape.  No two-level list.
+__global__ void __launch_bounds__(kBlock) k_build_shaped(DevAtoms a, const int *cell_of, const int *rank,
+                                                         const int *start, double rc2)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    if (a.statu[i] & MSMGB_STATU_OUTOFBOX) { a.kvois[i] = 0; return; }
+    const DevBox &b = a.box[a.boxid[i]];
+    int nc[3], pd[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        nc[k] = b.nc[k];
+        pd[k] = b.ifpd[k];
+    }
+    const int cell0 = b.cell0;
+    const int c = cell_of[i] - cell0;
+    const int ix = c % nc[0], iy = (c / nc[0]) % nc[1], iz = c / (nc[0] * nc[1]);
+    int nn = 0;
+    const size_t ld = (size_t)a.ld;
+    const int mxk = a.mxk;
+    int *const indi = a.indi + i;
+    const double4_32a p = a.pos[i];
+    for (int s = 0; s < 27; ++s) {
+        int j3[3] = {ix + c_nix[s], iy + c_niy[s], iz + c_niz[s]};
+        bool skip = false;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            if (pd[k]) j3[k] = (j3[k] + nc[k]) % nc[k];
+            else if (j3[k] < 0 || j3[k] >= nc[k]) skip = true;
+        }
+        if (skip) continue;
+        const int g = rank[cell0 + j3[0] + nc[0] * (j3[1] + nc[1] * j3[2])];
+        const int j0 = start[g], e = start[g + 1];
+        for (int j = j0; j < e; ++j) {
+            const double4_32a q = a.pos[j];
+            double dx = mi64(p.x - q.x, b.len[0], b.half[0], b.ifpd[0]);
+            double dy = mi64(p.y - q.y, b.len[1], b.half[1], b.ifpd[1]);
+            double dz = mi64(p.z - q.z, b.len[2], b.half[2], b.ifpd[2]);
+            shape_sep(b, dx, dy, dz);
+            if (j != i && dx * dx + dy * dy + dz * dz < rc2) {
+                if (nn < mxk) indi[(size_t)nn * ld] = j;
+                ++nn;
+            }
+        }
+    }
+    if (nn > mxk) {
+        atomicOr(&a.flags[kFlagErr], kErrOverflow);
+        nn = mxk;
+    }
+    a.kvois[i] = nn;
+    atomicMax(&a.flags[kFlagMaxK], nn);
+}
+
 // ---- two-level list -----------------------------------------------------------------------
 // With an outer skin s_o > 0 a full rebuild (binning, sort, permutation) stores, per atom, the
 // candidates within rc_nl + s_o (k_build_cand, FP32 test with the prefilter margin: a superset
@@ -677,7 +732,7 @@ static void prefilter_band(const msmgb_ctx *c, double rc2, float *lo, float *hi)
 
 bool two_level(const msmgb_ctx *c)
 {
-    return c->outer_skin > 0.0 && c->bin_rc >= c->p.rc_nl + c->outer_skin;
+    return c->outer_skin > 0.0 && c->bin_rc >= c->p.rc_nl + c->outer_skin && !c->any_shaped;
 }
 
 static int ensure_candidates(msmgb_ctx *c, int need = 0)
@@ -745,6 +800,9 @@ int build_full(msmgb_ctx *c)
         prefilter_band(c, ro * ro, &d2lo, &d2hi);
         k_build_cand<<<nblk(n, kBlock), kBlock, 0, s>>>(a, c->cell_of, c->cell_rank, c->cell_start, c->cand,
                                                         c->kcand, c->mxo, d2hi, ro * ro);
+    } else if (c->any_shaped) {
+        k_build_shaped<<<nblk(n, kBlock), kBlock, 0, s>>>(a, c->cell_of, c->cell_rank, c->cell_start,
+                                                          c->p.rc_nl * c->p.rc_nl);
     } else {
         double rc2 = c->p.rc_nl * c->p.rc_nl;
         float d2lo, d2hi;

@@ -591,6 +591,12 @@ class Engine:
         codes = (C.c_int * 3)(density, force, fused)
         self._ck(self.lib.msmgb_set_tuning(self.ctx, codes))
 
+    def set_boxshape(self, ibox, shape):
+        """BOXSHAPE (3x3, row K maps SEP to the K-th length component) of box ibox; applies
+        from the next copyin.  Non-cubic states support the FP64 static calls only."""
+        bs = np.ascontiguousarray(np.asarray(shape, np.float64).reshape(9))
+        self._ck(self.lib.msmgb_set_boxshape(self.ctx, int(ibox), _d(bs)))
+
     def set_outer_skin(self, skin):
         """Outer skin of the two-level list (0: off); applies from the next copyin."""
         self._ck(self.lib.msmgb_set_outer_skin(self.ctx, float(skin)))

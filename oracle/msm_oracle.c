@@ -749,6 +749,17 @@ static inline double slope(const double *T, int nkind, int ntab, int k, int kk)
     return tab(T, nkind, ntab, k, kk + 1) - tab(T, nkind, ntab, k, kk);
 }
 
+/* non-cubic box: DXYZ(K) = sum(BOXSHAPE(K,1:3)*SEP(1:3)), MD_FS_ForceTable.F90:235,333 and
+   MD_NeighborsList.F90:362-364 (the Fortran sum adds left to right) */
+static inline void shape_sep(const orc_box *b, double *sx, double *sy, double *sz)
+{
+    if (!b->shaped) return;
+    const double x = *sx, y = *sy, z = *sz;
+    *sx = b->bs[0] * x + b->bs[1] * y + b->bs[2] * z;
+    *sy = b->bs[3] * x + b->bs[4] * y + b->bs[5] * z;
+    *sz = b->bs[6] * x + b->bs[7] * y + b->bs[8] * z;
+}
+
 /* minimum image, MD_FS_ForceTable_GPU.F90:464-476 */
 static inline double min_image(double s, double len, double half, int pd)
 {
@@ -769,6 +780,10 @@ int orc_nlist(int n, const double *x, const double *y, const double *z, const in
 {
     const double eps = 0.0001;
     int nc[3];
+    if (box->shaped) {   /* cells of rc_nl in box units need not cover rc_nl after the shape */
+        if (ncell3) ncell3[0] = ncell3[1] = ncell3[2] = 0;
+        return orc_nlist_brute(n, x, y, z, statu, box, rc_nl, mxkvois, kvois, indi);
+    }
     for (int k = 0; k < 3; ++k) {
         nc[k] = (int)(box->len[k] / (1.0 * rc_nl) - eps);   /* :476 */
         if (nc[k] < 3) nc[k] = 3;                            /* :478, C_ITHR */
@@ -869,11 +884,11 @@ int orc_nlist_brute(int n, const double *x, const double *y, const double *z, co
         if (!(statu[i] & ORC_STATU_OUTOFBOX)) {
             for (int j = 0; j < n; ++j) {
                 if (j == i || (statu[j] & ORC_STATU_OUTOFBOX)) continue;
-                double d2 = 0.0;
-                for (int k = 0; k < 3; ++k) {
-                    double s = min_image(xp[k][i] - xp[k][j], box->len[k], half[k], box->ifpd[k]);
-                    d2 += s * s;
-                }
+                double sv[3];
+                for (int k = 0; k < 3; ++k)
+                    sv[k] = min_image(xp[k][i] - xp[k][j], box->len[k], half[k], box->ifpd[k]);
+                shape_sep(box, &sv[0], &sv[1], &sv[2]);
+                const double d2 = sv[0] * sv[0] + sv[1] * sv[1] + sv[2] * sv[2];
                 if (d2 < rc2) {
                     if (nn >= mxkvois) { overflow = 1; break; }
                     indi[(size_t)nn * (size_t)n + (size_t)i] = j;
@@ -934,6 +949,7 @@ int orc_force(int n, const double *x, const double *y, const double *z, const in
                 double sepx = min_image(posx - x[j], bx, hbx, px);
                 double sepy = min_image(posy - y[j], by, hby, py);
                 double sepz = min_image(posz - z[j], bz, hbz, pz);
+                shape_sep(box, &sepx, &sepy, &sepz);
                 double r2 = sepx * sepx + sepy * sepy + sepz * sepz;
                 if (r2 <= t->ru2) {
                     int ktab = t->kpair[(ityp[j] - 1) * ng + (ityi - 1)] - 1;
@@ -979,6 +995,7 @@ int orc_force(int n, const double *x, const double *y, const double *z, const in
                     double sepx = min_image(posx - x[j], bx, hbx, px);
                     double sepy = min_image(posy - y[j], by, hby, py);
                     double sepz = min_image(posz - z[j], bz, hbz, pz);
+                    shape_sep(box, &sepx, &sepy, &sepz);
                     double r2 = sepx * sepx + sepy * sepy + sepz * sepz;
                     if (r2 <= t->ru2) {
                         int ityj = ityp[j];
@@ -1151,6 +1168,7 @@ void orc_atomic_stress(int n, const double *x, const double *y, const double *z,
                 s[0] = min_image(x[ic] - x[j], bx, 0.5 * bx, px);
                 s[1] = min_image(y[ic] - y[j], by, 0.5 * by, py);
                 s[2] = min_image(z[ic] - z[j], bz, 0.5 * bz, pz);
+                shape_sep(box, &s[0], &s[1], &s[2]);
                 double r2 = s[0] * s[0] + s[1] * s[1] + s[2] * s[2];
                 if (r2 > t->ru2) continue;
                 int ityj = ityp[j];

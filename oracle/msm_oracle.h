@@ -74,6 +74,8 @@ typedef struct {
     double lo[3];
     double len[3];
     int ifpd[3];
+    int shaped;           /* nonzero: separations are BOXSHAPE . SEP (MD_FS_ForceTable.F90:235,333) */
+    double bs[9];         /* BOXSHAPE(K, 1:3) in row K */
 } orc_box;
 
 /* potential functions: value and -derivative in the reference's conventions */

@@ -34,7 +34,8 @@ class OrcTables(C.Structure):
 
 
 class OrcBox(C.Structure):
-    _fields_ = [("lo", C.c_double * 3), ("len", C.c_double * 3), ("ifpd", C.c_int * 3)]
+    _fields_ = [("lo", C.c_double * 3), ("len", C.c_double * 3), ("ifpd", C.c_int * 3),
+                ("shaped", C.c_int), ("bs", C.c_double * 9)]
 
 
 _lib = None
@@ -390,12 +391,17 @@ def moldy_tables(d, rmax, ntab=10000, nembd=10000, rhoscal=20.0):
                 dfembd=np.where(q > 0.0, -0.5 / np.sqrt(safe), 0.0))
 
 
-def make_box(lo, length, ifpd=(1, 1, 1)):
+def make_box(lo, length, ifpd=(1, 1, 1), shape=None):
+    """shape: BOXSHAPE as a 3x3 array (row K maps SEP to DXYZ(K)); None = cubic."""
     b = OrcBox()
     for k in range(3):
         b.lo[k] = float(lo[k])
         b.len[k] = float(length[k])
         b.ifpd[k] = int(ifpd[k])
+    bs = np.eye(3) if shape is None else np.asarray(shape, np.float64).reshape(3, 3)
+    for m in range(9):
+        b.bs[m] = float(bs.reshape(-1)[m])
+    b.shaped = 0 if shape is None or np.array_equal(bs, np.eye(3)) else 1
     return b
 
 
