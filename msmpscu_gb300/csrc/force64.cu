@@ -55,7 +55,7 @@ __device__ __forceinline__ double embed_lookup(const double *__restrict__ T, int
     return a + (sk - kk) * (b - a);
 }
 
-template <int POT, bool MULTI, bool EPOT>
+template <int POT, bool MULTI, bool EPOT, bool SHAPED = false>
 __global__ void __launch_bounds__(kBlock) k_density64(DevAtoms a, DevTables t)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -81,7 +81,7 @@ __global__ void __launch_bounds__(kBlock) k_density64(DevAtoms a, DevTables t)
         double sx = mi(p.x - q.x, lx, hx, px);
         double sy = mi(p.y - q.y, ly, hy, py);
         double sz = mi(p.z - q.z, lz, hz, pz);
-        shape_sep(b, sx, sy, sz);
+        if (SHAPED) shape_sep(b, sx, sy, sz);   // a state with a non-cubic box
         double r2 = sx * sx + sy * sy + sz * sz;
         if (r2 <= t.ru2) {
             int k = pair_kind<MULTI>(t, ti, MULTI ? a.ityp[j] - 1 : 0);
@@ -127,7 +127,7 @@ __device__ __forceinline__ void virial_flush(DevAtoms &a, int box, double v[6])
     }
 }
 
-template <int POT, bool MULTI, bool VIRIAL>
+template <int POT, bool MULTI, bool VIRIAL, bool SHAPED = false>
 __global__ void __launch_bounds__(kBlock) k_force64(DevAtoms a, DevTables t)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -152,7 +152,7 @@ __global__ void __launch_bounds__(kBlock) k_force64(DevAtoms a, DevTables t)
             double sx = mi(p.x - q.x, lx, hx, px);
             double sy = mi(p.y - q.y, ly, hy, py);
             double sz = mi(p.z - q.z, lz, hz, pz);
-            shape_sep(b, sx, sy, sz);
+            if (SHAPED) shape_sep(b, sx, sy, sz);   // a state with a non-cubic box
             double r2 = sx * sx + sy * sy + sz * sz;
             if (r2 <= t.ru2) {
                 int tj = MULTI ? a.ityp[j] - 1 : 0;
@@ -191,7 +191,7 @@ __global__ void __launch_bounds__(kBlock) k_force64(DevAtoms a, DevTables t)
 // Per-atom virial tensor from the F'(rho) of the last FP64 density pass.  ap holds 9 slabs
 // of n doubles (component 3a+b, the reference's AP(NAPDEV, 9)); atom i goes to row gid[i]
 // (caller order) or i (sorted order).
-template <bool MULTI>
+template <bool MULTI, bool SHAPED = false>
 __global__ void __launch_bounds__(kBlock) k_stress64(DevAtoms a, DevTables t, int sorted, double *ap)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -211,7 +211,7 @@ __global__ void __launch_bounds__(kBlock) k_stress64(DevAtoms a, DevTables t, in
             s[0] = mi(pi.x - q.x, b.len[0], b.half[0], b.ifpd[0]);
             s[1] = mi(pi.y - q.y, b.len[1], b.half[1], b.ifpd[1]);
             s[2] = mi(pi.z - q.z, b.len[2], b.half[2], b.ifpd[2]);
-            shape_sep(b, s[0], s[1], s[2]);
+            if (SHAPED) shape_sep(b, s[0], s[1], s[2]);
             const double r2 = s[0] * s[0] + s[1] * s[1] + s[2] * s[2];
             if (r2 > t.ru2) continue;
             const int tj = MULTI ? a.ityp[j] - 1 : 0;
@@ -242,16 +242,26 @@ template <int POT, bool MULTI>
 static void dens_dispatch(msmgb_ctx *c, bool epot)
 {
     const int bs = block_for(c->n), g = nblk(c->n, bs);
-    if (epot) k_density64<POT, MULTI, true><<<g, bs, 0, c->stream>>>(c->a, c->tab);
-    else k_density64<POT, MULTI, false><<<g, bs, 0, c->stream>>>(c->a, c->tab);
+    if (c->any_shaped) {
+        if (epot) k_density64<POT, MULTI, true, true><<<g, bs, 0, c->stream>>>(c->a, c->tab);
+        else k_density64<POT, MULTI, false, true><<<g, bs, 0, c->stream>>>(c->a, c->tab);
+    } else {
+        if (epot) k_density64<POT, MULTI, true><<<g, bs, 0, c->stream>>>(c->a, c->tab);
+        else k_density64<POT, MULTI, false><<<g, bs, 0, c->stream>>>(c->a, c->tab);
+    }
 }
 
 template <int POT, bool MULTI>
 static void force_dispatch(msmgb_ctx *c, bool vir)
 {
     const int bs = block_for(c->n), g = nblk(c->n, bs);
-    if (vir) k_force64<POT, MULTI, true><<<g, bs, 0, c->stream>>>(c->a, c->tab);
-    else k_force64<POT, MULTI, false><<<g, bs, 0, c->stream>>>(c->a, c->tab);
+    if (c->any_shaped) {
+        if (vir) k_force64<POT, MULTI, true, true><<<g, bs, 0, c->stream>>>(c->a, c->tab);
+        else k_force64<POT, MULTI, false, true><<<g, bs, 0, c->stream>>>(c->a, c->tab);
+    } else {
+        if (vir) k_force64<POT, MULTI, true><<<g, bs, 0, c->stream>>>(c->a, c->tab);
+        else k_force64<POT, MULTI, false><<<g, bs, 0, c->stream>>>(c->a, c->tab);
+    }
 }
 
 int launch_density(msmgb_ctx *c, bool want_epot)
@@ -272,8 +282,13 @@ int launch_density(msmgb_ctx *c, bool want_epot)
 int launch_stress(msmgb_ctx *c, int sorted, double *ap)
 {
     const int bs = block_for(c->n), g = nblk(c->n, bs);
-    if (c->tab.ngroup > 1) k_stress64<true><<<g, bs, 0, c->stream>>>(c->a, c->tab, sorted, ap);
-    else k_stress64<false><<<g, bs, 0, c->stream>>>(c->a, c->tab, sorted, ap);
+    if (c->any_shaped) {
+        if (c->tab.ngroup > 1) k_stress64<true, true><<<g, bs, 0, c->stream>>>(c->a, c->tab, sorted, ap);
+        else k_stress64<false, true><<<g, bs, 0, c->stream>>>(c->a, c->tab, sorted, ap);
+    } else {
+        if (c->tab.ngroup > 1) k_stress64<true><<<g, bs, 0, c->stream>>>(c->a, c->tab, sorted, ap);
+        else k_stress64<false><<<g, bs, 0, c->stream>>>(c->a, c->tab, sorted, ap);
+    }
     c->launches += 1;
     return check_launch(c, "atomic stress pass");
 }
