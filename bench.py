@@ -271,6 +271,33 @@ def make_engine(n, precision, device=0, outer_skin=None):
     return e
 
 
+def steady_state(pos, vel, L, steps=1000, device=0):
+    """The whole 1,000-step NVE run of the 2,048,000-atom Cu workload in each precision, from
+    the copied-in state (list built at the copy-in), timed with CUDA events over all steps:
+    atom-steps/s, list rebuilds inside the run (all and full ones) and the whole-step roofline
+    of the run.  The mixed/FP64 and float-float/FP64 ratios come from these same runs."""
+    n = len(pos)
+    box = [(n, (0, 0, 0), tuple(L), (1, 1, 1))]
+    hbm, _ = peaks()
+    out = {"steps": steps}
+    for prec in ("mixed", "ff", "fp64"):
+        e = make_engine(n, prec, device)
+        e.copyin(box, pos, vel)
+        rc0 = e.rebuild_counts()        # the list, first forces, tuning and graphs: untimed
+        ms, reb = e.time_steps(steps, DT)
+        rc1 = e.rebuild_counts()
+        _, kmean = e.list_stats()
+        v = n * steps / (ms / 1e3)
+        b = bytes_model(kmean)["step"]
+        out[prec] = {"value": v, "ms_per_step": ms / steps, "rebuilds": rc1[0] - rc0[0],
+                     "full_rebuilds": rc1[1] - rc0[1],
+                     "step_roofline_frac": b * v / 1e9 / hbm, "bytes_per_atom_step": b}
+        e.close()
+    out["mixed_vs_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
+    out["ff_vs_fp64"] = out["ff"]["value"] / out["fp64"]["value"]
+    return out
+
+
 def bytes_model(kmean):
     """Algorithmic bytes per atom and launch (design-independent): int32 list entries read
     once per pass, own FP64 position (24 B), F'(rho) write/read (8 B each), force write
@@ -428,6 +455,49 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def run_case(args):
+    """One differentiation kernel pair on its own, for a profiler capture or a quick timing:
+    `hvp` on bcc W ncell^3 cells with the <111> dumbbell (Marinica EAM2, ncell 20 = the 16,001-atom
+    case), `adjoint` on `snapshots` fcc Cu boxes of ncell^3 cells (Cleri-Rosato, sigma 0.1 A,
+    targets from the parameters x 1.02; ncell 10 and 64 snapshots = the 64 x 4,000-atom case).
+    Prints one JSON line with the device or wall times."""
+    from msmpscu_gb300 import build as lib_build
+    from msmpscu_gb300 import Engine, ForceTable, lattice as lt
+    from msmpscu_gb300 import _lib as L
+    lib_build.build()
+    if args.case == "hvp":
+        pos, box_len = lt.w_sia_config(args.ncell, 0.0, 1)
+        e = Engine(len(pos), lt.W_RC_NL, mxkvois=96)
+        e.init_forcetable(ForceTable.marinica_eam2())
+        e.copyin([(len(pos), (0, 0, 0), tuple(box_len), (1, 1, 1))], pos)
+        v = np.random.default_rng(0).normal(size=pos.shape)
+        v /= np.linalg.norm(v)
+        ms_hvp, ms_force = e.time_hvp(v, reps=args.steps)
+        e.close()
+        out = {"case": "hvp", "atoms": len(pos), "hvp_ms": ms_hvp, "force_call_ms": ms_force,
+               "hvp_cost_force_calls": ms_hvp / ms_force}
+    else:
+        snaps = [lt.cu_config(args.ncell, 0.1, 300.0, 1000 + s) for s in range(args.snapshots)]
+        pos = np.vstack([s[0] for s in snaps])
+        desc = [(len(s[0]), (0, 0, 0), tuple(s[2]), (1, 1, 1)) for s in snaps]
+        prm = np.array([lt.CU_CR[k] for k in ("A", "xi", "p", "q", "r0")])
+        e = Engine(len(pos), lt.CU_RC_NL, max_boxes=len(snaps), mxkvois=MXKVOIS)
+        e.init_forcetable(ForceTable(L.POT_CR, prm * 1.02, lt.CU_RC, lt.CU_RC, L.FS_TYPE))
+        e.copyin(desc, pos)
+        e.calforce()
+        ft = e.get_force()
+        e.init_forcetable(ForceTable(L.POT_CR, prm, lt.CU_RC, lt.CU_RC, L.FS_TYPE))
+        e.param_adjoint(prm, ft)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            e.param_adjoint(prm, ft)
+        t1 = time.perf_counter()
+        e.close()
+        out = {"case": "adjoint", "atoms": len(pos), "snapshots": len(snaps),
+               "adjoint_wall_ms": (t1 - t0) / args.steps * 1e3}
+    print(json.dumps(out), flush=True)
+
+
 def run_ours(args):
     ws, rank, local = dist_env()
     dist = None
@@ -513,6 +583,7 @@ def run_ours(args):
         extras["adjoint"] = adjoint_cu_snapshots(device)
         extras["nve_drift"] = nve_drift(device)
         extras["oracle_parity"] = oracle_parity(pos, vel, L, device)
+        extras["steady_state_1000"] = steady_state(pos, vel, L, 1000, device)
         e = None
 
     cpu = None
@@ -603,12 +674,17 @@ def main():
     ap.add_argument("--pin", default=None,
                     help="mixed passes: kernel variant codes density,force,fused instead of the tuner's")
     ap.add_argument("--cpu-steps", type=int, default=2)
+    ap.add_argument("--case", default="md", choices=["md", "hvp", "adjoint"],
+                    help="hvp / adjoint: only that differentiation call (profiling captures)")
+    ap.add_argument("--snapshots", type=int, default=64, help="--case adjoint: number of Cu boxes")
     ap.add_argument("--ref-budget-s", type=float, default=150.0)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.case != "md":
+        run_case(args)
     else:
         run_ours(args)
 

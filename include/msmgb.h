@@ -291,10 +291,14 @@ int  msmgb_cr_param_tables(const double *prm, double rmax, int ntab, double *d);
  * sits in a fixed array compiled into the library (8 MiB per GPU, held until exit), so at
  * most MSMGB_NOALLOC_MAX_ATOMS atoms can be handled (larger n returns MSMGB_ERR_CAPACITY).
  * The first call on a device, made with that device current, looks up the device address of
- * that array; make this first call before any stream capture.  All calls on a device share
+ * that array; under CUDA's lazy module loading (the default) that first call also loads the
+ * library's device code onto the device, which synchronises it, so make this first call at
+ * set-up, before any stream capture and before time-critical work.  All calls on a device share
  * the array and it keeps the last call's contents (the error word is cleared at the start of
  * every call); calls whose work overlaps on the GPU race on it, so serialise them.
  * FP64, single species (tables of kind 1), orthorhombic box; the call synchronises `stream`.
+ * INDI holds 0-based neighbour ids (the reference's INDI is 1-based: subtract 1 first); an id
+ * outside 0..n-1 is not read, its slot is skipped and the call returns MSMGB_ERR_ARG.
  * Results equal msmgb_calforce's to rounding. */
 #define MSMGB_NOALLOC_MAX_ATOMS 1048576
 typedef struct {

@@ -629,11 +629,19 @@ extern "C" int msmgb_copyin_simbox(msmgb_ctx *c, int nbox, const msmgb_box *boxe
             d.halff[k] = (float)d.half[k];
             d.ifpd[k] = boxes[b].ifpd[k] ? 1 : 0;
             if (d.len[k] <= 0.0) return set_err(c, MSMGB_ERR_ARG, "box length must be positive");
-            if (d.ifpd[k] && d.len[k] <= 2.0 * c->p.rc_nl)
-                return set_err(c, MSMGB_ERR_BOX_TOO_SMALL, "periodic box edge must exceed twice the list cutoff");
+            // a pair within rc_nl has |SEP_k| <= rc_nl * |row k of BOXSHAPE^-1| (nrm = 1 for a
+            // cubic box): the single-shift minimum image is unique only below half the edge
+            if (d.ifpd[k] && d.len[k] <= 2.0 * c->p.rc_nl * nrm[k])
+                return set_err(c, MSMGB_ERR_BOX_TOO_SMALL,
+                               d.shaped ? "periodic box edge must exceed twice the list cutoff times the norm of "
+                                          "the matching row of BOXSHAPE^-1"
+                                        : "periodic box edge must exceed twice the list cutoff");
             // MD_NeighborsList_GPU.F90:289-292 with the cell size rc_nl, or rc_nl + the outer
             // skin for a two-level list (the candidates must lie in the 27-cell stencil)
-            int nc = (int)(d.len[k] / ((d.shaped ? c->p.rc_nl : bin_rc) * nrm[k]) - 0.0001);
+            const double ncd = d.len[k] / ((d.shaped ? c->p.rc_nl : bin_rc) * nrm[k]) - 0.0001;
+            if (!(ncd < (double)(1 << 24)))      // a strongly stretching BOXSHAPE
+                return set_err(c, MSMGB_ERR_CAPACITY, "too many cells along one box edge");
+            const int nc = (int)ncd;
             d.nc[k] = nc < 3 ? 3 : nc;
         }
         {   // |lo_i - lo_j| <= ulp(2L) (u in [L, 2L]) and |L - float(L)| <= ulp(L)/2
@@ -1571,6 +1579,7 @@ extern "C" int msmgb_time_steps(msmgb_ctx *c, int nsteps, double h, float *ms, i
 extern "C" int msmgb_time_passes(msmgb_ctx *c, int reps, float *out)
 {
     if (!c || !out || reps < 1) return MSMGB_ERR_ARG;
+    RET(need_cubic(c, "pass timing"));      // it times the integrator and the step kernels
     RET(ready_for_force(c));
     if (!c->have_masses) return set_err(c, MSMGB_ERR_ARG, "no masses: call msmgb_set_masses");
     const bool mixed = c->p.precision == MSMGB_PREC_MIXED;
@@ -1783,6 +1792,7 @@ extern "C" int msmgb_set_boxshape(msmgb_ctx *c, int ibox, const double *bs)
 extern "C" int msmgb_time_rebuilds(msmgb_ctx *c, int reps, float *full_ms, float *inner_ms)
 {
     if (!c || !full_ms || !inner_ms || reps < 1) return MSMGB_ERR_ARG;
+    RET(need_cubic(c, "rebuild timing"));   // rebuilds inside MD steps need cubic boxes
     RET(ready_for_force(c));
     cudaEvent_t ev[2];
     CK(cudaEventCreate(&ev[0]), "event");

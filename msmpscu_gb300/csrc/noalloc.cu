@@ -14,7 +14,10 @@
 //
 // The host cannot use the names of those arrays as device addresses (in host code the name
 // is a host-side stand-in), so the first call on each device, with that device current,
-// looks the addresses up with cudaGetSymbolAddress and keeps them for later calls.
+// looks the addresses up with cudaGetSymbolAddress and keeps them for later calls.  Under
+// CUDA's lazy module loading (the default) that lookup is also what loads this library's
+// device code onto the device, with the synchronisation a module load implies; a caller
+// that must avoid it mid-step makes one call at set-up (a call with n = 1 will do).
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -29,7 +32,8 @@ constexpr int kMaxDevices = 64;
 
 // F'(rho) per atom, shared by every call on this device (contents persist between calls)
 static __device__ __align__(256) double g_den_scratch[kNoAllocMaxAtoms];
-// error bits of the running call (bit 0: density beyond the F(rho) table); cleared per call
+// error bits of the running call (bit 0: density beyond the F(rho) table; bit 1: a
+// neighbour id outside 0..n-1, whose slot is skipped); cleared at the start of every call
 static __device__ __align__(256) int g_err_scratch[64];
 
 struct DevScratch {
@@ -83,6 +87,10 @@ __global__ void __launch_bounds__(256) k_na_density(NaArgs a, double *den, int *
         const int kn = a.kvois[i];
         for (int w = 0; w < kn; ++w) {
             int j = __ldg(a.indi + i + (size_t)w * a.ld);
+            if ((unsigned)j >= (unsigned)a.n) {      // e.g. 1-based ids: flagged, not read
+                atomicOr(err, 2);
+                continue;
+            }
             double sx = mi(px - a.x[j], a.len[0], a.half[0], a.ifpd[0]);
             double sy = mi(py - a.y[j], a.len[1], a.half[1], a.ifpd[1]);
             double sz = mi(pz - a.z[j], a.len[2], a.half[2], a.ifpd[2]);
@@ -107,7 +115,7 @@ __global__ void __launch_bounds__(256) k_na_density(NaArgs a, double *den, int *
     den[i] = rho;
 }
 
-__global__ void __launch_bounds__(256) k_na_force(NaArgs a, const double *den)
+__global__ void __launch_bounds__(256) k_na_force(NaArgs a, const double *den, int *err)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
@@ -118,6 +126,10 @@ __global__ void __launch_bounds__(256) k_na_force(NaArgs a, const double *den)
         const int kn = a.kvois[i];
         for (int w = 0; w < kn; ++w) {
             int j = __ldg(a.indi + i + (size_t)w * a.ld);
+            if ((unsigned)j >= (unsigned)a.n) {
+                atomicOr(err, 2);
+                continue;
+            }
             double sx = mi(px - a.x[j], a.len[0], a.half[0], a.ifpd[0]);
             double sy = mi(py - a.y[j], a.len[1], a.half[1], a.ifpd[1]);
             double sz = mi(pz - a.z[j], a.len[2], a.half[2], a.ifpd[2]);
@@ -228,7 +240,7 @@ extern "C" int msmgb_calforce_noalloc(const msmgb_force_noalloc *args)
     int grid = (a.n + 255) / 256;
     if (e == cudaSuccess) {
         k_na_density<<<grid, 256, 0, st>>>(k, s->den, s->err);
-        k_na_force<<<grid, 256, 0, st>>>(k, s->den);
+        k_na_force<<<grid, 256, 0, st>>>(k, s->den, s->err);
         e = cudaGetLastError();
     }
     int herr = 0;
@@ -239,6 +251,11 @@ extern "C" int msmgb_calforce_noalloc(const msmgb_force_noalloc *args)
         snprintf(buf, sizeof(buf), "msmgb_calforce_noalloc: CUDA error %s", cudaGetErrorString(e));
         put_msg(args, buf);
         return MSMGB_ERR_CUDA;
+    }
+    if (herr & 2) {
+        put_msg(args, "msmgb_calforce_noalloc: a neighbour id in INDI lies outside 0..n-1 (the ids are "
+                      "0-based; a 1-based Fortran list must be converted first); those slots were skipped");
+        return MSMGB_ERR_ARG;
     }
     if (herr & 1) {
         put_msg(args, "msmgb_calforce_noalloc: electron density beyond the F(rho) table");

@@ -17,7 +17,10 @@ Run once in a container that has the reference mounted; the output files are com
 import os
 import sys
 
-SRC = "/root/reference/examples/use_ForceTableGen/EM_TB_WANGJUN_W-HE_2010.pair"
+# root of the reference tree: $MSMPSCU_REFERENCE, else where this container mounts it;
+# the first command-line argument overrides the whole path
+REF_ROOT = os.environ.get("MSMPSCU_REFERENCE", "/root/reference")
+SRC = os.path.join(REF_ROOT, "examples/use_ForceTableGen/EM_TB_WANGJUN_W-HE_2010.pair")
 OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "ackland_ww_pair_rows.txt")
 OUT2 = os.path.join(os.path.dirname(os.path.abspath(__file__)), "wangjun_pair_rows.txt")
 # piece boundaries (A) of tables #2-#5: He-He 1.0, 1.3; He-W 1.5778 ... 3.5, switch 4.3, 7.3;

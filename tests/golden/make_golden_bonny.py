@@ -15,7 +15,10 @@ import sys
 
 import numpy as np
 
-REF = "/root/reference/examples/use_ForceTableGen/EAM_WHeH_Bonny_JPCM26_2014.embd"
+# root of the reference tree: $MSMPSCU_REFERENCE, else where this container mounts it;
+# the first command-line argument overrides the whole path
+REF_ROOT = os.environ.get("MSMPSCU_REFERENCE", "/root/reference")
+REF = os.path.join(REF_ROOT, "examples/use_ForceTableGen/EAM_WHeH_Bonny_JPCM26_2014.embd")
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 

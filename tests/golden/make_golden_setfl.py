@@ -21,7 +21,10 @@ import sys
 
 import numpy as np
 
-REF = "/root/reference/examples/NIST_Potentials/Cu_EAM"
+# root of the reference tree: $MSMPSCU_REFERENCE, else where this container mounts it;
+# the first command-line argument overrides the whole path
+REF_ROOT = os.environ.get("MSMPSCU_REFERENCE", "/root/reference")
+REF = os.path.join(REF_ROOT, "examples/NIST_Potentials/Cu_EAM")
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 
