@@ -409,6 +409,39 @@ int  msmgb_lspt_tables(const char *path, int flags, int ntab, int nembd, double 
                        double *potr, double *fpotr, double *potb, double *fpotb, double *fembd,
                        double *dfembd, int *kpair, int *kembd, double *rhod);
 
+/* ---- tables exported by the reference and read back (Import_ForceTable,
+ *      Register_Imported_ForceTable, Export_ForceTable; MD_TypeDef_ForceTable.F90:1315-1855) ---- */
+/* Units of the tables these calls return or take: the files are in Angstrom / eV;
+ * MSMGB_UNITS_CGS applies the reference's conversions on import (:1529-1540, 1583-1585) so the
+ * tables match its CGS force table (lengths in cm, energies in erg, FS densities in erg^2). */
+#define MSMGB_UNITS_EV_A 0
+#define MSMGB_UNITS_CGS  1
+/* Header of stem.pair / stem.embd: potential type, table ids (FPAIR, up to 256) and grid
+ * sizes of both files.  Host only.  Returns MSMGB_ERR_ARG for a missing or malformed file. */
+int  msmgb_import_info(const char *stem, int *pottype, int *ntables, int *ids, int *npoint,
+                       int *nembtables, int *emb_ids, int *nembpoint);
+/* Register_Imported_ForceTable (:1612-1855) for a box of ngroup atom types whose pairs use
+ * the file tables PTYPE(NGROUP,NGROUP) (column-major, ids as in the files): the tables named
+ * are numbered by first appearance (KPAIR, KEMBD as New_ForceTable :560-574, 600-610) and
+ * re-gridded by the reference's spline (SPLID1/SPLID2 with end slopes from the four end rows,
+ * LIB/sor/f/MiniUtilities/DINTF2.F:17-240) onto the sqrt(r) grid of ntab points up to rmax
+ * (0 beyond the file's largest r) and, for EAM, onto rho = (i-1)*RHOD with RHOD = RHOMX/nembd,
+ * RHOMX = RHO(N)*N/(N-1) of the file's N embedding rows.  Outputs in the (NKIND, NTAB) /
+ * (NKIND1, NEMBD) column-major layouts of msmgb_forcetable (caller allocates ngroup^2*ntab and
+ * ngroup*nembd); kpair (ngroup^2), kembd (ngroup, EAM only), *nkind, *nkind1 (0 for FS),
+ * *rhod, *pottype.  rmax, tables and RHOD in `units`.  Host only.  MSMGB_ERR_ARG for a
+ * missing file or a PTYPE id absent from either file (the reference stops there). */
+int  msmgb_import_forcetable(const char *stem, int units, int ngroup, const int *ptype, double rmax,
+                             int ntab, int nembd, double *potr, double *fpotr, double *potb,
+                             double *fpotb, double *fembd, double *dfembd, int *kpair, int *kembd,
+                             int *nkind, int *nkind1, double *rhod, int *pottype);
+/* Export_ForceTable (:1315-1459): writes stem.pair and stem.embd in the reference's layout
+ * (rows 1PE21.9 / 1PE16.8, tables in increasing id order) from the tables of ft (in `units`);
+ * ids / emb_ids name the NKIND pair and NKIND1 embedding tables (NULL: 1, 2, ...).  An FS
+ * table gets the reference's informational embedding file (F = -sqrt(rho) on RHOD).  Host only. */
+int  msmgb_export_forcetable(const char *stem, int units, const msmgb_forcetable *ft, const int *ids,
+                             const int *emb_ids);
+
 #ifdef __cplusplus
 }
 #endif

@@ -50,6 +50,7 @@ class Box(C.Structure):
 
 
 NOALLOC_MAX_ATOMS = 1048576
+UNITS_EV_A, UNITS_CGS = 0, 1
 
 
 class ForceNoAlloc(C.Structure):
@@ -121,6 +122,10 @@ SIGNATURES = [
     ("msmgb_calforce_noalloc", C.c_int, [C.POINTER(ForceNoAlloc)]),
     ("msmgb_create_forcetable", C.c_int, [C.c_int, _dp, C.c_double, C.c_int, C.c_int, C.c_double,
                                           _dp, _dp, _dp, _dp, _dp, _dp, _dp]),
+    ("msmgb_import_info", C.c_int, [C.c_char_p, _ip, _ip, _ip, _ip, _ip, _ip, _ip]),
+    ("msmgb_import_forcetable", C.c_int, [C.c_char_p, C.c_int, C.c_int, _ip, C.c_double, C.c_int, C.c_int,
+                                          _dp, _dp, _dp, _dp, _dp, _dp, _ip, _ip, _ip, _ip, _dp, _ip]),
+    ("msmgb_export_forcetable", C.c_int, [C.c_char_p, C.c_int, C.POINTER(ForceTable), _ip, _ip]),
 ]
 
 _lib = None

@@ -11,6 +11,7 @@
 // Grid (Create_Pairwise_ForceTable :949-976): T = i*CSIV, R = T*T, CSI = NTAB/sqrt(Rmax);
 // POTR = f1(R)*R, FPOTR = f2(R)*R, POTB = rho(R), FPOTB = -rho'(R);
 // RHOMX = RHOSCAL * max POTB, RHOD = RHOMX/NEMBD; F, F' at rho = (i-1)*RHOD (:1040-1048).
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -1353,5 +1354,412 @@ extern "C" int msmgb_moldy_tables(const char *path, double rmax, int ntab, int n
         dfembd[i - 1] = rho > 0.0 ? -0.5 / std::sqrt(rho) : 0.0;
     }
     if (rhod) *rhod = d;
+    return MSMGB_OK;
+}
+
+// ---- tables exported by the reference and read back (Export_ForceTable, Import_ForceTable,
+//      Register_Imported_ForceTable; MD_TypeDef_ForceTable.F90:1315-1459, 1463-1608, 1612-1855)
+//
+// The reference runs every potential it cannot generate itself (the NIST files, and any
+// library name with no built-in generator) from a pair of text files `stem.pair` and
+// `stem.embd` (MD_ForceLib_Register.F90:405-420): a header with &POTTYPE, &NUMTABLE (the
+// table ids) and &NUMPOINT, then one row per grid point.  Pair rows: index, r [A], and per
+// table 2 r V [eV A], -r dV/dr [eV], rho (FS: eV^2), -drho/dr [/A]; embedding rows: index,
+// rho, and per table F [eV], dF/drho (CGS: erg per rho unit; FS: 1/(2 F) in 1/erg).  The
+// import re-grids every column the box needs onto the run's sqrt(r) grid (T = K CSIV, CSIV =
+// 1/CSI, CSI = NTAB/sqrt(Rmax); value 0 where T^2 exceeds the file's largest r) and the
+// embedding columns onto rho = (K-1) RHOD with RHOMX = RHO(N) N/(N-1), RHOD = RHOMX/NEMBD,
+// through SPLID1/SPLID2 (LIB/sor/f/MiniUtilities/DINTF2.F:17-240) with IOP = 5 at both ends:
+// the cubic spline through the rows whose end slopes are those of the cubic through the
+// first (last) four rows, extended beyond the end rows by the end intervals' cubics.  Here
+// that spline is computed in slope (Hermite) form: one tridiagonal solve for the knot slopes.
+namespace {
+
+const double kA2CM = 1e-8;   // MSM_Const.F90:67
+
+struct ImpFile {
+    std::string pottype;
+    std::vector<int> ids;                    // table ids (FPAIR / FPAIR1) in file order
+    int npt = 0;
+    std::vector<double> x;                   // r or rho per row
+    std::vector<std::vector<double>> col;    // [table * ncol + c][row]
+};
+
+std::string upcase(std::string s)
+{
+    for (char &ch : s) ch = (char)toupper((unsigned char)ch);
+    return s;
+}
+
+// header keywords of Import_ForceTable (:1485-1512) and the rows after "&#"
+int read_imported(const char *path, int ncol, ImpFile &f, std::string &why)
+{
+    FILE *fh = fopen(path, "r");
+    if (!fh) {
+        why = std::string("cannot open ") + path;
+        return MSMGB_ERR_ARG;
+    }
+    char buf[65536];
+    bool header_done = false;
+    int nc = -1;
+    while (fgets(buf, sizeof(buf), fh)) {
+        std::string s = trim(buf);
+        if (s.empty() || s[0] == '!') continue;
+        if (s[0] != '&') continue;
+        const size_t sp = s.find_first_of(" \t");
+        const std::string key = upcase(s.substr(0, sp));
+        const std::string rest = sp == std::string::npos ? std::string() : s.substr(sp);
+        if (key == "&NUMTABLE") {
+            std::vector<int> nums;
+            const char *p = rest.c_str();
+            while (*p) {
+                if (isdigit((unsigned char)*p)) {
+                    char *e = nullptr;
+                    nums.push_back((int)strtol(p, &e, 10));
+                    p = e;
+                } else {
+                    ++p;
+                }
+            }
+            if (nums.empty() || nums[0] < 1 || (int)nums.size() < nums[0] + 1) break;
+            nc = nums[0];
+            f.ids.assign(nums.begin() + 1, nums.begin() + 1 + nc);
+        } else if (key == "&NUMPOINT") {
+            f.npt = atoi(rest.c_str());
+        } else if (key == "&POTTYPE") {
+            const std::vector<std::string> q = quoted(rest);
+            f.pottype = q.empty() ? trim(rest) : q[0];
+        } else if (key.compare(0, 2, "&#") == 0) {
+            header_done = true;
+            break;
+        }
+    }
+    if (!header_done || nc < 1 || f.npt < 4) {
+        fclose(fh);
+        why = std::string("bad header (need &NUMTABLE, &NUMPOINT >= 4 and the &# line) in ") + path;
+        return MSMGB_ERR_ARG;
+    }
+    f.x.assign((size_t)f.npt, 0.0);
+    f.col.assign((size_t)nc * ncol, std::vector<double>((size_t)f.npt, 0.0));
+    std::string t;
+    for (int r = 0; r < f.npt; ++r) {
+        for (int c = -1; c < nc * ncol + 1; ++c) {          // index, x, then the table columns
+            char *e = nullptr;
+            if (!next_token(fh, t)) goto short_file;
+            const double v = strtod(t.c_str(), &e);
+            if (e == t.c_str()) goto short_file;
+            if (c == 0) f.x[(size_t)r] = v;
+            else if (c > 0) f.col[(size_t)(c - 1)][(size_t)r] = v;
+        }
+    }
+    fclose(fh);
+    for (int r = 1; r < f.npt; ++r)
+        if (!(f.x[(size_t)r] > f.x[(size_t)r - 1])) {
+            why = std::string("grid not increasing in ") + path;
+            return MSMGB_ERR_ARG;
+        }
+    return MSMGB_OK;
+short_file:
+    fclose(fh);
+    why = std::string("fewer rows than &NUMPOINT in ") + path;
+    return MSMGB_ERR_ARG;
+}
+
+// slope of the cubic through (x[i0..i0+3], y[..]) at x[at] (Lagrange form)
+double lagrange4_slope(const double *x, const double *y, int at)
+{
+    double s = 0.0;
+    for (int j = 0; j < 4; ++j) {
+        if (j == at) {
+            double w = 0.0;
+            for (int k = 0; k < 4; ++k)
+                if (k != at) w += 1.0 / (x[at] - x[k]);
+            s += y[j] * w;
+        } else {
+            double num = 1.0, den = 1.0;
+            for (int k = 0; k < 4; ++k) {
+                if (k != j) den *= x[j] - x[k];
+                if (k != j && k != at) num *= x[at] - x[k];
+            }
+            s += y[j] * num / den;
+        }
+    }
+    return s;
+}
+
+// Clamped cubic spline in Hermite form: knot slopes d_i with d_0, d_{n-1} given and, inside,
+// h_i d_{i-1} + 2 (h_{i-1} + h_i) d_i + h_{i-1} d_{i+1} = 3 (h_i D_{i-1} + h_{i-1} D_i),
+// D_i = (y_{i+1} - y_i) / h_i, h_i = x_{i+1} - x_i (continuity of the second derivative).
+struct HSpline {
+    const double *x = nullptr, *y = nullptr;
+    int n = 0;
+    std::vector<double> d;
+};
+
+void hspline_build(HSpline &s, const double *x, const double *y, int n)
+{
+    s.x = x;
+    s.y = y;
+    s.n = n;
+    s.d.assign((size_t)n, 0.0);
+    s.d[0] = lagrange4_slope(x, y, 0);
+    s.d[(size_t)n - 1] = lagrange4_slope(x + n - 4, y + n - 4, 3);
+    std::vector<double> cp((size_t)n, 0.0), rp((size_t)n, 0.0);
+    // forward elimination of the interior rows (unknowns d_1..d_{n-2})
+    for (int i = 1; i <= n - 2; ++i) {
+        const double h0 = x[i] - x[i - 1], h1 = x[i + 1] - x[i];
+        const double D0 = (y[i] - y[i - 1]) / h0, D1 = (y[i + 1] - y[i]) / h1;
+        const double a = h1, b = 2.0 * (h0 + h1), c = h0;
+        double r = 3.0 * (h1 * D0 + h0 * D1);
+        if (i == 1) r -= a * s.d[0];
+        if (i == n - 2) r -= c * s.d[(size_t)n - 1];
+        const double den = b - (i > 1 ? a * cp[(size_t)i - 1] : 0.0);
+        cp[(size_t)i] = (i < n - 2) ? c / den : 0.0;
+        rp[(size_t)i] = (r - (i > 1 ? a * rp[(size_t)i - 1] : 0.0)) / den;
+    }
+    for (int i = n - 2; i >= 1; --i)
+        s.d[(size_t)i] = rp[(size_t)i] - (i < n - 2 ? cp[(size_t)i] * s.d[(size_t)i + 1] : 0.0);
+}
+
+// value at t: the interval x_i <= t < x_{i+1}; below x_0 the first, from x_{n-1} on the last
+// interval's cubic (SPLID2's interval choice)
+double hspline_at(const HSpline &s, double t)
+{
+    int lo = 0, hi = s.n - 1;
+    if (t <= s.x[0]) {
+        hi = 1;
+    } else if (t >= s.x[s.n - 1]) {
+        lo = s.n - 2;
+    } else {
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) / 2;
+            if (s.x[mid] <= t) lo = mid; else hi = mid;
+        }
+    }
+    const double h = s.x[hi] - s.x[lo], u = (t - s.x[lo]) / h;
+    const double u2 = u * u, u3 = u2 * u;
+    const double h00 = 2.0 * u3 - 3.0 * u2 + 1.0, h10 = u3 - 2.0 * u2 + u;
+    const double h01 = -2.0 * u3 + 3.0 * u2, h11 = u3 - u2;
+    return h00 * s.y[lo] + h10 * h * s.d[(size_t)lo] + h01 * s.y[hi] + h11 * h * s.d[(size_t)hi];
+}
+
+// first-appearance numbering of PTYPE(I,J) (I outer, J inner; New_ForceTable :560-574)
+void number_tables(int ng, const int *ptype, bool diag, std::vector<int> &ids, std::vector<int> &k)
+{
+    ids.clear();
+    k.assign((size_t)ng * ng, 0);
+    for (int i = 0; i < ng; ++i)
+        for (int j = 0; j < ng; ++j) {
+            if (diag && i != j) continue;
+            const int id = ptype[(size_t)j * ng + i];          // PTYPE(I,J), column-major
+            size_t q = 0;
+            while (q < ids.size() && ids[q] != id) ++q;
+            if (q == ids.size()) ids.push_back(id);
+            k[(size_t)j * ng + i] = (int)q + 1;
+        }
+}
+
+int file_table(const ImpFile &f, int id)
+{
+    for (size_t q = 0; q < f.ids.size(); ++q)
+        if (f.ids[q] == id) return (int)q;
+    return -1;
+}
+
+}  // namespace
+
+extern "C" int msmgb_import_info(const char *stem, int *pottype, int *ntables, int *ids, int *npoint,
+                                 int *nembtables, int *emb_ids, int *nembpoint)
+{
+    if (!stem) return MSMGB_ERR_ARG;
+    ImpFile p, e;
+    std::string why;
+    if (read_imported((std::string(stem) + ".pair").c_str(), 4, p, why) != MSMGB_OK) return MSMGB_ERR_ARG;
+    if (read_imported((std::string(stem) + ".embd").c_str(), 2, e, why) != MSMGB_OK) return MSMGB_ERR_ARG;
+    const std::string pt = upcase(p.pottype);
+    if (pottype) *pottype = pt == "EAM_TYPE" ? MSMGB_EAM_TYPE : MSMGB_FS_TYPE;
+    if (ntables) *ntables = (int)p.ids.size();
+    if (ids) for (size_t q = 0; q < p.ids.size(); ++q) ids[q] = p.ids[q];
+    if (npoint) *npoint = p.npt;
+    if (nembtables) *nembtables = (int)e.ids.size();
+    if (emb_ids) for (size_t q = 0; q < e.ids.size(); ++q) emb_ids[q] = e.ids[q];
+    if (nembpoint) *nembpoint = e.npt;
+    return MSMGB_OK;
+}
+
+extern "C" int msmgb_import_forcetable(const char *stem, int units, int ngroup, const int *ptype, double rmax,
+                                       int ntab, int nembd, double *potr, double *fpotr, double *potb,
+                                       double *fpotb, double *fembd, double *dfembd, int *kpair, int *kembd,
+                                       int *nkind, int *nkind1, double *rhod, int *pottype)
+{
+    if (!stem || !ptype || ngroup < 1 || ngroup > 16 || !(rmax > 0.0) || ntab < 2 || !potr || !fpotr || !potb ||
+        !fpotb || !kpair || (units != MSMGB_UNITS_EV_A && units != MSMGB_UNITS_CGS))
+        return MSMGB_ERR_ARG;
+    ImpFile p, e;
+    std::string why;
+    if (read_imported((std::string(stem) + ".pair").c_str(), 4, p, why) != MSMGB_OK) return MSMGB_ERR_ARG;
+    if (read_imported((std::string(stem) + ".embd").c_str(), 2, e, why) != MSMGB_OK) return MSMGB_ERR_ARG;
+    const bool eam = upcase(p.pottype) == "EAM_TYPE";
+    if (eam && (nembd < 2 || !fembd || !dfembd || !kembd)) return MSMGB_ERR_ARG;
+    // every table the box names must be in both files (:1631-1651)
+    for (int q = 0; q < ngroup * ngroup; ++q)
+        if (file_table(p, ptype[q]) < 0) return MSMGB_ERR_ARG;
+    for (int i = 0; i < ngroup; ++i)
+        if (file_table(e, ptype[(size_t)i * ngroup + i]) < 0) return MSMGB_ERR_ARG;
+    // unit conversion of Import_ForceTable (:1529-1540, 1583-1585); the files are in A / eV
+    const bool cgs = units == MSMGB_UNITS_CGS;
+    const double rhounit = (!eam && cgs) ? 1.0 / (kEVERG * kEVERG) : 1.0;
+    const double fx = cgs ? kA2CM : 1.0;
+    const double fc[4] = {0.5 * (cgs ? kEVERG * kA2CM : 1.0), cgs ? kEVERG : 1.0, 1.0 / rhounit,
+                          (cgs ? 1.0 / kA2CM : 1.0) / rhounit};
+    for (double &v : p.x) v *= fx;
+    for (size_t q = 0; q < p.ids.size(); ++q)
+        for (int c = 0; c < 4; ++c)
+            for (double &v : p.col[q * 4 + c]) v *= fc[c];
+    for (double &v : e.x) v /= rhounit;
+    for (size_t q = 0; q < e.ids.size(); ++q) {
+        for (double &v : e.col[q * 2]) v *= cgs ? kEVERG : 1.0;
+        if (!cgs)
+            for (double &v : e.col[q * 2 + 1]) v /= kEVERG;   // the file keeps dF/drho in CGS
+    }
+    // pair tables the box needs, first-appearance order, re-gridded (:1667-1760)
+    std::vector<int> ids, kp;
+    number_tables(ngroup, ptype, false, ids, kp);
+    const int nk = (int)ids.size();
+    const double csi = (double)ntab / std::sqrt(rmax), csiv = 1.0 / csi;
+    double trmax = p.x[0];
+    for (double v : p.x) trmax = std::max(trmax, v);
+    double *dst[4] = {potr, fpotr, potb, fpotb};
+    for (int k = 0; k < nk; ++k) {
+        const int q = file_table(p, ids[(size_t)k]);
+        for (int c = 0; c < 4; ++c) {
+            HSpline s;
+            hspline_build(s, p.x.data(), p.col[(size_t)q * 4 + c].data(), p.npt);
+            for (int i = 1; i <= ntab; ++i) {
+                const double t = (double)i * csiv, tt = t * t;
+                dst[c][(size_t)(i - 1) * nk + k] = tt <= trmax ? hspline_at(s, tt) : 0.0;
+            }
+        }
+    }
+    for (int q = 0; q < ngroup * ngroup; ++q) kpair[q] = kp[(size_t)q];
+    if (nkind) *nkind = nk;
+    if (pottype) *pottype = eam ? MSMGB_EAM_TYPE : MSMGB_FS_TYPE;
+    // embedding tables of the groups (:1785-1838); FS potentials have none
+    const int ne = e.npt;
+    double rmx = (e.x[(size_t)ne - 1] / (double)(ne - 1)) * (double)ne;
+    double rd = nembd > 0 ? rmx / (double)nembd : 1.0;
+    if (rd <= 1e-64) rd = 1.0;
+    if (rhod) *rhod = rd;
+    if (!eam) {
+        if (nkind1) *nkind1 = 0;
+        return MSMGB_OK;
+    }
+    std::vector<int> eids, ke;
+    number_tables(ngroup, ptype, true, eids, ke);
+    const int nk1 = (int)eids.size();
+    for (int k = 0; k < nk1; ++k) {
+        const int q = file_table(e, eids[(size_t)k]);
+        double *edst[2] = {fembd, dfembd};
+        for (int c = 0; c < 2; ++c) {
+            HSpline s;
+            hspline_build(s, e.x.data(), e.col[(size_t)q * 2 + c].data(), ne);
+            for (int i = 1; i <= nembd; ++i)
+                edst[c][(size_t)(i - 1) * nk1 + k] = hspline_at(s, (double)(i - 1) * rd);
+        }
+    }
+    for (int i = 0; i < ngroup; ++i) kembd[i] = ke[(size_t)i * ngroup + i];
+    if (nkind1) *nkind1 = nk1;
+    return MSMGB_OK;
+}
+
+// Export_ForceTable (:1315-1459): the two files in the reference's layout and number format
+// (1PE21.9 pair columns, 1PE16.8 embedding columns), tables in increasing id order.
+extern "C" int msmgb_export_forcetable(const char *stem, int units, const msmgb_forcetable *ft, const int *ids,
+                                       const int *emb_ids)
+{
+    if (!stem || !ft || !ft->potr || !ft->fpotr || !ft->potb || !ft->fpotb || ft->ntab < 1 || ft->nkind < 1 ||
+        !(ft->rmax > 0.0) || (units != MSMGB_UNITS_EV_A && units != MSMGB_UNITS_CGS))
+        return MSMGB_ERR_ARG;
+    const bool eam = ft->pottype == MSMGB_EAM_TYPE;
+    if (eam && (ft->nembd < 1 || ft->nkind1 < 1 || !ft->fembd || !ft->dfembd)) return MSMGB_ERR_ARG;
+    const bool cgs = units == MSMGB_UNITS_CGS;
+    const double rhounit = (!eam && cgs) ? 1.0 / (kEVERG * kEVERG) : 1.0;
+    const int nk = ft->nkind;
+    std::vector<int> id((size_t)nk), tid((size_t)nk);
+    for (int k = 0; k < nk; ++k) id[(size_t)k] = ids ? ids[k] : k + 1;
+    for (int k = 0; k < nk; ++k) tid[(size_t)k] = k;
+    std::stable_sort(tid.begin(), tid.end(), [&](int a, int b) { return id[(size_t)a] < id[(size_t)b]; });
+    const char *ptn = eam ? "EAM_TYPE" : "FS_TYPE";
+    FILE *f = fopen((std::string(stem) + ".pair").c_str(), "w");
+    if (!f) return MSMGB_ERR_ARG;
+    fprintf(f, "&MDPSCU_POTTAB.Pair\n !     exported by libmsmgb (msmgb_export_forcetable)\n");
+    fprintf(f, "!     \n!     NOTE: For FS potential, RHO is in eV^2, the potential calculated by\n"
+               "!           -sqrt(RHO)+V(r) \n!           is thus in unit eV, and the d(RHO)/dr in unit eV^2/A.\n"
+               "!           \n!           For EAM potential, not specific unit is assigned for RHO,\n"
+               "!           and for d(RHO)/dr. The potential calculated by \n"
+               "!           F(RHO)+V(r) is in unit eV.\n!           \n");
+    fprintf(f, "&POTTYPE \"%s\"\n&NUMTABLE %7d table IDs: ", ptn, nk);
+    for (int k = 0; k < nk; ++k) fprintf(f, "%5d", id[(size_t)tid[(size_t)k]]);
+    fprintf(f, "\n&NUMPOINT %7d\n&#     ", ft->ntab);
+    fprintf(f, "      Rij(A)     ");
+    for (int k = 0; k < nk; ++k) {
+        const int j = id[(size_t)tid[(size_t)k]];
+        fprintf(f, "      r*V%d(r)[eV*A]        -r*dV%d/dr[eV]            RHO%d(r)            -dRHO%d/dr[/A] ", j, j,
+                j, j);
+    }
+    fprintf(f, "\n");
+    const double csi = (double)ft->ntab / std::sqrt(ft->rmax), csiv = 1.0 / csi;
+    for (int i = 1; i <= ft->ntab; ++i) {
+        const double t = (double)i * csiv;
+        fprintf(f, " %6d %21.9E", i, (t * t) * (cgs ? 1.0 / kA2CM : 1.0));
+        for (int k = 0; k < nk; ++k) {
+            const size_t o = (size_t)(i - 1) * nk + tid[(size_t)k];
+            fprintf(f, "%21.9E%21.9E%21.9E%21.9E", ft->potr[o] * 2.0 * (cgs ? 1.0 / (kEVERG * kA2CM) : 1.0),
+                    ft->fpotr[o] * (cgs ? 1.0 / kEVERG : 1.0), ft->potb[o] * rhounit,
+                    ft->fpotb[o] * rhounit * (cgs ? kA2CM : 1.0));
+        }
+        fprintf(f, "\n");
+    }
+    if (fclose(f) != 0) return MSMGB_ERR_ARG;
+    // embedding file
+    const int nk1 = eam ? ft->nkind1 : 1;
+    std::vector<int> eid((size_t)nk1), etid((size_t)nk1);
+    for (int k = 0; k < nk1; ++k) eid[(size_t)k] = (eam && emb_ids) ? emb_ids[k] : k + 1;
+    for (int k = 0; k < nk1; ++k) etid[(size_t)k] = k;
+    std::stable_sort(etid.begin(), etid.end(), [&](int a, int b) { return eid[(size_t)a] < eid[(size_t)b]; });
+    f = fopen((std::string(stem) + ".embd").c_str(), "w");
+    if (!f) return MSMGB_ERR_ARG;
+    fprintf(f, "&MDPSCU_POTTAB.Embd\n !     exported by libmsmgb (msmgb_export_forcetable)\n");
+    fprintf(f, "&POTTYPE \"%s\"\n&NUMTABLE %7d table IDs: ", ptn, nk1);
+    for (int k = 0; k < nk1; ++k) fprintf(f, "%5d", eid[(size_t)etid[(size_t)k]]);
+    const int ne = eam ? ft->nembd : ft->ntab;
+    fprintf(f, "\n&NUMPOINT %7d\n&#     ", ne);
+    fprintf(f, "      RHO      ");
+    for (int k = 0; k < nk1; ++k) {
+        const int j = eid[(size_t)etid[(size_t)k]];
+        fprintf(f, "         F%d(RHO)      dF%d/d(RHO)", j, j);
+    }
+    fprintf(f, "\n");
+    // FS: RHOD of the density tables (Create_EMBDFUNTable); the column is informational
+    double rd = ft->rhod;
+    for (int i = 1; i <= ne; ++i) {
+        const double r = (double)(i - 1) * rd * rhounit;    // file rho (FS: eV^2)
+        fprintf(f, " %6d %16.8E", i, r);
+        for (int k = 0; k < nk1; ++k) {
+            double den, deni;
+            if (!eam) {
+                // DEN = -sqrt(rho)/ERGEV in erg, DENI = 1/(2 DEN) (:1444-1449)
+                den = r > 0.0 ? -std::sqrt(r) * kEVERG : 0.0;
+                deni = r > 0.0 ? 0.5 / den : 0.0;
+            } else {
+                const size_t o = (size_t)(i - 1) * nk1 + etid[(size_t)k];
+                den = ft->fembd[o] * (cgs ? 1.0 : kEVERG);      // erg
+                deni = ft->dfembd[o] * (cgs ? 1.0 : kEVERG);    // CGS per rho unit
+            }
+            fprintf(f, "%16.8E%16.8E", den / kEVERG, deni);
+        }
+        fprintf(f, "\n");
+    }
+    if (fclose(f) != 0) return MSMGB_ERR_ARG;
     return MSMGB_OK;
 }

@@ -154,6 +154,58 @@ class ForceTable:
         return self
 
     @classmethod
+    def imported(cls, stem, ptype, rmax, ntab=10000, nembd=10000, units=L.UNITS_EV_A):
+        """Tables read back from a pair of files stem.pair / stem.embd that the reference (or
+        export()) wrote (Register_Imported_ForceTable): the file tables PTYPE names (NGROUP x
+        NGROUP, host first, ids as in the files), re-gridded by the reference's spline onto the
+        sqrt(r) grid of ntab points up to rmax and, for EAM, onto nembd embedding points."""
+        lib = L.load()
+        ptype = np.asarray(ptype, np.int32)
+        ng = ptype.shape[0]
+        self = cls.__new__(cls)
+        self.pot, self.prm = None, np.zeros(5)
+        self.rmax = self.ru = float(rmax)
+        self.ntab, self.nembd = int(ntab), int(nembd)
+        self.potr, self.fpotr, self.potb, self.fpotb = (np.zeros(self.ntab * ng * ng) for _ in range(4))
+        fe, dfe = np.zeros(self.nembd * ng), np.zeros(self.nembd * ng)
+        self._kpair = np.zeros(ng * ng, np.int32)
+        self._kembd = np.ones(ng, np.int32)
+        nk, nk1, rhod, pt = C.c_int(), C.c_int(), C.c_double(), C.c_int()
+        pcol = np.ascontiguousarray(ptype.T).reshape(-1)
+        rc = lib.msmgb_import_forcetable(os.fsencode(stem), int(units), ng, _i(pcol), self.rmax, self.ntab,
+                                         self.nembd, _d(self.potr), _d(self.fpotr), _d(self.potb),
+                                         _d(self.fpotb), _d(fe), _d(dfe), _i(self._kpair), _i(self._kembd),
+                                         C.byref(nk), C.byref(nk1), C.byref(rhod), C.byref(pt))
+        if rc != L.OK:
+            raise MSMError(rc, "cannot import force tables %s.pair / .embd" % stem)
+        self.pottype = pt.value
+        self.nkind, self.nkind1, self.ngroup = nk.value, max(nk1.value, 1), ng
+        n = self.nkind * self.ntab
+        self.potr, self.fpotr, self.potb, self.fpotb = (a[:n].copy() for a in
+                                                        (self.potr, self.fpotr, self.potb, self.fpotb))
+        if self.pottype == L.EAM_TYPE:
+            self.fembd, self.dfembd = fe[:nk1.value * self.nembd].copy(), dfe[:nk1.value * self.nembd].copy()
+        else:
+            self.fembd = self.dfembd = None
+        self.rhod = rhod.value
+        self.masses = None
+        self.ptype = ptype
+        return self
+
+    def export(self, stem, ids=None, emb_ids=None, units=L.UNITS_EV_A):
+        """Writes stem.pair / stem.embd in the reference's layout (Export_ForceTable); ids and
+        emb_ids name the tables (default 1, 2, ...)."""
+        lib = L.load()
+        t = self.struct()
+        ia = None if ids is None else np.asarray(ids, np.int32)
+        ea = None if emb_ids is None else np.asarray(emb_ids, np.int32)
+        rc = lib.msmgb_export_forcetable(os.fsencode(stem), int(units), C.byref(t),
+                                         _i(ia) if ia is not None else None,
+                                         _i(ea) if ea is not None else None)
+        if rc != L.OK:
+            raise MSMError(rc, "cannot export force tables to %s" % stem)
+
+    @classmethod
     def moldy(cls, path, rmax, ntab=10000, nembd=10000, rhoscal=20.0):
         """One-element EAM potential (F = -sqrt(rho)) from a Moldy file
         (Register_ForceTableProc_Moldy), on the sqrt(r) grid up to the cutoff rmax."""

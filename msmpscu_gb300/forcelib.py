@@ -87,6 +87,46 @@ def ptype_from_symbols(libname, symbols):
     return pt
 
 
+def nist(path, ru, ntab=10000, nembd=10000, export_dir=None):
+    """A NIST potential file (.setfl or .lspt) the way the reference runs one
+    (Register_Internal_ForceLib, MDLIB/sor/Appshell/MD_ForceLib_Register.F90:405-420):
+    - if path.pair and path.embd exist, they are imported as they are;
+    - otherwise the file's tables are generated on its own r and rho ranges
+      (NIST_ForceTable.F90:140-175, 379-413: every element pair, groups in the file's element
+      order, table id (I-1)*NE + J for an I host with a J neighbour), exported in the
+      reference's format (to export_dir, default a temporary directory; the reference writes
+      them next to the file) and imported;
+    - the import re-grids them onto the sqrt(r) grid up to the cutoff ru (ntab points) and
+      the embedding functions onto nembd points (Register_Imported_ForceTable), so the
+      tables carry the export's 10-digit rounding exactly as the reference's do."""
+    import os
+    import tempfile
+    ext = path.rsplit(".", 1)[-1].upper()
+    masses = None
+    stem = path
+    if not (os.path.exists(path + ".pair") and os.path.exists(path + ".embd")):
+        if ext == "SETFL":
+            gen = ForceTable.setfl(path, ntab=ntab)
+            masses = gen.masses
+        else:
+            gen = ForceTable.lspt(path, ntab=ntab, nembd=nembd)
+        ne = gen.ngroup
+        out_dir = export_dir or tempfile.mkdtemp(prefix="msmgb_nist_")
+        stem = os.path.join(out_dir, os.path.basename(path))
+        gen.export(stem, ids=np.arange(1, ne * ne + 1), emb_ids=[i * ne + i + 1 for i in range(ne)])
+    import ctypes as C
+    nt = C.c_int()
+    rc = L.load().msmgb_import_info(os.fsencode(stem), None, C.byref(nt), None, None, None, None, None)
+    if rc != L.OK:
+        raise ValueError("cannot read the tables %s.pair / .embd" % stem)
+    ne = int(round(np.sqrt(nt.value)))
+    ptype = np.array([[i * ne + j + 1 for j in range(ne)] for i in range(ne)], np.int32)
+    out = ForceTable.imported(stem, ptype, ru, ntab=ntab, nembd=nembd)
+    out.masses = masses
+    out.library = path
+    return out
+
+
 def create(libname, ru, symbols=None, ptype=None, subtype=None, pottype=None, ntab=10000, nembd=10000,
            rhoscal=20.0):
     """ForceTable of library `libname` for groups given by `symbols` (element symbols) or by
@@ -99,11 +139,7 @@ def create(libname, ru, symbols=None, ptype=None, subtype=None, pottype=None, nt
     if ext == "MOLDY":
         return ForceTable.moldy(libname, rmax=ru, ntab=ntab, nembd=nembd, rhoscal=rhoscal)
     if ext in ("SETFL", "LSPT"):
-        # NIST files (NIST_ForceTable.F90:140-175): every element pair is tabulated, groups in
-        # the file's element order, on the file's own r and rho ranges
-        if ext == "SETFL":
-            return ForceTable.setfl(libname, ntab=ntab)
-        return ForceTable.lspt(libname, ntab=ntab, nembd=nembd)
+        return nist(libname, ru, ntab=ntab, nembd=nembd)
     if key not in LIBRARIES:
         raise ValueError("unknown force library %s" % libname)
     deftype, reg = LIBRARIES[key]

@@ -1540,3 +1540,109 @@ int orc_setfl_tables(int nrho, double drho, int nr, double cutoff, const double 
     free(m3);
     return 0;
 }
+
+/* ------------------------------------------------------------------------------------ */
+/* Re-grid of imported tables (Register_Imported_ForceTable, MD_TypeDef_ForceTable.F90:    */
+/* 1612-1855) through SPLID1 / SPLID2 (LIB/sor/f/MiniUtilities/DINTF2.F:17-240) with       */
+/* IOP(1) = IOP(2) = 5 and IJ = 1                                                          */
+/* ------------------------------------------------------------------------------------ */
+
+/* SPLID1 with IOP = 5 at both ends: the end first derivatives are those of the cubic through
+ * the four end points (DINTF2.F:75-96), and option 5 then proceeds as the clamped option 3
+ * (:120-130, 170-178).  The second derivatives w solve
+ *   row 1:      2 h_1 w_1 + h_1 w_2                       = 6 (D_1 - C1)
+ *   row i:      h_{i-1} w_{i-1} + 2 (h_{i-1} + h_i) w_i + h_i w_{i+1} = 6 (D_i - D_{i-1})
+ *   row N:      h_{N-1} w_{N-1} + 2 h_{N-1} w_N            = 6 (C2 - D_{N-1})
+ * with h_i = x_{i+1} - x_i, D_i = (f_{i+1} - f_i)/h_i; solved here by forward elimination
+ * and back substitution.  Requires n >= 4 (the reference prints a warning otherwise). */
+void orc_splid1(int n, const double *x, const double *f, double *w)
+{
+    const double a1 = x[0] - x[1], a2 = x[0] - x[2], a3 = x[0] - x[3];
+    const double a4 = x[1] - x[2], a5 = x[1] - x[3], a6 = x[2] - x[3];
+    const double c1 = f[0] * (1.0 / a1 + 1.0 / a2 + 1.0 / a3) - a2 * a3 * f[1] / (a1 * a4 * a5) +
+                      a1 * a3 * f[2] / (a2 * a4 * a6) - a1 * a2 * f[3] / (a3 * a5 * a6);
+    const double b1 = x[n - 1] - x[n - 4], b2 = x[n - 1] - x[n - 3], b3 = x[n - 1] - x[n - 2];
+    const double b4 = x[n - 2] - x[n - 4], b5 = x[n - 2] - x[n - 3], b6 = x[n - 3] - x[n - 4];
+    const double c2 = -b2 * b3 * f[n - 4] / (b6 * b4 * b1) + b1 * b3 * f[n - 3] / (b6 * b5 * b2) -
+                      b1 * b2 * f[n - 2] / (b4 * b5 * b3) + f[n - 1] * (1.0 / b1 + 1.0 / b2 + 1.0 / b3);
+    double *cp = (double *)malloc(sizeof(double) * (size_t)n);
+    double *rp = (double *)malloc(sizeof(double) * (size_t)n);
+    for (int i = 0; i < n; ++i) {
+        double lo = 0.0, di, up = 0.0, r;
+        if (i == 0) {
+            const double h = x[1] - x[0];
+            di = 2.0 * h;
+            up = h;
+            r = 6.0 * ((f[1] - f[0]) / h - c1);
+        } else if (i == n - 1) {
+            const double h = x[n - 1] - x[n - 2];
+            lo = h;
+            di = 2.0 * h;
+            r = 6.0 * (c2 - (f[n - 1] - f[n - 2]) / h);
+        } else {
+            const double h0 = x[i] - x[i - 1], h1 = x[i + 1] - x[i];
+            lo = h0;
+            di = 2.0 * (h0 + h1);
+            up = h1;
+            r = 6.0 * ((f[i + 1] - f[i]) / h1 - (f[i] - f[i - 1]) / h0);
+        }
+        const double piv = i > 0 ? di - lo * cp[i - 1] : di;
+        cp[i] = up / piv;
+        rp[i] = (i > 0 ? r - lo * rp[i - 1] : r) / piv;
+    }
+    w[n - 1] = rp[n - 1];
+    for (int i = n - 2; i >= 0; --i) w[i] = rp[i] - cp[i] * w[i + 1];
+    free(cp);
+    free(rp);
+}
+
+/* SPLID2 (DINTF2.F:176-218): the interval I with X(I) <= Y < X(I+1) (SEARCH), I = 1 for
+ * Y <= X(1) and I = N-1 for Y >= X(N), then the cubic of that interval at Y. */
+double orc_splid2(int n, const double *x, const double *f, const double *w, double y)
+{
+    int i;
+    if (y <= x[0]) {
+        i = 0;
+    } else if (y >= x[n - 1]) {
+        i = n - 2;
+    } else {
+        int lo = 0, hi = n - 1;
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (y >= x[mid]) lo = mid; else hi = mid;
+        }
+        i = lo;
+    }
+    const double flk = x[i + 1] - x[i];
+    const double u = x[i + 1] - y, v = y - x[i];
+    const double a = (w[i] * u * u * u + w[i + 1] * v * v * v) / (6.0 * flk);
+    const double b = (f[i + 1] / flk - w[i + 1] * flk / 6.0) * v;
+    const double c = (f[i] / flk - flk * w[i] / 6.0) * u;
+    return a + b + c;
+}
+
+/* one pair column on the run's grid (:1714-1724 and its three twins): T = K CSIV with
+ * CSIV = 1/CSI, CSI = NTAB/sqrt(Rmax) (New_ForceTable :591-594); 0 where T^2 > max R */
+void orc_import_regrid_pair(int nf, const double *rf, const double *yf, double rmax, int ntab, double *out)
+{
+    double *w = (double *)malloc(sizeof(double) * (size_t)nf);
+    orc_splid1(nf, rf, yf, w);
+    double trmax = rf[0];
+    for (int i = 1; i < nf; ++i)
+        if (rf[i] > trmax) trmax = rf[i];
+    const double csi = (double)ntab / sqrt(rmax), csiv = 1.0 / csi;
+    for (int k = 1; k <= ntab; ++k) {
+        const double t = (double)k * csiv, tt = t * t;
+        out[k - 1] = tt <= trmax ? orc_splid2(nf, rf, yf, w, tt) : 0.0;
+    }
+    free(w);
+}
+
+/* one embedding column (:1818-1830): rho = (K-1) RHOD, no range test */
+void orc_import_regrid_embd(int nf, const double *rhof, const double *yf, double rhod, int nembd, double *out)
+{
+    double *w = (double *)malloc(sizeof(double) * (size_t)nf);
+    orc_splid1(nf, rhof, yf, w);
+    for (int k = 1; k <= nembd; ++k) out[k - 1] = orc_splid2(nf, rhof, yf, w, (double)(k - 1) * rhod);
+    free(w);
+}

@@ -188,6 +188,18 @@ int  orc_adjoint_cr(int n, const double *x, const double *y, const double *z, co
                     const double *fty, const double *ftz, double *loss, double *grad,
                     int nthreads);
 
+/* Re-grid of imported tables (Register_Imported_ForceTable, MD_TypeDef_ForceTable.F90:1612-1855)
+ * through SPLID1/SPLID2 (LIB/sor/f/MiniUtilities/DINTF2.F) with end slopes from the four end
+ * points (IOP = 5):
+ *   orc_splid1: second derivatives w of the spline through (x, f), n >= 4
+ *   orc_splid2: its value at y (end intervals extended)
+ *   orc_import_regrid_pair: a pair column onto T = K/CSI, K = 1..ntab (0 beyond max r)
+ *   orc_import_regrid_embd: an embedding column onto rho = (K-1) rhod, K = 1..nembd        */
+void   orc_splid1(int n, const double *x, const double *f, double *w);
+double orc_splid2(int n, const double *x, const double *f, const double *w, double y);
+void   orc_import_regrid_pair(int nf, const double *rf, const double *yf, double rmax, int ntab, double *out);
+void   orc_import_regrid_embd(int nf, const double *rhof, const double *yf, double rhod, int nembd, double *out);
+
 #ifdef __cplusplus
 }
 #endif

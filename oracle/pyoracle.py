@@ -62,6 +62,9 @@ def lib():
         _lib.orc_spline_knots_eval.restype = None
         _lib.orc_pot_eval.restype = C.c_int
         _lib.orc_embed_eval.restype = C.c_int
+        _lib.orc_splid2.restype = C.c_double
+        _lib.orc_import_regrid_pair.restype = None
+        _lib.orc_import_regrid_embd.restype = None
     return _lib
 
 
@@ -506,3 +509,100 @@ def adjoint_cr(pos, ityp, statu, box, kvois, indi, tables, dtab, ft, nthreads=0)
                          _i(kv), _i(ind), ind.shape[1] if ind.ndim == 2 else n, C.byref(tables.s),
                          _d(d), _d(tx), _d(ty_), _d(tz), C.byref(loss), _d(grad), nthreads)
     return loss.value, grad
+
+
+# ---- tables the reference exported, read back -------------------------------------------
+EVERG, A2CM = 1.60219e-12, 1e-8        # MSM_Const.F90:67, 83
+
+
+def read_imported(path, ncol):
+    """One exported table file (Import_ForceTable, MD_TypeDef_ForceTable.F90:1485-1527):
+    header lines until "&#" -- &POTTYPE "name", &NUMTABLE NC followed by the NC table ids,
+    &NUMPOINT NT (comment lines start with "!") -- then NT rows of index, x and ncol numbers
+    per table, read as a stream of numbers (list-directed READ)."""
+    pottype, ids, npt = None, None, None
+    with open(path) as fh:
+        lines = fh.read().splitlines()
+    k = 0
+    while k < len(lines):
+        s = lines[k].strip()
+        k += 1
+        if not s.startswith("&"):
+            continue
+        key = s.split()[0].upper()
+        if key == "&NUMTABLE":
+            nums = [int(v) for v in re.findall(r"\d+", s[len("&NUMTABLE"):])]
+            ids = nums[1:1 + nums[0]]
+        elif key == "&NUMPOINT":
+            npt = int(s.split()[1])
+        elif key == "&POTTYPE":
+            m = re.search(r'"([^"]*)"', s)
+            pottype = m.group(1) if m else s.split()[1]
+        elif key.startswith("&#"):
+            break
+    vals = np.array(" ".join(lines[k:]).split()[: npt * (2 + ncol * len(ids))], np.float64)
+    rows = vals.reshape(npt, 2 + ncol * len(ids))
+    return dict(pottype=pottype.strip().upper(), ids=ids, x=rows[:, 1].copy(),
+                cols=rows[:, 2:].reshape(npt, len(ids), ncol))
+
+
+def import_tables(stem, ptype, rmax, ntab=10000, nembd=10000, cgs=False):
+    """Register_Imported_ForceTable (MD_TypeDef_ForceTable.F90:1612-1855) for a box of groups
+    whose pairs use the file tables PTYPE (NGROUP x NGROUP, host first): the named tables in
+    first-appearance order (New_ForceTable :560-574, 600-610), unit conversion of the import
+    (:1529-1540, 1583-1585; the files are in A / eV, `cgs` gives the reference's CGS tables),
+    pair columns re-gridded by SPLID1/SPLID2 onto T = K/CSI, embedding columns onto
+    rho = (K-1) RHOD, RHOD = RHO(N) N/(N-1) / NEMBD.  Returns the dict layout of lspt_tables
+    (arrays (NTAB, NKIND), kpair (NGROUP, NGROUP) with KPAIR(I, J) at [I-1, J-1])."""
+    pair = read_imported(stem + ".pair", 4)
+    embd = read_imported(stem + ".embd", 2)
+    eam = pair["pottype"] == "EAM_TYPE"
+    rhounit = 1.0 / (EVERG * EVERG) if (cgs and not eam) else 1.0
+    fx = A2CM if cgs else 1.0
+    fc = np.array([0.5 * (EVERG * A2CM if cgs else 1.0), EVERG if cgs else 1.0, 1.0 / rhounit,
+                   (1.0 / A2CM if cgs else 1.0) / rhounit])
+    r = pair["x"] * fx
+    pcols = pair["cols"] * fc[None, None, :]
+    rho = embd["x"] / rhounit
+    ecols = embd["cols"].copy()
+    ecols[:, :, 0] *= EVERG if cgs else 1.0
+    if not cgs:
+        ecols[:, :, 1] /= EVERG
+    ptype = np.asarray(ptype, np.int32)
+    ng = ptype.shape[0]
+    order = []
+    for i in range(ng):
+        for j in range(ng):
+            if int(ptype[i, j]) not in order:
+                order.append(int(ptype[i, j]))
+    kpair = np.array([[order.index(int(ptype[i, j])) + 1 for j in range(ng)] for i in range(ng)], np.int32)
+    nk = len(order)
+    out = {name: np.zeros((ntab, nk)) for name in ("potr", "fpotr", "potb", "fpotb")}
+    for k, tid in enumerate(order):
+        q = pair["ids"].index(tid)
+        for c, name in enumerate(("potr", "fpotr", "potb", "fpotb")):
+            col = np.zeros(ntab)
+            lib().orc_import_regrid_pair(len(r), _d(f64(r)), _d(f64(pcols[:, q, c])), C.c_double(rmax), ntab,
+                                         _d(col))
+            out[name][:, k] = col
+    ne = len(rho)
+    rhod = (rho[-1] / float(ne - 1)) * float(ne) / float(nembd)
+    if rhod <= 1e-64:
+        rhod = 1.0
+    emb = []
+    for i in range(ng):
+        if int(ptype[i, i]) not in emb:
+            emb.append(int(ptype[i, i]))
+    kembd = np.array([emb.index(int(ptype[i, i])) + 1 for i in range(ng)], np.int32)
+    fembd, dfembd = np.zeros((nembd, len(emb))), np.zeros((nembd, len(emb)))
+    if eam:
+        for k, tid in enumerate(emb):
+            q = embd["ids"].index(tid)
+            for c, dst in ((0, fembd), (1, dfembd)):
+                col = np.zeros(nembd)
+                lib().orc_import_regrid_embd(ne, _d(f64(rho)), _d(f64(ecols[:, q, c])), C.c_double(rhod), nembd,
+                                             _d(col))
+                dst[:, k] = col
+    return dict(potr=out["potr"], fpotr=out["fpotr"], potb=out["potb"], fpotb=out["fpotb"],
+                fembd=fembd if eam else None, dfembd=dfembd if eam else None, rhod=rhod, kpair=kpair,
+                kembd=kembd, ntab=ntab, nembd=nembd, rmax=rmax, pottype=EAM if eam else FS, ids=order)

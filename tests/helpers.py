@@ -23,3 +23,19 @@ def sorted_sets(kvois, indi):
 def rel_err(a, b):
     a, b = np.asarray(a), np.asarray(b)
     return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+def reference_export(tmp_dir, name):
+    """Writes the reference's exported table files tests/golden/ref_<name>.{pair,embd}.xz
+    (byte copies of its Export_ForceTable output, see tests/golden/make_golden_import.py) into
+    tmp_dir and returns their common stem."""
+    import lzma
+    import os
+    here = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    stem = os.path.join(str(tmp_dir), name)
+    for ext in ("pair", "embd"):
+        with open(os.path.join(here, "ref_%s.%s.xz" % (name, ext)), "rb") as fh:
+            data = lzma.decompress(fh.read())
+        with open(stem + "." + ext, "wb") as fh:
+            fh.write(data)
+    return stem
