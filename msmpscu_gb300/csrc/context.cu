@@ -483,6 +483,16 @@ extern "C" int msmgb_init_forcetable(msmgb_ctx *c, const msmgb_forcetable *ft)
         o[1] = (float)(v - (double)o[0]);
     };
     std::vector<float> fd((size_t)4 * nk * rowp), ff8((size_t)8 * nk * rowp), fe((size_t)4 * nk1 * nep);
+    // rows of the table-assisted mixed density pass: value, slope, r2 of the grid point
+    std::vector<float> fq((size_t)4 * nk * rowp);
+    for (size_t k = 0; k < nk; ++k)
+        for (size_t i = 0; i < rowp; ++i) {
+            size_t o = k * rowp + i;
+            fq[4 * o] = f2[2 * o];
+            fq[4 * o + 1] = f2[2 * o + 1];
+            const double g = (double)i / t.csi, r2g = (g * g) * (g * g);
+            split(r2g, &fq[4 * o + 2]);
+        }
     for (size_t k = 0; k < nk; ++k)
         for (size_t i = 0; i < rowp; ++i) {
             size_t o = k * rowp + i, o1 = i + 1 < rowp ? o + 1 : o;
@@ -505,7 +515,8 @@ extern "C" int msmgb_init_forcetable(msmgb_ctx *c, const msmgb_forcetable *ft)
     CK(cudaStreamSynchronize(c->stream), "synchronize");
     if (c->tab_mem) { cudaFree(c->tab_mem); c->tab_mem = nullptr; }
     const size_t bytes = nd * sizeof(double) +
-                         (f2.size() + f4.size() + e2.size() + fd.size() + ff8.size() + fe.size()) * sizeof(float) +
+                         (f2.size() + f4.size() + e2.size() + fd.size() + ff8.size() + fe.size() + fq.size()) *
+                             sizeof(float) +
                          2048;
     CK(cudaMalloc(&c->tab_mem, bytes), "table alloc");
     char *base = (char *)c->tab_mem;
@@ -518,10 +529,12 @@ extern "C" int msmgb_init_forcetable(msmgb_ctx *c, const msmgb_forcetable *ft)
     float *dfd = (float *)a16;
     float *dff8 = dfd + fd.size();
     float *dfe = dff8 + ff8.size();
+    float *dfq = dfe + fe.size();          // fe.size() is a multiple of 4: 16-byte aligned
     CK(cudaMemcpy(dd, hd.data(), nd * sizeof(double), cudaMemcpyHostToDevice), "table upload");
     CK(cudaMemcpy(dfd, fd.data(), fd.size() * sizeof(float), cudaMemcpyHostToDevice), "table upload");
     CK(cudaMemcpy(dff8, ff8.data(), ff8.size() * sizeof(float), cudaMemcpyHostToDevice), "table upload");
     if (eam) CK(cudaMemcpy(dfe, fe.data(), fe.size() * sizeof(float), cudaMemcpyHostToDevice), "table upload");
+    CK(cudaMemcpy(dfq, fq.data(), fq.size() * sizeof(float), cudaMemcpyHostToDevice), "table upload");
     CK(cudaMemcpy(df4, f4.data(), f4.size() * sizeof(float), cudaMemcpyHostToDevice), "table upload");
     CK(cudaMemcpy(df2, f2.data(), f2.size() * sizeof(float), cudaMemcpyHostToDevice), "table upload");
     if (eam) CK(cudaMemcpy(de2, e2.data(), e2.size() * sizeof(float), cudaMemcpyHostToDevice), "table upload");
@@ -536,6 +549,7 @@ extern "C" int msmgb_init_forcetable(msmgb_ctx *c, const msmgb_forcetable *ft)
     t.densff = (const float4 *)dfd;
     t.forceff = (const float4 *)dff8;
     t.embff = eam ? (const float4 *)dfe : nullptr;
+    t.densq = (const float4 *)dfq;
     {
         const double ir = 1.0 / t.rhod;
         t.irhodh = (float)ir;
@@ -1726,8 +1740,11 @@ extern "C" int msmgb_set_tuning(msmgb_ctx *c, const int *codes)
     const bool multi = c->tab.ngroup > 1;
     // density +128 (128-thread blocks) on the one-thread-per-atom families only
     const int d = codes[0];
-    const bool d_ok = d < 0 || in(d, valid_d, 15) || ((d & 128) && (d & ~128) < 32 && (d & 8) == 0 &&
-                                                       in(d & ~128, valid_d, 15));
+    // +256 (single kind): the table-assisted density pass, 2-5 in the low bits, +16, +128
+    const bool d_q = !multi && d >= 0 && (d & 256) && (d & ~(256 | 128 | 16 | 7)) == 0 && (d & 7) >= 2 &&
+                     (d & 7) <= 5;
+    const bool d_ok = d < 0 || d_q || in(d, valid_d, 15) ||
+                      ((d & 128) && (d & ~128) < 32 && (d & 8) == 0 && in(d & ~128, valid_d, 15));
     // fused: 0-23 (several kinds 0-3), + 32 for 0-17 (0-3) in 128-thread blocks
     const int u = codes[2];
     const bool u_ok = u < 0 || u < (multi ? 4 : 24) || (u >= 32 && u < 32 + (multi ? 4 : 18));

@@ -26,6 +26,8 @@
 // prefetch, batched gathers, TMA-streamed list tiles, shared-memory table windows) that
 // the autotuner times once per atom count.
 #include <algorithm>
+#include <cstdio>
+#include <cstdlib>
 
 #include <vector>
 
@@ -34,6 +36,13 @@
 namespace msmgb {
 
 constexpr unsigned kSkip = 0xffffffffu;     // pair beyond RU
+
+// MSMGB_TUNE_LOG=1: the autotuners print every variant's time per launch to stderr
+static bool tune_log()
+{
+    const char *v = getenv("MSMGB_TUNE_LOG");
+    return v && v[0] == '1';
+}
 constexpr int kDkBits = 18;
 constexpr float kDkScale = 262144.0f;       // 2^18
 constexpr float kDkInv = 1.0f / 262144.0f;
@@ -266,6 +275,193 @@ __global__ void __launch_bounds__(kBlock, MINB) k_density32(DevAtoms a, DevTable
     PosFF r = pi;
     r.d = d;
     st_ff(a.rec + i, r);
+}
+
+// ---- table-assisted density pass --------------------------------------------------------
+// The same pass as k_density32 (same pk codes, rho within FP32 rounding of the terms) with
+// fewer instructions per pair:
+//   * exact sum of squares: each hi part is rounded once more to a multiple of q, a power of
+//     two chosen so that every component of an accepted pair is below 2^11 q; the rounded hi
+//     differences dh are then exact multiples of q and dhx^2 + dhy^2 + dhz^2 is an integer
+//     times q^2 below 2^24 q^2, exact in FP32; the rest dl = u - hi(q) (below q) enters r^2 as
+//     C = sum dl (2 dh + dl), and r^2 = S + C as a float-float pair needs no two-sum;
+//   * the sqrt(r) index by one table row: SK0 = CSI rsqrt(rsqrt(r^2)) (FP32) gives the grid
+//     point k = int(SK0); the row holds r2_k = (k/CSI)^4 as float-float, and with
+//     D = r^2 - r2_k (exact difference) the fraction is
+//         DK = SK - k = (SK/(4 r^2)) D (1 + 3/8 D/r^2)  (Taylor expansion of SK(r^2) about r^2,
+//     third-order rest below 1e-6 of DK for k >= 1000, i.e. r > (1000/CSI)^2), instead of a
+//     Newton correction in float-float; the same row carries POTB(k) and its slope.
+// When FP32 rounding puts SK0 in the neighbouring segment, DK lands just outside [0, 1): the
+// pk code is then moved to the reference's segment (k -/+ 1), and rho takes the value of
+// segment k extended by at most 2e-3 of a step (a difference below 1e-8 of the term).
+struct QBox {
+    float lq[3], ll[3], half[3];    // box edge rounded to a multiple of q, and its rest
+    int pd;                         // periodic directions, bit k
+};
+
+__device__ __forceinline__ float qround(float h, float m)   // nearest multiple of q (m = 1.5 2^23 q)
+{
+    return __fsub_rn(__fadd_rn(h, m), m);
+}
+
+template <int POT, int UNR, int MINB, bool PF>
+__global__ void __launch_bounds__(kBlock, MINB) k_density32q(DevAtoms a, DevTables t, float qm, float rejs)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    const int kn = a.kvois[i];
+    unsigned *__restrict__ pk = a.pk + i;
+    const size_t ld = (size_t)a.ld;
+    if ((a.statu[i] & MSMGB_STATU_ACTIVE) != MSMGB_STATU_ACTIVE) {
+        a.den32[i] = 0.0f;
+        st_ff(a.rec + i, ld_ff(a.posff + i));
+        return;
+    }
+    const DevBox &bb = a.box[a.boxid[i]];
+    QBox b;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        b.lq[k] = qround(bb.lenf[k], qm);
+        b.ll[k] = __fadd_rn(__fsub_rn(bb.lenf[k], b.lq[k]), bb.lenlo[k]);
+        b.half[k] = bb.halff[k];
+    }
+    b.pd = (bb.ifpd[0] ? 1 : 0) | (bb.ifpd[1] ? 2 : 0) | (bb.ifpd[2] ? 4 : 0);
+    const PosFF pi = ld_ff(a.posff + i);
+    float ih[3], il[3];
+    {
+        const float h[3] = {pi.hx, pi.hy, pi.hz}, l[3] = {pi.lx, pi.ly, pi.lz};
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            ih[k] = qround(h[k], qm);
+            il[k] = __fadd_rn(__fsub_rn(h[k], ih[k]), l[k]);
+        }
+    }
+    const int *__restrict__ nb = a.indi + i;
+    const float4 *__restrict__ rows = t.densq;
+    KSum racc;
+    auto pair = [&](const PosFF &pj, unsigned &code) -> float {
+        const float h[3] = {pj.hx, pj.hy, pj.hz}, l[3] = {pj.lx, pj.ly, pj.lz};
+        float dh[3], dl[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const float hq = qround(h[k], qm);
+            dh[k] = ih[k] - hq;                                   // exact multiple of q
+            dl[k] = il[k] - __fadd_rn(__fsub_rn(h[k], hq), l[k]);
+            if (((b.pd >> k) & 1) && fabsf(dh[k]) > b.half[k]) {
+                const float sg = copysignf(1.0f, dh[k]);
+                dh[k] = fmaf(-sg, b.lq[k], dh[k]);                // exact
+                dl[k] = fmaf(-sg, b.ll[k], dl[k]);
+            }
+        }
+        const float S = fmaf(dh[0], dh[0], fmaf(dh[1], dh[1], dh[2] * dh[2]));   // exact
+        code = kSkip;
+        if (S > rejs) return 0.0f;
+        const float C = fmaf(dl[0], fmaf(2.0f, dh[0], dl[0]),
+                             fmaf(dl[1], fmaf(2.0f, dh[1], dl[1]), dl[2] * fmaf(2.0f, dh[2], dl[2])));
+        const float r2h = S + C;
+        const float r2l = C - (r2h - S);
+        if (r2h > t.ru2h || (r2h == t.ru2h && r2l > t.ru2l)) return 0.0f;
+        const float ti = rsqrtf(r2h);
+        const float sk0 = t.csih * rsqrtf(ti);
+        int kk = min(max((int)sk0, 1), t.ntab);
+        const float4 e = __ldg(rows + kk);
+        const float d = (r2h - e.z) + (r2l - e.w);
+        const float x = d * (ti * ti);
+        float dk = 0.25f * sk0 * x * fmaf(0.375f, x, 1.0f);
+        const float v = fmaf(dk, e.y, e.x);
+        if (dk < 0.0f) { kk -= 1; dk += 1.0f; }
+        else if (dk >= 1.0f) { kk += 1; dk -= 1.0f; }
+        kk = min(max(kk, 0), t.ntab);
+        dk = fminf(fmaxf(dk, 0.0f), 1.0f);
+        const unsigned q = (unsigned)fminf(fmaf(dk, kDkScale, 0.5f), kDkScale - 1.0f);
+        code = ((unsigned)kk << kDkBits) | q;
+        return v;
+    };
+    if (PF) {
+        int jn[UNR];
+#pragma unroll
+        for (int u = 0; u < UNR; ++u) jn[u] = u < kn ? __ldg(nb + u * ld) : -1;
+        for (int w = 0; w < kn; w += UNR) {
+            int j[UNR];
+#pragma unroll
+            for (int u = 0; u < UNR; ++u) j[u] = jn[u];
+#pragma unroll
+            for (int u = 0; u < UNR; ++u) {
+                const int sl = w + UNR + u;
+                jn[u] = sl < kn ? __ldg(nb + sl * ld) : -1;
+            }
+            PosFF p[UNR];
+#pragma unroll
+            for (int u = 0; u < UNR; ++u) p[u] = ld_ff(a.posff + (j[u] >= 0 ? j[u] : i));
+#pragma unroll
+            for (int u = 0; u < UNR; ++u) {
+                unsigned c;
+                const float v = pair(p[u], c);
+                if (j[u] >= 0) {
+                    pk[(w + u) * ld] = c;
+                    if (c != kSkip) racc.add(v);
+                }
+            }
+        }
+    } else {
+        int w = 0;
+        for (; w + UNR <= kn; w += UNR) {
+            int j[UNR];
+            PosFF p[UNR];
+#pragma unroll
+            for (int u = 0; u < UNR; ++u) j[u] = __ldg(nb + (w + u) * ld);
+#pragma unroll
+            for (int u = 0; u < UNR; ++u) p[u] = ld_ff(a.posff + j[u]);
+#pragma unroll
+            for (int u = 0; u < UNR; ++u) {
+                unsigned c;
+                const float v = pair(p[u], c);
+                pk[(w + u) * ld] = c;
+                if (c != kSkip) racc.add(v);
+            }
+        }
+        for (; w < kn; ++w) {
+            unsigned c;
+            const float v = pair(ld_ff(a.posff + __ldg(nb + w * ld)), c);
+            pk[w * ld] = c;
+            if (c != kSkip) racc.add(v);
+        }
+    }
+    const float rho = racc.value();
+    float d = rho;
+    if (POT == MSMGB_FS_TYPE) {
+        if (rho > 0.0f) d = -0.5f * rsqrtf(rho);
+    } else if (rho > 0.0f) {
+        const float sk = rho / t.rhodf + 1.0f;
+        int kk = (int)(sk + 0.000001f);
+        if (kk + 1 > t.nembd) {
+            atomicOr(&a.flags[kFlagErr], kErrRho);
+            kk = t.nembd;
+        }
+        const float2 e = __ldg(t.embd2 + kk);
+        d = fmaf(sk - (float)kk, e.y, e.x);
+    }
+    a.den32[i] = d;
+    PosFF r = pi;
+    r.d = d;
+    st_ff(a.rec + i, r);
+}
+
+// Quantum of the table-assisted density pass for the current tables and boxes: the smallest
+// power of two q such that 3 (RU + 0.05)^2 < (2^12 q)^2 (the exact sum of squares of an
+// accepted pair, whose components stay below RU + 1.5 q) and that every shifted coordinate
+// u = x - lo + L < 2L lies below 2^22 q (hi + 1.5 2^23 q then rounds hi to a multiple of q).
+// rejs bounds S of an accepted pair: r^2 - S = C, |C| <= 3 sqrt(3) RU q + 7 q^2 (|dl| <= 1.5 q).
+static void density_q_params(const msmgb_ctx *c, float *qm, float *rejs)
+{
+    const double ru = std::sqrt(c->tab.ru2);
+    double ext = 0.0;
+    for (const DevBox &b : c->hbox)
+        for (int k = 0; k < 3; ++k) ext = std::max(ext, 2.0 * b.len[k]);
+    const double need = std::max((ru + 0.05) * std::sqrt(3.0) / 4096.0, ext / std::ldexp(1.0, 22));
+    const double q = std::ldexp(1.0, (int)std::ceil(std::log2(need)));
+    *qm = (float)(1.5 * std::ldexp(q, 23));
+    *rejs = (float)(c->tab.ru2 * (1.0 + 1e-5) + 3.0 * std::sqrt(3.0) * ru * q + 7.0 * q * q);
 }
 
 // FP32 separation for the force direction (dh exact, dl small)
@@ -592,7 +788,7 @@ template <int UNR, int MINB, int PF, bool MULTI = false>
 __global__ void __launch_bounds__(kBlock, MINB) k_force32_vv(DevAtoms a, DevTables t, double th)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    double dmax = 0.0;
+    float dmax = 0.0f;
     if (i < a.n) {
         const int stat = a.statu[i];
         KSum fx, fy, fz;
@@ -826,7 +1022,7 @@ __global__ void __launch_bounds__(kBlock, MINB) k_force32_vv_t(DevAtoms a, DevTa
     float4 *s_hi = s_halo, *s_lo = s_halo + cap;
     const bool tiled = stage_halo(a, a.rec, s_hi, s_lo, cap);
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    double dmax = 0.0;
+    float dmax = 0.0f;
     if (i < a.n) {
         const int stat = a.statu[i];
         KSum fx, fy, fz;
@@ -1028,7 +1224,7 @@ __global__ void __launch_bounds__(kBlock, 4)
         if (tid == 0) atomicOr(&a.flags[kFlagErr], kErrTimeout);
         return;
     }
-    double dmax = 0.0;
+    float dmax = 0.0f;
     if (in) {
         const double Fx = fx.value64(), Fy = fy.value64(), Fz = fz.value64();
         a.fx[i] = Fx;
@@ -1185,6 +1381,7 @@ int autotune_fused(msmgb_ctx *c)
         cudaEventSynchronize(e1);
         float ms = 0.f;
         cudaEventElapsedTime(&ms, e0, e1);
+        if (tune_log()) fprintf(stderr, "msmgb tune: n=%d fused variant %d: %.4f ms\n", c->n, code, ms / 3.0f);
         if (ms < best) { best = ms; bestc = code; }
     }
     c->tune_fused = bestc;
@@ -1230,6 +1427,22 @@ static void dens_variant(msmgb_ctx *c, int unr)
     const int bs = (unr & 128) ? 128 : kBlock;
     unr &= ~128;
     const int g = nblk(c->n, bs);
+    if (!MULTI && (unr & 256)) {      // table-assisted index (+16: list slots one batch ahead)
+        float qm, rejs;
+        density_q_params(c, &qm, &rejs);
+        const bool pf = (unr & 16) != 0;
+        switch (unr & 7) {
+        case 3: if (pf) k_density32q<POT, 2, 5, true><<<g, bs, 0, c->stream>>>(c->a, c->tab, qm, rejs);
+                else k_density32q<POT, 2, 5, false><<<g, bs, 0, c->stream>>>(c->a, c->tab, qm, rejs); break;
+        case 4: if (pf) k_density32q<POT, 4, 1, true><<<g, bs, 0, c->stream>>>(c->a, c->tab, qm, rejs);
+                else k_density32q<POT, 4, 1, false><<<g, bs, 0, c->stream>>>(c->a, c->tab, qm, rejs); break;
+        case 5: if (pf) k_density32q<POT, 4, 4, true><<<g, bs, 0, c->stream>>>(c->a, c->tab, qm, rejs);
+                else k_density32q<POT, 4, 4, false><<<g, bs, 0, c->stream>>>(c->a, c->tab, qm, rejs); break;
+        default: if (pf) k_density32q<POT, 2, 1, true><<<g, bs, 0, c->stream>>>(c->a, c->tab, qm, rejs);
+                 else k_density32q<POT, 2, 1, false><<<g, bs, 0, c->stream>>>(c->a, c->tab, qm, rejs); break;
+        }
+        return;
+    }
     if (!MULTI && (unr & 64)) {   // cell tiles: +16 the larger halo capacity
         const bool large = (unr & 16) != 0;
         if ((unr & 7) == 4) {
@@ -1351,19 +1564,27 @@ int autotune_mixed(msmgb_ctx *c)
     const bool single = c->tab.ngroup == 1;
     // +64 (density, single kind): cell tiles (+16: larger halo capacity)
     // +128: 128-thread blocks
-    const int dcands[19] = {1, 2, 4, 3, 5, 18, 20, 19, 21, 131, 133, 147, 149, 9, 10, 66, 68, 82, 84};
+    // +256 (single kind): table-assisted index (k_density32q), 2/4 in flight, registers capped
+    // for 5 (2 in flight) or 4 (4 in flight) blocks of 256 threads, prefetch, 128-thread blocks
+    std::vector<int> dc = {1, 2, 4, 3, 5, 18, 20, 19, 21, 131, 133, 147, 149};
+    if (single) {
+        dc.push_back(9);
+        dc.push_back(10);
+        if (enable_halo(c) == MSMGB_OK)
+            for (int v : {66, 68, 82, 84}) dc.push_back(v);
+        for (int v : {258, 259, 260, 261, 274, 275, 276, 277, 386, 387, 388, 389, 402, 403, 404, 405})
+            dc.push_back(v);
+    }
     const int fcands[15] = {1, 2, 4, 3, 5, 18, 20, 19, 21, 50, 52, 51, 53, 9, 10};
-    const int *cands = dcands;
-    const bool tiles = single && enable_halo(c) == MSMGB_OK;
-    int ncand = single ? (tiles ? 19 : 15) : 13;
+    const bool log = tune_log();
     cudaEvent_t e0, e1;
     cudaError_t err = cudaEventCreate(&e0);
     if (err == cudaSuccess) err = cudaEventCreate(&e1);
     if (err != cudaSuccess) return cuda_err(c, err, "autotune events");
     float best_d = 1e30f, best_f = 1e30f;
     int bd = 2, bf = 2;
-    for (int k = 0; k < ncand; ++k) {
-        c->tune_dens_unroll = cands[k];
+    for (int code : dc) {
+        c->tune_dens_unroll = code;
         for (int r = 0; r < 4; ++r) {
             if (r == 1) cudaEventRecord(e0, c->stream);
             int rc = launch_density32(c);
@@ -1373,15 +1594,15 @@ int autotune_mixed(msmgb_ctx *c)
         cudaEventSynchronize(e1);
         float ms = 0.f;
         cudaEventElapsedTime(&ms, e0, e1);
-        if (ms < best_d) { best_d = ms; bd = cands[k]; }
+        if (log) fprintf(stderr, "msmgb tune: n=%d density variant %d: %.4f ms\n", c->n, code, ms / 3.0f);
+        if (ms < best_d) { best_d = ms; bd = code; }
     }
     c->tune_dens_unroll = bd;
     int rc = launch_density32(c);
     if (rc) return rc;
-    cands = fcands;
-    ncand = single ? 15 : 9;
+    const int ncand = single ? 15 : 9;
     for (int k = 0; k < ncand; ++k) {
-        c->tune_force_unroll = cands[k];
+        c->tune_force_unroll = fcands[k];
         for (int r = 0; r < 4; ++r) {
             if (r == 1) cudaEventRecord(e0, c->stream);
             rc = launch_force32(c);
@@ -1391,7 +1612,8 @@ int autotune_mixed(msmgb_ctx *c)
         cudaEventSynchronize(e1);
         float ms = 0.f;
         cudaEventElapsedTime(&ms, e0, e1);
-        if (ms < best_f) { best_f = ms; bf = cands[k]; }
+        if (log) fprintf(stderr, "msmgb tune: n=%d force variant %d: %.4f ms\n", c->n, fcands[k], ms / 3.0f);
+        if (ms < best_f) { best_f = ms; bf = fcands[k]; }
     }
     c->tune_force_unroll = bf;
     c->tune_ms[0] = best_d / 3.0f;

@@ -368,7 +368,7 @@ template <bool MULTI>
 __global__ void __launch_bounds__(kBlock) k_force_ff_vv(DevAtoms a, DevTables t, double th)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    double dmax = 0.0;
+    float dmax = 0.0f;
     if (i < a.n) {
         const int stat = a.statu[i];
         ff F[3] = {{0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}};

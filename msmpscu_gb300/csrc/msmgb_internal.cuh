@@ -122,6 +122,9 @@ struct DevTables {
     const float4 *densff;          // [nkind][ntp] POTB
     const float4 *forceff;         // [nkind][ntp][2] FPOTR, FPOTB
     const float4 *embff;           // [nkind1][nep] DFEMBD
+    // table-assisted index of the mixed density pass: per kind and grid point k
+    // {POTB(k), POTB(k+1) - POTB(k), hi and lo of r2_k = (k/CSI)^4}
+    const float4 *densq;           // [nkind][ntp]
     float irhodh, irhodl;          // 1 / RHOD as float-float
     float csih, csil;              // CSI as float-float
     float ru2h, ru2l;              // RU^2 as float-float
@@ -242,7 +245,7 @@ __device__ __forceinline__ double advance(double x0, double v, double a, double 
 // Corrector of step n (v += h/2 F/m) followed by the predictor of step n+1 for one active
 // atom (Correction_KERNEL :741-749 then Predictor_KERNEL0 :290-378); positions are read from
 // pin and written to pout / fout.  Returns the squared displacement since the last build.
-__device__ __forceinline__ double vv_atom(const DevAtoms &a, int i, int stat, const DevBox &b, double th,
+__device__ __forceinline__ float vv_atom(const DevAtoms &a, int i, int stat, const DevBox &b, double th,
                                           bool corrector, double fx, double fy, double fz,
                                           const double4_32a &p, double4_32a *pout, PosFF *fout)
 {
@@ -284,7 +287,25 @@ __device__ __forceinline__ double vv_atom(const DevAtoms &a, int i, int stat, co
     const float ex = mi32f(f.hx - q.x, b.lenf[0], b.halff[0], b.ifpd[0]);
     const float ey = mi32f(f.hy - q.y, b.lenf[1], b.halff[1], b.ifpd[1]);
     const float ez = mi32f(f.hz - q.z, b.lenf[2], b.halff[2], b.ifpd[2]);
-    return (double)(ex * ex + ey * ey + ez * ez);
+    return ex * ex + ey * ey + ez * ez;
+}
+
+// block max of a non-negative float (reduced in FP32, off the FP64 pipe), one atomicMax on
+// the bit pattern of its double per block
+__device__ __forceinline__ void block_max_flush(float v, unsigned long long *dst)
+{
+    __shared__ float smf[32];
+    const unsigned full = 0xffffffffu;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_down_sync(full, v, o));
+    if ((threadIdx.x & 31) == 0) smf[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float m = smf[0];
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) m = fmaxf(m, smf[w]);
+        // non-negative doubles order like their bit patterns
+        if (m > 0.0f) atomicMax(dst, (unsigned long long)__double_as_longlong((double)m));
+    }
 }
 
 // block max of a non-negative double, one atomicMax (on its bit pattern) per block

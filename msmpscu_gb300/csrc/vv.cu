@@ -22,7 +22,7 @@ namespace msmgb {
 __global__ void __launch_bounds__(kBlock) k_vv(DevAtoms a, double th, int mode)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    double dmax = 0.0;
+    float dmax = 0.0f;
     const int pend = (mode == 2) ? 1 : (mode == 1 ? a.flags[kFlagPending] : 0);
     if (i < a.n) {
         const int stat = a.statu[i];
