@@ -176,6 +176,16 @@ def batched_uneven_boxes(steps, steps_perbox, device=0):
     out = {"boxes": len(boxes), "atoms": int(len(pos)),
            "box_atoms_min": int(min(len(b[0]) for b in boxes)),
            "box_atoms_max": int(max(len(b[0]) for b in boxes))}
+
+    def wall(e, k):
+        """host wall clock around k steps (enqueued, then finished; device synchronised on
+        both sides): the clock the per-box contexts are timed with"""
+        e.synchronize()
+        t0 = time.perf_counter()
+        e.enqueue_steps(k, DT)
+        e.finish_steps(DT)
+        return time.perf_counter() - t0
+
     for prec in ("mixed", "ff", "fp64"):
         e = Engine(len(pos), lt.CU_RC_NL, max_boxes=len(boxes), mxkvois=MXKVOIS, skin_trigger=0.15,
                    precision=prec, device=device)
@@ -183,12 +193,22 @@ def batched_uneven_boxes(steps, steps_perbox, device=0):
         e.set_masses([lt.CU_MASS])
         e.copyin(desc, pos, vel)
         e.run_steps(3, DT)
-        l0 = e.launches
+        l0, g0 = e.launches, e.graph_launches
         ms, reb = e.time_steps(steps, DT)
         out["batched_%s_box_steps_per_s" % prec] = len(boxes) * steps / (ms / 1e3)
         out["batched_%s_atom_steps_per_s" % prec] = len(pos) * steps / (ms / 1e3)
         out["batched_%s_ms_per_step" % prec] = ms / steps
         out["batched_%s_launches_per_step" % prec] = (e.launches - l0) / steps
+        out["batched_%s_graph_launches_per_step" % prec] = (e.graph_launches - g0) / steps
+        if prec == "mixed":
+            out["batched_mixed_wall_box_steps_per_s"] = len(boxes) * steps_perbox / wall(e, steps_perbox)
+            # ten steps per graph launch
+            e.set_steps_per_graph(10)
+            e.run_steps(10, DT)
+            g0 = e.graph_launches
+            t = wall(e, steps_perbox)
+            out["batched_mixed_k10_wall_box_steps_per_s"] = len(boxes) * steps_perbox / t
+            out["batched_mixed_k10_graph_launches_per_step"] = (e.graph_launches - g0) / steps_perbox
         e.close()
     engines = []
     for (p, v, L), d in zip(boxes, desc):
@@ -210,8 +230,14 @@ def batched_uneven_boxes(steps, steps_perbox, device=0):
     for e in engines:
         e.close()
     out["perbox_mixed_box_steps_per_s"] = len(boxes) * steps_perbox / (t1 - t0)
-    out["batched_vs_perbox"] = out["batched_mixed_box_steps_per_s"] / out["perbox_mixed_box_steps_per_s"]
-    out["perbox_timing"] = "host wall clock around %d steps of 512 contexts (device synchronised both sides)" % steps_perbox
+    out["perbox_graph_launches_per_step"] = len(boxes)
+    # both sides on the host wall clock (the device-time figure is kept beside it)
+    out["batched_vs_perbox"] = out["batched_mixed_wall_box_steps_per_s"] / out["perbox_mixed_box_steps_per_s"]
+    out["batched_vs_perbox_device_vs_wall"] = (out["batched_mixed_box_steps_per_s"] /
+                                               out["perbox_mixed_box_steps_per_s"])
+    out["batched_k10_vs_perbox"] = out["batched_mixed_k10_wall_box_steps_per_s"] / out["perbox_mixed_box_steps_per_s"]
+    out["perbox_timing"] = ("host wall clock around %d steps of 512 contexts and around %d steps of the "
+                            "batched context (device synchronised both sides)" % (steps_perbox, steps_perbox))
     return out
 
 

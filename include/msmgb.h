@@ -216,6 +216,14 @@ int  msmgb_time_passes(msmgb_ctx *ctx, int reps, float *out);
  * time per launch.  Tuning runs at the first mixed force call / step graph for a given
  * atom count. */
 int  msmgb_get_tuning(const msmgb_ctx *ctx, int *out, float *ms);
+/* Number of MD steps captured into one CUDA graph (1..64, default 1): msmgb_run_steps and
+ * msmgb_enqueue_steps then launch one graph per k steps (the rest one per step), each step
+ * keeping its own device-decided rebuild; the step graphs are rebuilt at the next call.  Fewer
+ * host launches per step for small systems and batches of small boxes.  No counterpart in the
+ * reference (it launches every kernel of a step from the host, MD_Method_GenericMD_GPU.F90:596-627). */
+int  msmgb_set_steps_per_graph(msmgb_ctx *ctx, int k);
+/* Graph launches issued by MD steps since the context was created. */
+int  msmgb_graph_launch_count(const msmgb_ctx *ctx, int64_t *n);
 /* Pins the kernel variants of the mixed passes (codes as returned by msmgb_get_tuning:
  * codes[0] density, codes[1] force, codes[2] fused step kernel; a negative code leaves that
  * choice to the tuner).  Pinned choices are kept for the context's atom count and skip the
@@ -257,6 +265,37 @@ int  msmgb_list_stats(msmgb_ctx *ctx, int *maxk, double *meank);
  * most 8192 atoms in at most 256 runs), mean and largest halo size over those.  All zero
  * when no tiles are built.  No counterpart in the reference. */
 int  msmgb_tile_stats(msmgb_ctx *ctx, int *blocks, int *tiled, double *mean_halo, int *max_halo);
+
+/* ---- external forces (AddExtForce_ForceClass0 / ClearExtForce_ForceClass0 and
+ *      Cumulate_ExtForce0, MD_ForceClass_Register_GPU.F90:584-606, 636-656, 982-1180) -------- */
+/* What an external-force routine sees: the context's stream, the atoms in the library's
+ * sorted device order and the force arrays to add to.  All pointers are device memory. */
+typedef struct {
+    int           n;          /* atoms                                                        */
+    int           nbox;       /* boxes                                                        */
+    void         *stream;     /* cudaStream_t: enqueue the work here, do not synchronise      */
+    const double *pos;        /* positions, 4 doubles per atom (x, y, z, unused)              */
+    double       *fx, *fy, *fz;   /* forces of the force pass just done: add to them          */
+    const int    *gid;        /* caller (original) index of each sorted atom                  */
+    const int    *ityp, *statu, *boxid;
+} msmgb_extforce_view;
+/* An external force routine (the reference's pForce procedure of an MDExtForceList entry):
+ * returns 0, or a nonzero code that fails the force call with MSMGB_ERR_ARG. */
+typedef int (*msmgb_extforce_fn)(void *user, const msmgb_extforce_view *view);
+/* Registers fn (with its tag and user pointer) to run after every force pass, in the order of
+ * registration, as Calforce_ForceClass0 runs Cumulate_ExtForce0 after pCalForce.  Inside MD
+ * steps the step runs unfused (integrator, density pass, force pass, external forces) and is
+ * a CUDA graph: fn is called while the step graph is built, so the device work it enqueues
+ * on view->stream is replayed every step; its pointers must stay valid and it must not
+ * synchronise.  HVP and adjoint calls add no external forces. */
+int  msmgb_add_extforce(msmgb_ctx *ctx, const char *tag, msmgb_extforce_fn fn, void *user);
+/* ClearExtForce_ForceClass0: removes every registered routine and the field below. */
+int  msmgb_clear_extforce(msmgb_ctx *ctx);
+/* A constant external force per atom, fext = XP(N,3) layout in the caller's order (host or
+ * device memory, copied), added to every active atom after each force pass (a built-in
+ * external-force routine: fields, springs held fixed over a run, boosts); NULL removes it.
+ * It applies to the current atom count; a copy-in with a different count removes it. */
+int  msmgb_set_extforce_field(msmgb_ctx *ctx, const double *fext);
 
 /* ---- differentiation --------------------------------------------------------------------- */
 /* Device time of one Hessian-vector product and of one FP64 force call (density + force

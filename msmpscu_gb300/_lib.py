@@ -63,6 +63,15 @@ class ForceNoAlloc(C.Structure):
                 ("stream", C.c_void_p), ("errbuf", C.c_char_p), ("errlen", C.c_int)]
 
 
+class ExtForceView(C.Structure):
+    _fields_ = [("n", C.c_int), ("nbox", C.c_int), ("stream", C.c_void_p), ("pos", C.c_void_p),
+                ("fx", C.c_void_p), ("fy", C.c_void_p), ("fz", C.c_void_p), ("gid", C.c_void_p),
+                ("ityp", C.c_void_p), ("statu", C.c_void_p), ("boxid", C.c_void_p)]
+
+
+EXTFORCE_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.POINTER(ExtForceView))
+
+
 # (name, restype, argtypes) of every exported entry point
 SIGNATURES = [
     ("msmgb_create", C.c_int, [C.POINTER(C.c_void_p), C.POINTER(Params)]),
@@ -126,6 +135,11 @@ SIGNATURES = [
     ("msmgb_import_forcetable", C.c_int, [C.c_char_p, C.c_int, C.c_int, _ip, C.c_double, C.c_int, C.c_int,
                                           _dp, _dp, _dp, _dp, _dp, _dp, _ip, _ip, _ip, _ip, _dp, _ip]),
     ("msmgb_export_forcetable", C.c_int, [C.c_char_p, C.c_int, C.POINTER(ForceTable), _ip, _ip]),
+    ("msmgb_set_steps_per_graph", C.c_int, [C.c_void_p, C.c_int]),
+    ("msmgb_graph_launch_count", C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),
+    ("msmgb_add_extforce", C.c_int, [C.c_void_p, C.c_char_p, EXTFORCE_FN, C.c_void_p]),
+    ("msmgb_clear_extforce", C.c_int, [C.c_void_p]),
+    ("msmgb_set_extforce_field", C.c_int, [C.c_void_p, C.c_void_p]),
 ]
 
 _lib = None

@@ -80,7 +80,8 @@ static void free_graph(msmgb_ctx *c)
     if (c->step_graph) cudaGraphExecDestroy(c->step_graph);
     c->step_graph = nullptr;
     c->graph_n = -1;
-    cudaGraphExec_t *gs[5] = {&c->g_pre, &c->g_loop[0], &c->g_loop[1], &c->g_final[0], &c->g_final[1]};
+    cudaGraphExec_t *gs[8] = {&c->g_pre,    &c->g_loop[0],  &c->g_loop[1],  &c->g_final[0],
+                              &c->g_final[1], &c->g_loopk[0], &c->g_loopk[1], &c->step_graphk};
     for (cudaGraphExec_t *g : gs) {
         if (*g) cudaGraphExecDestroy(*g);
         *g = nullptr;
@@ -306,7 +307,7 @@ extern "C" int msmgb_destroy(msmgb_ctx *c)
                     a.den32, a.kvois, a.indi, a.pk, a.rec, a.posfx, a.recfx, c->cell_of, c->perm, c->dbox, c->cm, c->icm,
                     c->flags, c->maxdisp, c->virial, c->scratch, c->cell_start,
                     c->cell_cursor, c->scan_tmp, c->cell_rank, c->cell_unrank, c->tab_mem, c->adj_mem, c->hvp_pair,
-                    c->pos2, c->posff2, a.lidx, a.hmeta, a.hruns, c->cand, c->kcand};
+                    c->pos2, c->posff2, a.lidx, a.hmeta, a.hruns, c->cand, c->kcand, c->ext_field};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     if (c->h_flags) cudaFreeHost(c->h_flags);
@@ -758,6 +759,12 @@ extern "C" int msmgb_copyin_simbox(msmgb_ctx *c, int nbox, const msmgb_box *boxe
     for (int b = 0; b < nbox; ++b)
         c->max_density = std::max(c->max_density, boxes[b].natom / (boxes[b].len[0] * boxes[b].len[1] * boxes[b].len[2]));
     c->nbox = nbox;
+    if (c->ext_field && c->ext_field_n != n) {     // the field belonged to another atom count
+        cudaFree(c->ext_field);
+        c->ext_field = nullptr;
+        c->ext_field_n = 0;
+        free_graph(c);
+    }
     c->n = n;
     c->a.n = n;
     c->boxes.assign(boxes, boxes + nbox);
@@ -887,6 +894,78 @@ extern "C" int msmgb_update_positions(msmgb_ctx *c, const double *xp)
     return MSMGB_OK;
 }
 
+// ---- several MD steps per graph launch ---------------------------------------------------------
+extern "C" int msmgb_set_steps_per_graph(msmgb_ctx *c, int k)
+{
+    if (!c || k < 1 || k > 64) return MSMGB_ERR_ARG;
+    if (k != c->steps_per_graph) {
+        c->steps_per_graph = k;
+        free_graph(c);
+    }
+    return MSMGB_OK;
+}
+
+extern "C" int msmgb_graph_launch_count(const msmgb_ctx *c, int64_t *n)
+{
+    if (!c || !n) return MSMGB_ERR_ARG;
+    *n = c->graph_launches;
+    return MSMGB_OK;
+}
+
+// ---- external forces ----------------------------------------------------------------------
+extern "C" int msmgb_add_extforce(msmgb_ctx *c, const char *tag, msmgb_extforce_fn fn, void *user)
+{
+    if (!c || !fn) return MSMGB_ERR_ARG;
+    c->ext.push_back({tag ? std::string(tag) : std::string(), fn, user});
+    free_graph(c);                 // the step graphs are rebuilt, unfused, with the routine
+    c->force_valid = false;
+    return MSMGB_OK;
+}
+
+extern "C" int msmgb_clear_extforce(msmgb_ctx *c)
+{
+    if (!c) return MSMGB_ERR_ARG;
+    c->ext.clear();
+    if (c->ext_field) {
+        RET(use_device(c));
+        CK(cudaStreamSynchronize(c->stream), "synchronize");
+        cudaFree(c->ext_field);
+        c->ext_field = nullptr;
+    }
+    c->ext_field_n = 0;
+    free_graph(c);
+    c->force_valid = false;
+    return MSMGB_OK;
+}
+
+extern "C" int msmgb_set_extforce_field(msmgb_ctx *c, const double *fext)
+{
+    NvtxRange nvtx_range("msmgb_set_extforce_field");
+    if (!c) return MSMGB_ERR_ARG;
+    RET(use_device(c));
+    if (!fext) {
+        if (c->ext_field) {
+            CK(cudaStreamSynchronize(c->stream), "synchronize");
+            cudaFree(c->ext_field);
+            c->ext_field = nullptr;
+        }
+        c->ext_field_n = 0;
+    } else {
+        RET(need_state(c));
+        if (!c->ext_field) {
+            CK(cudaStreamSynchronize(c->stream), "synchronize");
+            CK(cudaMalloc(&c->ext_field, sizeof(double) * 3 * (size_t)c->cap_atoms), "cudaMalloc external field");
+        }
+        CK(cudaMemcpyAsync(c->ext_field, fext, sizeof(double) * 3 * (size_t)c->n, cudaMemcpyDefault, c->stream),
+           "external field copy-in");
+        CK(cudaStreamSynchronize(c->stream), "synchronize");
+        c->ext_field_n = c->n;
+    }
+    free_graph(c);
+    c->force_valid = false;
+    return MSMGB_OK;
+}
+
 extern "C" int msmgb_copyout_force(msmgb_ctx *c, double *fp, int order)
 {
     NvtxRange nvtx_range("msmgb_copyout_force");
@@ -1004,6 +1083,49 @@ static int ready_for_force(msmgb_ctx *c)
     return MSMGB_OK;
 }
 
+// constant external force of every active atom, from the caller-order field (XP layout)
+__global__ void k_add_extfield(DevAtoms a, const double *f)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n || (a.statu[i] & MSMGB_STATU_ACTIVE) != MSMGB_STATU_ACTIVE) return;
+    const size_t g = (size_t)a.gid[i], n = (size_t)a.n;
+    a.fx[i] += f[g];
+    a.fy[i] += f[n + g];
+    a.fz[i] += f[2 * n + g];
+}
+
+// Cumulate_ExtForce0 (MD_ForceClass_Register_GPU.F90:584-606): the field, then every
+// registered routine in order, on the forces of the force pass just enqueued
+static int apply_extforces(msmgb_ctx *c)
+{
+    if (c->ext_field) {
+        if (c->ext_field_n != c->n)
+            return set_err(c, MSMGB_ERR_ARG, "the external force field was set for another atom count");
+        k_add_extfield<<<nblk(c->n, kBlock), kBlock, 0, c->stream>>>(c->a, c->ext_field);
+        c->launches += 1;
+        RET(check_launch(c, "external force field"));
+    }
+    for (const auto &x : c->ext) {
+        msmgb_extforce_view v;
+        v.n = c->n;
+        v.nbox = c->nbox;
+        v.stream = (void *)c->stream;
+        v.pos = (const double *)c->a.pos;
+        v.fx = c->a.fx;
+        v.fy = c->a.fy;
+        v.fz = c->a.fz;
+        v.gid = c->a.gid;
+        v.ityp = c->a.ityp;
+        v.statu = c->a.statu;
+        v.boxid = c->a.boxid;
+        const int rc = x.fn(x.user, &v);
+        if (rc != 0)
+            return set_err(c, MSMGB_ERR_ARG, "external force '" + x.tag + "' returned " + std::to_string(rc));
+        RET(check_launch(c, "external force routine"));
+    }
+    return MSMGB_OK;
+}
+
 static int force_passes(msmgb_ctx *c, bool virial, bool epot)
 {
     if (c->p.precision != MSMGB_PREC_FP64 && !virial && !epot) RET(need_cubic(c, "a reduced-precision force pass"));
@@ -1022,7 +1144,7 @@ static int force_passes(msmgb_ctx *c, bool virial, bool epot)
         RET(launch_density(c, epot));
         RET(launch_force(c, virial));
     }
-    return MSMGB_OK;
+    return apply_extforces(c);
 }
 
 extern "C" int msmgb_calforce(msmgb_ctx *c)
@@ -1221,6 +1343,67 @@ static int finish_step_graph(msmgb_ctx *c, int rc, cudaGraph_t g, const RebuildN
     return rc;
 }
 
+// k step bodies in one graph (msmgb_set_steps_per_graph): step s issues pre(s), the decision
+// kernel with its own IF nodes (a conditional handle belongs to one node) and post(s); the
+// rebuild bodies of step s work on the atom view view_after(s), the buffer step s leaves the
+// state in.  *kernels receives the kernels of the k bodies outside the rebuild bodies.
+template <class Pre, class Post, class View>
+static int capture_k_steps(msmgb_ctx *c, int k, Pre pre, Post post, View view_after, cudaGraphExec_t *out,
+                           int64_t *kernels)
+{
+    cudaGraph_t g = nullptr;
+    CK(cudaGraphCreate(&g, 0), "graph create");
+    std::vector<RebuildNodes> rn((size_t)k);
+    cudaError_t e = cudaSuccess;
+    for (int s = 0; s < k && e == cudaSuccess; ++s) {
+        e = cudaGraphConditionalHandleCreate(&rn[(size_t)s].cond, g, 0, cudaGraphCondAssignDefault);
+        if (e == cudaSuccess && two_level(c))
+            e = cudaGraphConditionalHandleCreate(&rn[(size_t)s].cond_inner, g, 0, cudaGraphCondAssignDefault);
+    }
+    if (e == cudaSuccess)
+        e = cudaStreamBeginCaptureToGraph(c->stream, g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) {
+        cudaGraphDestroy(g);
+        return cuda_err(c, e, "graph capture");
+    }
+    const DevAtoms base = c->a;
+    const int64_t l0 = c->launches;
+    int rc = MSMGB_OK;
+    for (int s = 0; s < k && !rc; ++s) {
+        rc = pre(s);
+        if (!rc) rc = launch_decide(c, c->p.skin_trigger, c->p.nb_uptab, rn[(size_t)s].cond, true,
+                                    rn[(size_t)s].cond_inner);
+        if (!rc) rc = add_rebuild_nodes(c, &rn[(size_t)s]);
+        if (!rc) rc = post(s);
+        c->a = base;
+    }
+    *kernels = c->launches - l0;
+    c->launches = l0;
+    cudaGraph_t ended = nullptr;
+    e = cudaStreamEndCapture(c->stream, &ended);
+    if (!rc && e != cudaSuccess) rc = cuda_err(c, e, "graph capture");
+    for (int s = 0; s < k && !rc; ++s) {
+        c->a = view_after(s);
+        c->gk_inner = 0;
+        if (rn[(size_t)s].body_inner) {
+            rc = fill_rebuild_body(c, rn[(size_t)s].body, 1, &c->gk_body);
+            if (!rc) rc = fill_rebuild_body(c, rn[(size_t)s].body_inner, 2, &c->gk_inner);
+        } else {
+            rc = fill_rebuild_body(c, rn[(size_t)s].body, 0, &c->gk_body);
+        }
+        c->a = base;
+    }
+    if (!rc) {
+        e = cudaGraphInstantiate(out, g, 0);
+        if (e != cudaSuccess) {
+            *out = nullptr;
+            rc = cuda_err(c, e, "graph instantiate");
+        }
+    }
+    cudaGraphDestroy(g);
+    return rc;
+}
+
 static int capture_step(msmgb_ctx *c, double h)
 {
     free_graph(c);
@@ -1236,6 +1419,13 @@ static int capture_step(msmgb_ctx *c, double h)
     RET(finish_step_graph(c, rc, g, rn, &c->step_graph, c->a));
     c->graph_kernels = nk;
     c->launches = l0;
+    if (c->steps_per_graph > 1) {
+        const DevAtoms base = c->a;
+        RET(capture_k_steps(
+            c, c->steps_per_graph, [&](int) { return launch_vv(c, h, 1); },
+            [&](int) { return force_passes(c, false, false); }, [&](int) { return base; }, &c->step_graphk,
+            &c->graph_kernels_k));
+    }
     c->graph_h = h;
     c->graph_prec = c->p.precision;
     c->graph_n = c->n;
@@ -1246,7 +1436,9 @@ static int capture_step(msmgb_ctx *c, double h)
 // ---- fused step: force pass + integrator in one kernel (mixed single species, float-float)
 static bool fused_mixed(const msmgb_ctx *c)
 {
-    return c->p.precision == MSMGB_PREC_MIXED || c->p.precision == MSMGB_PREC_FF;
+    // external forces go between the force pass and the corrector: the unfused step then
+    return (c->p.precision == MSMGB_PREC_MIXED || c->p.precision == MSMGB_PREC_FF) && c->ext.empty() &&
+           !c->ext_field;
 }
 
 static int step_density(msmgb_ctx *c)
@@ -1348,6 +1540,21 @@ static int capture_fused(msmgb_ctx *c, double h)
         RET(end_capture(c, rc, &c->g_final[p]));
         c->gk_final = c->launches - l0;
     }
+    if (c->steps_per_graph > 1) {
+        for (int p = 0; p < 2; ++p) {
+            rc = capture_k_steps(
+                c, c->steps_per_graph,
+                [&](int st) {
+                    c->a = atoms_on(c, base, (p + st) & 1);
+                    int r = step_density(c);
+                    return r ? r : step_force_vv(c, h);
+                },
+                [&](int) { return MSMGB_OK; }, [&](int st) { return atoms_on(c, base, 1 - ((p + st) & 1)); },
+                &c->g_loopk[p], &c->gk_loopk);
+            c->a = base;
+            RET(rc);
+        }
+    }
     c->launches = l_start;            // capturing launches nothing; graph launches are counted
     c->fg_h = h;
     c->fg_n = c->n;
@@ -1399,23 +1606,43 @@ extern "C" int msmgb_rebuild_counts(const msmgb_ctx *c, int64_t *rebuilds, int64
 static int issue_steps(msmgb_ctx *c, int nsteps, double h)
 {
     if (nsteps <= 0) return MSMGB_OK;
+    const int k = c->steps_per_graph;
     if (!fused_mixed(c)) {
-        for (int s = 0; s < nsteps; ++s) {
-            CK(cudaGraphLaunch(c->step_graph, c->stream), "graph launch");
-            c->launches += c->graph_kernels;
+        for (int s = 0; s < nsteps;) {
+            if (k > 1 && c->step_graphk && nsteps - s >= k) {
+                CK(cudaGraphLaunch(c->step_graphk, c->stream), "graph launch");
+                c->launches += c->graph_kernels_k;
+                s += k;
+            } else {
+                CK(cudaGraphLaunch(c->step_graph, c->stream), "graph launch");
+                c->launches += c->graph_kernels;
+                ++s;
+            }
+            ++c->graph_launches;
         }
         return MSMGB_OK;
     }
     CK(cudaGraphLaunch(c->g_pre, c->stream), "graph launch");
     c->launches += c->gk_pre;
+    ++c->graph_launches;
     int p = 0;
-    for (int s = 1; s < nsteps; ++s) {
-        CK(cudaGraphLaunch(c->g_loop[p], c->stream), "graph launch");
-        c->launches += c->gk_loop;
-        p ^= 1;
+    for (int s = 1; s < nsteps;) {
+        if (k > 1 && c->g_loopk[p] && nsteps - s >= k) {
+            CK(cudaGraphLaunch(c->g_loopk[p], c->stream), "graph launch");
+            c->launches += c->gk_loopk;
+            s += k;
+            p = (p + k) & 1;
+        } else {
+            CK(cudaGraphLaunch(c->g_loop[p], c->stream), "graph launch");
+            c->launches += c->gk_loop;
+            p ^= 1;
+            ++s;
+        }
+        ++c->graph_launches;
     }
     CK(cudaGraphLaunch(c->g_final[p], c->stream), "graph launch");
     c->launches += c->gk_final;
+    ++c->graph_launches;
     if (p) {   // the state ended in the second buffer: bring it back to the primary one
         CK(cudaMemcpyAsync(c->a.pos, c->pos2, sizeof(double4_32a) * (size_t)c->n, cudaMemcpyDeviceToDevice,
                            c->stream), "position copy");

@@ -381,6 +381,16 @@ struct msmgb_ctx {
     bool have_tables = false;
     bool have_masses = false;
 
+    // external forces added after every force pass (Cumulate_ExtForce0)
+    struct ExtForce {
+        std::string tag;
+        msmgb_extforce_fn fn;
+        void *user;
+    };
+    std::vector<ExtForce> ext;         // registered routines, in order
+    double *ext_field = nullptr;       // constant per-atom force, XP(N,3) caller order
+    int ext_field_n = 0;               // atom count the field was given for
+
     bool list_valid = false;
     bool force_valid = false;
     bool den_is32 = false;             // the last density pass was the mixed one
@@ -400,6 +410,12 @@ struct msmgb_ctx {
     msmgb::PosFF *posff2 = nullptr;
     cudaGraphExec_t g_pre = nullptr, g_loop[2] = {nullptr, nullptr}, g_final[2] = {nullptr, nullptr};
     int64_t gk_pre = 0, gk_loop = 0, gk_final = 0;
+    // several steps per graph launch (msmgb_set_steps_per_graph): k step bodies in one graph
+    int steps_per_graph = 1;
+    cudaGraphExec_t g_loopk[2] = {nullptr, nullptr};   // fused path, first step on buffer p
+    cudaGraphExec_t step_graphk = nullptr;             // unfused path
+    int64_t gk_loopk = 0, graph_kernels_k = 0;
+    int64_t graph_launches = 0;                        // graph launches issued by MD steps
     int64_t gk_body = 0;         // kernels of the conditional rebuild body of a step graph
     int64_t gk_inner = 0;        // two-level list: kernels of the body that runs on every rebuild
     int64_t step_rebuilds = 0, step_full = 0;   // list rebuilds inside MD steps, and the full ones

@@ -535,6 +535,36 @@ class Engine:
             xp = np.ascontiguousarray(np.asarray(x, np.float64).T).reshape(-1)
             self._ck(self.lib.msmgb_update_positions(self.ctx, xp.ctypes.data_as(C.c_void_p)))
 
+    def set_steps_per_graph(self, k):
+        """MD steps captured into one CUDA graph launch (1..64)."""
+        self._ck(self.lib.msmgb_set_steps_per_graph(self.ctx, int(k)))
+
+    @property
+    def graph_launches(self):
+        n = C.c_int64()
+        self._ck(self.lib.msmgb_graph_launch_count(self.ctx, C.byref(n)))
+        return n.value
+
+    def set_extforce_field(self, fext):
+        """Constant external force per atom ((N, 3), caller order), added after every force
+        pass (None removes it); MD steps then run unfused."""
+        if fext is None:
+            self._ck(self.lib.msmgb_set_extforce_field(self.ctx, None))
+            return
+        f = np.ascontiguousarray(np.asarray(fext, np.float64).T).reshape(-1)
+        self._ck(self.lib.msmgb_set_extforce_field(self.ctx, f.ctypes.data_as(C.c_void_p)))
+
+    def add_extforce(self, tag, fn):
+        """Registers fn(view) -> int, called after every force pass with an ExtForceView of
+        device pointers (msmgb.h); the ctypes callback is kept alive by the engine."""
+        cb = L.EXTFORCE_FN(lambda user, view: int(fn(view.contents)))
+        self._ext_cbs = getattr(self, "_ext_cbs", []) + [cb]
+        self._ck(self.lib.msmgb_add_extforce(self.ctx, tag.encode(), cb, None))
+
+    def clear_extforce(self):
+        self._ck(self.lib.msmgb_clear_extforce(self.ctx))
+        self._ext_cbs = []
+
     def set_masses(self, cm):
         cm = np.ascontiguousarray(np.atleast_1d(cm), dtype=np.float64)
         self._ck(self.lib.msmgb_set_masses(self.ctx, int(cm.size), _d(cm)))

@@ -1097,10 +1097,33 @@ void orc_corrector(int n, double *vx, double *vy, double *vz, const double *fx, 
     }
 }
 
+/* external force fext (3n, x block then y then z; may be NULL) added to every active atom
+ * after each force evaluation, as Calforce_ForceClass0 runs Cumulate_ExtForce0 after pCalForce
+ * (MD_ForceClass_Register_GPU.F90:584-606, 636-656) */
+static void add_ext(int n, const double *fext, const int *statu, double *fx, double *fy, double *fz)
+{
+    if (!fext) return;
+    for (int i = 0; i < n; ++i) {
+        if ((statu[i] & 1) != 1) continue;
+        fx[i] += fext[i];
+        fy[i] += fext[n + i];
+        fz[i] += fext[2 * n + i];
+    }
+}
+
 int orc_md(int n, double *x, double *y, double *z, double *vx, double *vy, double *vz,
            double *fx, double *fy, double *fz, int *statu, const int *ityp, const orc_box *box,
            const orc_tables *t, const double *cm, double h, int nsteps, double rc_nl,
            double skin_trigger, int nb_uptab, int mxkvois, int nthreads)
+{
+    return orc_md_ext(n, x, y, z, vx, vy, vz, fx, fy, fz, statu, ityp, box, t, cm, h, nsteps, rc_nl,
+                      skin_trigger, nb_uptab, mxkvois, nthreads, NULL);
+}
+
+int orc_md_ext(int n, double *x, double *y, double *z, double *vx, double *vy, double *vz,
+               double *fx, double *fy, double *fz, int *statu, const int *ityp, const orc_box *box,
+               const orc_tables *t, const double *cm, double h, int nsteps, double rc_nl,
+               double skin_trigger, int nb_uptab, int mxkvois, int nthreads, const double *fext)
 {
 #ifdef _OPENMP
     if (nthreads > 0) omp_set_num_threads(nthreads);
@@ -1113,6 +1136,7 @@ int orc_md(int n, double *x, double *y, double *z, double *vx, double *vy, doubl
     rc = orc_nlist(n, x, y, z, statu, box, rc_nl, mxkvois, kvois, indi, NULL);
     if (rc) goto done;
     orc_force(n, x, y, z, ityp, statu, box, kvois, indi, n, t, NULL, fx, fy, fz, NULL, NULL, nthreads);
+    add_ext(n, fext, statu, fx, fy, fz);
     for (int step = 1; step <= nsteps; ++step) {
         orc_predictor(n, x, y, z, vx, vy, vz, fx, fy, fz, dsb, dsb + nn, dsb + 2 * nn, statu, ityp, cm, h, box);
         int rebuild = 0;
@@ -1133,6 +1157,7 @@ int orc_md(int n, double *x, double *y, double *z, double *vx, double *vy, doubl
             ++rebuilds;
         }
         orc_force(n, x, y, z, ityp, statu, box, kvois, indi, n, t, NULL, fx, fy, fz, NULL, NULL, nthreads);
+        add_ext(n, fext, statu, fx, fy, fz);
         orc_corrector(n, vx, vy, vz, fx, fy, fz, statu, ityp, cm, h);
     }
     rc = rebuilds;

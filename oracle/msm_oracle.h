@@ -167,6 +167,12 @@ int  orc_md(int n, double *x, double *y, double *z, double *vx, double *vy, doub
             double *fx, double *fy, double *fz, int *statu, const int *ityp, const orc_box *box,
             const orc_tables *t, const double *cm, double h, int nsteps, double rc_nl,
             double skin_trigger, int nb_uptab, int mxkvois, int nthreads);
+/* orc_md with an external force fext (3n: x block, y block, z block; NULL for none) added to
+ * every active atom after each force evaluation (Cumulate_ExtForce0) */
+int  orc_md_ext(int n, double *x, double *y, double *z, double *vx, double *vy, double *vz,
+                double *fx, double *fy, double *fz, int *statu, const int *ityp, const orc_box *box,
+                const orc_tables *t, const double *cm, double h, int nsteps, double rc_nl,
+                double skin_trigger, int nb_uptab, int mxkvois, int nthreads, const double *fext);
 
 /* Hessian-vector product of the table-mode force: hv = -dF/dx . v, with the exact
  * derivative of the piecewise-linear interpolants. */

@@ -51,6 +51,7 @@ def lib():
         _lib.orc_nlist_brute.restype = C.c_int
         _lib.orc_force.restype = C.c_int
         _lib.orc_md.restype = C.c_int
+        _lib.orc_md_ext.restype = C.c_int
         _lib.orc_hvp.restype = C.c_int
         _lib.orc_adjoint_cr.restype = C.c_int
         _lib.orc_atomic_stress.restype = None
@@ -472,8 +473,9 @@ def hvp(pos, ityp, statu, box, kvois, indi, tables, v, nthreads=0):
 
 
 def md(pos, vel, ityp, statu, box, tables, cm, h, nsteps, rc_nl, skin_trigger=0.0, nb_uptab=10,
-       mxkvois=128, nthreads=0):
-    """Runs the NVE loop in place on copies; returns (pos, vel, force, statu, rebuilds)."""
+       mxkvois=128, nthreads=0, fext=None):
+    """Runs the NVE loop in place on copies; returns (pos, vel, force, statu, rebuilds).
+    fext (N, 3): external force added to every active atom after each force evaluation."""
     n = pos.shape[0]
     x, y, z = (f64(pos[:, k]).copy() for k in range(3))
     vx, vy, vz = (f64(vel[:, k]).copy() for k in range(3))
@@ -481,10 +483,11 @@ def md(pos, vel, ityp, statu, box, tables, cm, h, nsteps, rc_nl, skin_trigger=0.
     st = i32(statu).copy()
     ty = i32(ityp)
     cmv = f64(cm)
-    rc = lib().orc_md(n, _d(x), _d(y), _d(z), _d(vx), _d(vy), _d(vz), _d(fx), _d(fy), _d(fz),
-                      _i(st), _i(ty), C.byref(box), C.byref(tables.s), _d(cmv), C.c_double(h),
-                      nsteps, C.c_double(rc_nl), C.c_double(skin_trigger), nb_uptab, mxkvois,
-                      nthreads)
+    fe = None if fext is None else f64(np.asarray(fext, np.float64).T.reshape(-1))
+    rc = lib().orc_md_ext(n, _d(x), _d(y), _d(z), _d(vx), _d(vy), _d(vz), _d(fx), _d(fy), _d(fz),
+                          _i(st), _i(ty), C.byref(box), C.byref(tables.s), _d(cmv), C.c_double(h),
+                          nsteps, C.c_double(rc_nl), C.c_double(skin_trigger), nb_uptab, mxkvois,
+                          nthreads, _d(fe) if fe is not None else None)
     if rc < 0:
         raise RuntimeError("oracle md failed: %d" % rc)
     return (np.stack([x, y, z], 1), np.stack([vx, vy, vz], 1), np.stack([fx, fy, fz], 1), st, rc)
