@@ -1968,13 +1968,15 @@ extern "C" int msmgb_set_tuning(msmgb_ctx *c, const int *codes)
     // density +128 (128-thread blocks) on the one-thread-per-atom families only
     const int d = codes[0];
     // +256 (single kind): the table-assisted density pass, 2-5 in the low bits, +16, +128
-    const bool d_q = !multi && d >= 0 && (d & 256) && (d & ~(256 | 128 | 16 | 7)) == 0 && (d & 7) >= 2 &&
-                     (d & 7) <= 5;
+    // +512: one box, its constants as a kernel parameter
+    const bool d_q = !multi && d >= 0 && (d & 256) && (d & ~(512 | 256 | 128 | 16 | 7)) == 0 && (d & 7) >= 2 &&
+                     (d & 7) <= 5 && (!(d & 512) || c->nbox == 1);
     const bool d_ok = d < 0 || d_q || in(d, valid_d, 15) ||
                       ((d & 128) && (d & ~128) < 32 && (d & 8) == 0 && in(d & ~128, valid_d, 15));
     // fused: 0-23 (several kinds 0-3), + 32 for 0-17 (0-3) in 128-thread blocks
     const int u = codes[2];
-    const bool u_ok = u < 0 || u < (multi ? 4 : 24) || (u >= 32 && u < 32 + (multi ? 4 : 18));
+    const bool u_sb = !multi && c->nbox == 1 && u >= 64 && ((u & ~32) - 64) >= 12 && ((u & ~32) - 64) < 18;
+    const bool u_ok = u < 0 || u_sb || u < (multi ? 4 : 24) || (u >= 32 && u < 32 + (multi ? 4 : 18));
     if (!d_ok || (codes[1] >= 0 && !in(codes[1], valid_f, 15)) || !u_ok)
         return set_err(c, MSMGB_ERR_ARG, "unknown kernel variant code");
     if (((codes[0] >= 0 && (codes[0] & 64)) || (codes[2] >= 20 && codes[2] < 24)) &&

@@ -26,6 +26,7 @@
 // prefetch, batched gathers, TMA-streamed list tiles, shared-memory table windows) that
 // the autotuner times once per atom count.
 #include <algorithm>
+#include <cstring>
 #include <cstdio>
 #include <cstdlib>
 
@@ -95,7 +96,7 @@ struct BoxF {
     float dlmax;          // bound on |dl| per component
 };
 
-__device__ __forceinline__ BoxF load_boxf(const DevBox &b)
+__host__ __device__ __forceinline__ BoxF load_boxf(const DevBox &b)
 {
     BoxF o;
 #pragma unroll
@@ -299,13 +300,38 @@ struct QBox {
     int pd;                         // periodic directions, bit k
 };
 
-__device__ __forceinline__ float qround(float h, float m)   // nearest multiple of q (m = 1.5 2^23 q)
+__host__ __device__ __forceinline__ float qround(float h, float m)   // nearest multiple of q (m = 1.5 2^23 q)
 {
+#ifdef __CUDA_ARCH__
     return __fsub_rn(__fadd_rn(h, m), m);
+#else
+    volatile float s = h + m;            // IEEE single additions on the host as on the device
+    return s - m;
+#endif
 }
 
-template <int POT, int UNR, int MINB, bool PF>
-__global__ void __launch_bounds__(kBlock, MINB) k_density32q(DevAtoms a, DevTables t, float qm, float rejs)
+__host__ __device__ __forceinline__ QBox qbox_of(const DevBox &bb, float qm)
+{
+    QBox b;
+    for (int k = 0; k < 3; ++k) {
+        b.lq[k] = qround(bb.lenf[k], qm);
+#ifdef __CUDA_ARCH__
+        b.ll[k] = __fadd_rn(__fsub_rn(bb.lenf[k], b.lq[k]), bb.lenlo[k]);
+#else
+        volatile float d = bb.lenf[k] - b.lq[k];
+        b.ll[k] = d + bb.lenlo[k];
+#endif
+        b.half[k] = bb.halff[k];
+    }
+    b.pd = (bb.ifpd[0] ? 1 : 0) | (bb.ifpd[1] ? 2 : 0) | (bb.ifpd[2] ? 4 : 0);
+    return b;
+}
+
+// SB (one box): the box constants come from the kernel parameter qbp (the constant bank)
+// instead of per-thread registers loaded from the box array.
+template <int POT, int UNR, int MINB, bool PF, bool SB = false>
+__global__ void __launch_bounds__(kBlock, MINB) k_density32q(DevAtoms a, DevTables t, float qm, float rejs,
+                                                             QBox qbp)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
@@ -317,15 +343,12 @@ __global__ void __launch_bounds__(kBlock, MINB) k_density32q(DevAtoms a, DevTabl
         st_ff(a.rec + i, ld_ff(a.posff + i));
         return;
     }
-    const DevBox &bb = a.box[a.boxid[i]];
-    QBox b;
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        b.lq[k] = qround(bb.lenf[k], qm);
-        b.ll[k] = __fadd_rn(__fsub_rn(bb.lenf[k], b.lq[k]), bb.lenlo[k]);
-        b.half[k] = bb.halff[k];
+    QBox bl;
+    if (!SB) {
+        const DevBox &bb = a.box[a.boxid[i]];
+        bl = qbox_of(bb, qm);
     }
-    b.pd = (bb.ifpd[0] ? 1 : 0) | (bb.ifpd[1] ? 2 : 0) | (bb.ifpd[2] ? 4 : 0);
+    const QBox &b = SB ? qbp : bl;
     const PosFF pi = ld_ff(a.posff + i);
     float ih[3], il[3];
     {
@@ -819,6 +842,37 @@ __global__ void __launch_bounds__(kBlock, MINB) k_force32_vv(DevAtoms a, DevTabl
         const double4_32a p = a.pos[i];
         if ((stat & MSMGB_STATU_ACTIVE) == MSMGB_STATU_ACTIVE) {
             dmax = vv_atom(a, i, stat, bb, th, true, Fx, Fy, Fz, p, a.pos_nxt, a.posff_nxt);
+        } else {
+            a.pos_nxt[i] = p;
+            a.posff_nxt[i] = a.posff[i];
+        }
+    }
+    block_max_flush(dmax, a.maxdisp);
+}
+
+// One box: the fused step kernel with the box constants as kernel parameters (bfp for the pair
+// loop, bp for the integrator) instead of per-thread registers loaded from the box array; the
+// same arithmetic in the same order as k_force32_vv<UNR, MINB, 2>, so bitwise the same results.
+template <int UNR, int MINB>
+__global__ void __launch_bounds__(kBlock, MINB) k_force32_vv_sb(DevAtoms a, DevTables t, double th, DevBox bp,
+                                                                BoxF bfp)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    float dmax = 0.0f;
+    if (i < a.n) {
+        const int stat = a.statu[i];
+        KSum fx, fy, fz;
+        if ((stat & MSMGB_STATU_ACTIVE) == MSMGB_STATU_ACTIVE) {
+            const PosFF pi = ld_ff(a.rec + i);
+            force_loop_batched<UNR>(a, t, i, pi, pi.d, bfp, fx, fy, fz);
+        }
+        const double Fx = fx.value64(), Fy = fy.value64(), Fz = fz.value64();
+        a.fx[i] = Fx;
+        a.fy[i] = Fy;
+        a.fz[i] = Fz;
+        const double4_32a p = a.pos[i];
+        if ((stat & MSMGB_STATU_ACTIVE) == MSMGB_STATU_ACTIVE) {
+            dmax = vv_atom(a, i, stat, bp, th, true, Fx, Fy, Fz, p, a.pos_nxt, a.posff_nxt);
         } else {
             a.pos_nxt[i] = p;
             a.posff_nxt[i] = a.posff[i];
@@ -1339,6 +1393,13 @@ static void fused_variant(msmgb_ctx *c, int code, double h)
     case 21: fused_tile<4, 3>(c, h, kTileCapSmall); break;
     case 22: fused_tile<2, 2>(c, h, kTileCapLarge); break;
     case 23: fused_tile<4, 2>(c, h, kTileCapLarge); break;
+    // +64 (one box): 12-17 with the box constants as kernel parameters
+    case 64 + 12: k_force32_vv_sb<2, 1><<<g, bs, 0, c->stream>>>(c->a, c->tab, h, c->hbox[0], load_boxf(c->hbox[0])); break;
+    case 64 + 13: k_force32_vv_sb<4, 1><<<g, bs, 0, c->stream>>>(c->a, c->tab, h, c->hbox[0], load_boxf(c->hbox[0])); break;
+    case 64 + 14: k_force32_vv_sb<2, 4><<<g, bs, 0, c->stream>>>(c->a, c->tab, h, c->hbox[0], load_boxf(c->hbox[0])); break;
+    case 64 + 15: k_force32_vv_sb<4, 4><<<g, bs, 0, c->stream>>>(c->a, c->tab, h, c->hbox[0], load_boxf(c->hbox[0])); break;
+    case 64 + 16: k_force32_vv_sb<2, 5><<<g, bs, 0, c->stream>>>(c->a, c->tab, h, c->hbox[0], load_boxf(c->hbox[0])); break;
+    case 64 + 17: k_force32_vv_sb<4, 5><<<g, bs, 0, c->stream>>>(c->a, c->tab, h, c->hbox[0], load_boxf(c->hbox[0])); break;
     default: k_force32_vv<2, 1, 0><<<g, bs, 0, c->stream>>>(c->a, c->tab, h); break;
     }
 }
@@ -1370,6 +1431,11 @@ int autotune_fused(msmgb_ctx *c)
     std::vector<int> codes;
     for (int code = 0; code < (multi ? kFusedVariantsMulti : kFusedVariants); ++code) codes.push_back(code);
     for (int code = multi ? 0 : 6; code < (multi ? kFusedVariantsMulti : 18); ++code) codes.push_back(32 + code);
+    if (!multi && c->nbox == 1)
+        for (int code = 12; code < 18; ++code) {
+            codes.push_back(64 + code);
+            codes.push_back(64 + 32 + code);
+        }
     for (int code : codes) {
         if ((code == 18 || code == 19) && !tma) continue;
         if (code >= 20 && code < 24 && !tiles) continue;
@@ -1431,16 +1497,26 @@ static void dens_variant(msmgb_ctx *c, int unr)
         float qm, rejs;
         density_q_params(c, &qm, &rejs);
         const bool pf = (unr & 16) != 0;
+        // +512: one box, its constants as a kernel parameter
+        const bool sb = (unr & 512) != 0 && c->nbox == 1;
+        const QBox qb = qbox_of(c->hbox[0], qm);
+#define MSMGB_DQ(U, M)                                                                                       \
+    do {                                                                                                     \
+        if (sb) {                                                                                            \
+            if (pf) k_density32q<POT, U, M, true, true><<<g, bs, 0, c->stream>>>(c->a, c->tab, qm, rejs, qb); \
+            else k_density32q<POT, U, M, false, true><<<g, bs, 0, c->stream>>>(c->a, c->tab, qm, rejs, qb); \
+        } else {                                                                                             \
+            if (pf) k_density32q<POT, U, M, true><<<g, bs, 0, c->stream>>>(c->a, c->tab, qm, rejs, qb);      \
+            else k_density32q<POT, U, M, false><<<g, bs, 0, c->stream>>>(c->a, c->tab, qm, rejs, qb);        \
+        }                                                                                                    \
+    } while (0)
         switch (unr & 7) {
-        case 3: if (pf) k_density32q<POT, 2, 5, true><<<g, bs, 0, c->stream>>>(c->a, c->tab, qm, rejs);
-                else k_density32q<POT, 2, 5, false><<<g, bs, 0, c->stream>>>(c->a, c->tab, qm, rejs); break;
-        case 4: if (pf) k_density32q<POT, 4, 1, true><<<g, bs, 0, c->stream>>>(c->a, c->tab, qm, rejs);
-                else k_density32q<POT, 4, 1, false><<<g, bs, 0, c->stream>>>(c->a, c->tab, qm, rejs); break;
-        case 5: if (pf) k_density32q<POT, 4, 4, true><<<g, bs, 0, c->stream>>>(c->a, c->tab, qm, rejs);
-                else k_density32q<POT, 4, 4, false><<<g, bs, 0, c->stream>>>(c->a, c->tab, qm, rejs); break;
-        default: if (pf) k_density32q<POT, 2, 1, true><<<g, bs, 0, c->stream>>>(c->a, c->tab, qm, rejs);
-                 else k_density32q<POT, 2, 1, false><<<g, bs, 0, c->stream>>>(c->a, c->tab, qm, rejs); break;
+        case 3: MSMGB_DQ(2, 5); break;
+        case 4: MSMGB_DQ(4, 1); break;
+        case 5: MSMGB_DQ(4, 4); break;
+        default: MSMGB_DQ(2, 1); break;
         }
+#undef MSMGB_DQ
         return;
     }
     if (!MULTI && (unr & 64)) {   // cell tiles: +16 the larger halo capacity
@@ -1572,8 +1648,10 @@ int autotune_mixed(msmgb_ctx *c)
         dc.push_back(10);
         if (enable_halo(c) == MSMGB_OK)
             for (int v : {66, 68, 82, 84}) dc.push_back(v);
-        for (int v : {258, 259, 260, 261, 274, 275, 276, 277, 386, 387, 388, 389, 402, 403, 404, 405})
+        for (int v : {258, 259, 260, 261, 274, 275, 276, 277, 386, 387, 388, 389, 402, 403, 404, 405}) {
             dc.push_back(v);
+            if (c->nbox == 1) dc.push_back(512 + v);      // box constants as a kernel parameter
+        }
     }
     const int fcands[15] = {1, 2, 4, 3, 5, 18, 20, 19, 21, 50, 52, 51, 53, 9, 10};
     const bool log = tune_log();

@@ -94,3 +94,29 @@ def test_density_q_md_steps(oracle):
     kv, ind = oracle.nlist(x, st, box, lt.CU_RC_NL, 96)
     ref = oracle.force(x, st, st, box, kv, ind, cu_tables(oracle))["f"]
     assert _rel(f, ref) < 1e-6
+
+
+@pytest.mark.parametrize("dens,fused,dens_sb,fused_sb", [(275, 14, 787, 78), (403, 46, 915, 110),
+                                                        (261, 16, 773, 80)])
+def test_single_box_parameter_variants_bitwise(dens, fused, dens_sb, fused_sb):
+    """One box: the density and fused step kernels with the box constants as kernel
+    parameters against the same kernels reading them from the box array per thread: the
+    same arithmetic, bitwise the same forces and trajectory."""
+    pos, vel, L_ = lt.cu_config(12, 0.08, 1200.0, 17)
+    n = len(pos)
+    out = []
+    for d, f in ((dens, fused), (dens_sb, fused_sb)):
+        e = Engine(n, lt.CU_RC_NL, mxkvois=64, precision="mixed", skin_trigger=0.15)
+        e.init_forcetable(ForceTable.cleri_rosato(**lt.CU_CR, rc=lt.CU_RC))
+        e.set_masses([lt.CU_MASS])
+        e.copyin([(n, (0, 0, 0), tuple(L_), (1, 1, 1))], pos, vel)
+        e.set_tuning(density=d, force=FORCE, fused=f)
+        reb = e.run_steps(30, 1.0)
+        x, v, _, _ = e.get_state()
+        out.append((x, v, e.get_force(), reb))
+        t = e.tuning()
+        assert (t["density_variant"], t["fused_variant"]) == (d, f)
+        e.close()
+    (xa, va, fa, ra), (xb, vb, fb, rb) = out
+    assert np.array_equal(xa, xb) and np.array_equal(va, vb) and np.array_equal(fa, fb)
+    assert ra == rb and ra > 0
