@@ -109,7 +109,7 @@ __global__ void k_pack(DevAtoms a, const double *xp, const double *xp1, const in
     a.pos[i] = make_double4_32a(x, y, z, 0.0);
     PosFF f = make_posff(x, y, z, a.box[boxid[i]]);
     a.posff[i] = f;
-    a.pos_bld[i] = make_float4(f.hx, f.hy, f.hz, 0.0f);
+    a.pos_bld[i] = pos_f32(f);
     a.vx[i] = xp1 ? xp1[i] : 0.0;
     a.vy[i] = xp1 ? xp1[n + i] : 0.0;
     a.vz[i] = xp1 ? xp1[2 * n + i] : 0.0;
@@ -164,9 +164,10 @@ __global__ void __launch_bounds__(kBlock) k_update_pos(DevAtoms a, const double 
         const PosFF f = make_posff(x[0], x[1], x[2], b);
         a.posff[s] = f;
         const float4 q = a.pos_bld[s];
-        const float ex = mi32f(f.hx - q.x, b.lenf[0], b.halff[0], b.ifpd[0]);
-        const float ey = mi32f(f.hy - q.y, b.lenf[1], b.halff[1], b.ifpd[1]);
-        const float ez = mi32f(f.hz - q.z, b.lenf[2], b.halff[2], b.ifpd[2]);
+        const float4 g = pos_f32(f);
+        const float ex = mi32f(g.x - q.x, b.lenf[0], b.halff[0], b.ifpd[0]);
+        const float ey = mi32f(g.y - q.y, b.lenf[1], b.halff[1], b.ifpd[1]);
+        const float ez = mi32f(g.z - q.z, b.lenf[2], b.halff[2], b.ifpd[2]);
         d2 = (double)(ex * ex + ey * ey + ez * ez);
     }
     block_max_flush(d2, a.maxdisp);
@@ -604,6 +605,16 @@ extern "C" int msmgb_copyin_simbox(msmgb_ctx *c, int nbox, const msmgb_box *boxe
     std::vector<int> boxid((size_t)n);
     int cells = 0, atom0 = 0;
     bool any_shaped = false;
+    // quantum of the hi parts of the mixed positions, one power of two for all boxes: every
+    // shifted coordinate u = x - lo + L in [L, 2L] (and an atom that left the box by up to L)
+    // lies below 2^22 q, so that hi + 1.5 2^23 q rounds to a multiple of q, and q >= 2^-7 A
+    // keeps the exact FP32 sums of squared hi differences of the density pass for pairs up to
+    // ~18 A
+    double posq = ldexp(1.0, -7);
+    for (int b = 0; b < nbox; ++b)
+        for (int k = 0; k < 3; ++k)
+            if (boxes[b].len[k] > 0.0)
+                posq = std::max(posq, ldexp(1.0, (int)std::ceil(std::log2(3.0 * boxes[b].len[k] / ldexp(1.0, 22)))));
     for (int b = 0; b < nbox; ++b) {
         DevBox &d = hb[(size_t)b];
         memset(&d, 0, sizeof(d));
@@ -659,9 +670,12 @@ extern "C" int msmgb_copyin_simbox(msmgb_ctx *c, int nbox, const msmgb_box *boxe
             const int nc = (int)ncd;
             d.nc[k] = nc < 3 ? 3 : nc;
         }
-        {   // |lo_i - lo_j| <= ulp(2L) (u in [L, 2L]) and |L - float(L)| <= ulp(L)/2
+        {   // hi parts are multiples of the quantum posq; |lo_i - lo_j| <= posq
             double ext = 2.0 * std::max(d.len[0], std::max(d.len[1], d.len[2]));
-            d.dlmax = (float)(2.0 * ldexp(1.0, ilogb(ext) - 23));
+            d.qq = (float)posq;
+            d.qmag = (float)(1.5 * ldexp(posq, 23));
+            d.dlmax = (float)(2.0 * posq);
+            d.dlfx = (float)(2.0 * ldexp(1.0, ilogb(ext) - 23));   // |u - float(u)| <= ulp(2L)/2
             // float-float passes: remainders u - float(u) (|.| <= ulp(2L)/2) in units of
             // 2^-30 ulp(2L), i.e. |q| <= 2^29
             const double ulp2l = ldexp(1.0, ilogb(ext) - 23);

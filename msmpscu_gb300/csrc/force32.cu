@@ -71,25 +71,6 @@ struct KSum {
     __device__ __forceinline__ double value64() const { return (double)s - (double)c; }
 };
 
-// One 256-bit load / store per 32 B record (sm_100+ vector width): a gather of 32 lanes'
-// records then touches each sector once instead of once per 16 B half.  The records are
-// 32 B aligned (PosFF is __align__(32), buffers come from cudaMalloc).
-__device__ __forceinline__ PosFF ld_ff(const PosFF *p)
-{
-    PosFF r;
-    asm("ld.global.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
-        : "=f"(r.hx), "=f"(r.hy), "=f"(r.hz), "=f"(r.d), "=f"(r.lx), "=f"(r.ly), "=f"(r.lz), "=f"(r.lw)
-        : "l"(p));
-    return r;
-}
-
-__device__ __forceinline__ void st_ff(PosFF *p, const PosFF &r)
-{
-    asm volatile("st.global.v8.f32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"l"(p), "f"(r.hx), "f"(r.hy),
-                 "f"(r.hz), "f"(r.d), "f"(r.lx), "f"(r.ly), "f"(r.lz), "f"(r.lw)
-                 : "memory");
-}
-
 struct BoxF {
     float lh[3], ll[3], half[3];
     int pd[3];
@@ -145,8 +126,9 @@ __device__ __forceinline__ unsigned pair_index(const PosFF &pi, const PosFF &pj,
     float t1, e1, t2, e2;
     two_sum(px, py, t1, e1);
     two_sum(t1, pz, t2, e2);
+    // the lo parts (up to the positions' quantum) enter as dl (2 dh + dl)
     const float small = (e1 + e2) + fmaf(xh, xh, -px) + fmaf(yh, yh, -py) + fmaf(zh, zh, -pz) +
-                        2.0f * (xh * xl + yh * yl + zh * zl);
+                        (xl * fmaf(2.0f, xh, xl) + yl * fmaf(2.0f, yh, yl) + zl * fmaf(2.0f, zh, zl));
     const float r2h = t2 + small;
     const float r2l = small - (r2h - t2);
     if (r2h > t.ru2h || (r2h == t.ru2h && r2l > t.ru2l)) return kSkip;
@@ -281,11 +263,12 @@ __global__ void __launch_bounds__(kBlock, MINB) k_density32(DevAtoms a, DevTable
 // ---- table-assisted density pass --------------------------------------------------------
 // The same pass as k_density32 (same pk codes, rho within FP32 rounding of the terms) with
 // fewer instructions per pair:
-//   * exact sum of squares: each hi part is rounded once more to a multiple of q, a power of
-//     two chosen so that every component of an accepted pair is below 2^11 q; the rounded hi
-//     differences dh are then exact multiples of q and dhx^2 + dhy^2 + dhz^2 is an integer
-//     times q^2 below 2^24 q^2, exact in FP32; the rest dl = u - hi(q) (below q) enters r^2 as
-//     C = sum dl (2 dh + dl), and r^2 = S + C as a float-float pair needs no two-sum;
+//   * exact sum of squares: the hi parts of the positions are multiples of the box quantum q,
+//     a power of two with every component of an accepted pair below 2^11 q (RU below ~18 A at
+//     the smallest q, 2^-7 A); the hi differences dh are exact multiples of q and
+//     dhx^2 + dhy^2 + dhz^2 is an integer times q^2 below 2^24 q^2, exact in FP32; the lo
+//     parts' difference dl (below q) enters r^2 as C = sum dl (2 dh + dl), and r^2 = S + C as
+//     a float-float pair needs no two-sum;
 //   * the sqrt(r) index by one table row: SK0 = CSI rsqrt(rsqrt(r^2)) (FP32) gives the grid
 //     point k = int(SK0); the row holds r2_k = (k/CSI)^4 as float-float, and with
 //     D = r^2 - r2_k (exact difference) the fraction is
@@ -350,15 +333,7 @@ __global__ void __launch_bounds__(kBlock, MINB) k_density32q(DevAtoms a, DevTabl
     }
     const QBox &b = SB ? qbp : bl;
     const PosFF pi = ld_ff(a.posff + i);
-    float ih[3], il[3];
-    {
-        const float h[3] = {pi.hx, pi.hy, pi.hz}, l[3] = {pi.lx, pi.ly, pi.lz};
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            ih[k] = qround(h[k], qm);
-            il[k] = __fadd_rn(__fsub_rn(h[k], ih[k]), l[k]);
-        }
-    }
+    const float ih[3] = {pi.hx, pi.hy, pi.hz}, il[3] = {pi.lx, pi.ly, pi.lz};
     const int *__restrict__ nb = a.indi + i;
     const float4 *__restrict__ rows = t.densq;
     KSum racc;
@@ -367,9 +342,8 @@ __global__ void __launch_bounds__(kBlock, MINB) k_density32q(DevAtoms a, DevTabl
         float dh[3], dl[3];
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
-            const float hq = qround(h[k], qm);
-            dh[k] = ih[k] - hq;                                   // exact multiple of q
-            dl[k] = il[k] - __fadd_rn(__fsub_rn(h[k], hq), l[k]);
+            dh[k] = ih[k] - h[k];                                 // exact multiple of q
+            dl[k] = il[k] - l[k];
             if (((b.pd >> k) & 1) && fabsf(dh[k]) > b.half[k]) {
                 const float sg = copysignf(1.0f, dh[k]);
                 dh[k] = fmaf(-sg, b.lq[k], dh[k]);                // exact
@@ -470,21 +444,21 @@ __global__ void __launch_bounds__(kBlock, MINB) k_density32q(DevAtoms a, DevTabl
     st_ff(a.rec + i, r);
 }
 
-// Quantum of the table-assisted density pass for the current tables and boxes: the smallest
-// power of two q such that 3 (RU + 0.05)^2 < (2^12 q)^2 (the exact sum of squares of an
-// accepted pair, whose components stay below RU + 1.5 q) and that every shifted coordinate
-// u = x - lo + L < 2L lies below 2^22 q (hi + 1.5 2^23 q then rounds hi to a multiple of q).
-// rejs bounds S of an accepted pair: r^2 - S = C, |C| <= 3 sqrt(3) RU q + 7 q^2 (|dl| <= 1.5 q).
-static void density_q_params(const msmgb_ctx *c, float *qm, float *rejs)
+// Constants of the table-assisted density pass for the current tables and boxes, false when
+// the pass does not apply: the positions' quantum q (the same for every box) must satisfy
+// 3 (RU + 0.05)^2 < (2^12 q)^2, so that the sum of squares of the hi differences of an
+// accepted pair (components below RU + 1.5 q) is exact.  qm = 1.5 2^23 q rounds the box edges
+// to q; rejs bounds S of an accepted pair: r^2 - S = C, |C| <= 3 sqrt(3) RU q + 7 q^2
+// (|dl| <= 1.5 q).
+static bool density_q_params(const msmgb_ctx *c, float *qm, float *rejs)
 {
+    if (c->hbox.empty()) return false;
     const double ru = std::sqrt(c->tab.ru2);
-    double ext = 0.0;
-    for (const DevBox &b : c->hbox)
-        for (int k = 0; k < 3; ++k) ext = std::max(ext, 2.0 * b.len[k]);
-    const double need = std::max((ru + 0.05) * std::sqrt(3.0) / 4096.0, ext / std::ldexp(1.0, 22));
-    const double q = std::ldexp(1.0, (int)std::ceil(std::log2(need)));
-    *qm = (float)(1.5 * std::ldexp(q, 23));
+    const double q = c->hbox[0].qq;
+    if ((ru + 0.05) * std::sqrt(3.0) / 4096.0 > q) return false;
+    *qm = c->hbox[0].qmag;
     *rejs = (float)(c->tab.ru2 * (1.0 + 1e-5) + 3.0 * std::sqrt(3.0) * ru * q + 7.0 * q * q);
+    return true;
 }
 
 // FP32 separation for the force direction (dh exact, dl small)
@@ -1495,7 +1469,10 @@ static void dens_variant(msmgb_ctx *c, int unr)
     const int g = nblk(c->n, bs);
     if (!MULTI && (unr & 256)) {      // table-assisted index (+16: list slots one batch ahead)
         float qm, rejs;
-        density_q_params(c, &qm, &rejs);
+        if (!density_q_params(c, &qm, &rejs)) {   // RU too long for the positions' quantum
+            dens_variant<POT, MULTI>(c, 2);
+            return;
+        }
         const bool pf = (unr & 16) != 0;
         // +512: one box, its constants as a kernel parameter
         const bool sb = (unr & 512) != 0 && c->nbox == 1;
@@ -1648,7 +1625,10 @@ int autotune_mixed(msmgb_ctx *c)
         dc.push_back(10);
         if (enable_halo(c) == MSMGB_OK)
             for (int v : {66, 68, 82, 84}) dc.push_back(v);
+        float qm, rejs;
+        const bool q_ok = density_q_params(c, &qm, &rejs);
         for (int v : {258, 259, 260, 261, 274, 275, 276, 277, 386, 387, 388, 389, 402, 403, 404, 405}) {
+            if (!q_ok) break;
             dc.push_back(v);
             if (c->nbox == 1) dc.push_back(512 + v);      // box constants as a kernel parameter
         }

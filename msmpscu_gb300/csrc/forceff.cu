@@ -114,7 +114,7 @@ __device__ __forceinline__ BoxFF load_boxff(const DevBox &b)
         o.lq[k] = b.lq[k];
         o.pd[k] = b.ifpd[k];
     }
-    o.dlmax = b.dlmax;
+    o.dlmax = b.dlfx;
     o.q = b.fxq;
     return o;
 }

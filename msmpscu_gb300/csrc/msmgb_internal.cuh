@@ -97,7 +97,12 @@ struct DevBox {
     float lenf[3];       // float-float box length (hi, lo) and FP32 half length
     float lenlo[3];
     float halff[3];
-    float dlmax;         // bound on the low part of a float-float separation component
+    float dlmax;         // bound on the low part of a float-float separation component (posff)
+    float dlfx;          // the same for the integer-remainder records of the float-float passes
+    // hi parts of the float-float positions are multiples of the quantum qq (a power of two):
+    // hi differences and their squares are exact in FP32 for pairs below ~18 A; qmag =
+    // 1.5 2^23 qq rounds a hi value to the quantum by one add and one subtract
+    float qq, qmag;
     float fxq;           // float-float passes: quantum of the integer remainders (power of 2)
     double fxinv;        // 1 / fxq
     double bs[9];        // BOXSHAPE(K, 1:3) in row K: separations in length units are bs . SEP
@@ -188,15 +193,51 @@ __device__ __forceinline__ void split_ff(double u, float &h, float &l)
     l = __double2float_rn(u - (double)h);
 }
 
+// u = hi + lo with hi the nearest multiple of the box's quantum qq to float(u) and lo = u - hi
+// (|lo| <= qq/2, carried to ~2^-24 of qq)
+__device__ __forceinline__ void split_q(double u, float qmag, float &h, float &l)
+{
+    float h0, l0;
+    split_ff(u, h0, l0);
+    h = __fsub_rn(__fadd_rn(h0, qmag), qmag);
+    l = __fadd_rn(__fsub_rn(h0, h), l0);
+}
+
 __device__ __forceinline__ PosFF make_posff(double x, double y, double z, const DevBox &b)
 {
     PosFF p;
-    split_ff(x + b.ushift[0], p.hx, p.lx);
-    split_ff(y + b.ushift[1], p.hy, p.ly);
-    split_ff(z + b.ushift[2], p.hz, p.lz);
+    split_q(x + b.ushift[0], b.qmag, p.hx, p.lx);
+    split_q(y + b.ushift[1], b.qmag, p.hy, p.ly);
+    split_q(z + b.ushift[2], b.qmag, p.hz, p.lz);
     p.d = 0.0f;
     p.lw = 0.0f;
     return p;
+}
+
+// One 256-bit load / store per 32 B record (sm_100+ vector width): a gather of 32 lanes'
+// records then touches each sector once instead of once per 16 B half.  The records are
+// 32 B aligned (PosFF is __align__(32), buffers come from cudaMalloc).
+__device__ __forceinline__ PosFF ld_ff(const PosFF *p)
+{
+    PosFF r;
+    asm("ld.global.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=f"(r.hx), "=f"(r.hy), "=f"(r.hz), "=f"(r.d), "=f"(r.lx), "=f"(r.ly), "=f"(r.lz), "=f"(r.lw)
+        : "l"(p));
+    return r;
+}
+
+__device__ __forceinline__ void st_ff(PosFF *p, const PosFF &r)
+{
+    asm volatile("st.global.v8.f32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"l"(p), "f"(r.hx), "f"(r.hy),
+                 "f"(r.hz), "f"(r.d), "f"(r.lx), "f"(r.ly), "f"(r.lz), "f"(r.lw)
+                 : "memory");
+}
+
+// the position as one FP32 value per component (hi + lo), for the list prefilter and the skin
+// trigger: within one ulp of float(u)
+__device__ __forceinline__ float4 pos_f32(const PosFF &f)
+{
+    return make_float4(f.hx + f.lx, f.hy + f.ly, f.hz + f.lz, 0.0f);
 }
 
 // non-cubic box: DXYZ(K) = sum(BOXSHAPE(K,1:3)*SEP(1:3)) after the minimum image
@@ -281,12 +322,13 @@ __device__ __forceinline__ float vv_atom(const DevAtoms &a, int i, int stat, con
     if (hi) a.statu[i] = MSMGB_STATU_OUTOFBOX | MSMGB_STATU_REFLECT;
     else if (lo) a.statu[i] = MSMGB_STATU_OUTOFBOX | MSMGB_STATU_TRANSMIT;
     if (hi | lo) atomicOr(&a.flags[kFlagOob], 1);
-    // displacement since the last build from the exact FP32 hi parts (the trigger needs
-    // ~1e-4 A, the hi parts are within 3e-5 A of the FP64 positions)
+    // displacement since the last build from the FP32 positions hi + lo (the trigger needs
+    // ~1e-4 A, they are within 3e-5 A of the FP64 positions)
     const float4 q = a.pos_bld[i];
-    const float ex = mi32f(f.hx - q.x, b.lenf[0], b.halff[0], b.ifpd[0]);
-    const float ey = mi32f(f.hy - q.y, b.lenf[1], b.halff[1], b.ifpd[1]);
-    const float ez = mi32f(f.hz - q.z, b.lenf[2], b.halff[2], b.ifpd[2]);
+    const float4 g = pos_f32(f);
+    const float ex = mi32f(g.x - q.x, b.lenf[0], b.halff[0], b.ifpd[0]);
+    const float ey = mi32f(g.y - q.y, b.lenf[1], b.halff[1], b.ifpd[1]);
+    const float ez = mi32f(g.z - q.z, b.lenf[2], b.halff[2], b.ifpd[2]);
     return ex * ex + ey * ey + ez * ez;
 }
 

@@ -200,7 +200,7 @@ __global__ void k_copyback(DevAtoms a, Stage s, int *cell_of)
     a.pos[i] = p;
     const PosFF f = make_posff(p.x, p.y, p.z, a.box[s.boxid[i]]);
     a.posff[i] = f;
-    a.pos_bld[i] = make_float4(f.hx, f.hy, f.hz, 0.0f);   // skin reference and k_build candidates
+    a.pos_bld[i] = pos_f32(f);   // skin reference and k_build candidates
     a.vx[i] = s.vx[i]; a.vy[i] = s.vy[i]; a.vz[i] = s.vz[i];
     a.dx[i] = s.dx[i]; a.dy[i] = s.dy[i]; a.dz[i] = s.dz[i];
     a.ityp[i] = s.ityp[i];
@@ -245,7 +245,7 @@ __global__ void __launch_bounds__(kBlock, 6) k_build(DevAtoms a, const int *cell
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
-    const PosFF pf = a.posff[i];
+    const float4 pf = pos_f32(a.posff[i]);
     if (a.statu[i] & MSMGB_STATU_OUTOFBOX) { a.kvois[i] = 0; return; }
     const DevBox &b = a.box[a.boxid[i]];
     int nc[3], pd[3];
@@ -287,9 +287,9 @@ __global__ void __launch_bounds__(kBlock, 6) k_build(DevAtoms a, const int *cell
         if (wide) {
             for (int j = j0; j < e; ++j) {
                 const float4 q = hi[j];
-                const float sx = (pf.hx - q.x) + sh[0];      // hi difference exact (Sterbenz)
-                const float sy = (pf.hy - q.y) + sh[1];
-                const float sz = (pf.hz - q.z) + sh[2];
+                const float sx = (pf.x - q.x) + sh[0];       // difference exact (Sterbenz)
+                const float sy = (pf.y - q.y) + sh[1];
+                const float sz = (pf.z - q.z) + sh[2];
                 const float d2f = fmaf(sx, sx, fmaf(sy, sy, sz * sz));
                 if (j != i && accept(d2f, d2lo, d2hi, a, i, j, b, rc2)) {
                     if (nn < mxk) indi[(size_t)nn * ld] = j;
@@ -300,9 +300,9 @@ __global__ void __launch_bounds__(kBlock, 6) k_build(DevAtoms a, const int *cell
             const float h0 = b.halff[0], h1 = b.halff[1], h2 = b.halff[2];
             for (int j = j0; j < e; ++j) {
                 const float4 q = hi[j];
-                const float sx = mi32(pf.hx - q.x, lf[0], h0, pd[0]);
-                const float sy = mi32(pf.hy - q.y, lf[1], h1, pd[1]);
-                const float sz = mi32(pf.hz - q.z, lf[2], h2, pd[2]);
+                const float sx = mi32(pf.x - q.x, lf[0], h0, pd[0]);
+                const float sy = mi32(pf.y - q.y, lf[1], h1, pd[1]);
+                const float sz = mi32(pf.z - q.z, lf[2], h2, pd[2]);
                 const float d2f = fmaf(sx, sx, fmaf(sy, sy, sz * sz));
                 if (j != i && accept(d2f, d2lo, d2hi, a, i, j, b, rc2)) {
                     if (nn < mxk) indi[(size_t)nn * ld] = j;
@@ -474,14 +474,14 @@ __global__ void __launch_bounds__(kBlock, 6) k_build_cand(DevAtoms a, const int 
 // makes the next rebuild full (kFlagOob).
 constexpr int kInnerUnr = 4;
 
-__global__ void __launch_bounds__(kBlock) k_inner(DevAtoms a, const int *cand, const int *kcand, double rc2,
+__global__ void __launch_bounds__(kBlock, 4) k_inner(DevAtoms a, const int *cand, const int *kcand, double rc2,
                                                   float d2lo, float d2hi)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
-    const PosFF pf = a.posff[i];
-    a.pos_bld[i] = make_float4(pf.hx, pf.hy, pf.hz, 0.0f);
-    if (!(isfinite(pf.hx) && isfinite(pf.hy) && isfinite(pf.hz))) atomicOr(&a.flags[kFlagErr], kErrNonFinite);
+    const float4 pf = pos_f32(a.posff[i]);
+    a.pos_bld[i] = pf;
+    if (!(isfinite(pf.x) && isfinite(pf.y) && isfinite(pf.z))) atomicOr(&a.flags[kFlagErr], kErrNonFinite);
     // an atom outside its box neither has nor is a neighbour (the full rebuild puts it into
     // the sentinel cell)
     if (a.statu[i] & MSMGB_STATU_OUTOFBOX) { a.kvois[i] = 0; return; }
@@ -499,14 +499,13 @@ __global__ void __launch_bounds__(kBlock) k_inner(DevAtoms a, const int *cand, c
     const int mxk = a.mxk;
     int *const indi = a.indi + i;
     const int *const cd = cand + i;
-    const float4 *const hp = reinterpret_cast<const float4 *>(a.posff);   // hi halves: every 2nd float4
     int nn = 0;
     int jn[kInnerUnr];
 #pragma unroll
     for (int u = 0; u < kInnerUnr; ++u) jn[u] = u < kc ? __ldg(cd + (size_t)u * ld) : i;
     for (int s = 0; s < kc; s += kInnerUnr) {
         int j[kInnerUnr];
-        float4 q[kInnerUnr];
+        PosFF q[kInnerUnr];
 #pragma unroll
         for (int u = 0; u < kInnerUnr; ++u) {
             j[u] = jn[u];
@@ -514,13 +513,14 @@ __global__ void __launch_bounds__(kBlock) k_inner(DevAtoms a, const int *cand, c
             jn[u] = sl < kc ? __ldg(cd + (size_t)sl * ld) : i;
         }
 #pragma unroll
-        for (int u = 0; u < kInnerUnr; ++u) q[u] = __ldg(hp + 2 * (size_t)j[u]);
+        for (int u = 0; u < kInnerUnr; ++u) q[u] = ld_ff(a.posff + j[u]);   // one 256-bit load
 #pragma unroll
         for (int u = 0; u < kInnerUnr; ++u) {
             if (s + u >= kc) break;
-            const float sx = mi32(pf.hx - q[u].x, lf[0], hf[0], pd[0]);
-            const float sy = mi32(pf.hy - q[u].y, lf[1], hf[1], pd[1]);
-            const float sz = mi32(pf.hz - q[u].z, lf[2], hf[2], pd[2]);
+            const float4 g = pos_f32(q[u]);
+            const float sx = mi32(pf.x - g.x, lf[0], hf[0], pd[0]);
+            const float sy = mi32(pf.y - g.y, lf[1], hf[1], pd[1]);
+            const float sz = mi32(pf.z - g.z, lf[2], hf[2], pd[2]);
             const float d2f = fmaf(sx, sx, fmaf(sy, sy, sz * sz));
             if (accept(d2f, d2lo, d2hi, a, i, j[u], b, rc2)) {
                 if (nn < mxk) indi[(size_t)nn * ld] = j[u];

@@ -120,3 +120,28 @@ def test_single_box_parameter_variants_bitwise(dens, fused, dens_sb, fused_sb):
     (xa, va, fa, ra), (xb, vb, fb, rb) = out
     assert np.array_equal(xa, xb) and np.array_equal(va, vb) and np.array_equal(fa, fb)
     assert ra == rb and ra > 0
+
+
+def test_density_q_long_box(oracle):
+    """A box of 20,000 A along x (open faces there): the hi parts of the positions take a
+    coarser quantum (2^-6 A instead of 2^-7 A, so that every shifted coordinate rounds to a
+    multiple of it), and the exact sums of squares, the list and the forces still hold."""
+    p, L_ = lt.fcc(8, 8, 8, lt.CU_A)
+    p = p + np.random.default_rng(12).normal(scale=0.06, size=p.shape)
+    p -= np.floor(p / L_) * L_
+    p[:, 0] += 15000.0
+    L = (20000.0, float(L_[1]), float(L_[2]))
+    n = len(p)
+    box = oracle.make_box([0, 0, 0], L, ifpd=(0, 1, 1))
+    st = np.ones(n, np.int32)
+    kv, ind = oracle.nlist(p, st, box, lt.CU_RC_NL, 96)
+    ref = oracle.force(p, st, st, box, kv, ind, cu_tables(oracle))
+    e = Engine(n, lt.CU_RC_NL, mxkvois=64, precision="mixed")
+    e.init_forcetable(ForceTable.cleri_rosato(**lt.CU_CR, rc=lt.CU_RC))
+    e.copyin([(n, (0, 0, 0), L, (0, 1, 1))], p)
+    for dens in (258, 277, 386, 405):
+        f, d = _forces(e, dens)
+        assert e.tuning()["density_variant"] == dens
+        assert _rel(f, ref["f"]) < 1e-6, dens
+        assert _rel(d, ref["den"]) < 2e-7, dens
+    e.close()
