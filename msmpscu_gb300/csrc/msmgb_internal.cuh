@@ -9,8 +9,8 @@
 //   vx..vz   double   velocities (SoA, streamed)
 //   fx..fz   double   forces (SoA, streamed)
 //   dis      double   accumulated displacement DIS (reference MD_DiffScheme_GPU.F90:364-366)
-//   pos_bld  float4   hi parts of the shifted positions at the last list build (skin
-//                     trigger; hi_i - hi_bld is exact)
+//   pos_bld  float4   FP32 shifted positions (hi + lo) at the last list build (skin
+//                     trigger and list-build candidates; differences are exact)
 //   ityp, statu, gid (sorted -> original), boxid
 //   kvois    int32    neighbour count, INDI column-major int32 [mxkvois][cap] (reference
 //                     layout INDI(NAPDEV,MXKVOIS), MD_NeighborsList_GPU.F90:75-85)

@@ -238,7 +238,7 @@ __device__ __forceinline__ bool accept(float d2f, float d2lo, float d2hi, const 
 // Full neighbour list, one thread per (sorted) atom.  Cells of a box are at least rc_nl
 // wide unless the box forced NCELL to 3 (the reference's rule for small boxes); in the wide
 // case the periodic image of every candidate is the one of its stencil cell, so the
-// separation is the exact hi-part difference plus a per-cell shift of -L, 0 or +L, with no
+// separation is the exact difference of the FP32 positions plus a per-cell shift of -L, 0 or +L, with no
 // per-candidate minimum-image test.  Narrow boxes take the minimum image per candidate.
 __global__ void __launch_bounds__(kBlock, 6) k_build(DevAtoms a, const int *cell_of, const int *rank,
                                                   const int *start, double rc2, float d2lo, float d2hi)
@@ -266,7 +266,7 @@ __global__ void __launch_bounds__(kBlock, 6) k_build(DevAtoms a, const int *cell
     const size_t ld = (size_t)a.ld;
     const int mxk = a.mxk;
     int *const indi = a.indi + i;
-    const float4 *const hi = a.pos_bld;   // hi parts, 16 B per atom (written by k_copyback)
+    const float4 *const hi = a.pos_bld;   // FP32 positions, 16 B per atom (written by k_copyback)
     for (int s = 0; s < 27; ++s) {
         int j3[3] = {ix + c_nix[s], iy + c_niy[s], iz + c_niz[s]};
         float sh[3];
@@ -712,10 +712,11 @@ int enable_halo(msmgb_ctx *c)
     return MSMGB_OK;
 }
 
-// Margin of the FP32 prefilter: it uses the hi parts of the shifted coordinates
-// (u in [L, 2L]): hi_i - hi_j and the image shift by float(L) are exact (Sterbenz), so a
-// separation component is off by at most |lo_i - lo_j| + |L - float(L)| <= 1.5 ulp(2L);
-// the band below allows 4 ulp of the largest coordinate extent plus the rounding of d^2.
+// Margin of the FP32 prefilter: it uses the FP32 positions hi + lo of the shifted coordinates
+// (u in [L, 2L], each within ~ulp(u)/2 of u): their difference and the image shift by float(L)
+// are exact (Sterbenz), so a separation component is off by at most ulp(2L) +
+// |L - float(L)| <= 1.5 ulp(2L); the band below allows 4 ulp of the largest coordinate extent
+// plus the rounding of d^2.
 static void prefilter_band(const msmgb_ctx *c, double rc2, float *lo, float *hi)
 {
     double ext = 1.0;

@@ -109,7 +109,7 @@ int launch_decide(msmgb_ctx *c, double skin_trigger, int nb_uptab, cudaGraphCond
                   cudaGraphConditionalHandle cond_inner)
 {
     double thr2 = skin_trigger > 0.0 ? skin_trigger * skin_trigger : 0.0;
-    // the displacement bound comes from FP32 hi parts (within 3e-5 A of the positions): 1e-3 A margin
+    // the displacement bound comes from the FP32 positions hi + lo (within 3e-5 A of the positions): 1e-3 A margin
     const float half_outer = (use_cond && two_level(c)) ? (float)(0.5 * c->outer_skin - 1e-3) : 0.0f;
     k_decide<<<1, 1, 0, c->stream>>>(c->a.flags, c->a.maxdisp, thr2, nb_uptab, cond, use_cond ? 1 : 0, half_outer,
                                      cond_inner);
