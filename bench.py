@@ -257,6 +257,22 @@ def hvp_w_dumbbell(device=0):
             "hvp_cost_force_calls": ms_hvp / ms_force}
 
 
+def hvp_cu_large(device=0):
+    """fcc Cu 80^3 cells (2,048,000 atoms, sigma 0.05 A), Cleri-Rosato: device time of one HVP
+    against one FP64 force call, and the size of the HVP's pair buffer."""
+    from msmpscu_gb300 import Engine, ForceTable, lattice as lt
+    pos, _, L = lt.cu_config(80, 0.05, 600.0, 5)
+    e = Engine(len(pos), lt.CU_RC_NL, mxkvois=64, device=device)
+    e.init_forcetable(ForceTable.cleri_rosato(**lt.CU_CR, rc=lt.CU_RC))
+    e.copyin([(len(pos), (0, 0, 0), tuple(L), (1, 1, 1))], pos)
+    v = np.random.default_rng(0).normal(size=pos.shape)
+    v /= np.linalg.norm(v)
+    ms_hvp, ms_force = e.time_hvp(v, reps=5)
+    e.close()
+    return {"atoms": len(pos), "hvp_ms": ms_hvp, "force_call_ms": ms_force,
+            "hvp_cost_force_calls": ms_hvp / ms_force, "pair_buffer_bytes": 40 * 64 * len(pos)}
+
+
 def adjoint_cu_snapshots(device=0):
     """64 fcc Cu snapshots of 4,000 atoms (sigma 0.1 A), targets from parameters x 1.02:
     wall time of one adjoint call (FP64 forces + adjoint passes + host derivative tables)
@@ -606,6 +622,7 @@ def run_ours(args):
         e.close()
         extras["batched_boxes"] = batched_uneven_boxes(max(10, min(args.steps, 100)), 20, device)
         extras["hvp"] = hvp_w_dumbbell(device)
+        extras["hvp_cu_2048k"] = hvp_cu_large(device)
         extras["adjoint"] = adjoint_cu_snapshots(device)
         extras["nve_drift"] = nve_drift(device)
         extras["oracle_parity"] = oracle_parity(pos, vel, L, device)

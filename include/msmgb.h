@@ -304,7 +304,10 @@ int  msmgb_set_extforce_field(msmgb_ctx *ctx, const double *fext);
 int  msmgb_time_hvp(msmgb_ctx *ctx, const double *v, int reps, float *ms_hvp, float *ms_force);
 /* Hessian-vector product of the table-mode force (exact derivative of the interpolants):
  * hv = -dF/dx . v.  v and hv are 3*N arrays in XP layout, caller's order, in host or device
- * memory.  No counterpart in the reference: it replaces finite-difference force pairs
+ * memory.  The first call allocates the pair buffer that hands each pair's geometry from the
+ * first pass to the second: 40 B x MXKVOIS per atom of the context's capacity (5.2 GB for
+ * 2,048,000 atoms at MXKVOIS 64), kept until msmgb_destroy; MSMGB_ERR_CUDA if it does not fit.
+ * No counterpart in the reference: it replaces finite-difference force pairs
  * (MD_Method_ART_GPU.F90:454-576). */
 int  msmgb_hvp(msmgb_ctx *ctx, const double *v, double *hv);
 

@@ -13,7 +13,7 @@ import pytest
 from msmpscu_gb300 import Engine, ForceTable, lattice as lt
 from msmpscu_gb300 import _lib as L
 from msmpscu_gb300.lanczos import lanczos_lowest, fd_hvp
-from tests.helpers import w_tables, rel_err
+from tests.helpers import cu_tables, w_tables, rel_err
 
 pytestmark = pytest.mark.gpu
 
@@ -66,6 +66,37 @@ def test_c4_hvp_vs_fd_oracle_and_lanczos(oracle):
     assert float((mode * hm).sum()) == pytest.approx(lam, rel=1e-6, abs=1e-8)
     ms_hvp, ms_force = e.time_hvp(mode, reps=10)
     assert ms_hvp > 0 and ms_force > 0
+    e.close()
+
+
+@pytest.mark.parametrize("system", ["w_250k", "cu_2048k"])
+def test_hvp_large_systems_vs_oracle(oracle, system):
+    """The HVP at the sizes where its pair buffer (40 B x MXKVOIS per atom slot, allocated on the
+    first call) grows large: bcc W 50^3 cells + a <111> dumbbell (250,001 atoms, EAM) and fcc Cu
+    80^3 cells (2,048,000 atoms, FS; 5.2 GB of pair buffer at MXKVOIS 64), against the oracle's
+    HVP at 1e-10, and linear in the probe."""
+    if system == "w_250k":
+        pos, L_ = lt.w_sia_config(50, 0.02, 3)
+        e = _w_engine(len(pos))
+        t, rcnl, mxk = w_tables(oracle), lt.W_RC_NL, 128
+    else:
+        pos, _, L_ = lt.cu_config(80, 0.05, 600.0, 5)
+        e = Engine(len(pos), lt.CU_RC_NL, mxkvois=64)
+        e.init_forcetable(ForceTable.cleri_rosato(**lt.CU_CR, rc=lt.CU_RC))
+        t, rcnl, mxk = cu_tables(oracle), lt.CU_RC_NL, 96
+    n = len(pos)
+    e.copyin([(n, (0, 0, 0), tuple(L_), (1, 1, 1))], pos)
+    ob = oracle.make_box([0, 0, 0], L_)
+    st = np.ones(n, np.int32)
+    kv, ind = oracle.nlist(pos, st, ob, rcnl, mxk)
+    rng = np.random.default_rng(11)
+    v1 = rng.normal(size=pos.shape)
+    v2 = rng.normal(size=pos.shape)
+    h1 = e.hvp(v1)
+    assert rel_err(h1, oracle.hvp(pos, st, st, ob, kv, ind, t, v1)) < 1e-10
+    h2 = e.hvp(v2)
+    h12 = e.hvp(v1 + 2.0 * v2)
+    assert rel_err(h12, h1 + 2.0 * h2) < 1e-12
     e.close()
 
 
