@@ -279,7 +279,8 @@ extern "C" int msmgb_create(msmgb_ctx **out, const msmgb_params *p)
     if ((e = cudaMallocHost((void **)&c->h_virial, sizeof(double) * 6 * c->cap_boxes)) != cudaSuccess) return fail(e, "pinned");
     if ((e = cudaMemsetAsync(c->flags, 0, sizeof(int) * kFlagWords, c->stream)) != cudaSuccess) return fail(e, "memset");
     if ((e = cudaMemsetAsync(c->maxdisp, 0, sizeof(unsigned long long), c->stream)) != cudaSuccess) return fail(e, "memset");
-    if (p->precision == MSMGB_PREC_MIXED && (e = dalloc(&a.pk, LD * (size_t)p->mxkvois)) != cudaSuccess)
+    if (p->precision == MSMGB_PREC_MIXED &&
+        ((e = dalloc(&a.pk, LD * (size_t)p->mxkvois)) != cudaSuccess || (e = dalloc(&a.rec16, N)) != cudaSuccess))
         return fail(e, "cudaMalloc pair index");
     if (p->precision != MSMGB_PREC_FP64 && (e = dalloc(&a.rec, N)) != cudaSuccess)
         return fail(e, "cudaMalloc records");
@@ -305,7 +306,7 @@ extern "C" int msmgb_destroy(msmgb_ctx *c)
     DevAtoms &a = c->a;
     void *ptrs[] = {a.pos, a.posff, a.pos_bld, a.vx, a.vy, a.vz, a.fx, a.fy, a.fz,
                     a.dx, a.dy, a.dz, a.ityp, a.statu, a.gid, a.boxid, a.den, a.epot,
-                    a.den32, a.kvois, a.indi, a.pk, a.rec, a.posfx, a.recfx, c->cell_of, c->perm, c->dbox, c->cm, c->icm,
+                    a.den32, a.kvois, a.indi, a.pk, a.rec, a.rec16, a.posfx, a.recfx, c->cell_of, c->perm, c->dbox, c->cm, c->icm,
                     c->flags, c->maxdisp, c->virial, c->scratch, c->cell_start,
                     c->cell_cursor, c->scan_tmp, c->cell_rank, c->cell_unrank, c->tab_mem, c->adj_mem, c->hvp_pair,
                     c->pos2, c->posff2, a.lidx, a.hmeta, a.hruns, c->cand, c->kcand, c->ext_field};
@@ -331,6 +332,11 @@ extern "C" int msmgb_set_precision(msmgb_ctx *c, int precision)
         RET(use_device(c));
         CK(cudaStreamSynchronize(c->stream), "synchronize");
         CK(dalloc(&c->a.pk, (size_t)c->a.ld * (size_t)c->p.mxkvois), "cudaMalloc pair index");
+        CK(dalloc(&c->a.rec16, (size_t)c->cap_atoms), "cudaMalloc fixed-point records");
+        bool fix_ok = !c->hbox.empty();
+        for (const DevBox &b : c->hbox)
+            for (int k = 0; k < 3; ++k) fix_ok = fix_ok && (b.ifpd[k] ? b.len[k] : 2.0 * b.len[k]) <= kFixMaxSpan;
+        c->a.fix_on = fix_ok ? 1 : 0;
     }
     if (precision == MSMGB_PREC_FF && !c->a.posfx) {
         RET(use_device(c));
@@ -605,6 +611,7 @@ extern "C" int msmgb_copyin_simbox(msmgb_ctx *c, int nbox, const msmgb_box *boxe
     std::vector<int> boxid((size_t)n);
     int cells = 0, atom0 = 0;
     bool any_shaped = false;
+    bool fix_ok = true;           // every box edge within the fixed-point records' span
     // quantum of the hi parts of the mixed positions, one power of two for all boxes: every
     // shifted coordinate u = x - lo + L in [L, 2L] (and an atom that left the box by up to L)
     // lies below 2^22 q, so that hi + 1.5 2^23 q rounds to a multiple of q, and q >= 2^-7 A
@@ -654,6 +661,12 @@ extern "C" int msmgb_copyin_simbox(msmgb_ctx *c, int nbox, const msmgb_box *boxe
             d.lenlo[k] = (float)(d.len[k] - (double)d.lenf[k]);
             d.halff[k] = (float)d.half[k];
             d.ifpd[k] = boxes[b].ifpd[k] ? 1 : 0;
+            {   // fixed-point unit: the edge (periodic) or twice the edge (open) over 2^32
+                const double span = d.ifpd[k] ? d.len[k] : 2.0 * d.len[k];
+                d.fixu[k] = (float)(span / 4294967296.0);
+                d.fixinv[k] = 4294967296.0 / span;
+                if (span > kFixMaxSpan) fix_ok = false;
+            }
             if (d.len[k] <= 0.0) return set_err(c, MSMGB_ERR_ARG, "box length must be positive");
             // a pair within rc_nl has |SEP_k| <= rc_nl * |row k of BOXSHAPE^-1| (nrm = 1 for a
             // cubic box): the single-shift minimum image is unique only below half the edge
@@ -769,6 +782,7 @@ extern "C" int msmgb_copyin_simbox(msmgb_ctx *c, int nbox, const msmgb_box *boxe
     c->ncell_total = cells;
     c->bin_rc = bin_rc;
     c->any_shaped = any_shaped;
+    c->a.fix_on = (fix_ok && c->a.rec16) ? 1 : 0;
     c->max_density = 0.0;
     for (int b = 0; b < nbox; ++b)
         c->max_density = std::max(c->max_density, boxes[b].natom / (boxes[b].len[0] * boxes[b].len[1] * boxes[b].len[2]));
@@ -1989,9 +2003,17 @@ extern "C" int msmgb_set_tuning(msmgb_ctx *c, const int *codes)
                       ((d & 128) && (d & ~128) < 32 && (d & 8) == 0 && in(d & ~128, valid_d, 15));
     // fused: 0-23 (several kinds 0-3), + 32 for 0-17 (0-3) in 128-thread blocks
     const int u = codes[2];
-    const bool u_sb = !multi && c->nbox == 1 && u >= 64 && ((u & ~32) - 64) >= 12 && ((u & ~32) - 64) < 18;
-    const bool u_ok = u < 0 || u_sb || u < (multi ? 4 : 24) || (u >= 32 && u < 32 + (multi ? 4 : 18));
-    if (!d_ok || (codes[1] >= 0 && !in(codes[1], valid_f, 15)) || !u_ok)
+    const bool u_sb = !multi && c->nbox == 1 && u >= 64 && u < 128 && ((u & ~32) - 64) >= 12 &&
+                      ((u & ~32) - 64) < 18;
+    // +128 (single kind, fixed-point records on): 12-17, +32, +64 (one box)
+    const int ub = u & ~(128 | 64 | 32);
+    const bool u_fix = !multi && c->a.fix_on && u >= 128 && u < 256 && ub >= 12 && ub < 18 &&
+                       (!(u & 64) || c->nbox == 1);
+    const bool u_ok = u < 0 || u_sb || u_fix || u < (multi ? 4 : 24) || (u >= 32 && u < 32 + (multi ? 4 : 18));
+    // force +128 (single kind, fixed-point records on): the batched codes 50-53
+    const int f = codes[1];
+    const bool f_fix = !multi && c->a.fix_on && f >= 128 && f < 256 && (f - 128) >= 50 && (f - 128) <= 53;
+    if (!d_ok || (f >= 0 && !f_fix && !in(f, valid_f, 15)) || !u_ok)
         return set_err(c, MSMGB_ERR_ARG, "unknown kernel variant code");
     if (((codes[0] >= 0 && (codes[0] & 64)) || (codes[2] >= 20 && codes[2] < 24)) &&
         (c->tab.ngroup > 1 || c->p.precision != MSMGB_PREC_MIXED))

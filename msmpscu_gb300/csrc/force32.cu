@@ -38,6 +38,14 @@ namespace msmgb {
 
 constexpr unsigned kSkip = 0xffffffffu;     // pair beyond RU
 
+// The density pass's per-atom output: the 32 B float-float record {position, F'(rho)} and,
+// when the fixed-point records are on, the 16 B record the fixed-point force variants gather.
+__device__ __forceinline__ void store_rec(const DevAtoms &a, int i, const PosFF &r)
+{
+    st_ff(a.rec + i, r);
+    if (a.fix_on) a.rec16[i] = fix_record(r, r.d, a.box[a.boxid[i]]);
+}
+
 // MSMGB_TUNE_LOG=1: the autotuners print every variant's time per launch to stderr
 static bool tune_log()
 {
@@ -161,7 +169,7 @@ __global__ void __launch_bounds__(kBlock, MINB) k_density32(DevAtoms a, DevTable
     const size_t ld = (size_t)a.ld;
     if ((a.statu[i] & MSMGB_STATU_ACTIVE) != MSMGB_STATU_ACTIVE) {   // the force pass skips it
         a.den32[i] = 0.0f;
-        st_ff(a.rec + i, ld_ff(a.posff + i));          // d = 0
+        store_rec(a, i, ld_ff(a.posff + i));          // d = 0
         return;
     }
     const BoxF b = load_boxf(a.box[a.boxid[i]]);
@@ -257,7 +265,7 @@ __global__ void __launch_bounds__(kBlock, MINB) k_density32(DevAtoms a, DevTable
     a.den32[i] = d;
     PosFF r = pi;
     r.d = d;
-    st_ff(a.rec + i, r);
+    store_rec(a, i, r);
 }
 
 // ---- table-assisted density pass --------------------------------------------------------
@@ -323,7 +331,7 @@ __global__ void __launch_bounds__(kBlock, MINB) k_density32q(DevAtoms a, DevTabl
     const size_t ld = (size_t)a.ld;
     if ((a.statu[i] & MSMGB_STATU_ACTIVE) != MSMGB_STATU_ACTIVE) {
         a.den32[i] = 0.0f;
-        st_ff(a.rec + i, ld_ff(a.posff + i));
+        store_rec(a, i, ld_ff(a.posff + i));
         return;
     }
     QBox bl;
@@ -441,7 +449,7 @@ __global__ void __launch_bounds__(kBlock, MINB) k_density32q(DevAtoms a, DevTabl
     a.den32[i] = d;
     PosFF r = pi;
     r.d = d;
-    st_ff(a.rec + i, r);
+    store_rec(a, i, r);
 }
 
 // Constants of the table-assisted density pass for the current tables and boxes, false when
@@ -619,6 +627,92 @@ __device__ __forceinline__ void force_loop_batched(const DevAtoms &a, const DevT
     }
 }
 
+// ---- fixed-point records ----------------------------------------------------------------
+// The force loop below gathers each neighbour's 16 B fixed-point record (fix_record) instead of
+// its 32 B float-float one: a separation component is (float)(int)(q_i - q_j) * unit, the
+// wrapping int32 difference being the minimum image along a periodic edge, so the image test
+// and the lo parts disappear from the pair term and a lane's gather is half a sector.  The
+// table index is still the density pass's exact one (pk); only the direction and 1/R come
+// from the fixed-point separation (~1e-7 of its length against ~6e-8 for the float-float one).
+__device__ __forceinline__ void force_pair_fix(const uint4 &pi, const uint4 &pj, unsigned c, float di,
+                                               const float4 &e, const float *fu, KSum &fx, KSum &fy,
+                                               KSum &fz)
+{
+    const float sx = (float)(int)(pi.x - pj.x) * fu[0];
+    const float sy = (float)(int)(pi.y - pj.y) * fu[1];
+    const float sz = (float)(int)(pi.z - pj.z) * fu[2];
+    const float y = rsqrtf(fmaf(sx, sx, fmaf(sy, sy, sz * sz)));
+    const float dk = (float)(c & ((1u << kDkBits) - 1)) * kDkInv;
+    const float P = fmaf(dk, e.y, e.x);
+    const float B = fmaf(dk, e.w, e.z);
+    const float ft = fmaf(P, y, B * (di + __uint_as_float(pj.w))) * y;
+    fx.fma_add(ft, sx);
+    fy.fma_add(ft, sy);
+    fz.fma_add(ft, sz);
+}
+
+// force_loop_batched on the fixed-point records (pi: atom i's record, fu: its box's units)
+template <int UNR>
+__device__ __forceinline__ void force_loop_fix(const DevAtoms &a, const DevTables &t, int i, const uint4 &pi,
+                                               const float *fu, KSum &fx, KSum &fy, KSum &fz)
+{
+    const int *__restrict__ nb = a.indi + i;
+    const unsigned *__restrict__ pk = a.pk + i;
+    const size_t ld = (size_t)a.ld;
+    const int kn = a.kvois[i];
+    const float di = __uint_as_float(pi.w);
+    unsigned cn[UNR];
+    int jn[UNR];
+#pragma unroll
+    for (int u = 0; u < UNR; ++u) {
+        cn[u] = u < kn ? __ldg(pk + u * ld) : kSkip;
+        jn[u] = u < kn ? __ldg(nb + u * ld) : i;
+    }
+    for (int w = 0; w < kn; w += UNR) {
+        unsigned c[UNR];
+        int j[UNR];
+#pragma unroll
+        for (int u = 0; u < UNR; ++u) {
+            c[u] = cn[u];
+            j[u] = jn[u];
+        }
+#pragma unroll
+        for (int u = 0; u < UNR; ++u) {
+            const int sl = w + UNR + u;
+            cn[u] = sl < kn ? __ldg(pk + sl * ld) : kSkip;
+            jn[u] = sl < kn ? __ldg(nb + sl * ld) : i;
+        }
+        uint4 pj[UNR];
+        float4 e[UNR];
+#pragma unroll
+        for (int u = 0; u < UNR; ++u) {
+            const unsigned row = c[u] == kSkip ? 0u : (c[u] >> kDkBits);
+            pj[u] = __ldg(a.rec16 + j[u]);
+            e[u] = __ldg(t.force4 + row);
+        }
+#pragma unroll
+        for (int u = 0; u < UNR; ++u)
+            if (c[u] != kSkip) force_pair_fix(pi, pj[u], c[u], di, e[u], fu, fx, fy, fz);
+    }
+}
+
+// the mixed force pass (single kind) on the fixed-point records
+template <int UNR, int MINB>
+__global__ void __launch_bounds__(kBlock, MINB) k_force32_fix(DevAtoms a, DevTables t)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    KSum fx, fy, fz;
+    if ((a.statu[i] & MSMGB_STATU_ACTIVE) == MSMGB_STATU_ACTIVE) {
+        const DevBox &bb = a.box[a.boxid[i]];
+        const float fu[3] = {bb.fixu[0], bb.fixu[1], bb.fixu[2]};
+        force_loop_fix<UNR>(a, t, i, __ldg(a.rec16 + i), fu, fx, fy, fz);
+    }
+    a.fx[i] = fx.value64();
+    a.fy[i] = fy.value64();
+    a.fz[i] = fz.value64();
+}
+
 template <bool MULTI, int UNR, int MINB, int PF>
 __global__ void __launch_bounds__(kBlock, MINB) k_force32(DevAtoms a, DevTables t)
 {
@@ -662,7 +756,7 @@ __global__ void __launch_bounds__(kBlock) k_density32s(DevAtoms a, DevTables t, 
         unsigned *__restrict__ pk = a.pk + i;
         if ((a.statu[i] & MSMGB_STATU_ACTIVE) != MSMGB_STATU_ACTIVE) {
             a.den32[i] = 0.0f;
-            st_ff(a.rec + i, ld_ff(a.posff + i));
+            store_rec(a, i, ld_ff(a.posff + i));
             continue;
         }
         const BoxF b = load_boxf(a.box[a.boxid[i]]);
@@ -719,7 +813,7 @@ __global__ void __launch_bounds__(kBlock) k_density32s(DevAtoms a, DevTables t, 
         a.den32[i] = d;
         PosFF r = pi;
         r.d = d;
-        st_ff(a.rec + i, r);
+        store_rec(a, i, r);
     }
 }
 
@@ -855,6 +949,47 @@ __global__ void __launch_bounds__(kBlock, MINB) k_force32_vv_sb(DevAtoms a, DevT
     block_max_flush(dmax, a.maxdisp);
 }
 
+// The fused step kernel (single kind) on the fixed-point records; SB: one box, its constants and
+// units as kernel parameters.
+template <int UNR, int MINB, bool SB>
+__global__ void __launch_bounds__(kBlock, MINB) k_force32_vv_fix(DevAtoms a, DevTables t, double th, DevBox bp,
+                                                                 float3 fup)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    float dmax = 0.0f;
+    if (i < a.n) {
+        const int stat = a.statu[i];
+        const bool act = (stat & MSMGB_STATU_ACTIVE) == MSMGB_STATU_ACTIVE;
+        const int bi = SB ? 0 : a.boxid[i];
+        KSum fx, fy, fz;
+        if (act) {
+            float fu[3];
+            if (SB) {
+                fu[0] = fup.x;
+                fu[1] = fup.y;
+                fu[2] = fup.z;
+            } else {
+#pragma unroll
+                for (int k = 0; k < 3; ++k) fu[k] = a.box[bi].fixu[k];
+            }
+            force_loop_fix<UNR>(a, t, i, __ldg(a.rec16 + i), fu, fx, fy, fz);
+        }
+        const double Fx = fx.value64(), Fy = fy.value64(), Fz = fz.value64();
+        a.fx[i] = Fx;
+        a.fy[i] = Fy;
+        a.fz[i] = Fz;
+        const double4_32a p = a.pos[i];
+        if (act) {
+            if (SB) dmax = vv_atom(a, i, stat, bp, th, true, Fx, Fy, Fz, p, a.pos_nxt, a.posff_nxt);
+            else dmax = vv_atom(a, i, stat, a.box[bi], th, true, Fx, Fy, Fz, p, a.pos_nxt, a.posff_nxt);
+        } else {
+            a.pos_nxt[i] = p;
+            a.posff_nxt[i] = a.posff[i];
+        }
+    }
+    block_max_flush(dmax, a.maxdisp);
+}
+
 // ---- cell-tile variants (single kind) ----------------------------------------------------
 // The block's halo (built by k_halo after each list build: the atoms of every cell in the
 // 27-cell stencils of the block's cells, as runs of consecutive sorted atoms) is staged in
@@ -974,7 +1109,7 @@ __global__ void __launch_bounds__(kBlock, MINB) k_density32t(DevAtoms a, DevTabl
     const size_t ld = (size_t)a.ld;
     if ((a.statu[i] & MSMGB_STATU_ACTIVE) != MSMGB_STATU_ACTIVE) {   // the force pass skips it
         a.den32[i] = 0.0f;
-        st_ff(a.rec + i, ld_ff(a.posff + i));          // d = 0
+        store_rec(a, i, ld_ff(a.posff + i));          // d = 0
         return;
     }
     const BoxF b = load_boxf(a.box[a.boxid[i]]);
@@ -993,7 +1128,7 @@ __global__ void __launch_bounds__(kBlock, MINB) k_density32t(DevAtoms a, DevTabl
     a.den32[i] = d;
     PosFF r = pi;
     r.d = d;
-    st_ff(a.rec + i, r);
+    store_rec(a, i, r);
 }
 
 // force loop of the fused tile kernel: force_loop_batched with the neighbour records read
@@ -1334,6 +1469,30 @@ static void fused_variant(msmgb_ctx *c, int code, double h)
     code &= ~32;
     const int g = nblk(c->n, bs);
     const int g256 = nblk(c->n, kBlock);
+    // variants tuned for one box or for the fixed-point records fall back to the same loop on
+    // the box array / the 32 B records when the state no longer allows them
+    if ((code & 64) && c->nbox != 1) code &= ~64;
+    if ((code & 128) && !(c->a.fix_on && c->tab.ngroup == 1)) code &= ~128;
+    if (code & 128) {      // fixed-point records: 128 + 12..17 (+64 one box)
+        const bool sb = (code & 64) != 0;
+        const DevBox &b0 = c->hbox[0];
+        const float3 fu = make_float3(b0.fixu[0], b0.fixu[1], b0.fixu[2]);
+#define MSMGB_FX(U, M)                                                                                         \
+    do {                                                                                                       \
+        if (sb) k_force32_vv_fix<U, M, true><<<g, bs, 0, c->stream>>>(c->a, c->tab, h, b0, fu);                \
+        else k_force32_vv_fix<U, M, false><<<g, bs, 0, c->stream>>>(c->a, c->tab, h, b0, fu);                 \
+    } while (0)
+        switch (code & 63) {
+        case 13: MSMGB_FX(4, 1); break;
+        case 14: MSMGB_FX(2, 4); break;
+        case 15: MSMGB_FX(4, 4); break;
+        case 16: MSMGB_FX(2, 5); break;
+        case 17: MSMGB_FX(4, 5); break;
+        default: MSMGB_FX(2, 1); break;
+        }
+#undef MSMGB_FX
+        return;
+    }
     if (c->tab.ngroup > 1) {      // several table kinds: codes 0-3
         switch (code) {
         case 1: k_force32_vv<4, 1, 0, true><<<g, bs, 0, c->stream>>>(c->a, c->tab, h); break;
@@ -1409,6 +1568,15 @@ int autotune_fused(msmgb_ctx *c)
         for (int code = 12; code < 18; ++code) {
             codes.push_back(64 + code);
             codes.push_back(64 + 32 + code);
+        }
+    if (!multi && c->a.fix_on)      // +128: the fixed-point records (+64 one box)
+        for (int code = 12; code < 18; ++code) {
+            codes.push_back(128 + code);
+            codes.push_back(128 + 32 + code);
+            if (c->nbox == 1) {
+                codes.push_back(128 + 64 + code);
+                codes.push_back(128 + 64 + 32 + code);
+            }
         }
     for (int code : codes) {
         if ((code == 18 || code == 19) && !tma) continue;
@@ -1551,6 +1719,15 @@ static void force_variant(msmgb_ctx *c, int unr)
         }
         return;
     }
+    if (!MULTI && (unr & 128) && c->a.fix_on) {     // +128: the batched loop on the fixed-point records
+        switch (unr & 7) {
+        case 4: k_force32_fix<4, 1><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
+        case 5: k_force32_fix<4, 6><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
+        case 3: k_force32_fix<2, 6><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
+        default: k_force32_fix<2, 1><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
+        }
+        return;
+    }
     if (!MULTI && (unr & 32)) {
         switch (unr & 7) {
         case 4: k_force32<MULTI, 4, 1, 2><<<g, kBlock, 0, c->stream>>>(c->a, c->tab); break;
@@ -1633,7 +1810,13 @@ int autotune_mixed(msmgb_ctx *c)
             if (c->nbox == 1) dc.push_back(512 + v);      // box constants as a kernel parameter
         }
     }
-    const int fcands[15] = {1, 2, 4, 3, 5, 18, 20, 19, 21, 50, 52, 51, 53, 9, 10};
+    // +128 (single kind): the batched loop on the fixed-point records
+    std::vector<int> fcands = {1, 2, 4, 3, 5, 18, 20, 19, 21};
+    if (single) {
+        for (int v : {50, 52, 51, 53, 9, 10}) fcands.push_back(v);
+        if (c->a.fix_on)
+            for (int v : {50, 52, 51, 53}) fcands.push_back(128 + v);
+    }
     const bool log = tune_log();
     cudaEvent_t e0, e1;
     cudaError_t err = cudaEventCreate(&e0);
@@ -1658,8 +1841,7 @@ int autotune_mixed(msmgb_ctx *c)
     c->tune_dens_unroll = bd;
     int rc = launch_density32(c);
     if (rc) return rc;
-    const int ncand = single ? 15 : 9;
-    for (int k = 0; k < ncand; ++k) {
+    for (size_t k = 0; k < fcands.size(); ++k) {
         c->tune_force_unroll = fcands[k];
         for (int r = 0; r < 4; ++r) {
             if (r == 1) cudaEventRecord(e0, c->stream);

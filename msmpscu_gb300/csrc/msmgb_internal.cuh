@@ -39,6 +39,9 @@ struct NvtxRange {
 
 constexpr int kBlock = 256;
 constexpr int kMaxGroups = 16;          // mp_MXGROUP, MD_Const.F90:77
+// longest edge span (the edge, or twice an open edge) of the fixed-point force records: a unit
+// of at most 2.4e-7 A
+constexpr double kFixMaxSpan = 1024.0;
 
 // cell tiles (k_halo): a block of kBlock sorted atoms spanning at most kHaloCells cells,
 // whose halo has at most kHaloRuns runs and kHaloMax atoms, gets a tile; others none
@@ -105,6 +108,11 @@ struct DevBox {
     float qq, qmag;
     float fxq;           // float-float passes: quantum of the integer remainders (power of 2)
     double fxinv;        // 1 / fxq
+    // fixed-point records of the mixed force passes: coordinate k as (x - lo) / fixu[k] mod 2^32,
+    // fixu[k] = L_k / 2^32 on a periodic edge (the wrapping int32 difference is the minimum
+    // image) or 2 L_k / 2^32 on an open one; fixinv[k] = 1 / fixu[k]
+    double fixinv[3];
+    float fixu[3];
     double bs[9];        // BOXSHAPE(K, 1:3) in row K: separations in length units are bs . SEP
     int shaped;          // bs is not the identity (FP64 static calls only)
     int lq[3];           // (L - float(L)) / fxq, exact
@@ -164,6 +172,10 @@ struct DevAtoms {
     const double *icm;   // reciprocal masses per type
     unsigned *pk;        // mixed passes: per-pair table index (KK << 18 | DK * 2^18), ELL layout
     PosFF *rec;          // mixed passes: {position, F'(rho)} records written by the density pass
+    // mixed passes: 16 B fixed-point records {x, y, z (DevBox::fixu units), F'(rho) bits}, also
+    // written by the density pass when fix_on (every box edge short enough, see fix_record)
+    uint4 *rec16;
+    int fix_on;
     PosFX *posfx;        // float-float passes: positions (k_fix) ...
     PosFX *recfx;        // ... and {position, F'(rho)} records written by the density pass
     // cell tiles of the mixed passes (k_halo, after each list build): for the 256 atoms of
@@ -238,6 +250,22 @@ __device__ __forceinline__ void st_ff(PosFF *p, const PosFF &r)
 __device__ __forceinline__ float4 pos_f32(const PosFF &f)
 {
     return make_float4(f.hx + f.lx, f.hy + f.ly, f.hz + f.lz, 0.0f);
+}
+
+// 16 B fixed-point record of an atom for the mixed force passes, from its float-float position
+// (x - lo = hi + lo - L exactly in FP64) and its F'(rho).  With edges up to 1,024 A (2,048 A
+// mapped range on an open edge) the unit is at most 2.4e-7 A, so a separation formed from two
+// records, (float)(int)(q_i - q_j) * unit, carries ~1e-7 of its length.
+__device__ __forceinline__ uint4 fix_record(const PosFF &p, float d, const DevBox &b)
+{
+    const float h[3] = {p.hx, p.hy, p.hz}, l[3] = {p.lx, p.ly, p.lz};
+    unsigned q[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const double t = (((double)h[k] + (double)l[k]) - b.len[k]) * b.fixinv[k];
+        q[k] = (unsigned)(unsigned long long)__double2ll_rn(t);   // mod 2^32
+    }
+    return make_uint4(q[0], q[1], q[2], __float_as_uint(d));
 }
 
 // non-cubic box: DXYZ(K) = sum(BOXSHAPE(K,1:3)*SEP(1:3)) after the minimum image
