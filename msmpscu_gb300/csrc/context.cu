@@ -663,8 +663,12 @@ extern "C" int msmgb_copyin_simbox(msmgb_ctx *c, int nbox, const msmgb_box *boxe
             d.ifpd[k] = boxes[b].ifpd[k] ? 1 : 0;
             {   // fixed-point unit: the edge (periodic) or twice the edge (open) over 2^32
                 const double span = d.ifpd[k] ? d.len[k] : 2.0 * d.len[k];
+                const double S = 4294967296.0 / span;
                 d.fixu[k] = (float)(span / 4294967296.0);
-                d.fixinv[k] = 4294967296.0 / span;
+                d.fixs[k] = (float)S;
+                d.fixlq[k] = (float)(std::nearbyint(d.len[k] / posq) * posq);
+                d.fixll[k] = (float)(d.len[k] - (double)d.fixlq[k]);
+                d.fixa[k] = span > kFixMaxSpan ? 0ull : (unsigned long long)std::llround(posq * S * 4294967296.0);
                 if (span > kFixMaxSpan) fix_ok = false;
             }
             if (d.len[k] <= 0.0) return set_err(c, MSMGB_ERR_ARG, "box length must be positive");
@@ -686,6 +690,7 @@ extern "C" int msmgb_copyin_simbox(msmgb_ctx *c, int nbox, const msmgb_box *boxe
         {   // hi parts are multiples of the quantum posq; |lo_i - lo_j| <= posq
             double ext = 2.0 * std::max(d.len[0], std::max(d.len[1], d.len[2]));
             d.qq = (float)posq;
+            d.qinv = (float)(1.0 / posq);
             d.qmag = (float)(1.5 * ldexp(posq, 23));
             d.dlmax = (float)(2.0 * posq);
             d.dlfx = (float)(2.0 * ldexp(1.0, ilogb(ext) - 23));   // |u - float(u)| <= ulp(2L)/2

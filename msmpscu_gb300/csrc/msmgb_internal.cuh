@@ -110,9 +110,14 @@ struct DevBox {
     double fxinv;        // 1 / fxq
     // fixed-point records of the mixed force passes: coordinate k as (x - lo) / fixu[k] mod 2^32,
     // fixu[k] = L_k / 2^32 on a periodic edge (the wrapping int32 difference is the minimum
-    // image) or 2 L_k / 2^32 on an open one; fixinv[k] = 1 / fixu[k]
-    double fixinv[3];
+    // image) or 2 L_k / 2^32 on an open one.  From a float-float position (hi a multiple of the
+    // quantum qq): x - lo = m qq + r with m = (hi - fixlq) / qq an integer and r = lo - fixll
+    // (fixlq: L rounded to qq, fixll = L - fixlq), and (x - lo) / unit = m fixa 2^-32 + r fixs,
+    // fixa = round(qq / unit 2^32), fixs = 1 / unit
     float fixu[3];
+    float fixlq[3], fixll[3], fixs[3];
+    unsigned long long fixa[3];
+    float qinv;          // 1 / qq
     double bs[9];        // BOXSHAPE(K, 1:3) in row K: separations in length units are bs . SEP
     int shaped;          // bs is not the identity (FP64 static calls only)
     int lq[3];           // (L - float(L)) / fxq, exact
@@ -253,17 +258,23 @@ __device__ __forceinline__ float4 pos_f32(const PosFF &f)
 }
 
 // 16 B fixed-point record of an atom for the mixed force passes, from its float-float position
-// (x - lo = hi + lo - L exactly in FP64) and its F'(rho).  With edges up to 1,024 A (2,048 A
-// mapped range on an open edge) the unit is at most 2.4e-7 A, so a separation formed from two
-// records, (float)(int)(q_i - q_j) * unit, carries ~1e-7 of its length.
+// and its F'(rho), in integer and FP32 arithmetic (DevBox::fixa): the whole units come from the
+// exact 64-bit product m fixa (taken mod 2^64, so mod 2^32 after the shift), the rest
+// (fraction of that product + r / unit, below ~1.2e5 units) in FP32; within one unit of the
+// rounded (x - lo) / unit.  With edge spans up to 1,024 A the unit is at most 2.4e-7 A, so a
+// separation formed from two records, (float)(int)(q_i - q_j) * unit, carries ~1e-7 of its
+// length.
 __device__ __forceinline__ uint4 fix_record(const PosFF &p, float d, const DevBox &b)
 {
     const float h[3] = {p.hx, p.hy, p.hz}, l[3] = {p.lx, p.ly, p.lz};
     unsigned q[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-        const double t = (((double)h[k] + (double)l[k]) - b.len[k]) * b.fixinv[k];
-        q[k] = (unsigned)(unsigned long long)__double2ll_rn(t);   // mod 2^32
+        const int m = __float2int_rn((h[k] - b.fixlq[k]) * b.qinv);           // exact
+        const unsigned long long P = (unsigned long long)(long long)m * b.fixa[k];
+        const float fr = __uint2float_rn((unsigned)P) * 2.3283064365386963e-10f;   // 2^-32
+        const float f = fmaf(l[k] - b.fixll[k], b.fixs[k], fr);
+        q[k] = (unsigned)(P >> 32) + (unsigned)__float2int_rn(f);
     }
     return make_uint4(q[0], q[1], q[2], __float_as_uint(d));
 }
