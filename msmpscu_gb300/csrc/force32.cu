@@ -708,9 +708,10 @@ __global__ void __launch_bounds__(kBlock, MINB) k_force32_fix(DevAtoms a, DevTab
         const float fu[3] = {bb.fixu[0], bb.fixu[1], bb.fixu[2]};
         force_loop_fix<UNR>(a, t, i, __ldg(a.rec16 + i), fu, fx, fy, fz);
     }
-    a.fx[i] = fx.value64();
-    a.fy[i] = fy.value64();
-    a.fz[i] = fz.value64();
+    // the compensated sums finished in FP32 as in the fused kernel on these records
+    a.fx[i] = (double)fx.value();
+    a.fy[i] = (double)fy.value();
+    a.fz[i] = (double)fz.value();
 }
 
 template <bool MULTI, int UNR, int MINB, int PF>
@@ -974,7 +975,9 @@ __global__ void __launch_bounds__(kBlock, MINB) k_force32_vv_fix(DevAtoms a, Dev
             }
             force_loop_fix<UNR>(a, t, i, __ldg(a.rec16 + i), fu, fx, fy, fz);
         }
-        const double Fx = fx.value64(), Fy = fy.value64(), Fz = fz.value64();
+        // the compensated sums finished in FP32 (one rounding, ~6e-8 of the force) and widened
+        // once: two FP64 instructions fewer per component in the FP64-heavy epilogue
+        const double Fx = (double)fx.value(), Fy = (double)fy.value(), Fz = (double)fz.value();
         a.fx[i] = Fx;
         a.fy[i] = Fy;
         a.fz[i] = Fz;
