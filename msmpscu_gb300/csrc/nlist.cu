@@ -220,19 +220,25 @@ __device__ __forceinline__ float mi32(float s, float len, float half, int pd)
     return (pd && fabsf(s) > half) ? s - copysignf(len, s) : s;
 }
 
-// Records a candidate that passed the FP32 test or, inside the narrow band around the
-// cutoff, the exact FP64 rule of the oracle.
-__device__ __forceinline__ bool accept(float d2f, float d2lo, float d2hi, const DevAtoms &a, int i, int j,
-                                       const DevBox &b, double rc2)
+// The exact FP64 rule of the oracle: d^2 < rc^2 on the FP64 positions after the minimum image.
+__device__ __forceinline__ bool fp64_rule(const DevAtoms &a, int i, int j, const DevBox &b, double rc2)
 {
-    if (d2f < d2lo) return true;
-    if (d2f > d2hi) return false;
     const double4_32a p = a.pos[i];
     const double4_32a qd = a.pos[j];
     const double dx = mi64(p.x - qd.x, b.len[0], b.half[0], b.ifpd[0]);
     const double dy = mi64(p.y - qd.y, b.len[1], b.half[1], b.ifpd[1]);
     const double dz = mi64(p.z - qd.z, b.len[2], b.half[2], b.ifpd[2]);
     return (dx * dx + dy * dy + dz * dz) < rc2;
+}
+
+// Records a candidate that passed the FP32 test or, inside the narrow band around the
+// cutoff, the exact FP64 rule.
+__device__ __forceinline__ bool accept(float d2f, float d2lo, float d2hi, const DevAtoms &a, int i, int j,
+                                       const DevBox &b, double rc2)
+{
+    if (d2f < d2lo) return true;
+    if (d2f > d2hi) return false;
+    return fp64_rule(a, i, j, b, rc2);
 }
 
 // Full neighbour list, one thread per (sorted) atom.  Cells of a box are at least rc_nl
@@ -468,6 +474,38 @@ __global__ void __launch_bounds__(kBlock, 6) k_build_cand(DevAtoms a, const int 
     kcand[i] = nn;
 }
 
+// accept() for a candidate whose float-float record pj is at hand: inside the FP32 band, the
+// float-float distance of the two records (hi parts on the quantum, so the sum of squared hi
+// differences is exact; the lo parts as dl (2 dh + dl)) lies within ~5e-8 A^2 of the FP64 one
+// (lo parts rounded to ~2^-25 of the quantum, the rounding of the lo terms), so the FP64 rule
+// decides only pairs within 2e-7 A^2 of rc^2: the same sets, with the FP64 pipe nearly idle.
+__device__ __forceinline__ bool accept_ff(float d2f, float d2lo, float d2hi, const DevAtoms &a, int i, int j,
+                                          const PosFF &pj, const DevBox &b, double rc2, float rc2h, float rc2l)
+{
+    if (d2f < d2lo) return true;
+    if (d2f > d2hi) return false;
+    const PosFF pi = ld_ff(a.posff + i);
+    const float hi[3] = {pi.hx, pi.hy, pi.hz}, li[3] = {pi.lx, pi.ly, pi.lz};
+    const float hj[3] = {pj.hx, pj.hy, pj.hz}, lj[3] = {pj.lx, pj.ly, pj.lz};
+    float S = 0.0f, C = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        float dh = hi[k] - hj[k];                      // exact multiple of the quantum
+        float dl = li[k] - lj[k];
+        if (b.ifpd[k] && fabsf(dh) > b.halff[k]) {
+            const float sg = copysignf(1.0f, dh);
+            dh = fmaf(-sg, b.fixlq[k], dh);            // exact (L rounded to the quantum)
+            dl = fmaf(-sg, b.fixll[k], dl);
+        }
+        S = fmaf(dh, dh, S);                           // exact
+        C = fmaf(dl, fmaf(2.0f, dh, dl), C);
+    }
+    const float diff = (S - rc2h) + (C - rc2l);        // S - rc2h exact (Sterbenz)
+    if (diff < -2e-7f) return true;
+    if (diff > 2e-7f) return false;
+    return fp64_rule(a, i, j, b, rc2);
+}
+
 // The list from the candidates at the current positions; also the skin reference pos_bld.
 // Candidates are taken kInnerUnr at a time, their indices one group ahead, so the position
 // gathers of a group overlap.  No candidate has left its box: an exit since the full rebuild
@@ -475,7 +513,7 @@ __global__ void __launch_bounds__(kBlock, 6) k_build_cand(DevAtoms a, const int 
 constexpr int kInnerUnr = 4;
 
 __global__ void __launch_bounds__(kBlock, 4) k_inner(DevAtoms a, const int *cand, const int *kcand, double rc2,
-                                                  float d2lo, float d2hi)
+                                                  float d2lo, float d2hi, float rc2h, float rc2l)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
@@ -522,7 +560,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_inner(DevAtoms a, const int *cand
             const float sy = mi32(pf.y - g.y, lf[1], hf[1], pd[1]);
             const float sz = mi32(pf.z - g.z, lf[2], hf[2], pd[2]);
             const float d2f = fmaf(sx, sx, fmaf(sy, sy, sz * sz));
-            if (accept(d2f, d2lo, d2hi, a, i, j[u], b, rc2)) {
+            if (accept_ff(d2f, d2lo, d2hi, a, i, j[u], q[u], b, rc2, rc2h, rc2l)) {
                 if (nn < mxk) indi[(size_t)nn * ld] = j[u];
                 ++nn;
             }
@@ -830,7 +868,8 @@ int build_inner(msmgb_ctx *c)
     const double rc2 = c->p.rc_nl * c->p.rc_nl;
     float d2lo, d2hi;
     prefilter_band(c, rc2, &d2lo, &d2hi);
-    k_inner<<<nblk(c->n, kBlock), kBlock, 0, c->stream>>>(c->a, c->cand, c->kcand, rc2, d2lo, d2hi);
+    const float rc2h = (float)rc2, rc2l = (float)(rc2 - (double)rc2h);
+    k_inner<<<nblk(c->n, kBlock), kBlock, 0, c->stream>>>(c->a, c->cand, c->kcand, rc2, d2lo, d2hi, rc2h, rc2l);
     c->launches += 1;
     return finish_list(c);
 }

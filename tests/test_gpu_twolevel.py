@@ -208,3 +208,31 @@ def test_two_species_fused_128_thread_blocks(oracle, u256, u128):
         out.append((x, v, e.get_force()))
         e.close()
     assert all(np.array_equal(a, b) for a, b in zip(out[0], out[1]))
+
+
+def test_pairs_at_the_cutoff_decided_by_the_fp64_rule(oracle):
+    """Pairs placed at rc_nl itself and one or a few FP64 ulps either side: the re-selection's
+    float-float distance cannot separate them from rc_nl, so they fall through to the exact
+    FP64 rule, and the sets equal the oracle's (d^2 < rc^2 in FP64)."""
+    rng = np.random.default_rng(17)
+    p, L_ = lt.fcc(8, 8, 8, lt.CU_A)
+    p = lt.displace(p, 0.05, rng, np.zeros(3), L_)
+    n = len(p)
+    rc = lt.CU_RC_NL
+    # move atom b of some pairs so that |x_a - x_b| is rc (and rc +- k ulp) along a random direction
+    picks = rng.choice(n, 40, replace=False)
+    for m in range(0, 40, 2):
+        a_, b_ = picks[m], picks[m + 1]
+        d = rng.normal(size=3)
+        d /= np.linalg.norm(d)
+        r = np.nextafter(rc, np.inf if m % 4 == 0 else -np.inf) if m % 8 else rc
+        p[b_] = (p[a_] + r * d) % L_
+    for prec in ("fp64", "mixed"):
+        e = _engine(n, prec, 1.0)
+        e.copyin([(n, (0, 0, 0), tuple(L_), (1, 1, 1))], p)
+        e.calforce()
+        kv, ind = e.get_neighborelist()
+        x = e.get_state()[0]
+        okv, oind = oracle.nlist(x, np.ones(n, np.int32), oracle.make_box([0, 0, 0], L_), rc, 96)
+        assert sorted_sets(kv, ind) == sorted_sets(okv, oind), prec
+        e.close()
