@@ -590,13 +590,12 @@ def run_ours(args):
 
     # e2e: the reference-facing C-ABI with pinned host buffers: copy-in of the state, the K
     # steps, copy-out of positions, velocities and forces, all inside the timed region
-    xp, xp1, ty, st, fo = pinned_buffers(n)
+    xp, xp1, ty, st, fo, xo, vo = pinned_buffers(n)
     xp[:] = np.ascontiguousarray(pos.T).reshape(-1)
     xp1[:] = np.ascontiguousarray(vel.T).reshape(-1)
     ty[:] = 1
     st[:] = 1
     barr = e.pack_boxes(box)
-    xo, vo = np.empty_like(xp), np.empty_like(xp1)
     e.synchronize()
     t0 = time.perf_counter()
     e.copyin_raw(barr, 1, ty, st, xp, xp1)
@@ -674,16 +673,19 @@ def run_ours(args):
 
 
 def pinned_buffers(n):
+    """Page-locked host arrays for the end-to-end leg: positions, velocities, types and status
+    going in; forces, positions and velocities coming out."""
     try:
         import torch
         if torch.cuda.is_available():
             mk = lambda k, dt: torch.empty(k, dtype=dt, pin_memory=True).numpy()
             return (mk(3 * n, torch.float64), mk(3 * n, torch.float64), mk(n, torch.int32),
-                    mk(n, torch.int32), mk(3 * n, torch.float64))
+                    mk(n, torch.int32), mk(3 * n, torch.float64), mk(3 * n, torch.float64),
+                    mk(3 * n, torch.float64))
     except Exception:
         pass
     return (np.empty(3 * n), np.empty(3 * n), np.empty(n, np.int32), np.empty(n, np.int32),
-            np.empty(3 * n))
+            np.empty(3 * n), np.empty(3 * n), np.empty(3 * n))
 
 
 def read_traffic(prec, kernel):
