@@ -2,8 +2,9 @@
 the box, F'(rho) in the fourth word; the table index still the density pass's exact one):
 forces within the mixed bar of 1e-6 of the FP64 oracle and within 5e-7 of the variants on
 the 32 B float-float records, in FS and EAM, with inactive atoms, open faces and several
-boxes; MD with the fused step kernel on them; the fall-back to the 32 B records when an edge
-exceeds the records' span, and of the one-box variants when the state has several boxes."""
+boxes; MD with the fused step kernel on them, bitwise equal to the unfused step; the
+fall-back to the 32 B records when an edge exceeds the records' span, and of the one-box
+variants when the state has several boxes."""
 import numpy as np
 import pytest
 
@@ -170,3 +171,27 @@ def test_one_box_variants_fall_back_with_several_boxes(oracle):
     assert _rel(f, np.vstack(refs)) < 1e-6
     e.run_steps(5, 1.0)
     e.close()
+
+
+@pytest.mark.parametrize("fused", [128 + 64 + 32 + 15, 128 + 32 + 15])
+def test_fused_step_equals_unfused_step_bitwise(fused):
+    """The fused step kernel on the fixed-point records against the unfused step (the
+    integrator kernel, the density pass and the fixed-point force pass, forced by a zero
+    external field): the same forces, corrector and predictor arithmetic, so bitwise the same
+    trajectory, forces and list rebuilds."""
+    pos, vel, L_ = lt.cu_config(12, 0.08, 1200.0, 29)
+    n = len(pos)
+    out = []
+    for zero_field in (False, True):
+        e = _cu_engine(n, skin_trigger=0.15)
+        e.copyin([(n, (0, 0, 0), tuple(L_), (1, 1, 1))], pos, vel)
+        e.set_tuning(density=275, force=128 + 52, fused=fused)
+        if zero_field:
+            e.set_extforce_field(np.zeros((n, 3)))
+        reb = e.run_steps(40, 1.0)
+        x, v, _, dis = e.get_state()
+        out.append((x, v, dis, e.get_force(), reb))
+        e.close()
+    for u, w in zip(out[0][:4], out[1][:4]):
+        assert np.array_equal(u, w)
+    assert out[0][4] == out[1][4] and out[0][4] > 0
