@@ -310,6 +310,34 @@ def _force_err(f, ref):
     return (np.linalg.norm(f - ref) / np.linalg.norm(ref), np.abs(f - ref).max() / np.abs(ref).max())
 
 
+def test_full_size_c2_mixed_md_properties_and_parity(oracle):
+    """2,048,000-atom Cu in mixed precision with the autotuned kernels (the fixed-point force
+    records, the two-level list): after 60 MD steps with list rebuilds inside the step graph,
+    the forces at the final positions against the FP64 oracle's (norm and max below 1e-6),
+    momentum conservation of the force field, and the neighbour sets of a sample of atoms
+    after a full list build at those positions."""
+    pos, vel, L_ = lt.cu_config(80, 0.05, 600.0, 7)
+    n = len(pos)
+    e = _cu_engine(n, precision="mixed")
+    e.set_masses([lt.CU_MASS])
+    e.copyin(_box(n, L_), pos, vel)
+    reb = e.run_steps(60, 1.0)
+    assert reb > 0
+    x = e.get_state()[0]
+    f = e.get_force()
+    assert np.abs(f.sum(0)).max() < 1e-6 * np.sqrt(n) * np.abs(f).max()
+    t = cu_tables(oracle)
+    ref, okv, oind = _oracle_force(oracle, x, L_, t, mxk=80)
+    nrm, mx = _force_err(f, ref["f"])
+    assert nrm < 1e-6 and mx < 1e-6, (nrm, mx)
+    e.cal_neighborelist()            # a full build at the final positions
+    kv, ind = e.get_neighborelist()
+    rng = np.random.default_rng(1)
+    for i in rng.choice(n, 2000, replace=False):
+        assert sorted(ind[:kv[i], i].tolist()) == sorted(oind[:okv[i], i].tolist())
+    e.close()
+
+
 @pytest.mark.parametrize("ncell,sigma,seed", [(10, 0.05, 2024), (8, 0.1, 5)])
 def test_mixed_force_error_below_1e6(oracle, ncell, sigma, seed):
     """FP32 pair/density/table terms: force error against the FP64 oracle (norm-wise and
