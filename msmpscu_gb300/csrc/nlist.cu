@@ -441,11 +441,14 @@ __global__ void __launch_bounds__(kBlock, 6) k_build_cand(DevAtoms a, const int 
         const int g = rank[cell0 + j3[0] + nc[0] * (j3[1] + nc[1] * j3[2])];
         const int j0 = start[g], e = start[g + 1];
         if (wide) {   // cells of at least rc_nl + skin: the stencil cell's image is the nearest
+            // atom i's position shifted once per stencil cell (the shift's rounding, at most
+            // ulp(3L)/2 per component, lies inside the prefilter margin of this superset test)
+            const float px = pf.x + sh[0], py = pf.y + sh[1], pz = pf.z + sh[2];
             for (int j = j0; j < e; ++j) {
                 const float4 q = hi[j];
-                const float sx = (pf.x - q.x) + sh[0];
-                const float sy = (pf.y - q.y) + sh[1];
-                const float sz = (pf.z - q.z) + sh[2];
+                const float sx = px - q.x;
+                const float sy = py - q.y;
+                const float sz = pz - q.z;
                 const float d2f = fmaf(sx, sx, fmaf(sy, sy, sz * sz));
                 if (j != i && d2f < d2o) {
                     if (nn < mxo) out[(size_t)nn * ld] = j;
