@@ -555,6 +555,8 @@ def run_ours(args):
     n = len(pos)
     prec = args.precision
     e = make_engine(n, prec, device, args.outer_skin)
+    if args.steps_per_graph > 1:
+        e.set_steps_per_graph(args.steps_per_graph)
     box = [(n, (0, 0, 0), tuple(L), (1, 1, 1))]
     e.copyin(box, pos, vel)
     if args.pin:
@@ -719,6 +721,8 @@ def main():
     ap.add_argument("--pin", default=None,
                     help="mixed passes: kernel variant codes density,force,fused instead of the tuner's")
     ap.add_argument("--cpu-steps", type=int, default=2)
+    ap.add_argument("--steps-per-graph", type=int, default=1,
+                    help="MD steps captured per CUDA graph launch (msmgb_set_steps_per_graph)")
     ap.add_argument("--case", default="md", choices=["md", "hvp", "adjoint"],
                     help="hvp / adjoint: only that differentiation call (profiling captures)")
     ap.add_argument("--snapshots", type=int, default=64, help="--case adjoint: number of Cu boxes")
