@@ -6,25 +6,29 @@
 // neighbour shell, and the Cleri-Rosato exponentials change by ~11x the relative change of r,
 // so an index SK = CSI sqrt(r) taken from FP32 r^2 alone would carry ~1e-6 relative error
 // into every pair term.  The index is therefore computed from an exact separation:
-//   * positions are kept as float-float in the shifted frame u = x - lo + L in [L, 2L], so
-//     dh = hi_i - hi_j is exact (Sterbenz) and so is the image shift by float(L); the rest
-//     dl = lo_i - lo_j (+ the low part of L) is below 1e-4 A;
-//   * r^2 = sum dh^2 + 2 dh dl is formed in float-float (exact squares through fma, exact
-//     sums through two-sum); the cutoff test compares it with float-float RU^2, i.e. the
-//     FP64 rule up to ~1e-13 relative;
-//   * SK = CSI r2^(1/4): two MUFU reciprocal square roots and one Newton correction
-//     evaluated in float-float give DK to ~1e-7.
+//   * positions are kept as float-float in the shifted frame u = x - lo + L in [L, 2L], the
+//     hi parts on a power-of-two quantum, so dh = hi_i - hi_j is exact and so is the image
+//     shift by L rounded to the quantum; the rest dl = lo_i - lo_j (+ the rest of L) is below
+//     the quantum;
+//   * r^2 = sum dh^2 + sum dl (2 dh + dl) as a float-float pair (sum dh^2 exact in FP32); the
+//     cutoff test compares it with float-float RU^2;
+//   * SK from one table row holding r2_k = (k/CSI)^4 (k_density32q) or from two MUFU
+//     reciprocal square roots and one Newton correction in float-float (k_density32).
 // The density pass stores the table index of every pair it accepts (KK << 18 | DK * 2^18,
 // DK quantised to 4e-6, i.e. a table-value error below 1e-8) in the ELL layout of the
 // list; the force pass reads it back instead of recomputing the separation in float-float
-// and only forms the FP32 separation for the force direction and 1/R.
+// and only forms an FP32 separation for the force direction and 1/R.
 // Table values come from interleaved {value, slope} FP32 rows (one 8 B or 16 B load per
-// pair); rho and F accumulate in FP32 (measured error ~3e-7 of the FP64 forces).
+// pair); rho and F accumulate in compensated FP32 (measured error ~3e-7 of the FP64 forces).
 // Positions, the integrator and the list stay FP64.  The density pass also writes each
-// atom's {position, F'(rho)} record, so the force pass gets both with one 32 B gather.
+// atom's {position, F'(rho)} record, 32 B float-float and, while every box edge span is
+// within 1,024 A, 16 B fixed-point (coordinates as 32-bit fractions of the box), so the force
+// pass gets both with one gather; on the fixed-point records a separation is the wrapping
+// int32 difference times the unit.
 // Every pass exists in several variants (neighbours in flight, register caps, list
-// prefetch, batched gathers, TMA-streamed list tiles, shared-memory table windows) that
-// the autotuner times once per atom count.
+// prefetch, batched gathers, one-box constants, the two record formats, TMA-streamed list
+// tiles, cell tiles, shared-memory table windows) that the autotuner times once per atom
+// count.
 #include <algorithm>
 #include <cstring>
 #include <cstdio>
