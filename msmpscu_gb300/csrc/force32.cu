@@ -371,17 +371,18 @@ __global__ void __launch_bounds__(kBlock, MINB) k_density32q(DevAtoms a, DevTabl
         const float r2l = C - (r2h - S);
         if (r2h > t.ru2h || (r2h == t.ru2h && r2l > t.ru2l)) return 0.0f;
         const float ti = rsqrtf(r2h);
-        const float sk0 = t.csih * rsqrtf(ti);
-        int kk = min(max((int)sk0, 1), t.ntab);
+        const float sk0 = t.csih * rsqrtf(ti);          // >= 0
+        int kk = min((int)sk0, t.ntab);
         const float4 e = __ldg(rows + kk);
         const float d = (r2h - e.z) + (r2l - e.w);
         const float x = d * (ti * ti);
         float dk = 0.25f * sk0 * x * fmaf(0.375f, x, 1.0f);
         const float v = fmaf(dk, e.y, e.x);
-        if (dk < 0.0f) { kk -= 1; dk += 1.0f; }
-        else if (dk >= 1.0f) { kk += 1; dk -= 1.0f; }
-        kk = min(max(kk, 0), t.ntab);
-        dk = fminf(fmaxf(dk, 0.0f), 1.0f);
+        // DK just outside [0, 1) moves the code to the neighbouring segment (dk - floor(dk) is
+        // exact)
+        const float fl = floorf(dk);
+        kk = min(max(kk + (int)fl, 0), t.ntab);
+        dk -= fl;
         const unsigned q = (unsigned)fminf(fmaf(dk, kDkScale, 0.5f), kDkScale - 1.0f);
         code = ((unsigned)kk << kDkBits) | q;
         return v;
