@@ -367,14 +367,14 @@ __global__ void __launch_bounds__(kBlock, MINB) k_density32q(DevAtoms a, DevTabl
         if (S > rejs) return 0.0f;
         const float C = fmaf(dl[0], fmaf(2.0f, dh[0], dl[0]),
                              fmaf(dl[1], fmaf(2.0f, dh[1], dl[1]), dl[2] * fmaf(2.0f, dh[2], dl[2])));
-        const float r2h = S + C;
-        const float r2l = C - (r2h - S);
-        if (r2h > t.ru2h || (r2h == t.ru2h && r2l > t.ru2l)) return 0.0f;
-        const float ti = rsqrtf(r2h);
+        // the cutoff rule r^2 = S + C <= RU^2 and D = r^2 - r2_k without forming r^2 as a
+        // float-float pair: S - RU^2_hi and S - r2_k hi are exact (Sterbenz) where it matters
+        if ((S - t.ru2h) + (C - t.ru2l) > 0.0f) return 0.0f;
+        const float ti = rsqrtf(S + C);
         const float sk0 = t.csih * rsqrtf(ti);          // >= 0
         int kk = min((int)sk0, t.ntab);
         const float4 e = __ldg(rows + kk);
-        const float d = (r2h - e.z) + (r2l - e.w);
+        const float d = (S - e.z) + (C - e.w);
         const float x = d * (ti * ti);
         float dk = 0.25f * sk0 * x * fmaf(0.375f, x, 1.0f);
         const float v = fmaf(dk, e.y, e.x);
