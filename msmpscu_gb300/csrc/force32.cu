@@ -279,8 +279,8 @@ __global__ void __launch_bounds__(kBlock, MINB) k_density32(DevAtoms a, DevTable
 //     a power of two with every component of an accepted pair below 2^11 q (RU below ~18 A at
 //     the smallest q, 2^-7 A); the hi differences dh are exact multiples of q and
 //     dhx^2 + dhy^2 + dhz^2 is an integer times q^2 below 2^24 q^2, exact in FP32; the lo
-//     parts' difference dl (below q) enters r^2 as C = sum dl (2 dh + dl), and r^2 = S + C as
-//     a float-float pair needs no two-sum;
+//     parts' difference dl (below q) enters r^2 as C = sum dl (2 dh + dl), and the cutoff test
+//     and D below take S and C as they are (S - RU^2 and S - r2_k exact by Sterbenz);
 //   * the sqrt(r) index by one table row: SK0 = CSI rsqrt(rsqrt(r^2)) (FP32) gives the grid
 //     point k = int(SK0); the row holds r2_k = (k/CSI)^4 as float-float, and with
 //     D = r^2 - r2_k (exact difference) the fraction is
