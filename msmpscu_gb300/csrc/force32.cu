@@ -323,8 +323,9 @@ __host__ __device__ __forceinline__ QBox qbox_of(const DevBox &bb, float qm)
 }
 
 // SB (one box): the box constants come from the kernel parameter qbp (the constant bank)
-// instead of per-thread registers loaded from the box array.
-template <int POT, int UNR, int MINB, bool PF, bool SB = false>
+// instead of per-thread registers loaded from the box array.  PER: every box is periodic along
+// all three edges (no per-edge periodicity test in the image).
+template <int POT, int UNR, int MINB, bool PF, bool SB = false, bool PER = false>
 __global__ void __launch_bounds__(kBlock, MINB) k_density32q(DevAtoms a, DevTables t, float qm, float rejs,
                                                              QBox qbp)
 {
@@ -356,7 +357,7 @@ __global__ void __launch_bounds__(kBlock, MINB) k_density32q(DevAtoms a, DevTabl
         for (int k = 0; k < 3; ++k) {
             dh[k] = ih[k] - h[k];                                 // exact multiple of q
             dl[k] = il[k] - l[k];
-            if (((b.pd >> k) & 1) && fabsf(dh[k]) > b.half[k]) {
+            if ((PER || ((b.pd >> k) & 1)) && fabsf(dh[k]) > b.half[k]) {
                 const float sg = copysignf(1.0f, dh[k]);
                 dh[k] = fmaf(-sg, b.lq[k], dh[k]);                // exact
                 dl[k] = fmaf(-sg, b.ll[k], dl[k]);
@@ -1653,15 +1654,23 @@ static void dens_variant(msmgb_ctx *c, int unr)
         // +512: one box, its constants as a kernel parameter
         const bool sb = (unr & 512) != 0 && c->nbox == 1;
         const QBox qb = qbox_of(c->hbox[0], qm);
-#define MSMGB_DQ(U, M)                                                                                       \
-    do {                                                                                                     \
-        if (sb) {                                                                                            \
-            if (pf) k_density32q<POT, U, M, true, true><<<g, bs, 0, c->stream>>>(c->a, c->tab, qm, rejs, qb); \
-            else k_density32q<POT, U, M, false, true><<<g, bs, 0, c->stream>>>(c->a, c->tab, qm, rejs, qb); \
-        } else {                                                                                             \
-            if (pf) k_density32q<POT, U, M, true><<<g, bs, 0, c->stream>>>(c->a, c->tab, qm, rejs, qb);      \
-            else k_density32q<POT, U, M, false><<<g, bs, 0, c->stream>>>(c->a, c->tab, qm, rejs, qb);        \
-        }                                                                                                    \
+        // the prefetch variants also exist for states whose boxes are all periodic in x, y, z
+        bool per = true;
+        for (const DevBox &bx : c->hbox) per = per && bx.ifpd[0] && bx.ifpd[1] && bx.ifpd[2];
+#define MSMGB_DQ(U, M)                                                                                        \
+    do {                                                                                                      \
+        if (sb) {                                                                                             \
+            if (pf && per)                                                                                    \
+                k_density32q<POT, U, M, true, true, true><<<g, bs, 0, c->stream>>>(c->a, c->tab, qm, rejs, qb); \
+            else if (pf)                                                                                      \
+                k_density32q<POT, U, M, true, true><<<g, bs, 0, c->stream>>>(c->a, c->tab, qm, rejs, qb);     \
+            else k_density32q<POT, U, M, false, true><<<g, bs, 0, c->stream>>>(c->a, c->tab, qm, rejs, qb);  \
+        } else {                                                                                              \
+            if (pf && per)                                                                                    \
+                k_density32q<POT, U, M, true, false, true><<<g, bs, 0, c->stream>>>(c->a, c->tab, qm, rejs, qb); \
+            else if (pf) k_density32q<POT, U, M, true><<<g, bs, 0, c->stream>>>(c->a, c->tab, qm, rejs, qb);  \
+            else k_density32q<POT, U, M, false><<<g, bs, 0, c->stream>>>(c->a, c->tab, qm, rejs, qb);         \
+        }                                                                                                     \
     } while (0)
         switch (unr & 7) {
         case 3: MSMGB_DQ(2, 5); break;
