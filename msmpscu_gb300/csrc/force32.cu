@@ -640,9 +640,12 @@ __device__ __forceinline__ void force_loop_batched(const DevAtoms &a, const DevT
 // and the lo parts disappear from the pair term and a lane's gather is half a sector.  The
 // table index is still the density pass's exact one (pk); only the direction and 1/R come
 // from the fixed-point separation (~1e-7 of its length against ~6e-8 for the float-float one).
-__device__ __forceinline__ void force_pair_fix(const uint4 &pi, const uint4 &pj, unsigned c, float di,
-                                               const float4 &e, const float *fu, KSum &fx, KSum &fy,
-                                               KSum &fz)
+
+// The pair term on two fixed-point records as the three products ft s_k (zero for a skipped
+// slot)
+__device__ __forceinline__ void pair_terms_fix(const uint4 &pi, const uint4 &pj, unsigned c, float di,
+                                               const float4 &e, const float *fu, float &tx, float &ty,
+                                               float &tz)
 {
     const float sx = (float)(int)(pi.x - pj.x) * fu[0];
     const float sy = (float)(int)(pi.y - pj.y) * fu[1];
@@ -651,13 +654,16 @@ __device__ __forceinline__ void force_pair_fix(const uint4 &pi, const uint4 &pj,
     const float dk = (float)(c & ((1u << kDkBits) - 1)) * kDkInv;
     const float P = fmaf(dk, e.y, e.x);
     const float B = fmaf(dk, e.w, e.z);
-    const float ft = fmaf(P, y, B * (di + __uint_as_float(pj.w))) * y;
-    fx.fma_add(ft, sx);
-    fy.fma_add(ft, sy);
-    fz.fma_add(ft, sz);
+    const float ft = c != kSkip ? fmaf(P, y, B * (di + __uint_as_float(pj.w))) * y : 0.0f;
+    tx = ft * sx;
+    ty = ft * sy;
+    tz = ft * sz;
 }
 
-// force_loop_batched on the fixed-point records (pi: atom i's record, fu: its box's units)
+// force_loop_batched on the fixed-point records (pi: atom i's record, fu: its box's units).
+// The pair terms of list slots 2m and 2m + 1 are added in FP32 and their sum enters the
+// compensated sum, so its four additions per component are paid once per two slots; the
+// pairing follows the slots, not the batch (UNR is even), so every variant sums alike.
 template <int UNR>
 __device__ __forceinline__ void force_loop_fix(const DevAtoms &a, const DevTables &t, int i, const uint4 &pi,
                                                const float *fu, KSum &fx, KSum &fy, KSum &fz)
@@ -696,9 +702,16 @@ __device__ __forceinline__ void force_loop_fix(const DevAtoms &a, const DevTable
             pj[u] = __ldg(a.rec16 + j[u]);
             e[u] = __ldg(t.force4 + row);
         }
+        static_assert(UNR % 2 == 0, "slots are paired");
+        float tx[UNR], ty[UNR], tz[UNR];
 #pragma unroll
-        for (int u = 0; u < UNR; ++u)
-            if (c[u] != kSkip) force_pair_fix(pi, pj[u], c[u], di, e[u], fu, fx, fy, fz);
+        for (int u = 0; u < UNR; ++u) pair_terms_fix(pi, pj[u], c[u], di, e[u], fu, tx[u], ty[u], tz[u]);
+#pragma unroll
+        for (int u = 0; u < UNR; u += 2) {
+            fx.add(tx[u] + tx[u + 1]);
+            fy.add(ty[u] + ty[u + 1]);
+            fz.add(tz[u] + tz[u + 1]);
+        }
     }
 }
 
