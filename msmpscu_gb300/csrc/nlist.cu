@@ -482,11 +482,14 @@ __global__ void __launch_bounds__(kBlock, 6) k_build_cand(DevAtoms a, const int 
 // differences is exact; the lo parts as dl (2 dh + dl)) lies within ~5e-8 A^2 of the FP64 one
 // (lo parts rounded to ~2^-25 of the quantum, the rounding of the lo terms), so the FP64 rule
 // decides only pairs within 2e-7 A^2 of rc^2: the same sets, with the FP64 pipe nearly idle.
+// The sum of squared hi differences is exact below 2^24 quanta^2 (rc below 32 A at the smallest
+// quantum); beyond that the caller passes rc2h < 0 and every band pair takes the FP64 rule.
 __device__ __forceinline__ bool accept_ff(float d2f, float d2lo, float d2hi, const DevAtoms &a, int i, int j,
                                           const PosFF &pj, const DevBox &b, double rc2, float rc2h, float rc2l)
 {
     if (d2f < d2lo) return true;
     if (d2f > d2hi) return false;
+    if (rc2h < 0.0f) return fp64_rule(a, i, j, b, rc2);
     const PosFF pi = ld_ff(a.posff + i);
     const float hi[3] = {pi.hx, pi.hy, pi.hz}, li[3] = {pi.lx, pi.ly, pi.lz};
     const float hj[3] = {pj.hx, pj.hy, pj.hz}, lj[3] = {pj.lx, pj.ly, pj.lz};
@@ -871,7 +874,12 @@ int build_inner(msmgb_ctx *c)
     const double rc2 = c->p.rc_nl * c->p.rc_nl;
     float d2lo, d2hi;
     prefilter_band(c, rc2, &d2lo, &d2hi);
-    const float rc2h = (float)rc2, rc2l = (float)(rc2 - (double)rc2h);
+    float rc2h = (float)rc2, rc2l = (float)(rc2 - (double)rc2h);
+    {   // the band's float-float decision needs exact sums of squared hi differences (d2hi is
+        // the band's upper edge)
+        const double q = c->hbox.empty() ? 0.0 : (double)c->hbox[0].qq;
+        if (!((double)d2hi < 0.9 * 16777216.0 * q * q)) rc2h = -1.0f;
+    }
     k_inner<<<nblk(c->n, kBlock), kBlock, 0, c->stream>>>(c->a, c->cand, c->kcand, rc2, d2lo, d2hi, rc2h, rc2l);
     c->launches += 1;
     return finish_list(c);
