@@ -100,6 +100,7 @@ def test_identity_shape_is_the_cubic_box():
         if shape is not None:
             e.set_boxshape(0, shape)
         e.copyin([(n, (0, 0, 0), tuple(L_), (1, 1, 1))], pos, vel)
+        e.set_tuning(density=275, force=128 + 50, fused=128 + 32 + 15)   # the same variants in both
         e.run_steps(10, 1.0)
         out.append(e.get_state()[0])
         e.close()
