@@ -929,7 +929,7 @@ __global__ void __launch_bounds__(kBlock, MINB) k_force32_vv(DevAtoms a, DevTabl
         a.fz[i] = Fz;
         const double4_32a p = a.pos[i];
         if ((stat & MSMGB_STATU_ACTIVE) == MSMGB_STATU_ACTIVE) {
-            dmax = vv_atom(a, i, stat, bb, th, true, Fx, Fy, Fz, p, a.pos_nxt, a.posff_nxt);
+            dmax = vv_atom<true>(a, i, stat, bb, th, true, Fx, Fy, Fz, p, a.pos_nxt, a.posff_nxt);
         } else {
             a.pos_nxt[i] = p;
             a.posff_nxt[i] = a.posff[i];
@@ -960,7 +960,7 @@ __global__ void __launch_bounds__(kBlock, MINB) k_force32_vv_sb(DevAtoms a, DevT
         a.fz[i] = Fz;
         const double4_32a p = a.pos[i];
         if ((stat & MSMGB_STATU_ACTIVE) == MSMGB_STATU_ACTIVE) {
-            dmax = vv_atom(a, i, stat, bp, th, true, Fx, Fy, Fz, p, a.pos_nxt, a.posff_nxt);
+            dmax = vv_atom<true>(a, i, stat, bp, th, true, Fx, Fy, Fz, p, a.pos_nxt, a.posff_nxt);
         } else {
             a.pos_nxt[i] = p;
             a.posff_nxt[i] = a.posff[i];
@@ -1002,8 +1002,8 @@ __global__ void __launch_bounds__(kBlock, MINB) k_force32_vv_fix(DevAtoms a, Dev
         a.fz[i] = Fz;
         const double4_32a p = a.pos[i];
         if (act) {
-            if (SB) dmax = vv_atom(a, i, stat, bp, th, true, Fx, Fy, Fz, p, a.pos_nxt, a.posff_nxt);
-            else dmax = vv_atom(a, i, stat, a.box[bi], th, true, Fx, Fy, Fz, p, a.pos_nxt, a.posff_nxt);
+            if (SB) dmax = vv_atom<true>(a, i, stat, bp, th, true, Fx, Fy, Fz, p, a.pos_nxt, a.posff_nxt);
+            else dmax = vv_atom<true>(a, i, stat, a.box[bi], th, true, Fx, Fy, Fz, p, a.pos_nxt, a.posff_nxt);
         } else {
             a.pos_nxt[i] = p;
             a.posff_nxt[i] = a.posff[i];
@@ -1224,7 +1224,7 @@ __global__ void __launch_bounds__(kBlock, MINB) k_force32_vv_t(DevAtoms a, DevTa
         a.fz[i] = Fz;
         const double4_32a p = a.pos[i];
         if ((stat & MSMGB_STATU_ACTIVE) == MSMGB_STATU_ACTIVE) {
-            dmax = vv_atom(a, i, stat, bb, th, true, Fx, Fy, Fz, p, a.pos_nxt, a.posff_nxt);
+            dmax = vv_atom<true>(a, i, stat, bb, th, true, Fx, Fy, Fz, p, a.pos_nxt, a.posff_nxt);
         } else {
             a.pos_nxt[i] = p;
             a.posff_nxt[i] = a.posff[i];
@@ -1417,7 +1417,7 @@ __global__ void __launch_bounds__(kBlock, 4)
         a.fz[i] = Fz;
         const double4_32a p = a.pos[i];
         if (act) {
-            dmax = vv_atom(a, i, stat, a.box[a.boxid[i]], th, true, Fx, Fy, Fz, p, a.pos_nxt, a.posff_nxt);
+            dmax = vv_atom<true>(a, i, stat, a.box[a.boxid[i]], th, true, Fx, Fy, Fz, p, a.pos_nxt, a.posff_nxt);
         } else {
             a.pos_nxt[i] = p;
             a.posff_nxt[i] = a.posff[i];

@@ -322,36 +322,76 @@ __device__ __forceinline__ double advance(double x0, double v, double a, double 
     return x;
 }
 
+// The same coordinate with the displacement formed from the advanced velocity: vk = v + k F
+// (k = the kicks' h/2 or h times 1/m), DIS = h vk.  With k = h/(2m) DIS = h v + h^2/2 F/m as
+// above; with k = h/m (the corrector's and the predictor's half kicks by the same force) vk is
+// v(n+1/2) and DIS = h v(n) + h^2/2 F/m with v(n) the corrected velocity.  Two FP64
+// instructions per component instead of five (F/m, the two kicks, h v, the FMA).  v becomes
+// vk unless the component's velocity is fixed.
+__device__ __forceinline__ double advance_hv(double x0, double &v, double f, double k, bool fv, double th,
+                                             bool fix, int pd, double len, long long klo, long long kub,
+                                             double &dis, int &oob_hi, int &oob_lo)
+{
+    const double vk = fma(k, f, v);
+    const double d = fix ? 0.0 : th * vk;
+    if (!fv) v = vk;
+    double x = x0 + d;
+    long long key = okey(x);
+    if (pd) {
+        if (key > kub) { x = x - len; key = okey(x); }
+        else if (key < klo) { x = x + len; key = okey(x); }
+    }
+    oob_hi |= key > kub;
+    oob_lo |= key < klo;
+    dis = d;
+    return x;
+}
+
 // Corrector of step n (v += h/2 F/m) followed by the predictor of step n+1 for one active
 // atom (Correction_KERNEL :741-749 then Predictor_KERNEL0 :290-378); positions are read from
 // pin and written to pout / fout.  Returns the squared displacement since the last build.
+// HV (the mixed-precision passes): advance_hv, the same update in fewer FP64 instructions,
+// rounded differently (the passes' FP32 forces carry ~1e-7 of the force, far above that);
+// the FP64 and float-float passes keep the reference's operation order.  A fixed velocity
+// component (FIXVEL or FIXPOS) gets no corrector kick, so its k stays h/(2m).
+template <bool HV = false>
 __device__ __forceinline__ float vv_atom(const DevAtoms &a, int i, int stat, const DevBox &b, double th,
                                           bool corrector, double fx, double fy, double fz,
                                           const double4_32a &p, double4_32a *pout, PosFF *fout)
 {
-    const double hs2 = th * 0.5, h2s2 = th * th * 0.5;
     const double icm = a.icm[a.ityp[i] - 1];
     double vx = a.vx[i], vy = a.vy[i], vz = a.vz[i];
-    const double ax = fx * icm, ay = fy * icm, az = fz * icm;
     const bool fvx = (stat & (MSMGB_STATU_FIXVELX | MSMGB_STATU_FIXPOSX)) != 0;
     const bool fvy = (stat & (MSMGB_STATU_FIXVELY | MSMGB_STATU_FIXPOSY)) != 0;
     const bool fvz = (stat & (MSMGB_STATU_FIXVELZ | MSMGB_STATU_FIXPOSZ)) != 0;
-    if (corrector) {
+    int hi = 0, lo = 0;
+    double dx, dy, dz, x, y, z;
+    if constexpr (HV) {
+        const double kf = (th * 0.5) * icm, kv = corrector ? th * icm : kf;
+        x = advance_hv(p.x, vx, fx, fvx ? kf : kv, fvx, th, (stat & MSMGB_STATU_FIXPOSX) != 0, b.ifpd[0],
+                       b.len[0], b.klo[0], b.kub[0], dx, hi, lo);
+        y = advance_hv(p.y, vy, fy, fvy ? kf : kv, fvy, th, (stat & MSMGB_STATU_FIXPOSY) != 0, b.ifpd[1],
+                       b.len[1], b.klo[1], b.kub[1], dy, hi, lo);
+        z = advance_hv(p.z, vz, fz, fvz ? kf : kv, fvz, th, (stat & MSMGB_STATU_FIXPOSZ) != 0, b.ifpd[2],
+                       b.len[2], b.klo[2], b.kub[2], dz, hi, lo);
+    } else {
+        const double hs2 = th * 0.5, h2s2 = th * th * 0.5;
+        const double ax = fx * icm, ay = fy * icm, az = fz * icm;
+        if (corrector) {
+            if (!fvx) vx = fma(hs2, ax, vx);
+            if (!fvy) vy = fma(hs2, ay, vy);
+            if (!fvz) vz = fma(hs2, az, vz);
+        }
+        x = advance(p.x, vx, ax, th, h2s2, (stat & MSMGB_STATU_FIXPOSX) != 0, b.ifpd[0], b.len[0],
+                    b.klo[0], b.kub[0], dx, hi, lo);
+        y = advance(p.y, vy, ay, th, h2s2, (stat & MSMGB_STATU_FIXPOSY) != 0, b.ifpd[1], b.len[1],
+                    b.klo[1], b.kub[1], dy, hi, lo);
+        z = advance(p.z, vz, az, th, h2s2, (stat & MSMGB_STATU_FIXPOSZ) != 0, b.ifpd[2], b.len[2],
+                    b.klo[2], b.kub[2], dz, hi, lo);
         if (!fvx) vx = fma(hs2, ax, vx);
         if (!fvy) vy = fma(hs2, ay, vy);
         if (!fvz) vz = fma(hs2, az, vz);
     }
-    int hi = 0, lo = 0;
-    double dx, dy, dz;
-    const double x = advance(p.x, vx, ax, th, h2s2, (stat & MSMGB_STATU_FIXPOSX) != 0, b.ifpd[0], b.len[0],
-                             b.klo[0], b.kub[0], dx, hi, lo);
-    const double y = advance(p.y, vy, ay, th, h2s2, (stat & MSMGB_STATU_FIXPOSY) != 0, b.ifpd[1], b.len[1],
-                             b.klo[1], b.kub[1], dy, hi, lo);
-    const double z = advance(p.z, vz, az, th, h2s2, (stat & MSMGB_STATU_FIXPOSZ) != 0, b.ifpd[2], b.len[2],
-                             b.klo[2], b.kub[2], dz, hi, lo);
-    if (!fvx) vx = fma(hs2, ax, vx);
-    if (!fvy) vy = fma(hs2, ay, vy);
-    if (!fvz) vz = fma(hs2, az, vz);
     pout[i] = make_double4_32a(x, y, z, p.w);
     const PosFF f = make_posff(x, y, z, b);
     fout[i] = f;

@@ -8,7 +8,9 @@
 //              displacement since the last list build (skin trigger) and refreshes the
 //              float-float copy of the positions used by the list prefilter and the mixed
 //              passes.  The per-atom work is vv_atom() in msmgb_internal.cuh, shared with
-//              the fused mixed force kernel.
+//              the fused mixed force kernel.  Under the mixed-precision passes it runs the
+//              form of the update with fewer FP64 instructions (vv_atom<true>) that the
+//              fused mixed kernel runs, so a fused and an unfused step stay bitwise equal.
 //   k_correct  Correction_KERNEL alone (end of a run, or msmgb_correction()).
 //   k_decide   one thread: rebuild flag for this step from the skin trigger (or the
 //              reference's fixed NB_UPTAB interval, MD_Method_GenericMD_GPU.F90:599-601);
@@ -19,6 +21,7 @@ namespace msmgb {
 
 // mode 0: predictor only; mode 1: corrector of the previous step first when
 // flags[kFlagPending] is set (graph replay), mode 2: always fused.
+template <bool HV>
 __global__ void __launch_bounds__(kBlock) k_vv(DevAtoms a, double th, int mode)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -29,7 +32,7 @@ __global__ void __launch_bounds__(kBlock) k_vv(DevAtoms a, double th, int mode)
         if ((stat & MSMGB_STATU_ACTIVE) == MSMGB_STATU_ACTIVE) {
             const DevBox &b = a.box[a.boxid[i]];
             const double4_32a p = a.pos[i];
-            dmax = vv_atom(a, i, stat, b, th, pend != 0, a.fx[i], a.fy[i], a.fz[i], p, a.pos, a.posff);
+            dmax = vv_atom<HV>(a, i, stat, b, th, pend != 0, a.fx[i], a.fy[i], a.fz[i], p, a.pos, a.posff);
         }
     }
     block_max_flush(dmax, a.maxdisp);
@@ -91,7 +94,10 @@ static inline int nblk(long n, int b) { return (int)((n + b - 1) / b); }
 int launch_vv(msmgb_ctx *c, double h, int mode)
 {
     const int bs = block_for(c->n);
-    k_vv<<<nblk(c->n, bs), bs, 0, c->stream>>>(c->a, h, mode);
+    if (c->p.precision == MSMGB_PREC_MIXED)
+        k_vv<true><<<nblk(c->n, bs), bs, 0, c->stream>>>(c->a, h, mode);
+    else
+        k_vv<false><<<nblk(c->n, bs), bs, 0, c->stream>>>(c->a, h, mode);
     c->launches += 1;
     return check_launch(c, "integrator");
 }
