@@ -302,6 +302,26 @@ __device__ __forceinline__ long long okey(double x)
     return k ^ ((k >> 63) & 0x7fffffffffffffffLL);
 }
 
+// periodic wrap of one new coordinate (x - L above the box, x + L below it; x + (-L) is x - L
+// exactly) and the out-of-box flags from its integer key.  Few atoms cross a face in one step:
+// the shift sits behind a vote of the lanes running this code, so a warp with no crossing lane
+// skips it (if-converted, both shifts ran for every atom).
+__device__ __forceinline__ double wrap_coord(double x, int pd, double len, long long klo, long long kub,
+                                             int &oob_hi, int &oob_lo)
+{
+    long long k = okey(x);
+    const bool out = pd && (k > kub || k < klo);
+    if (__any_sync(__activemask(), out)) {
+        if (out) {
+            x = x + (k > kub ? -len : len);
+            k = okey(x);
+        }
+    }
+    oob_hi |= k > kub;
+    oob_lo |= k < klo;
+    return x;
+}
+
 // one coordinate of Predictor_KERNEL0 (MD_DiffScheme_GPU.F90:314-349): DIS = h v + h^2/2 a
 // (0 if FIXPOS), x += DIS, periodic wrap when x > lo + L or x < lo.  The box tests compare
 // integer keys (same order as the doubles) so they stay off the FP64 pipe.
@@ -309,17 +329,9 @@ __device__ __forceinline__ double advance(double x0, double v, double a, double 
                                           int pd, double len, long long klo, long long kub, double &dis,
                                           int &oob_hi, int &oob_lo)
 {
-    double d = fix ? 0.0 : fma(h2s2, a, th * v);
-    double x = x0 + d;
-    long long k = okey(x);
-    if (pd) {
-        if (k > kub) { x = x - len; k = okey(x); }
-        else if (k < klo) { x = x + len; k = okey(x); }
-    }
-    oob_hi |= k > kub;
-    oob_lo |= k < klo;
+    const double d = fix ? 0.0 : fma(h2s2, a, th * v);
     dis = d;
-    return x;
+    return wrap_coord(x0 + d, pd, len, klo, kub, oob_hi, oob_lo);
 }
 
 // The same coordinate with the displacement formed from the advanced velocity: vk = v + k F
@@ -335,16 +347,8 @@ __device__ __forceinline__ double advance_hv(double x0, double &v, double f, dou
     const double vk = fma(k, f, v);
     const double d = fix ? 0.0 : th * vk;
     if (!fv) v = vk;
-    double x = x0 + d;
-    long long key = okey(x);
-    if (pd) {
-        if (key > kub) { x = x - len; key = okey(x); }
-        else if (key < klo) { x = x + len; key = okey(x); }
-    }
-    oob_hi |= key > kub;
-    oob_lo |= key < klo;
     dis = d;
-    return x;
+    return wrap_coord(x0 + d, pd, len, klo, kub, oob_hi, oob_lo);
 }
 
 // Corrector of step n (v += h/2 F/m) followed by the predictor of step n+1 for one active
@@ -367,7 +371,8 @@ __device__ __forceinline__ float vv_atom(const DevAtoms &a, int i, int stat, con
     int hi = 0, lo = 0;
     double dx, dy, dz, x, y, z;
     if constexpr (HV) {
-        const double kf = (th * 0.5) * icm, kv = corrector ? th * icm : kf;
+        // (h/m)/2 is (h/2)/m exactly
+        const double k1 = th * icm, kf = k1 * 0.5, kv = corrector ? k1 : kf;
         x = advance_hv(p.x, vx, fx, fvx ? kf : kv, fvx, th, (stat & MSMGB_STATU_FIXPOSX) != 0, b.ifpd[0],
                        b.len[0], b.klo[0], b.kub[0], dx, hi, lo);
         y = advance_hv(p.y, vy, fy, fvy ? kf : kv, fvy, th, (stat & MSMGB_STATU_FIXPOSY) != 0, b.ifpd[1],
