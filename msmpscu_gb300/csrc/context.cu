@@ -692,6 +692,10 @@ extern "C" int msmgb_copyin_simbox(msmgb_ctx *c, int nbox, const msmgb_box *boxe
             d.qq = (float)posq;
             d.qinv = (float)(1.0 / posq);
             d.qmag = (float)(1.5 * ldexp(posq, 23));
+            // the float-float records' fixed-point frame: 2^32 units per quantum
+            d.pscale = 4294967296.0 / posq;
+            d.plo = (float)(posq / 4294967296.0);
+            for (int k = 0; k < 3; ++k) d.ushs[k] = d.ushift[k] * d.pscale;
             d.dlmax = (float)(2.0 * posq);
             d.dlfx = (float)(2.0 * ldexp(1.0, ilogb(ext) - 23));   // |u - float(u)| <= ulp(2L)/2
             // float-float passes: remainders u - float(u) (|.| <= ulp(2L)/2) in units of

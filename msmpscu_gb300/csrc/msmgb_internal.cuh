@@ -96,6 +96,9 @@ struct DevBox {
     double len[3];
     double half[3];
     double ushift[3];    // L - lo: u = x + ushift is the float-float frame coordinate
+    double ushs[3];      // ushift 2^S, 2^S = pscale = 2^32 / qq (make_posff)
+    double pscale;
+    float plo;           // 2^-S
     long long klo[3], kub[3];   // order-preserving integer keys of lo and lo + L
     float lenf[3];       // float-float box length (hi, lo) and FP32 half length
     float lenlo[3];
@@ -204,28 +207,29 @@ inline int block_for(int n)
     return 64;
 }
 
-__device__ __forceinline__ void split_ff(double u, float &h, float &l)
+// u = x + ushift = hi + lo with hi the nearest multiple of the box's quantum qq to u and lo the
+// rest, through u in fixed point with 2^32 units per quantum: M = rint(u 2^S), 2^S = 2^32 / qq
+// (the FMA forms (x + ushift) 2^S, rounded once as x + ushift would be: scaling by a power of
+// two commutes with the rounding).  The high word of M + 2^31 is round(u / qq), so hi = that
+// times qq (exact in FP32: |u| < 2^23 qq); the low word less 2^31 is the remainder r in
+// [-2^31, 2^31) units and lo = float(r) 2^-S, |lo| <= qq/2, within qq (2^-26 + 2^-33) of
+// u - hi.  Two FP64-pipe instructions (the FMA and the conversion) instead of the five of a
+// split by conversions to FP32 and back.
+__device__ __forceinline__ void split_q(double x, double scale, double ushs, float qq, float plo, float &h,
+                                        float &l)
 {
-    h = __double2float_rn(u);
-    l = __double2float_rn(u - (double)h);
-}
-
-// u = hi + lo with hi the nearest multiple of the box's quantum qq to float(u) and lo = u - hi
-// (|lo| <= qq/2, carried to ~2^-24 of qq)
-__device__ __forceinline__ void split_q(double u, float qmag, float &h, float &l)
-{
-    float h0, l0;
-    split_ff(u, h0, l0);
-    h = __fsub_rn(__fadd_rn(h0, qmag), qmag);
-    l = __fadd_rn(__fsub_rn(h0, h), l0);
+    // unsigned add: no signed overflow for a saturated conversion of a coordinate far outside
+    const unsigned long long m = (unsigned long long)__double2ll_rn(fma(x, scale, ushs)) + 0x80000000ull;
+    h = __int2float_rn((int)((long long)m >> 32)) * qq;
+    l = __int2float_rn((int)((unsigned)m ^ 0x80000000u)) * plo;
 }
 
 __device__ __forceinline__ PosFF make_posff(double x, double y, double z, const DevBox &b)
 {
     PosFF p;
-    split_q(x + b.ushift[0], b.qmag, p.hx, p.lx);
-    split_q(y + b.ushift[1], b.qmag, p.hy, p.ly);
-    split_q(z + b.ushift[2], b.qmag, p.hz, p.lz);
+    split_q(x, b.pscale, b.ushs[0], b.qq, b.plo, p.hx, p.lx);
+    split_q(y, b.pscale, b.ushs[1], b.qq, b.plo, p.hy, p.ly);
+    split_q(z, b.pscale, b.ushs[2], b.qq, b.plo, p.hz, p.lz);
     p.d = 0.0f;
     p.lw = 0.0f;
     return p;
