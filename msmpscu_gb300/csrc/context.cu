@@ -1278,10 +1278,12 @@ extern "C" int msmgb_correction(msmgb_ctx *c, double h)
 // A step graph is captured into a graph that owns an IF node: k_decide sets its condition on
 // the device, and the node's body holds the list rebuild, so a step without a rebuild runs
 // none of the rebuild kernels.
-// With a two-level list there are two IF nodes in sequence: the full rebuild (binning, sort,
-// candidates) and the list selection from the candidates, which runs on every rebuild.
+// With a two-level list the IF node runs on every rebuild and holds k_set_full, a nested IF
+// node of the full rebuild (binning, sort, candidates) and the list selection from the
+// candidates; a step without a rebuild evaluates that one node (two nodes in sequence cost
+// 12.5 instead of ~6 us per step on a GB300).
 struct RebuildNodes {
-    cudaGraphConditionalHandle cond = 0, cond_inner = 0;
+    cudaGraphConditionalHandle cond = 0, cond_inner = 0;   // single-level: cond; two-level: cond_inner
     cudaGraph_t body = nullptr, body_inner = nullptr;
 };
 
@@ -1289,9 +1291,8 @@ static int begin_step_capture(msmgb_ctx *c, cudaGraph_t *g, RebuildNodes *rn)
 {
     *g = nullptr;
     CK(cudaGraphCreate(g, 0), "graph create");
-    cudaError_t e = cudaGraphConditionalHandleCreate(&rn->cond, *g, 0, cudaGraphCondAssignDefault);
-    if (e == cudaSuccess && two_level(c))
-        e = cudaGraphConditionalHandleCreate(&rn->cond_inner, *g, 0, cudaGraphCondAssignDefault);
+    cudaError_t e = two_level(c) ? cudaGraphConditionalHandleCreate(&rn->cond_inner, *g, 0, cudaGraphCondAssignDefault)
+                                 : cudaGraphConditionalHandleCreate(&rn->cond, *g, 0, cudaGraphCondAssignDefault);
     if (e == cudaSuccess)
         e = cudaStreamBeginCaptureToGraph(c->stream, *g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) {
@@ -1325,12 +1326,11 @@ static int add_rebuild_node(msmgb_ctx *c, cudaGraphConditionalHandle cond, cudaG
     return MSMGB_OK;
 }
 
-// the IF nodes of a rebuild at the current position of the capture
+// the IF node of a rebuild at the current position of the capture
 static int add_rebuild_nodes(msmgb_ctx *c, RebuildNodes *rn)
 {
-    RET(add_rebuild_node(c, rn->cond, &rn->body));
-    if (rn->cond_inner) RET(add_rebuild_node(c, rn->cond_inner, &rn->body_inner));
-    return MSMGB_OK;
+    if (rn->cond_inner) return add_rebuild_node(c, rn->cond_inner, &rn->body_inner);
+    return add_rebuild_node(c, rn->cond, &rn->body);
 }
 
 // the rebuild stage `stage` (0: the whole list build, 1: the full part of a two-level build,
@@ -1351,22 +1351,47 @@ static int fill_rebuild_body(msmgb_ctx *c, cudaGraph_t body, int stage, int64_t 
     return MSMGB_OK;
 }
 
+// the body of a two-level rebuild: k_set_full, the nested IF node of the full rebuild (its
+// body filled with stage 1) and the list selection (stage 2); *nk_full and *nk_inner receive
+// the kernels of the nested body and of the rest
+static int fill_two_level_body(msmgb_ctx *c, cudaGraph_t body, int64_t *nk_full, int64_t *nk_inner)
+{
+    cudaGraphConditionalHandle hf = 0;
+    CK(cudaGraphConditionalHandleCreate(&hf, body, 0, cudaGraphCondAssignDefault), "conditional handle");
+    CK(cudaStreamBeginCaptureToGraph(c->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal),
+       "graph capture");
+    const int64_t l0 = c->launches;
+    cudaGraph_t full = nullptr;
+    int rc = launch_set_full(c, hf);
+    if (!rc) rc = add_rebuild_node(c, hf, &full);
+    if (!rc) rc = build_inner(c);
+    cudaGraph_t out = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(c->stream, &out);
+    *nk_inner = c->launches - l0;
+    c->launches = l0;
+    if (rc) return rc;
+    if (e != cudaSuccess) return cuda_err(c, e, "graph capture");
+    return fill_rebuild_body(c, full, 1, nk_full);
+}
+
+// the rebuild body of one step (two-level or single-level list)
+static int fill_step_rebuild(msmgb_ctx *c, const RebuildNodes &rn)
+{
+    c->gk_inner = 0;
+    if (rn.body_inner) return fill_two_level_body(c, rn.body_inner, &c->gk_body, &c->gk_inner);
+    return fill_rebuild_body(c, rn.body, 0, &c->gk_body);
+}
+
 static int finish_step_graph(msmgb_ctx *c, int rc, cudaGraph_t g, const RebuildNodes &rn, cudaGraphExec_t *out,
                              const DevAtoms &body_view)
 {
     cudaGraph_t ended = nullptr;
     const cudaError_t e = cudaStreamEndCapture(c->stream, &ended);
     if (!rc && e != cudaSuccess) rc = cuda_err(c, e, "graph capture");
-    if (!rc && rn.body) {
+    if (!rc && (rn.body || rn.body_inner)) {
         const DevAtoms keep = c->a;
         c->a = body_view;
-        c->gk_inner = 0;
-        if (rn.body_inner) {
-            rc = fill_rebuild_body(c, rn.body, 1, &c->gk_body);
-            if (!rc) rc = fill_rebuild_body(c, rn.body_inner, 2, &c->gk_inner);
-        } else {
-            rc = fill_rebuild_body(c, rn.body, 0, &c->gk_body);
-        }
+        rc = fill_step_rebuild(c, rn);
         c->a = keep;
     }
     if (!rc) {
@@ -1392,11 +1417,9 @@ static int capture_k_steps(msmgb_ctx *c, int k, Pre pre, Post post, View view_af
     CK(cudaGraphCreate(&g, 0), "graph create");
     std::vector<RebuildNodes> rn((size_t)k);
     cudaError_t e = cudaSuccess;
-    for (int s = 0; s < k && e == cudaSuccess; ++s) {
-        e = cudaGraphConditionalHandleCreate(&rn[(size_t)s].cond, g, 0, cudaGraphCondAssignDefault);
-        if (e == cudaSuccess && two_level(c))
-            e = cudaGraphConditionalHandleCreate(&rn[(size_t)s].cond_inner, g, 0, cudaGraphCondAssignDefault);
-    }
+    for (int s = 0; s < k && e == cudaSuccess; ++s)
+        e = two_level(c) ? cudaGraphConditionalHandleCreate(&rn[(size_t)s].cond_inner, g, 0, cudaGraphCondAssignDefault)
+                         : cudaGraphConditionalHandleCreate(&rn[(size_t)s].cond, g, 0, cudaGraphCondAssignDefault);
     if (e == cudaSuccess)
         e = cudaStreamBeginCaptureToGraph(c->stream, g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) {
@@ -1421,13 +1444,7 @@ static int capture_k_steps(msmgb_ctx *c, int k, Pre pre, Post post, View view_af
     if (!rc && e != cudaSuccess) rc = cuda_err(c, e, "graph capture");
     for (int s = 0; s < k && !rc; ++s) {
         c->a = view_after(s);
-        c->gk_inner = 0;
-        if (rn[(size_t)s].body_inner) {
-            rc = fill_rebuild_body(c, rn[(size_t)s].body, 1, &c->gk_body);
-            if (!rc) rc = fill_rebuild_body(c, rn[(size_t)s].body_inner, 2, &c->gk_inner);
-        } else {
-            rc = fill_rebuild_body(c, rn[(size_t)s].body, 0, &c->gk_body);
-        }
+        rc = fill_step_rebuild(c, rn[(size_t)s]);
         c->a = base;
     }
     if (!rc) {

@@ -70,6 +70,7 @@ enum {
     kFlagAcc = 7,        // float bits: bound on the displacement since the last full rebuild
     kFlagOob = 8,        // an atom left its box since the last full rebuild (next one is full)
     kFlagMaxCand = 9,    // largest candidate count of the last full rebuild (two-level list)
+    kFlagFullNow = 10,   // 1: this step's rebuild is full (two-level list, read by k_set_full)
     kFlagWords = 16
 };
 
@@ -600,5 +601,6 @@ int launch_vv(msmgb_ctx *c, double h, int mode);   // mode 0: predictor; 1: fuse
 int launch_correct(msmgb_ctx *c, double h, bool only_if_pending);
 int launch_decide(msmgb_ctx *c, double skin_trigger, int nb_uptab, cudaGraphConditionalHandle cond = 0,
                   bool use_cond = false, cudaGraphConditionalHandle cond_inner = 0);
+int launch_set_full(msmgb_ctx *c, cudaGraphConditionalHandle cond_full);
 
 }  // namespace msmgb

@@ -15,6 +15,8 @@
 //   k_decide   one thread: rebuild flag for this step from the skin trigger (or the
 //              reference's fixed NB_UPTAB interval, MD_Method_GenericMD_GPU.F90:599-601);
 //              in a step graph it also sets the conditional node that runs the rebuild.
+//   k_set_full one thread, first node of a two-level rebuild body: sets the nested
+//              conditional node of the full rebuild from the decision.
 #include "msmgb_internal.cuh"
 
 namespace msmgb {
@@ -58,8 +60,10 @@ __global__ void k_clear_pending(int *flags) { flags[kFlagPending] = 0; }
 // Two-level list (half_outer > 0): a rebuild is full (binning, sort, candidates) when the
 // displacement since the last full rebuild may exceed half the outer skin, bounded by the sum
 // of the interval maxima (each the largest displacement since the previous build); otherwise
-// only the list is re-selected from the candidates.  cond: the full body; cond_inner: the body
-// that runs on every rebuild.
+// only the list is re-selected from the candidates.  Single-level list: cond, the rebuild
+// body.  Two-level list: cond_inner, the body that runs on every rebuild; the full rebuild is
+// a conditional node nested in that body (a step without a rebuild evaluates one node), whose
+// condition k_set_full sets there from flags[kFlagFullNow].
 __global__ void k_decide(int *flags, unsigned long long *maxdisp, double thr2, int nb_uptab,
                          cudaGraphConditionalHandle cond, int use_cond, float half_outer,
                          cudaGraphConditionalHandle cond_inner)
@@ -81,12 +85,18 @@ __global__ void k_decide(int *flags, unsigned long long *maxdisp, double thr2, i
     }
     flags[kFlagRebuild] = rebuild;
     if (rebuild) flags[kFlagRebuilds] += 1;
+    flags[kFlagFullNow] = full;
     if (use_cond) {
-        cudaGraphSetConditional(cond, full ? 1u : 0u);
         if (half_outer > 0.0f) cudaGraphSetConditional(cond_inner, rebuild ? 1u : 0u);
+        else cudaGraphSetConditional(cond, full ? 1u : 0u);
     }
     *maxdisp = 0ull;
     flags[kFlagPending] = 1;
+}
+
+__global__ void k_set_full(const int *flags, cudaGraphConditionalHandle cond_full)
+{
+    cudaGraphSetConditional(cond_full, flags[kFlagFullNow] ? 1u : 0u);
 }
 
 static inline int nblk(long n, int b) { return (int)((n + b - 1) / b); }
@@ -109,6 +119,13 @@ int launch_correct(msmgb_ctx *c, double h, bool only_if_pending)
     k_clear_pending<<<1, 1, 0, c->stream>>>(c->a.flags);
     c->launches += 2;
     return check_launch(c, "corrector");
+}
+
+int launch_set_full(msmgb_ctx *c, cudaGraphConditionalHandle cond_full)
+{
+    k_set_full<<<1, 1, 0, c->stream>>>(c->a.flags, cond_full);
+    c->launches += 1;
+    return check_launch(c, "rebuild decision");
 }
 
 int launch_decide(msmgb_ctx *c, double skin_trigger, int nb_uptab, cudaGraphConditionalHandle cond, bool use_cond,
