@@ -480,7 +480,7 @@ __global__ void __launch_bounds__(kBlock, 6) k_build_cand(DevAtoms a, const int 
 // accept() for a candidate whose float-float record pj is at hand: inside the FP32 band, the
 // float-float distance of the two records (hi parts on the quantum, so the sum of squared hi
 // differences is exact; the lo parts as dl (2 dh + dl)) lies within ~5e-8 A^2 of the FP64 one
-// (lo parts rounded to ~2^-25 of the quantum, the rounding of the lo terms), so the FP64 rule
+// (lo parts within (2^-26 + 2^-33) of the quantum, the rounding of the lo terms), so the FP64 rule
 // decides only pairs within 2e-7 A^2 of rc^2: the same sets, with the FP64 pipe nearly idle.
 // The sum of squared hi differences is exact below 2^24 quanta^2 (rc below 32 A at the smallest
 // quantum); beyond that the caller passes rc2h < 0 and every band pair takes the FP64 rule.
