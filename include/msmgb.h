@@ -260,6 +260,12 @@ int  msmgb_rebuild_counts(const msmgb_ctx *ctx, int64_t *rebuilds, int64_t *full
 int  msmgb_selftest_wait(msmgb_ctx *ctx);
 /* Largest and mean neighbour count of the current list. */
 int  msmgb_list_stats(msmgb_ctx *ctx, int *maxk, double *meank);
+/* Check of the float-float position records (hi + lo, the list's and the reduced-precision
+ * passes' copy of the positions) against the FP64 positions, for every active atom: hi a
+ * multiple of the positions' quantum q, |lo| <= q/2, and |hi + lo - (x - lo_box + L)|.
+ * *max_err receives the largest of the last in units of q, *violations the number of atoms
+ * that break one of the first two.  Diagnostics; no counterpart in the reference. */
+int  msmgb_check_records(msmgb_ctx *ctx, double *max_err, int *violations);
 /* Cell tiles of the mixed passes for the current list (built after each list build while a
  * selected variant reads them): blocks of 256 sorted atoms, blocks with a tile (a halo of at
  * most 8192 atoms in at most 256 runs), mean and largest halo size over those.  All zero

@@ -107,6 +107,7 @@ SIGNATURES = [
     ("msmgb_time_steps", C.c_int, [C.c_void_p, C.c_int, C.c_double, C.POINTER(C.c_float), _ip]),
     ("msmgb_time_passes", C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_float)]),
     ("msmgb_list_stats", C.c_int, [C.c_void_p, _ip, _dp]),
+    ("msmgb_check_records", C.c_int, [C.c_void_p, _dp, _ip]),
     ("msmgb_tile_stats", C.c_int, [C.c_void_p, _ip, _ip, _dp, _ip]),
     ("msmgb_set_outer_skin", C.c_int, [C.c_void_p, C.c_double]),
     ("msmgb_set_boxshape", C.c_int, [C.c_void_p, C.c_int, _dp]),

@@ -1939,6 +1939,53 @@ extern "C" int msmgb_list_stats(msmgb_ctx *c, int *maxk, double *meank)
     return MSMGB_OK;
 }
 
+// float-float record of each active atom against its FP64 position (msmgb_check_records):
+// the error in units of the quantum as the bits of a non-negative double (ordered like the
+// values), and the atoms whose hi is off the quantum or whose |lo| exceeds half of it
+__global__ void k_check_records(DevAtoms a, unsigned long long *worst, int *bad)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n || (a.statu[i] & MSMGB_STATU_ACTIVE) != MSMGB_STATU_ACTIVE) return;
+    const DevBox &b = a.box[a.boxid[i]];
+    const PosFF f = ld_ff(a.posff + i);
+    const double4_32a p = a.pos[i];
+    const double x[3] = {p.x, p.y, p.z};
+    const float h[3] = {f.hx, f.hy, f.hz}, l[3] = {f.lx, f.ly, f.lz};
+    const double q = (double)b.qq;
+    double e = 0.0;
+    int broken = 0;
+    for (int k = 0; k < 3; ++k) {
+        const double m = (double)h[k] / q;
+        if (m != rint(m) || fabs((double)l[k]) > 0.5 * q) broken = 1;
+        e = fmax(e, fabs(((double)h[k] - (x[k] + b.ushift[k])) + (double)l[k]) / q);
+    }
+    if (broken) atomicAdd(bad, 1);
+    if (e > 0.0) atomicMax(worst, (unsigned long long)__double_as_longlong(e));
+}
+
+extern "C" int msmgb_check_records(msmgb_ctx *c, double *max_err, int *violations)
+{
+    if (!c) return MSMGB_ERR_ARG;
+    RET(need_state(c));
+    RET(use_device(c));
+    unsigned long long *w = nullptr;
+    CK(cudaMalloc((void **)&w, 2 * sizeof(unsigned long long)), "cudaMalloc check");
+    cudaError_t e = cudaMemsetAsync(w, 0, 2 * sizeof(unsigned long long), c->stream);
+    if (e == cudaSuccess) {
+        k_check_records<<<(c->n + kBlock - 1) / kBlock, kBlock, 0, c->stream>>>(c->a, w, (int *)(w + 1));
+        e = cudaGetLastError();
+    }
+    unsigned long long hw[2] = {0ull, 0ull};
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hw, w, sizeof(hw), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    cudaFree(w);
+    if (e != cudaSuccess) return cuda_err(c, e, "record check");
+    c->launches += 1;
+    if (max_err) std::memcpy(max_err, &hw[0], sizeof(double));   // bits of a non-negative double
+    if (violations) *violations = (int)(unsigned)hw[1];
+    return MSMGB_OK;
+}
+
 extern "C" int msmgb_tile_stats(msmgb_ctx *c, int *blocks, int *tiled, double *mean_halo, int *max_halo)
 {
     if (!c) return MSMGB_ERR_ARG;

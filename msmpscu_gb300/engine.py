@@ -702,6 +702,14 @@ class Engine:
         self._ck(self.lib.msmgb_tile_stats(self.ctx, C.byref(nb), C.byref(nt), C.byref(mean), C.byref(mx)))
         return dict(blocks=nb.value, tiled=nt.value, mean_halo=mean.value, max_halo=mx.value)
 
+    def check_records(self):
+        """Largest |hi + lo - u| of the float-float position records in units of the positions'
+        quantum, and the number of atoms whose hi is off the quantum or |lo| > quantum / 2."""
+        err = C.c_double()
+        bad = C.c_int()
+        self._ck(self.lib.msmgb_check_records(self.ctx, C.byref(err), C.byref(bad)))
+        return err.value, bad.value
+
     def list_stats(self):
         mk = C.c_int()
         mean = C.c_double()
