@@ -39,3 +39,35 @@ def reference_export(tmp_dir, name):
         with open(stem + "." + ext, "wb") as fh:
             fh.write(data)
     return stem
+
+
+# The reference's GMD run of examples/NEB_Test (tests/golden/make_golden_neb.py): RU = 1.9
+# lattice units, neighbour cutoff NB_RM = 1.2 RU (MD_SimBoxArray_ToolShell_14_CPU.F90:669-674),
+# tables of 10,000 points up to RMAX = RU (MD_TypeDef_ForceTable.F90:591), Bonny EAM1 with the
+# box file's tables W: 1 2, H: 4 5
+NEB_RU_LU = 1.9
+NEB_NB_FACTOR = 1.2
+NEB_PTYPE = np.array([[1, 2], [4, 5]], np.int32)
+
+
+def neb_reference_configs():
+    """The two step-0 configurations in A and eV: types, positions, box low corner and edges,
+    the reference's forces (eV/A) and per-atom energies (eV, the file prints -EPOT), RU, rc_nl."""
+    import os
+    d = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "neb_w2000h1_bonny_eam1.npz"))
+    out = []
+    for k in range(2):
+        latt = float(d["c%d_latt" % k])
+        ru = NEB_RU_LU * latt
+        out.append(dict(typ=d["c%d_typ" % k], pos=d["c%d_pos" % k] * latt, lo=d["c%d_boxlow" % k] * latt,
+                        length=d["c%d_boxsize" % k] * latt, force=d["c%d_force" % k] / latt,
+                        epot=-d["c%d_pot" % k], ru=ru, rc_nl=NEB_NB_FACTOR * ru))
+    return out
+
+
+def neb_far_from_h(c, dist=8.0):
+    """Atoms farther than dist A (minimum image) from the H atom."""
+    h = c["pos"][c["typ"] == 2][0]
+    dx = c["pos"] - h
+    dx -= np.round(dx / c["length"]) * c["length"]
+    return np.linalg.norm(dx, axis=1) > dist
