@@ -1333,15 +1333,14 @@ static int add_rebuild_nodes(msmgb_ctx *c, RebuildNodes *rn)
     return add_rebuild_node(c, rn->cond, &rn->body);
 }
 
-// the rebuild stage `stage` (0: the whole list build, 1: the full part of a two-level build,
-// 2: its list selection) of the current atom view c->a into a conditional body; its kernel
-// count is returned in *nk
+// the rebuild stage `stage` (0: the whole list build, 1: the full part of a two-level build)
+// of the current atom view c->a into a conditional body; its kernel count is returned in *nk
 static int fill_rebuild_body(msmgb_ctx *c, cudaGraph_t body, int stage, int64_t *nk)
 {
     CK(cudaStreamBeginCaptureToGraph(c->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal),
        "graph capture");
     const int64_t l0 = c->launches;
-    const int rc = stage == 0 ? build_list(c) : (stage == 1 ? build_full(c) : build_inner(c));
+    const int rc = stage == 0 ? build_list(c) : build_full(c);
     cudaGraph_t out = nullptr;
     const cudaError_t e = cudaStreamEndCapture(c->stream, &out);
     *nk = c->launches - l0;
