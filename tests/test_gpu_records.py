@@ -7,7 +7,8 @@ through the fixed-point form of the coordinate, in every precision, for the smal
 import numpy as np
 import pytest
 
-from msmpscu_gb300 import Engine, ForceTable, lattice as lt
+from msmpscu_gb300 import Engine, ForceTable, MSMError, lattice as lt
+from msmpscu_gb300 import _lib as L
 
 pytestmark = pytest.mark.gpu
 
@@ -55,3 +56,11 @@ def test_records_coarse_quantum_open_faces():
     e.close()
     assert bad == 0
     assert 0.0 < err <= BOUND
+
+
+def test_check_records_needs_a_state():
+    e = _engine(100, "mixed")
+    with pytest.raises(MSMError) as ei:
+        e.check_records()
+    assert ei.value.code == L.ERR_ARG
+    e.close()
