@@ -5,9 +5,9 @@ box (Bonny W-H-He EAM, subtype EAM1) at step 0 of the reference's GMD run in exa
 
 The file prints 9 digits and was written by the reference of 2019: per-atom energies agree to
 1e-6 eV (1e-7 of the W cohesive energy), forces on W atoms farther than 8 A from the H atom to
-4e-6 eV/A, and forces next to the H atom to ~8e-5 eV/A, where the W-H terms of that version
-and of the current reference (the oracle's source, pinned to its table exports) differ
-slightly.  The bars below sit a few times above those figures; a planted mistake (the H atom
+4e-6 eV/A, and forces next to the H atom to ~8e-5 eV/A: the residual sits at the W-H terms,
+which that version may evaluate slightly differently from the current reference (the oracle's
+source, pinned to its table exports).  The bars below sit a few times above those figures; a planted mistake (the H atom
 evaluated as W) must break them."""
 import numpy as np
 import pytest
