@@ -272,11 +272,12 @@ class ForceTable:
         return cls(L.POT_CR, prm, rc, rc, L.FS_TYPE, ntab=ntab, nembd=ntab)
 
     @classmethod
-    def marinica_eam2(cls, rc=5.4604375, ntab=10000, nembd=10000, rhoscal=20.0, subtype="EAM2"):
+    def marinica_eam2(cls, rc=5.4604375, ntab=10000, nembd=10000, rhoscal=20.0, subtype="EAM2", rmax=None):
         """Marinica W (EAM type), subtype EAM2 (the reference's default), EAM3 or EAM4
-        (EAM_ForceTable_Marinica_JPCM25_2013.F90:31-44)."""
+        (EAM_ForceTable_Marinica_JPCM25_2013.F90:31-44); tables up to rmax (default rc)."""
         pot = {"EAM2": L.POT_MARINICA2, "EAM3": L.POT_MARINICA3, "EAM4": L.POT_MARINICA4}[subtype.upper()]
-        return cls(pot, None, rc, rc, L.EAM_TYPE, ntab=ntab, nembd=nembd, rhoscal=rhoscal)
+        return cls(pot, None, rc if rmax is None else rmax, rc, L.EAM_TYPE, ntab=ntab, nembd=nembd,
+                   rhoscal=rhoscal)
 
     @classmethod
     def ackland_ww(cls, rmax, ru=None, ntab=10000):
@@ -329,15 +330,16 @@ class ForceTable:
         return self
 
     @classmethod
-    def bonny_wheh(cls, subtype="EAM1", rmax=5.4604375, ntab=10000, nembd=10000, rhoscal=20.0):
+    def bonny_wheh(cls, subtype="EAM1", rmax=5.4604375, ntab=10000, nembd=10000, rhoscal=20.0, ru=None):
         """The reference's W-H-He EAM of Bonny, Grigorev, Terentyev (EAM_WHeH_Bonny_JPCM26_2014),
         subtype "EAM1" (H, He pair-only) or "EAM2" (H embedded in the W density); groups
-        W = 1, H = 2, He = 3."""
+        W = 1, H = 2, He = 3.  Tables up to rmax, cutoff ru (default rmax)."""
         lib = L.load()
         sub = {"EAM1": 1, "EAM2": 2}[subtype.upper()]
         self = cls.__new__(cls)
         self.pot, self.pottype, self.prm = None, L.EAM_TYPE, np.zeros(5)
-        self.rmax = self.ru = float(rmax)
+        self.rmax = float(rmax)
+        self.ru = float(rmax if ru is None else ru)
         self.ntab, self.nembd = int(ntab), int(nembd)
         arrs = [np.zeros(10 * self.ntab) for _ in range(4)]
         self.fembd, self.dfembd = np.zeros(3 * self.nembd), np.zeros(3 * self.nembd)

@@ -128,10 +128,11 @@ def nist(path, ru, ntab=10000, nembd=10000, export_dir=None):
 
 
 def create(libname, ru, symbols=None, ptype=None, subtype=None, pottype=None, ntab=10000, nembd=10000,
-           rhoscal=20.0):
+           rhoscal=20.0, rmax=None):
     """ForceTable of library `libname` for groups given by `symbols` (element symbols) or by
-    `ptype` (NGROUP x NGROUP table numbers, host first), on the sqrt(r) grid up to the cutoff
-    `ru`.  `subtype` selects EAM2/EAM3/EAM4 (Marinica) or EAM1/EAM2 (Bonny); `pottype`
+    `ptype` (NGROUP x NGROUP table numbers, host first), on the sqrt(r) grid up to `rmax`
+    (default the cutoff `ru`: the reference's Rmax = max RU, MD_TypeDef_ForceTable.F90:591;
+    versions of the reference took the largest neighbour cutoff, max NB_RM, instead).  `subtype` selects EAM2/EAM3/EAM4 (Marinica) or EAM1/EAM2 (Bonny); `pottype`
     "EAM_TYPE" gives EM_TB_WangJun_W-HE_2010 its EAM variant (every table embedded with
     F = -sqrt(rho), FS_EMEDMENTFUN, MD_TypeDef_ForceTable.F90:1859-1882)."""
     key = libname.upper()
@@ -168,23 +169,26 @@ def create(libname, ru, symbols=None, ptype=None, subtype=None, pottype=None, nt
             emb_ids.append(int(ptype[i, i]))
     kembd = np.array([emb_ids.index(int(ptype[i, i])) + 1 for i in range(ng)], np.int32)
 
+    rm = float(ru if rmax is None else rmax)
     cols, emb = [], {}
     bonny = None
     for tid in order:
         gen = reg[tid - 1][1]
         if gen[0] == "single":
             prm = _cr_element_prm(gen[2]) if isinstance(gen[2], str) else gen[2]
-            t = ForceTable(gen[1], prm, ru, ru, deftype, ntab=ntab, nembd=nembd, rhoscal=rhoscal)
+            t = ForceTable(gen[1], prm, rm, ru, deftype, ntab=ntab, nembd=nembd, rhoscal=rhoscal)
             cols.append(t)
             if t.pottype == EAM:
                 emb[tid] = (t.fembd, t.dfembd, t.rhod)
         elif gen[0] == "marinica":
-            t = ForceTable.marinica_eam2(rc=ru, ntab=ntab, nembd=nembd, rhoscal=rhoscal, subtype=subtype or "EAM2")
+            t = ForceTable.marinica_eam2(rc=ru, ntab=ntab, nembd=nembd, rhoscal=rhoscal, subtype=subtype or "EAM2",
+                                         rmax=rm)
             cols.append(t)
             emb[tid] = (t.fembd, t.dfembd, t.rhod)
         else:
             if bonny is None:
-                bonny = ForceTable.bonny_wheh(subtype or "EAM1", rmax=ru, ntab=ntab, nembd=nembd, rhoscal=rhoscal)
+                bonny = ForceTable.bonny_wheh(subtype or "EAM1", rmax=rm, ntab=ntab, nembd=nembd, rhoscal=rhoscal,
+                                              ru=ru)
             k = gen[1]
             cols.append(SimpleNamespace(**{name: getattr(bonny, name).reshape(ntab, bonny.nkind)[:, k].copy()
                                            for name in ("potr", "fpotr", "potb", "fpotb")}))
@@ -196,7 +200,7 @@ def create(libname, ru, symbols=None, ptype=None, subtype=None, pottype=None, nt
     out = ForceTable.__new__(ForceTable)
     out.pot, out.prm = None, np.zeros(5)
     out.pottype = ptyp
-    out.rmax = out.ru = float(ru)
+    out.rmax, out.ru = rm, float(ru)
     out.ntab, out.nembd = int(ntab), int(nembd)
     nk = len(order)
     out.nkind, out.ngroup, out.nkind1 = nk, ng, len(emb_ids)

@@ -6,11 +6,11 @@
  * that bench.py times; nothing in the product links or calls it.
  *
  * Parity status: the table generator is pinned by the reference's exported table fixture
- * (see tests/golden/); the force and per-atom energy evaluation is pinned to the
- * reference's own output for a 2,001-atom W + H box (its NEB example's step-0 GMD records,
- * tests/golden/make_golden_neb.py) at the precision those records carry (energies 1e-6 eV,
- * forces 8e-5 eV/A); lists, virial and trajectories have no reference record and are a
- * statement-level restatement ("parity unpinned" there).
+ * (see tests/golden/); the force and per-atom energy evaluation reproduces the reference's
+ * own output for a 2,001-atom W + H box (its NEB example's step-0 GMD records,
+ * tests/golden/make_golden_neb.py) to the records' printed digits; lists, virial and
+ * trajectories have no reference record and are a statement-level restatement ("parity
+ * unpinned" there).
  *
  * Deliberate deviations from the reference, each cited where it happens:
  *   - the cell list uses minimum-image distances, so boxes whose cells are smaller than

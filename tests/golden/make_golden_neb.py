@@ -7,9 +7,11 @@ W_2000_H1_EAM1_box.dat (2,000 W + 1 H, potential library EAM_WHeH_Bonny_JPCM26_2
 EAM1, tables W: 1 2, H: 4 5), control file CtrlFile0K.dat (cutoff RU = 1.9 lattice units,
 TABLESIZE 10000, neighbour cutoff NB_RM = 1.2 RU, periodic).  At step 0 the forces and
 energies in the file are the reference's evaluation at the positions it prints, which are
-the initial configuration's 5-digit decimals (in lattice units, LATT = 3.14 A).  The later
-records (.0001) print the quenched positions with forces of another iteration, so they are
-not used.
+the initial configuration's 5-digit decimals (in lattice units, LATT = 3.14 A).  The version
+that wrote them gridded the tables up to max NB_RM (the form left commented at
+MD_TypeDef_ForceTable.F90:591); with that grid they are reproduced to their printed digits.
+The later records (.0001) print the quenched positions with forces of another iteration, so
+they are not used.
 
 Per atom the file holds TYPE, POS (LU), VEL, STATU, FOR (eV/LU), POT (eV, printed as -EPOT),
 K.E., DISPLACE.  Writes neb_w2000h1_bonny_eam1.npz with, per configuration, the types, the
